@@ -1,0 +1,376 @@
+"""Benchmark of the GB300 FLAC step: element-steps/s on the 1000x300-quad
+two-phase extension model (config 2 of the workload list).
+
+A "step" is one call of the reference's `flac` (fl_therm, change_phase every
+ifreq_rmasses steps, fl_rheol, fl_node, fl_move, rmasses / dt_mass every
+ifreq_* steps) over the whole mesh.  `value` is the FP64 path (device-resident
+state, graph-replayed steps, CUDA events on the library's stream, L2 flushed
+between timed steps); the mixed-precision path is reported beside it.
+`e2e` drives the same steps through the per-subroutine C-ABI calls a
+Fortran drop-in makes (clock scalars in, cord and vel copied back to pinned
+host memory every step as the reference's OpenACC build does at
+fl_move.f90:34).
+
+--impl reference times the oracle (the serial/OpenMP FP64 restatement of the
+reference's loops; the Fortran reference cannot be built on these machines)
+on the host cores.
+
+Multi-GPU: the path does not shard (one mesh per GPU); N>1 runs N
+independent replicas, one per rank, and `value` sums their throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "element-steps/s on 1 GB300: FP64 vs mixed vs batched; surrogate sweep speedup @err"
+WORKLOAD = "config2: two-phase extension, 1000x300 quads (300,000 elements, 301,301 nodes), 1000 km x 300 km"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _ncu_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def _make_model(inp: str, mode: str):
+    import torch
+
+    from geoflac_gb300 import new_state
+    from geoflac_gb300.flac import Flac
+
+    p, c, s = new_state(inp)
+    bufs = []
+
+    def pinned(nbytes):
+        t = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        bufs.append(t)
+        return t.numpy()
+
+    # the arrays the drop-in path copies every step live in pinned memory
+    s.rehome(["cord", "vel"], pinned)
+    g = Flac(p, c, s, mode)
+    g._pinned = bufs
+    return g
+
+
+def _time_device(g, steps: int, warmup: int, flush):
+    """Per-step device time with CUDA events on the library's stream, L2
+    flushed (a 512 MiB write) before each timed step."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(g.stream)
+    g.step(warmup)
+    torch.cuda.synchronize()
+    total = 0.0
+    launches0 = g.launches
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        g.step(1)
+        ev1.record(stream)
+        ev1.synchronize()
+        total += ev0.elapsed_time(ev1) / 1e3
+    wall = time.perf_counter() - t0
+    return total, g.launches - launches0, wall
+
+
+def _time_kernel(g, routine: str, reps: int, flush):
+    """Average duration of one routine's kernels (CUDA events on the stream)."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(g.stream)
+    g.set_sync(False)
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        getattr(g, routine)()
+        ev1.record(stream)
+        ev1.synchronize()
+        times.append(ev0.elapsed_time(ev1) / 1e3)
+    g.set_sync(True)
+    g.status()
+    return sum(times) / len(times)
+
+
+def _time_e2e(g, steps: int):
+    """Drop-in path: per-subroutine C-ABI calls with the reference's host
+    synchronisation (clock scalars in/out, cord+vel back every step)."""
+    import ctypes as C
+
+    import torch
+
+    from geoflac_gb300 import capi
+
+    p = g.params
+    N = p.nx * p.nz
+    lib = g.lib
+    k = capi.GfClock()
+    capi.check(lib.gf_get_clock(g.ctx, C.byref(k)), "gf_get_clock")
+    g.set_sync(False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        capi.check(lib.gf_set_clock(g.ctx, C.byref(k)), "gf_set_clock")
+        g.fl_therm()
+        if k.nloop % p.ifreq_rmasses == 0:
+            g.change_phase()
+        g.fl_rheol()
+        g.fl_node()
+        g.fl_move()
+        if k.nloop % p.ifreq_rmasses == 0:
+            g.rmasses()
+        if k.nloop % p.ifreq_imasses == 0:
+            g.dt_mass()
+        # par.f90:84-87 on the host: read dt back, advance nloop and time
+        capi.check(lib.gf_get_clock(g.ctx, C.byref(k)), "gf_get_clock")
+        k.nloop += 1
+        k.time += k.dt
+        # the reference copies cord and vel to the host every step; the
+        # host arrays are pinned
+        capi.check(lib.gf_download(g.ctx, capi.F_CORD | capi.F_VEL), "gf_download")
+    capi.check(lib.gf_set_clock(g.ctx, C.byref(k)), "gf_set_clock")
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    g.set_sync(True)
+    g.status()
+    h2d = C.sizeof(capi.GfClock)
+    d2h = 4 * N * 8 + C.sizeof(capi.GfClock)
+    return wall, h2d, d2h
+
+
+def run_ours(args):
+    import torch
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from geoflac_gb300 import bytes_model, inpgen
+
+    d = tempfile.mkdtemp(prefix="gfbench")
+    inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    E = 1000 * 300
+    res = {}
+    for mode in ("fp64", "mixed"):
+        g = _make_model(inp, mode)
+        with ClockSampler(local) as cs:
+            if ws > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            dev_t, launches, wall = _time_device(g, args.steps, args.warmup, flush)
+            torch.cuda.synchronize()
+        t = torch.tensor([dev_t], dtype=torch.float64, device="cuda")
+        if ws > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_t = float(t.item())
+        res[mode] = dict(g=g, t=dev_t, launches=launches, clocks=cs.summary(), wall=wall)
+    fp = res["fp64"]
+    value = ws * E * args.steps / fp["t"]
+    mixed_value = ws * E * args.steps / res["mixed"]["t"]
+    # dominant kernel: fl_rheol (k_rheol), timed alone
+    g = fp["g"]
+    t_rheol = _time_kernel(g, "fl_rheol", 10, flush)
+    peak, peak_kind = _peaks()
+    alg = bytes_model.rheol_bytes_per_element(g.params.nphase, "fp64") * E
+    achieved = alg / t_rheol / 1e9
+    traffic = _ncu_traffic("k_rheol_fp64")
+    # e2e through the per-subroutine C-ABI (drop-in path)
+    e2e_steps = max(5, min(args.steps, 20))
+    e2e_wall, h2d, d2h = _time_e2e(g, e2e_steps)
+    e2e_value = ws * E * e2e_steps / e2e_wall
+    out = {
+        "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * fp["t"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .inp model)",
+        "config": {"workload": WORKLOAD, "mode": "fp64", "elements": E, "nodes": 1001 * 301,
+                   "markers_per_element": 9, "parallelism": f"replicas x{ws}",
+                   "l2": "512 MiB buffer written between timed steps"},
+        "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
+                  "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes"},
+        "e2e": {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "path": "per-subroutine C-ABI calls, clock scalars in/out, cord+vel to host every step"},
+        "roofline": {"bound": "hbm", "kernel": "k_rheol (fl_rheol, FP64)", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "avg_launch_s": t_rheol,
+                     "algorithmic_bytes_per_launch": alg},
+        "gpu_launches": fp["launches"],
+        "clocks": fp["clocks"],
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(inp, steps=args.cpu_steps)
+    for r in res.values():
+        r["g"].close()
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
+    """The oracle (OpenMP FP64 restatement of the reference's loops) on the
+    host cores, on a bounded sample of the same workload."""
+    from geoflac_gb300 import new_state
+    from oracle.oracle import Oracle
+
+    n = threads or os.cpu_count() or 1
+    p, c, s = new_state(inp)
+    o = Oracle(p, c, s, threads=n)
+    o.finish_setflac()
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    E = (p.nx - 1) * (p.nz - 1)
+    return {"value": E * steps / dt, "unit": "element-steps/s", "cores": n, "kind": "port",
+            "sample": f"{steps} full FLAC steps of the 1000x300 mesh ({E} elements), {n} OpenMP threads"}
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    from geoflac_gb300 import inpgen, new_state
+    from oracle.oracle import Oracle
+
+    d = tempfile.mkdtemp(prefix="gfbench")
+    inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    n = os.cpu_count() or 1
+    p, c, s = new_state(inp)
+    o = Oracle(p, c, s, threads=n)
+    o.finish_setflac()
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    E = (p.nx - 1) * (p.nz - 1)
+    v = E * args.steps / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "element-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded .inp model)",
+        "config": {"workload": WORKLOAD, "mode": "fp64", "elements": E},
+        "cpu_baseline": {"value": v, "unit": "element-steps/s", "cores": n, "kind": "port",
+                         "sample": f"{args.steps} full FLAC steps of the 1000x300 mesh, {n} OpenMP threads"},
+        "e2e": {"value": v, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

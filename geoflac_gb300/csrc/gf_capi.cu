@@ -1,0 +1,656 @@
+// C-ABI of the GB300 FLAC step (include/geoflac_gb300.h): context
+// management, host<->device sync points, the per-subroutine entry points
+// and the graph-captured multi-step driver.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/geoflac_gb300.h"
+#include "gf_ctx.h"
+
+namespace {
+
+struct GraphEntry {
+    unsigned sig;
+    cudaGraphExec_t exec;
+    long long nlaunch;
+};
+
+} // namespace
+
+struct gf_ctx {
+    gf_params p;
+    gf_layout L;
+    int mode;
+    GfDims d;
+    cudaStream_t s = nullptr;
+    DevParams *dP = nullptr;
+    DevClock *dC = nullptr;
+    DevArrays A{};
+    double *staging = nullptr; // FP64 staging for mixed-mode conversions
+    double *d_angle = nullptr;
+    // host mirrors of the host-controlled scalars
+    int nloop = 0, nsrate = -1, nmarkers = 0, need_remeshing = 0;
+    long long launches = 0;
+    std::vector<GraphEntry> graphs;
+    std::vector<void *> allocs;
+    int sweeps = 0; // cap on the thermal sweeps (0: library cap)
+    int sync = 1;
+};
+
+namespace {
+
+int cuda_err(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return GF_OK;
+    std::fprintf(stderr, "geoflac_gb300: CUDA error in %s: %s\n", what, cudaGetErrorString(e));
+    return GF_ERR_CUDA;
+}
+
+#define GF_CK(call)                                                                                                    \
+    do {                                                                                                               \
+        int _rc = cuda_err((call), #call);                                                                             \
+        if (_rc) return _rc;                                                                                           \
+    } while (0)
+
+template <class T> int dalloc(gf_ctx *c, T **ptr, size_t count) {
+    *ptr = nullptr;
+    if (count == 0) count = 1;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+    cudaMemset(p, 0, count * sizeof(T));
+    c->allocs.push_back(p);
+    *ptr = (T *)p;
+    return GF_OK;
+}
+
+size_t rsize(const gf_ctx *c) { return c->mode == GF_MODE_MIXED ? sizeof(float) : sizeof(double); }
+
+int ralloc(gf_ctx *c, void **ptr, size_t count) {
+    if (c->mode == GF_MODE_MIXED) return dalloc(c, (float **)ptr, count);
+    return dalloc(c, (double **)ptr, count);
+}
+
+void fill_params(DevParams &P, const gf_params &p) {
+    std::memset(&P, 0, sizeof P);
+    P.nx = p.nx; P.nz = p.nz; P.nphase = p.nphase;
+    P.ndim = p.ndim; P.mix_strain = p.mix_strain; P.mix_stress = p.mix_stress;
+    P.istress_therm = p.istress_therm; P.ishearh = p.ishearh; P.itherm = p.itherm; P.itemp_bc = p.itemp_bc;
+    P.nyhydro = p.nyhydro; P.iphsub = p.iphsub > 0 ? p.iphsub : 1; P.i_prestress = p.i_prestress;
+    P.idt_scale = p.idt_scale; P.i_rey = p.i_rey; P.ivis_present = p.ivis_present;
+    P.itype_melting = p.itype_melting; P.nystressbc = p.nystressbc; P.movegrid = p.movegrid;
+    P.nelem_serp = p.nelem_serp; P.eclogite_rule = p.eclogite_rule;
+    for (int k = 0; k < GF_MAXPH; ++k) {
+        P.irheol[k] = p.irheol[k];
+        P.rl[k] = p.rl[k]; P.rm[k] = p.rm[k]; P.den[k] = p.den[k]; P.alfa[k] = p.alfa[k]; P.beta[k] = p.beta[k];
+        P.pln[k] = p.pln[k]; P.acoef[k] = p.acoef[k]; P.eactiv[k] = p.eactiv[k]; P.vactiv[k] = p.vactiv[k];
+        P.plstrain1[k] = p.plstrain1[k]; P.plstrain2[k] = p.plstrain2[k]; P.fric1[k] = p.fric1[k];
+        P.fric2[k] = p.fric2[k]; P.cohesion1[k] = p.cohesion1[k]; P.cohesion2[k] = p.cohesion2[k];
+        P.dilat1[k] = p.dilat1[k]; P.dilat2[k] = p.dilat2[k]; P.conduct[k] = p.conduct[k]; P.cp[k] = p.cp[k];
+    }
+    int w = 0;
+    for (int k = 0; k < p.inhom && k < GF_MAXINH; ++k)
+        if (p.igeom[k] == 100) {
+            P.w_ix1[w] = p.ix1[k]; P.w_ix2[w] = p.ix2[k]; P.w_iy1[w] = p.iy1[k]; P.w_iy2[w] = p.iy2[k];
+            ++w;
+        }
+    P.ninh100 = w;
+    P.g = p.g; P.demf = p.demf; P.ten_off = p.ten_off; P.tau_heal = p.tau_heal; P.v_min = p.v_min;
+    P.v_max = p.v_max; P.t_top = p.t_top; P.t_bot = p.t_bot; P.bot_bc = p.bot_bc; P.pisos = p.pisos;
+    P.drosub = p.drosub; P.rzbo = p.rzbo; P.rxbo = p.rxbo; P.vbc = p.vbc; P.fmagma_max = p.fmagma_max;
+    P.rho_magma = p.rho_magma; P.weaken_ratio_plastic = p.weaken_ratio_plastic;
+    P.weaken_ratio_viscous = p.weaken_ratio_viscous; P.xReyn = p.xReyn; P.strain_inert = p.strain_inert;
+    P.dt_scale = p.dt_scale; P.fracm = p.fracm;
+}
+
+GfLaunch launch_of(gf_ctx *c) {
+    GfLaunch g;
+    g.P = c->dP;
+    g.C = c->dC;
+    g.A = c->A;
+    g.d = c->d;
+    g.s = c->s;
+    g.launches = &c->launches;
+    return g;
+}
+
+// Copy one FP64 host array to a device array of the context's precision
+// (dir = 1 upload, 0 download).
+int xfer_r(gf_ctx *c, double *host, void *dev, long long n, int dir) {
+    if (!host || n <= 0) return GF_OK;
+    if (c->mode == GF_MODE_FP64) {
+        if (dir)
+            GF_CK(cudaMemcpyAsync(dev, host, n * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        else
+            GF_CK(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+        return GF_OK;
+    }
+    GfLaunch g = launch_of(c);
+    if (dir) {
+        GF_CK(cudaMemcpyAsync(c->staging, host, n * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        GfKernels<float>::convert_in(g, 1, c->staging, dev, n);
+    } else {
+        GfKernels<float>::convert_in(g, 0, c->staging, dev, n);
+        GF_CK(cudaMemcpyAsync(host, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    }
+    GF_CK(cudaStreamSynchronize(c->s));
+    return GF_OK;
+}
+
+template <class T> int xfer(gf_ctx *c, T *host, T *dev, long long n, int dir) {
+    if (!host || n <= 0) return GF_OK;
+    if (dir)
+        GF_CK(cudaMemcpyAsync(dev, host, n * sizeof(T), cudaMemcpyHostToDevice, c->s));
+    else
+        GF_CK(cudaMemcpyAsync(host, dev, n * sizeof(T), cudaMemcpyDeviceToHost, c->s));
+    return GF_OK;
+}
+
+int move_fields(gf_ctx *c, unsigned m, int dir) {
+    const gf_layout &L = c->L;
+    DevArrays &A = c->A;
+    long long N = c->d.N, E = c->d.E;
+    int rc = 0;
+#define T_(x)                                                                                                          \
+    do {                                                                                                               \
+        if ((rc = (x))) return rc;                                                                                     \
+    } while (0)
+    if (m & GF_F_CORD) T_(xfer(c, L.cord, A.cord, 2 * N, dir));
+    if (m & GF_F_VEL) T_(xfer(c, L.vel, A.vel, 2 * N, dir));
+    if (m & GF_F_TEMP) {
+        T_(xfer(c, L.temp, A.temp, N, dir));
+        T_(xfer(c, L.temp0, A.temp0, N, dir));
+    }
+    if (m & GF_F_MASS) {
+        T_(xfer(c, L.amass, A.amass, N, dir));
+        T_(xfer(c, L.rmass, A.rmass, N, dir));
+    }
+    if (m & GF_F_BC) {
+        T_(xfer(c, L.bc, A.bc, 2 * N, dir));
+        T_(xfer(c, L.ncod, A.ncod, 2 * N, dir));
+    }
+    if (m & GF_F_STRESS) T_(xfer_r(c, L.stress0, A.stress0, 16 * E, dir));
+    if (m & GF_F_AREA) {
+        T_(xfer_r(c, L.area, A.area, 4 * E, dir));
+        T_(xfer_r(c, L.dvol, A.dvol, 4 * E, dir));
+    }
+    if (m & GF_F_STRAIN) T_(xfer_r(c, L.strain, A.strain, 3 * E, dir));
+    if (m & GF_F_APS) T_(xfer_r(c, L.aps, A.aps, E, dir));
+    if (m & GF_F_VISN) T_(xfer_r(c, L.visn, A.visn, E, dir));
+    if (m & GF_F_PHASE) {
+        T_(xfer(c, L.iphase, A.iphase, E, dir));
+        T_(xfer(c, L.phase_ratio, A.phase_ratio, (long long)c->p.nphase * E, dir));
+        T_(xfer(c, L.jmoho, A.jmoho, c->p.nx - 1, dir));
+    }
+    if (m & GF_F_RATE) {
+        T_(xfer_r(c, L.e2sr, A.e2sr, E, dir));
+        T_(xfer_r(c, L.se2sr, A.se2sr, 3 * E, dir));
+        T_(xfer_r(c, L.shrheat, A.shrheat, E, dir));
+        T_(xfer_r(c, L.sshrheat, A.sshrheat, E, dir));
+        T_(xfer(c, L.source, A.source, E, dir));
+        T_(xfer(c, L.fmagma, A.fmagma, E, dir));
+        T_(xfer(c, L.fmagma2, A.fmagma2, E, dir));
+        T_(xfer(c, L.dike_released, A.dike_released, E, dir));
+    }
+    if (m & GF_F_MARKERS) {
+        long long M = L.max_markers;
+        T_(xfer(c, L.mark_a1, A.mark_a1, M, dir));
+        T_(xfer(c, L.mark_a2, A.mark_a2, M, dir));
+        T_(xfer(c, L.mark_age, A.mark_age, M, dir));
+        T_(xfer(c, L.mark_dead, A.mark_dead, M, dir));
+        T_(xfer(c, L.mark_phase, A.mark_phase, M, dir));
+        T_(xfer(c, L.mark_ntriag, A.mark_ntriag, M, dir));
+        T_(xfer(c, L.mark_id_elem, A.mark_id_elem, (long long)GF_MAX_MARKERS_PER_ELEM * E, dir));
+        T_(xfer(c, L.nmark_elem, A.nmark_elem, E, dir));
+        T_(xfer(c, L.dhacc_correction, A.dhacc_correction, c->p.nx, dir));
+    }
+#undef T_
+    GF_CK(cudaStreamSynchronize(c->s));
+    return GF_OK;
+}
+
+// Read and clear the device status word.
+int take_status(gf_ctx *c);
+
+// Status after a per-subroutine call: waits only in sync mode.
+int call_status(gf_ctx *c) {
+    if (!c->sync) {
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? GF_OK : cuda_err(e, "launch");
+    }
+    return take_status(c);
+}
+
+int take_status(gf_ctx *c) {
+    int st = 0;
+    cudaError_t e = cudaStreamSynchronize(c->s);
+    if (e != cudaSuccess) return cuda_err(e, "step");
+    e = cudaMemcpy(&st, &c->dC->status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "status");
+    if (st) {
+        int zero = 0;
+        cudaMemcpy(&c->dC->status, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    }
+    return st;
+}
+
+__global__ void k_clock_advance(DevClock *C) { C->time = C->time + C->dt; }
+
+// ---- dispatch on precision
+void k_therm(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::therm(g, c->sweeps);
+    else GfKernels<double>::therm(g, c->sweeps);
+}
+void k_rheol(gf_ctx *c, int upd, int avg) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::rheol(g, upd, avg);
+    else GfKernels<double>::rheol(g, upd, avg);
+}
+void k_node(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::node(g);
+    else GfKernels<double>::node(g);
+}
+void k_move(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::move(g);
+    else GfKernels<double>::move(g);
+}
+void k_rmasses(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::rmasses(g);
+    else GfKernels<double>::rmasses(g);
+}
+void k_dt_mass(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::dt_mass(g);
+    else GfKernels<double>::dt_mass(g);
+}
+void k_init_visc(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::init_visc(g);
+    else GfKernels<double>::init_visc(g);
+}
+void k_change_phase(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) GfKernels<float>::change_phase(g, c->nmarkers);
+    else GfKernels<double>::change_phase(g, c->nmarkers);
+}
+
+// The launch sequence of one `flac` call depends only on these flags.
+unsigned step_signature(const gf_ctx *c) {
+    const gf_params &p = c->p;
+    unsigned sig = 0;
+    if (p.itherm != 2) {
+        sig |= 1u;
+        if (c->nloop % p.ifreq_rmasses == 0) sig |= 2u | 16u;
+        if (c->nloop % p.ifreq_visc == 0) sig |= 4u;
+        if (c->nsrate == p.ifreq_avgsr) sig |= 8u << 8;
+        else if (c->nsrate == -1) sig |= 4u << 8;
+        if (c->nloop % p.ifreq_imasses == 0) sig |= 32u;
+    }
+    return sig;
+}
+
+// Enqueue one step (flac.f90:5-91 + par.f90:84-87) for a signature.
+void enqueue_step(gf_ctx *c, unsigned sig) {
+    k_therm(c);
+    if (sig & 1u) {
+        if (sig & 2u) k_change_phase(c);
+        int avg = (sig & (8u << 8)) ? 2 : ((sig & (4u << 8)) ? 1 : 0);
+        k_rheol(c, (sig & 4u) ? 1 : 0, avg);
+        k_node(c);
+        k_move(c);
+        if (sig & 16u) k_rmasses(c);
+        if (sig & 32u) k_dt_mass(c);
+    }
+    k_clock_advance<<<1, 1, 0, c->s>>>(c->dC);
+    ++c->launches;
+}
+
+// host bookkeeping that mirrors the device's after one step
+void advance_host(gf_ctx *c, unsigned sig) {
+    if (sig & 1u) {
+        if (sig & (8u << 8)) c->nsrate = 0;
+        c->nsrate = c->nsrate + 1;
+    }
+    c->nloop = c->nloop + 1;
+}
+
+int run_graph(gf_ctx *c, unsigned sig) {
+    for (auto &g : c->graphs)
+        if (g.sig == sig) {
+            GF_CK(cudaGraphLaunch(g.exec, c->s));
+            c->launches += g.nlaunch;
+            return GF_OK;
+        }
+    cudaGraph_t graph;
+    long long before = c->launches;
+    GF_CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(c, sig);
+    GF_CK(cudaStreamEndCapture(c->s, &graph));
+    cudaGraphExec_t exec;
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_err(e, "cudaGraphInstantiate");
+    long long n = c->launches - before;
+    c->launches = before;
+    c->graphs.push_back(GraphEntry{sig, exec, n});
+    GF_CK(cudaGraphLaunch(exec, c->s));
+    c->launches += n;
+    return GF_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
+    if (!out || !p || !L) return GF_ERR_ARG;
+    *out = nullptr;
+    if (mode != GF_MODE_FP64 && mode != GF_MODE_MIXED) return GF_ERR_ARG;
+    if (L->nx != p->nx || L->nz != p->nz || L->nphase != p->nphase || p->nx < 2 || p->nz < 2) return GF_ERR_ARG;
+    if (p->nystressbc != 0 || p->itype_melting != 0 || p->topo_kappa > 0.0) return GF_ERR_UNSUPPORTED;
+    if (p->nphase > 32) return GF_ERR_UNSUPPORTED;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        std::fprintf(stderr, "geoflac_gb300: no CUDA device\n");
+        return GF_ERR_CUDA;
+    }
+    gf_ctx *c = new (std::nothrow) gf_ctx();
+    if (!c) return GF_ERR_NOMEM;
+    c->p = *p;
+    c->L = *L;
+    c->mode = mode;
+    c->d = GfDims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)};
+    c->sweeps = p->therm_sweeps;
+    long long N = c->d.N, E = c->d.E, M = L->max_markers;
+    int rc = 0;
+#define A_(x)                                                                                                          \
+    do {                                                                                                               \
+        if ((rc = (x))) {                                                                                              \
+            gf_destroy(c);                                                                                             \
+            return rc;                                                                                                 \
+        }                                                                                                              \
+    } while (0)
+    A_(cuda_err(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "cudaStreamCreate"));
+    A_(dalloc(c, &c->dP, 1));
+    A_(dalloc(c, &c->dC, 1));
+    DevArrays &A = c->A;
+    A_(dalloc(c, &A.cord, 2 * N));
+    A_(dalloc(c, &A.vel, 2 * N));
+    A_(dalloc(c, &A.temp, N));
+    A_(dalloc(c, &A.temp0, N));
+    A_(dalloc(c, &A.amass, N));
+    A_(dalloc(c, &A.rmass, N));
+    A_(dalloc(c, &A.bc, 2 * N));
+    A_(dalloc(c, &A.ncod, 2 * N));
+    A_(dalloc(c, &A.dhacc_correction, p->nx));
+    A_(ralloc(c, &A.stress0, 16 * E));
+    A_(ralloc(c, &A.area, 4 * E));
+    A_(ralloc(c, &A.dvol, 4 * E));
+    A_(ralloc(c, &A.strain, 3 * E));
+    A_(ralloc(c, &A.se2sr, 3 * E));
+    A_(ralloc(c, &A.aps, E));
+    A_(ralloc(c, &A.visn, E));
+    A_(ralloc(c, &A.e2sr, E));
+    A_(ralloc(c, &A.shrheat, E));
+    A_(ralloc(c, &A.sshrheat, E));
+    A_(dalloc(c, &A.source, E));
+    A_(dalloc(c, &A.fmagma, E));
+    A_(dalloc(c, &A.fmagma2, E));
+    A_(dalloc(c, &A.dike_released, E));
+    A_(dalloc(c, &A.phase_ratio, (size_t)p->nphase * E));
+    A_(dalloc(c, &A.iphase, E));
+    A_(dalloc(c, &A.jmoho, p->nx));
+    A_(dalloc(c, &A.mark_a1, M));
+    A_(dalloc(c, &A.mark_a2, M));
+    A_(dalloc(c, &A.mark_age, M));
+    A_(dalloc(c, &A.mark_dead, M));
+    A_(dalloc(c, &A.mark_phase, M));
+    A_(dalloc(c, &A.mark_ntriag, M));
+    A_(dalloc(c, &A.mark_id_elem, (size_t)GF_MAX_MARKERS_PER_ELEM * E));
+    A_(dalloc(c, &A.nmark_elem, E));
+    A_(dalloc(c, &A.t_delta0, N));
+    A_(dalloc(c, &A.t_delta1, N));
+    A_(dalloc(c, &A.t_coef, (size_t)18 * E));
+    A_(dalloc(c, &A.e_dens, E));
+    A_(dalloc(c, &A.e_rho, E));
+    A_(dalloc(c, &A.e_flag, E));
+    A_(dalloc(c, &A.nmarkers, 1));
+    A_(dalloc(c, &c->d_angle, 1));
+    if (mode == GF_MODE_MIXED) A_(dalloc(c, &c->staging, 16 * E));
+    DevParams P;
+    fill_params(P, *p);
+    A_(cuda_err(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice), "params"));
+    DevClock C0;
+    std::memset(&C0, 0, sizeof C0);
+    C0.frac = p->frac;
+    A_(cuda_err(cudaMemcpy(c->dC, &C0, sizeof C0, cudaMemcpyHostToDevice), "clock"));
+#undef A_
+    *out = c;
+    return GF_OK;
+}
+
+void gf_destroy(gf_ctx *c) {
+    if (!c) return;
+    if (c->s) cudaStreamSynchronize(c->s);
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->s) cudaStreamDestroy(c->s);
+    delete c;
+}
+
+int gf_upload(gf_ctx *c, unsigned mask) {
+    if (!c) return GF_ERR_ARG;
+    return move_fields(c, mask, 1);
+}
+
+int gf_download(gf_ctx *c, unsigned mask) {
+    if (!c) return GF_ERR_ARG;
+    return move_fields(c, mask, 0);
+}
+
+int gf_set_params(gf_ctx *c, const gf_params *p) {
+    if (!c || !p) return GF_ERR_ARG;
+    if (p->nx != c->p.nx || p->nz != c->p.nz || p->nphase != c->p.nphase) return GF_ERR_ARG;
+    c->p = *p;
+    c->sweeps = p->therm_sweeps;
+    DevParams P;
+    fill_params(P, *p);
+    GF_CK(cudaStreamSynchronize(c->s));
+    GF_CK(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice));
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+    return GF_OK;
+}
+
+int gf_set_clock(gf_ctx *c, const gf_clock *k) {
+    if (!c || !k) return GF_ERR_ARG;
+    GF_CK(cudaStreamSynchronize(c->s));
+    DevClock C;
+    GF_CK(cudaMemcpy(&C, c->dC, sizeof C, cudaMemcpyDeviceToHost));
+    C.dt = k->dt; C.time = k->time; C.dtavg = k->dtavg; C.dt_elastic = k->dt_elastic;
+    C.dt_maxwell = k->dt_maxwell; C.dtmax_therm = k->dtmax_therm; C.frac = k->frac;
+    C.vel_max = k->vel_max; C.dlmin = k->dlmin;
+    GF_CK(cudaMemcpy(c->dC, &C, sizeof C, cudaMemcpyHostToDevice));
+    c->nloop = k->nloop;
+    c->nsrate = k->nsrate;
+    c->nmarkers = k->nmarkers;
+    c->need_remeshing = k->need_remeshing;
+    return GF_OK;
+}
+
+int gf_get_clock(gf_ctx *c, gf_clock *k) {
+    if (!c || !k) return GF_ERR_ARG;
+    GF_CK(cudaStreamSynchronize(c->s));
+    DevClock C;
+    GF_CK(cudaMemcpy(&C, c->dC, sizeof C, cudaMemcpyDeviceToHost));
+    k->dt = C.dt; k->time = C.time; k->dtavg = C.dtavg; k->dt_elastic = C.dt_elastic;
+    k->dt_maxwell = C.dt_maxwell; k->dtmax_therm = C.dtmax_therm; k->frac = C.frac;
+    k->vel_max = C.vel_max; k->dlmin = C.dlmin;
+    k->therm_sweeps = C.therm_sweeps_used;
+    k->therm_unconverged = C.therm_unconverged;
+    k->nloop = c->nloop;
+    k->nsrate = c->nsrate;
+    k->nmarkers = c->nmarkers;
+    k->need_remeshing = c->need_remeshing;
+    return GF_OK;
+}
+
+// One reference subroutine per entry point; each waits for its kernels and
+// returns the device status (the reference's stop code where it would stop).
+int gf_fl_therm(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_therm(c);
+    return call_status(c);
+}
+
+int gf_change_phase(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_change_phase(c);
+    return call_status(c);
+}
+
+int gf_fl_rheol(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    const gf_params &p = c->p;
+    int avg = (c->nsrate == p.ifreq_avgsr) ? 2 : (c->nsrate == -1 ? 1 : 0);
+    k_rheol(c, c->nloop % p.ifreq_visc == 0, avg);
+    if (avg == 2) c->nsrate = 0;
+    c->nsrate = c->nsrate + 1;
+    return call_status(c);
+}
+
+int gf_fl_node(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_node(c);
+    return call_status(c);
+}
+
+int gf_fl_move(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    if (c->p.movegrid == 0) return GF_OK;
+    k_move(c);
+    return call_status(c);
+}
+
+int gf_rmasses(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_rmasses(c);
+    return call_status(c);
+}
+
+int gf_dt_mass(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_dt_mass(c);
+    return call_status(c);
+}
+
+int gf_init_visc(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_init_visc(c);
+    return call_status(c);
+}
+
+int gf_marker2elem(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    return GF_ERR_UNSUPPORTED;
+}
+
+int gf_finish_setflac(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    k_rmasses(c);
+    if (c->p.ivis_present == 1) k_init_visc(c);
+    k_dt_mass(c);
+    int st = take_status(c);
+    if (st) return st;
+    gf_clock k;
+    int rc = gf_get_clock(c, &k);
+    if (rc) return rc;
+    k.dtavg = 0.0;
+    k.nsrate = -1;
+    return gf_set_clock(c, &k);
+}
+
+int gf_flac(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    unsigned sig = step_signature(c);
+    enqueue_step(c, sig);
+    advance_host(c, sig);
+    return call_status(c);
+}
+
+int gf_step(gf_ctx *c, int nsteps) {
+    if (!c || nsteps < 0) return GF_ERR_ARG;
+    for (int k = 0; k < nsteps; ++k) {
+        unsigned sig = step_signature(c);
+        int rc = run_graph(c, sig);
+        if (rc) return rc;
+        advance_host(c, sig);
+    }
+    return take_status(c);
+}
+
+int gf_itest_mesh(gf_ctx *c, double *min_angle) {
+    if (!c) return GF_ERR_ARG;
+    double init = 180.0;
+    GF_CK(cudaMemcpyAsync(c->d_angle, &init, sizeof init, cudaMemcpyHostToDevice, c->s));
+    GfLaunch g = launch_of(c);
+    GfKernels<double>::min_angle(g, c->d_angle);
+    double a = 0.0;
+    GF_CK(cudaMemcpyAsync(&a, c->d_angle, sizeof a, cudaMemcpyDeviceToHost, c->s));
+    GF_CK(cudaStreamSynchronize(c->s));
+    if (min_angle) *min_angle = a;
+    c->need_remeshing = (a <= c->p.angle_rem) ? 1 : 0;
+    return GF_OK;
+}
+
+int gf_remesh(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    return GF_ERR_UNSUPPORTED;
+}
+
+int gf_set_sync(gf_ctx *c, int sync) {
+    if (!c) return GF_ERR_ARG;
+    c->sync = sync ? 1 : 0;
+    return GF_OK;
+}
+
+void *gf_stream(gf_ctx *c) { return c ? (void *)c->s : nullptr; }
+
+int gf_status(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    return take_status(c);
+}
+
+long long gf_launch_count(gf_ctx *c) { return c ? c->launches : 0; }
+
+const char *gf_strerror(int code) {
+    switch (code) {
+    case GF_OK: return "ok";
+    case GF_ERR_CUDA: return "CUDA error";
+    case GF_ERR_ARG: return "bad argument";
+    case GF_ERR_IO: return "cannot open file";
+    case GF_ERR_PARSE: return "malformed .inp file";
+    case GF_ERR_UNSUPPORTED: return "feature not supported by the GPU path";
+    case GF_ERR_TIMEOUT: return "device wait timed out";
+    case GF_ERR_NOMEM: return "out of memory";
+    case GF_ERR_NONFINITE: return "non-finite value";
+    case 22: return "Maxwell: time step too large (reference stop 22)";
+    case 40: return "negative area (reference stop 40)";
+    case 41: return "negative area at start-up (reference stop 41)";
+    case 133: return "marker top-up failed (reference stop 133)";
+    case 134: return "no markers in an element";
+    default: return code > 0 ? "reference stop code" : "unknown error";
+    }
+}
+
+} // extern "C"

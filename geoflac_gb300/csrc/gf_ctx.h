@@ -1,0 +1,96 @@
+// Device-side state of one model (one gf_ctx) and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/geoflac_gb300.h"
+#include "gf_index.h"
+
+#define GF_THREADS 256
+#define GF_THERM_KMAX 24 // cap on the thermal fixed-point sweeps per fl_therm
+
+// Read-only model constants the kernels use (copied once per context into
+// device global memory; every thread of a warp reads the same entries).
+struct DevParams {
+    int nx, nz, nphase;
+    int ndim, mix_strain, mix_stress, istress_therm, ishearh, itherm, itemp_bc;
+    int nyhydro, iphsub, i_prestress, idt_scale, i_rey, ivis_present, itype_melting;
+    int nystressbc, movegrid, nelem_serp, eclogite_rule, ninh100;
+    int irheol[GF_MAXPH];
+    double rl[GF_MAXPH], rm[GF_MAXPH], den[GF_MAXPH], alfa[GF_MAXPH], beta[GF_MAXPH], pln[GF_MAXPH],
+        acoef[GF_MAXPH], eactiv[GF_MAXPH], vactiv[GF_MAXPH], plstrain1[GF_MAXPH], plstrain2[GF_MAXPH],
+        fric1[GF_MAXPH], fric2[GF_MAXPH], cohesion1[GF_MAXPH], cohesion2[GF_MAXPH], dilat1[GF_MAXPH],
+        dilat2[GF_MAXPH], conduct[GF_MAXPH], cp[GF_MAXPH];
+    // Eff_visc fixed weak zones (igeom == 100), 1-based element ranges
+    int w_ix1[GF_MAXINH], w_ix2[GF_MAXINH], w_iy1[GF_MAXINH], w_iy2[GF_MAXINH];
+    double g, demf, ten_off, tau_heal, v_min, v_max, t_top, t_bot, bot_bc, pisos, drosub, rzbo, rxbo, vbc,
+        fmagma_max, rho_magma, weaken_ratio_plastic, weaken_ratio_viscous, xReyn, strain_inert, dt_scale, fracm;
+};
+
+// Scalars the step reads and writes, resident on the device so that a
+// captured step needs no host round trip.
+struct DevClock {
+    double dt, time, dtavg;
+    double dt_elastic, dt_maxwell, dtmax_therm, frac, vel_max, dlmin;
+    // reduction slots (bit patterns of non-negative doubles order like ints)
+    unsigned long long r_dlmin, r_velmax, r_diffmax;
+    long long frac_writer; // serial position + 1 of the last Eff_dens that wrote frac
+    unsigned int phase_mask;
+    int status;     // first error code (reference stop code or GF_ERR_*)
+    int status_aux; // element/node index of the first error
+    int therm_sweeps_used;  // sweeps of the last fl_therm (converged at the last)
+    int therm_unconverged;  // fl_therm calls that hit the sweep cap
+    int therm_flags[GF_THERM_KMAX]; // sweep k changed some value
+};
+
+// Device arrays of a context.  In GF_MODE_MIXED the element fields listed
+// under "R" are FP32 (R = float); in GF_MODE_FP64 everything is double.
+struct DevArrays {
+    // node fields (always FP64: coordinates, temperature, masses)
+    double *cord, *vel, *temp, *temp0, *amass, *rmass, *bc;
+    int *ncod;
+    double *dhacc_correction;
+    // element fields stored as R
+    void *stress0, *area, *dvol, *strain, *se2sr, *aps, *visn, *e2sr, *shrheat, *sshrheat;
+    // element fields always FP64
+    double *source, *fmagma, *fmagma2, *dike_released, *phase_ratio;
+    int *iphase, *jmoho;
+    // markers
+    double *mark_a1, *mark_a2, *mark_age;
+    int8_t *mark_dead, *mark_phase;
+    int *mark_ntriag, *mark_id_elem, *nmark_elem;
+    // scratch
+    double *t_delta0, *t_delta1; // thermal sweep iterates (node)
+    double *t_coef;              // thermal per-element coefficients (18 per element)
+    double *e_dens;                                   // per-element density (rmasses)
+    double *e_rho;                                    // per-element inertial density (dt_mass)
+    uint8_t *e_flag;                                  // change_phase element flags
+    int *m_count, *m_offset;                          // marker2elem scan
+    double *cord_old;                                 // remesh
+    int *nmarkers;                                    // device marker count
+};
+
+struct GfLaunch {
+    const DevParams *P;
+    DevClock *C;
+    DevArrays A;
+    GfDims d;
+    cudaStream_t s;
+    long long *launches;
+};
+
+// Launchers, one set per precision (template instantiated in its own TU).
+template <class R> struct GfKernels {
+    static void therm(const GfLaunch &g, int sweeps);
+    static void rheol(const GfLaunch &g, int update_visc, int avg_mode);
+    static void node(const GfLaunch &g);
+    static void move(const GfLaunch &g);
+    static void rmasses(const GfLaunch &g);
+    static void dt_mass(const GfLaunch &g);
+    static void init_visc(const GfLaunch &g);
+    static void change_phase(const GfLaunch &g, int nmarkers);
+    static void min_angle(const GfLaunch &g, double *d_out);
+    static void convert_in(const GfLaunch &g, unsigned mask, const double *src, void *dst, long long n);
+};
+

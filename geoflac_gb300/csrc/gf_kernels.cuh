@@ -1,0 +1,368 @@
+// Kernels of the explicit FLAC step, templated on the element-field type R
+// (double for GF_MODE_FP64, float for GF_MODE_MIXED).  Each __device__
+// routine restates one reference routine in the reference's evaluation order;
+// the FP64 translation unit is compiled without FMA contraction so that its
+// arithmetic is the serial Fortran's.
+//
+// Layout: element e = i*(nz-1)+j and node n = i*nz+j (j = depth, fastest), so
+// consecutive threads touch consecutive addresses of every field.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "gf_ctx.h"
+#include "gf_math.h"
+
+// internal linkage: each precision's translation unit has its own copy
+namespace {
+namespace gfk {
+
+// ---------------------------------------------------------------- math
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_sin(double x) { return gfm::sin(x); }
+__device__ __forceinline__ float m_sin(float x) { return sinf(x); }
+__device__ __forceinline__ double m_tan(double x) { return gfm::tan(x); }
+__device__ __forceinline__ float m_tan(float x) { return tanf(x); }
+__device__ __forceinline__ double m_abs(double x) { return fabs(x); }
+__device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
+
+__device__ __forceinline__ void set_status(DevClock *C, int code, int where) {
+    if (atomicCAS(&C->status, 0, code) == 0) C->status_aux = where;
+}
+
+// atomic min / max on non-negative doubles through their bit patterns
+__device__ __forceinline__ void atomic_min_pos(unsigned long long *slot, double v) {
+    atomicMin(slot, (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_max_pos(unsigned long long *slot, double v) {
+    atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+}
+
+template <class T> __device__ __forceinline__ T warp_min(T v) {
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <class T> __device__ __forceinline__ T warp_max(T v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+struct Quad {
+    double x[4], y[4]; // nodes 1..4 = (j,i), (j+1,i), (j,i+1), (j+1,i+1)
+};
+
+__device__ __forceinline__ void load_quad(const double *__restrict__ cord, const GfDims &d, int j, int i, Quad &q) {
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    q.x[0] = cord[n1];
+    q.x[1] = cord[n1 + 1];
+    q.x[2] = cord[n3];
+    q.x[3] = cord[n3 + 1];
+    q.y[0] = cord[d.N + n1];
+    q.y[1] = cord[d.N + n1 + 1];
+    q.y[2] = cord[d.N + n3];
+    q.y[3] = cord[d.N + n3 + 1];
+}
+
+// Shape-function derivatives of the four triangles (fl_rheol.f90:98-132):
+// dx[m][k], dz[m][k] for local vertex m of triangle k.  Coordinate
+// differences are taken in FP64, then rounded to R.
+template <class R>
+__device__ __forceinline__ void shape_derivs(const Quad &q, const R ar[4], R dx[3][4], R dz[3][4]) {
+    const double *x = q.x, *y = q.y;
+    dx[0][0] = R(y[1] - y[2]) * ar[0]; dx[1][0] = R(y[2] - y[0]) * ar[0]; dx[2][0] = R(y[0] - y[1]) * ar[0];
+    dz[0][0] = R(x[2] - x[1]) * ar[0]; dz[1][0] = R(x[0] - x[2]) * ar[0]; dz[2][0] = R(x[1] - x[0]) * ar[0];
+    dx[0][1] = R(y[1] - y[3]) * ar[1]; dx[1][1] = R(y[3] - y[2]) * ar[1]; dx[2][1] = R(y[2] - y[1]) * ar[1];
+    dz[0][1] = R(x[3] - x[1]) * ar[1]; dz[1][1] = R(x[2] - x[3]) * ar[1]; dz[2][1] = R(x[1] - x[2]) * ar[1];
+    dx[0][2] = R(y[1] - y[3]) * ar[2]; dx[1][2] = R(y[3] - y[0]) * ar[2]; dx[2][2] = R(y[0] - y[1]) * ar[2];
+    dz[0][2] = R(x[3] - x[1]) * ar[2]; dz[1][2] = R(x[0] - x[3]) * ar[2]; dz[2][2] = R(x[1] - x[0]) * ar[2];
+    dx[0][3] = R(y[3] - y[2]) * ar[3]; dx[1][3] = R(y[2] - y[0]) * ar[3]; dx[2][3] = R(y[0] - y[3]) * ar[3];
+    dz[0][3] = R(x[2] - x[3]) * ar[3]; dz[1][3] = R(x[0] - x[2]) * ar[3]; dz[2][3] = R(x[3] - x[0]) * ar[3];
+}
+
+// ---------------------------------------------------------------- matprops
+
+// Eff_visc (matprops.f90:136-215), always in FP64.
+template <class R>
+__device__ double eff_visc(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+                           const R *__restrict__ st) {
+    for (int k = 0; k < P.ninh100; ++k)
+        if (i + 1 >= P.w_ix1[k] && i + 1 <= P.w_ix2[k] && j + 1 >= P.w_iy1[k] && j + 1 <= P.w_iy2[k]) return P.v_min;
+    const double adi_grad = 3e-1, r = 8.31448;
+    const double *cord = A.cord, *temp = A.temp;
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
+    double tmpr0 = 0.25 * (temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
+    double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
+    double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
+    double s11 = 0.25 * ((double)st[gf_s(d, e, 0, 0)] + (double)st[gf_s(d, e, 0, 1)] + (double)st[gf_s(d, e, 0, 2)] +
+                         (double)st[gf_s(d, e, 0, 3)]);
+    double s22 = 0.25 * ((double)st[gf_s(d, e, 1, 0)] + (double)st[gf_s(d, e, 1, 1)] + (double)st[gf_s(d, e, 1, 2)] +
+                         (double)st[gf_s(d, e, 1, 3)]);
+    double s33 = 0.25 * ((double)st[gf_s(d, e, 3, 0)] + (double)st[gf_s(d, e, 3, 1)] + (double)st[gf_s(d, e, 3, 2)] +
+                         (double)st[gf_s(d, e, 3, 3)]);
+    double pres = -1 * (s11 + s22 + s33) / 3.0;
+    double deptmpr410 = -101.58 * (tmpr + 273.0) - 216828.0;
+    double deptmpr660 = 66.55 * (tmpr + 273.0) - 788494.0;
+    double ev;
+    if (zcord < deptmpr660) {
+        ev = 1e22 * gfm::exp(-0.0115 * (tmpr - P.t_bot));
+        return fmin(P.v_max, fmax(P.v_min, ev));
+    } else if (zcord < deptmpr410) {
+        ev = 1e21 * gfm::exp(-0.0115 * (tmpr - P.t_bot));
+        return fmin(P.v_max, fmax(P.v_min, ev));
+    }
+    double srat = (double)((const R *)A.e2sr)[e];
+    if (srat == 0) srat = P.vbc / P.rxbo;
+    ev = 0.0;
+    for (int k = 0; k < P.nphase; ++k) {
+        double ratio = A.phase_ratio[gf_pr(d, e, k)];
+        if (ratio < 0.01) continue;
+        double pw = 1.0 / P.pln[k] - 1.0;
+        double pw1 = -1.0 / P.pln[k];
+        double vis = 0.25 * gfm::pow(srat, pw) * gfm::pow(0.75 * P.acoef[k], pw1) *
+                     gfm::exp((P.eactiv[k] + P.vactiv[k] * pres) / (P.pln[k] * r * (tmpr + 273.0))) * 1e6;
+        if (vis < P.v_min) vis = P.v_min;
+        if (vis > P.v_max) vis = P.v_max;
+        ev = ev + ratio / vis;
+    }
+    ev = 1 / ev;
+    if (P.itype_melting == 1) {
+        double fma = fmin(A.fmagma[e] + A.fmagma2[e], P.fmagma_max);
+        ev = ev * gfm::exp(P.weaken_ratio_viscous * fma / P.fmagma_max);
+    }
+    return fmin(P.v_max, fmax(P.v_min, ev));
+}
+
+// Eff_dens (matprops.f90:3-83), FP64.  *wrote_frac/*frac_val report the
+// write of the global frac the reference performs (matprops.f90:37,48).
+template <class R>
+__device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+                           int *wrote_frac, double *frac_val) {
+    const double adi_grad = 3e-1, den_ramp_dist = 30e3, amp410 = 0.05, amp660 = 0.085;
+    const double *cord = A.cord, *temp = A.temp;
+    const R *st = (const R *)A.stress0;
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
+    double tmpr0 = 0.25 * (temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
+    double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
+    double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
+    int iph = A.iphase[e];
+    double deptmpr410 = -101.58 * (tmpr + 273.0) - 216828.0;
+    double deptmpr420 = deptmpr410 - den_ramp_dist;
+    double den_amp = 1.0;
+    *wrote_frac = 0;
+    if (deptmpr410 > zcord) {
+        double f = (deptmpr410 - zcord) / (deptmpr410 - deptmpr420);
+        if (f < 0.0) f = 0.0;
+        if (f > 1.0) f = 1.0;
+        *wrote_frac = 1;
+        *frac_val = f;
+        den_amp = 1.0 + amp410 * f;
+    }
+    double deptmpr660 = 66.55 * (tmpr + 273.0) - 788494.0;
+    double deptmpr670 = deptmpr660 - den_ramp_dist;
+    if (deptmpr660 > zcord) {
+        double f = (deptmpr660 - zcord) / (deptmpr660 - deptmpr670);
+        if (f < 0.0) f = 0.0;
+        if (f > 1.0) f = 1.0;
+        *wrote_frac = 1;
+        *frac_val = f;
+        den_amp = 1.05 + amp660 * f;
+    }
+    double press = 0;
+    for (int k = 0; k < 4; ++k)
+        press = press - ((double)st[gf_s(d, e, 0, k)] + (double)st[gf_s(d, e, 1, k)] + (double)st[gf_s(d, e, 3, k)]);
+    press = press / 12;
+    double ed = 0.0;
+    for (int k = 0; k < P.nphase; ++k) {
+        double ratio = A.phase_ratio[gf_pr(d, e, k)];
+        if (ratio < 0.01) continue;
+        double dens = P.den[k] * (1 - P.alfa[k] * tmpr + P.beta[k] * press);
+        press = dens * P.g * zcord;
+        dens = P.den[k] * (1 - P.alfa[k] * tmpr + P.beta[k] * press);
+        ed = ed + ratio * dens;
+    }
+    if (iph == 4 || iph == 8 || iph == 9 || iph == 16 || iph == 18) ed = ed * den_amp;
+    double fma = fmin(A.fmagma[e] + A.fmagma2[e], P.fmagma_max);
+    ed = ed - fma * (ed - P.rho_magma);
+    return ed;
+}
+
+// ---------------------------------------------------------------- rheology
+
+template <class R>
+__device__ __forceinline__ void elastic(R bulkm, R rmu, R &s11, R &s22, R &s33, R &s12, R de11, R de22, R de12) {
+    const R c4d3 = R(4.0 / 3.0), c2d3 = R(2.0 / 3.0);
+    R a1 = bulkm + c4d3 * rmu;
+    R a2 = bulkm - c2d3 * rmu;
+    s11 = s11 + a1 * de11 + a2 * de22;
+    s22 = s22 + a2 * de11 + a1 * de22;
+    s12 = s12 + R(2) * rmu * de12;
+    s33 = s33 + a2 * (de11 + de22);
+}
+
+// maxwell (rh_maxwell.f90:34-108).  Returns false where the reference stops
+// with code 22.
+template <class R>
+__device__ __forceinline__ bool maxwell(R bulkm, R rmu0, R viscosity, R &s11, R &s22, R &s33, R &s12, R de11, R de22,
+                                        R de33, R de12, R dv, int ndim, R dt) {
+    const R c1d3 = R(1.0 / 3.0), visc_cut = R(1e19);
+    R rmu = viscosity < visc_cut ? rmu0 * viscosity / visc_cut : rmu0;
+    R temp = rmu / (R(2) * viscosity) * dt;
+    bool ok = !(temp > R(0.5));
+    R vic1 = R(1) - temp;
+    R vic2 = R(1.0) / (R(1.0) + temp);
+    R dev, de11d, de22d, de33d, s0, s11d, s22d, s33d;
+    if (ndim == 2) {
+        dev = de11 + de22;
+        de11d = de11 - R(0.5) * dev;
+        de22d = de22 - R(0.5) * dev;
+        de33d = 0;
+        s0 = R(0.5) * (s11 + s22);
+        s11d = s11 - s0;
+        s22d = s22 - s0;
+        s33d = 0;
+    } else {
+        dev = de11 + de22 + de33;
+        de11d = de11 - c1d3 * dev;
+        de22d = de22 - c1d3 * dev;
+        de33d = de33 - c1d3 * dev;
+        s0 = c1d3 * (s11 + s22 + s33);
+        s11d = s11 - s0;
+        s22d = s22 - s0;
+        s33d = s33 - s0;
+    }
+    s11d = (s11d * vic1 + R(2) * rmu * de11d) * vic2;
+    s22d = (s22d * vic1 + R(2) * rmu * de22d) * vic2;
+    s33d = (s33d * vic1 + R(2) * rmu * de33d) * vic2;
+    s12 = (s12 * vic1 + R(2) * rmu * de12) * vic2;
+    s0 = s0 + bulkm * dv;
+    s11 = s11d + s0;
+    s22 = s22d + s0;
+    s33 = s33d + s0;
+    return ok;
+}
+
+// Per-element constants of the plastic return map (rh_plastic.f90:141-154).
+// The reference evaluates them once per triangle with identical inputs; they
+// are evaluated once per element here (same values, a quarter of the
+// transcendental work).
+template <class R> struct PlasticConsts {
+    R anphi, anpsi, amc, e1, e2, x1, ten_max;
+};
+
+template <class R>
+__device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh, R phi, R psi, R ten_off) {
+    const R pi = R(3.14159265358979323846);
+    const R degrad = R(3.14159265358979323846 / 180.0);
+    const R c4d3 = R(4.0 / 3.0), c2d3 = R(2.0 / 3.0);
+    (void)pi;
+    PlasticConsts<R> c;
+    R sphi = m_sin(phi * degrad);
+    R spsi = m_sin(psi * degrad);
+    c.anphi = (R(1.0) + sphi) / (R(1.0) - sphi);
+    c.anpsi = (R(1.0) + spsi) / (R(1.0) - spsi);
+    c.amc = R(2.0) * coh * m_sqrt(c.anphi);
+    c.e1 = bulkm + c4d3 * rmu;
+    c.e2 = bulkm - c2d3 * rmu;
+    c.x1 = (c.e1 - c.e2 * c.anpsi + c.e1 * c.anphi * c.anpsi - c.e2 * c.anphi);
+    c.ten_max = (phi == R(0.0)) ? ten_off : fmin(ten_off, coh / (m_tan(phi * degrad)));
+    return c;
+}
+
+// plastic (rh_plastic.f90:111-332), 2-D branch (icase = 1).
+template <class R>
+__device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &depls, R hardn, R &s11, R &s22, R &s33,
+                                        R &s12, R de11, R de22, R de33, R de12) {
+    depls = R(0.0);
+    R e1 = c.e1, e2 = c.e2, anphi = c.anphi, anpsi = c.anpsi, ten_max = c.ten_max;
+    R s11i = s11 + (de22 + de33) * e2 + de11 * e1;
+    R s22i = s22 + (de11 + de33) * e2 + de22 * e1;
+    R s12i = s12 + de12 * R(2.0) * rmu;
+    R s33i = s33 + (de11 + de22) * e2 + de33 * e1;
+    R sdif = s11i - s22i;
+    R s0 = R(0.5) * (s11i + s22i);
+    R rad = R(0.5) * m_sqrt(sdif * sdif + R(4.0) * s12i * s12i);
+    R si = s0 - rad, sii = s0 + rad, psdif = si - sii;
+    R s1 = si, s2 = s33i, s3 = sii;
+    if (s1 >= ten_max) {
+        s11 = ten_max; s22 = ten_max; s12 = R(0.0); s33 = ten_max;
+        return;
+    }
+    if (s3 >= ten_max) s3 = ten_max;
+    R fs = s1 - s3 * anphi + c.amc;
+    if (fs < R(0.0)) {
+        R alams = fs / (c.x1 + hardn);
+        s1 = s1 - alams * (e1 - e2 * anpsi);
+        s2 = s2 - alams * e2 * (R(1.0) - anpsi);
+        s3 = s3 - alams * (e2 - e1 * anpsi);
+        R dep1 = alams;
+        R dep3 = -alams * anpsi;
+        depls = R(0.5) * m_abs(dep1 - dep3);
+    } else {
+        s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;
+        return;
+    }
+    if (s1 >= ten_max) {
+        s11 = ten_max; s22 = ten_max; s12 = R(0.0); s33 = ten_max;
+        return;
+    }
+    if (s3 >= ten_max) s3 = ten_max;
+    R cs2, si2;
+    if (psdif == R(0.0)) {
+        cs2 = R(1.0);
+        si2 = R(0.0);
+    } else {
+        cs2 = sdif / psdif;
+        si2 = R(2.0) * s12i / psdif;
+    }
+    R dc2 = (s1 - s3) * cs2;
+    R dss = s1 + s3;
+    s11 = R(0.5) * (dss + dc2);
+    s22 = R(0.5) * (dss - dc2);
+    s12 = R(0.5) * (s1 - s3) * si2;
+    s33 = s2;
+}
+
+// pre_plast (rh_plastic.f90:339-399)
+template <class R>
+__device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, long long e,
+                                          R aps_e, R &coh, R &phi, R &psi, R &hardn) {
+    R pls_curr = aps_e;
+    phi = 0; coh = 0; psi = 0; hardn = 0;
+    for (int k = 0; k < P.nphase; ++k) {
+        R ratio = R(A.phase_ratio[gf_pr(d, e, k)]);
+        if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
+        R f, c, dd, h;
+        R pl1 = R(P.plstrain1[k]), pl2 = R(P.plstrain2[k]);
+        if (pls_curr < pl1) {
+            f = R(P.fric1[k]); c = R(P.cohesion1[k]); dd = R(P.dilat1[k]); h = 0;
+        } else if (pls_curr < pl2) {
+            R dpl = (pls_curr - pl1) / (pl2 - pl1);
+            f = R(P.fric1[k]) + (R(P.fric2[k]) - R(P.fric1[k])) * dpl;
+            dd = R(P.dilat1[k]) + (R(P.dilat2[k]) - R(P.dilat1[k])) * dpl;
+            c = R(P.cohesion1[k]) + (R(P.cohesion2[k]) - R(P.cohesion1[k])) * dpl;
+            h = (R(P.cohesion2[k]) - R(P.cohesion1[k])) / (pl2 - pl1);
+        } else {
+            f = R(P.fric2[k]); c = R(P.cohesion2[k]); dd = R(P.dilat2[k]); h = 0;
+        }
+        phi = phi + ratio / f;
+        coh = coh + ratio / c;
+        psi = psi + ratio * dd;
+        hardn = hardn + ratio * h;
+    }
+    phi = R(1) / phi;
+    coh = R(1) / coh;
+    if (P.itype_melting == 1) {
+        R fma = R(fmin(A.fmagma[e] + A.fmagma2[e], P.fmagma_max));
+        R fm = R(P.fmagma_max), w = R(P.weaken_ratio_plastic);
+        phi = phi * (R(1) - (R(1) - w) * fma / fm);
+        coh = coh * (R(1) - (R(1) - w) * fma / fm);
+    }
+}
+
+} // namespace gfk
+} // namespace

@@ -1,0 +1,1097 @@
+// Kernel bodies and launchers of the FLAC step; included once per precision.
+#pragma once
+
+#include "gf_kernels.cuh"
+
+// internal linkage: each precision's translation unit has its own copy
+namespace {
+namespace gfk {
+
+__device__ __forceinline__ void elem_ji(const GfDims &d, long long e, int &j, int &i) {
+    i = (int)(e / (d.nz - 1));
+    j = (int)(e - (long long)i * (d.nz - 1));
+}
+__device__ __forceinline__ void node_ji(const GfDims &d, long long n, int &j, int &i) {
+    i = (int)(n / d.nz);
+    j = (int)(n - (long long)i * d.nz);
+}
+
+inline unsigned grid_for(long long n) { return (unsigned)((n + GF_THREADS - 1) / GF_THREADS); }
+
+// ======================================================================
+// fl_rheol (fl_rheol.f90:4-389): one thread per element.
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                      DevArrays A, GfDims d, int update_visc, int nloop) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const DevParams &P = *Pp;
+    int j, i;
+    elem_ji(d, e, j, i);
+    const double dtd = C->dt;
+    const R dt = R(dtd);
+    R *st = (R *)A.stress0;
+    const R *area = (const R *)A.area;
+
+    const double *vel = A.vel;
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    R vx[4], vy[4];
+    vx[0] = R(vel[n1]); vx[1] = R(vel[n1 + 1]); vx[2] = R(vel[n3]); vx[3] = R(vel[n3 + 1]);
+    vy[0] = R(vel[d.N + n1]); vy[1] = R(vel[d.N + n1 + 1]); vy[2] = R(vel[d.N + n3]); vy[3] = R(vel[d.N + n3 + 1]);
+    Quad q;
+    load_quad(A.cord, d, j, i, q);
+    R ar[4];
+    for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
+    R dx[3][4], dz[3][4], sr[3][4];
+    shape_derivs<R>(q, ar, dx, dz);
+    // node triplets of triangles A,B,C,D: (1,2,3), (3,2,4), (1,2,4), (1,4,3)
+    const int tn[4][3] = {{0, 1, 2}, {2, 1, 3}, {0, 1, 3}, {0, 3, 2}};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        R a0 = vx[tn[k][0]], a1 = vx[tn[k][1]], a2 = vx[tn[k][2]];
+        R b0 = vy[tn[k][0]], b1 = vy[tn[k][1]], b2 = vy[tn[k][2]];
+        sr[0][k] = a0 * dx[0][k] + a1 * dx[1][k] + a2 * dx[2][k];
+        sr[1][k] = b0 * dz[0][k] + b1 * dz[1][k] + b2 * dz[2][k];
+        sr[2][k] = R(0.5) * (a0 * dz[0][k] + a1 * dz[1][k] + a2 * dz[2][k] + b0 * dx[0][k] + b1 * dx[1][k] + b2 * dx[2][k]);
+    }
+    if (P.mix_strain == 1) {
+#pragma unroll
+        for (int k = 0; k < 4; k += 2) {
+            R em = R(0.5) * (sr[0][k] + sr[1][k] + sr[0][k + 1] + sr[1][k + 1]);
+            R eda = sr[0][k] - sr[1][k];
+            R edb = sr[0][k + 1] - sr[1][k + 1];
+            sr[0][k] = R(0.5) * (em + eda);
+            sr[1][k] = R(0.5) * (em - eda);
+            sr[0][k + 1] = R(0.5) * (em + edb);
+            sr[1][k + 1] = R(0.5) * (em - edb);
+        }
+    }
+    R *se2sr = (R *)A.se2sr;
+    R *sshrheat = (R *)A.sshrheat;
+    R s11 = R(0.25) * (sr[0][0] + sr[0][1] + sr[0][2] + sr[0][3]);
+    R s22 = R(0.25) * (sr[1][0] + sr[1][1] + sr[1][2] + sr[1][3]);
+    R s12 = R(0.25) * (sr[2][0] + sr[2][1] + sr[2][2] + sr[2][3]);
+    R srII = R(0.5) * m_sqrt((s11 - s22) * (s11 - s22) + R(4.0) * s12 * s12);
+    R srI = R(0.5) * (s11 + s22);
+    R srs2 = (s11 - srI) * (s11 - srI) + (s22 - srI) * (s22 - srI) + R(2.0) * s12 * s12;
+    se2sr[gf_ek(d, e, 0)] = se2sr[gf_ek(d, e, 0)] + s11 * dt;
+    se2sr[gf_ek(d, e, 1)] = se2sr[gf_ek(d, e, 1)] + s22 * dt;
+    se2sr[gf_ek(d, e, 2)] = se2sr[gf_ek(d, e, 2)] + s12 * dt;
+    R s0v[4][4]; // start-of-step stresses [comp][tri]
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) s0v[c][k] = st[gf_s(d, e, c, k)];
+    s11 = R(0.25) * (s0v[0][0] + s0v[0][1] + s0v[0][2] + s0v[0][3]);
+    s22 = R(0.25) * (s0v[1][0] + s0v[1][1] + s0v[1][2] + s0v[1][3]);
+    s12 = R(0.25) * (s0v[2][0] + s0v[2][1] + s0v[2][2] + s0v[2][3]);
+    R stII = R(0.5) * m_sqrt((s11 - s22) * (s11 - s22) + R(4.0) * s12 * s12);
+    R shr = sshrheat[e];
+    if (srII != R(0.0)) shr = shr + stII / srII * srs2 * dt;
+
+    int iph = A.iphase[e] - 1;
+    int irh = P.irheol[iph];
+    R bulkm = R(P.rl[iph] + 2.0 * P.rm[iph] / 3.0);
+    R rmu = R(P.rm[iph]);
+    R stherm = R(0.0);
+    if (P.istress_therm > 0)
+        stherm = R(-P.alfa[iph] * (P.rl[iph] + 2.0 * P.rm[iph] / 3.0) * (A.temp[n1] - A.temp0[n1]));
+    R *aps = (R *)A.aps;
+    R aps_e = aps[e];
+    R coh = 0, phi = 0, psi = 0, hardn = 0;
+    if (irh == 6 || irh >= 11) pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
+    R *visn = (R *)A.visn;
+    R vis;
+    if ((irh == 3 || irh >= 11) && update_visc) {
+        vis = R(eff_visc<R>(P, A, d, j, i, e, st));
+        visn[e] = vis;
+    } else {
+        vis = visn[e];
+    }
+    PlasticConsts<R> pc;
+    if (irh == 6 || irh >= 11) pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi, R(P.ten_off));
+    R dike = A.dike_released ? R(A.dike_released[e]) : R(0);
+    const R *dvol = (const R *)A.dvol;
+    R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        R de11 = sr[0][k] * dt, de22 = sr[1][k] * dt, de12 = sr[2][k] * dt, de33 = R(0.0);
+        R dv = dvol[gf_ek(d, e, k)] - dike;
+        sp[0][k] = s0v[0][k] + stherm;
+        sp[1][k] = s0v[1][k] + stherm;
+        sp[2][k] = s0v[2][k];
+        sp[3][k] = s0v[3][k] + stherm;
+        sv[0][k] = sp[0][k]; sv[1][k] = sp[1][k]; sv[2][k] = sp[2][k]; sv[3][k] = sp[3][k];
+        if (irh == 1) {
+            elastic<R>(bulkm, rmu, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de12);
+        } else if (irh == 3) {
+            ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
+        } else if (irh == 6) {
+            plastic<R>(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12);
+        } else if (irh >= 11) {
+            plastic<R>(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12);
+            ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
+        }
+    }
+    if (!ok) set_status(C, 22, (int)e);
+    R sn[4][4]; // new stresses [comp][tri]
+    bool use_visc = (irh == 3);
+    if (irh >= 11) {
+        R a = sp[0][0] + sp[0][1] + sp[0][2] + sp[0][3] - sp[1][0] - sp[1][1] - sp[1][2] - sp[1][3];
+        R b = sp[2][0] + sp[2][1] + sp[2][2] + sp[2][3];
+        R sII_plas = a * a + R(4.0) * (b * b);
+        a = sv[0][0] + sv[0][1] + sv[0][2] + sv[0][3] - sv[1][0] - sv[1][1] - sv[1][2] - sv[1][3];
+        b = sv[2][0] + sv[2][1] + sv[2][2] + sv[2][3];
+        R sII_visc = a * a + R(4.0) * (b * b);
+        use_visc = !(sII_plas < sII_visc);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) sn[c][k] = use_visc ? sv[c][k] : sp[c][k];
+    if (P.mix_stress == 1) {
+#pragma unroll
+        for (int h = 0; h < 4; h += 2) {
+            R ra = ar[h], rb = ar[h + 1];
+            R quad_area = R(1.0) / ra + R(1.0) / rb;
+            R s0a = R(0.5) * (sn[0][h] + sn[1][h]);
+            R s0b = R(0.5) * (sn[0][h + 1] + sn[1][h + 1]);
+            R s0 = (s0a / rb + s0b / ra) / quad_area;
+            sn[0][h] = sn[0][h] - s0a + s0;
+            sn[1][h] = sn[1][h] - s0a + s0;
+            sn[0][h + 1] = sn[0][h + 1] - s0b + s0;
+            sn[1][h + 1] = sn[1][h + 1] - s0b + s0;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        sn[0][k] = sn[0][k] - stherm;
+        sn[1][k] = sn[1][k] - stherm;
+        sn[3][k] = sn[3][k] - stherm;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = sn[c][k];
+    if (irh == 6 || irh >= 11) {
+        R quad_area = ar[0] + ar[1] + ar[2] + ar[3];
+        aps_e = aps_e + (depl[0] * ar[0] + depl[1] * ar[1] + depl[2] * ar[2] + depl[3] * ar[3]) / quad_area;
+        if (aps_e < R(0.0)) aps_e = R(0.0);
+        if (P.tau_heal != 0.0) aps_e = aps_e / (R(1.0) + dt / R(P.tau_heal));
+        aps[e] = aps_e;
+    }
+    // accumulates the element-averaged start-of-step stress (s11/s22/s12 are
+    // reassigned before this point in fl_rheol.f90:181-183)
+    R *strain = (R *)A.strain;
+    strain[gf_ek(d, e, 0)] = strain[gf_ek(d, e, 0)] + s11 * dt;
+    strain[gf_ek(d, e, 1)] = strain[gf_ek(d, e, 1)] + s22 * dt;
+    strain[gf_ek(d, e, 2)] = strain[gf_ek(d, e, 2)] + s12 * dt;
+    if (P.ishearh == 1) {
+        R qsum = R(0.0);
+        R lambda = bulkm - R(2.0 / 3.0) * rmu, mu = rmu;
+        R den_el = R(3.0) * lambda + R(2.0) * mu;
+        if (m_abs(den_el) < R(1e-30)) den_el = den_el < R(0) ? R(-1e-30) : R(1e-30);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
+            R tr0 = s0v[0][k] + s0v[1][k] + s0v[3][k];
+            R e11a = (s0v[0][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+            R e22a = (s0v[1][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+            R e33a = (s0v[3][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+            R e12a = s0v[2][k] / (R(2.0) * mu);
+            R tr1 = f11 + f22 + f33;
+            R e11b = (f11 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+            R e22b = (f22 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+            R e33b = (f33 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+            R e12b = f12 / (R(2.0) * mu);
+            R d11 = sr[0][k] * dt - (e11b - e11a);
+            R d22 = sr[1][k] * dt - (e22b - e22a);
+            R d12 = sr[2][k] * dt - (e12b - e12a);
+            R d33 = R(0.0) - (e33b - e33a);
+            R a11 = R(0.5) * (s0v[0][k] + f11), a22 = R(0.5) * (s0v[1][k] + f22), a12 = R(0.5) * (s0v[2][k] + f12),
+              a33 = R(0.5) * (s0v[3][k] + f33);
+            R qk = a11 * d11 + a22 * d22 + R(2.0) * a12 * d12 + a33 * d33;
+            qsum = qsum + R(0.25) * qk;
+        }
+        shr = shr + qsum;
+    }
+    sshrheat[e] = shr;
+    (void)nloop;
+}
+
+// Periodic time averaging (fl_rheol.f90:393-421); mode 1 resets the sums.
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    R *se2sr = (R *)A.se2sr;
+    R *e2sr = (R *)A.e2sr;
+    R *shrheat = (R *)A.shrheat;
+    R *sshrheat = (R *)A.sshrheat;
+    R dtavg = R(C->dtavg);
+    R a = se2sr[gf_ek(d, e, 0)], b = se2sr[gf_ek(d, e, 1)], q = se2sr[gf_ek(d, e, 2)];
+    e2sr[e] = (R(0.5) * m_sqrt((a - b) * (a - b) + R(4.0) * q * q)) / dtavg;
+    shrheat[e] = sshrheat[e] / dtavg;
+    if (reset) {
+        se2sr[gf_ek(d, e, 0)] = R(0.0);
+        se2sr[gf_ek(d, e, 1)] = R(0.0);
+        se2sr[gf_ek(d, e, 2)] = R(0.0);
+        sshrheat[e] = R(0.0);
+    }
+}
+
+// scalar bookkeeping of fl_rheol: dtavg += dt at entry; dtavg = 0 at a reset
+__global__ void k_rheol_clock(DevClock *C, int phase) {
+    if (phase == 0)
+        C->dtavg = C->dtavg + C->dt;
+    else
+        C->dtavg = 0.0;
+}
+
+// ======================================================================
+// fl_node (fl_node.f90:3-393): one thread per node, forces gathered from
+// the 4 adjacent quads in the reference's order, no atomics.
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                     DevArrays A, GfDims d) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    const DevParams &P = *Pp;
+    int j, i;
+    node_ji(d, n, j, i);
+    const int nx = d.nx, nz = d.nz;
+    const R *st = (const R *)A.stress0;
+    const R *area = (const R *)A.area;
+    // kk/mm tables of fl_node.f90:7-8 (0-based)
+    const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
+    const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
+    R fx0 = R(0.0), fy0 = R(0.0);
+#pragma unroll
+    for (int qd = 0; qd < 4; ++qd) {
+        int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+        if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
+        long long e = gf_elem(d, je, ie);
+        Quad q;
+        load_quad(A.cord, d, je, ie, q);
+        R ar[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
+        R dx[3][4], dz[3][4];
+        shape_derivs<R>(q, ar, dx, dz);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int t = kk[qd][k], m = mm[qd][k];
+            R factor = R(0.25) / ar[t];
+            R sxx = st[gf_s(d, e, 0, t)], szz = st[gf_s(d, e, 1, t)], sxz = st[gf_s(d, e, 2, t)];
+            R fx = factor * (sxx * dx[m][t] + sxz * dz[m][t]);
+            R fy = factor * (sxz * dx[m][t] + szz * dz[m][t]);
+            fx0 = fx0 - fx;
+            fy0 = fy0 - fy;
+        }
+    }
+    double f0 = (double)fx0;
+    double f1 = (double)fy0 - A.rmass[n] * P.g;
+    const double *cord = A.cord;
+    if (P.nyhydro > 0 && j == 0) { // water load on the surface
+        double rho_water_g = 1030.0 * P.g;
+        double water_depth = (i < nx - 1) ? 0.5 * (cord[d.N + gf_node(d, 0, i + 1)] + cord[d.N + gf_node(d, 0, i)])
+                                          : 0.5 * (cord[d.N + gf_node(d, 0, i - 1)] + cord[d.N + gf_node(d, 0, i)]);
+        if (water_depth < 0.0) {
+            double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
+            if (i > 0) {
+                pl = rho_water_g * ((cord[d.N + gf_node(d, 0, i - 1)] + cord[d.N + gf_node(d, 0, i)]) / 2.0);
+                dlxl = cord[gf_node(d, 0, i)] - cord[gf_node(d, 0, i - 1)];
+                dlyl = cord[d.N + gf_node(d, 0, i)] - cord[d.N + gf_node(d, 0, i - 1)];
+            }
+            if (i < nx - 1) {
+                pr = rho_water_g * ((cord[d.N + gf_node(d, 0, i + 1)] + cord[d.N + gf_node(d, 0, i)]) / 2.0);
+                dlxr = cord[gf_node(d, 0, i + 1)] - cord[gf_node(d, 0, i)];
+                dlyr = cord[d.N + gf_node(d, 0, i + 1)] - cord[d.N + gf_node(d, 0, i)];
+            }
+            f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
+            f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
+        }
+    }
+    if (P.nyhydro > 0 && j == nz - 1) { // Winkler foundation
+        int ips = P.iphsub - 1;
+        double zb = cord[d.N + n];
+        double p_est = P.pisos + 0.5 * (P.den[ips] + P.drosub) * P.g * (zb - P.rzbo);
+        double rosubg = P.g * (P.den[ips] + P.drosub) * (1 - P.alfa[ips] * A.temp[n] + P.beta[ips] * p_est);
+        double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
+        if (i > 0) {
+            long long m = gf_node(d, nz - 1, i - 1);
+            pl = P.pisos - rosubg * ((cord[d.N + m] + zb) / 2.0 - P.rzbo);
+            dlxl = cord[n] - cord[m];
+            dlyl = zb - cord[d.N + m];
+        }
+        if (i < nx - 1) {
+            long long m = gf_node(d, nz - 1, i + 1);
+            pr = P.pisos - rosubg * ((cord[d.N + m] + zb) / 2.0 - P.rzbo);
+            dlxr = cord[m] - cord[n];
+            dlyr = cord[d.N + m] - zb;
+        }
+        f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
+        f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
+    }
+    double dt = C->dt;
+    double drat = dt / C->dt_elastic;
+    if (drat < 1.0) drat = 1.0;
+    double *vel = A.vel;
+    double v0 = vel[n], v1 = vel[d.N + n];
+    int c0 = A.ncod[n], c1 = A.ncod[d.N + n];
+    if ((c0 & 1) != 1 && fabs(v0) > 1.0e-13) f0 = f0 - P.demf * copysign(fabs(f0), v0);
+    if ((c1 & 2) != 2 && fabs(v1) > 1.0e-13) f1 = f1 - P.demf * copysign(fabs(f1), v1);
+    double am = A.amass[n];
+    v0 = (c0 == 1) ? A.bc[n] : v0 + dt * f0 / (am * drat * drat);
+    v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + dt * f1 / (am * drat * drat);
+    if (P.i_prestress == 1 && C->time < 600e3 * GF_SEC_YEAR) {
+        if (j == nz - 1 || i == 0 || i == nx - 1) {
+            v0 = 0.0;
+            v1 = 0.0;
+        }
+    }
+    vel[n] = v0;
+    vel[d.N + n] = v1;
+}
+
+// ======================================================================
+// fl_move (fl_move.f90:3-132)
+__global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= 2 * d.N) return;
+    A.cord[n] = A.cord[n] + A.vel[n] * C->dt;
+}
+
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    int j, i;
+    elem_ji(d, e, j, i);
+    const double dtd = C->dt;
+    Quad q;
+    load_quad(A.cord, d, j, i, q);
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    const double *vel = A.vel;
+    double xv[4] = {vel[n1], vel[n1 + 1], vel[n3], vel[n3 + 1]};
+    double yv[4] = {vel[d.N + n1], vel[d.N + n1 + 1], vel[d.N + n3], vel[d.N + n3 + 1]};
+    R *area = (R *)A.area;
+    R *dvol = (R *)A.dvol;
+    R *st = (R *)A.stress0;
+    R *strain = (R *)A.strain;
+    const int nd1[4] = {0, 2, 0, 0}, nd2[4] = {1, 1, 1, 3}, nd3[4] = {2, 3, 3, 2};
+    bool neg = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int a = nd1[k], b = nd2[k], c = nd3[k];
+        const double *xc = q.x, *yc = q.y;
+        double det = ((xc[b] * yc[c] - yc[b] * xc[c]) - (xc[a] * yc[c] - yc[a] * xc[c])) + (xc[a] * yc[b] - yc[a] * xc[b]);
+        R ar_old = area[gf_ek(d, e, k)];
+        dvol[gf_ek(d, e, k)] = R(det * (double)ar_old - 1.0);
+        R ar_new = R(1.0 / det);
+        area[gf_ek(d, e, k)] = ar_new;
+        neg |= !(ar_new > R(0));
+        double dw = 0.5 * (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) + yv[a] * (yc[c] - yc[b]) +
+                           yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])) /
+                    det * dtd;
+        R dw12 = R(dw);
+        R s11 = st[gf_s(d, e, 0, k)], s22 = st[gf_s(d, e, 1, k)], s12 = st[gf_s(d, e, 2, k)];
+        st[gf_s(d, e, 0, k)] = s11 + s12 * R(2) * dw12;
+        st[gf_s(d, e, 1, k)] = s22 - s12 * R(2) * dw12;
+        st[gf_s(d, e, 2, k)] = s12 + dw12 * (s22 - s11);
+        if (k == 0) {
+            R e11 = strain[gf_ek(d, e, 0)], e22 = strain[gf_ek(d, e, 1)], e12 = strain[gf_ek(d, e, 2)];
+            strain[gf_ek(d, e, 0)] = e11 + e12 * R(2) * dw12;
+            strain[gf_ek(d, e, 1)] = e22 - e12 * R(2) * dw12;
+            strain[gf_ek(d, e, 2)] = e12 + dw12 * (e22 - e11);
+        }
+    }
+    if (neg) set_status(C, 40, (int)e);
+}
+
+// ======================================================================
+// fl_therm (fl_therm.f90:393-598).
+//
+// The reference updates temp in place, i outer and j inner: node (j,i) reads
+// new values at its upstream neighbours (j-1,i), (j,i-1), (j+1,i-1) and old
+// values at itself and downstream.  Its result is the unique fixed point of
+//   Tnew(n) = f_n(Tnew(upstream), Told(rest))
+// with f_n the reference's floating-point expression.  The system is lower
+// triangular, so iterating Jacobi-style sweeps of f_n from Told reaches that
+// fixed point exactly (bit for bit) after finitely many sweeps; each sweep
+// contracts the distance by ~kappa*dt/h^2, so a handful of sweeps suffice.
+// A sweep that changes no value proves convergence; later sweeps exit at once.
+//
+// k_therm_prep computes, per element, everything of the triangles A and B that
+// does not depend on temperature (fl_therm.f90:424-567): the shape-derivative
+// products K_ab, real_area13 = (1/area)/6, 0.5*diff/area and
+// src*real_area13, each with the reference's operations.
+
+#define GF_TC 18 // doubles per element: KA[6], KB[6], raA, raB, preA, preB, srA, srB
+// K index of (a,b), a,b in 0..2 (symmetric)
+__device__ __forceinline__ int kidx(int a, int b) {
+    int lo = a < b ? a : b, hi = a < b ? b : a;
+    return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
+
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
+                                                           double *__restrict__ tc) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const DevParams &P = *Pp;
+    int j, i;
+    elem_ji(d, e, j, i);
+    int iph = A.iphase[e] - 1;
+    double cp_eff = P.cp[iph], cond_eff = P.conduct[iph];
+    double dissip = (P.ishearh == 1 && P.itherm != 2) ? (double)((const R *)A.shrheat)[e] : 0.0;
+    double diff = cond_eff / P.den[iph] / cp_eff;
+    double src = (A.source[e] + dissip / P.den[iph]) / cp_eff;
+    Quad q;
+    load_quad(A.cord, d, j, i, q);
+    const R *area = (const R *)A.area;
+    const long long E = d.E;
+    // triangle A: local vertices (q1,q2,q3); triangle B: (q3,q2,q4)
+    const int tv[2][3] = {{0, 1, 2}, {2, 1, 3}};
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        double a = (double)area[gf_ek(d, e, t)];
+        double y1 = q.y[tv[t][0]], y2 = q.y[tv[t][1]], y3 = q.y[tv[t][2]];
+        double x1 = q.x[tv[t][0]], x2 = q.x[tv[t][1]], x3 = q.x[tv[t][2]];
+        double dd[3] = {(y2 - y3) * a, (y3 - y1) * a, (y1 - y2) * a};
+        double zz[3] = {(x3 - x2) * a, (x1 - x3) * a, (x2 - x1) * a};
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = dd[m] * dd[n] + zz[m] * zz[n];
+        double inv_area = 1.0 / a;
+        double ra = inv_area / 6.0;
+        tc[(12 + t) * E + e] = ra;
+        tc[(14 + t) * E + e] = 0.5 * diff * inv_area;
+        tc[(16 + t) * E + e] = src * ra;
+    }
+}
+
+// One sweep.  Tup holds the current iterate (Told for sweep 0); self and
+// downstream values always come from Told (A.temp).
+__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d,
+                                                            const double *__restrict__ tc,
+                                                            const double *__restrict__ Tup, double *__restrict__ Tout,
+                                                            int k) {
+    if (k > 0 && C->therm_flags[k - 1] == 0) return; // converged one sweep ago
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool changed = false;
+    if (n < d.N) {
+        int j, i;
+        node_ji(d, n, j, i);
+        const int nx = d.nx, nz = d.nz;
+        const long long E = d.E;
+        const double *T = A.temp;
+        double rhs = 0.0, area_n = 0.0;
+        auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
+        // triangle t of element e; vs = local index of the updated node; the
+        // three (local vertex, temperature) terms in the reference's order
+        auto tri = [&](long long e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
+            double ra = tc[(12 + t) * E + e];
+            area_n = area_n + ra;
+            const double *K = tc + (long long)t * 6 * E + e;
+            rhs = rhs + tc[(16 + t) * E + e] -
+                  tc[(14 + t) * E + e] * (T0 * K[kidx(v0, vs) * E] + T1 * K[kidx(v1, vs) * E] + T2 * K[kidx(v2, vs) * E]);
+        };
+        double Ts = T[n];
+        if (j != 0 && i != 0) // element (j-1,i-1), triangle B: vertices (j-1,i), (j,i-1), node
+            tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, Tup[Nd(j - 1, i)], 1, Tup[Nd(j, i - 1)], 2, Ts);
+        if (j != 0 && i != nx - 1) { // element (j-1,i), triangles A and B
+            long long e = gf_elem(d, j - 1, i);
+            tri(e, 0, 1, 0, Tup[Nd(j - 1, i)], 1, Ts, 2, T[Nd(j - 1, i + 1)]);
+            tri(e, 1, 1, 0, T[Nd(j - 1, i + 1)], 1, Ts, 2, T[Nd(j, i + 1)]);
+        }
+        if (j != nz - 1 && i != 0) { // element (j,i-1), triangles A and B
+            long long e = gf_elem(d, j, i - 1);
+            tri(e, 0, 2, 0, Tup[Nd(j, i - 1)], 1, Tup[Nd(j + 1, i - 1)], 2, Ts);
+            tri(e, 1, 0, 0, Ts, 1, Tup[Nd(j + 1, i - 1)], 2, T[Nd(j + 1, i)]);
+        }
+        if (j != nz - 1 && i != nx - 1) // element (j,i), triangle A
+            tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
+        double tn = Ts + rhs * C->dt / area_n;
+        Tout[n] = tn;
+        changed = (tn != Tup[n]);
+    }
+    if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
+}
+
+// temp0 = temp; temp = converged iterate (fl_therm.f90:46-48, 569)
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(DevClock *__restrict__ C, DevArrays A, GfDims d,
+                                                            const double *__restrict__ b0,
+                                                            const double *__restrict__ b1, int kmax) {
+    int kc = kmax;
+    for (int k = 0; k < kmax; ++k)
+        if (C->therm_flags[k] == 0) {
+            kc = k;
+            break;
+        }
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n == 0) {
+        C->therm_sweeps_used = kc + 1;
+        if (kc == kmax) C->therm_unconverged += 1;
+    }
+    if (n >= d.N) return;
+    // sweep kc (or the last one) wrote buffer kc & 1
+    int k = kc < kmax ? kc : kmax - 1;
+    const double *src = (k & 1) ? b1 : b0;
+    A.temp0[n] = A.temp[n];
+    A.temp[n] = src[n];
+}
+
+__global__ void k_therm_reset(DevClock *C) {
+    for (int k = 0; k < GF_THERM_KMAX; ++k) C->therm_flags[k] = 0;
+}
+
+__global__ void k_therm_bc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    const DevParams &P = *Pp;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = d.nx, nz = d.nz;
+    // top and bottom rows first (all columns), then the side columns: one
+    // block does everything in the reference's order (nx, nz are small).
+    for (int i = t; i < nx; i += blockDim.x) {
+        A.temp[gf_node(d, 0, i)] = P.t_top;
+        if (P.itemp_bc == 1)
+            A.temp[gf_node(d, nz - 1, i)] = P.bot_bc;
+        else if (P.itemp_bc == 2) {
+            int ie = i < nx - 2 ? i : nx - 2;
+            double cond_eff = P.conduct[A.iphase[gf_elem(d, nz - 2, ie)] - 1];
+            A.temp[gf_node(d, nz - 1, i)] =
+                A.temp[gf_node(d, nz - 2, i)] +
+                P.bot_bc * (A.cord[d.N + gf_node(d, nz - 2, i)] - A.cord[d.N + gf_node(d, nz - 1, i)]) / cond_eff;
+        }
+    }
+    __syncthreads();
+    for (int j = t; j < nz; j += blockDim.x) {
+        A.temp[gf_node(d, j, 0)] = A.temp[gf_node(d, j, 1)];
+        A.temp[gf_node(d, j, nx - 1)] = A.temp[gf_node(d, j, nx - 2)];
+    }
+}
+
+// ======================================================================
+// rmasses (rmasses.f90:236-295): per-element density, then a node gather in
+// the reference's colour order with each element's triangles in order.
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                          DevArrays A, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    int j, i;
+    elem_ji(d, e, j, i);
+    int wrote = 0;
+    double fval = 0.0;
+    A.e_dens[e] = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
+    if (wrote) {
+        // serial position of this element in the coloured sweep
+        int ib = i & 1, jb = j & 1;
+        long long ci = (long long)(d.nx - 1 - ib + 1) / 2; // columns of this colour
+        long long cj = (long long)(d.nz - 1 - jb + 1) / 2;
+        long long before = 0;
+        for (int b = 0; b < ib * 2 + jb; ++b) {
+            int bi = b >> 1, bj = b & 1;
+            before += (long long)((d.nx - 1 - bi + 1) / 2) * ((d.nz - 1 - bj + 1) / 2);
+        }
+        long long pos = before + (long long)(i >> 1) * cj + (j >> 1);
+        (void)ci;
+        atomicMax((unsigned long long *)&C->frac_writer, (unsigned long long)(pos + 1));
+    }
+}
+
+template <class R>
+__global__ void k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    long long w = C->frac_writer;
+    if (w <= 0) return;
+    long long pos = w - 1;
+    for (int b = 0; b < 4; ++b) {
+        int bi = b >> 1, bj = b & 1;
+        long long ci = (d.nx - 1 - bi + 1) / 2, cj = (d.nz - 1 - bj + 1) / 2;
+        if (pos < ci * cj) {
+            int i = (int)(pos / cj) * 2 + bi, j = (int)(pos % cj) * 2 + bj;
+            int wrote = 0;
+            double f = 0.0;
+            eff_dens<R>(*Pp, A, d, j, i, gf_elem(d, j, i), &wrote, &f);
+            if (wrote) C->frac = f;
+            break;
+        }
+        pos -= ci * cj;
+    }
+    C->frac_writer = 0;
+}
+
+// Contribution lists: for local vertex v of a quad (1:(j,i) 2:(j+1,i)
+// 3:(j,i+1) 4:(j+1,i+1)), the triangles that contain it, in order.
+__device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3}, {1, 2, 3}};
+
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_node_rmass(DevArrays A, GfDims d) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    int j, i;
+    node_ji(d, n, j, i);
+    const R *area = (const R *)A.area;
+    const double c1d12 = 1.0 / 12.0;
+    double acc = 0.0;
+    // adjacent elements in colour order: colour index = (ie&1)*2 + (je&1)
+    int ord[4];
+    // the node is vertex 4 of quad (j-1,i-1), 2 of (j-1,i), 3 of (j,i-1), 1 of (j,i)
+    int je_[4] = {j - 1, j - 1, j, j}, ie_[4] = {i - 1, i, i - 1, i}, lv[4] = {3, 1, 2, 0};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ord[q] = ((ie_[q] & 1) << 1) | (je_[q] & 1);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (ord[q] != c) continue;
+            int je = je_[q], ie = ie_[q];
+            if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
+            long long e = gf_elem(d, je, ie);
+            double dens = A.e_dens[e];
+#pragma unroll
+            for (int t = 0; t < 3; ++t) acc = acc + c1d12 / (double)area[gf_ek(d, e, c_vtx_tris[lv[q]][t])] * dens;
+        }
+    A.rmass[n] = acc;
+}
+
+// ======================================================================
+// dt_mass (dt_mass.f90:16-232)
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                          DevArrays A, GfDims d) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const DevParams &P = *Pp;
+    double dl = 1e300, vmax = 0.0, dmax = 0.0;
+    unsigned pm = 0;
+    if (t < d.E) {
+        long long e = t;
+        int j, i;
+        elem_ji(d, e, j, i);
+        const R *area = (const R *)A.area;
+        Quad q;
+        load_quad(A.cord, d, j, i, q);
+        auto len = [&](int a, int b) {
+            double ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
+            return sqrt(ddx * ddx + ddy * ddy);
+        };
+        double a0 = (double)area[gf_ek(d, e, 0)], a1 = (double)area[gf_ek(d, e, 1)], a2 = (double)area[gf_ek(d, e, 2)],
+               a3 = (double)area[gf_ek(d, e, 3)];
+        double l;
+        l = len(1, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a2 * l));
+        l = len(3, 1); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a2 * l));
+        l = len(3, 2); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+        l = len(2, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+        l = len(3, 0); dl = fmin(dl, 1.0 / (a2 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+        l = len(1, 2); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a1 * l));
+        int iph = A.iphase[e] - 1;
+        dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
+        pm = 1u << iph;
+    }
+    if (t < d.N) vmax = fmax(fabs(A.vel[t]), fabs(A.vel[d.N + t]));
+    dl = warp_min(dl);
+    vmax = warp_max(vmax);
+    dmax = warp_max(dmax);
+    for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
+    if ((threadIdx.x & 31) == 0) {
+        atomic_min_pos(&C->r_dlmin, dl);
+        atomic_max_pos(&C->r_velmax, vmax);
+        atomic_max_pos(&C->r_diffmax, dmax);
+        atomicOr(&C->phase_mask, pm);
+    }
+}
+
+__global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restrict__ C) {
+    const DevParams &P = *Pp;
+    double dlmin = fmin(1e28, __longlong_as_double((long long)C->r_dlmin));
+    double vel_max = __longlong_as_double((long long)C->r_velmax);
+    double diffmax = __longlong_as_double((long long)C->r_diffmax);
+    C->dlmin = dlmin;
+    C->vel_max = vel_max;
+    if (P.idt_scale == 1)
+        C->dt_elastic = P.dt_scale;
+    else if (P.idt_scale == 2) {
+        if (P.vbc == 0)
+            C->dt_elastic = dlmin * C->frac * P.strain_inert / (1.0 / GF_SEC_YEAR / 100);
+        else
+            C->dt_elastic = dlmin * C->frac * P.strain_inert / P.vbc;
+    }
+    // min over elements of dlmin^2/diff == dlmin^2 / max(diff) (rounded
+    // division is monotone in the divisor)
+    double dtmax_therm = 1e28;
+    if (diffmax > 0.0) dtmax_therm = fmin(dtmax_therm, dlmin * dlmin / diffmax);
+    double dt_maxwell = 1e28;
+    double dt_elastic = C->dt_elastic;
+    unsigned pm = C->phase_mask;
+    for (int k = 0; k < P.nphase; ++k) {
+        if (!(pm & (1u << k))) continue;
+        if (P.idt_scale == 0) {
+            // dt_mass.f90:122-126: a running minimum that starts from the
+            // previous dt_elastic
+            double pwave = P.rl[k] + 0.6666 * P.rm[k];
+            double dte = C->frac * dlmin * sqrt(P.den[k] / pwave);
+            dt_elastic = fmin(dt_elastic, dte);
+        }
+        if (P.ivis_present == 1 && (P.irheol[k] == 3 || P.irheol[k] == 12) && P.rm[k] < 1e11) {
+            double visc_cut = 1e10;
+            double rmu = (P.v_min < visc_cut) ? P.rm[k] * P.v_min / visc_cut : P.rm[k];
+            double dt_m = P.v_min / rmu * P.fracm;
+            dt_maxwell = fmin(dt_m, dt_maxwell);
+        }
+    }
+    C->dt_elastic = dt_elastic;
+    C->dt_maxwell = dt_maxwell;
+    C->dtmax_therm = dtmax_therm;
+    C->dt = fmin(fmin(dt_elastic, dt_maxwell), dtmax_therm);
+}
+
+// amass node gather (dt_mass.f90:74-154), colour order as in k_node_rmass
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_node_amass(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                           DevArrays A, GfDims d) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    const DevParams &P = *Pp;
+    int j, i;
+    node_ji(d, n, j, i);
+    if (P.idt_scale == 0) {
+        A.amass[n] = A.rmass[n];
+        return;
+    }
+    const R *area = (const R *)A.area;
+    const double c1d12 = 1.0 / 12.0;
+    double dlmin = C->dlmin, frac = C->frac, dt_elastic = C->dt_elastic, vel_max = C->vel_max;
+    double vel_sound = dlmin * frac / dt_elastic;
+    double acc = 0.0;
+    // the node is vertex 4 of quad (j-1,i-1), 2 of (j-1,i), 3 of (j,i-1), 1 of (j,i)
+    int je_[4] = {j - 1, j - 1, j, j}, ie_[4] = {i - 1, i, i - 1, i}, lv[4] = {3, 1, 2, 0};
+    int ord[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ord[q] = ((ie_[q] & 1) << 1) | (je_[q] & 1);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (ord[q] != c) continue;
+            int je = je_[q], ie = ie_[q];
+            if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
+            long long e = gf_elem(d, je, ie);
+            int iph = A.iphase[e] - 1;
+            double pwave = P.rl[iph] + 0.6666 * P.rm[iph];
+            double rho_inert = pwave / (vel_sound * vel_sound);
+            if (P.i_rey == 1 && vel_max > 0.0) {
+                double rho_inert2 = (P.xReyn * P.v_min) / (vel_max * fabs(P.rzbo));
+                if (rho_inert > rho_inert2) rho_inert = rho_inert2;
+            }
+#pragma unroll
+            for (int t = 0; t < 3; ++t) acc = acc + c1d12 * rho_inert / (double)area[gf_ek(d, e, c_vtx_tris[lv[q]][t])];
+        }
+    A.amass[n] = acc;
+}
+
+__global__ void k_dt_reset(DevClock *C) {
+    C->r_dlmin = (unsigned long long)__double_as_longlong(1e300);
+    C->r_velmax = 0ull;
+    C->r_diffmax = 0ull;
+    C->phase_mask = 0u;
+}
+
+// ======================================================================
+// init_visc
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    int j, i;
+    elem_ji(d, e, j, i);
+    ((R *)A.visn)[e] = R(eff_visc<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
+}
+
+// ======================================================================
+// change_phase (change_phase.f90:35-262)
+__global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
+                                                              int nmarkers) {
+    long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= nmarkers) return;
+    if (A.mark_dead[kk] == 0) return;
+    const DevParams &P = *Pp;
+    const int nz = d.nz;
+    int n = A.mark_ntriag[kk];
+    int k = (n - 1) % 2 + 1;
+    int j = ((n - k) / 2) % (nz - 1);
+    int i = (n - k) / 2 / (nz - 1);
+    double a1 = A.mark_a1[kk], a2 = A.mark_a2[kk];
+    const double *cord = A.cord, *T = A.temp;
+    double yy, tmpr;
+    long long p1, p2, p3;
+    if (k == 1) {
+        p1 = gf_node(d, j, i); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j, i + 1);
+    } else {
+        p1 = gf_node(d, j, i + 1); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j + 1, i + 1);
+    }
+    yy = cord[d.N + p1] * a1 + cord[d.N + p2] * a2 + cord[d.N + p3] * (1 - a1 - a2);
+    tmpr = T[p1] * a1 + T[p2] * a2 + T[p3] * (1 - a1 - a2);
+    double depth = 0.5 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]) - yy;
+    if (depth > 200e3) return;
+    int iph = A.mark_phase[kk];
+    long long e = gf_elem(d, j, i);
+    const double mantle_density = 3000.0;
+    long long total = (long long)P.nphase * d.E;
+    auto pr = [&](long long eb, int ph1) {
+        long long off = (long long)(ph1 - 1) + (long long)P.nphase * eb;
+        return (off < 0 || off >= total) ? 0.0 : A.phase_ratio[off];
+    };
+    int newph = 0;
+    switch (iph) {
+    case 4: case 8: {
+        if (depth > 150e3) break;
+        double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
+        double trpres2 = 2.1e9 + (0.6e9 - 2.1e9) * (tmpr - 730.0) / (670.0 - 730.0);
+        double press = mantle_density * P.g * depth;
+        double pg = fabs(press * 1e-9);
+        double solidus = -5.02 * (pg * pg) + 1.32e2 * pg + 1.09e3 + 35.0;
+        if (press < trpres && press > trpres2) {
+            int jb0 = min(j + 2, nz - 1), jb1 = min(j + 1 + P.nelem_serp, nz - 1);
+            for (int jb = jb0; jb <= jb1; ++jb) {
+                long long eb = gf_elem(d, jb - 1, i);
+                if (pr(eb, 3) > 0.8 || pr(eb, 7) > 0.8 || pr(eb, 1) > 0.8 || pr(eb, 11) > 0.8) {
+                    newph = 9;
+                    break;
+                }
+            }
+        } else if (tmpr >= solidus + 35.0) {
+            newph = 18;
+        }
+        break;
+    }
+    case 10: case 3: case 7: {
+        double press = mantle_density * P.g * depth;
+        if (P.eclogite_rule == 1) {
+            if (tmpr >= 600.0 && press >= 1.5e9) newph = 13;
+        } else {
+            double trpres = -0.3e9 + 2.2e6 * tmpr;
+            double trpres2 = 20.1e9 - 0.0375e9 * tmpr;
+            if (!(tmpr < 400.0 || depth < 20e3 || press < trpres || press < trpres2)) newph = 13;
+        }
+        break;
+    }
+    case 9: {
+        double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
+        double trpres2 = 2.1e9 + (0.2e9 - 2.1e9) * (tmpr - 730.0) / (650.0 - 730.0);
+        double press = mantle_density * P.g * depth;
+        if (!(tmpr < 550.0 || (press < trpres && press > trpres2))) newph = 4;
+        break;
+    }
+    case 1:
+        if (!(tmpr < 80.0 && depth < 2e3)) newph = 11;
+        break;
+    case 11:
+        if (!(tmpr < 250.0 && depth < 7e3)) newph = 17;
+        break;
+    case 17: {
+        double trpres = 0.88e9 - (0.88e9 - 0.704e9) * (710.8 - tmpr) / (710.8 - 662.3);
+        double press = mantle_density * P.g * depth;
+        if (!(press < trpres)) newph = 5;
+        break;
+    }
+    case 5: {
+        double trpres = 0.0e9 - (0.0e9 - 1.2e9) * (500.0 - tmpr) / (500.0 - 600.0);
+        double press = mantle_density * P.g * depth;
+        if (!(press > trpres)) newph = 19;
+        break;
+    }
+    case 16: {
+        double dd = depth - 62e3;
+        double trtmpr = 880 - 35e-9 * (dd * dd);
+        if (!(tmpr < trtmpr)) newph = 4;
+        break;
+    }
+    default:
+        break;
+    }
+    if (newph) {
+        A.e_flag[e] = 1;
+        A.mark_phase[kk] = (int8_t)newph;
+    }
+}
+
+// count_phase_ratio (marker_data.f90:140-172) for flagged elements + aps
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                              DevArrays A, GfDims d, int all) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    if (!all && !A.e_flag[e]) return;
+    const DevParams &P = *Pp;
+    int nm = A.nmark_elem[e];
+    if (nm == 0) {
+        set_status(C, 134, (int)e);
+        return;
+    }
+    int cnt[GF_MAXPH + 1];
+#pragma unroll
+    for (int k = 0; k <= GF_MAXPH; ++k) cnt[k] = 0;
+    for (int m = 0; m < nm; ++m) {
+        int kk = A.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + m];
+        int iph = A.mark_phase[kk - 1];
+        if (iph >= 1 && iph <= GF_MAXPH) cnt[iph] += 1;
+    }
+    int best = 0, iph = 1;
+    for (int k = 1; k <= P.nphase; ++k) {
+        A.phase_ratio[gf_pr(d, e, k - 1)] = cnt[k] / (nm * 1.0);
+        if (cnt[k] > best) {
+            best = cnt[k];
+            iph = k;
+        }
+    }
+    A.iphase[e] = iph;
+    if (!all) {
+        R *aps = (R *)A.aps;
+        R a0 = aps[e];
+        R v = a0 - a0 / R((float)nm);
+        aps[e] = v > R(0.0) ? v : R(0.0);
+        A.e_flag[e] = 0;
+    }
+}
+
+// ======================================================================
+// itest_mesh angle criterion (rem_test.f90:77-118): min over all triangles
+__global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d, unsigned long long *out) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double amin = 180.0;
+    if (e < d.E) {
+        int j, i;
+        elem_ji(d, e, j, i);
+        Quad q;
+        load_quad(A.cord, d, j, i, q);
+        const double raddeg = 180.0 / 3.14159265358979323846;
+        // local vertex ids of the 4 triangles (rem_test.f90:84-92)
+        const int tv[4][3] = {{0, 1, 2}, {1, 3, 2}, {0, 1, 3}, {0, 3, 2}};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            int v[4] = {tv[t][0], tv[t][1], tv[t][2], tv[t][0]};
+            double ang[3];
+#pragma unroll
+            for (int k = 1; k <= 2; ++k) {
+                double xa = q.x[v[k + 1]] - q.x[v[k]], ya = q.y[v[k + 1]] - q.y[v[k]];
+                double xxal = sqrt(xa * xa + ya * ya);
+                double xb = q.x[v[k - 1]] - q.x[v[k]], yb = q.y[v[k - 1]] - q.y[v[k]];
+                double xxbl = sqrt(xb * xb + yb * yb);
+                ang[k] = raddeg * acos((xa * xb + ya * yb) / (xxal * xxbl));
+            }
+            ang[0] = 180.0 - ang[1] - ang[2];
+            amin = fmin(amin, fmin(ang[0], fmin(ang[1], ang[2])));
+        }
+    }
+    amin = warp_min(amin);
+    if ((threadIdx.x & 31) == 0) atomic_min_pos(out, fmax(amin, 0.0));
+}
+
+// FP64 host array -> R device array
+template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = R(src[t]);
+}
+template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) dst[t] = (double)src[t];
+}
+
+} // namespace gfk
+} // namespace
+
+// ---------------------------------------------------------------- launchers
+#define GF_LAUNCH(kern, n, ...)                                                                                        \
+    do {                                                                                                               \
+        if ((n) > 0) {                                                                                                 \
+            kern<<<gfk::grid_for(n), GF_THREADS, 0, g.s>>>(__VA_ARGS__);                                               \
+            ++*g.launches;                                                                                             \
+        }                                                                                                              \
+    } while (0)
+
+template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps) {
+    using namespace gfk;
+    int kmax = sweeps > 0 ? (sweeps < GF_THERM_KMAX ? sweeps : GF_THERM_KMAX) : GF_THERM_KMAX;
+    k_therm_reset<<<1, 1, 0, g.s>>>(g.C);
+    ++*g.launches;
+    GF_LAUNCH(k_therm_prep<R>, g.d.E, g.P, g.A, g.d, g.A.t_coef);
+    double *bufs[2] = {g.A.t_delta0, g.A.t_delta1};
+    for (int k = 0; k < kmax; ++k) {
+        const double *up = k == 0 ? g.A.temp : bufs[(k - 1) & 1];
+        GF_LAUNCH(k_therm_sweep, g.d.N, g.C, g.A, g.d, g.A.t_coef, up, bufs[k & 1], k);
+    }
+    GF_LAUNCH(k_therm_apply, g.d.N, g.C, g.A, g.d, bufs[0], bufs[1], kmax);
+    k_therm_bc<<<1, 1024, 0, g.s>>>(g.P, g.A, g.d);
+    ++*g.launches;
+}
+
+template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {
+    using namespace gfk;
+    k_rheol_clock<<<1, 1, 0, g.s>>>(g.C, 0);
+    ++*g.launches;
+    GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
+    if (avg_mode > 0) {
+        GF_LAUNCH(k_rheol_avg<R>, g.d.E, g.C, g.A, g.d, avg_mode == 2 ? 1 : 0);
+        if (avg_mode == 2) {
+            k_rheol_clock<<<1, 1, 0, g.s>>>(g.C, 1);
+            ++*g.launches;
+        }
+    }
+}
+
+template <class R> void GfKernels<R>::node(const GfLaunch &g) {
+    using namespace gfk;
+    GF_LAUNCH(k_node<R>, g.d.N, g.P, g.C, g.A, g.d);
+}
+
+template <class R> void GfKernels<R>::move(const GfLaunch &g) {
+    using namespace gfk;
+    GF_LAUNCH(k_move_cord, 2 * g.d.N, g.C, g.A, g.d);
+    GF_LAUNCH(k_move_elem<R>, g.d.E, g.C, g.A, g.d);
+}
+
+template <class R> void GfKernels<R>::rmasses(const GfLaunch &g) {
+    using namespace gfk;
+    GF_LAUNCH(k_elem_dens<R>, g.d.E, g.P, g.C, g.A, g.d);
+    k_frac_fix<R><<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d);
+    ++*g.launches;
+    GF_LAUNCH(k_node_rmass<R>, g.d.N, g.A, g.d);
+}
+
+template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
+    using namespace gfk;
+    k_dt_reset<<<1, 1, 0, g.s>>>(g.C);
+    ++*g.launches;
+    long long n = g.d.E > g.d.N ? g.d.E : g.d.N;
+    GF_LAUNCH(k_dt_reduce<R>, n, g.P, g.C, g.A, g.d);
+    k_dt_scalars<<<1, 1, 0, g.s>>>(g.P, g.C);
+    ++*g.launches;
+    GF_LAUNCH(k_node_amass<R>, g.d.N, g.P, g.C, g.A, g.d);
+}
+
+template <class R> void GfKernels<R>::init_visc(const GfLaunch &g) {
+    using namespace gfk;
+    GF_LAUNCH(k_init_visc<R>, g.d.E, g.P, g.A, g.d);
+}
+
+template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarkers) {
+    using namespace gfk;
+    GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
+    GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 0);
+}
+
+template <class R> void GfKernels<R>::min_angle(const GfLaunch &g, double *d_out) {
+    using namespace gfk;
+    GF_LAUNCH(k_min_angle, g.d.E, g.A, g.d, (unsigned long long *)d_out);
+}
+
+template <class R>
+void GfKernels<R>::convert_in(const GfLaunch &g, unsigned mask, const double *src, void *dst, long long n) {
+    using namespace gfk;
+    if (mask)
+        GF_LAUNCH(k_convert<R>, n, src, (R *)dst, n);
+    else
+        GF_LAUNCH(k_convert_back<R>, n, (const R *)dst, (double *)src, n);
+}

@@ -1,0 +1,1350 @@
+// ORACLE -- test infrastructure only, never part of the product path.
+//
+// Serial FP64 restatement of GeoFLAC's explicit time step, written from the
+// reference's Fortran (tan2/geoflac, src/*.f90) loop by loop, in the same
+// evaluation order (left-to-right sums, no FMA contraction: build with
+// -ffp-contract=off).  With one thread it is the parity oracle for the CUDA
+// kernels; with OpenMP threads (loops parallelised where the reference has
+// `!$OMP do`) it is the timed host baseline.
+//
+// It works on the same state as the product (gf_params / gf_clock /
+// gf_layout from include/geoflac_gb300.h, the reference's column-major array
+// layout) so that a test can take one initial state, advance it with both
+// and compare every field.
+//
+// Parity pinning: the reference cannot be compiled in this environment (no
+// Fortran compiler), and it commits no golden outputs.  The oracle is pinned
+// by the reference's known-answer tutorials (elastic bar E_eff = 80 GPa,
+// Maxwell relaxation time 1.584 kyr, Mohr-Coulomb UCS 69.282 MPa) and by
+// hand-derived identities; see tests/test_oracle_known_answers.py.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/geoflac_gb300.h"
+#include "../geoflac_gb300/csrc/gf_index.h"
+#include "../geoflac_gb300/csrc/gf_math.h"
+
+namespace {
+
+int g_threads = 1;
+
+struct Stop {
+    int code;
+};
+
+struct St {
+    gf_params *p;
+    gf_clock *c;
+    gf_layout *L;
+    GfDims d;
+    double cord(int j, int i, int k) const { return L->cord[gf_n2(d, j, i, k)]; }
+    double &cordr(int j, int i, int k) { return L->cord[gf_n2(d, j, i, k)]; }
+    double vel(int j, int i, int k) const { return L->vel[gf_n2(d, j, i, k)]; }
+    double &temp(int j, int i) { return L->temp[gf_node(d, j, i)]; }
+    long long e(int j, int i) const { return gf_elem(d, j, i); }
+    double area(long long e, int k) const { return L->area[gf_ek(d, e, k)]; }
+    double &st(long long e, int c, int k) { return L->stress0[gf_s(d, e, c, k)]; }
+    // phase_ratio(iph, e) with the reference's flat-memory semantics for a
+    // phase id above nphase (read the neighbouring entries, 0 past the end)
+    double pr(long long e, int iph1) const {
+        long long off = (long long)(iph1 - 1) + (long long)p->nphase * e;
+        long long total = (long long)p->nphase * d.E;
+        if (off < 0 || off >= total) return 0.0;
+        return L->phase_ratio[off];
+    }
+};
+
+St make(gf_params *p, gf_clock *c, gf_layout *L) {
+    return St{p, c, L, GfDims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)}};
+}
+
+// --------------------------------------------------------------------------
+// Material functions (src/matprops.f90)
+
+// Eff_dens (matprops.f90:3-83).  Writes the global `frac` exactly where the
+// reference does (matprops.f90:37-39, 48-50); the caller passes the slot.
+double eff_dens(St &s, int j, int i, double *frac_slot) {
+    const gf_params &p = *s.p;
+    double adi_grad = 3e-1, den_ramp_dist = 30e3, amp410 = 0.05, amp660 = 0.085;
+    long long e = s.e(j, i);
+    double zcord = 0.25 * (s.cord(j, i, 1) + s.cord(j + 1, i, 1) + s.cord(j, i + 1, 1) + s.cord(j + 1, i + 1, 1));
+    double tmpr0 = 0.25 * (s.L->temp[gf_node(s.d, j, i)] + s.L->temp[gf_node(s.d, j + 1, i)] +
+                           s.L->temp[gf_node(s.d, j, i + 1)] + s.L->temp[gf_node(s.d, j + 1, i + 1)]);
+    double zsurf = 0.50 * (s.cord(0, i, 1) + s.cord(0, i + 1, 1));
+    double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
+    int iph = s.L->iphase[e];
+    double deptmpr410 = -101.58 * (tmpr + 273.0) - 216828.0;
+    double deptmpr420 = deptmpr410 - den_ramp_dist;
+    double den_amp = 1.0;
+    if (deptmpr410 > zcord) {
+        double f = (deptmpr410 - zcord) / (deptmpr410 - deptmpr420);
+        if (f < 0.0) f = 0.0;
+        if (f > 1.0) f = 1.0;
+        *frac_slot = f;
+        den_amp = 1.0 + amp410 * f;
+    }
+    double deptmpr660 = 66.55 * (tmpr + 273.0) - 788494.0;
+    double deptmpr670 = deptmpr660 - den_ramp_dist;
+    if (deptmpr660 > zcord) {
+        double f = (deptmpr660 - zcord) / (deptmpr660 - deptmpr670);
+        if (f < 0.0) f = 0.0;
+        if (f > 1.0) f = 1.0;
+        *frac_slot = f;
+        den_amp = 1.05 + amp660 * f;
+    }
+    double press = 0;
+    for (int k = 0; k < 4; ++k)
+        press = press - (s.L->stress0[gf_s(s.d, e, 0, k)] + s.L->stress0[gf_s(s.d, e, 1, k)] + s.L->stress0[gf_s(s.d, e, 3, k)]);
+    press = press / 12;
+    double ed = 0.0;
+    for (int k = 0; k < p.nphase; ++k) {
+        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        if (ratio < 0.01) continue;
+        double dens = p.den[k] * (1 - p.alfa[k] * tmpr + p.beta[k] * press);
+        press = dens * p.g * zcord;
+        dens = p.den[k] * (1 - p.alfa[k] * tmpr + p.beta[k] * press);
+        ed = ed + ratio * dens;
+    }
+    if (iph == 4 || iph == 8 || iph == 9 || iph == 16 || iph == 18) ed = ed * den_amp;
+    double fm = (s.L->fmagma ? s.L->fmagma[e] : 0.0) + (s.L->fmagma2 ? s.L->fmagma2[e] : 0.0);
+    double fma = std::min(fm, p.fmagma_max);
+    ed = ed - fma * (ed - p.rho_magma);
+    return ed;
+}
+
+// Eff_visc (matprops.f90:136-215); i, j are 0-based.
+double eff_visc(St &s, int j, int i) {
+    const gf_params &p = *s.p;
+    for (int k = 0; k < p.inhom; ++k)
+        if (p.igeom[k] == 100 && i + 1 >= p.ix1[k] && i + 1 <= p.ix2[k] && j + 1 >= p.iy1[k] && j + 1 <= p.iy2[k])
+            return p.v_min;
+    long long e = s.e(j, i);
+    double adi_grad = 3e-1, r = 8.31448;
+    double zcord = 0.25 * (s.cord(j, i, 1) + s.cord(j + 1, i, 1) + s.cord(j, i + 1, 1) + s.cord(j + 1, i + 1, 1));
+    double tmpr0 = 0.25 * (s.L->temp[gf_node(s.d, j, i)] + s.L->temp[gf_node(s.d, j + 1, i)] +
+                           s.L->temp[gf_node(s.d, j, i + 1)] + s.L->temp[gf_node(s.d, j + 1, i + 1)]);
+    double zsurf = 0.50 * (s.cord(0, i, 1) + s.cord(0, i + 1, 1));
+    double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
+    double s11 = 0.25 * (s.st(e, 0, 0) + s.st(e, 0, 1) + s.st(e, 0, 2) + s.st(e, 0, 3));
+    double s22 = 0.25 * (s.st(e, 1, 0) + s.st(e, 1, 1) + s.st(e, 1, 2) + s.st(e, 1, 3));
+    double s33 = 0.25 * (s.st(e, 3, 0) + s.st(e, 3, 1) + s.st(e, 3, 2) + s.st(e, 3, 3));
+    double pres = -1 * (s11 + s22 + s33) / 3.0;
+    double deptmpr410 = -101.58 * (tmpr + 273.0) - 216828.0;
+    double deptmpr660 = 66.55 * (tmpr + 273.0) - 788494.0;
+    double ev;
+    if (zcord < deptmpr660) {
+        ev = 1e22 * gfm::exp(-0.0115 * (tmpr - p.t_bot));
+        return std::min(p.v_max, std::max(p.v_min, ev));
+    } else if (zcord < deptmpr410) {
+        ev = 1e21 * gfm::exp(-0.0115 * (tmpr - p.t_bot));
+        return std::min(p.v_max, std::max(p.v_min, ev));
+    }
+    double srat = s.L->e2sr[e];
+    if (srat == 0) srat = p.vbc / p.rxbo;
+    ev = 0.0;
+    for (int k = 0; k < p.nphase; ++k) {
+        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        if (ratio < 0.01) continue;
+        double pw = 1.0 / p.pln[k] - 1.0;
+        double pw1 = -1.0 / p.pln[k];
+        double vis = 0.25 * gfm::pow(srat, pw) * gfm::pow(0.75 * p.acoef[k], pw1) *
+                     gfm::exp((p.eactiv[k] + p.vactiv[k] * pres) / (p.pln[k] * r * (tmpr + 273.0))) * 1e6;
+        if (vis < p.v_min) vis = p.v_min;
+        if (vis > p.v_max) vis = p.v_max;
+        ev = ev + ratio / vis;
+    }
+    ev = 1 / ev;
+    double fm = (s.L->fmagma ? s.L->fmagma[e] : 0.0) + (s.L->fmagma2 ? s.L->fmagma2[e] : 0.0);
+    double fma = std::min(fm, p.fmagma_max);
+    if (p.itype_melting == 1) ev = ev * gfm::exp(p.weaken_ratio_viscous * fma / p.fmagma_max);
+    return std::min(p.v_max, std::max(p.v_min, ev));
+}
+
+// --------------------------------------------------------------------------
+// Constitutive updates (src/rh_elastic.f90, rh_maxwell.f90, rh_plastic.f90)
+
+void elastic(double bulkm, double rmu, double &s11, double &s22, double &s33, double &s12, double de11, double de22,
+             double de12) {
+    const double c4d3 = 4.0 / 3.0, c2d3 = 2.0 / 3.0;
+    double a1 = bulkm + c4d3 * rmu;
+    double a2 = bulkm - c2d3 * rmu;
+    s11 = s11 + a1 * de11 + a2 * de22;
+    s22 = s22 + a2 * de11 + a1 * de22;
+    s12 = s12 + 2 * rmu * de12;
+    s33 = s33 + a2 * (de11 + de22);
+}
+
+void maxwell(double bulkm, double rmu0, double viscosity, double &s11, double &s22, double &s33, double &s12, double de11,
+             double de22, double de33, double de12, double dv, int ndim, double dt) {
+    const double c1d3 = 1.0 / 3.0, visc_cut = 1e19;
+    double rmu = viscosity < visc_cut ? rmu0 * viscosity / visc_cut : rmu0;
+    double temp = rmu / (2 * viscosity) * dt;
+    if (temp > 0.5) throw Stop{22};
+    double vic1 = 1 - temp;
+    double vic2 = 1.0 / (1.0 + temp);
+    double dev, de11d, de22d, de33d, s0, s11d, s22d, s33d;
+    if (ndim == 2) {
+        dev = de11 + de22;
+        de11d = de11 - 0.5 * dev;
+        de22d = de22 - 0.5 * dev;
+        de33d = 0;
+        s0 = 0.5 * (s11 + s22);
+        s11d = s11 - s0;
+        s22d = s22 - s0;
+        s33d = 0;
+    } else {
+        dev = de11 + de22 + de33;
+        de11d = de11 - c1d3 * dev;
+        de22d = de22 - c1d3 * dev;
+        de33d = de33 - c1d3 * dev;
+        s0 = c1d3 * (s11 + s22 + s33);
+        s11d = s11 - s0;
+        s22d = s22 - s0;
+        s33d = s33 - s0;
+    }
+    s11d = (s11d * vic1 + 2 * rmu * de11d) * vic2;
+    s22d = (s22d * vic1 + 2 * rmu * de22d) * vic2;
+    s33d = (s33d * vic1 + 2 * rmu * de33d) * vic2;
+    s12 = (s12 * vic1 + 2 * rmu * de12) * vic2;
+    s0 = s0 + bulkm * dv;
+    s11 = s11d + s0;
+    s22 = s22d + s0;
+    s33 = s33d + s0;
+}
+
+void plastic(double bulkm, double rmu, double coh, double phi, double psi, double &depls, double hardn, double &s11,
+             double &s22, double &s33, double &s12, double de11, double de22, double de33, double de12, double ten_off,
+             int ndim) {
+    const double pi = 3.14159265358979323846;
+    const double degrad = pi / 180.0;
+    const double c4d3 = 4.0 / 3.0, c2d3 = 2.0 / 3.0;
+    depls = 0.0;
+    double sphi = gfm::sin(phi * degrad);
+    double spsi = gfm::sin(psi * degrad);
+    double anphi = (1.0 + sphi) / (1.0 - sphi);
+    double anpsi = (1.0 + spsi) / (1.0 - spsi);
+    double amc = 2.0 * coh * std::sqrt(anphi);
+    double e1 = bulkm + c4d3 * rmu;
+    double e2 = bulkm - c2d3 * rmu;
+    double x1 = (e1 - e2 * anpsi + e1 * anphi * anpsi - e2 * anphi);
+    double ten_max = (phi == 0.0) ? ten_off : std::min(ten_off, coh / (gfm::tan(phi * degrad)));
+    double s11i = s11 + (de22 + de33) * e2 + de11 * e1;
+    double s22i = s22 + (de11 + de33) * e2 + de22 * e1;
+    double s12i = s12 + de12 * 2.0 * rmu;
+    double s33i = s33 + (de11 + de22) * e2 + de33 * e1;
+    double sdif = s11i - s22i;
+    double s0 = 0.5 * (s11i + s22i);
+    double rad = 0.5 * std::sqrt(sdif * sdif + 4.0 * s12i * s12i);
+    double si = s0 - rad, sii = s0 + rad, psdif = si - sii;
+    int icase = 1;
+    double s1 = si, s2 = s33i, s3 = sii;
+    if (ndim == 3) {
+        if (s33i > sii) {
+            icase = 3; s1 = si; s2 = sii; s3 = s33i;
+        } else if (s33i < si) {
+            icase = 2; s1 = s33i; s2 = si; s3 = sii;
+        } else {
+            icase = 1; s1 = si; s2 = s33i; s3 = sii;
+        }
+    }
+    if (s1 >= ten_max) {
+        s11 = ten_max; s22 = ten_max; s12 = 0.0; s33 = ten_max;
+        return;
+    }
+    if (s2 >= ten_max && ndim == 3) {
+        s2 = ten_max;
+        s3 = ten_max;
+    }
+    if (s3 >= ten_max) s3 = ten_max;
+    double fs = s1 - s3 * anphi + amc;
+    if (fs < 0.0) {
+        double alams = fs / (x1 + hardn);
+        s1 = s1 - alams * (e1 - e2 * anpsi);
+        s2 = s2 - alams * e2 * (1.0 - anpsi);
+        s3 = s3 - alams * (e2 - e1 * anpsi);
+        double dep1 = alams;
+        double dep3 = -alams * anpsi;
+        depls = 0.5 * std::fabs(dep1 - dep3);
+    } else {
+        s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;
+        return;
+    }
+    if (s1 >= ten_max) {
+        s11 = ten_max; s22 = ten_max; s12 = 0.0; s33 = ten_max;
+        return;
+    }
+    if (s2 >= ten_max && ndim == 3) {
+        s2 = ten_max;
+        s3 = ten_max;
+    } else if (s3 >= ten_max) {
+        s3 = ten_max;
+    }
+    double cs2, si2;
+    if (psdif == 0.0) {
+        cs2 = 1.0;
+        si2 = 0.0;
+    } else {
+        cs2 = sdif / psdif;
+        si2 = 2.0 * s12i / psdif;
+    }
+    double dc2, dss;
+    if (icase == 1) {
+        dc2 = (s1 - s3) * cs2; dss = s1 + s3;
+        s11 = 0.5 * (dss + dc2); s22 = 0.5 * (dss - dc2); s12 = 0.5 * (s1 - s3) * si2; s33 = s2;
+    } else if (icase == 2) {
+        dc2 = (s2 - s3) * cs2; dss = s2 + s3;
+        s11 = 0.5 * (dss + dc2); s22 = 0.5 * (dss - dc2); s12 = 0.5 * (s2 - s3) * si2; s33 = s1;
+    } else {
+        dc2 = (s1 - s2) * cs2; dss = s1 + s2;
+        s11 = 0.5 * (dss + dc2); s22 = 0.5 * (dss - dc2); s12 = 0.5 * (s1 - s2) * si2; s33 = s3;
+    }
+}
+
+// pre_plast (rh_plastic.f90:339-399)
+void pre_plast(St &s, long long e, double &coh, double &phi, double &psi, double &hardn) {
+    const gf_params &p = *s.p;
+    double pls_curr = s.L->aps[e];
+    phi = 0; coh = 0; psi = 0; hardn = 0;
+    for (int k = 0; k < p.nphase; ++k) {
+        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        if (ratio < 0.01) continue;
+        double f, c, d, h;
+        if (pls_curr < p.plstrain1[k]) {
+            f = p.fric1[k]; c = p.cohesion1[k]; d = p.dilat1[k]; h = 0;
+        } else if (pls_curr < p.plstrain2[k]) {
+            double dpl = (pls_curr - p.plstrain1[k]) / (p.plstrain2[k] - p.plstrain1[k]);
+            f = p.fric1[k] + (p.fric2[k] - p.fric1[k]) * dpl;
+            d = p.dilat1[k] + (p.dilat2[k] - p.dilat1[k]) * dpl;
+            c = p.cohesion1[k] + (p.cohesion2[k] - p.cohesion1[k]) * dpl;
+            h = (p.cohesion2[k] - p.cohesion1[k]) / (p.plstrain2[k] - p.plstrain1[k]);
+        } else {
+            f = p.fric2[k]; c = p.cohesion2[k]; d = p.dilat2[k]; h = 0;
+        }
+        phi = phi + ratio / f;
+        coh = coh + ratio / c;
+        psi = psi + ratio * d;
+        hardn = hardn + ratio * h;
+    }
+    phi = 1 / phi;
+    coh = 1 / coh;
+    if (p.itype_melting == 1) {
+        double fm = (s.L->fmagma ? s.L->fmagma[e] : 0.0) + (s.L->fmagma2 ? s.L->fmagma2[e] : 0.0);
+        double fma = std::min(fm, p.fmagma_max);
+        phi = phi * (1 - (1 - p.weaken_ratio_plastic) * fma / p.fmagma_max);
+        coh = coh * (1 - (1 - p.weaken_ratio_plastic) * fma / p.fmagma_max);
+    }
+}
+
+// --------------------------------------------------------------------------
+// fl_rheol (src/fl_rheol.f90:4-424)
+
+void fl_rheol_elem(St &s, int j, int i, double dt) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    long long e = s.e(j, i);
+    double vx1 = s.vel(j, i, 0), vy1 = s.vel(j, i, 1);
+    double vx2 = s.vel(j + 1, i, 0), vy2 = s.vel(j + 1, i, 1);
+    double vx3 = s.vel(j, i + 1, 0), vy3 = s.vel(j, i + 1, 1);
+    double vx4 = s.vel(j + 1, i + 1, 0), vy4 = s.vel(j + 1, i + 1, 1);
+    double x1 = s.cord(j, i, 0), y1 = s.cord(j, i, 1);
+    double x2 = s.cord(j + 1, i, 0), y2 = s.cord(j + 1, i, 1);
+    double x3 = s.cord(j, i + 1, 0), y3 = s.cord(j, i + 1, 1);
+    double x4 = s.cord(j + 1, i + 1, 0), y4 = s.cord(j + 1, i + 1, 1);
+    double ar1 = s.area(e, 0), ar2 = s.area(e, 1), ar3 = s.area(e, 2), ar4 = s.area(e, 3);
+    double dx[3][4], dz[3][4], sr[3][4];
+    dx[0][0] = (y2 - y3) * ar1; dx[1][0] = (y3 - y1) * ar1; dx[2][0] = (y1 - y2) * ar1;
+    dz[0][0] = (x3 - x2) * ar1; dz[1][0] = (x1 - x3) * ar1; dz[2][0] = (x2 - x1) * ar1;
+    dx[0][1] = (y2 - y4) * ar2; dx[1][1] = (y4 - y3) * ar2; dx[2][1] = (y3 - y2) * ar2;
+    dz[0][1] = (x4 - x2) * ar2; dz[1][1] = (x3 - x4) * ar2; dz[2][1] = (x2 - x3) * ar2;
+    dx[0][2] = (y2 - y4) * ar3; dx[1][2] = (y4 - y1) * ar3; dx[2][2] = (y1 - y2) * ar3;
+    dz[0][2] = (x4 - x2) * ar3; dz[1][2] = (x1 - x4) * ar3; dz[2][2] = (x2 - x1) * ar3;
+    dx[0][3] = (y4 - y3) * ar4; dx[1][3] = (y3 - y1) * ar4; dx[2][3] = (y1 - y4) * ar4;
+    dz[0][3] = (x3 - x4) * ar4; dz[1][3] = (x1 - x3) * ar4; dz[2][3] = (x4 - x1) * ar4;
+    // node triplets of the triangles A,B,C,D: (1,2,3), (3,2,4), (1,2,4), (1,4,3)
+    const double vxa[4][3] = {{vx1, vx2, vx3}, {vx3, vx2, vx4}, {vx1, vx2, vx4}, {vx1, vx4, vx3}};
+    const double vya[4][3] = {{vy1, vy2, vy3}, {vy3, vy2, vy4}, {vy1, vy2, vy4}, {vy1, vy4, vy3}};
+    for (int k = 0; k < 4; ++k) {
+        sr[0][k] = vxa[k][0] * dx[0][k] + vxa[k][1] * dx[1][k] + vxa[k][2] * dx[2][k];
+        sr[1][k] = vya[k][0] * dz[0][k] + vya[k][1] * dz[1][k] + vya[k][2] * dz[2][k];
+        sr[2][k] = 0.5 * (vxa[k][0] * dz[0][k] + vxa[k][1] * dz[1][k] + vxa[k][2] * dz[2][k] + vya[k][0] * dx[0][k] +
+                          vya[k][1] * dx[1][k] + vya[k][2] * dx[2][k]);
+    }
+    if (p.mix_strain == 1) {
+        for (int k = 0; k < 4; k += 2) {
+            double em = 0.5 * (sr[0][k] + sr[1][k] + sr[0][k + 1] + sr[1][k + 1]);
+            double eda = sr[0][k] - sr[1][k];
+            double edb = sr[0][k + 1] - sr[1][k + 1];
+            sr[0][k] = 0.5 * (em + eda);
+            sr[1][k] = 0.5 * (em - eda);
+            sr[0][k + 1] = 0.5 * (em + edb);
+            sr[1][k + 1] = 0.5 * (em - edb);
+        }
+    }
+    double s11 = 0.25 * (sr[0][0] + sr[0][1] + sr[0][2] + sr[0][3]);
+    double s22 = 0.25 * (sr[1][0] + sr[1][1] + sr[1][2] + sr[1][3]);
+    double s12 = 0.25 * (sr[2][0] + sr[2][1] + sr[2][2] + sr[2][3]);
+    double srII = 0.5 * std::sqrt((s11 - s22) * (s11 - s22) + 4.0 * s12 * s12);
+    double srI = 0.5 * (s11 + s22);
+    double srs2 = (s11 - srI) * (s11 - srI) + (s22 - srI) * (s22 - srI) + 2.0 * s12 * s12;
+    L.se2sr[gf_ek(s.d, e, 0)] = L.se2sr[gf_ek(s.d, e, 0)] + s11 * dt;
+    L.se2sr[gf_ek(s.d, e, 1)] = L.se2sr[gf_ek(s.d, e, 1)] + s22 * dt;
+    L.se2sr[gf_ek(s.d, e, 2)] = L.se2sr[gf_ek(s.d, e, 2)] + s12 * dt;
+    s11 = 0.25 * (s.st(e, 0, 0) + s.st(e, 0, 1) + s.st(e, 0, 2) + s.st(e, 0, 3));
+    s22 = 0.25 * (s.st(e, 1, 0) + s.st(e, 1, 1) + s.st(e, 1, 2) + s.st(e, 1, 3));
+    s12 = 0.25 * (s.st(e, 2, 0) + s.st(e, 2, 1) + s.st(e, 2, 2) + s.st(e, 2, 3));
+    double stII = 0.5 * std::sqrt((s11 - s22) * (s11 - s22) + 4.0 * s12 * s12);
+    if (srII != 0.0) L.sshrheat[e] = L.sshrheat[e] + stII / srII * srs2 * dt;
+
+    int iph = L.iphase[e] - 1;
+    int irh = p.irheol[iph];
+    double bulkm = p.rl[iph] + 2.0 * p.rm[iph] / 3.0;
+    double rmu = p.rm[iph];
+    double stherm = 0.0;
+    if (p.istress_therm > 0) stherm = -p.alfa[iph] * bulkm * (L.temp[gf_node(s.d, j, i)] - L.temp0[gf_node(s.d, j, i)]);
+    double coh = 0, phi = 0, psi = 0, hardn = 0;
+    if (irh == 6 || irh >= 11) pre_plast(s, e, coh, phi, psi, hardn);
+    if (irh == 3 || irh >= 11) {
+        if (s.c->nloop % p.ifreq_visc == 0) L.visn[e] = eff_visc(s, j, i);
+    }
+    double vis = L.visn[e];
+    double s11s[4], s22s[4], s12s[4], s33s[4];
+    for (int k = 0; k < 4; ++k) {
+        s11s[k] = s.st(e, 0, k); s22s[k] = s.st(e, 1, k); s12s[k] = s.st(e, 2, k); s33s[k] = s.st(e, 3, k);
+    }
+    double s11p[4], s22p[4], s12p[4], s33p[4], s11v[4], s22v[4], s12v[4], s33v[4], depl[4] = {0, 0, 0, 0};
+    double dike = L.dike_released ? L.dike_released[e] : 0.0;
+    for (int k = 0; k < 4; ++k) {
+        double de11 = sr[0][k] * dt, de22 = sr[1][k] * dt, de12 = sr[2][k] * dt, de33 = 0.0;
+        double dv = L.dvol[gf_ek(s.d, e, k)] - dike;
+        s11p[k] = s.st(e, 0, k) + stherm;
+        s22p[k] = s.st(e, 1, k) + stherm;
+        s12p[k] = s.st(e, 2, k);
+        s33p[k] = s.st(e, 3, k) + stherm;
+        s11v[k] = s11p[k]; s22v[k] = s22p[k]; s12v[k] = s12p[k]; s33v[k] = s33p[k];
+        if (irh == 1) {
+            elastic(bulkm, rmu, s11p[k], s22p[k], s33p[k], s12p[k], de11, de22, de12);
+            s.st(e, 0, k) = s11p[k]; s.st(e, 1, k) = s22p[k]; s.st(e, 2, k) = s12p[k]; s.st(e, 3, k) = s33p[k];
+        } else if (irh == 3) {
+            maxwell(bulkm, rmu, vis, s11v[k], s22v[k], s33v[k], s12v[k], de11, de22, de33, de12, dv, p.ndim, dt);
+            s.st(e, 0, k) = s11v[k]; s.st(e, 1, k) = s22v[k]; s.st(e, 2, k) = s12v[k]; s.st(e, 3, k) = s33v[k];
+        } else if (irh == 6) {
+            plastic(bulkm, rmu, coh, phi, psi, depl[k], hardn, s11p[k], s22p[k], s33p[k], s12p[k], de11, de22, de33, de12,
+                    p.ten_off, p.ndim);
+            s.st(e, 0, k) = s11p[k]; s.st(e, 1, k) = s22p[k]; s.st(e, 2, k) = s12p[k]; s.st(e, 3, k) = s33p[k];
+        } else if (irh >= 11) {
+            plastic(bulkm, rmu, coh, phi, psi, depl[k], hardn, s11p[k], s22p[k], s33p[k], s12p[k], de11, de22, de33, de12,
+                    p.ten_off, p.ndim);
+            maxwell(bulkm, rmu, vis, s11v[k], s22v[k], s33v[k], s12v[k], de11, de22, de33, de12, dv, p.ndim, dt);
+        }
+    }
+    if (irh >= 11) {
+        double a = s11p[0] + s11p[1] + s11p[2] + s11p[3] - s22p[0] - s22p[1] - s22p[2] - s22p[3];
+        double b = s12p[0] + s12p[1] + s12p[2] + s12p[3];
+        double sII_plas = a * a + 4.0 * (b * b);
+        a = s11v[0] + s11v[1] + s11v[2] + s11v[3] - s22v[0] - s22v[1] - s22v[2] - s22v[3];
+        b = s12v[0] + s12v[1] + s12v[2] + s12v[3];
+        double sII_visc = a * a + 4.0 * (b * b);
+        if (sII_plas < sII_visc) {
+            for (int k = 0; k < 4; ++k) {
+                s.st(e, 0, k) = s11p[k]; s.st(e, 1, k) = s22p[k]; s.st(e, 2, k) = s12p[k]; s.st(e, 3, k) = s33p[k];
+            }
+        } else {
+            for (int k = 0; k < 4; ++k) {
+                s.st(e, 0, k) = s11v[k]; s.st(e, 1, k) = s22v[k]; s.st(e, 2, k) = s12v[k]; s.st(e, 3, k) = s33v[k];
+            }
+        }
+    }
+    if (p.mix_stress == 1) {
+        for (int h = 0; h < 4; h += 2) {
+            double ra = s.area(e, h), rb = s.area(e, h + 1);
+            double quad_area = 1.0 / ra + 1.0 / rb;
+            double s0a = 0.5 * (s.st(e, 0, h) + s.st(e, 1, h));
+            double s0b = 0.5 * (s.st(e, 0, h + 1) + s.st(e, 1, h + 1));
+            double s0 = (s0a / rb + s0b / ra) / quad_area;
+            s.st(e, 0, h) = s.st(e, 0, h) - s0a + s0;
+            s.st(e, 1, h) = s.st(e, 1, h) - s0a + s0;
+            s.st(e, 0, h + 1) = s.st(e, 0, h + 1) - s0b + s0;
+            s.st(e, 1, h + 1) = s.st(e, 1, h + 1) - s0b + s0;
+        }
+    }
+    for (int k = 0; k < 4; ++k) {
+        s.st(e, 0, k) = s.st(e, 0, k) - stherm;
+        s.st(e, 1, k) = s.st(e, 1, k) - stherm;
+        s.st(e, 3, k) = s.st(e, 3, k) - stherm;
+    }
+    if (irh == 6 || irh >= 11) {
+        double quad_area = ar1 + ar2 + ar3 + ar4;
+        L.aps[e] = L.aps[e] + (depl[0] * ar1 + depl[1] * ar2 + depl[2] * ar3 + depl[3] * ar4) / quad_area;
+        if (L.aps[e] < 0.0) L.aps[e] = 0.0;
+        if (p.tau_heal != 0.0) L.aps[e] = L.aps[e] / (1.0 + dt / p.tau_heal);
+    }
+    // the reference accumulates the element-averaged *stress* here
+    // (s11/s22/s12 were reassigned at fl_rheol.f90:181-183)
+    L.strain[gf_ek(s.d, e, 0)] = L.strain[gf_ek(s.d, e, 0)] + s11 * dt;
+    L.strain[gf_ek(s.d, e, 1)] = L.strain[gf_ek(s.d, e, 1)] + s22 * dt;
+    L.strain[gf_ek(s.d, e, 2)] = L.strain[gf_ek(s.d, e, 2)] + s12 * dt;
+    if (p.ishearh == 1) {
+        double q = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            double f11 = s.st(e, 0, k), f22 = s.st(e, 1, k), f12 = s.st(e, 2, k), f33 = s.st(e, 3, k);
+            double lambda = bulkm - 2.0 / 3.0 * rmu, mu = rmu;
+            double den_el = 3.0 * lambda + 2.0 * mu;
+            if (std::fabs(den_el) < 1e-30) den_el = std::copysign(1e-30, den_el);
+            double tr0 = s11s[k] + s22s[k] + s33s[k];
+            double e11a = (s11s[k] - (lambda / den_el) * tr0) / (2.0 * mu);
+            double e22a = (s22s[k] - (lambda / den_el) * tr0) / (2.0 * mu);
+            double e33a = (s33s[k] - (lambda / den_el) * tr0) / (2.0 * mu);
+            double e12a = s12s[k] / (2.0 * mu);
+            double tr1 = f11 + f22 + f33;
+            double e11b = (f11 - (lambda / den_el) * tr1) / (2.0 * mu);
+            double e22b = (f22 - (lambda / den_el) * tr1) / (2.0 * mu);
+            double e33b = (f33 - (lambda / den_el) * tr1) / (2.0 * mu);
+            double e12b = f12 / (2.0 * mu);
+            double d11 = sr[0][k] * dt - (e11b - e11a);
+            double d22 = sr[1][k] * dt - (e22b - e22a);
+            double d12 = sr[2][k] * dt - (e12b - e12a);
+            double d33 = 0.0 - (e33b - e33a);
+            double a11 = 0.5 * (s11s[k] + f11), a22 = 0.5 * (s22s[k] + f22), a12 = 0.5 * (s12s[k] + f12),
+                   a33 = 0.5 * (s33s[k] + f33);
+            double qk = a11 * d11 + a22 * d22 + 2.0 * a12 * d12 + a33 * d33;
+            q = q + 0.25 * qk;
+        }
+        L.sshrheat[e] = L.sshrheat[e] + q;
+    }
+}
+
+void fl_rheol(St &s) {
+    const gf_params &p = *s.p;
+    gf_clock &c = *s.c;
+    c.dtavg = c.dtavg + c.dt;
+    int nx = p.nx, nz = p.nz;
+    int err = 0;
+#pragma omp parallel for schedule(guided) num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            try {
+                fl_rheol_elem(s, j, i, c.dt);
+            } catch (const Stop &st) {
+#pragma omp critical
+                if (!err) err = st.code;
+            }
+        }
+    if (err) throw Stop{err};
+    gf_layout &L = *s.L;
+    if (c.nsrate == p.ifreq_avgsr || c.nsrate == -1) {
+        bool reset = c.nsrate == p.ifreq_avgsr;
+        for (long long e = 0; e < s.d.E; ++e) {
+            double a = L.se2sr[gf_ek(s.d, e, 0)], b = L.se2sr[gf_ek(s.d, e, 1)], q = L.se2sr[gf_ek(s.d, e, 2)];
+            L.e2sr[e] = (0.5 * std::sqrt((a - b) * (a - b) + 4.0 * q * q)) / c.dtavg;
+            L.shrheat[e] = L.sshrheat[e] / c.dtavg;
+            if (reset) {
+                L.se2sr[gf_ek(s.d, e, 0)] = 0.0;
+                L.se2sr[gf_ek(s.d, e, 1)] = 0.0;
+                L.se2sr[gf_ek(s.d, e, 2)] = 0.0;
+                L.sshrheat[e] = 0.0;
+            }
+        }
+        if (reset) {
+            c.dtavg = 0.0;
+            c.nsrate = 0;
+        }
+    }
+    c.nsrate = c.nsrate + 1;
+}
+
+// --------------------------------------------------------------------------
+// fl_node (src/fl_node.f90:3-393)
+
+void fl_node(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const gf_clock &c = *s.c;
+    int nx = p.nx, nz = p.nz;
+    if (p.nystressbc != 0) throw Stop{GF_ERR_UNSUPPORTED};
+    static const int kk[4][3] = {{2, 3, 4}, {1, 2, 3}, {1, 2, 4}, {1, 3, 4}};
+    static const int mm[4][3] = {{3, 3, 2}, {2, 2, 2}, {3, 1, 3}, {1, 1, 1}};
+    double drat = c.dt / c.dt_elastic;
+    if (drat < 1.0) drat = 1.0;
+    std::vector<double> force(2 * (size_t)s.d.N, 0.0);
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+            double fx0 = 0.0, fy0 = 0.0;
+            // elements (j-1,i-1), (j-1,i), (j,i-1), (j,i) in that order
+            const int dj[4] = {-1, -1, 0, 0}, di[4] = {-1, 0, -1, 0};
+            for (int q = 0; q < 4; ++q) {
+                int je = j + dj[q], ie = i + di[q];
+                if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
+                long long e = s.e(je, ie);
+                double x1 = s.cord(je, ie, 0), y1 = s.cord(je, ie, 1);
+                double x2 = s.cord(je + 1, ie, 0), y2 = s.cord(je + 1, ie, 1);
+                double x3 = s.cord(je, ie + 1, 0), y3 = s.cord(je, ie + 1, 1);
+                double x4 = s.cord(je + 1, ie + 1, 0), y4 = s.cord(je + 1, ie + 1, 1);
+                double ar[4] = {s.area(e, 0), s.area(e, 1), s.area(e, 2), s.area(e, 3)};
+                double dx[3][4], dz[3][4];
+                dx[0][0] = (y2 - y3) * ar[0]; dx[1][0] = (y3 - y1) * ar[0]; dx[2][0] = (y1 - y2) * ar[0];
+                dz[0][0] = (x3 - x2) * ar[0]; dz[1][0] = (x1 - x3) * ar[0]; dz[2][0] = (x2 - x1) * ar[0];
+                dx[0][1] = (y2 - y4) * ar[1]; dx[1][1] = (y4 - y3) * ar[1]; dx[2][1] = (y3 - y2) * ar[1];
+                dz[0][1] = (x4 - x2) * ar[1]; dz[1][1] = (x3 - x4) * ar[1]; dz[2][1] = (x2 - x3) * ar[1];
+                dx[0][2] = (y2 - y4) * ar[2]; dx[1][2] = (y4 - y1) * ar[2]; dx[2][2] = (y1 - y2) * ar[2];
+                dz[0][2] = (x4 - x2) * ar[2]; dz[1][2] = (x1 - x4) * ar[2]; dz[2][2] = (x2 - x1) * ar[2];
+                dx[0][3] = (y4 - y3) * ar[3]; dx[1][3] = (y3 - y1) * ar[3]; dx[2][3] = (y1 - y4) * ar[3];
+                dz[0][3] = (x3 - x4) * ar[3]; dz[1][3] = (x1 - x3) * ar[3]; dz[2][3] = (x4 - x1) * ar[3];
+                for (int k = 0; k < 3; ++k) {
+                    int t = kk[q][k] - 1, m = mm[q][k] - 1;
+                    double factor = 0.25 / ar[t];
+                    double fx = factor * (L.stress0[gf_s(s.d, e, 0, t)] * dx[m][t] + L.stress0[gf_s(s.d, e, 2, t)] * dz[m][t]);
+                    double fy = factor * (L.stress0[gf_s(s.d, e, 2, t)] * dx[m][t] + L.stress0[gf_s(s.d, e, 1, t)] * dz[m][t]);
+                    fx0 = fx0 - fx;
+                    fy0 = fy0 - fy;
+                }
+            }
+            fy0 = fy0 - L.rmass[gf_node(s.d, j, i)] * p.g;
+            force[gf_n2(s.d, j, i, 0)] = fx0;
+            force[gf_n2(s.d, j, i, 1)] = fy0;
+        }
+    if (p.nyhydro > 0) {
+        for (int i = 0; i < nx; ++i) {
+            double rho_water_g = 1030.0 * p.g;
+            double water_depth = (i < nx - 1) ? 0.5 * (s.cord(0, i + 1, 1) + s.cord(0, i, 1))
+                                              : 0.5 * (s.cord(0, i - 1, 1) + s.cord(0, i, 1));
+            if (water_depth < 0.0) {
+                double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
+                if (i > 0) {
+                    pl = rho_water_g * ((s.cord(0, i - 1, 1) + s.cord(0, i, 1)) / 2.0);
+                    dlxl = s.cord(0, i, 0) - s.cord(0, i - 1, 0);
+                    dlyl = s.cord(0, i, 1) - s.cord(0, i - 1, 1);
+                }
+                if (i < nx - 1) {
+                    pr = rho_water_g * ((s.cord(0, i + 1, 1) + s.cord(0, i, 1)) / 2.0);
+                    dlxr = s.cord(0, i + 1, 0) - s.cord(0, i, 0);
+                    dlyr = s.cord(0, i + 1, 1) - s.cord(0, i, 1);
+                }
+                double &f0 = force[gf_n2(s.d, 0, i, 0)];
+                double &f1 = force[gf_n2(s.d, 0, i, 1)];
+                f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
+                f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
+            }
+        }
+        int ips = p.iphsub - 1;
+        for (int i = 0; i < nx; ++i) {
+            double p_est = p.pisos + 0.5 * (p.den[ips] + p.drosub) * p.g * (s.cord(nz - 1, i, 1) - p.rzbo);
+            double rosubg = p.g * (p.den[ips] + p.drosub) *
+                            (1 - p.alfa[ips] * L.temp[gf_node(s.d, nz - 1, i)] + p.beta[ips] * p_est);
+            double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
+            if (i > 0) {
+                pl = p.pisos - rosubg * ((s.cord(nz - 1, i - 1, 1) + s.cord(nz - 1, i, 1)) / 2.0 - p.rzbo);
+                dlxl = s.cord(nz - 1, i, 0) - s.cord(nz - 1, i - 1, 0);
+                dlyl = s.cord(nz - 1, i, 1) - s.cord(nz - 1, i - 1, 1);
+            }
+            if (i < nx - 1) {
+                pr = p.pisos - rosubg * ((s.cord(nz - 1, i + 1, 1) + s.cord(nz - 1, i, 1)) / 2.0 - p.rzbo);
+                dlxr = s.cord(nz - 1, i + 1, 0) - s.cord(nz - 1, i, 0);
+                dlyr = s.cord(nz - 1, i + 1, 1) - s.cord(nz - 1, i, 1);
+            }
+            double &f0 = force[gf_n2(s.d, nz - 1, i, 0)];
+            double &f1 = force[gf_n2(s.d, nz - 1, i, 1)];
+            f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
+            f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
+        }
+    }
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+            long long n0 = gf_n2(s.d, j, i, 0), n1 = gf_n2(s.d, j, i, 1);
+            double f0 = force[n0], f1 = force[n1];
+            int c0 = L.ncod[n0], c1 = L.ncod[n1];
+            if ((c0 & 1) != 1 && std::fabs(L.vel[n0]) > 1.0e-13) f0 = f0 - p.demf * std::copysign(std::fabs(f0), L.vel[n0]);
+            if ((c1 & 2) != 2 && std::fabs(L.vel[n1]) > 1.0e-13) f1 = f1 - p.demf * std::copysign(std::fabs(f1), L.vel[n1]);
+            double am = L.amass[gf_node(s.d, j, i)];
+            if (c0 == 1)
+                L.vel[n0] = L.bc[n0];
+            else
+                L.vel[n0] = L.vel[n0] + c.dt * f0 / (am * drat * drat);
+            if (c1 == 1)
+                L.vel[n1] = L.bc[n1];
+            else
+                L.vel[n1] = L.vel[n1] + c.dt * f1 / (am * drat * drat);
+        }
+    if (p.i_prestress == 1 && c.time < 600e3 * GF_SEC_YEAR) {
+        for (int k = 0; k < 2; ++k)
+            for (int i = 0; i < nx; ++i) L.vel[gf_n2(s.d, nz - 1, i, k)] = 0.0;
+        for (int k = 0; k < 2; ++k)
+            for (int j = 0; j < nz; ++j) {
+                L.vel[gf_n2(s.d, j, 0, k)] = 0.0;
+                L.vel[gf_n2(s.d, j, nx - 1, k)] = 0.0;
+            }
+    }
+}
+
+// --------------------------------------------------------------------------
+// fl_move (src/fl_move.f90:3-132)
+
+void fl_move(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    double dt = s.c->dt;
+    if (p.movegrid == 0) return;
+    int nx = p.nx, nz = p.nz;
+    for (long long n = 0; n < s.d.N; ++n) {
+        L.cord[n] = L.cord[n] + L.vel[n] * dt;
+        L.cord[s.d.N + n] = L.cord[s.d.N + n] + L.vel[s.d.N + n] * dt;
+    }
+    if (p.topo_kappa > 0.0) throw Stop{GF_ERR_UNSUPPORTED};
+    static const int nd1[4] = {1, 3, 1, 1}, nd2[4] = {2, 2, 2, 4}, nd3[4] = {3, 4, 4, 3};
+    int err = 0;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            double xc[4] = {s.cord(j, i, 0), s.cord(j + 1, i, 0), s.cord(j, i + 1, 0), s.cord(j + 1, i + 1, 0)};
+            double yc[4] = {s.cord(j, i, 1), s.cord(j + 1, i, 1), s.cord(j, i + 1, 1), s.cord(j + 1, i + 1, 1)};
+            double xv[4] = {s.vel(j, i, 0), s.vel(j + 1, i, 0), s.vel(j, i + 1, 0), s.vel(j + 1, i + 1, 0)};
+            double yv[4] = {s.vel(j, i, 1), s.vel(j + 1, i, 1), s.vel(j, i + 1, 1), s.vel(j + 1, i + 1, 1)};
+            bool neg = false;
+            for (int k = 0; k < 4; ++k) {
+                int a = nd1[k] - 1, b = nd2[k] - 1, cc = nd3[k] - 1;
+                double det = ((xc[b] * yc[cc] - yc[b] * xc[cc]) - (xc[a] * yc[cc] - yc[a] * xc[cc])) + (xc[a] * yc[b] - yc[a] * xc[b]);
+                L.dvol[gf_ek(s.d, e, k)] = det * L.area[gf_ek(s.d, e, k)] - 1.0;
+                L.area[gf_ek(s.d, e, k)] = 1.0 / det;
+                double dw12 = 0.5 * (xv[a] * (xc[cc] - xc[b]) + xv[b] * (xc[a] - xc[cc]) + xv[cc] * (xc[b] - xc[a]) +
+                                     yv[a] * (yc[cc] - yc[b]) + yv[b] * (yc[a] - yc[cc]) + yv[cc] * (yc[b] - yc[a])) /
+                              det * dt;
+                double s11 = s.st(e, 0, k), s22 = s.st(e, 1, k), s12 = s.st(e, 2, k);
+                s.st(e, 0, k) = s11 + s12 * 2 * dw12;
+                s.st(e, 1, k) = s22 - s12 * 2 * dw12;
+                s.st(e, 2, k) = s12 + dw12 * (s22 - s11);
+                if (k == 0) {
+                    double e11 = L.strain[gf_ek(s.d, e, 0)], e22 = L.strain[gf_ek(s.d, e, 1)], e12 = L.strain[gf_ek(s.d, e, 2)];
+                    L.strain[gf_ek(s.d, e, 0)] = e11 + e12 * 2 * dw12;
+                    L.strain[gf_ek(s.d, e, 1)] = e22 - e12 * 2 * dw12;
+                    L.strain[gf_ek(s.d, e, 2)] = e12 + dw12 * (e22 - e11);
+                }
+            }
+            for (int k = 0; k < 4; ++k)
+                if (L.area[gf_ek(s.d, e, k)] <= 0) neg = true;
+            if (neg) {
+#pragma omp critical
+                err = 40;
+            }
+        }
+    if (err) throw Stop{40};
+}
+
+// --------------------------------------------------------------------------
+// rmasses (src/rmasses.f90:236-295) and dt_mass (src/dt_mass.f90:16-232)
+
+void rmasses(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const double c1d12 = 1.0 / 12.0;
+    int nx = p.nx, nz = p.nz;
+    for (long long n = 0; n < s.d.N; ++n) L.rmass[n] = 0;
+    // serial order of frac writes: colour by colour, i then j
+    for (int ib = 0; ib < 2; ++ib)
+        for (int jb = 0; jb < 2; ++jb) {
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+            for (int i = ib; i < nx - 1; i += 2)
+                for (int j = jb; j < nz - 1; j += 2) {
+                    double dens = eff_dens(s, j, i, &s.c->frac);
+                    long long e = s.e(j, i);
+                    double a0 = s.area(e, 0), a1 = s.area(e, 1), a2 = s.area(e, 2), a3 = s.area(e, 3);
+                    double *rm = L.rmass;
+                    long long n11 = gf_node(s.d, j, i), n21 = gf_node(s.d, j + 1, i), n12 = gf_node(s.d, j, i + 1),
+                              n22 = gf_node(s.d, j + 1, i + 1);
+                    rm[n11] = rm[n11] + c1d12 / a0 * dens;
+                    rm[n21] = rm[n21] + c1d12 / a0 * dens;
+                    rm[n12] = rm[n12] + c1d12 / a0 * dens;
+                    rm[n22] = rm[n22] + c1d12 / a1 * dens;
+                    rm[n21] = rm[n21] + c1d12 / a1 * dens;
+                    rm[n12] = rm[n12] + c1d12 / a1 * dens;
+                    rm[n11] = rm[n11] + c1d12 / a2 * dens;
+                    rm[n21] = rm[n21] + c1d12 / a2 * dens;
+                    rm[n22] = rm[n22] + c1d12 / a2 * dens;
+                    rm[n11] = rm[n11] + c1d12 / a3 * dens;
+                    rm[n22] = rm[n22] + c1d12 / a3 * dens;
+                    rm[n12] = rm[n12] + c1d12 / a3 * dens;
+                }
+        }
+}
+
+double dlmin_prop(St &s) {
+    int nx = s.p->nx, nz = s.p->nz;
+    double dlmin = 1e28;
+#pragma omp parallel for reduction(min : dlmin) num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            auto len = [&](int ja, int ia, int jb, int ib) {
+                double ddx = s.cord(ja, ia, 0) - s.cord(jb, ib, 0), ddy = s.cord(ja, ia, 1) - s.cord(jb, ib, 1);
+                return std::sqrt(ddx * ddx + ddy * ddy);
+            };
+            double dl;
+            dl = len(j + 1, i, j, i);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 0) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 2) * dl));
+            dl = len(j + 1, i + 1, j + 1, i);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 1) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 2) * dl));
+            dl = len(j + 1, i + 1, j, i + 1);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 1) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 3) * dl));
+            dl = len(j, i + 1, j, i);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 0) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 3) * dl));
+            dl = len(j + 1, i + 1, j, i);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 2) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 3) * dl));
+            dl = len(j + 1, i, j, i + 1);
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 0) * dl));
+            dlmin = std::min(dlmin, 1.0 / (s.area(e, 1) * dl));
+        }
+    return dlmin;
+}
+
+void dt_mass(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    gf_clock &c = *s.c;
+    const double c1d12 = 1.0 / 12.0;
+    int nx = p.nx, nz = p.nz;
+    double dlmin = dlmin_prop(s);
+    c.dlmin = dlmin;
+    if (p.idt_scale == 1)
+        c.dt_elastic = p.dt_scale;
+    else if (p.idt_scale == 2) {
+        if (p.vbc == 0)
+            c.dt_elastic = dlmin * c.frac * p.strain_inert / (1.0 / GF_SEC_YEAR / 100);
+        else
+            c.dt_elastic = dlmin * c.frac * p.strain_inert / p.vbc;
+    }
+    double dtmax_therm = 1e28, dt_maxwell = 1e28, dt_elastic = c.dt_elastic;
+    double vel_max = 0.0;
+    for (long long n = 0; n < 2 * s.d.N; ++n) vel_max = std::max(vel_max, std::fabs(L.vel[n]));
+    c.vel_max = vel_max;
+    for (long long n = 0; n < s.d.N; ++n) L.amass[n] = (p.idt_scale == 0) ? L.rmass[n] : 0.0;
+    for (int ib = 0; ib < 2; ++ib)
+        for (int jb = 0; jb < 2; ++jb) {
+            double dte_min = dt_elastic, dtt_min = dtmax_therm, dtm_min = dt_maxwell;
+#pragma omp parallel for reduction(min : dte_min, dtt_min, dtm_min) num_threads(g_threads) if (g_threads > 1)
+            for (int i = ib; i < nx - 1; i += 2)
+                for (int j = jb; j < nz - 1; j += 2) {
+                    long long e = s.e(j, i);
+                    int iph = L.iphase[e] - 1;
+                    double pwave = p.rl[iph] + 0.6666 * p.rm[iph];
+                    double dens = p.den[iph];
+                    double vel_sound = dlmin * c.frac / dt_elastic;
+                    double rho_inert = pwave / (vel_sound * vel_sound);
+                    if (p.i_rey == 1 && vel_max > 0.0) {
+                        double rho_inert2 = (p.xReyn * p.v_min) / (vel_max * std::fabs(p.rzbo));
+                        if (rho_inert > rho_inert2) rho_inert = rho_inert2;
+                    }
+                    if (p.idt_scale > 0) {
+                        double *am = L.amass;
+                        long long n11 = gf_node(s.d, j, i), n21 = gf_node(s.d, j + 1, i), n12 = gf_node(s.d, j, i + 1),
+                                  n22 = gf_node(s.d, j + 1, i + 1);
+                        double am3 = c1d12 * rho_inert / s.area(e, 0);
+                        am[n11] = am[n11] + am3; am[n21] = am[n21] + am3; am[n12] = am[n12] + am3;
+                        am3 = c1d12 * rho_inert / s.area(e, 1);
+                        am[n21] = am[n21] + am3; am[n22] = am[n22] + am3; am[n12] = am[n12] + am3;
+                        am3 = c1d12 * rho_inert / s.area(e, 2);
+                        am[n11] = am[n11] + am3; am[n21] = am[n21] + am3; am[n22] = am[n22] + am3;
+                        am3 = c1d12 * rho_inert / s.area(e, 3);
+                        am[n11] = am[n11] + am3; am[n22] = am[n22] + am3; am[n12] = am[n12] + am3;
+                    } else {
+                        double dte = c.frac * dlmin * std::sqrt(dens / pwave);
+                        dte_min = std::min(dte_min, dte);
+                    }
+                    double diff = p.conduct[iph] / p.den[iph] / p.cp[iph];
+                    double dtt = dlmin * dlmin / diff;
+                    dtt_min = std::min(dtt_min, dtt);
+                    if (p.ivis_present == 1) {
+                        if ((p.irheol[iph] == 3 || p.irheol[iph] == 12) && p.rm[iph] < 1e11) {
+                            double visc_cut = 1e10;
+                            double rmu = (p.v_min < visc_cut) ? p.rm[iph] * p.v_min / visc_cut : p.rm[iph];
+                            double dt_m = p.v_min / rmu * p.fracm;
+                            dtm_min = std::min(dt_m, dtm_min);
+                        }
+                    }
+                }
+            dt_elastic = dte_min;
+            dtmax_therm = dtt_min;
+            dt_maxwell = dtm_min;
+        }
+    c.dt_elastic = dt_elastic;
+    c.dt_maxwell = dt_maxwell;
+    c.dtmax_therm = dtmax_therm;
+    c.dt = std::min(std::min(dt_elastic, dt_maxwell), dtmax_therm);
+}
+
+void init_visc(St &s) {
+    int nx = s.p->nx, nz = s.p->nz;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) s.L->visn[s.e(j, i)] = eff_visc(s, j, i);
+}
+
+// --------------------------------------------------------------------------
+// fl_therm (src/fl_therm.f90:393-598); the magma sub-model (itype_melting=1,
+// fl_therm.f90:56-391) is not part of this path.
+
+void fl_therm(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    double dt = s.c->dt;
+    int nx = p.nx, nz = p.nz;
+    if (p.itype_melting == 1) throw Stop{GF_ERR_UNSUPPORTED};
+    std::memcpy(L.temp0, L.temp, sizeof(double) * (size_t)s.d.N);
+    std::vector<double> diff(s.d.E), src(s.d.E);
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            int iph = L.iphase[e] - 1;
+            double cp_eff = p.cp[iph], cond_eff = p.conduct[iph];
+            double dissip = (p.ishearh == 1 && p.itherm != 2) ? L.shrheat[e] : 0;
+            diff[e] = cond_eff / p.den[iph] / cp_eff;
+            src[e] = (L.source[e] + dissip / p.den[iph]) / cp_eff;
+        }
+    auto C = [&](int j, int i, int k) { return L.cord[gf_n2(s.d, j, i, k)]; };
+    auto T = [&](int j, int i) { return L.temp[gf_node(s.d, j, i)]; };
+    // in place, lexicographic (i outer, j inner): a Gauss-Seidel sweep
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+            double rhs = 0.0, area_n = 0.0;
+            if (j != 0 && i != 0) { // element (j-1,i-1), triangle B
+                long long e = s.e(j - 1, i - 1);
+                double a = s.area(e, 1), inv_area = 1.0 / a, ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                double y2 = C(j, i - 1, 1), y3 = C(j - 1, i, 1), y4 = C(j, i, 1);
+                double x2 = C(j, i - 1, 0), x3 = C(j - 1, i, 0), x4 = C(j, i, 0);
+                double d1 = (y2 - y4) * a, d2 = (y4 - y3) * a, d3 = (y3 - y2) * a;
+                double z1 = (x4 - x2) * a, z2 = (x3 - x4) * a, z3 = (x2 - x3) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j - 1, i) * (d1 * d3 + z1 * z3) + T(j, i - 1) * (d2 * d3 + z2 * z3) + T(j, i) * (d3 * d3 + z3 * z3));
+            }
+            if (j != 0 && i != nx - 1) { // element (j-1,i), triangles A and B
+                long long e = s.e(j - 1, i);
+                double a = s.area(e, 0), inv_area = 1.0 / a, ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                double y1 = C(j - 1, i, 1), y2 = C(j, i, 1), y3 = C(j - 1, i + 1, 1);
+                double x1 = C(j - 1, i, 0), x2 = C(j, i, 0), x3 = C(j - 1, i + 1, 0);
+                double d1 = (y2 - y3) * a, d2 = (y3 - y1) * a, d3 = (y1 - y2) * a;
+                double z1 = (x3 - x2) * a, z2 = (x1 - x3) * a, z3 = (x2 - x1) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j - 1, i) * (d1 * d2 + z1 * z2) + T(j, i) * (d2 * d2 + z2 * z2) + T(j - 1, i + 1) * (d3 * d2 + z3 * z2));
+                a = s.area(e, 1); inv_area = 1.0 / a; ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                y2 = C(j, i, 1); y3 = C(j - 1, i + 1, 1); double y4 = C(j, i + 1, 1);
+                x2 = C(j, i, 0); x3 = C(j - 1, i + 1, 0); double x4 = C(j, i + 1, 0);
+                d1 = (y2 - y4) * a; d2 = (y4 - y3) * a; d3 = (y3 - y2) * a;
+                z1 = (x4 - x2) * a; z2 = (x3 - x4) * a; z3 = (x2 - x3) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j - 1, i + 1) * (d1 * d2 + z1 * z2) + T(j, i) * (d2 * d2 + z2 * z2) + T(j, i + 1) * (d3 * d2 + z3 * z2));
+            }
+            if (j != nz - 1 && i != 0) { // element (j,i-1), triangles A and B
+                long long e = s.e(j, i - 1);
+                double a = s.area(e, 0), inv_area = 1.0 / a, ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                double y1 = C(j, i - 1, 1), y2 = C(j + 1, i - 1, 1), y3 = C(j, i, 1);
+                double x1 = C(j, i - 1, 0), x2 = C(j + 1, i - 1, 0), x3 = C(j, i, 0);
+                double d1 = (y2 - y3) * a, d2 = (y3 - y1) * a, d3 = (y1 - y2) * a;
+                double z1 = (x3 - x2) * a, z2 = (x1 - x3) * a, z3 = (x2 - x1) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j, i - 1) * (d1 * d3 + z1 * z3) + T(j + 1, i - 1) * (d2 * d3 + z2 * z3) + T(j, i) * (d3 * d3 + z3 * z3));
+                a = s.area(e, 1); inv_area = 1.0 / a; ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                y2 = C(j + 1, i - 1, 1); y3 = C(j, i, 1); double y4 = C(j + 1, i, 1);
+                x2 = C(j + 1, i - 1, 0); x3 = C(j, i, 0); double x4 = C(j + 1, i, 0);
+                d1 = (y2 - y4) * a; d2 = (y4 - y3) * a; d3 = (y3 - y2) * a;
+                z1 = (x4 - x2) * a; z2 = (x3 - x4) * a; z3 = (x2 - x3) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j, i) * (d1 * d1 + z1 * z1) + T(j + 1, i - 1) * (d2 * d1 + z2 * z1) + T(j + 1, i) * (d3 * d1 + z3 * z1));
+            }
+            if (j != nz - 1 && i != nx - 1) { // element (j,i), triangle A
+                long long e = s.e(j, i);
+                double a = s.area(e, 0), inv_area = 1.0 / a, ra = inv_area / 6.0;
+                area_n = area_n + ra;
+                double y1 = C(j, i, 1), y2 = C(j + 1, i, 1), y3 = C(j, i + 1, 1);
+                double x1 = C(j, i, 0), x2 = C(j + 1, i, 0), x3 = C(j, i + 1, 0);
+                double d1 = (y2 - y3) * a, d2 = (y3 - y1) * a, d3 = (y1 - y2) * a;
+                double z1 = (x3 - x2) * a, z2 = (x1 - x3) * a, z3 = (x2 - x1) * a;
+                rhs = rhs + src[e] * ra -
+                      0.5 * diff[e] * inv_area *
+                          (T(j, i) * (d1 * d1 + z1 * z1) + T(j + 1, i) * (d2 * d1 + z2 * z1) + T(j, i + 1) * (d3 * d1 + z3 * z1));
+            }
+            L.temp[gf_node(s.d, j, i)] = T(j, i) + rhs * dt / area_n;
+        }
+    for (int i = 0; i < nx; ++i) {
+        L.temp[gf_node(s.d, 0, i)] = p.t_top;
+        if (p.itemp_bc == 1)
+            L.temp[gf_node(s.d, nz - 1, i)] = p.bot_bc;
+        else if (p.itemp_bc == 2) {
+            int ie = std::min(i, nx - 2);
+            double cond_eff = p.conduct[L.iphase[s.e(nz - 2, ie)] - 1];
+            L.temp[gf_node(s.d, nz - 1, i)] = T(nz - 2, i) + p.bot_bc * (C(nz - 2, i, 1) - C(nz - 1, i, 1)) / cond_eff;
+        }
+    }
+    for (int j = 0; j < nz; ++j) {
+        L.temp[gf_node(s.d, j, 0)] = T(j, 1);
+        L.temp[gf_node(s.d, j, nx - 1)] = T(j, nx - 2);
+    }
+}
+
+// --------------------------------------------------------------------------
+// Markers: count_phase_ratio, marker2elem, change_phase
+
+void count_phase_ratio(St &s, int j, int i) {
+    gf_layout &L = *s.L;
+    long long e = s.e(j, i);
+    int nm = L.nmark_elem[e];
+    if (nm == 0) throw Stop{134};
+    int cnt[GF_MAXPH + 1] = {0};
+    for (int n = 0; n < nm; ++n) {
+        int kk = L.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + n];
+        int iph = L.mark_phase[kk - 1];
+        if (iph >= 1 && iph <= GF_MAXPH) cnt[iph] += 1;
+    }
+    for (int k = 1; k <= s.p->nphase; ++k) L.phase_ratio[gf_pr(s.d, e, k - 1)] = cnt[k] / (nm * 1.0);
+    int iph = 1, best = 0;
+    for (int k = 1; k <= s.p->nphase; ++k)
+        if (cnt[k] > best) {
+            best = cnt[k];
+            iph = k;
+        }
+    L.iphase[e] = iph;
+}
+
+int check_inside(St &s, double x, double y, double &bar1, double &bar2, int &ntr, int i, int j) {
+    for (int k = 0; k < 2; ++k) {
+        double x1, x2, x3, y1, y2, y3;
+        if (k == 0) {
+            x1 = s.cord(j, i, 0); x2 = s.cord(j + 1, i, 0); x3 = s.cord(j, i + 1, 0);
+            y1 = s.cord(j, i, 1); y2 = s.cord(j + 1, i, 1); y3 = s.cord(j, i + 1, 1);
+        } else {
+            x1 = s.cord(j, i + 1, 0); x2 = s.cord(j + 1, i, 0); x3 = s.cord(j + 1, i + 1, 0);
+            y1 = s.cord(j, i + 1, 1); y2 = s.cord(j + 1, i, 1); y3 = s.cord(j + 1, i + 1, 1);
+        }
+        double det = ((x2 * y3 - y2 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y2 - y1 * x2);
+        double m11 = (x2 * y3 - y2 * x3) / det, m12 = (y2 - y3) / det, m13 = (x3 - x2) / det;
+        double m21 = (x3 * y1 - y3 * x1) / det, m22 = (y3 - y1) / det, m23 = (x1 - x3) / det;
+        bar1 = m11 + m12 * x + y * m13;
+        bar2 = m21 + m22 * x + y * m23;
+        if (bar1 >= 0.0 && bar2 >= 0.0 && bar1 + bar2 <= 1.0) {
+            ntr = 2 * ((s.p->nz - 1) * i + j) + k + 1;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+int add_marker(St &s, double x, double y, int iph, double age, int j, int i) {
+    double b1, b2;
+    int ntr;
+    if (!check_inside(s, x, y, b1, b2, ntr, i, j)) return 0;
+    gf_layout &L = *s.L;
+    int kk = s.c->nmarkers + 1;
+    long long e = s.e(j, i);
+    int nm = L.nmark_elem[e] + 1;
+    if (nm > GF_MAX_MARKERS_PER_ELEM || kk > L.max_markers) return -1;
+    s.c->nmarkers = kk;
+    L.nmark_elem[e] = nm;
+    L.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + (nm - 1)] = kk;
+    L.mark_dead[kk - 1] = 1;
+    L.mark_a1[kk - 1] = b1;
+    L.mark_a2[kk - 1] = b2;
+    L.mark_age[kk - 1] = age;
+    L.mark_ntriag[kk - 1] = ntr;
+    L.mark_phase[kk - 1] = (int8_t)iph;
+    return 1;
+}
+
+void marker2elem(St &s) {
+    int nx = s.p->nx, nz = s.p->nz;
+    gf_layout &L = *s.L;
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            int iseed = s.c->nloop + (i + 1) + (j + 1);
+            int kinc = L.nmark_elem[s.e(j, i)];
+            int icount = 0;
+            while (kinc <= 4) {
+                double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
+                double x1 = s.cord(j, i, 0) * (1 - r1) + s.cord(j, i + 1, 0) * r1;
+                double y1 = s.cord(j, i, 1) * (1 - r1) + s.cord(j, i + 1, 1) * r1;
+                double x2 = s.cord(j + 1, i, 0) * (1 - r1) + s.cord(j + 1, i + 1, 0) * r1;
+                double y2 = s.cord(j + 1, i, 1) * (1 - r1) + s.cord(j + 1, i + 1, 1) * r1;
+                double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
+                int inc = add_marker(s, xx, yy, L.iphase[s.e(j, i)], 0.0, j, i);
+                icount = icount + 1;
+                if (icount > 100) throw Stop{133};
+                if (inc <= 0) continue;
+                kinc = kinc + 1;
+            }
+            count_phase_ratio(s, j, i);
+        }
+    static const int mantle[5] = {4, 8, 9, 16, 18};
+    if (L.jmoho)
+        for (int i = 0; i < nx - 1; ++i) {
+            L.jmoho[i] = nz - 1;
+            for (int j = 0; j < nz - 1; ++j) {
+                double sum = 0.0;
+                for (int m = 0; m < 5; ++m) sum += s.pr(s.e(j, i), mantle[m]);
+                if (sum > 0.5) {
+                    L.jmoho[i] = j + 1;
+                    break;
+                }
+            }
+        }
+}
+
+// change_phase (src/change_phase.f90:35-262); melting (:264+) not on this path.
+void change_phase(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    const double max_basalt_depth = 150e3, min_eclogite_temp = 400.0, min_eclogite_depth = 20e3,
+                 mantle_density = 3000.0, max_melting_depth = 200e3, serpentine_temp = 550.0;
+    std::vector<uint8_t> itmp(s.d.E, 0);
+    int nmk = s.c->nmarkers;
+#pragma omp parallel for schedule(guided) num_threads(g_threads) if (g_threads > 1)
+    for (int kk = 0; kk < nmk; ++kk) {
+        if (L.mark_dead[kk] == 0) continue;
+        int n = L.mark_ntriag[kk];
+        int k = (n - 1) % 2 + 1;
+        int j = ((n - k) / 2) % (nz - 1);
+        int i = (n - k) / 2 / (nz - 1);
+        double a1 = L.mark_a1[kk], a2 = L.mark_a2[kk];
+        double yy, tmpr;
+        auto Tn = [&](int jj, int ii) { return L.temp[gf_node(s.d, jj, ii)]; };
+        if (k == 1) {
+            yy = s.cord(j, i, 1) * a1 + s.cord(j + 1, i, 1) * a2 + s.cord(j, i + 1, 1) * (1 - a1 - a2);
+            tmpr = Tn(j, i) * a1 + Tn(j + 1, i) * a2 + Tn(j, i + 1) * (1 - a1 - a2);
+        } else {
+            yy = s.cord(j, i + 1, 1) * a1 + s.cord(j + 1, i, 1) * a2 + s.cord(j + 1, i + 1, 1) * (1 - a1 - a2);
+            tmpr = Tn(j, i + 1) * a1 + Tn(j + 1, i) * a2 + Tn(j + 1, i + 1) * (1 - a1 - a2);
+        }
+        double depth = 0.5 * (s.cord(0, i, 1) + s.cord(0, i + 1, 1)) - yy;
+        if (depth > max_melting_depth) continue;
+        int iph = L.mark_phase[kk];
+        long long e = s.e(j, i);
+        int newph = 0;
+        switch (iph) {
+        case 2: case 6:
+            break;
+        case 4: case 8: {
+            if (depth > max_basalt_depth) break;
+            double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
+            double trpres2 = 2.1e9 + (0.6e9 - 2.1e9) * (tmpr - 730.0) / (670.0 - 730.0);
+            double press = mantle_density * p.g * depth;
+            double pg = std::fabs(press * 1e-9);
+            double solidus = -5.02 * (pg * pg) + 1.32e2 * pg + 1.09e3 + 35.0;
+            if (press < trpres && press > trpres2) {
+                int jb0 = std::min(j + 2, nz - 1), jb1 = std::min(j + 1 + p.nelem_serp, nz - 1);
+                for (int jb = jb0; jb <= jb1; ++jb) {
+                    long long eb = s.e(jb - 1, i);
+                    if (s.pr(eb, 3) > 0.8 || s.pr(eb, 7) > 0.8 || s.pr(eb, 1) > 0.8 || s.pr(eb, 11) > 0.8) {
+                        newph = 9;
+                        break;
+                    }
+                }
+            } else if (tmpr >= solidus + 35.0) {
+                newph = 18;
+            }
+            break;
+        }
+        case 10: case 3: case 7: {
+            double press = mantle_density * p.g * depth;
+            if (p.eclogite_rule == 1) {
+                if (tmpr >= 600.0 && press >= 1.5e9) newph = 13;
+            } else {
+                double trpres = -0.3e9 + 2.2e6 * tmpr;
+                double trpres2 = 20.1e9 - 0.0375e9 * tmpr;
+                if (!(tmpr < min_eclogite_temp || depth < min_eclogite_depth || press < trpres || press < trpres2)) newph = 13;
+            }
+            break;
+        }
+        case 9: {
+            double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
+            double trpres2 = 2.1e9 + (0.2e9 - 2.1e9) * (tmpr - 730.0) / (650.0 - 730.0);
+            double press = mantle_density * p.g * depth;
+            if (!(tmpr < serpentine_temp || (press < trpres && press > trpres2))) newph = 4;
+            break;
+        }
+        case 1:
+            if (!(tmpr < 80.0 && depth < 2e3)) newph = 11;
+            break;
+        case 11:
+            if (!(tmpr < 250.0 && depth < 7e3)) newph = 17;
+            break;
+        case 17: {
+            double trpres = 0.88e9 - (0.88e9 - 0.704e9) * (710.8 - tmpr) / (710.8 - 662.3);
+            double press = mantle_density * p.g * depth;
+            if (!(press < trpres)) newph = 5;
+            break;
+        }
+        case 5: {
+            double trpres = 0.0e9 - (0.0e9 - 1.2e9) * (500.0 - tmpr) / (500.0 - 600.0);
+            double press = mantle_density * p.g * depth;
+            if (!(press > trpres)) newph = 19;
+            break;
+        }
+        case 16: {
+            double dd = depth - 62e3;
+            double trtmpr = 880 - 35e-9 * (dd * dd);
+            if (!(tmpr < trtmpr)) newph = 4;
+            break;
+        }
+        default:
+            break;
+        }
+        if (newph) {
+            itmp[e] = 1;
+            L.mark_phase[kk] = (int8_t)newph;
+        }
+    }
+    int err = 0;
+#pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            if (!itmp[e]) continue;
+            try {
+                count_phase_ratio(s, j, i);
+            } catch (const Stop &st) {
+#pragma omp critical
+                err = st.code;
+            }
+            int kinc = L.nmark_elem[e];
+            double a0 = L.aps[e];
+            L.aps[e] = std::max(a0 - a0 / (double)(float)kinc, 0.0);
+        }
+    if (err) throw Stop{err};
+}
+
+// --------------------------------------------------------------------------
+// itest_mesh (src/rem_test.f90:70-136), angle criterion only
+
+double min_angle(St &s) {
+    int nx = s.p->nx, nz = s.p->nz;
+    const double pi = 3.14159265358979323846, raddeg = 180.0 / pi;
+    double anglemint = 180.0;
+#pragma omp parallel for reduction(min : anglemint) num_threads(g_threads) if (g_threads > 1)
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j)
+            for (int t = 0; t < 4; ++t) {
+                int iv[4], jv[4];
+                if (t == 0) { iv[0] = i; jv[0] = j; iv[1] = i; jv[1] = j + 1; iv[2] = i + 1; jv[2] = j; }
+                else if (t == 1) { iv[0] = i; jv[0] = j + 1; iv[1] = i + 1; jv[1] = j + 1; iv[2] = i + 1; jv[2] = j; }
+                else if (t == 2) { iv[0] = i; jv[0] = j; iv[1] = i; jv[1] = j + 1; iv[2] = i + 1; jv[2] = j + 1; }
+                else { iv[0] = i; jv[0] = j; iv[1] = i + 1; jv[1] = j + 1; iv[2] = i + 1; jv[2] = j; }
+                iv[3] = iv[0]; jv[3] = jv[0];
+                double ang[3];
+                for (int k = 1; k <= 2; ++k) {
+                    double xa = s.cord(jv[k + 1], iv[k + 1], 0) - s.cord(jv[k], iv[k], 0);
+                    double ya = s.cord(jv[k + 1], iv[k + 1], 1) - s.cord(jv[k], iv[k], 1);
+                    double xxal = std::sqrt(xa * xa + ya * ya);
+                    double xb = s.cord(jv[k - 1], iv[k - 1], 0) - s.cord(jv[k], iv[k], 0);
+                    double yb = s.cord(jv[k - 1], iv[k - 1], 1) - s.cord(jv[k], iv[k], 1);
+                    double xxbl = std::sqrt(xb * xb + yb * yb);
+                    ang[k] = raddeg * std::acos((xa * xb + ya * yb) / (xxal * xxbl));
+                }
+                ang[0] = 180.0 - ang[1] - ang[2];
+                double m = std::min(ang[0], std::min(ang[1], ang[2]));
+                anglemint = std::min(anglemint, m);
+            }
+    return anglemint;
+}
+
+template <class F> int guard(F &&f) {
+    try {
+        f();
+    } catch (const Stop &st) {
+        return st.code;
+    }
+    return 0;
+}
+
+} // namespace
+
+extern "C" {
+
+void or_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+int or_get_threads(void) { return g_threads; }
+
+#define OR_ENTRY(name, body)                                                                                           \
+    int or_##name(gf_params *p, gf_clock *c, gf_layout *L) {                                                             \
+        St s = make(p, c, L);                                                                                          \
+        return guard([&] { body; });                                                                                   \
+    }
+
+OR_ENTRY(fl_therm, fl_therm(s))
+OR_ENTRY(change_phase, change_phase(s))
+OR_ENTRY(fl_rheol, fl_rheol(s))
+OR_ENTRY(fl_node, fl_node(s))
+OR_ENTRY(fl_move, fl_move(s))
+OR_ENTRY(rmasses, rmasses(s))
+OR_ENTRY(dt_mass, dt_mass(s))
+OR_ENTRY(init_visc, init_visc(s))
+OR_ENTRY(marker2elem, marker2elem(s))
+
+// rmasses, init_visc, dt_mass and the averaging reset of setflac.f90:71-81
+int or_finish_setflac(gf_params *p, gf_clock *c, gf_layout *L) {
+    St s = make(p, c, L);
+    return guard([&] {
+        rmasses(s);
+        if (p->ivis_present == 1) init_visc(s);
+        dt_mass(s);
+        c->dtavg = 0;
+        c->nsrate = -1;
+    });
+}
+
+// flac (src/flac.f90:5-91) followed by par.f90:84-87
+int or_flac(gf_params *p, gf_clock *c, gf_layout *L) {
+    St s = make(p, c, L);
+    return guard([&] {
+        fl_therm(s);
+        if (p->itherm != 2) {
+            if (c->nloop % p->ifreq_rmasses == 0) change_phase(s);
+            fl_rheol(s);
+            fl_node(s);
+            fl_move(s);
+            if (c->nloop % p->ifreq_rmasses == 0) rmasses(s);
+            if (c->nloop % p->ifreq_imasses == 0) dt_mass(s);
+        }
+        c->nloop = c->nloop + 1;
+        c->time = c->time + c->dt;
+    });
+}
+
+int or_step(gf_params *p, gf_clock *c, gf_layout *L, int nsteps) {
+    for (int k = 0; k < nsteps; ++k) {
+        int rc = or_flac(p, c, L);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+int or_itest_mesh(gf_params *p, gf_clock *c, gf_layout *L, double *angle) {
+    St s = make(p, c, L);
+    double a = min_angle(s);
+    if (angle) *angle = a;
+    c->need_remeshing = (a <= p->angle_rem) ? 1 : 0;
+    return 0;
+}
+
+} // extern "C"

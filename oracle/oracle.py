@@ -1,0 +1,75 @@
+"""ctypes binding of the oracle (test infrastructure, never the product).
+
+Only tests/, the smoke check and the CPU-baseline leg of bench.py use this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+from geoflac_gb300.capi import GfClock, GfLayout, GfParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = C.CDLL(LIB_PATH)
+    P, K, L = C.POINTER(GfParams), C.POINTER(GfClock), C.POINTER(GfLayout)
+    for name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
+                 "init_visc", "marker2elem", "finish_setflac", "flac"):
+        f = getattr(lib, "or_" + name)
+        f.restype = C.c_int
+        f.argtypes = [P, K, L]
+    lib.or_step.restype = C.c_int
+    lib.or_step.argtypes = [P, K, L, C.c_int]
+    lib.or_itest_mesh.restype = C.c_int
+    lib.or_itest_mesh.argtypes = [P, K, L, C.POINTER(C.c_double)]
+    lib.or_set_threads.argtypes = [C.c_int]
+    lib.or_set_threads.restype = None
+    _lib = lib
+    return lib
+
+
+class Oracle:
+    """Runs the oracle's routines on one host state (params, clock, arrays)."""
+
+    def __init__(self, params: GfParams, clock: GfClock, state, threads: int = 1):
+        self.lib = load()
+        self.p = params
+        self.c = clock
+        self.s = state
+        self.lib.or_set_threads(threads)
+
+    def _call(self, name, *extra):
+        rc = getattr(self.lib, "or_" + name)(C.byref(self.p), C.byref(self.c), C.byref(self.s.layout), *extra)
+        if rc:
+            raise RuntimeError(f"oracle {name}: status {rc}")
+        return rc
+
+    def __getattr__(self, name):
+        if name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
+                    "init_visc", "marker2elem", "finish_setflac", "flac"):
+            return lambda: self._call(name)
+        raise AttributeError(name)
+
+    def step(self, n: int):
+        return self._call("step", C.c_int(n))
+
+    def itest_mesh(self) -> float:
+        a = C.c_double()
+        self._call("itest_mesh", C.byref(a))
+        return a.value
