@@ -246,6 +246,14 @@ def run_ours(args):
 
     d = tempfile.mkdtemp(prefix="gfbench")
     inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    if args.profile:
+        # profiling run: only `warmup + steps` graph-replayed steps of one mode
+        g = _make_model(inp, args.profile)
+        g.step(args.warmup + args.steps)
+        g.status()
+        print(json.dumps({"profile": args.profile, "steps": args.warmup + args.steps, "launches": g.launches}))
+        g.close()
+        return
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     E = 1000 * 300
     res = {}
@@ -263,6 +271,14 @@ def run_ours(args):
         dev_t = float(t.item())
         res[mode] = dict(g=g, t=dev_t, launches=launches, clocks=cs.summary(), wall=wall)
     fp = res["fp64"]
+    # both modes advanced the same number of steps from the same state:
+    # per-field error of the mixed path, max|a-b| / max|b|
+    mixed_err = {}
+    fp["g"].download()
+    res["mixed"]["g"].download()
+    for f in ("vel", "cord", "temp", "stress0", "aps"):
+        a, b = res["mixed"]["g"].state[f], fp["g"].state[f]
+        mixed_err[f] = float(abs(a - b).max() / max(abs(b).max(), 1e-300))
     value = ws * E * args.steps / fp["t"]
     mixed_value = ws * E * args.steps / res["mixed"]["t"]
     # dominant kernel: fl_rheol (k_rheol), timed alone
@@ -284,7 +300,9 @@ def run_ours(args):
                    "markers_per_element": 9, "parallelism": f"replicas x{ws}",
                    "l2": "512 MiB buffer written between timed steps"},
         "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
-                  "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes"},
+                  "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes",
+                  "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup},
+        "therm_sweeps_fp64": fp["g"].clock.therm_sweeps,
         "e2e": {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "path": "per-subroutine C-ABI calls, clock scalars in/out, cord+vel to host every step"},
@@ -364,6 +382,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["fp64", "mixed"], default=None,
+                    help="run warmup+steps steps of one mode and nothing else (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

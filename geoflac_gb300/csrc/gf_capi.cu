@@ -117,6 +117,8 @@ GfLaunch launch_of(gf_ctx *c) {
     g.d = c->d;
     g.s = c->s;
     g.launches = &c->launches;
+    g.idt_scale = c->p.idt_scale;
+    g.advance_time = 0;
     return g;
 }
 
@@ -175,7 +177,22 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.bc, A.bc, 2 * N, dir));
         T_(xfer(c, L.ncod, A.ncod, 2 * N, dir));
     }
-    if (m & GF_F_STRESS) T_(xfer_r(c, L.stress0, A.stress0, 16 * E, dir));
+    if ((m & GF_F_STRESS) && L.stress0) {
+        if (c->mode == GF_MODE_FP64) {
+            T_(xfer_r(c, L.stress0, A.stress0, 16 * E, dir));
+        } else {
+            // mixed: FP32 deviations from the element's reference pressure
+            GfLaunch g = launch_of(c);
+            if (dir) {
+                GF_CK(cudaMemcpyAsync(c->staging, L.stress0, 16 * E * sizeof(double), cudaMemcpyHostToDevice, c->s));
+                GfKernels<float>::stress_in(g, c->staging);
+            } else {
+                GfKernels<float>::stress_out(g, c->staging);
+                GF_CK(cudaMemcpyAsync(L.stress0, c->staging, 16 * E * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+            }
+            GF_CK(cudaStreamSynchronize(c->s));
+        }
+    }
     if (m & GF_F_AREA) {
         T_(xfer_r(c, L.area, A.area, 4 * E, dir));
         T_(xfer_r(c, L.dvol, A.dvol, 4 * E, dir));
@@ -258,8 +275,9 @@ void k_node(gf_ctx *c) {
     if (c->mode == GF_MODE_MIXED) GfKernels<float>::node(g);
     else GfKernels<double>::node(g);
 }
-void k_move(gf_ctx *c) {
+void k_move(gf_ctx *c, int advance_time = 0) {
     GfLaunch g = launch_of(c);
+    g.advance_time = advance_time;
     if (c->mode == GF_MODE_MIXED) GfKernels<float>::move(g);
     else GfKernels<double>::move(g);
 }
@@ -302,17 +320,25 @@ unsigned step_signature(const gf_ctx *c) {
 // Enqueue one step (flac.f90:5-91 + par.f90:84-87) for a signature.
 void enqueue_step(gf_ctx *c, unsigned sig) {
     k_therm(c);
+    // par.f90:86 adds the dt that dt_mass may have just changed, so time
+    // advances inside fl_move's kernel only on steps without dt_mass
+    bool folded = false;
     if (sig & 1u) {
         if (sig & 2u) k_change_phase(c);
         int avg = (sig & (8u << 8)) ? 2 : ((sig & (4u << 8)) ? 1 : 0);
         k_rheol(c, (sig & 4u) ? 1 : 0, avg);
         k_node(c);
-        k_move(c);
+        if (c->p.movegrid != 0) {
+            folded = !(sig & 32u);
+            k_move(c, folded ? 1 : 0);
+        }
         if (sig & 16u) k_rmasses(c);
         if (sig & 32u) k_dt_mass(c);
     }
-    k_clock_advance<<<1, 1, 0, c->s>>>(c->dC);
-    ++c->launches;
+    if (!folded) {
+        k_clock_advance<<<1, 1, 0, c->s>>>(c->dC);
+        ++c->launches;
+    }
 }
 
 // host bookkeeping that mirrors the device's after one step
@@ -422,6 +448,8 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.t_delta1, N));
     A_(dalloc(c, &A.t_coef, (size_t)18 * E));
     A_(dalloc(c, &A.e_dens, E));
+    A_(dalloc(c, &A.e_tri, 4 * E));
+    A_(dalloc(c, &A.p_ref, E));
     A_(dalloc(c, &A.e_rho, E));
     A_(dalloc(c, &A.e_flag, E));
     A_(dalloc(c, &A.nmarkers, 1));

@@ -63,7 +63,9 @@ struct DevArrays {
     // scratch
     double *t_delta0, *t_delta1; // thermal sweep iterates (node)
     double *t_coef;              // thermal per-element coefficients (18 per element)
+    double *p_ref; // mixed: per-element reference pressure; stored normal stresses are total + p_ref
     double *e_dens;                                   // per-element density (rmasses)
+    double *e_tri;                                    // per-triangle mass shares (4 per element)
     double *e_rho;                                    // per-element inertial density (dt_mass)
     uint8_t *e_flag;                                  // change_phase element flags
     int *m_count, *m_offset;                          // marker2elem scan
@@ -78,6 +80,8 @@ struct GfLaunch {
     GfDims d;
     cudaStream_t s;
     long long *launches;
+    int idt_scale;   // host copy of the mass-scaling mode (selects launches)
+    int advance_time; // fold par.f90's time += dt into the step's last kernel
 };
 
 // Launchers, one set per precision (template instantiated in its own TU).
@@ -92,5 +96,8 @@ template <class R> struct GfKernels {
     static void change_phase(const GfLaunch &g, int nmarkers);
     static void min_angle(const GfLaunch &g, double *d_out);
     static void convert_in(const GfLaunch &g, unsigned mask, const double *src, void *dst, long long n);
+    // mixed: total stress (FP64 staging) <-> stored deviations from -p_ref
+    static void stress_in(const GfLaunch &g, const double *src);
+    static void stress_out(const GfLaunch &g, double *dst);
 };
 

@@ -136,6 +136,61 @@ __device__ double eff_visc(const DevParams &P, const DevArrays &A, const GfDims 
     return fmin(P.v_max, fmax(P.v_min, ev));
 }
 
+// Eff_visc in FP32 for the mixed-precision path: the power-law viscosity is
+// evaluated as a sum of logarithms and clamped in log space, so no
+// intermediate leaves the FP32 range (A^(-1/n) e^(E/nRT) alone can exceed it).
+__device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+                              const float *__restrict__ st) {
+    for (int k = 0; k < P.ninh100; ++k)
+        if (i + 1 >= P.w_ix1[k] && i + 1 <= P.w_ix2[k] && j + 1 >= P.w_iy1[k] && j + 1 <= P.w_iy2[k])
+            return (float)P.v_min;
+    const double *cord = A.cord, *temp = A.temp;
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
+    double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
+    float tmpr0 = 0.25f * float(temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
+    float tmpr = float(zsurf - zcord) * 1e-3f * 0.3f + tmpr0;
+    float s11 = 0.25f * (st[gf_s(d, e, 0, 0)] + st[gf_s(d, e, 0, 1)] + st[gf_s(d, e, 0, 2)] + st[gf_s(d, e, 0, 3)]);
+    float s22 = 0.25f * (st[gf_s(d, e, 1, 0)] + st[gf_s(d, e, 1, 1)] + st[gf_s(d, e, 1, 2)] + st[gf_s(d, e, 1, 3)]);
+    float s33 = 0.25f * (st[gf_s(d, e, 3, 0)] + st[gf_s(d, e, 3, 1)] + st[gf_s(d, e, 3, 2)] + st[gf_s(d, e, 3, 3)]);
+    float pres = -(s11 + s22 + s33) / 3.0f + (float)A.p_ref[e]; // stored stresses are deviations from -p_ref
+    float zc = float(zcord);
+    float deptmpr410 = -101.58f * (tmpr + 273.0f) - 216828.0f;
+    float deptmpr660 = 66.55f * (tmpr + 273.0f) - 788494.0f;
+    float vmin = (float)P.v_min, vmax = (float)P.v_max;
+    if (zc < deptmpr660 || zc < deptmpr410) {
+        float ev = (zc < deptmpr660 ? 1e22f : 1e21f) * expf(-0.0115f * (tmpr - (float)P.t_bot));
+        return fminf(vmax, fmaxf(vmin, ev));
+    }
+    float srat = ((const float *)A.e2sr)[e];
+    if (srat == 0.0f) srat = float(P.vbc / P.rxbo);
+    const float lmin = logf(vmin), lmax = logf(vmax);
+    const float lsr = logf(srat), lbase = logf(0.25f * 1e6f);
+    float ev = 0.0f;
+    for (int k = 0; k < P.nphase; ++k) {
+        float ratio = (float)A.phase_ratio[gf_pr(d, e, k)];
+        if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
+        float n = (float)P.pln[k];
+        float lv = lbase + (1.0f / n - 1.0f) * lsr - (1.0f / n) * logf(0.75f * (float)P.acoef[k]) +
+                   ((float)P.eactiv[k] + (float)P.vactiv[k] * pres) / (n * 8.31448f * (tmpr + 273.0f));
+        lv = fminf(lmax, fmaxf(lmin, lv));
+        ev += ratio / expf(lv);
+    }
+    ev = 1.0f / ev;
+    if (P.itype_melting == 1) {
+        float fma = fminf(float(A.fmagma[e] + A.fmagma2[e]), (float)P.fmagma_max);
+        ev *= expf((float)P.weaken_ratio_viscous * fma / (float)P.fmagma_max);
+    }
+    return fminf(vmax, fmaxf(vmin, ev));
+}
+
+template <class R>
+__device__ __forceinline__ double visc_of(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i,
+                                          long long e, const R *__restrict__ st) {
+    if (sizeof(R) == sizeof(float)) return (double)eff_visc_f32(P, A, d, j, i, e, (const float *)st);
+    return eff_visc<R>(P, A, d, j, i, e, st);
+}
+
 // Eff_dens (matprops.f90:3-83), FP64.  *wrote_frac/*frac_val report the
 // write of the global frac the reference performs (matprops.f90:37,48).
 template <class R>
@@ -176,6 +231,7 @@ __device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims 
     for (int k = 0; k < 4; ++k)
         press = press - ((double)st[gf_s(d, e, 0, k)] + (double)st[gf_s(d, e, 1, k)] + (double)st[gf_s(d, e, 3, k)]);
     press = press / 12;
+    if (sizeof(R) == sizeof(float)) press = press + A.p_ref[e]; // mixed: stored stresses exclude -p_ref
     double ed = 0.0;
     for (int k = 0; k < P.nphase; ++k) {
         double ratio = A.phase_ratio[gf_pr(d, e, k)];
@@ -325,6 +381,70 @@ __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &dep
     s22 = R(0.5) * (dss - dc2);
     s12 = R(0.5) * (s1 - s3) * si2;
     s33 = s2;
+}
+
+// plastic in the mixed path, where normal stresses are stored as deviations
+// from the element's reference pressure p (total = stored - p): the same
+// return map, with the tension cut-off and the yield function shifted by p so
+// that no total stress (up to 1e10 Pa at depth) is formed in FP32.
+__device__ __forceinline__ void plastic_dev(const PlasticConsts<float> &c, float rmu, float &depls, float hardn,
+                                            float &s11, float &s22, float &s33, float &s12, float de11, float de22,
+                                            float de33, float de12, float p) {
+    depls = 0.0f;
+    float e1 = c.e1, e2 = c.e2, anphi = c.anphi, anpsi = c.anpsi;
+    float tm = c.ten_max + p; // tension cut-off in stored (deviation) units
+    float s11i = s11 + (de22 + de33) * e2 + de11 * e1;
+    float s22i = s22 + (de11 + de33) * e2 + de22 * e1;
+    float s12i = s12 + de12 * 2.0f * rmu;
+    float s33i = s33 + (de11 + de22) * e2 + de33 * e1;
+    float sdif = s11i - s22i;
+    float s0 = 0.5f * (s11i + s22i);
+    float rad = 0.5f * sqrtf(sdif * sdif + 4.0f * s12i * s12i);
+    float si = s0 - rad, sii = s0 + rad, psdif = si - sii;
+    float s1 = si, s2 = s33i, s3 = sii;
+    if (s1 >= tm) {
+        s11 = tm; s22 = tm; s12 = 0.0f; s33 = tm;
+        return;
+    }
+    if (s3 >= tm) s3 = tm;
+    float fs = (s1 - s3 * anphi + c.amc) - p * (1.0f - anphi);
+    if (fs < 0.0f) {
+        float alams = fs / (c.x1 + hardn);
+        s1 = s1 - alams * (e1 - e2 * anpsi);
+        s2 = s2 - alams * e2 * (1.0f - anpsi);
+        s3 = s3 - alams * (e2 - e1 * anpsi);
+        depls = 0.5f * fabsf(alams + alams * anpsi);
+    } else {
+        s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;
+        return;
+    }
+    if (s1 >= tm) {
+        s11 = tm; s22 = tm; s12 = 0.0f; s33 = tm;
+        return;
+    }
+    if (s3 >= tm) s3 = tm;
+    float cs2 = 1.0f, si2 = 0.0f;
+    if (psdif != 0.0f) {
+        cs2 = sdif / psdif;
+        si2 = 2.0f * s12i / psdif;
+    }
+    float dc2 = (s1 - s3) * cs2;
+    float dss = s1 + s3;
+    s11 = 0.5f * (dss + dc2);
+    s22 = 0.5f * (dss - dc2);
+    s12 = 0.5f * (s1 - s3) * si2;
+    s33 = s2;
+}
+
+__device__ __forceinline__ void plastic_sel(const PlasticConsts<double> &c, double rmu, double &depls, double hardn,
+                                            double &s11, double &s22, double &s33, double &s12, double de11,
+                                            double de22, double de33, double de12, double) {
+    plastic<double>(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12);
+}
+__device__ __forceinline__ void plastic_sel(const PlasticConsts<float> &c, float rmu, float &depls, float hardn,
+                                            float &s11, float &s22, float &s33, float &s12, float de11, float de22,
+                                            float de33, float de12, float pref) {
+    plastic_dev(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12, pref);
 }
 
 // pre_plast (rh_plastic.f90:339-399)

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
     int j, i;
     elem_ji(d, e, j, i);
     const double dtd = C->dt;
+    if (e == 0) C->dtavg = C->dtavg + dtd; // fl_rheol.f90:43 (no thread reads dtavg here)
     const R dt = R(dtd);
     R *st = (R *)A.stress0;
     const R *area = (const R *)A.area;
@@ -98,12 +99,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
         stherm = R(-P.alfa[iph] * (P.rl[iph] + 2.0 * P.rm[iph] / 3.0) * (A.temp[n1] - A.temp0[n1]));
     R *aps = (R *)A.aps;
     R aps_e = aps[e];
+    // mixed path: stored normal stresses are deviations from -pref
+    const R pref = sizeof(R) == sizeof(float) ? R(A.p_ref[e]) : R(0);
     R coh = 0, phi = 0, psi = 0, hardn = 0;
     if (irh == 6 || irh >= 11) pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
     R *visn = (R *)A.visn;
     R vis;
     if ((irh == 3 || irh >= 11) && update_visc) {
-        vis = R(eff_visc<R>(P, A, d, j, i, e, st));
+        vis = R(visc_of<R>(P, A, d, j, i, e, st));
         visn[e] = vis;
     } else {
         vis = visn[e];
@@ -128,9 +131,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
         } else if (irh == 3) {
             ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
         } else if (irh == 6) {
-            plastic<R>(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12);
+            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref);
         } else if (irh >= 11) {
-            plastic<R>(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12);
+            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref);
             ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
         }
     }
@@ -184,6 +187,10 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
     // accumulates the element-averaged start-of-step stress (s11/s22/s12 are
     // reassigned before this point in fl_rheol.f90:181-183)
     R *strain = (R *)A.strain;
+    if (sizeof(R) == sizeof(float)) { // total stress, not the stored deviation
+        s11 = s11 - pref;
+        s22 = s22 - pref;
+    }
     strain[gf_ek(d, e, 0)] = strain[gf_ek(d, e, 0)] + s11 * dt;
     strain[gf_ek(d, e, 1)] = strain[gf_ek(d, e, 1)] + s22 * dt;
     strain[gf_ek(d, e, 2)] = strain[gf_ek(d, e, 2)] + s12 * dt;
@@ -212,6 +219,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
             R a11 = R(0.5) * (s0v[0][k] + f11), a22 = R(0.5) * (s0v[1][k] + f22), a12 = R(0.5) * (s0v[2][k] + f12),
               a33 = R(0.5) * (s0v[3][k] + f33);
             R qk = a11 * d11 + a22 * d22 + R(2.0) * a12 * d12 + a33 * d33;
+            if (sizeof(R) == sizeof(float)) qk -= pref * (d11 + d22 + d33); // isotropic reference part
             qsum = qsum + R(0.25) * qk;
         }
         shr = shr + qsum;
@@ -266,32 +274,91 @@ __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict
     // kk/mm tables of fl_node.f90:7-8 (0-based)
     const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
     const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
-    R fx0 = R(0.0), fy0 = R(0.0);
+    double f0, f1;
+    const bool interior = j > 0 && j < nz - 1 && i > 0 && i < nx - 1;
+    if (sizeof(R) == sizeof(float) && interior) {
+        // Mixed path.  Stored normal stresses are deviations from the
+        // element's reference pressure p_ref.  Around an interior node the
+        // triangle edges close, so subtracting one neighbouring triangle's
+        // stress (sigma_n) from every term leaves the force unchanged in
+        // exact arithmetic while the FP32 terms become small differences.
+        const long long en = gf_elem(d, j - 1, i - 1);
+        const float nxx = (float)st[gf_s(d, en, 0, 1)], nzz = (float)st[gf_s(d, en, 1, 1)],
+                    nxz = (float)st[gf_s(d, en, 2, 1)];
+        const double pn = A.p_ref[en];
+        float fx0 = 0.0f, fy0 = 0.0f;
 #pragma unroll
-    for (int qd = 0; qd < 4; ++qd) {
-        int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
-        if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
-        long long e = gf_elem(d, je, ie);
-        Quad q;
-        load_quad(A.cord, d, je, ie, q);
-        R ar[4];
+        for (int qd = 0; qd < 4; ++qd) {
+            int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+            long long e = gf_elem(d, je, ie);
+            Quad q;
+            load_quad(A.cord, d, je, ie, q);
+            float ar[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
-        R dx[3][4], dz[3][4];
-        shape_derivs<R>(q, ar, dx, dz);
+            for (int k = 0; k < 4; ++k) ar[k] = (float)area[gf_ek(d, e, k)];
+            float dx[3][4], dz[3][4];
+            shape_derivs<float>(q, ar, dx, dz);
+            float dp = float(A.p_ref[e] - pn);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            int t = kk[qd][k], m = mm[qd][k];
-            R factor = R(0.25) / ar[t];
-            R sxx = st[gf_s(d, e, 0, t)], szz = st[gf_s(d, e, 1, t)], sxz = st[gf_s(d, e, 2, t)];
-            R fx = factor * (sxx * dx[m][t] + sxz * dz[m][t]);
-            R fy = factor * (sxz * dx[m][t] + szz * dz[m][t]);
-            fx0 = fx0 - fx;
-            fy0 = fy0 - fy;
+            for (int k = 0; k < 3; ++k) {
+                int t = kk[qd][k], m = mm[qd][k];
+                float factor = 0.25f / ar[t];
+                float sxx = ((float)st[gf_s(d, e, 0, t)] - nxx) - dp;
+                float szz = ((float)st[gf_s(d, e, 1, t)] - nzz) - dp;
+                float sxz = (float)st[gf_s(d, e, 2, t)] - nxz;
+                fx0 -= factor * (sxx * dx[m][t] + sxz * dz[m][t]);
+                fy0 -= factor * (sxz * dx[m][t] + szz * dz[m][t]);
+            }
         }
+        f0 = (double)fx0;
+        f1 = (double)fy0 - A.rmass[n] * P.g;
+    } else {
+        // FP64 path (and boundary nodes of the mixed path, from total stresses)
+        const bool dev = sizeof(R) == sizeof(float);
+        R fx0 = R(0.0), fy0 = R(0.0);
+        double gx = 0.0, gy = 0.0;
+#pragma unroll
+        for (int qd = 0; qd < 4; ++qd) {
+            int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+            if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
+            long long e = gf_elem(d, je, ie);
+            Quad q;
+            load_quad(A.cord, d, je, ie, q);
+            R ar[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
+            if (!dev) {
+                R dx[3][4], dz[3][4];
+                shape_derivs<R>(q, ar, dx, dz);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    int t = kk[qd][k], m = mm[qd][k];
+                    R factor = R(0.25) / ar[t];
+                    R sxx = st[gf_s(d, e, 0, t)], szz = st[gf_s(d, e, 1, t)], sxz = st[gf_s(d, e, 2, t)];
+                    R fx = factor * (sxx * dx[m][t] + sxz * dz[m][t]);
+                    R fy = factor * (sxz * dx[m][t] + szz * dz[m][t]);
+                    fx0 = fx0 - fx;
+                    fy0 = fy0 - fy;
+                }
+            } else {
+                double ard[4] = {(double)ar[0], (double)ar[1], (double)ar[2], (double)ar[3]};
+                double dx[3][4], dz[3][4];
+                shape_derivs<double>(q, ard, dx, dz);
+                double pe = A.p_ref[e];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    int t = kk[qd][k], m = mm[qd][k];
+                    double factor = 0.25 / ard[t];
+                    double sxx = (double)st[gf_s(d, e, 0, t)] - pe, szz = (double)st[gf_s(d, e, 1, t)] - pe,
+                           sxz = (double)st[gf_s(d, e, 2, t)];
+                    gx -= factor * (sxx * dx[m][t] + sxz * dz[m][t]);
+                    gy -= factor * (sxz * dx[m][t] + szz * dz[m][t]);
+                }
+            }
+        }
+        f0 = dev ? gx : (double)fx0;
+        f1 = (dev ? gy : (double)fy0) - A.rmass[n] * P.g;
     }
-    double f0 = (double)fx0;
-    double f1 = (double)fy0 - A.rmass[n] * P.g;
     const double *cord = A.cord;
     if (P.nyhydro > 0 && j == 0) { // water load on the surface
         double rho_water_g = 1030.0 * P.g;
@@ -343,8 +410,15 @@ __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict
     if ((c0 & 1) != 1 && fabs(v0) > 1.0e-13) f0 = f0 - P.demf * copysign(fabs(f0), v0);
     if ((c1 & 2) != 2 && fabs(v1) > 1.0e-13) f1 = f1 - P.demf * copysign(fabs(f1), v1);
     double am = A.amass[n];
-    v0 = (c0 == 1) ? A.bc[n] : v0 + dt * f0 / (am * drat * drat);
-    v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + dt * f1 / (am * drat * drat);
+    if (sizeof(R) == sizeof(float)) {
+        // FP32 increment on the FP64 velocity
+        float s = float(dt) / (float(am) * float(drat) * float(drat));
+        v0 = (c0 == 1) ? A.bc[n] : v0 + (double)(s * float(f0));
+        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + (double)(s * float(f1));
+    } else {
+        v0 = (c0 == 1) ? A.bc[n] : v0 + dt * f0 / (am * drat * drat);
+        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + dt * f1 / (am * drat * drat);
+    }
     if (P.i_prestress == 1 && C->time < 600e3 * GF_SEC_YEAR) {
         if (j == nz - 1 || i == 0 || i == nx - 1) {
             v0 = 0.0;
@@ -364,12 +438,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__
 }
 
 template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d) {
+__global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d,
+                                                          int advance_time) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
     const double dtd = C->dt;
+    if (advance_time && e == 0) C->time = C->time + dtd; // par.f90:86, after every reader of time
     Quad q;
     load_quad(A.cord, d, j, i, q);
     long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
@@ -382,20 +458,47 @@ __global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__
     R *strain = (R *)A.strain;
     const int nd1[4] = {0, 2, 0, 0}, nd2[4] = {1, 1, 1, 3}, nd3[4] = {2, 3, 3, 2};
     bool neg = false;
+    const bool fp32 = sizeof(R) == sizeof(float);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int a = nd1[k], b = nd2[k], c = nd3[k];
         const double *xc = q.x, *yc = q.y;
-        double det = ((xc[b] * yc[c] - yc[b] * xc[c]) - (xc[a] * yc[c] - yc[a] * xc[c])) + (xc[a] * yc[b] - yc[a] * xc[b]);
         R ar_old = area[gf_ek(d, e, k)];
-        dvol[gf_ek(d, e, k)] = R(det * (double)ar_old - 1.0);
-        R ar_new = R(1.0 / det);
+        R dw12, ar_new;
+        if (!fp32) {
+            // fl_move.f90:70-90 with the reference's operations
+            double det =
+                ((xc[b] * yc[c] - yc[b] * xc[c]) - (xc[a] * yc[c] - yc[a] * xc[c])) + (xc[a] * yc[b] - yc[a] * xc[b]);
+            dvol[gf_ek(d, e, k)] = R(det * (double)ar_old - 1.0);
+            ar_new = R(1.0 / det);
+            double dw = 0.5 *
+                        (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) +
+                         yv[a] * (yc[c] - yc[b]) + yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])) /
+                        det * dtd;
+            dw12 = R(dw);
+        } else {
+            // FP32 from edge vectors (FP64 differences): det = B x C with
+            // B = b - a, C = c - a.  dvol = det_new*area_old - 1 is taken as
+            // (det_new - det_old)*area_old with the change of det expanded in
+            // this step's displacements u = vel*dt, which FP32 resolves.
+            float Bx = float(xc[b] - xc[a]), By = float(yc[b] - yc[a]);
+            float Cx = float(xc[c] - xc[a]), Cy = float(yc[c] - yc[a]);
+            float dBx = float((xv[b] - xv[a]) * dtd), dBy = float((yv[b] - yv[a]) * dtd);
+            float dCx = float((xv[c] - xv[a]) * dtd), dCy = float((yv[c] - yv[a]) * dtd);
+            float Box = Bx - dBx, Boy = By - dBy, Cox = Cx - dCx, Coy = Cy - dCy;
+            float ddet = (Box * dCy - Boy * dCx) + (dBx * Coy - dBy * Cox) + (dBx * dCy - dBy * dCx);
+            float det = Bx * Cy - By * Cx;
+            dvol[gf_ek(d, e, k)] = R(ddet * (float)ar_old);
+            ar_new = R(1.0f / det);
+            // 0.5 * curl of the velocity over the triangle, times dt
+            float wx = float(xv[a]) * float(xc[c] - xc[b]) + float(xv[b]) * float(xc[a] - xc[c]) +
+                       float(xv[c]) * float(xc[b] - xc[a]);
+            float wy = float(yv[a]) * float(yc[c] - yc[b]) + float(yv[b]) * float(yc[a] - yc[c]) +
+                       float(yv[c]) * float(yc[b] - yc[a]);
+            dw12 = R(0.5f * (wx + wy) / det * float(dtd));
+        }
         area[gf_ek(d, e, k)] = ar_new;
         neg |= !(ar_new > R(0));
-        double dw = 0.5 * (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) + yv[a] * (yc[c] - yc[b]) +
-                           yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])) /
-                    det * dtd;
-        R dw12 = R(dw);
         R s11 = st[gf_s(d, e, 0, k)], s22 = st[gf_s(d, e, 1, k)], s12 = st[gf_s(d, e, 2, k)];
         st[gf_s(d, e, 0, k)] = s11 + s12 * R(2) * dw12;
         st[gf_s(d, e, 1, k)] = s22 - s12 * R(2) * dw12;
@@ -436,9 +539,11 @@ __device__ __forceinline__ int kidx(int a, int b) {
 }
 
 template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
-                                                           double *__restrict__ tc) {
+__global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                           DevArrays A, GfDims d, double *__restrict__ tc) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 0)
+        for (int k = 0; k < GF_THERM_KMAX; ++k) C->therm_flags[k] = 0; // before any sweep runs
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -521,9 +626,30 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict
     if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
 }
 
-// temp0 = temp; temp = converged iterate (fl_therm.f90:46-48, 569)
-__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(DevClock *__restrict__ C, DevArrays A, GfDims d,
-                                                            const double *__restrict__ b0,
+// Temperature after the boundary conditions of fl_therm.f90:573-598 (top
+// row t_top, bottom row bot_bc or the flux condition, then the side columns
+// copied from their inner neighbours), read from the swept values `src`.
+__device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevArrays &A, const GfDims &d,
+                                                 const double *__restrict__ src, int j, int i) {
+    const int nx = d.nx, nz = d.nz;
+    int ii = (i == 0 || nx == 2) ? 1 : (i == nx - 1 ? nx - 2 : i);
+    if (j == 0) return P.t_top;
+    if (j == nz - 1) {
+        if (P.itemp_bc == 1) return P.bot_bc;
+        if (P.itemp_bc == 2) {
+            int ie = ii < nx - 2 ? ii : nx - 2;
+            double cond_eff = P.conduct[A.iphase[gf_elem(d, nz - 2, ie)] - 1];
+            return src[gf_node(d, nz - 2, ii)] +
+                   P.bot_bc * (A.cord[d.N + gf_node(d, nz - 2, ii)] - A.cord[d.N + gf_node(d, nz - 1, ii)]) / cond_eff;
+        }
+    }
+    return src[gf_node(d, j, ii)];
+}
+
+// temp0 = temp (fl_therm.f90:46-48); temp = converged iterate with the
+// boundary conditions applied.
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                            DevArrays A, GfDims d, const double *__restrict__ b0,
                                                             const double *__restrict__ b1, int kmax) {
     int kc = kmax;
     for (int k = 0; k < kmax; ++k)
@@ -540,37 +666,114 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_apply(DevClock *__restrict
     // sweep kc (or the last one) wrote buffer kc & 1
     int k = kc < kmax ? kc : kmax - 1;
     const double *src = (k & 1) ? b1 : b0;
+    int j, i;
+    node_ji(d, n, j, i);
+    double t = therm_bc_value(*Pp, A, d, src, j, i);
     A.temp0[n] = A.temp[n];
-    A.temp[n] = src[n];
+    A.temp[n] = t;
 }
 
-__global__ void k_therm_reset(DevClock *C) {
-    for (int k = 0; k < GF_THERM_KMAX; ++k) C->therm_flags[k] = 0;
-}
-
-__global__ void k_therm_bc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+// ---- mixed precision: FP32 coefficients, two sweeps.
+// The diffusion sum is taken over temperature differences to the updated
+// node (the rows of the triangle stiffness sum to zero), so FP32 keeps the
+// accuracy that a sum of ~1000 C values would lose.  Sweep 0 is the all-old
+// (Jacobi) update, sweep 1 reuses the upstream increments of sweep 0, which
+// leaves an error of order (kappa dt/h^2)^2 relative to the increment.
+__global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
+                                                             float *__restrict__ tc) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
     const DevParams &P = *Pp;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int j, i;
+    elem_ji(d, e, j, i);
+    int iph = A.iphase[e] - 1;
+    float cp_eff = (float)P.cp[iph], cond_eff = (float)P.conduct[iph], den = (float)P.den[iph];
+    float dissip = (P.ishearh == 1 && P.itherm != 2) ? ((const float *)A.shrheat)[e] : 0.0f;
+    float diff = cond_eff / den / cp_eff;
+    float src = ((float)A.source[e] + dissip / den) / cp_eff;
+    Quad q;
+    load_quad(A.cord, d, j, i, q);
+    const float *area = (const float *)A.area;
+    const long long E = d.E;
+    const int tv[2][3] = {{0, 1, 2}, {2, 1, 3}};
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        float a = area[gf_ek(d, e, t)];
+        const int v1 = tv[t][0], v2 = tv[t][1], v3 = tv[t][2];
+        float dd[3] = {float(q.y[v2] - q.y[v3]) * a, float(q.y[v3] - q.y[v1]) * a, float(q.y[v1] - q.y[v2]) * a};
+        float zz[3] = {float(q.x[v3] - q.x[v2]) * a, float(q.x[v1] - q.x[v3]) * a, float(q.x[v2] - q.x[v1]) * a};
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = dd[m] * dd[n] + zz[m] * zz[n];
+        float inv_area = 1.0f / a;
+        float ra = inv_area / 6.0f;
+        tc[(12 + t) * E + e] = ra;
+        tc[(14 + t) * E + e] = 0.5f * diff * inv_area;
+        tc[(16 + t) * E + e] = src * ra;
+    }
+}
+
+// sweep 0 (final = 0): dT0 = increment with old values; sweep 1 (final = 1):
+// upstream neighbours use T + dT0, then the BCs are applied.
+__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp,
+                                                              DevClock *__restrict__ C, DevArrays A, GfDims d,
+                                                              const float *__restrict__ tc, float *__restrict__ d0,
+                                                              double *__restrict__ tnew, int final_sweep) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    int j, i;
+    node_ji(d, n, j, i);
     const int nx = d.nx, nz = d.nz;
-    // top and bottom rows first (all columns), then the side columns: one
-    // block does everything in the reference's order (nx, nz are small).
-    for (int i = t; i < nx; i += blockDim.x) {
-        A.temp[gf_node(d, 0, i)] = P.t_top;
-        if (P.itemp_bc == 1)
-            A.temp[gf_node(d, nz - 1, i)] = P.bot_bc;
-        else if (P.itemp_bc == 2) {
-            int ie = i < nx - 2 ? i : nx - 2;
-            double cond_eff = P.conduct[A.iphase[gf_elem(d, nz - 2, ie)] - 1];
-            A.temp[gf_node(d, nz - 1, i)] =
-                A.temp[gf_node(d, nz - 2, i)] +
-                P.bot_bc * (A.cord[d.N + gf_node(d, nz - 2, i)] - A.cord[d.N + gf_node(d, nz - 1, i)]) / cond_eff;
-        }
+    const long long E = d.E;
+    const double *T = A.temp;
+    const double Ts = T[n];
+    float rhs = 0.0f, area_n = 0.0f;
+    auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
+    // temperature difference to the updated node; upstream nodes carry the
+    // increment of sweep 0 in the final sweep
+    auto dT = [&](long long m, bool up) {
+        float v = float(T[m] - Ts);
+        if (up && final_sweep) v += d0[m];
+        return v;
+    };
+    auto tri = [&](long long e, int t, int vs, int v0, float D0, int v1, float D1, int v2, float D2) {
+        float ra = tc[(12 + t) * E + e];
+        area_n += ra;
+        const float *K = tc + (long long)t * 6 * E + e;
+        rhs += tc[(16 + t) * E + e] - tc[(14 + t) * E + e] * (D0 * K[kidx(v0, vs) * E] + D1 * K[kidx(v1, vs) * E] +
+                                                           D2 * K[kidx(v2, vs) * E]);
+    };
+    if (j != 0 && i != 0)
+        tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, dT(Nd(j - 1, i), true), 1, dT(Nd(j, i - 1), true), 2, 0.0f);
+    if (j != 0 && i != nx - 1) {
+        long long e = gf_elem(d, j - 1, i);
+        tri(e, 0, 1, 0, dT(Nd(j - 1, i), true), 1, 0.0f, 2, dT(Nd(j - 1, i + 1), false));
+        tri(e, 1, 1, 0, dT(Nd(j - 1, i + 1), false), 1, 0.0f, 2, dT(Nd(j, i + 1), false));
     }
-    __syncthreads();
-    for (int j = t; j < nz; j += blockDim.x) {
-        A.temp[gf_node(d, j, 0)] = A.temp[gf_node(d, j, 1)];
-        A.temp[gf_node(d, j, nx - 1)] = A.temp[gf_node(d, j, nx - 2)];
+    if (j != nz - 1 && i != 0) {
+        long long e = gf_elem(d, j, i - 1);
+        tri(e, 0, 2, 0, dT(Nd(j, i - 1), true), 1, dT(Nd(j + 1, i - 1), true), 2, 0.0f);
+        tri(e, 1, 0, 0, 0.0f, 1, dT(Nd(j + 1, i - 1), true), 2, dT(Nd(j + 1, i), false));
     }
+    if (j != nz - 1 && i != nx - 1)
+        tri(gf_elem(d, j, i), 0, 0, 0, 0.0f, 1, dT(Nd(j + 1, i), false), 2, dT(Nd(j, i + 1), false));
+    float inc = rhs * float(C->dt) / area_n;
+    if (!final_sweep)
+        d0[n] = inc;
+    else
+        tnew[n] = Ts + (double)inc;
+}
+
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
+                                                              const double *__restrict__ tnew) {
+    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    int j, i;
+    node_ji(d, n, j, i);
+    double t = therm_bc_value(*Pp, A, d, tnew, j, i);
+    A.temp0[n] = A.temp[n];
+    A.temp[n] = t;
 }
 
 // ======================================================================
@@ -585,7 +788,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__res
     elem_ji(d, e, j, i);
     int wrote = 0;
     double fval = 0.0;
-    A.e_dens[e] = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
+    double dens = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
+    A.e_dens[e] = dens;
+    // each triangle's share c1d12/area*dens (rmasses.f90:271-287), computed
+    // once here with the reference's operations and gathered per node
+    const R *area = (const R *)A.area;
+    const double c1d12 = 1.0 / 12.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 / (double)area[gf_ek(d, e, k)] * dens;
     if (wrote) {
         // serial position of this element in the coloured sweep
         int ib = i & 1, jb = j & 1;
@@ -627,16 +837,18 @@ __global__ void k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restric
 // 3:(j,i+1) 4:(j+1,i+1)), the triangles that contain it, in order.
 __device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3}, {1, 2, 3}};
 
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_node_rmass(DevArrays A, GfDims d) {
+// Node gather of per-triangle shares tri[k*E + e] in the reference's order:
+// adjacent elements by colour ((ie&1)*2 + (je&1), rmasses.f90:257-262,
+// dt_mass.f90:74-81), then each element's triangles containing the node in
+// the order A, B, C, D.  Every element in a node's neighbourhood has a
+// different colour, so this is the serial order of the coloured scatter.
+__global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const double *__restrict__ tri,
+                                                                double *__restrict__ out, GfDims d) {
     long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
-    const R *area = (const R *)A.area;
-    const double c1d12 = 1.0 / 12.0;
     double acc = 0.0;
-    // adjacent elements in colour order: colour index = (ie&1)*2 + (je&1)
     int ord[4];
     // the node is vertex 4 of quad (j-1,i-1), 2 of (j-1,i), 3 of (j,i-1), 1 of (j,i)
     int je_[4] = {j - 1, j - 1, j, j}, ie_[4] = {i - 1, i, i - 1, i}, lv[4] = {3, 1, 2, 0};
@@ -650,11 +862,10 @@ __global__ void __launch_bounds__(GF_THREADS) k_node_rmass(DevArrays A, GfDims d
             int je = je_[q], ie = ie_[q];
             if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
             long long e = gf_elem(d, je, ie);
-            double dens = A.e_dens[e];
 #pragma unroll
-            for (int t = 0; t < 3; ++t) acc = acc + c1d12 / (double)area[gf_ek(d, e, c_vtx_tris[lv[q]][t])] * dens;
+            for (int t = 0; t < 3; ++t) acc = acc + tri[c_vtx_tris[lv[q]][t] * d.E + e];
         }
-    A.rmass[n] = acc;
+    out[n] = acc;
 }
 
 // ======================================================================
@@ -747,48 +958,27 @@ __global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restr
     C->dt = fmin(fmin(dt_elastic, dt_maxwell), dtmax_therm);
 }
 
-// amass node gather (dt_mass.f90:74-154), colour order as in k_node_rmass
+// inertial mass share of each triangle c1d12*rho_inert/area
+// (dt_mass.f90:83-120), one element per thread
 template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_node_amass(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                           DevArrays A, GfDims d) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= d.N) return;
+__global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                         DevArrays A, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
     const DevParams &P = *Pp;
-    int j, i;
-    node_ji(d, n, j, i);
-    if (P.idt_scale == 0) {
-        A.amass[n] = A.rmass[n];
-        return;
-    }
     const R *area = (const R *)A.area;
     const double c1d12 = 1.0 / 12.0;
     double dlmin = C->dlmin, frac = C->frac, dt_elastic = C->dt_elastic, vel_max = C->vel_max;
+    int iph = A.iphase[e] - 1;
+    double pwave = P.rl[iph] + 0.6666 * P.rm[iph];
     double vel_sound = dlmin * frac / dt_elastic;
-    double acc = 0.0;
-    // the node is vertex 4 of quad (j-1,i-1), 2 of (j-1,i), 3 of (j,i-1), 1 of (j,i)
-    int je_[4] = {j - 1, j - 1, j, j}, ie_[4] = {i - 1, i, i - 1, i}, lv[4] = {3, 1, 2, 0};
-    int ord[4];
+    double rho_inert = pwave / (vel_sound * vel_sound);
+    if (P.i_rey == 1 && vel_max > 0.0) {
+        double rho_inert2 = (P.xReyn * P.v_min) / (vel_max * fabs(P.rzbo));
+        if (rho_inert > rho_inert2) rho_inert = rho_inert2;
+    }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) ord[q] = ((ie_[q] & 1) << 1) | (je_[q] & 1);
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            if (ord[q] != c) continue;
-            int je = je_[q], ie = ie_[q];
-            if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
-            long long e = gf_elem(d, je, ie);
-            int iph = A.iphase[e] - 1;
-            double pwave = P.rl[iph] + 0.6666 * P.rm[iph];
-            double rho_inert = pwave / (vel_sound * vel_sound);
-            if (P.i_rey == 1 && vel_max > 0.0) {
-                double rho_inert2 = (P.xReyn * P.v_min) / (vel_max * fabs(P.rzbo));
-                if (rho_inert > rho_inert2) rho_inert = rho_inert2;
-            }
-#pragma unroll
-            for (int t = 0; t < 3; ++t) acc = acc + c1d12 * rho_inert / (double)area[gf_ek(d, e, c_vtx_tris[lv[q]][t])];
-        }
-    A.amass[n] = acc;
+    for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
 }
 
 __global__ void k_dt_reset(DevClock *C) {
@@ -806,7 +996,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__res
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
-    ((R *)A.visn)[e] = R(eff_visc<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
+    ((R *)A.visn)[e] = R(visc_of<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
 }
 
 // ======================================================================
@@ -1013,24 +1203,27 @@ template <class R> __global__ void k_convert_back(const R *__restrict__ src, dou
 
 template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps) {
     using namespace gfk;
+    if (sizeof(R) == sizeof(float)) {
+        float *tc = (float *)g.A.t_coef;
+        float *d0 = (float *)g.A.t_delta0;
+        GF_LAUNCH(k_therm_prep32, g.d.E, g.P, g.A, g.d, tc);
+        GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 0);
+        GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 1);
+        GF_LAUNCH(k_therm_apply32, g.d.N, g.P, g.A, g.d, g.A.t_delta1);
+        return;
+    }
     int kmax = sweeps > 0 ? (sweeps < GF_THERM_KMAX ? sweeps : GF_THERM_KMAX) : GF_THERM_KMAX;
-    k_therm_reset<<<1, 1, 0, g.s>>>(g.C);
-    ++*g.launches;
-    GF_LAUNCH(k_therm_prep<R>, g.d.E, g.P, g.A, g.d, g.A.t_coef);
+    GF_LAUNCH(k_therm_prep<R>, g.d.E, g.P, g.C, g.A, g.d, g.A.t_coef);
     double *bufs[2] = {g.A.t_delta0, g.A.t_delta1};
     for (int k = 0; k < kmax; ++k) {
         const double *up = k == 0 ? g.A.temp : bufs[(k - 1) & 1];
         GF_LAUNCH(k_therm_sweep, g.d.N, g.C, g.A, g.d, g.A.t_coef, up, bufs[k & 1], k);
     }
-    GF_LAUNCH(k_therm_apply, g.d.N, g.C, g.A, g.d, bufs[0], bufs[1], kmax);
-    k_therm_bc<<<1, 1024, 0, g.s>>>(g.P, g.A, g.d);
-    ++*g.launches;
+    GF_LAUNCH(k_therm_apply, g.d.N, g.P, g.C, g.A, g.d, bufs[0], bufs[1], kmax);
 }
 
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {
     using namespace gfk;
-    k_rheol_clock<<<1, 1, 0, g.s>>>(g.C, 0);
-    ++*g.launches;
     GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
     if (avg_mode > 0) {
         GF_LAUNCH(k_rheol_avg<R>, g.d.E, g.C, g.A, g.d, avg_mode == 2 ? 1 : 0);
@@ -1049,7 +1242,7 @@ template <class R> void GfKernels<R>::node(const GfLaunch &g) {
 template <class R> void GfKernels<R>::move(const GfLaunch &g) {
     using namespace gfk;
     GF_LAUNCH(k_move_cord, 2 * g.d.N, g.C, g.A, g.d);
-    GF_LAUNCH(k_move_elem<R>, g.d.E, g.C, g.A, g.d);
+    GF_LAUNCH(k_move_elem<R>, g.d.E, g.C, g.A, g.d, g.advance_time);
 }
 
 template <class R> void GfKernels<R>::rmasses(const GfLaunch &g) {
@@ -1057,7 +1250,7 @@ template <class R> void GfKernels<R>::rmasses(const GfLaunch &g) {
     GF_LAUNCH(k_elem_dens<R>, g.d.E, g.P, g.C, g.A, g.d);
     k_frac_fix<R><<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d);
     ++*g.launches;
-    GF_LAUNCH(k_node_rmass<R>, g.d.N, g.A, g.d);
+    GF_LAUNCH(k_node_gather_tri, g.d.N, g.A.e_tri, g.A.rmass, g.d);
 }
 
 template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
@@ -1068,7 +1261,12 @@ template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
     GF_LAUNCH(k_dt_reduce<R>, n, g.P, g.C, g.A, g.d);
     k_dt_scalars<<<1, 1, 0, g.s>>>(g.P, g.C);
     ++*g.launches;
-    GF_LAUNCH(k_node_amass<R>, g.d.N, g.P, g.C, g.A, g.d);
+    if (g.idt_scale == 0) {
+        cudaMemcpyAsync(g.A.amass, g.A.rmass, sizeof(double) * g.d.N, cudaMemcpyDeviceToDevice, g.s);
+    } else {
+        GF_LAUNCH(k_elem_am3<R>, g.d.E, g.P, g.C, g.A, g.d);
+        GF_LAUNCH(k_node_gather_tri, g.d.N, g.A.e_tri, g.A.amass, g.d);
+    }
 }
 
 template <class R> void GfKernels<R>::init_visc(const GfLaunch &g) {
@@ -1094,4 +1292,50 @@ void GfKernels<R>::convert_in(const GfLaunch &g, unsigned mask, const double *sr
         GF_LAUNCH(k_convert<R>, n, src, (R *)dst, n);
     else
         GF_LAUNCH(k_convert_back<R>, n, (const R *)dst, (double *)src, n);
+}
+
+namespace {
+namespace gfk {
+// total stress -> (p_ref, total + p_ref on the normal components)
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restrict__ tot, R *__restrict__ st,
+                                                          double *__restrict__ p_ref, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s += tot[gf_s(d, e, 0, k)] + tot[gf_s(d, e, 1, k)] + tot[gf_s(d, e, 3, k)];
+    double p = -s / 12.0;
+    p_ref[e] = p;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = R(c == 2 ? tot[gf_s(d, e, c, k)] : tot[gf_s(d, e, c, k)] + p);
+}
+
+template <class R>
+__global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref,
+                                                           double *__restrict__ tot, GfDims d) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    double p = p_ref[e];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            double v = (double)st[gf_s(d, e, c, k)];
+            tot[gf_s(d, e, c, k)] = c == 2 ? v : v - p;
+        }
+}
+} // namespace gfk
+} // namespace
+
+template <class R> void GfKernels<R>::stress_in(const GfLaunch &g, const double *src) {
+    using namespace gfk;
+    GF_LAUNCH(k_stress_in<R>, g.d.E, src, (R *)g.A.stress0, g.A.p_ref, g.d);
+}
+
+template <class R> void GfKernels<R>::stress_out(const GfLaunch &g, double *dst) {
+    using namespace gfk;
+    GF_LAUNCH(k_stress_out<R>, g.d.E, (const R *)g.A.stress0, g.A.p_ref, dst, g.d);
 }
