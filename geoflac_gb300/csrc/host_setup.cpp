@@ -799,3 +799,49 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
     }
     return GF_OK;
 }
+
+// Geotherm of node columns i_first..i_last (0-based) for age zone `zone`
+// (init_geotherm_profile, src/init_temp.f90:127-310), on host arrays in the
+// reference layout: used by the remesh event for material entering through a
+// side wall (sidewalltemp, src/init_temp.f90:313-353).
+int gf_host_geotherm_columns(gf_params *p, gf_layout *L, int zone, int i_first, int i_last) {
+    gf_clock c{};
+    S s{p, &c, L, GfDims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)}};
+    try {
+        for (int i = i_first; i <= i_last; ++i) geotherm(s, zone, i, p->age_1[zone], p->tp1[zone], p->tp2[zone]);
+    } catch (const Stop &st) {
+        return st.code;
+    }
+    return GF_OK;
+}
+
+// The zone pattern of mesh1 before scaling: x_k = x1 + t[k] * (x2 - x1) / all_ratio
+// (src/init_cord.f90:289-327), so a device can regrid with the host's exact values.
+void gf_host_mesh_template(int n, int nzon, const int *nelz, const double *sizez, double *t, double *all_ratio) {
+    double ar = 0.0;
+    for (int k = 0; k < nzon - 1; k += 2) {
+        ar = ar + nelz[k] * sizez[k];
+        double ratio = std::pow(sizez[k + 2] / sizez[k], 1.0 / (double)(nelz[k + 1] + 1));
+        for (int i = 1; i <= nelz[k + 1]; ++i) ar = ar + sizez[k] * ipow(ratio, i);
+    }
+    ar = ar + nelz[nzon - 1] * sizez[nzon - 1];
+    int nel = 0;
+    t[0] = 0.0;
+    for (int k = 0; k < nzon - 1; k += 2) {
+        for (int i = 0; i < nelz[k]; ++i) {
+            nel = nel + 1;
+            t[nel] = t[nel - 1] + sizez[k];
+        }
+        double ratio = std::pow(sizez[k + 2] / sizez[k], 1.0 / (double)(nelz[k + 1] + 1));
+        for (int i = 1; i <= nelz[k + 1]; ++i) {
+            nel = nel + 1;
+            t[nel] = t[nel - 1] + sizez[k] * ipow(ratio, i);
+        }
+    }
+    for (int k = 0; k < nelz[nzon - 1]; ++k) {
+        nel = nel + 1;
+        t[nel] = t[nel - 1] + sizez[nzon - 1];
+    }
+    *all_ratio = ar;
+    (void)n;
+}

@@ -1269,6 +1269,532 @@ double min_angle(St &s) {
     return anglemint;
 }
 
+// --------------------------------------------------------------------------
+// Remesh event (src/par.f90:94-110): bar2euler, remesh, lpeuler2bar,
+// marker2elem.
+
+double ipow(double x, int m) {
+    unsigned n = m < 0 ? (unsigned)(-m) : (unsigned)m;
+    double y = (n % 2) ? x : 1.0;
+    while (n >>= 1) {
+        x = x * x;
+        if (n % 2) y = y * x;
+    }
+    return m < 0 ? 1.0 / y : y;
+}
+
+// mesh1 (init_cord.f90:289-327)
+void mesh1(double x1, double x2, double *xmesh, int n, int nzon, const int *nelz, const double *sizez) {
+    double all_ratio = 0.0;
+    int nel = 0;
+    xmesh[0] = 0.0;
+    for (int k = 0; k < nzon - 1; k += 2) {
+        all_ratio = all_ratio + nelz[k] * sizez[k];
+        for (int i = 0; i < nelz[k]; ++i) {
+            nel = nel + 1;
+            xmesh[nel] = xmesh[nel - 1] + sizez[k];
+        }
+        double ratio = std::pow(sizez[k + 2] / sizez[k], 1.0 / (double)(nelz[k + 1] + 1));
+        for (int i = 1; i <= nelz[k + 1]; ++i) {
+            nel = nel + 1;
+            xmesh[nel] = xmesh[nel - 1] + sizez[k] * ipow(ratio, i);
+            all_ratio = all_ratio + sizez[k] * ipow(ratio, i);
+        }
+    }
+    for (int k = 0; k < nelz[nzon - 1]; ++k) {
+        nel = nel + 1;
+        xmesh[nel] = xmesh[nel - 1] + sizez[nzon - 1];
+    }
+    all_ratio = all_ratio + nelz[nzon - 1] * sizez[nzon - 1];
+    double magnification = (x2 - x1) / all_ratio;
+    for (int k = 0; k < n; ++k) xmesh[k] = x1 + xmesh[k] * magnification;
+}
+
+// init_geotherm_profile (init_temp.f90:127-310) for node column i (0-based)
+void geotherm_column(St &s, int n, int i, double age_1n, double tp1n, double tp2n) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nz = p.nz, nx = p.nx;
+    const double pi = 3.14159265358979323846;
+    double t_top = p.t_top, t_bot = p.t_bot;
+    auto T = [&](int j) -> double & { return L.temp[gf_node(s.d, j, i)]; };
+    auto Y = [&](int j) { return s.cord(j, i, 1); };
+    int ic = p.ictherm[n];
+    if (ic == 1) {
+        for (int j = 0; j < nz; ++j) {
+            double f = (Y(0) - Y(j)) / std::sqrt(4 * 1e-6 * age_1n * 1e6 * GF_SEC_YEAR);
+            T(j) = t_top + (t_bot - t_top) * std::erf(f);
+        }
+    } else if (ic == 2 || ic == 12) {
+        double yL0 = tp1n, age_init = age_1n * GF_SEC_YEAR * 1e6, tau_d = yL0 * yL0 * 1e6 / (pi * pi * 1e-6);
+        double cond = 3.3, dens_c = 2700.0, ymoho = tp2n, tm = 0, qm = 0;
+        if (ic == 12) {
+            double rr = ymoho / (yL0 - ymoho);
+            tm = (t_top + rr * t_bot + dens_c * p.hs * p.hr * p.hr * 1e6 / cond * (1.0 - std::exp(-ymoho / p.hr))) / (1 + rr);
+            qm = cond * (t_bot - tm) / (yL0 - ymoho);
+        }
+        for (int j = 0; j < nz; ++j) {
+            double y = (Y(0) - Y(j)) * 1e-3;
+            double tss;
+            if (ic == 2)
+                tss = t_top + (t_bot - t_top) * y / yL0;
+            else if (y <= ymoho)
+                tss = t_top + qm / cond * y + (dens_c * p.hs * p.hr * p.hr * 1e6 / cond) * (1.0 - std::exp(-y / p.hr));
+            else if (y <= yL0)
+                tss = tm + qm / cond * (y - ymoho);
+            else
+                tss = t_bot;
+            double tt = 0.0;
+            for (int k = 1; k <= 100; ++k) tt = tt + 1.0 / k * std::exp(-k * k * age_init / tau_d) * std::sin(pi * k * y / yL0);
+            T(j) = tss + 2.0 / pi * (t_bot - t_top) * tt;
+            if (T(j) > t_bot || y > yL0) T(j) = t_bot;
+        }
+    } else if (ic == 21) {
+        for (int j = 0; j < nz; ++j) {
+            double y = (Y(0) - Y(j)) * 1e-3;
+            T(j) = y * (t_bot - t_top) / age_1n;
+            if (T(j) > t_bot) T(j) = t_bot;
+        }
+    } else if (ic == 22) {
+        for (int j = 0; j < nz; ++j) {
+            double y = (Y(0) - Y(j)) * 1e-3;
+            if (y <= tp1n)
+                T(j) = t_top + (age_1n - t_top) * y / tp1n;
+            else
+                T(j) = age_1n + (t_bot - age_1n) * (y - tp1n) / (tp2n - tp1n);
+            if (T(j) > t_bot) T(j) = t_bot;
+        }
+    } else if (ic == 13) {
+        double cond_c = 2.3, cond_m = 3.3, Fpart = 0.74, alc = 0.4e-6, am = 0.02e-6;
+        double auc = (1.0 - Fpart) * age_1n * 1.0e-3 / (tp1n * 1000.0);
+        double Q = age_1n * 1.0e-3;
+        T(0) = t_top;
+        int kl = 0;
+        for (int j = 0; j < nz - 1; ++j) {
+            double y = (Y(0) - Y(j)) * 1.0e-3, xdz = std::fabs(Y(j + 1) - Y(j));
+            double *src = (i < nx - 1) ? &L.source[s.e(j, i)] : nullptr;
+            double Qn = Q;
+            if (y < tp1n) {
+                T(j + 1) = T(j) + (Q / cond_c) * xdz - (auc) / (2.0 * cond_c) * (xdz * xdz);
+                Qn = Q - auc * xdz;
+                if (src) *src = auc * 1.0e-3;
+            }
+            if (y >= tp1n && y < (tp2n + tp1n)) {
+                T(j + 1) = T(j) + (Q / cond_c) * xdz - (alc) / (2.0 * cond_c) * (xdz * xdz);
+                Qn = Q - alc * xdz;
+                if (src) *src = alc * 1.0e-3;
+            }
+            if (y >= (tp2n + tp1n) && kl == 0) {
+                T(j + 1) = T(j) + (Q / cond_m) * xdz - (am) / (2.0 * cond_m) * (xdz * xdz);
+                Qn = Q - am * xdz;
+                if (src) *src = am * 1.0e-3;
+                if (T(j + 1) >= t_bot) kl = 1;
+            }
+            if (kl == 1) {
+                T(j + 1) = t_bot;
+                if (src) *src = 0.0;
+            }
+            Q = Qn;
+        }
+    } else {
+        throw Stop{1};
+    }
+}
+
+// marker2xy (bar2euler.f90:235-279); bar2euler writes x,y into mark_a1/a2
+void bar2euler(St &s) {
+    gf_layout &L = *s.L;
+    int nz = s.p->nz;
+    for (int m = 0; m < s.c->nmarkers; ++m) {
+        if (L.mark_dead[m] == 0) continue;
+        int n = L.mark_ntriag[m];
+        int k = (n - 1) % 2 + 1;
+        int jj = ((n - k) / 2) % (nz - 1);
+        int ii = (n - k) / 2 / (nz - 1);
+        double ba1 = L.mark_a1[m], ba2 = L.mark_a2[m];
+        double ba3 = 1.0 - ba1 - ba2;
+        int i1, i2, i3, j1, j2, j3;
+        if (k == 1) {
+            i1 = ii; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj;
+        } else {
+            i1 = ii + 1; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj + 1;
+        }
+        double x = s.cord(j1, i1, 0) * ba1 + s.cord(j2, i2, 0) * ba2 + s.cord(j3, i3, 0) * ba3;
+        double y = s.cord(j1, i1, 1) * ba1 + s.cord(j2, i2, 1) * ba2 + s.cord(j3, i3, 1) * ba3;
+        if (L.dhacc_correction) {
+            if (j1 == 0) y = y - L.dhacc_correction[i1] * ba1;
+            if (j2 == 0) y = y - L.dhacc_correction[i2] * ba2;
+            if (j3 == 0) y = y - L.dhacc_correction[i3] * ba3;
+        }
+        L.mark_a1[m] = x;
+        L.mark_a2[m] = y;
+    }
+}
+
+// euler2bar (euler2bar.f90:1-98): the element itself, then rings of 2, 6, 12
+int euler2bar(St &s, double x, double y, double &b1, double &b2, int &ntr, int &ii, int &jj) {
+    int nx = s.p->nx, nz = s.p->nz;
+    if (check_inside(s, x, y, b1, b2, ntr, ii, jj)) return 1;
+    const int rings[3] = {2, 6, 12};
+    for (int r = 0; r < 3; ++r) {
+        int n = rings[r], prev = r == 0 ? 0 : rings[r - 1];
+        for (int j = std::max(0, jj - n); j <= std::min(nz - 2, jj + n); ++j)
+            for (int i = std::max(0, ii - n); i <= std::min(nx - 2, ii + n); ++i) {
+                if (r == 0) {
+                    if (i == ii && j == jj) continue;
+                } else if (std::abs(i - ii) <= prev && std::abs(j - jj) <= prev) {
+                    continue;
+                }
+                if (check_inside(s, x, y, b1, b2, ntr, i, j)) {
+                    ii = i;
+                    jj = j;
+                    return 1;
+                }
+            }
+    }
+    return 0;
+}
+
+// lpeuler2bar (lpeuler2bar.f90:343-404), serial marker order
+void lpeuler2bar(St &s) {
+    gf_layout &L = *s.L;
+    int nz = s.p->nz;
+    std::memset(L.mark_id_elem, 0, sizeof(int) * (size_t)s.d.E * GF_MAX_MARKERS_PER_ELEM);
+    std::memset(L.nmark_elem, 0, sizeof(int) * (size_t)s.d.E);
+    for (int m = 0; m < s.c->nmarkers; ++m) {
+        if (L.mark_dead[m] == 0) continue;
+        int nt = L.mark_ntriag[m];
+        int k = (nt - 1) % 2 + 1;
+        int j = ((nt - k) / 2) % (nz - 1);
+        int i = (nt - k) / 2 / (nz - 1);
+        double xx = L.mark_a1[m], yy = L.mark_a2[m], b1, b2;
+        int ntr;
+        if (!euler2bar(s, xx, yy, b1, b2, ntr, i, j)) {
+            L.mark_dead[m] = 0;
+            continue;
+        }
+        L.mark_a1[m] = b1;
+        L.mark_a2[m] = b2;
+        L.mark_ntriag[m] = ntr;
+        long long e = s.e(j, i);
+        if (L.nmark_elem[e] == GF_MAX_MARKERS_PER_ELEM) {
+            L.mark_dead[m] = 0;
+            continue;
+        }
+        L.nmark_elem[e] += 1;
+        L.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + L.nmark_elem[e] - 1] = m + 1;
+    }
+}
+
+// rem_cord (rem_cord.f90:140-220)
+void rem_cord(St &s, const std::vector<double> &cordo) {
+    const gf_params &p = *s.p;
+    int nx = p.nx, nz = p.nz;
+    std::vector<double> st(std::max(nx, nz) + 2);
+    auto CO = [&](int j, int i, int k) { return cordo[gf_n2(s.d, j, i, k)]; };
+    for (int j = 0; j < nz; ++j) {
+        double xl = 0, xr = 0;
+        if (p.mode_rem == 1) {
+            xl = s.cord(j, 0, 0);
+            xr = s.cord(j, nx - 1, 0);
+        } else if (p.mode_rem == 11 || p.mode_rem == 3) {
+            xl = p.x0;
+            xr = p.x0 + p.rxbo;
+        } else if (p.mode_rem == 4) {
+            xl = s.cord(0, 0, 0);
+            xr = s.cord(0, nx - 1, 0);
+        }
+        mesh1(xl, xr, st.data(), nx, p.nzonx, p.nelz_x, p.sizez_x);
+        for (int i = 0; i < nx; ++i) s.cordr(j, i, 0) = st[i];
+    }
+    bool is_flex = false;
+    for (int b = 0; b < p.nofbc; ++b)
+        if (p.nbc[b] == 200 && p.nofside[b] == 2) is_flex = true;
+    for (int i = 0; i < nx; ++i) {
+        for (int j = 0; j < nz; j += nz - 1) {
+            double xx = s.cord(j, i, 0);
+            if (xx <= CO(j, 0, 0))
+                s.cordr(j, i, 1) = CO(j, 0, 1);
+            else if (xx >= CO(j, nx - 1, 0))
+                s.cordr(j, i, 1) = CO(j, nx - 1, 1);
+            else
+                for (int ii = 0; ii < nx - 1; ++ii) {
+                    double xl = CO(j, ii, 0), xr = CO(j, ii + 1, 0);
+                    if (xx >= xl && xx <= xr) {
+                        double zl = CO(j, ii, 1), zr = CO(j, ii + 1, 1);
+                        s.cordr(j, i, 1) = zl + (xx - xl) * (zr - zl) / (xr - xl);
+                        break;
+                    }
+                }
+            if (nz == 1) break;
+        }
+        if (!is_flex && (p.mode_rem == 3 || p.mode_rem == 1)) s.cordr(nz - 1, i, 1) = p.z0 + p.rzbo;
+        mesh1(s.cord(0, i, 1), s.cord(nz - 1, i, 1), st.data(), nz, p.nzony, p.nelz_y, p.sizez_y);
+        for (int j = 0; j < nz; ++j) s.cordr(j, i, 1) = st[j];
+    }
+}
+
+// rem_trpars / rem_barcord / rem_interpolate (remesh.f90:266-491) on a
+// (nzt x nxt) point grid with old points `cold` and new points `cnew`
+struct Interp {
+    int nzt, nxt;
+    std::vector<int> numtr;
+    std::vector<double> bc; // 3 per point
+};
+
+Interp rem_barcord(const std::vector<double> &cold, const std::vector<double> &cnew, int nzt, int nxt) {
+    auto OX = [&](int j, int i) { return cold[(size_t)2 * ((size_t)i * nzt + j)]; };
+    auto OY = [&](int j, int i) { return cold[(size_t)2 * ((size_t)i * nzt + j) + 1]; };
+    // rem_trpars
+    size_t ntri = (size_t)2 * (nzt - 1) * (nxt - 1);
+    std::vector<double> pt(ntri * 6);
+    for (int i = 0; i < nxt - 1; ++i)
+        for (int j = 0; j < nzt - 1; ++j)
+            for (int k = 1; k <= 2; ++k) {
+                double x1, x2, x3, y1, y2, y3;
+                if (k == 1) {
+                    x1 = OX(j, i); x2 = OX(j + 1, i); x3 = OX(j, i + 1);
+                    y1 = OY(j, i); y2 = OY(j + 1, i); y3 = OY(j, i + 1);
+                } else {
+                    x1 = OX(j, i + 1); x2 = OX(j + 1, i); x3 = OX(j + 1, i + 1);
+                    y1 = OY(j, i + 1); y2 = OY(j + 1, i); y3 = OY(j + 1, i + 1);
+                }
+                double det = ((x2 * y3 - y2 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y2 - y1 * x2);
+                size_t n = (size_t)2 * ((size_t)(nzt - 1) * i + j) + (k - 1);
+                double *q = &pt[n * 6];
+                q[0] = (x2 * y3 - y2 * x3) / det;
+                q[1] = (y2 - y3) / det;
+                q[2] = (x3 - x2) / det;
+                q[3] = (x3 * y1 - y3 * x1) / det;
+                q[4] = (y3 - y1) / det;
+                q[5] = (x1 - x3) / det;
+            }
+    Interp r{nzt, nxt, std::vector<int>((size_t)nzt * nxt), std::vector<double>((size_t)3 * nzt * nxt)};
+    const double perr = 1e-4;
+    const int mm = 4;
+    for (int i = 0; i < nxt; ++i)
+        for (int j = 0; j < nzt; ++j) {
+            size_t pidx = (size_t)i * nzt + j;
+            double xx = cnew[2 * pidx], yy = cnew[2 * pidx + 1];
+            double amodmin = 1e10;
+            int nmin = 0, found = 0;
+            for (int io = std::max(0, i - mm); io <= std::min(nxt - 2, i + mm) && !found; ++io)
+                for (int jo = std::max(0, j - mm); jo <= std::min(nzt - 2, j + mm) && !found; ++jo)
+                    for (int k = 1; k <= 2; ++k) {
+                        int n1 = 2 * ((nzt - 1) * io + jo) + k; // 1-based triangle number
+                        const double *q = &pt[(size_t)(n1 - 1) * 6];
+                        double a1 = q[0] + xx * q[1] + yy * q[2];
+                        double a2 = q[3] + xx * q[4] + yy * q[5];
+                        double a3 = 1.0 - a1 - a2;
+                        double amod = a1 * a1 + a2 * a2 + a3 * a3;
+                        if (amod < amodmin) {
+                            amodmin = amod;
+                            nmin = n1;
+                        }
+                        if (a1 <= -perr || a1 >= (1.0 + perr)) continue;
+                        if (a2 <= -perr || a2 >= (1.0 + perr)) continue;
+                        if (a3 <= -perr || a3 >= (1.0 + perr)) continue;
+                        r.numtr[pidx] = n1;
+                        r.bc[3 * pidx] = a1;
+                        r.bc[3 * pidx + 1] = a2;
+                        r.bc[3 * pidx + 2] = a3;
+                        found = 1;
+                        break;
+                    }
+            if (!found) {
+                r.numtr[pidx] = nmin;
+                int numqu = (nmin + 1) / 2;
+                int io = (numqu - 1) / (nzt - 1), jo = numqu - io * (nzt - 1) - 1; // 0-based
+                double d1, d2, d3;
+                auto dist = [&](int jj, int ii) {
+                    double dx = xx - OX(jj, ii), dy = yy - OY(jj, ii);
+                    return std::sqrt(dx * dx + dy * dy);
+                };
+                if (nmin % 2 == 0) {
+                    d1 = dist(jo, io + 1); d2 = dist(jo + 1, io); d3 = dist(jo + 1, io + 1);
+                } else {
+                    d1 = dist(jo, io); d2 = dist(jo + 1, io); d3 = dist(jo, io + 1);
+                }
+                double *b = &r.bc[3 * pidx];
+                auto w2 = [&](double da, double db, double &wa, double &wb) {
+                    wa = 1.0 / da / (1.0 / da + 1.0 / db);
+                    wb = 1.0 / db / (1.0 / da + 1.0 / db);
+                };
+                if (d1 > d2) {
+                    if (d2 > d3) {
+                        b[0] = 0.0; w2(d2, d3, b[1], b[2]);
+                    } else if (d1 > d3) {
+                        b[0] = 0.0; w2(d2, d3, b[1], b[2]);
+                    } else {
+                        w2(d1, d2, b[0], b[1]); b[2] = 0.0;
+                    }
+                } else {
+                    if (d3 > d1) {
+                        if (d2 > d3) {
+                            w2(d1, d3, b[0], b[2]); b[1] = 0.0;
+                        } else {
+                            w2(d1, d2, b[0], b[1]); b[2] = 0.0;
+                        }
+                    } else {
+                        w2(d1, d3, b[0], b[2]); b[1] = 0.0;
+                    }
+                }
+            }
+        }
+    return r;
+}
+
+// rem_interpolate on a plane arr (nzt x nxt, j fastest)
+void rem_interpolate(const Interp &r, double *arr) {
+    int nzt = r.nzt, nxt = r.nxt;
+    std::vector<double> dummy(arr, arr + (size_t)nzt * nxt);
+    auto Dm = [&](int j, int i) { return dummy[(size_t)i * nzt + j]; };
+    for (int i = 0; i < nxt; ++i)
+        for (int j = 0; j < nzt; ++j) {
+            size_t pidx = (size_t)i * nzt + j;
+            int n = r.numtr[pidx];
+            int numq = (n + 1) / 2;
+            int io = (numq - 1) / (nzt - 1), jo = numq - io * (nzt - 1) - 1;
+            double f1, f2, f3;
+            if (n % 2 == 0) {
+                f1 = Dm(jo, io + 1); f2 = Dm(jo + 1, io); f3 = Dm(jo + 1, io + 1);
+            } else {
+                f1 = Dm(jo, io); f2 = Dm(jo + 1, io); f3 = Dm(jo, io + 1);
+            }
+            const double *b = &r.bc[3 * pidx];
+            arr[pidx] = b[0] * f1 + b[1] * f2 + b[2] * f3;
+        }
+}
+
+void newphase2marker(St &s, int j1, int j2, int i1, int i2, int iph) {
+    gf_layout &L = *s.L;
+    for (int i = i1; i <= i2; ++i)
+        for (int j = j1; j <= j2; ++j) {
+            long long e = s.e(j - 1, i - 1);
+            for (int n = 0; n < L.nmark_elem[e]; ++n) L.mark_phase[L.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + n] - 1] = (int8_t)iph;
+            L.iphase[e] = iph;
+            for (int k = 0; k < s.p->nphase; ++k) L.phase_ratio[gf_pr(s.d, e, k)] = 0.0;
+            L.phase_ratio[gf_pr(s.d, e, iph - 1)] = 1.0;
+        }
+}
+
+void init_areas(St &s) {
+    int nx = s.p->nx, nz = s.p->nz;
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            double x1 = s.cord(j, i, 0), y1 = s.cord(j, i, 1), x2 = s.cord(j + 1, i, 0), y2 = s.cord(j + 1, i, 1);
+            double x3 = s.cord(j, i + 1, 0), y3 = s.cord(j, i + 1, 1), x4 = s.cord(j + 1, i + 1, 0), y4 = s.cord(j + 1, i + 1, 1);
+            long long e = s.e(j, i);
+            double *a = s.L->area;
+            a[gf_ek(s.d, e, 0)] = 1.0 / (((x2 * y3 - y2 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y2 - y1 * x2));
+            a[gf_ek(s.d, e, 1)] = 1.0 / (((x2 * y4 - y2 * x4) - (x3 * y4 - y3 * x4)) + (x3 * y2 - y3 * x2));
+            a[gf_ek(s.d, e, 2)] = 1.0 / (((x2 * y4 - y2 * x4) - (x1 * y4 - y1 * x4)) + (x1 * y2 - y1 * x2));
+            a[gf_ek(s.d, e, 3)] = 1.0 / (((x4 * y3 - y4 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y4 - y1 * x4));
+            for (int k = 0; k < 4; ++k)
+                if (a[gf_ek(s.d, e, k)] < 0) throw Stop{41};
+        }
+}
+
+// remesh (remesh.f90:1-259) without the surface accumulators dhacc/extr_acc
+// and the magma fields, which belong to models this path does not run
+void remesh(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    size_t N = (size_t)s.d.N, E = (size_t)s.d.E;
+    std::vector<double> cordo(L.cord, L.cord + 2 * N);
+    rem_cord(s, cordo);
+    // element fields: barycentric interpolation between element centres
+    int nzt = nz - 1, nxt = nx - 1;
+    std::vector<double> cold(2 * E), cnew(2 * E);
+    auto CO = [&](int j, int i, int k) { return cordo[gf_n2(s.d, j, i, k)]; };
+    for (int i = 0; i < nxt; ++i)
+        for (int j = 0; j < nzt; ++j) {
+            size_t q = (size_t)i * nzt + j;
+            for (int k = 0; k < 2; ++k) {
+                cold[2 * q + k] = 0.25 * (CO(j, i, k) + CO(j + 1, i, k) + CO(j, i + 1, k) + CO(j + 1, i + 1, k));
+                cnew[2 * q + k] = 0.25 * (s.cord(j, i, k) + s.cord(j + 1, i, k) + s.cord(j, i + 1, k) + s.cord(j + 1, i + 1, k));
+            }
+        }
+    Interp r = rem_barcord(cold, cnew, nzt, nxt);
+    for (int k = 0; k < 4; ++k)
+        for (int c = 0; c < 4; ++c) rem_interpolate(r, L.stress0 + (size_t)(c + 4 * k) * E);
+    for (int k = 0; k < 3; ++k) rem_interpolate(r, L.strain + (size_t)k * E);
+    rem_interpolate(r, L.aps);
+    for (size_t e = 0; e < E; ++e)
+        if (L.aps[e] < 0.0) L.aps[e] = 0.0;
+    // material entering through the side walls (remesh.f90:129-194)
+    const int idist = 2;
+    int ju = 1, jl = 1;
+    if (p.incoming_left == 1) {
+        for (int j = 0; j < nz - 1; ++j)
+            for (int i = 0; i <= idist; ++i) L.aps[s.e(j, i)] = 0.0;
+        int n = 0, i = 1;
+        for (int m = 0; m < p.nph_layer[n] - 1; ++m) {
+            ju = jl;
+            for (int j = jl; j <= nz - 1; ++j)
+                if ((s.cord(0, i - 1, 1) - 0.5 * (s.cord(j - 1, i - 1, 1) + s.cord(j, i - 1, 1))) > p.hc[n][m] * 1e3) {
+                    jl = j;
+                    break;
+                }
+            newphase2marker(s, ju, jl - 1, i, i + idist, p.iph_col[n][m]);
+        }
+        newphase2marker(s, jl, nz - 1, i, i + idist, p.iph_col[n][p.nph_layer[n] - 1]);
+    }
+    if (p.incoming_right == 1) {
+        for (int j = 0; j < nz - 1; ++j)
+            for (int i = nx - 2 - idist; i <= nx - 2; ++i) L.aps[s.e(j, i)] = 0.0;
+        int n = p.nzone_age - 1, i = nx - 1;
+        for (int m = 0; m < p.nph_layer[n] - 1; ++m) {
+            ju = jl;
+            for (int j = jl; j <= nz - 1; ++j)
+                if ((s.cord(0, i, 1) - 0.5 * (s.cord(j - 1, i, 1) + s.cord(j, i, 1))) > p.hc[n][m] * 1e3) {
+                    jl = j;
+                    break;
+                }
+            newphase2marker(s, ju, jl - 1, i - idist, i, p.iph_col[n][m]);
+        }
+        newphase2marker(s, jl, nz - 1, i - idist, i, p.iph_col[n][p.nph_layer[n] - 1]);
+    }
+    rem_interpolate(r, L.source);
+    // node fields: barycentric interpolation on the old node mesh
+    std::vector<double> coldn(2 * N), cnewn(2 * N);
+    for (size_t q = 0; q < N; ++q)
+        for (int k = 0; k < 2; ++k) {
+            coldn[2 * q + k] = cordo[k * N + q];
+            cnewn[2 * q + k] = L.cord[k * N + q];
+        }
+    std::memcpy(L.temp0, L.temp, sizeof(double) * N);
+    Interp rn = rem_barcord(coldn, cnewn, nz, nx);
+    for (int k = 0; k < 2; ++k) rem_interpolate(rn, L.vel + (size_t)k * N);
+    rem_interpolate(rn, L.temp);
+    // side-wall geotherms for incoming material (sidewalltemp, init_temp.f90:313-353)
+    if (p.incoming_left == 1) {
+        for (int i = 0; i <= idist; ++i) geotherm_column(s, 0, i, p.age_1[0], p.tp1[0], p.tp2[0]);
+        for (int i = 0; i < idist; ++i)
+            for (int j = 0; j < nz - 1; ++j) L.source[s.e(j, i)] = L.source[s.e(j, idist)];
+    }
+    if (p.incoming_right == 1) {
+        int n = p.nzone_age - 1;
+        for (int i = nx - 1 - idist; i <= nx - 1; ++i) geotherm_column(s, n, i, p.age_1[n], p.tp1[n], p.tp2[n]);
+        for (int i = nx - 1 - idist; i < nx - 1; ++i)
+            for (int j = 0; j < nz - 1; ++j) L.source[s.e(j, i)] = L.source[s.e(j, nx - 2 - idist)];
+    }
+    if (p.ivis_present == 1) init_visc(s);
+    init_areas(s);
+    rmasses(s);
+    dt_mass(s);
+}
+
+void remesh_event(St &s) {
+    bar2euler(s);
+    remesh(s);
+    lpeuler2bar(s);
+    marker2elem(s);
+    if (s.L->dhacc_correction)
+        for (int i = 0; i < s.p->nx; ++i) s.L->dhacc_correction[i] = 0.0;
+}
+
 template <class F> int guard(F &&f) {
     try {
         f();
@@ -1300,6 +1826,10 @@ OR_ENTRY(rmasses, rmasses(s))
 OR_ENTRY(dt_mass, dt_mass(s))
 OR_ENTRY(init_visc, init_visc(s))
 OR_ENTRY(marker2elem, marker2elem(s))
+OR_ENTRY(bar2euler, bar2euler(s))
+OR_ENTRY(lpeuler2bar, lpeuler2bar(s))
+OR_ENTRY(remesh, remesh(s))
+OR_ENTRY(remesh_event, remesh_event(s))
 
 // rmasses, init_visc, dt_mass and the averaging reset of setflac.f90:71-81
 int or_finish_setflac(gf_params *p, gf_clock *c, gf_layout *L) {

@@ -30,7 +30,8 @@ def load():
     lib = C.CDLL(LIB_PATH)
     P, K, L = C.POINTER(GfParams), C.POINTER(GfClock), C.POINTER(GfLayout)
     for name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
-                 "init_visc", "marker2elem", "finish_setflac", "flac"):
+                 "init_visc", "marker2elem", "finish_setflac", "flac", "bar2euler", "lpeuler2bar", "remesh",
+                 "remesh_event"):
         f = getattr(lib, "or_" + name)
         f.restype = C.c_int
         f.argtypes = [P, K, L]
@@ -62,7 +63,8 @@ class Oracle:
 
     def __getattr__(self, name):
         if name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
-                    "init_visc", "marker2elem", "finish_setflac", "flac"):
+                    "init_visc", "marker2elem", "finish_setflac", "flac", "bar2euler", "lpeuler2bar", "remesh",
+                    "remesh_event"):
             return lambda: self._call(name)
         raise AttributeError(name)
 
