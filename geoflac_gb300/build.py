@@ -27,6 +27,7 @@ UNITS = [
     ("gf_fp64.cu", ["-fmad=false"]),
     ("gf_mixed.cu", ["-fmad=true"]),
     ("gf_capi.cu", ["-fmad=false"]),
+    ("gf_noalloc.cu", ["-fmad=false"]),
     ("host_inp.cpp", None),
     ("host_setup.cpp", None),
 ]

@@ -26,7 +26,7 @@ F_ALL = 0xFFFFFFFF
 
 ERR = {0: "ok", -1: "CUDA error", -2: "bad argument", -3: "cannot open file",
        -4: "malformed .inp file", -5: "unsupported", -6: "timeout", -7: "out of memory",
-       -8: "non-finite value"}
+       -8: "non-finite value", -9: "input larger than a fixed device scratch"}
 
 _d = C.c_double
 _i = C.c_int

@@ -672,6 +672,7 @@ const char *gf_strerror(int code) {
     case GF_ERR_TIMEOUT: return "device wait timed out";
     case GF_ERR_NOMEM: return "out of memory";
     case GF_ERR_NONFINITE: return "non-finite value";
+    case GF_ERR_LIMIT: return "input larger than the fixed device scratch (gf_min_angle_noalloc: 2,097,152 elements at most)";
     case 22: return "Maxwell: time step too large (reference stop 22)";
     case 40: return "negative area (reference stop 40)";
     case 41: return "negative area at start-up (reference stop 41)";

@@ -60,6 +60,7 @@ extern "C" {
 #define GF_ERR_TIMEOUT (-6)
 #define GF_ERR_NOMEM (-7)
 #define GF_ERR_NONFINITE (-8)
+#define GF_ERR_LIMIT (-9) /* input larger than a fixed device scratch array */
 
 /* Precision modes of a context. */
 #define GF_MODE_FP64 0  /* every field and every operation in FP64          */
@@ -295,6 +296,21 @@ int gf_status(gf_ctx *ctx);
 long long gf_launch_count(gf_ctx *ctx);
 /* Human-readable description of a status code. */
 const char *gf_strerror(int code);
+/* Smallest triangle angle (degrees) of the mesh held in the caller's device
+ * array d_cord (the reference's cord(nz,nx,2) layout: depth fastest, then x
+ * column, then component), the test of src/rem_test.f90:77-118, for callers
+ * that must not allocate device memory: code whose device arrays belong to
+ * an OpenACC data region or a caching allocator, where a cudaMalloc bypasses
+ * that runtime and cudaFree stalls the whole device.  Allocates nothing: its
+ * scratch is a fixed 65,792-byte array inside this library, so at most
+ * 2,097,152 elements ((nx-1)*(nz-1)); larger meshes return GF_ERR_LIMIT.
+ * The first call on each device looks up that array's address: make it
+ * before any stream capture begins.  All calls share the array, so calls
+ * must not overlap in time on one device (serialise them on one stream).
+ * Runs on `stream` (a cudaStream_t; NULL = default stream) and waits for it.
+ * No reference counterpart (itest_mesh works on the host's module arrays). */
+int gf_min_angle_noalloc(const double *d_cord, int nx, int nz, void *stream, double *min_angle);
+
 /* sizeof(gf_params), sizeof(gf_clock), sizeof(gf_layout) for which = 0, 1, 2:
  * lets a binding (ctypes, cgo, ISO_C_BINDING) check its struct mirrors.
  * No reference counterpart (the reference shares modules, not structs). */
