@@ -28,6 +28,7 @@ UNITS = [
     ("gf_mixed.cu", ["-fmad=true"]),
     ("gf_capi.cu", ["-fmad=false"]),
     ("gf_noalloc.cu", ["-fmad=false"]),
+    ("gf_remesh.cu", ["-fmad=false"]),
     ("host_inp.cpp", None),
     ("host_setup.cpp", None),
 ]

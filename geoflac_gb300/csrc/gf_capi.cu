@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -13,6 +14,7 @@
 
 #include "../../include/geoflac_gb300.h"
 #include "gf_ctx.h"
+#include "gf_internal.h"
 
 namespace {
 
@@ -35,6 +37,8 @@ struct gf_ctx {
     DevArrays A{};
     double *staging = nullptr; // FP64 staging for mixed-mode conversions
     double *d_angle = nullptr;
+    GfRemeshBufs rb{};         // remesh scratch
+    double ar_x = 0, ar_z = 0; // mesh1 zone-pattern totals
     // host mirrors of the host-controlled scalars
     int nloop = 0, nsrate = -1, nmarkers = 0, need_remeshing = 0;
     long long launches = 0;
@@ -303,6 +307,110 @@ void k_change_phase(gf_ctx *c) {
 }
 
 // The launch sequence of one `flac` call depends only on these flags.
+// mesh1 zone patterns of the x and z directions (init_cord.f90:289-327),
+// computed on the host exactly as the start-up mesh and kept on the device
+int mesh_templates(gf_ctx *c) {
+    const gf_params &p = c->p;
+    int nex = 0, nez = 0;
+    for (int k = 0; k < p.nzonx; ++k) nex += p.nelz_x[k];
+    for (int k = 0; k < p.nzony; ++k) nez += p.nelz_y[k];
+    std::vector<double> tx((size_t)std::max(nex + 1, p.nx)), tz((size_t)std::max(nez + 1, p.nz));
+    gf_host_mesh_template(p.nx, p.nzonx, p.nelz_x, p.sizez_x, tx.data(), &c->ar_x);
+    gf_host_mesh_template(p.nz, p.nzony, p.nelz_y, p.sizez_y, tz.data(), &c->ar_z);
+    GF_CK(cudaMemcpy(c->rb.tx, tx.data(), sizeof(double) * p.nx, cudaMemcpyHostToDevice));
+    GF_CK(cudaMemcpy(c->rb.tz, tz.data(), sizeof(double) * p.nz, cudaMemcpyHostToDevice));
+    return GF_OK;
+}
+
+GfRemeshArgs remesh_args(const gf_ctx *c) {
+    const gf_params &p = c->p;
+    GfRemeshArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.mode_rem = p.mode_rem;
+    for (int b = 0; b < p.nofbc; ++b)
+        if (p.nbc[b] == 200 && p.nofside[b] == 2) a.is_flex = 1;
+    a.has_dhacc = 1;
+    a.x0 = p.x0; a.z0 = p.z0; a.rxbo = p.rxbo; a.rzbo = p.rzbo;
+    a.ar_x = c->ar_x; a.ar_z = c->ar_z;
+    a.incoming_left = p.incoming_left;
+    a.incoming_right = p.incoming_right;
+    int zl = 0, zr = p.nzone_age > 0 ? p.nzone_age - 1 : 0;
+    a.nl_left = std::min(std::max(p.nph_layer[zl], 1), GF_MAXZONE_LAYER);
+    a.nl_right = std::min(std::max(p.nph_layer[zr], 1), GF_MAXZONE_LAYER);
+    for (int m = 0; m < GF_MAXZONE_LAYER; ++m) {
+        a.hc_left[m] = p.hc[zl][m]; a.iph_left[m] = p.iph_col[zl][m];
+        a.hc_right[m] = p.hc[zr][m]; a.iph_right[m] = p.iph_col[zr][m];
+    }
+    a.nloop = c->nloop;
+    a.nmarkers = c->nmarkers;
+    a.max_markers = (int)c->L.max_markers;
+    return a;
+}
+
+// sidewalltemp (init_temp.f90:313-353) for material entering through a
+// wall: the age zone's geotherm on the three node columns next to it and
+// the heat source of the column behind them, on the host
+int sidewall_temps(gf_ctx *c) {
+    const gf_params &p = c->p;
+    const GfDims &d = c->d;
+    std::vector<double> cord(2 * d.N), temp(d.N), source(d.E);
+    GF_CK(cudaStreamSynchronize(c->s));
+    GF_CK(cudaMemcpy(cord.data(), c->A.cord, sizeof(double) * 2 * d.N, cudaMemcpyDeviceToHost));
+    GF_CK(cudaMemcpy(temp.data(), c->A.temp, sizeof(double) * d.N, cudaMemcpyDeviceToHost));
+    GF_CK(cudaMemcpy(source.data(), c->A.source, sizeof(double) * d.E, cudaMemcpyDeviceToHost));
+    gf_layout L = c->L;
+    L.cord = cord.data();
+    L.temp = temp.data();
+    L.source = source.data();
+    gf_params pp = p;
+    const int idist = 2, nx = p.nx, nz = p.nz;
+    if (p.incoming_left == 1) {
+        int rc = gf_host_geotherm_columns(&pp, &L, 0, 0, idist);
+        if (rc) return rc;
+        for (int i = 0; i < idist; ++i)
+            for (int j = 0; j < nz - 1; ++j) source[gf_elem(d, j, i)] = source[gf_elem(d, j, idist)];
+    }
+    if (p.incoming_right == 1) {
+        int rc = gf_host_geotherm_columns(&pp, &L, p.nzone_age - 1, nx - 1 - idist, nx - 1);
+        if (rc) return rc;
+        for (int i = nx - 1 - idist; i < nx - 1; ++i)
+            for (int j = 0; j < nz - 1; ++j) source[gf_elem(d, j, i)] = source[gf_elem(d, j, nx - 2 - idist)];
+    }
+    GF_CK(cudaMemcpy(c->A.temp, temp.data(), sizeof(double) * d.N, cudaMemcpyHostToDevice));
+    GF_CK(cudaMemcpy(c->A.source, source.data(), sizeof(double) * d.E, cudaMemcpyHostToDevice));
+    return GF_OK;
+}
+
+void drop_graphs(gf_ctx *c) {
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+// marker2elem's top-up, count_phase_ratio of every element and jmoho; the
+// device marker count follows, the host copy is read back by the caller
+template <class R> void enqueue_marker2elem(gf_ctx *c, const GfLaunch &g, const GfRemeshArgs &a) {
+    GfRemesh<R>::top_up_markers(g, a, c->rb);
+    GfKernels<R>::phase_recount_all(g);
+    GfRemesh<R>::jmoho(g);
+}
+
+template <class R> int enqueue_remesh(gf_ctx *c) {
+    GfLaunch g = launch_of(c);
+    GfRemeshArgs a = remesh_args(c);
+    GfRemesh<R>::regrid(g, a, c->rb);
+    if (c->p.incoming_left == 1 || c->p.incoming_right == 1) {
+        int rc = sidewall_temps(c);
+        if (rc) return rc;
+    }
+    if (c->p.ivis_present == 1) GfKernels<R>::init_visc(g);
+    GfRemesh<R>::init_areas(g);
+    GfKernels<R>::rmasses(g);
+    GfKernels<R>::dt_mass(g);
+    GfRemesh<R>::rebin_markers(g, a, c->rb);
+    enqueue_marker2elem<R>(c, g, a);
+    return GF_OK;
+}
+
 unsigned step_signature(const gf_ctx *c) {
     const gf_params &p = c->p;
     unsigned sig = 0;
@@ -454,6 +562,25 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.e_flag, E));
     A_(dalloc(c, &A.nmarkers, 1));
     A_(dalloc(c, &c->d_angle, 1));
+    A_(dalloc(c, &A.cord_old, 2 * N));
+    {
+        GfRemeshBufs &b = c->rb;
+        A_(dalloc(c, &b.tx, p->nx));
+        A_(dalloc(c, &b.tz, p->nz));
+        A_(dalloc(c, &b.cold, 2 * E));
+        A_(dalloc(c, &b.cnew, 2 * E));
+        A_(dalloc(c, &b.pt, 12 * E));
+        A_(dalloc(c, &b.numtr, N));
+        A_(dalloc(c, &b.bc, 3 * N));
+        A_(dalloc(c, &b.plane, N));
+        A_(dalloc(c, &b.m_elem, M));
+        A_(dalloc(c, &b.m_slot, M));
+        A_(dalloc(c, &b.e_count, E));
+        A_(dalloc(c, &b.e_offset, E + 1));
+        A_(dalloc(c, &b.e_fill, E));
+        A_(dalloc(c, &b.d_scalars, 4));
+        A_(mesh_templates(c));
+    }
     if (mode == GF_MODE_MIXED) A_(dalloc(c, &c->staging, 16 * E));
     DevParams P;
     fill_params(P, *p);
@@ -590,7 +717,17 @@ int gf_init_visc(gf_ctx *c) {
 
 int gf_marker2elem(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
-    return GF_ERR_UNSUPPORTED;
+    GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
+    GfLaunch g = launch_of(c);
+    GfRemeshArgs a = remesh_args(c);
+    if (c->mode == GF_MODE_MIXED)
+        enqueue_marker2elem<float>(c, g, a);
+    else
+        enqueue_marker2elem<double>(c, g, a);
+    GF_CK(cudaMemcpyAsync(&c->nmarkers, c->A.nmarkers, sizeof(int), cudaMemcpyDeviceToHost, c->s));
+    GF_CK(cudaStreamSynchronize(c->s));
+    drop_graphs(c); // change_phase's launch covers nmarkers markers
+    return take_status(c);
 }
 
 int gf_finish_setflac(gf_ctx *c) {
@@ -643,7 +780,18 @@ int gf_itest_mesh(gf_ctx *c, double *min_angle) {
 
 int gf_remesh(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
-    return GF_ERR_UNSUPPORTED;
+    const int mr = c->p.mode_rem;
+    if (!(mr == 1 || mr == 3 || mr == 4 || mr == 11)) return GF_ERR_UNSUPPORTED;
+    if (c->p.nx < 4 || c->p.nz < 3) return GF_ERR_UNSUPPORTED; // element-centre grid needs 2 x 3 cells
+    GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
+    int rc = c->mode == GF_MODE_MIXED ? enqueue_remesh<float>(c) : enqueue_remesh<double>(c);
+    if (rc) return rc;
+    GF_CK(cudaMemsetAsync(c->A.dhacc_correction, 0, sizeof(double) * c->p.nx, c->s));
+    GF_CK(cudaMemcpyAsync(&c->nmarkers, c->A.nmarkers, sizeof(int), cudaMemcpyDeviceToHost, c->s));
+    GF_CK(cudaStreamSynchronize(c->s));
+    drop_graphs(c);
+    c->need_remeshing = 0;
+    return take_status(c);
 }
 
 int gf_set_sync(gf_ctx *c, int sync) {

@@ -99,5 +99,43 @@ template <class R> struct GfKernels {
     // mixed: total stress (FP64 staging) <-> stored deviations from -p_ref
     static void stress_in(const GfLaunch &g, const double *src);
     static void stress_out(const GfLaunch &g, double *dst);
+    // count_phase_ratio of every element (marker2elem.f90:49)
+    static void phase_recount_all(const GfLaunch &g);
+};
+
+// Remesh event (par.f90:94-110): host-prepared constants, passed by value.
+struct GfRemeshArgs {
+    int mode_rem, is_flex, has_dhacc;
+    double x0, z0, rxbo, rzbo;
+    double ar_x, ar_z; // mesh1 zone-pattern totals (init_cord.f90:289-327)
+    int incoming_left, incoming_right;
+    int nl_left, nl_right; // nph_layer of the first / last age zone
+    double hc_left[GF_MAXZONE_LAYER], hc_right[GF_MAXZONE_LAYER];
+    int iph_left[GF_MAXZONE_LAYER], iph_right[GF_MAXZONE_LAYER];
+    int nloop, nmarkers, max_markers;
+};
+
+// Device scratch of the remesh event (allocated with the context).
+struct GfRemeshBufs {
+    double *tx, *tz;     // mesh1 zone patterns along x (nx) and z (nz)
+    double *cold, *cnew; // element centres, old and new mesh (2 planes of E)
+    double *pt;          // 6 barycentric coefficients per old-mesh triangle
+    int *numtr;          // containing old triangle (1-based) per new point
+    double *bc;          // 3 planes of barycentric weights per new point
+    double *plane;       // copy of the field being interpolated
+    int *m_elem;         // new element of each marker (-1: none)
+    int *m_slot;         // markers grouped by element
+    int *e_count, *e_offset, *e_fill; // per element (e_offset has E + 1)
+    int *d_scalars;      // [0] scan total
+};
+
+template <class R> struct GfRemesh {
+    // bar2euler, rem_cord, element and node interpolation, incoming phases
+    static void regrid(const GfLaunch &g, const GfRemeshArgs &a, const GfRemeshBufs &b);
+    static void init_areas(const GfLaunch &g);
+    // lpeuler2bar, then marker2elem's top-up and jmoho (phase recount by the caller)
+    static void rebin_markers(const GfLaunch &g, const GfRemeshArgs &a, const GfRemeshBufs &b);
+    static void top_up_markers(const GfLaunch &g, const GfRemeshArgs &a, const GfRemeshBufs &b);
+    static void jmoho(const GfLaunch &g);
 };
 

@@ -389,8 +389,9 @@ __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &dep
 // that no total stress (up to 1e10 Pa at depth) is formed in FP32.
 __device__ __forceinline__ void plastic_dev(const PlasticConsts<float> &c, float rmu, float &depls, float hardn,
                                             float &s11, float &s22, float &s33, float &s12, float de11, float de22,
-                                            float de33, float de12, float p) {
+                                            float de33, float de12, float p, bool &mod) {
     depls = 0.0f;
+    mod = true; // cleared below when the elastic trial stress is kept
     float e1 = c.e1, e2 = c.e2, anphi = c.anphi, anpsi = c.anpsi;
     float tm = c.ten_max + p; // tension cut-off in stored (deviation) units
     float s11i = s11 + (de22 + de33) * e2 + de11 * e1;
@@ -416,6 +417,7 @@ __device__ __forceinline__ void plastic_dev(const PlasticConsts<float> &c, float
         depls = 0.5f * fabsf(alams + alams * anpsi);
     } else {
         s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;
+        mod = false; // the elastic trial stress is kept
         return;
     }
     if (s1 >= tm) {
@@ -438,13 +440,37 @@ __device__ __forceinline__ void plastic_dev(const PlasticConsts<float> &c, float
 
 __device__ __forceinline__ void plastic_sel(const PlasticConsts<double> &c, double rmu, double &depls, double hardn,
                                             double &s11, double &s22, double &s33, double &s12, double de11,
-                                            double de22, double de33, double de12, double) {
+                                            double de22, double de33, double de12, double, bool &mod) {
     plastic<double>(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12);
+    mod = true;
 }
 __device__ __forceinline__ void plastic_sel(const PlasticConsts<float> &c, float rmu, float &depls, float hardn,
                                             float &s11, float &s22, float &s33, float &s12, float de11, float de22,
-                                            float de33, float de12, float pref) {
-    plastic_dev(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12, pref);
+                                            float de33, float de12, float pref, bool &mod) {
+    plastic_dev(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12, pref, mod);
+}
+
+// fl_rheol.f90:281-296 keeps the Maxwell stress unless the plastic one has
+// the smaller second invariant.  When no triangle left its elastic trial
+// stress, the two differ by the Maxwell relaxation alone, O(dt/tau) ~ 1e-8
+// of the invariant for stiff lithosphere: below FP32 resolution, so the
+// FP32 path decides with the difference written out analytically,
+//   sv_a = (sp_a - t*S - 2*(mu - mu')*D) / (1 + t)   (and alike for s12),
+//   use Maxwell  <=>  2*W + V - Q*t*(2 + t) <= 0,
+// with S, B the start-of-step sums of s11-s22 and s12, D, D12 those of the
+// strain increments, Q = sp_a^2 + 4 sp_b^2, W = sp_a*da + 4*sp_b*db,
+// V = da^2 + 4*db^2 (da, db the bracketed corrections).
+__device__ __forceinline__ bool maxwell_wins_unyielded(float sp_a, float sp_b, float S, float B, float D, float D12,
+                                                       float rmu, float vis, float dt) {
+    const float visc_cut = 1e19f;
+    float rmu_m = vis < visc_cut ? rmu * vis / visc_cut : rmu;
+    float t = rmu_m / (2.0f * vis) * dt;
+    float da = -t * S - 2.0f * (rmu - rmu_m) * D;
+    float db = -t * B - 2.0f * (rmu - rmu_m) * D12;
+    float Q = sp_a * sp_a + 4.0f * sp_b * sp_b;
+    float W = sp_a * da + 4.0f * sp_b * db;
+    float V = da * da + 4.0f * db * db;
+    return 2.0f * W + V - Q * t * (2.0f + t) <= 0.0f;
 }
 
 // pre_plast (rh_plastic.f90:339-399)

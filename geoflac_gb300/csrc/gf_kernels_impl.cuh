@@ -116,7 +116,8 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
     R dike = A.dike_released ? R(A.dike_released[e]) : R(0);
     const R *dvol = (const R *)A.dvol;
     R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
-    bool ok = true;
+    bool ok = true, plas_mod = false;
+    R sumD = 0, sumD12 = 0; // strain-increment sums for the FP32 selection
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         R de11 = sr[0][k] * dt, de22 = sr[1][k] * dt, de12 = sr[2][k] * dt, de33 = R(0.0);
@@ -131,10 +132,19 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
         } else if (irh == 3) {
             ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
         } else if (irh == 6) {
-            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref);
+            bool m;
+            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref,
+                        m);
         } else if (irh >= 11) {
-            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref);
+            bool m;
+            plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref,
+                        m);
+            plas_mod = plas_mod || m;
             ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
+            if (sizeof(R) == sizeof(float)) {
+                sumD = sumD + (de11 - de22);
+                sumD12 = sumD12 + de12;
+            }
         }
     }
     if (!ok) set_status(C, 22, (int)e);
@@ -148,6 +158,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
         b = sv[2][0] + sv[2][1] + sv[2][2] + sv[2][3];
         R sII_visc = a * a + R(4.0) * (b * b);
         use_visc = !(sII_plas < sII_visc);
+        if (sizeof(R) == sizeof(float) && !plas_mod) {
+            R pa = sp[0][0] + sp[0][1] + sp[0][2] + sp[0][3] - sp[1][0] - sp[1][1] - sp[1][2] - sp[1][3];
+            R pb = sp[2][0] + sp[2][1] + sp[2][2] + sp[2][3];
+            R S = s0v[0][0] + s0v[0][1] + s0v[0][2] + s0v[0][3] - s0v[1][0] - s0v[1][1] - s0v[1][2] - s0v[1][3];
+            R B = s0v[2][0] + s0v[2][1] + s0v[2][2] + s0v[2][3];
+            use_visc = maxwell_wins_unyielded(float(pa), float(pb), float(S), float(B), float(sumD), float(sumD12),
+                                              float(rmu), float(vis), float(dt));
+        }
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -1278,6 +1296,11 @@ template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarke
     using namespace gfk;
     GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
     GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 0);
+}
+
+template <class R> void GfKernels<R>::phase_recount_all(const GfLaunch &g) {
+    using namespace gfk;
+    GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 1);
 }
 
 template <class R> void GfKernels<R>::min_angle(const GfLaunch &g, double *d_out) {

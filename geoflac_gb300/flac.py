@@ -89,6 +89,34 @@ class Flac:
         """One call of the reference's `flac` plus nloop/time bookkeeping."""
         self._call("flac")
 
+    def set_params(self):
+        """Push edited parameters (e.g. remeshing settings) to the context."""
+        check(self.lib.gf_set_params(self.ctx, C.byref(self.params)), "gf_set_params")
+
+    def marker2elem(self):
+        """Top up elements with fewer than 5 markers and recount phase ratios."""
+        self._call("marker2elem")
+
+    def remesh(self):
+        """The remesh event of par.f90:94-108: bar2euler, remesh,
+        lpeuler2bar, marker2elem, dhacc_correction reset."""
+        self._call("remesh")
+
+    def run(self, blocks: int) -> int:
+        """par.f90:69-108 without output: `blocks` times, ntest_rem steps
+        then the mesh-quality test and, if it fails, a remesh.  Returns the
+        number of remesh events."""
+        events = 0
+        for _ in range(int(blocks)):
+            self.step(self.params.ntest_rem)
+            if self.params.ny_rem == 1 and self.params.itherm != 2:
+                self.itest_mesh()
+                check(self.lib.gf_get_clock(self.ctx, C.byref(self.clock)), "gf_get_clock")
+                if self.clock.need_remeshing:
+                    self.remesh()
+                    events += 1
+        return events
+
     def step(self, n: int):
         """n steps, each replayed from a captured CUDA graph."""
         check(self.lib.gf_step(self.ctx, int(n)), "gf_step")

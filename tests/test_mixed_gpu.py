@@ -25,11 +25,19 @@ from ._util import rel_diff
 pytestmark = pytest.mark.gpu
 
 
-def _pair(workdir, name):
+def _pair(workdir, name, perturbed=False):
     inp = inpgen.CONFIGS[name]().write(str(workdir / f"{name}_mx.inp"))
     p, c, s = new_state(inp)
     p2, c2, s2 = clone(p, c, s)
-    return Flac(p, c, s, "fp64"), Flac(p2, c2, s2, "mixed")
+    out = [Flac(p, c, s, "fp64"), Flac(p2, c2, s2, "mixed")]
+    if perturbed:
+        # FP64 with the initial stresses perturbed by +-1e-7 (FP32 rounding
+        # size): how far the model itself carries a rounding-size change
+        p3, c3, s3 = clone(p, c, s)
+        rng = np.random.default_rng(1)
+        s3["stress0"][...] *= 1 + 1e-7 * rng.choice([-1.0, 1.0], size=s3["stress0"].shape)
+        out.append(Flac(p3, c3, s3, "fp64"))
+    return out
 
 
 def _observables(g, z0):
@@ -60,32 +68,35 @@ def test_mixed_short_horizon(workdir, name):
     b.download()
     err = {f: rel_diff(b.state[f], a.state[f]) for f in ("vel", "cord", "temp", "stress0", "aps")}
     _report(f"{name}_10", {"steps": 10, "rel_err": err})
-    assert err["cord"] <= 1e-7 and err["temp"] <= 1e-6, err
-    assert err["stress0"] <= 1e-3 and err["vel"] <= 1e-2, err
+    assert err["cord"] <= 1e-8 and err["temp"] <= 1e-9, err
+    assert err["stress0"] <= 1e-6 and err["vel"] <= 2e-4, err
     a.close()
     b.close()
 
 
 @pytest.mark.parametrize("name", ["config1", "config3_small"])
 def test_mixed_long_run_observables(workdir, name):
-    """500 steps: mean stresses, total plastic strain and topography."""
-    a, b = _pair(workdir, name)
+    """500 steps: mean stresses, total plastic strain and topography, each
+    within a fixed bound or, where the model itself is that sensitive,
+    within 3x the change a 1e-7 perturbation of the FP64 run produces."""
+    a, b, c = _pair(workdir, name, perturbed=True)
     z0 = a.state["cord"][0, :, 1].copy()
-    a.step(500)
-    b.step(500)
-    a.download()
-    b.download()
-    oa, ob = _observables(a, z0), _observables(b, z0)
-    err = {
-        "mean_sxx": abs(ob["mean_sxx"] - oa["mean_sxx"]) / abs(oa["mean_sxx"]),
-        "mean_szz": abs(ob["mean_szz"] - oa["mean_szz"]) / abs(oa["mean_szz"]),
-        "total_aps": abs(ob["total_aps"] - oa["total_aps"]) / max(abs(oa["total_aps"]), 1e-300),
-        "topo": float(np.abs(ob["topo"] - oa["topo"]).max() / max(np.abs(oa["topo"]).max(), 1e-300)),
-        "vel_pointwise": rel_diff(b.state["vel"], a.state["vel"]),
-    }
-    _report(f"{name}_500", {"steps": 500, "rel_err": err})
-    assert err["mean_sxx"] <= 1e-3 and err["mean_szz"] <= 1e-3, err
-    assert err["total_aps"] <= 5e-2, err
-    assert err["topo"] <= 5e-2, err
-    a.close()
-    b.close()
+    for g in (a, b, c):
+        g.step(500)
+        g.download()
+    o = {k: _observables(g, z0) for k, g in (("fp64", a), ("mixed", b), ("pert", c))}
+
+    def rel(x, y):
+        if isinstance(x, np.ndarray):
+            return float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+        return abs(x - y) / max(abs(y), 1e-300)
+
+    bounds = {"mean_sxx": 1e-4, "mean_szz": 1e-4, "total_aps": 5e-2, "topo": 5e-3}
+    err = {k: rel(o["mixed"][k], o["fp64"][k]) for k in bounds}
+    sens = {k: rel(o["pert"][k], o["fp64"][k]) for k in bounds}
+    _report(f"{name}_500", {"steps": 500, "rel_err": err, "fp64_1e-7_sensitivity": sens,
+                            "vel_pointwise": rel_diff(b.state["vel"], a.state["vel"])})
+    for k, bound in bounds.items():
+        assert err[k] <= max(bound, 3.0 * sens[k]), (k, err, sens)
+    for g in (a, b, c):
+        g.close()
