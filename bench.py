@@ -313,15 +313,63 @@ def run_ours(args):
         "gpu_launches": fp["launches"],
         "clocks": fp["clocks"],
     }
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(inp, steps=args.cpu_steps)
     for r in res.values():
         r["g"].close()
+    if args.members > 0:
+        out["batched"] = bench_batch(args, d, local)
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(inp, steps=args.cpu_steps)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def bench_batch(args, workdir: str, local: int):
+    """The 256-member mixed-precision sweep (config 4 of the workload list)
+    advanced by the ensemble driver: autotuned, then `args.steps` steps timed
+    with CUDA events on the batch's stream (working set of several GB, far
+    above L2)."""
+    import torch
+
+    from geoflac_gb300 import bytes_model
+    from geoflac_gb300.batch import Batch, ensemble
+
+    t0 = time.time()
+    members = ensemble(args.members, workdir)
+    setup_s = time.time() - t0
+    models = [m for m, _ in members]
+    b = Batch(models)
+    tuned = b.tune(trial_steps=2)
+    b.step(args.warmup)
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as cs:
+        e0.record(stream)
+        b.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    E = b.elements
+    nodes = sum(m.params.nx * m.params.nz for m in models)
+    bpe = bytes_model.step_bytes_per_element("mixed", nphase=models[0].params.nphase, n_over_e=nodes / E)
+    peak, peak_kind = _peaks()
+    achieved = bpe * E * args.steps / t / 1e9
+    out = {"value": E * args.steps / t, "unit": "element-steps/s", "members": len(models), "elements": E,
+           "nodes": nodes, "ms_per_step": 1e3 * t / args.steps, "steps": args.steps, "dtype": "f32 element fields / f64 nodes",
+           "config": {k: v for k, v in tuned.items() if k != "ms_per_step"}, "grid_ctas": b.grid,
+           "gpu_launches": args.steps,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": peak_kind,
+                        "algorithmic_bytes_per_element_step": bpe},
+           "setup_s": setup_s, "clocks": cs.summary()}
+    b.close()
+    for m in models:
+        m.close()
+    return out
 
 
 def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
@@ -382,6 +430,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
     ap.add_argument("--profile", choices=["fp64", "mixed"], default=None,
                     help="run warmup+steps steps of one mode and nothing else (for ncu)")
     args = ap.parse_args()

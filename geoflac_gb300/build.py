@@ -29,6 +29,7 @@ UNITS = [
     ("gf_capi.cu", ["-fmad=false"]),
     ("gf_noalloc.cu", ["-fmad=false"]),
     ("gf_remesh.cu", ["-fmad=false"]),
+    ("gf_batch.cu", ["-fmad=true"]),
     ("host_inp.cpp", None),
     ("host_setup.cpp", None),
 ]

@@ -36,6 +36,10 @@ def _arr(t, n):
     return t * n
 
 
+class GfBatchConfig(C.Structure):
+    _fields_ = [("threads", _i), ("items_per_thread", _i), ("ctas_per_sm", _i), ("graph_steps", _i)]
+
+
 class GfParams(C.Structure):
     _fields_ = [
         ("nx", _i), ("nz", _i),
@@ -159,6 +163,15 @@ def load_library(path: str = LIB_PATH):
         "gf_struct_size": (C.c_size_t, [_i]),
         "gf_set_sync": (_i, [vp, _i]),
         "gf_stream": (vp, [vp]),
+        "gf_batch_create": (_i, [_P(vp), _P(vp), _i]),
+        "gf_batch_destroy": (None, [vp]),
+        "gf_batch_set_config": (_i, [vp, _P(GfBatchConfig)]),
+        "gf_batch_get_config": (_i, [vp, _P(GfBatchConfig)]),
+        "gf_batch_tune": (_i, [vp, _i, _P(GfBatchConfig), _P(_d)]),
+        "gf_batch_step": (_i, [vp, _i]),
+        "gf_batch_stream": (vp, [vp]),
+        "gf_batch_elements": (C.c_longlong, [vp]),
+        "gf_batch_grid": (_i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

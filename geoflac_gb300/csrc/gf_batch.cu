@@ -1,0 +1,575 @@
+// Ensemble driver: hundreds of independent models of uneven size advanced
+// by one persistent kernel per step.
+//
+// Each member is an ordinary mixed-precision context; a packed member table
+// (device pointers, dimensions, constants) and per-kind tile tables (element,
+// node, 2x node, marker and max(element, node) items) describe the ensemble.
+// A tile is `threads * items_per_thread` consecutive items of ONE member, so
+// a warp never mixes members and the per-member reductions stay warp-local.
+// Every phase of the step (fl_therm, change_phase, fl_rheol, fl_node,
+// fl_move, rmasses, dt_mass) walks all tiles of all members, each CTA a
+// contiguous run of tiles, and the phases are separated by a grid barrier:
+// the ensemble shares the step's phase order, not its dt or its size.  The
+// per-item work is the same device code as the single-model kernels; a
+// member's result does not depend on the other members, the tile depth or
+// the residency (FP32 contraction may differ from the separately compiled
+// single-model kernels at rounding level).
+//
+// The grid is co-resident (cooperative launch), sized from the occupancy of
+// the chosen CTA shape; the barrier gives up after a bounded wait and raises
+// an error flag instead of hanging.
+
+// Items written in one phase are read in the next within the same kernel:
+// no pointer here may be treated as read-only for the kernel's lifetime.
+#define __restrict__
+#include "gf_kernels_impl.cuh"
+#include "gf_member.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+enum { K_E = 0, K_N, K_N2, K_M, K_EN, K_KINDS };
+
+struct BatchMember {
+    const DevParams *P;
+    DevClock *C;
+    DevArrays A;
+    GfDims d;
+    int idt_scale, movegrid, nmarkers, pad;
+};
+
+struct BatchSync {
+    unsigned count, gen;
+    int err, pad;
+};
+
+struct BatchArgs {
+    const BatchMember *members;
+    int nmembers;
+    const int2 *tile[K_KINDS]; // (member, first item) per tile
+    int ntile[K_KINDS];
+    BatchSync *sync;
+    unsigned sig;
+    int ipt; // items per thread
+};
+
+// Bounded grid barrier (generation counter).  Returns false if any CTA gave
+// up waiting; the kernel then returns at once.
+__device__ bool grid_sync(BatchSync *s) {
+    __shared__ int bad;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &s->gen;
+        unsigned g = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(&s->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&s->count, 0u);
+            __threadfence();
+            atomicAdd(&s->gen, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == g) {
+                if (++it > (1LL << 24)) {
+                    atomicExch(&s->err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        bad = *(volatile int *)&s->err;
+    }
+    __syncthreads();
+    return bad == 0;
+}
+
+// All tiles of one item kind, a contiguous run per CTA; the member record is
+// staged in shared memory whenever the run crosses into the next member.
+template <class F> __device__ void for_tiles(const BatchArgs &a, int kind, BatchMember &sm, int &cur, F &&f) {
+    const int nt = a.ntile[kind];
+    const int per = (nt + gridDim.x - 1) / gridDim.x;
+    const int t0 = blockIdx.x * per, t1 = min(nt, t0 + per);
+    for (int t = t0; t < t1; ++t) {
+        const int2 tl = a.tile[kind][t];
+        if (tl.x != cur) {
+            __syncthreads();
+            const int *src = reinterpret_cast<const int *>(a.members + tl.x);
+            int *dst = reinterpret_cast<int *>(&sm);
+            for (int w = threadIdx.x; w < (int)(sizeof(BatchMember) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+            __syncthreads();
+            cur = tl.x;
+        }
+        for (int r = 0; r < a.ipt; ++r) f(sm, (long long)tl.y + (long long)r * blockDim.x + threadIdx.x);
+    }
+}
+
+// Per-member scalar work, one thread per member.
+template <class F> __device__ void for_members(const BatchArgs &a, F &&f) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < a.nmembers; m += gridDim.x * blockDim.x) f(a.members[m]);
+}
+
+// One FLAC step (flac.f90:5-91, mixed precision) of every member.
+template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(BatchArgs a) {
+    using namespace gfk;
+    typedef float R;
+    __shared__ BatchMember sm;
+    int cur = -1;
+    const unsigned sig = a.sig;
+#define GF_SYNC()                                                                                                      \
+    do {                                                                                                               \
+        if (!grid_sync(a.sync)) return;                                                                                \
+    } while (0)
+    // fl_therm
+    for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+        b_k_therm_prep32(m.P, m.A, m.d, (float *)m.A.t_coef, i);
+    });
+    GF_SYNC();
+    for (int sweep = 0; sweep < 2; ++sweep) {
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_therm_sweep32(m.P, m.C, m.A, m.d, (const float *)m.A.t_coef, (float *)m.A.t_delta0, m.A.t_delta1,
+                              sweep, i);
+        });
+        GF_SYNC();
+    }
+    for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+        b_k_therm_apply32(m.P, m.A, m.d, m.A.t_delta1, i);
+    });
+    GF_SYNC();
+    if (sig & 1u) {
+        if (sig & 2u) { // change_phase
+            for_tiles(a, K_M, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_phase_markers(m.P, m.A, m.d, m.nmarkers, i);
+            });
+            GF_SYNC();
+            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_phase_recount<R>(m.P, m.C, m.A, m.d, 0, i);
+            });
+            GF_SYNC();
+        }
+        const int upd = (sig & 4u) ? 1 : 0;
+        const int avg = (sig & (8u << 8)) ? 2 : ((sig & (4u << 8)) ? 1 : 0);
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_rheol<R>(m.P, m.C, m.A, m.d, upd, 0, i);
+        });
+        GF_SYNC();
+        if (avg > 0) {
+            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_rheol_avg<R>(m.C, m.A, m.d, avg == 2 ? 1 : 0, i);
+            });
+            GF_SYNC();
+            if (avg == 2) {
+                for_members(a, [&](const BatchMember &m) { b_k_rheol_clock(m.C, 1); });
+                GF_SYNC();
+            }
+        }
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) { b_k_node<R>(m.P, m.C, m.A, m.d, i); });
+        GF_SYNC();
+        const int dtm = (sig & 32u) ? 1 : 0;
+        for_tiles(a, K_N2, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.movegrid) b_k_move_cord(m.C, m.A, m.d, i);
+        });
+        GF_SYNC();
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.movegrid) b_k_move_elem<R>(m.C, m.A, m.d, dtm ? 0 : 1, i);
+        });
+        GF_SYNC();
+        if (sig & 16u) { // rmasses
+            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_elem_dens<R>(m.P, m.C, m.A, m.d, i);
+            });
+            GF_SYNC();
+            for_members(a, [&](const BatchMember &m) { b_k_frac_fix<R>(m.P, m.C, m.A, m.d); });
+            GF_SYNC();
+            for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_node_gather_tri(m.A.e_tri, m.A.rmass, m.d, i);
+            });
+            GF_SYNC();
+        }
+        if (dtm) { // dt_mass
+            for_members(a, [&](const BatchMember &m) { b_k_dt_reset(m.C); });
+            GF_SYNC();
+            for_tiles(a, K_EN, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_dt_reduce<R>(m.P, m.C, m.A, m.d, i);
+            });
+            GF_SYNC();
+            for_members(a, [&](const BatchMember &m) { b_k_dt_scalars(m.P, m.C); });
+            GF_SYNC();
+            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+                if (m.idt_scale != 0) b_k_elem_am3<R>(m.P, m.C, m.A, m.d, i);
+            });
+            GF_SYNC();
+            for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+                if (m.idt_scale != 0)
+                    b_k_node_gather_tri(m.A.e_tri, m.A.amass, m.d, i);
+                else if (i < m.d.N)
+                    m.A.amass[i] = m.A.rmass[i];
+            });
+            GF_SYNC();
+        }
+        // par.f90:86: time advanced inside fl_move on steps without dt_mass
+        for_members(a, [&](const BatchMember &m) {
+            if (!m.movegrid || dtm) m.C->time = m.C->time + m.C->dt;
+        });
+    } else {
+        for_members(a, [&](const BatchMember &m) { m.C->time = m.C->time + m.C->dt; });
+    }
+#undef GF_SYNC
+}
+
+typedef void (*BatchKernel)(BatchArgs);
+
+BatchKernel kernel_for(int threads) {
+    switch (threads) {
+    case 128: return k_batch_step<128>;
+    case 256: return k_batch_step<256>;
+    case 512: return k_batch_step<512>;
+    default: return nullptr;
+    }
+}
+
+} // namespace
+
+struct gf_batch {
+    std::vector<gf_ctx *> members;
+    std::vector<GfMemberView> views;
+    BatchMember *d_members = nullptr;
+    int2 *d_tiles[K_KINDS] = {};
+    int ntile[K_KINDS] = {};
+    BatchSync *d_sync = nullptr;
+    cudaStream_t s = nullptr;
+    gf_batch_config cfg{256, 2, 1, 10};
+    int grid = 0;
+    long long elements = 0;
+    struct Graph {
+        std::vector<unsigned> sigs;
+        cudaGraphExec_t exec;
+    };
+    std::vector<Graph> graphs;
+};
+
+namespace {
+
+int batch_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return GF_OK;
+    std::fprintf(stderr, "geoflac_gb300: CUDA error in %s: %s\n", what, cudaGetErrorString(e));
+    return GF_ERR_CUDA;
+}
+#define GB_CK(call)                                                                                                    \
+    do {                                                                                                               \
+        int _rc = batch_cuda((call), #call);                                                                           \
+        if (_rc) return _rc;                                                                                           \
+    } while (0)
+
+void drop_graphs(gf_batch *b) {
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
+    b->graphs.clear();
+}
+
+long long kind_count(const GfMemberView &v, int kind) {
+    switch (kind) {
+    case K_E: return v.d.E;
+    case K_N: return v.d.N;
+    case K_N2: return 2 * v.d.N;
+    case K_M: return v.nmarkers;
+    default: return std::max(v.d.E, v.d.N);
+    }
+}
+
+// tile tables and the co-resident grid for the current configuration
+int build_tables(gf_batch *b) {
+    const gf_batch_config &c = b->cfg;
+    BatchKernel k = kernel_for(c.threads);
+    if (!k || c.items_per_thread < 1 || c.items_per_thread > 64 || c.ctas_per_sm < 1) return GF_ERR_ARG;
+    int dev = 0, sms = 0, occ = 0;
+    GB_CK(cudaGetDevice(&dev));
+    GB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, c.threads, 0));
+    if (occ < 1) return GF_ERR_UNSUPPORTED;
+    b->grid = sms * std::min(occ, c.ctas_per_sm);
+    const long long tile = (long long)c.threads * c.items_per_thread;
+    for (int kind = 0; kind < K_KINDS; ++kind) {
+        std::vector<int2> t;
+        for (size_t m = 0; m < b->views.size(); ++m) {
+            long long n = kind_count(b->views[m], kind);
+            for (long long s = 0; s < n; s += tile) {
+                if (s > 0x7fffffff) return GF_ERR_ARG;
+                t.push_back(make_int2((int)m, (int)s));
+            }
+        }
+        if (b->d_tiles[kind]) cudaFree(b->d_tiles[kind]);
+        b->d_tiles[kind] = nullptr;
+        b->ntile[kind] = (int)t.size();
+        if (!t.empty()) {
+            GB_CK(cudaMalloc(&b->d_tiles[kind], t.size() * sizeof(int2)));
+            GB_CK(cudaMemcpy(b->d_tiles[kind], t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        }
+    }
+    drop_graphs(b);
+    return GF_OK;
+}
+
+int upload_members(gf_batch *b) {
+    std::vector<BatchMember> h(b->views.size());
+    for (size_t m = 0; m < h.size(); ++m) {
+        const GfMemberView &v = b->views[m];
+        std::memset(&h[m], 0, sizeof(BatchMember));
+        h[m].P = v.P;
+        h[m].C = v.C;
+        h[m].A = v.A;
+        h[m].d = v.d;
+        h[m].idt_scale = v.idt_scale;
+        h[m].movegrid = v.movegrid;
+        h[m].nmarkers = v.nmarkers;
+    }
+    GB_CK(cudaMemcpy(b->d_members, h.data(), h.size() * sizeof(BatchMember), cudaMemcpyHostToDevice));
+    return GF_OK;
+}
+
+BatchArgs args_of(const gf_batch *b, unsigned sig) {
+    BatchArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.members = b->d_members;
+    a.nmembers = (int)b->members.size();
+    for (int k = 0; k < K_KINDS; ++k) {
+        a.tile[k] = b->d_tiles[k];
+        a.ntile[k] = b->ntile[k];
+    }
+    a.sync = b->d_sync;
+    a.sig = sig;
+    a.ipt = b->cfg.items_per_thread;
+    return a;
+}
+
+int launch_step(gf_batch *b, unsigned sig) {
+    BatchArgs a = args_of(b, sig);
+    cudaLaunchConfig_t lc;
+    std::memset(&lc, 0, sizeof lc);
+    lc.gridDim = dim3((unsigned)b->grid);
+    lc.blockDim = dim3((unsigned)b->cfg.threads);
+    lc.stream = b->s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    GB_CK(cudaLaunchKernelEx(&lc, kernel_for(b->cfg.threads), a));
+    return GF_OK;
+}
+
+// Signatures of the next n steps (all members share them).
+std::vector<unsigned> next_sigs(gf_batch *b, int n, std::vector<int> &nl, std::vector<int> &ns) {
+    // simulate the host bookkeeping of member 0 without touching it
+    const GfMemberView &v = b->views[0];
+    std::vector<unsigned> sigs;
+    int nloop = v.nloop, nsrate = v.nsrate;
+    for (int k = 0; k < n; ++k) {
+        unsigned sig = 0;
+        if (v.itherm != 2) {
+            sig |= 1u;
+            if (nloop % v.ifreq_rmasses == 0) sig |= 2u | 16u;
+            if (nloop % v.ifreq_visc == 0) sig |= 4u;
+            if (nsrate == v.ifreq_avgsr) sig |= 8u << 8;
+            else if (nsrate == -1) sig |= 4u << 8;
+            if (nloop % v.ifreq_imasses == 0) sig |= 32u;
+            if (sig & (8u << 8)) nsrate = 0;
+            nsrate = nsrate + 1;
+        }
+        nloop = nloop + 1;
+        sigs.push_back(sig);
+    }
+    nl.assign(1, nloop);
+    ns.assign(1, nsrate);
+    return sigs;
+}
+
+int refresh_views(gf_batch *b) {
+    for (size_t m = 0; m < b->members.size(); ++m) {
+        int rc = gf_ctx_view(b->members[m], &b->views[m]);
+        if (rc) return rc;
+    }
+    return GF_OK;
+}
+
+int check_status(gf_batch *b) {
+    GB_CK(cudaStreamSynchronize(b->s));
+    BatchSync hs;
+    GB_CK(cudaMemcpy(&hs, b->d_sync, sizeof hs, cudaMemcpyDeviceToHost));
+    if (hs.err) return GF_ERR_TIMEOUT;
+    int first = GF_OK;
+    for (gf_ctx *c : b->members) {
+        int st = gf_ctx_take_status(c);
+        if (st && !first) first = st;
+    }
+    return first;
+}
+
+} // namespace
+
+extern "C" {
+
+int gf_batch_create(gf_batch **out, gf_ctx **members, int n) {
+    if (!out || !members || n <= 0) return GF_ERR_ARG;
+    *out = nullptr;
+    gf_batch *b = new (std::nothrow) gf_batch;
+    if (!b) return GF_ERR_NOMEM;
+    b->members.assign(members, members + n);
+    b->views.resize(n);
+    int rc = refresh_views(b);
+    for (int m = 0; m < n && !rc; ++m) {
+        const GfMemberView &v = b->views[m], &v0 = b->views[0];
+        if (v.mode != GF_MODE_MIXED) rc = GF_ERR_UNSUPPORTED;
+        else if (v.nloop != v0.nloop || v.nsrate != v0.nsrate || v.itherm != v0.itherm ||
+                 v.ifreq_rmasses != v0.ifreq_rmasses || v.ifreq_visc != v0.ifreq_visc ||
+                 v.ifreq_imasses != v0.ifreq_imasses || v.ifreq_avgsr != v0.ifreq_avgsr)
+            rc = GF_ERR_ARG; // the members must share the step schedule
+        b->elements += v.d.E;
+    }
+    if (!rc) rc = batch_cuda(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking), "stream");
+    if (!rc) rc = batch_cuda(cudaMalloc(&b->d_members, sizeof(BatchMember) * n), "members");
+    if (!rc) rc = batch_cuda(cudaMalloc(&b->d_sync, sizeof(BatchSync)), "sync");
+    if (!rc) rc = batch_cuda(cudaMemset(b->d_sync, 0, sizeof(BatchSync)), "sync");
+    if (!rc) rc = upload_members(b);
+    if (!rc) rc = build_tables(b);
+    if (rc) {
+        gf_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return GF_OK;
+}
+
+void gf_batch_destroy(gf_batch *b) {
+    if (!b) return;
+    if (b->s) cudaStreamSynchronize(b->s);
+    drop_graphs(b);
+    for (int k = 0; k < K_KINDS; ++k)
+        if (b->d_tiles[k]) cudaFree(b->d_tiles[k]);
+    if (b->d_members) cudaFree(b->d_members);
+    if (b->d_sync) cudaFree(b->d_sync);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+}
+
+int gf_batch_set_config(gf_batch *b, const gf_batch_config *cfg) {
+    if (!b || !cfg) return GF_ERR_ARG;
+    gf_batch_config old = b->cfg;
+    b->cfg = *cfg;
+    int rc = build_tables(b);
+    if (rc) {
+        b->cfg = old;
+        build_tables(b);
+    }
+    return rc;
+}
+
+int gf_batch_get_config(gf_batch *b, gf_batch_config *cfg) {
+    if (!b || !cfg) return GF_ERR_ARG;
+    *cfg = b->cfg;
+    return GF_OK;
+}
+
+long long gf_batch_elements(gf_batch *b) { return b ? b->elements : 0; }
+
+int gf_batch_grid(gf_batch *b) { return b ? b->grid : 0; }
+
+void *gf_batch_stream(gf_batch *b) { return b ? (void *)b->s : nullptr; }
+
+int gf_batch_step(gf_batch *b, int nsteps) {
+    if (!b || nsteps < 0) return GF_ERR_ARG;
+    // members must be idle: their own streams may still hold work
+    for (const GfMemberView &v : b->views) GB_CK(cudaStreamSynchronize(v.s));
+    int rc = refresh_views(b);
+    if (rc) return rc;
+    int done = 0;
+    const int G = b->cfg.graph_steps;
+    while (done < nsteps) {
+        int chunk = G > 0 ? std::min(G, nsteps - done) : 1;
+        std::vector<int> nl, ns;
+        std::vector<unsigned> sigs = next_sigs(b, chunk, nl, ns);
+        if (G > 0) {
+            cudaGraphExec_t exec = nullptr;
+            for (auto &g : b->graphs)
+                if (g.sigs == sigs) exec = g.exec;
+            if (!exec) {
+                cudaGraph_t graph;
+                GB_CK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
+                int lrc = GF_OK;
+                for (unsigned sig : sigs)
+                    if (!lrc) lrc = launch_step(b, sig);
+                cudaError_t e = cudaStreamEndCapture(b->s, &graph);
+                if (lrc) return lrc;
+                GB_CK(e);
+                GB_CK(cudaGraphInstantiate(&exec, graph, 0));
+                cudaGraphDestroy(graph);
+                b->graphs.push_back(gf_batch::Graph{sigs, exec});
+            }
+            GB_CK(cudaGraphLaunch(exec, b->s));
+        } else {
+            rc = launch_step(b, sigs[0]);
+            if (rc) return rc;
+        }
+        for (unsigned sig : sigs)
+            for (gf_ctx *c : b->members) gf_ctx_advance(c, sig);
+        rc = refresh_views(b);
+        if (rc) return rc;
+        done += chunk;
+    }
+    return check_status(b);
+}
+
+// Autotuner: every CTA shape (threads), tile depth (items per thread) and
+// residency (CTAs per SM) that fits, each timed over `trial_steps` steps
+// with CUDA events after one untimed step; the fastest is kept.  The trial
+// steps advance the members like any other steps.
+int gf_batch_tune(gf_batch *b, int trial_steps, gf_batch_config *best, double *best_ms) {
+    if (!b || trial_steps < 1) return GF_ERR_ARG;
+    gf_batch_config keep = b->cfg, win = b->cfg;
+    double win_ms = 1e300;
+    cudaEvent_t e0, e1;
+    GB_CK(cudaEventCreate(&e0));
+    GB_CK(cudaEventCreate(&e1));
+    const int threads[3] = {128, 256, 512};
+    const int ipts[4] = {1, 2, 4, 8};
+    int rc = GF_OK;
+    for (int t : threads) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(t), t, 0);
+        for (int ipt : ipts)
+            for (int cps = 1; cps <= std::min(occ, 4); ++cps) {
+                gf_batch_config c{t, ipt, cps, 0}; // direct launches: no capture inside the timing
+                b->cfg = c;
+                if (build_tables(b)) continue;
+                rc = gf_batch_step(b, 1);
+                if (rc) break;
+                cudaEventRecord(e0, b->s);
+                rc = gf_batch_step(b, trial_steps);
+                if (rc) break;
+                cudaEventRecord(e1, b->s);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                double per = ms / trial_steps;
+                if (per < win_ms) {
+                    win_ms = per;
+                    win = c;
+                }
+            }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    win.graph_steps = keep.graph_steps;
+    b->cfg = rc ? keep : win;
+    int rc2 = build_tables(b);
+    if (rc) return rc;
+    if (best) *best = win;
+    if (best_ms) *best_ms = win_ms;
+    return rc2;
+}
+
+} // extern "C"

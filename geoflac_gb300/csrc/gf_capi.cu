@@ -15,6 +15,7 @@
 #include "../../include/geoflac_gb300.h"
 #include "gf_ctx.h"
 #include "gf_internal.h"
+#include "gf_member.h"
 
 namespace {
 
@@ -752,6 +753,33 @@ int gf_flac(gf_ctx *c) {
     advance_host(c, sig);
     return call_status(c);
 }
+
+int gf_ctx_view(gf_ctx *c, GfMemberView *v) {
+    if (!c || !v) return GF_ERR_ARG;
+    v->P = c->dP;
+    v->C = c->dC;
+    v->A = c->A;
+    v->d = c->d;
+    v->mode = c->mode;
+    v->idt_scale = c->p.idt_scale;
+    v->movegrid = c->p.movegrid;
+    v->itherm = c->p.itherm;
+    v->nmarkers = c->nmarkers;
+    v->nloop = c->nloop;
+    v->nsrate = c->nsrate;
+    v->ifreq_rmasses = c->p.ifreq_rmasses;
+    v->ifreq_visc = c->p.ifreq_visc;
+    v->ifreq_imasses = c->p.ifreq_imasses;
+    v->ifreq_avgsr = c->p.ifreq_avgsr;
+    v->s = c->s;
+    return GF_OK;
+}
+
+unsigned gf_ctx_signature(const gf_ctx *c) { return step_signature(c); }
+
+void gf_ctx_advance(gf_ctx *c, unsigned sig) { advance_host(c, sig); }
+
+int gf_ctx_take_status(gf_ctx *c) { return take_status(c); }
 
 int gf_step(gf_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return GF_ERR_ARG;

@@ -20,10 +20,7 @@ inline unsigned grid_for(long long n) { return (unsigned)((n + GF_THREADS - 1) /
 
 // ======================================================================
 // fl_rheol (fl_rheol.f90:4-389): one thread per element.
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                      DevArrays A, GfDims d, int update_visc, int nloop) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -245,11 +242,12 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restric
     sshrheat[e] = shr;
     (void)nloop;
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
+    b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Periodic time averaging (fl_rheol.f90:393-421); mode 1 resets the sums.
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset, long long e) {
     if (e >= d.E) return;
     R *se2sr = (R *)A.se2sr;
     R *e2sr = (R *)A.e2sr;
@@ -266,22 +264,25 @@ __global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__
         sshrheat[e] = R(0.0);
     }
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset) {
+    b_k_rheol_avg<R>(C, A, d, reset, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // scalar bookkeeping of fl_rheol: dtavg += dt at entry; dtavg = 0 at a reset
-__global__ void k_rheol_clock(DevClock *C, int phase) {
+__device__ __forceinline__ void b_k_rheol_clock(DevClock *C, int phase) {
     if (phase == 0)
         C->dtavg = C->dtavg + C->dt;
     else
         C->dtavg = 0.0;
 }
+__global__ void k_rheol_clock(DevClock *C, int phase) {
+    b_k_rheol_clock(C, phase);
+}
 
 // ======================================================================
 // fl_node (fl_node.f90:3-393): one thread per node, forces gathered from
 // the 4 adjacent quads in the reference's order, no atomics.
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                     DevArrays A, GfDims d) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long n) {
     if (n >= d.N) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -446,19 +447,21 @@ __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict
     vel[n] = v0;
     vel[d.N + n] = v1;
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_node<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // fl_move (fl_move.f90:3-132)
-__global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d, long long n) {
     if (n >= 2 * d.N) return;
     A.cord[n] = A.cord[n] + A.vel[n] * C->dt;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_move_cord(C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d,
-                                                          int advance_time) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time, long long e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
@@ -530,6 +533,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__
     }
     if (neg) set_status(C, 40, (int)e);
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time) {
+    b_k_move_elem<R>(C, A, d, advance_time, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // fl_therm (fl_therm.f90:393-598).
@@ -556,10 +562,7 @@ __device__ __forceinline__ int kidx(int a, int b) {
     return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
 }
 
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                           DevArrays A, GfDims d, double *__restrict__ tc) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc, long long e) {
     if (e == 0)
         for (int k = 0; k < GF_THERM_KMAX; ++k) C->therm_flags[k] = 0; // before any sweep runs
     if (e >= d.E) return;
@@ -595,13 +598,13 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__re
         tc[(16 + t) * E + e] = src * ra;
     }
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc) {
+    b_k_therm_prep<R>(Pp, C, A, d, tc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // One sweep.  Tup holds the current iterate (Told for sweep 0); self and
 // downstream values always come from Told (A.temp).
-__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d,
-                                                            const double *__restrict__ tc,
-                                                            const double *__restrict__ Tup, double *__restrict__ Tout,
-                                                            int k) {
+__device__ __forceinline__ void b_k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ tc, const double *__restrict__ Tup, double *__restrict__ Tout, int k) {
     if (k > 0 && C->therm_flags[k - 1] == 0) return; // converged one sweep ago
     long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool changed = false;
@@ -643,6 +646,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict
     }
     if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ tc, const double *__restrict__ Tup, double *__restrict__ Tout, int k) {
+    b_k_therm_sweep(C, A, d, tc, Tup, Tout, k);
+}
 
 // Temperature after the boundary conditions of fl_therm.f90:573-598 (top
 // row t_top, bottom row bot_bc or the flux condition, then the side columns
@@ -666,9 +672,7 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
 
 // temp0 = temp (fl_therm.f90:46-48); temp = converged iterate with the
 // boundary conditions applied.
-__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                            DevArrays A, GfDims d, const double *__restrict__ b0,
-                                                            const double *__restrict__ b1, int kmax) {
+__device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax) {
     int kc = kmax;
     for (int k = 0; k < kmax; ++k)
         if (C->therm_flags[k] == 0) {
@@ -690,6 +694,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__r
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax) {
+    b_k_therm_apply(Pp, C, A, d, b0, b1, kmax);
+}
 
 // ---- mixed precision: FP32 coefficients, two sweeps.
 // The diffusion sum is taken over temperature differences to the updated
@@ -697,9 +704,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__r
 // accuracy that a sum of ~1000 C values would lose.  Sweep 0 is the all-old
 // (Jacobi) update, sweep 1 reuses the upstream increments of sweep 0, which
 // leaves an error of order (kappa dt/h^2)^2 relative to the increment.
-__global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
-                                                             float *__restrict__ tc) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc, long long e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -731,14 +736,13 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__
         tc[(16 + t) * E + e] = src * ra;
     }
 }
+__global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc) {
+    b_k_therm_prep32(Pp, A, d, tc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // sweep 0 (final = 0): dT0 = increment with old values; sweep 1 (final = 1):
 // upstream neighbours use T + dT0, then the BCs are applied.
-__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp,
-                                                              DevClock *__restrict__ C, DevArrays A, GfDims d,
-                                                              const float *__restrict__ tc, float *__restrict__ d0,
-                                                              double *__restrict__ tnew, int final_sweep) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
@@ -782,10 +786,11 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *_
     else
         tnew[n] = Ts + (double)inc;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep) {
+    b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-__global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
-                                                              const double *__restrict__ tnew) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
@@ -793,14 +798,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *_
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew) {
+    b_k_therm_apply32(Pp, A, d, tnew, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // rmasses (rmasses.f90:236-295): per-element density, then a node gather in
 // the reference's colour order with each element's triangles in order.
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                          DevArrays A, GfDims d) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
@@ -829,9 +834,11 @@ __global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__res
         atomicMax((unsigned long long *)&C->frac_writer, (unsigned long long)(pos + 1));
     }
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_elem_dens<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-template <class R>
-__global__ void k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+template <class R> __device__ __forceinline__ void b_k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
     long long w = C->frac_writer;
     if (w <= 0) return;
     long long pos = w - 1;
@@ -850,6 +857,9 @@ __global__ void k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restric
     }
     C->frac_writer = 0;
 }
+template <class R> __global__ void k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_frac_fix<R>(Pp, C, A, d);
+}
 
 // Contribution lists: for local vertex v of a quad (1:(j,i) 2:(j+1,i)
 // 3:(j,i+1) 4:(j+1,i+1)), the triangles that contain it, in order.
@@ -860,9 +870,7 @@ __device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3},
 // dt_mass.f90:74-81), then each element's triangles containing the node in
 // the order A, B, C, D.  Every element in a node's neighbourhood has a
 // different colour, so this is the serial order of the coloured scatter.
-__global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const double *__restrict__ tri,
-                                                                double *__restrict__ out, GfDims d) {
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_node_gather_tri(const double *__restrict__ tri, double *__restrict__ out, GfDims d, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
@@ -885,13 +893,13 @@ __global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const double *__
         }
     out[n] = acc;
 }
+__global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const double *__restrict__ tri, double *__restrict__ out, GfDims d) {
+    b_k_node_gather_tri(tri, out, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // dt_mass (dt_mass.f90:16-232)
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                          DevArrays A, GfDims d) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long t) {
     const DevParams &P = *Pp;
     double dl = 1e300, vmax = 0.0, dmax = 0.0;
     unsigned pm = 0;
@@ -931,8 +939,11 @@ __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__res
         atomicOr(&C->phase_mask, pm);
     }
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_dt_reduce<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-__global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restrict__ C) {
+__device__ __forceinline__ void b_k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restrict__ C) {
     const DevParams &P = *Pp;
     double dlmin = fmin(1e28, __longlong_as_double((long long)C->r_dlmin));
     double vel_max = __longlong_as_double((long long)C->r_velmax);
@@ -975,13 +986,13 @@ __global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restr
     C->dtmax_therm = dtmax_therm;
     C->dt = fmin(fmin(dt_elastic, dt_maxwell), dtmax_therm);
 }
+__global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restrict__ C) {
+    b_k_dt_scalars(Pp, C);
+}
 
 // inertial mass share of each triangle c1d12*rho_inert/area
 // (dt_mass.f90:83-120), one element per thread
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                         DevArrays A, GfDims d) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     const R *area = (const R *)A.area;
@@ -998,30 +1009,35 @@ __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__rest
 #pragma unroll
     for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    b_k_elem_am3<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-__global__ void k_dt_reset(DevClock *C) {
+__device__ __forceinline__ void b_k_dt_reset(DevClock *C) {
     C->r_dlmin = (unsigned long long)__double_as_longlong(1e300);
     C->r_velmax = 0ull;
     C->r_diffmax = 0ull;
     C->phase_mask = 0u;
 }
+__global__ void k_dt_reset(DevClock *C) {
+    b_k_dt_reset(C);
+}
 
 // ======================================================================
 // init_visc
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, long long e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
     ((R *)A.visn)[e] = R(visc_of<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    b_k_init_visc<R>(Pp, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // change_phase (change_phase.f90:35-262)
-__global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d,
-                                                              int nmarkers) {
-    long long kk = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, long long kk) {
     if (kk >= nmarkers) return;
     if (A.mark_dead[kk] == 0) return;
     const DevParams &P = *Pp;
@@ -1124,12 +1140,12 @@ __global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *_
         A.mark_phase[kk] = (int8_t)newph;
     }
 }
+__global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
+    b_k_phase_markers(Pp, A, d, nmarkers, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // count_phase_ratio (marker_data.f90:140-172) for flagged elements + aps
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
-                                                              DevArrays A, GfDims d, int all) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all, long long e) {
     if (e >= d.E) return;
     if (!all && !A.e_flag[e]) return;
     const DevParams &P = *Pp;
@@ -1163,11 +1179,13 @@ __global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *_
         A.e_flag[e] = 0;
     }
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all) {
+    b_k_phase_recount<R>(Pp, C, A, d, all, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ======================================================================
 // itest_mesh angle criterion (rem_test.f90:77-118): min over all triangles
-__global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d, unsigned long long *out) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void b_k_min_angle(DevArrays A, GfDims d, unsigned long long *out, long long e) {
     double amin = 180.0;
     if (e < d.E) {
         int j, i;
@@ -1196,15 +1214,22 @@ __global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d,
     amin = warp_min(amin);
     if ((threadIdx.x & 31) == 0) atomic_min_pos(out, fmax(amin, 0.0));
 }
+__global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d, unsigned long long *out) {
+    b_k_min_angle(A, d, out, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // FP64 host array -> R device array
-template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n, long long t) {
     if (t < n) dst[t] = R(src[t]);
 }
-template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n) {
+    b_k_convert<R>(src, dst, n, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+template <class R> __device__ __forceinline__ void b_k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n, long long t) {
     if (t < n) dst[t] = (double)src[t];
+}
+template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n) {
+    b_k_convert_back<R>(src, dst, n, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 } // namespace gfk
@@ -1320,10 +1345,7 @@ void GfKernels<R>::convert_in(const GfLaunch &g, unsigned mask, const double *sr
 namespace {
 namespace gfk {
 // total stress -> (p_ref, total + p_ref on the normal components)
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restrict__ tot, R *__restrict__ st,
-                                                          double *__restrict__ p_ref, GfDims d) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d, long long e) {
     if (e >= d.E) return;
     double s = 0.0;
 #pragma unroll
@@ -1335,11 +1357,11 @@ __global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restri
 #pragma unroll
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = R(c == 2 ? tot[gf_s(d, e, c, k)] : tot[gf_s(d, e, c, k)] + p);
 }
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d) {
+    b_k_stress_in<R>(tot, st, p_ref, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
-template <class R>
-__global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref,
-                                                           double *__restrict__ tot, GfDims d) {
-    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+template <class R> __device__ __forceinline__ void b_k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d, long long e) {
     if (e >= d.E) return;
     double p = p_ref[e];
 #pragma unroll
@@ -1349,6 +1371,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__
             double v = (double)st[gf_s(d, e, c, k)];
             tot[gf_s(d, e, c, k)] = c == 2 ? v : v - p;
         }
+}
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d) {
+    b_k_stress_out<R>(st, p_ref, tot, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 } // namespace gfk
 } // namespace

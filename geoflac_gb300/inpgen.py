@@ -361,3 +361,32 @@ def config3_small() -> Model:
 CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config3_small": config3_small,
            "elastic_bar": elastic_bar, "maxwell_column": maxwell_column,
            "plastic_bar": plastic_bar}
+
+
+# ---------------------------------------------------------------- ensembles
+ENSEMBLE_SEED = 20261203
+ELEMENT_KM = 2.5  # element edge of the ensemble meshes (aspect-matched domains)
+
+
+def ensemble_member(k: int, seed: int = ENSEMBLE_SEED, scale: tuple = (80, 25, 400, 120)):
+    """Member k of the parameter sweep: mesh drawn between 80x25 and
+    400x120 quads (both sides from one draw, so the domain keeps its aspect,
+    2.5 km elements), crust friction 10-35 deg, crust thickness 25-45 km,
+    Moho temperature 400-800 C (piecewise-linear geotherm, ictherm 22, 1330 C
+    at 100 km or the base), wall velocity 0.5-5 cm/yr, extension or
+    convergence.  Returns (Model, the 4 sampled parameters)."""
+    import numpy as np
+    rng = np.random.default_rng([seed, k])
+    s = rng.uniform()
+    nex = int(round(scale[0] + s * (scale[2] - scale[0])))
+    nez = int(round(scale[1] + s * (scale[3] - scale[1])))
+    fric = float(rng.uniform(10.0, 35.0))
+    crust_km = float(rng.uniform(25.0, 45.0))
+    moho_t = float(rng.uniform(400.0, 800.0))
+    v_cm = float(rng.uniform(0.5, 5.0)) * (1.0 if rng.uniform() < 0.5 else -1.0)
+    width, depth = nex * ELEMENT_KM * 1e3, nez * ELEMENT_KM * 1e3
+    m = two_phase_extension(nex, nez, width, depth, crust_km=crust_km, half_rate_cm_yr=v_cm)
+    m.phases[1] = crust(fric1=fric, fric2=fric)
+    base_km = min(100.0, depth / 1e3)
+    m.zones = [AgeZone(22, moho_t, crust_km, base_km, 1, nex + 1, [crust_km], [2, 4])]
+    return m, {"friction": fric, "crust_km": crust_km, "moho_t": moho_t, "v_cm_yr": v_cm}

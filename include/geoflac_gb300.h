@@ -311,6 +311,34 @@ const char *gf_strerror(int code);
  * No reference counterpart (itest_mesh works on the host's module arrays). */
 int gf_min_angle_noalloc(const double *d_cord, int nx, int nz, void *stream, double *min_angle);
 
+/* ---- Ensembles (no reference counterpart) -----------------------------
+ * A batch advances many independent models together: one persistent,
+ * co-resident kernel per step walks every member's elements and nodes in
+ * tiles of one member each, phase by phase (the reference runs one model
+ * per process).  Members are GF_MODE_MIXED contexts that share the step
+ * schedule (nloop, nsrate, ifreq_*, itherm); they stay owned by the caller,
+ * must outlive the batch, and must not be stepped by other calls while a
+ * batch step runs.  Their states stay readable with gf_download. */
+typedef struct gf_batch gf_batch;
+typedef struct gf_batch_config {
+    int threads;          /* threads per CTA: 128, 256 or 512 */
+    int items_per_thread; /* a tile is threads * items_per_thread items of one member */
+    int ctas_per_sm;      /* resident CTAs per SM (capped by occupancy) */
+    int graph_steps;      /* steps per captured CUDA graph; 0 = direct launches */
+} gf_batch_config;
+int gf_batch_create(gf_batch **out, gf_ctx **members, int n);
+void gf_batch_destroy(gf_batch *b);
+int gf_batch_set_config(gf_batch *b, const gf_batch_config *cfg);
+int gf_batch_get_config(gf_batch *b, gf_batch_config *cfg);
+/* Times every configuration over trial_steps steps (after one untimed step)
+ * and keeps the fastest; the trial steps advance the members. */
+int gf_batch_tune(gf_batch *b, int trial_steps, gf_batch_config *best, double *best_ms_per_step);
+/* nsteps steps of every member (flac.f90:5-91 and par.f90:84-87 each). */
+int gf_batch_step(gf_batch *b, int nsteps);
+void *gf_batch_stream(gf_batch *b);
+long long gf_batch_elements(gf_batch *b);
+int gf_batch_grid(gf_batch *b);
+
 /* sizeof(gf_params), sizeof(gf_clock), sizeof(gf_layout) for which = 0, 1, 2:
  * lets a binding (ctypes, cgo, ISO_C_BINDING) check its struct mirrors.
  * No reference counterpart (the reference shares modules, not structs). */
