@@ -30,6 +30,7 @@ UNITS = [
     ("gf_noalloc.cu", ["-fmad=false"]),
     ("gf_remesh.cu", ["-fmad=false"]),
     ("gf_batch.cu", ["-fmad=true"]),
+    ("fno_gemm.cu", ["-fmad=true"]),
     ("host_inp.cpp", None),
     ("host_setup.cpp", None),
 ]
@@ -62,7 +63,7 @@ def build(verbose: bool = False, ptxas_v: bool = False, force: bool = False) -> 
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(ROOT, "include", "geoflac_gb300.h"))
+    headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     jobs = []
     objs = []
     for src, extra in UNITS:

@@ -1,0 +1,66 @@
+"""tcgen05 BF16 GEMM of the surrogate against a plain PyTorch FP32 product
+of the same BF16 operands, through the C-ABI.
+
+Tolerance: 2e-3 of the output's largest magnitude (FP32 accumulation in a
+different order; BF16 output rounding adds 2^-8 relative for c_bf16)."""
+import ctypes as C
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from geoflac_gb300 import capi
+    lib = capi.load_library()
+    f = lib.gf_gemm_bf16
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p] * 3 + [C.c_int] * 4 + [C.c_longlong] * 6 + [C.c_int, C.c_float, C.c_float,
+                                                                         C.c_void_p, C.c_void_p]
+    lib.gf_gemm_error.restype = C.c_int
+    return lib
+
+
+@pytest.mark.parametrize("batch,M,N,K", [(1, 128, 64, 64), (1, 300, 48, 384), (3, 257, 200, 136),
+                                         (2, 1000, 128, 1024), (4, 64, 256, 64), (1, 129, 96, 8)])
+@pytest.mark.parametrize("c_bf16", [0, 1])
+def test_gemm_matches_torch(batch, M, N, K, c_bf16):
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    g = torch.Generator(device="cpu").manual_seed(M * 7 + N * 3 + K)
+    A = torch.randn(batch, M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(batch, N, K, generator=g).to(torch.bfloat16).cuda()
+    bias = torch.randn(N, generator=g).float().cuda()
+    ref = torch.matmul(A.float(), B.float().transpose(1, 2)) * 0.5 + bias
+    out = torch.zeros(batch, M, N, dtype=torch.bfloat16 if c_bf16 else torch.float32, device="cuda")
+    rc = lib.gf_gemm_bf16(A.data_ptr(), B.data_ptr(), out.data_ptr(), batch, M, N, K, K, M * K, K, N * K, N, M * N,
+                          c_bf16, 0.5, 0.0, bias.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert lib.gf_gemm_error() == 0
+    err = (out.float() - ref).abs().max().item() / ref.abs().max().item()
+    assert err <= (6e-3 if c_bf16 else 2e-3), err
+
+
+def test_gemm_beta_accumulates():
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    A = torch.randn(1, 256, 128).to(torch.bfloat16).cuda()
+    B = torch.randn(1, 64, 128).to(torch.bfloat16).cuda()
+    C0 = torch.randn(1, 256, 64).cuda()
+    out = C0.clone()
+    assert lib.gf_gemm_bf16(A.data_ptr(), B.data_ptr(), out.data_ptr(), 1, 256, 64, 128, 128, 0, 128, 0, 64, 0, 0,
+                            1.0, 1.0, None, None) == 0
+    ref = torch.matmul(A.float(), B.float().transpose(1, 2)) + C0
+    torch.cuda.synchronize()
+    assert (out - ref).abs().max().item() / ref.abs().max().item() <= 2e-3
+
+
+def test_gemm_rejects_unaligned_strides():
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    A = torch.zeros(64, 12, dtype=torch.bfloat16, device="cuda")
+    out = torch.zeros(64, 64, device="cuda")
+    # K = 12 is not a multiple of 8: the TMA row stride would be 24 bytes
+    assert lib.gf_gemm_bf16(A.data_ptr(), A.data_ptr(), out.data_ptr(), 1, 64, 64, 12, 12, 0, 12, 0, 64, 0, 0,
+                            1.0, 0.0, None, None) == -3
