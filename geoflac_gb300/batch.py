@@ -56,6 +56,21 @@ class Batch:
     def step(self, n: int):
         check(self.lib.gf_batch_step(self.handle, int(n)), "gf_batch_step")
 
+    def sample(self, grid, H: int, W: int, phase_id: int = 2):
+        """fields of every member on an H x W grid (device FP32 tensor
+        [n, H, W, 9])"""
+        check(self.lib.gf_batch_sample(self.handle, grid.data_ptr(), H, W, phase_id), "gf_batch_sample")
+
+    def inject(self, grid, H: int, W: int):
+        check(self.lib.gf_batch_inject(self.handle, grid.data_ptr(), H, W), "gf_batch_inject")
+
+    def force_residual(self):
+        import numpy as np
+        out = np.zeros(len(self.members))
+        check(self.lib.gf_batch_force_residual(self.handle, out.ctypes.data_as(C.POINTER(C.c_double))),
+              "gf_batch_force_residual")
+        return out
+
     def close(self):
         if self.handle:
             self.lib.gf_batch_destroy(self.handle)

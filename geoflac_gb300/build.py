@@ -31,6 +31,7 @@ UNITS = [
     ("gf_remesh.cu", ["-fmad=false"]),
     ("gf_batch.cu", ["-fmad=true"]),
     ("fno_gemm.cu", ["-fmad=true"]),
+    ("fno_ops.cu", ["-fmad=true"]),
     ("host_inp.cpp", None),
     ("host_setup.cpp", None),
 ]

@@ -172,6 +172,9 @@ def load_library(path: str = LIB_PATH):
         "gf_batch_stream": (vp, [vp]),
         "gf_batch_elements": (C.c_longlong, [vp]),
         "gf_batch_grid": (_i, [vp]),
+        "gf_batch_sample": (_i, [vp, vp, _i, _i, _i]),
+        "gf_batch_inject": (_i, [vp, vp, _i, _i]),
+        "gf_batch_force_residual": (_i, [vp, _P(_d)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -40,6 +40,7 @@ struct BatchMember {
     DevArrays A;
     GfDims d;
     int idt_scale, movegrid, nmarkers, pad;
+    double z0, rzbo; // undeformed surface and depth of the regular start-up mesh
 };
 
 struct BatchSync {
@@ -221,6 +222,228 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
 #undef GF_SYNC
 }
 
+// ---------------------------------------------------------------- surrogate I/O
+// Fields of every member resampled to an H x W grid (channels last, FP32):
+// 0 vx, 1 vz, 2 sxx, 3 szz, 4 sxz (total stress, mean of the 4 triangles),
+// 5 plastic strain, 6 temperature, 7 fraction of phase `phase_id`,
+// 8 vertical displacement from the regular start-up mesh.  Bilinear in the
+// node / element-centre index space of each member (the members' domains
+// keep the grid's aspect).
+constexpr int SAMPLE_CH = 9;
+
+struct GridArgs {
+    const BatchMember *members;
+    int n, H, W, phase_id;
+    float *grid;       // [n][H][W][SAMPLE_CH]
+    const float *pred; // injection source, same layout
+};
+
+__device__ __forceinline__ void lerp_index(float f, int n, int &i0, float &w) {
+    // f in [0, n-1] -> cell i0 in [0, n-2], weight of i0 + 1
+    if (n < 2) {
+        i0 = 0;
+        w = 0.0f;
+        return;
+    }
+    f = fminf(fmaxf(f, 0.0f), (float)(n - 1));
+    i0 = min((int)f, n - 2);
+    w = f - (float)i0;
+}
+
+__device__ double elem_value(const BatchMember &m, long long e, int ch, int phase_id) {
+    const float *st = (const float *)m.A.stress0;
+    const GfDims &d = m.d;
+    const double pr = m.A.p_ref[e];
+    switch (ch) {
+    case 2: case 3: {
+        int c = ch - 2;
+        double s = 0.0;
+        for (int k = 0; k < 4; ++k) s += (double)st[gf_s(d, e, c, k)];
+        return 0.25 * s - pr;
+    }
+    case 4: {
+        double s = 0.0;
+        for (int k = 0; k < 4; ++k) s += (double)st[gf_s(d, e, 2, k)];
+        return 0.25 * s;
+    }
+    case 5: return (double)((const float *)m.A.aps)[e];
+    default: return m.A.phase_ratio[gf_pr(d, e, phase_id - 1)];
+    }
+}
+
+__device__ double node_value(const BatchMember &m, long long n, int j, int ch) {
+    const GfDims &d = m.d;
+    switch (ch) {
+    case 0: return m.A.vel[n];
+    case 1: return m.A.vel[d.N + n];
+    case 6: return m.A.temp[n];
+    default: return m.A.cord[d.N + n] - (m.z0 + m.rzbo * (double)j / (double)(d.nz - 1));
+    }
+}
+
+__global__ void k_sample(GridArgs g) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = (long long)g.n * g.H * g.W;
+    if (t >= total) return;
+    const int gx = (int)(t % g.W), gy = (int)((t / g.W) % g.H), mi = (int)(t / ((long long)g.W * g.H));
+    const BatchMember &m = g.members[mi];
+    const int nx = m.d.nx, nz = m.d.nz;
+    float *out = g.grid + t * SAMPLE_CH;
+    // nodes
+    int i0, j0;
+    float wx, wy;
+    lerp_index((gx + 0.5f) * (nx - 1) / g.W, nx, i0, wx);
+    lerp_index((gy + 0.5f) * (nz - 1) / g.H, nz, j0, wy);
+    const int nch[4] = {0, 1, 6, 8};
+    for (int q = 0; q < 4; ++q) {
+        int ch = nch[q];
+        double a = node_value(m, gf_node(m.d, j0, i0), j0, ch), b = node_value(m, gf_node(m.d, j0, i0 + 1), j0, ch);
+        double c = node_value(m, gf_node(m.d, j0 + 1, i0), j0 + 1, ch),
+               dd = node_value(m, gf_node(m.d, j0 + 1, i0 + 1), j0 + 1, ch);
+        out[ch] = (float)((1 - wy) * ((1 - wx) * a + wx * b) + wy * ((1 - wx) * c + wx * dd));
+    }
+    // elements (centres)
+    lerp_index((gx + 0.5f) * (nx - 1) / g.W - 0.5f, nx - 1, i0, wx);
+    lerp_index((gy + 0.5f) * (nz - 1) / g.H - 0.5f, nz - 1, j0, wy);
+    const int ech[5] = {2, 3, 4, 5, 7};
+    const int i1 = min(i0 + 1, nx - 2), j1 = min(j0 + 1, nz - 2);
+    for (int q = 0; q < 5; ++q) {
+        int ch = ech[q];
+        double a = elem_value(m, gf_elem(m.d, j0, i0), ch, g.phase_id), b = elem_value(m, gf_elem(m.d, j0, i1), ch, g.phase_id);
+        double c = elem_value(m, gf_elem(m.d, j1, i0), ch, g.phase_id), dd = elem_value(m, gf_elem(m.d, j1, i1), ch, g.phase_id);
+        out[ch] = (float)((1 - wy) * ((1 - wx) * a + wx * b) + wy * ((1 - wx) * c + wx * dd));
+    }
+}
+
+// bilinear read of one channel of member mi's grid at grid coordinates (fy, fx)
+__device__ float grid_at(const GridArgs &g, int mi, float fy, float fx, int ch) {
+    int i0, j0;
+    float wx, wy;
+    lerp_index(fx, g.W, i0, wx);
+    lerp_index(fy, g.H, j0, wy);
+    const float *G = g.pred + (long long)mi * g.H * g.W * SAMPLE_CH;
+    auto at = [&](int j, int i) { return G[((long long)j * g.W + i) * SAMPLE_CH + ch]; };
+    return (1 - wy) * ((1 - wx) * at(j0, i0) + wx * at(j0, i0 + 1)) + wy * ((1 - wx) * at(j0 + 1, i0) + wx * at(j0 + 1, i0 + 1));
+}
+
+// grid -> member nodes: velocity, temperature, vertical position
+__global__ void k_inject_nodes(GridArgs g, const int2 *tiles, int ntile, int ipt) {
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const BatchMember &m = g.members[tl.x];
+        for (int r = 0; r < ipt; ++r) {
+            long long n = (long long)tl.y + (long long)r * blockDim.x + threadIdx.x;
+            if (n >= m.d.N) continue;
+            const int j = (int)(n % m.d.nz), i = (int)(n / m.d.nz);
+            const float fx = (float)i * g.W / (m.d.nx - 1) - 0.5f, fy = (float)j * g.H / (m.d.nz - 1) - 0.5f;
+            m.A.vel[n] = grid_at(g, tl.x, fy, fx, 0);
+            m.A.vel[m.d.N + n] = grid_at(g, tl.x, fy, fx, 1);
+            m.A.temp[n] = grid_at(g, tl.x, fy, fx, 6);
+            m.A.cord[m.d.N + n] = m.z0 + m.rzbo * (double)j / (double)(m.d.nz - 1) + (double)grid_at(g, tl.x, fy, fx, 8);
+        }
+    }
+}
+
+// grid -> member elements: stresses (the out-of-plane stress keeps its
+// deviation from the in-plane mean), plastic strain; areas of the moved mesh
+__global__ void k_inject_elems(GridArgs g, const int2 *tiles, int ntile, int ipt, DevClock *err) {
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const BatchMember &m = g.members[tl.x];
+        const GfDims &d = m.d;
+        for (int r = 0; r < ipt; ++r) {
+            long long e = (long long)tl.y + (long long)r * blockDim.x + threadIdx.x;
+            if (e >= d.E) continue;
+            const int j = (int)(e % (d.nz - 1)), i = (int)(e / (d.nz - 1));
+            const float fx = (i + 0.5f) * g.W / (d.nx - 1) - 0.5f, fy = (j + 0.5f) * g.H / (d.nz - 1) - 0.5f;
+            float *st = (float *)m.A.stress0;
+            const double pr = m.A.p_ref[e];
+            const double sxx = grid_at(g, tl.x, fy, fx, 2), szz = grid_at(g, tl.x, fy, fx, 3),
+                         sxz = grid_at(g, tl.x, fy, fx, 4);
+            for (int k = 0; k < 4; ++k) {
+                double oxx = (double)st[gf_s(d, e, 0, k)] - pr, ozz = (double)st[gf_s(d, e, 1, k)] - pr;
+                double oyy = (double)st[gf_s(d, e, 3, k)] - pr;
+                double nyy = oyy + 0.5 * ((sxx - oxx) + (szz - ozz));
+                st[gf_s(d, e, 0, k)] = (float)(sxx + pr);
+                st[gf_s(d, e, 1, k)] = (float)(szz + pr);
+                st[gf_s(d, e, 2, k)] = (float)sxz;
+                st[gf_s(d, e, 3, k)] = (float)(nyy + pr);
+            }
+            ((float *)m.A.aps)[e] = fmaxf(0.0f, grid_at(g, tl.x, fy, fx, 5));
+            gfk::Quad q;
+            gfk::load_quad(m.A.cord, d, j, i, q);
+            const double *x = q.x, *y = q.y;
+            double det[4] = {((x[1] * y[2] - y[1] * x[2]) - (x[0] * y[2] - y[0] * x[2])) + (x[0] * y[1] - y[0] * x[1]),
+                             ((x[1] * y[3] - y[1] * x[3]) - (x[2] * y[3] - y[2] * x[3])) + (x[2] * y[1] - y[2] * x[1]),
+                             ((x[1] * y[3] - y[1] * x[3]) - (x[0] * y[3] - y[0] * x[3])) + (x[0] * y[1] - y[0] * x[1]),
+                             ((x[3] * y[2] - y[3] * x[2]) - (x[0] * y[2] - y[0] * x[2])) + (x[0] * y[3] - y[0] * x[3])};
+            for (int k = 0; k < 4; ++k) {
+                ((float *)m.A.area)[gf_ek(d, e, k)] = (float)(1.0 / det[k]);
+                if (det[k] <= 0.0) gfk::set_status(m.C, 41, (int)e);
+            }
+        }
+    }
+    (void)err;
+}
+
+// Force imbalance at the free nodes (fl_node.f90 without damping): per member
+// sum |F| and sum (|gravity| + sum over triangles |stress-divergence term|).
+__global__ void k_force_residual(const BatchMember *members, const int2 *tiles, int ntile, int ipt, double *acc,
+                                 double g_acc) {
+    for (int t = blockIdx.x; t < ntile; t += gridDim.x) {
+        const int2 tl = tiles[t];
+        const BatchMember &m = members[tl.x];
+        const GfDims &d = m.d;
+        double sf = 0.0, ss = 0.0;
+        for (int r = 0; r < ipt; ++r) {
+            long long n = (long long)tl.y + (long long)r * blockDim.x + threadIdx.x;
+            if (n >= d.N) continue;
+            const int j = (int)(n % d.nz), i = (int)(n / d.nz);
+            const int c0 = m.A.ncod[n], c1 = m.A.ncod[d.N + n];
+            const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
+            const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
+            const float *st = (const float *)m.A.stress0;
+            const float *area = (const float *)m.A.area;
+            double fx = 0.0, fy = 0.0, mag = 0.0;
+            for (int qd = 0; qd < 4; ++qd) {
+                int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+                if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
+                long long e = gf_elem(d, je, ie);
+                gfk::Quad q;
+                gfk::load_quad(m.A.cord, d, je, ie, q);
+                double ar[4];
+                for (int k = 0; k < 4; ++k) ar[k] = (double)area[gf_ek(d, e, k)];
+                double dx[3][4], dz[3][4];
+                gfk::shape_derivs<double>(q, ar, dx, dz);
+                const double pe = m.A.p_ref[e];
+                for (int k = 0; k < 3; ++k) {
+                    int tt = kk[qd][k], mq = mm[qd][k];
+                    double factor = 0.25 / ar[tt];
+                    double sxx = (double)st[gf_s(d, e, 0, tt)] - pe, szz = (double)st[gf_s(d, e, 1, tt)] - pe,
+                           sxz = (double)st[gf_s(d, e, 2, tt)];
+                    double tx = factor * (sxx * dx[mq][tt] + sxz * dz[mq][tt]);
+                    double ty = factor * (sxz * dx[mq][tt] + szz * dz[mq][tt]);
+                    fx -= tx;
+                    fy -= ty;
+                    mag += sqrt(tx * tx + ty * ty);
+                }
+            }
+            const double grav = m.A.rmass[n] * g_acc;
+            fy -= grav;
+            if (c0 == 1) fx = 0.0; // fixed velocity components carry reactions
+            if (c1 == 1) fy = 0.0;
+            sf += sqrt(fx * fx + fy * fy);
+            ss += mag + fabs(grav);
+        }
+        sf = gfk::warp_sum(sf);
+        ss = gfk::warp_sum(ss);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&acc[2 * tl.x], sf);
+            atomicAdd(&acc[2 * tl.x + 1], ss);
+        }
+    }
+}
+
 typedef void (*BatchKernel)(BatchArgs);
 
 BatchKernel kernel_for(int threads) {
@@ -243,6 +466,7 @@ struct gf_batch {
     BatchSync *d_sync = nullptr;
     cudaStream_t s = nullptr;
     gf_batch_config cfg{256, 2, 1, 10};
+    double g = 10.0; // gravity of the members (one value; checked at creation)
     int grid = 0;
     long long elements = 0;
     struct Graph {
@@ -325,6 +549,8 @@ int upload_members(gf_batch *b) {
         h[m].idt_scale = v.idt_scale;
         h[m].movegrid = v.movegrid;
         h[m].nmarkers = v.nmarkers;
+        h[m].z0 = v.z0;
+        h[m].rzbo = v.rzbo;
     }
     GB_CK(cudaMemcpy(b->d_members, h.data(), h.size() * sizeof(BatchMember), cudaMemcpyHostToDevice));
     return GF_OK;
@@ -428,7 +654,9 @@ int gf_batch_create(gf_batch **out, gf_ctx **members, int n) {
                  v.ifreq_imasses != v0.ifreq_imasses || v.ifreq_avgsr != v0.ifreq_avgsr)
             rc = GF_ERR_ARG; // the members must share the step schedule
         b->elements += v.d.E;
+        if (v.g != b->views[0].g) rc = GF_ERR_ARG;
     }
+    if (!rc) b->g = b->views[0].g;
     if (!rc) rc = batch_cuda(cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking), "stream");
     if (!rc) rc = batch_cuda(cudaMalloc(&b->d_members, sizeof(BatchMember) * n), "members");
     if (!rc) rc = batch_cuda(cudaMalloc(&b->d_sync, sizeof(BatchSync)), "sync");
@@ -570,6 +798,45 @@ int gf_batch_tune(gf_batch *b, int trial_steps, gf_batch_config *best, double *b
     if (best) *best = win;
     if (best_ms) *best_ms = win_ms;
     return rc2;
+}
+
+int gf_batch_sample(gf_batch *b, float *grid, int H, int W, int phase_id) {
+    if (!b || !grid || H < 1 || W < 1 || phase_id < 1) return GF_ERR_ARG;
+    GridArgs g{b->d_members, (int)b->members.size(), H, W, phase_id, grid, nullptr};
+    long long n = (long long)g.n * H * W;
+    k_sample<<<(unsigned)((n + 255) / 256), 256, 0, b->s>>>(g);
+    GB_CK(cudaGetLastError());
+    return GF_OK;
+}
+
+int gf_batch_inject(gf_batch *b, const float *grid, int H, int W) {
+    if (!b || !grid || H < 2 || W < 2) return GF_ERR_ARG;
+    GridArgs g{b->d_members, (int)b->members.size(), H, W, 1, nullptr, grid};
+    const int T = b->cfg.threads, ipt = b->cfg.items_per_thread;
+    if (b->ntile[K_N]) k_inject_nodes<<<b->ntile[K_N], T, 0, b->s>>>(g, b->d_tiles[K_N], b->ntile[K_N], ipt);
+    if (b->ntile[K_E])
+        k_inject_elems<<<b->ntile[K_E], T, 0, b->s>>>(g, b->d_tiles[K_E], b->ntile[K_E], ipt, nullptr);
+    GB_CK(cudaGetLastError());
+    return check_status(b);
+}
+
+int gf_batch_force_residual(gf_batch *b, double *residual) {
+    if (!b || !residual) return GF_ERR_ARG;
+    const int n = (int)b->members.size();
+    double *acc = nullptr;
+    GB_CK(cudaMalloc(&acc, sizeof(double) * 2 * n));
+    cudaMemsetAsync(acc, 0, sizeof(double) * 2 * n, b->s);
+    const double g_acc = b->g;
+    if (b->ntile[K_N])
+        k_force_residual<<<b->ntile[K_N], b->cfg.threads, 0, b->s>>>(b->d_members, b->d_tiles[K_N], b->ntile[K_N],
+                                                                     b->cfg.items_per_thread, acc, g_acc);
+    std::vector<double> h(2 * n);
+    cudaError_t e = cudaMemcpyAsync(h.data(), acc, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, b->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->s);
+    cudaFree(acc);
+    GB_CK(e);
+    for (int m = 0; m < n; ++m) residual[m] = h[2 * m] / (h[2 * m + 1] > 0 ? h[2 * m + 1] : 1.0);
+    return GF_OK;
 }
 
 } // extern "C"

@@ -771,6 +771,9 @@ int gf_ctx_view(gf_ctx *c, GfMemberView *v) {
     v->ifreq_visc = c->p.ifreq_visc;
     v->ifreq_imasses = c->p.ifreq_imasses;
     v->ifreq_avgsr = c->p.ifreq_avgsr;
+    v->z0 = c->p.z0;
+    v->rzbo = c->p.rzbo;
+    v->g = c->p.g;
     v->s = c->s;
     return GF_OK;
 }

@@ -11,6 +11,7 @@ struct GfMemberView {
     int mode, idt_scale, movegrid, itherm, nmarkers;
     int nloop, nsrate;
     int ifreq_rmasses, ifreq_visc, ifreq_imasses, ifreq_avgsr;
+    double z0, rzbo, g;
     cudaStream_t s;
 };
 

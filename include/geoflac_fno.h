@@ -29,6 +29,53 @@ int gf_gemm_bf16(const void *A, const void *B, void *C, int batch, int M, int N,
 /* GF_FNO_ERR_TIMEOUT if a GEMM kernel gave up a wait since the last call. */
 int gf_gemm_error(void);
 
+/* Element types below: 0 = FP32, 1 = BF16. */
+/* dst[b][c][r] = src[b][r][c] for batch matrices of rows x cols. */
+int gf_fno_transpose(const void *src, void *dst, int batch, long long rows, int cols, int src_bf16, int dst_bf16,
+                     void *stream);
+int gf_fno_cast(const void *src, void *dst, long long n, int src_bf16, int dst_bf16, void *stream);
+/* a = GELU(z) (erf form); dz = da * GELU'(z). */
+int gf_fno_gelu(const float *z, void *a, long long n, int a_bf16, void *stream);
+int gf_fno_gelu_bwd(const float *z, const void *da, int da_bf16, float *dz, long long n, void *stream);
+/* Complex bookkeeping of the truncated 2-D DFT.  Y[(b, c, kp)][q]: for the
+ * W-transformed row kp (kp < m2 real part, kp >= m2 imaginary part of W-mode
+ * kp mod m2), cosine (q < Q) and sine (q >= Q) sums over the rows h of the Q
+ * kept H-modes.  U[(k2, q)][b][(c, re|im)] (BF16) is the 2-D DFT coefficient;
+ * the _bwd form maps dU (FP32, same layout) back to dY (BF16). */
+int gf_fno_spec_combine(const float *Y, void *U, int B, int C, int m2, int Q, void *stream);
+int gf_fno_spec_combine_bwd(const float *dU, void *dY, int B, int C, int m2, int Q, void *stream);
+/* Complex mode weights R[mode][i][o][re, im] (FP32) to the real 2C x 2C
+ * blocks Rm[mode][(o, part)][(i, part)] and RmT = transpose (BF16), and the
+ * gradient of R from the gradient of Rm. */
+int gf_fno_expand_modes(const float *R, void *Rm, void *RmT, int modes, int C, void *stream);
+int gf_fno_modes_grad(const float *dRm, float *dR, int modes, int C, void *stream);
+/* out[c] (+)= sum_r X[r][c]; dst[i] (+)= sum_b src[b][i]. */
+int gf_fno_colsum(const float *X, float *out, long long rows, int cols, int accum, void *stream);
+int gf_fno_sum_batches(const float *src, float *dst, int nb, long long n, int accum, void *stream);
+/* Adam (bias-corrected, decoupled from the loss scale), step counts from 1. */
+int gf_fno_adam(float *p, const float *g, float *m, float *v, long long n, float lr, float b1, float b2, float eps,
+                int step, float weight_decay, void *stream);
+/* loss += mean((pred - target)^2); dpred = scale * 2 (pred - target) / n. */
+int gf_fno_mse(const float *pred, const float *target, void *dpred, int dpred_bf16, double *loss, long long n,
+               float scale, void *stream);
+/* Surrogate input from a sampled grid raw [n][H][W][9] and member
+ * parameters [n][4]: (raw - mean) / std per channel, (params - pmean) /
+ * pstd, two grid coordinates in [-1, 1], one zero channel -> BF16
+ * [n][H][W][16].  stats = {mean[9], std[9], pmean[4], pstd[4]}. */
+int gf_fno_pack_input(const float *raw, const float *params, const float *stats, void *out, int n, int H, int W,
+                      void *stream);
+/* Training target from the later grid y and the earlier x: (y - x - mean_d) /
+ * std_d in channels 0..8 of 16 (FP32); stats_d = {mean_d[9], std_d[9]}. */
+int gf_fno_pack_target(const float *y, const float *x, const float *stats_d, float *out, long long points,
+                       void *stream);
+/* dst[r] = src[idx[r]] for nrows rows of row_bytes bytes (idx on the device). */
+int gf_fno_gather_rows(const void *src, void *dst, const long long *idx, int nrows, long long row_bytes,
+                       void *stream);
+/* Prediction back to fields: y = x + mean_d + std_d * pred. */
+int gf_fno_unpack(const float *pred, const float *x, const float *stats_d, float *y, long long points, void *stream);
+/* out = x + y (y may be NULL), FP32 and/or BF16 outputs. */
+int gf_fno_add(const float *x, const float *y, float *out, void *out_bf16, long long n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

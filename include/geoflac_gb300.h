@@ -336,6 +336,21 @@ int gf_batch_tune(gf_batch *b, int trial_steps, gf_batch_config *best, double *b
 /* nsteps steps of every member (flac.f90:5-91 and par.f90:84-87 each). */
 int gf_batch_step(gf_batch *b, int nsteps);
 void *gf_batch_stream(gf_batch *b);
+/* Every member's fields resampled to an H x W grid, FP32 [n][H][W][9]:
+ * vx, vz, sxx, szz, sxz (total stress), plastic strain, temperature, the
+ * fraction of phase `phase_id`, and the vertical displacement from the
+ * regular start-up mesh (device pointer; bilinear in each member's index
+ * space; asynchronous on the batch's stream). */
+int gf_batch_sample(gf_batch *b, float *grid, int H, int W, int phase_id);
+/* The inverse for a predicted grid of the same layout: velocities,
+ * temperatures and vertical node positions, stresses (the out-of-plane
+ * stress keeps its deviation) and plastic strain of every member, and the
+ * element areas of the moved mesh; stop 41 if an element inverts. */
+int gf_batch_inject(gf_batch *b, const float *grid, int H, int W);
+/* Force imbalance of every member's current state (fl_node.f90's forces
+ * without damping): sum over free nodes of |F| divided by the sum of
+ * |gravity| and the magnitudes of the stress-divergence terms. */
+int gf_batch_force_residual(gf_batch *b, double *residual);
 long long gf_batch_elements(gf_batch *b);
 int gf_batch_grid(gf_batch *b);
 
