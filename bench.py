@@ -246,6 +246,9 @@ def run_ours(args):
 
     d = tempfile.mkdtemp(prefix="gfbench")
     inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    if args.profile in ("fno", "batch"):
+        profile_extra(args, d)
+        return
     if args.profile:
         # profiling run: only `warmup + steps` graph-replayed steps of one mode
         g = _make_model(inp, args.profile)
@@ -317,6 +320,10 @@ def run_ours(args):
         r["g"].close()
     if args.members > 0:
         out["batched"] = bench_batch(args, d, local)
+        out["batched"]["surrogate"] = None
+        if args.sur_epochs > 0:
+            args.batch_cfg = {k: v for k, v in out["batched"]["config"].items()}
+            out["batched"]["surrogate"] = bench_surrogate(args, d)
     if rank == 0 and ws == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(inp, steps=args.cpu_steps)
     if rank == 0:
@@ -370,6 +377,113 @@ def bench_batch(args, workdir: str, local: int):
     for m in models:
         m.close()
     return out
+
+
+def bench_surrogate(args, workdir: str):
+    """Surrogate leg: snapshots of a 256-member sweep from the ensemble
+    driver, FNO training (the library's tcgen05 kernels), then screening of
+    a fresh 256-member sweep over `interval` steps against the plain
+    ensemble step of the same members (timed on the same GPU)."""
+    import numpy as np
+    import torch
+
+    from geoflac_gb300 import surrogate as S
+    from geoflac_gb300.batch import Batch, ensemble
+    from geoflac_gb300.fno import FnoConfig
+
+    cfg = FnoConfig()
+    n, interval = args.members, args.sur_interval
+    t0 = time.time()
+    tr = ensemble(n, workdir)
+    tb = Batch([m for m, _ in tr])
+    tb.set_config(**args.batch_cfg)
+    snaps = S.generate(tb, [p for _, p in tr], n_snap=args.sur_snaps, interval=interval, H=cfg.H, W=cfg.W)
+    cal = S.calibrate_tolerance(tb, cfg.H, cfg.W)
+    t_data = time.time() - t0
+    sur = S.Surrogate(cfg, S.Normaliser.fit(snaps), seed=0)
+    info = sur.train(snaps, epochs=args.sur_epochs, batch=64, lr=args.sur_lr)
+    pairs = n * (args.sur_snaps - 1)
+    del snaps
+    tb.close()
+    for m, _ in tr:
+        m.close()
+    # fresh sweep, two identical copies: plain truth and screened
+    d2 = os.path.join(workdir, "fresh")
+    os.makedirs(d2, exist_ok=True)
+    fa = ensemble(n, d2, seed=S_SEED_FRESH)
+    fb = ensemble(n, d2, seed=S_SEED_FRESH)
+    ba, bb = Batch([m for m, _ in fa]), Batch([m for m, _ in fb])
+    for b in (ba, bb):
+        b.set_config(**args.batch_cfg)
+    ba.step(args.sur_start)
+    bb.step(args.sur_start)
+    stream = torch.cuda.ExternalStream(ba.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ba.step(interval)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) / 1e3
+    truth = torch.empty((n, cfg.H, cfg.W, S.NCH), dtype=torch.float32, device="cuda")
+    ba.sample(truth, cfg.H, cfg.W, S.CRUST_PHASE)
+    torch.cuda.synchronize()
+    res = S.screen(bb, sur, [p for _, p in fb], interval, cal["tol"])
+    err = S.rel_errors(res["fields"], truth, res["raw_t"])
+    out = {"members": n, "interval_steps": interval, "grid": [cfg.H, cfg.W], "width": cfg.C,
+           "modes": [cfg.m1, cfg.m2], "layers": cfg.layers, "training_pairs": pairs, "epochs": args.sur_epochs,
+           "train_seconds": info["seconds"], "train_loss_first": info["first_loss"],
+           "train_loss_final": info["final_loss"], "data_seconds": t_data,
+           "plain_seconds": t_plain, "screen_seconds": res["seconds"], "screen_predict_seconds": res["seconds_predict"],
+           "screen_save_seconds": res["seconds_save"], "rerun_members": len(res["rerun"]),
+           "speedup_vs_plain": t_plain / res["seconds"],
+           "gate": {k: v for k, v in cal.items()},
+           "rel_err": {k: {"median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)), "max": float(np.max(v))}
+                       for k, v in err.items()}}
+    for b in (ba, bb):
+        b.close()
+    for m, _ in fa + fb:
+        m.close()
+    return out
+
+
+S_SEED_FRESH = 20261204
+
+
+def profile_extra(args, workdir: str):
+    """Profiling runs of the ensemble driver and the surrogate (for ncu):
+    batch = `warmup + steps` steps of a `--members` sweep; fno = `warmup +
+    steps` training steps of the full-size FNO (batch 64, 128 x 384) on
+    synthetic fields."""
+    import numpy as np
+    import torch
+
+    if args.profile == "batch":
+        from geoflac_gb300.batch import Batch, ensemble
+
+        ms = ensemble(args.members, workdir)
+        b = Batch([m for m, _ in ms])
+        b.set_config(threads=256, items_per_thread=2, ctas_per_sm=2, graph_steps=0)
+        b.step(args.warmup + args.steps)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "batch", "members": args.members, "elements": b.elements,
+                          "steps": args.warmup + args.steps}))
+        return
+    from geoflac_gb300.fno import Fno, FnoConfig
+
+    cfg = FnoConfig()
+    net = Fno(cfg, seed=0)
+    rng = np.random.default_rng(0)
+    nb = args.fno_batch
+    x = torch.from_numpy(rng.standard_normal((nb, cfg.H, cfg.W, cfg.cin)).astype(np.float32)).cuda().to(torch.bfloat16)
+    t = torch.from_numpy(rng.standard_normal((nb, cfg.H, cfg.W, cfg.cout)).astype(np.float32)).cuda()
+    for _ in range(args.warmup + args.steps):
+        out = net.forward(x, train=True)
+        loss, dout = net.loss_grad(out, t)
+        net.backward(dout)
+        net.adam(lr=1e-4)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "fno", "steps": args.warmup + args.steps, "loss": loss.item()}))
 
 
 def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
@@ -431,7 +545,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
-    ap.add_argument("--profile", choices=["fp64", "mixed"], default=None,
+    ap.add_argument("--sur-epochs", type=int, default=20, help="surrogate training epochs (0: skip the surrogate)")
+    ap.add_argument("--sur-snaps", type=int, default=17, help="snapshots per member (pairs = members x (snaps - 1))")
+    ap.add_argument("--sur-interval", type=int, default=500, help="steps between snapshots and of the forecast")
+    ap.add_argument("--sur-start", type=int, default=1000, help="plain steps of the fresh sweep before the forecast")
+    ap.add_argument("--sur-lr", type=float, default=2e-3)
+    ap.add_argument("--fno-batch", type=int, default=64, help="batch of the fno profiling run")
+    ap.add_argument("--profile", choices=["fp64", "mixed", "batch", "fno"], default=None,
                     help="run warmup+steps steps of one mode and nothing else (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

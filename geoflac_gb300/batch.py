@@ -71,6 +71,14 @@ class Batch:
               "gf_batch_force_residual")
         return out
 
+    def backup(self):
+        """device copy of the fields an injection overwrites"""
+        check(self.lib.gf_batch_backup(self.handle), "gf_batch_backup")
+
+    def restore(self, members):
+        arr = (C.c_int * len(members))(*[int(k) for k in members])
+        check(self.lib.gf_batch_restore(self.handle, arr, len(members)), "gf_batch_restore")
+
     def close(self):
         if self.handle:
             self.lib.gf_batch_destroy(self.handle)

@@ -175,6 +175,8 @@ def load_library(path: str = LIB_PATH):
         "gf_batch_sample": (_i, [vp, vp, _i, _i, _i]),
         "gf_batch_inject": (_i, [vp, vp, _i, _i]),
         "gf_batch_force_residual": (_i, [vp, _P(_d)]),
+        "gf_batch_backup": (_i, [vp]),
+        "gf_batch_restore": (_i, [vp, _P(_i), _i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

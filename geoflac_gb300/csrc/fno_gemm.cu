@@ -6,9 +6,11 @@
 //   C[z][m][n] = alpha * sum_k A[z][m][k] * B[z][n][k] + beta * C[z][m][n] + bias[n]
 //
 // A and B are K-major BF16 (row stride lda/ldb elements, batch stride
-// sA/sB), C is row-major FP32 or BF16.  One CTA computes a 128 x BN tile:
-// one thread issues TMA loads of 128x64 (A) and BNx64 (B) BF16 tiles into a
-// 4-stage ring of 128-byte-swizzled shared-memory buffers, one thread issues
+// sA/sB; sA = -1 shares one A among all batches), C is row-major FP32 or
+// BF16, with an optional BF16 copy of C or of GELU(C) (fused activation).
+// One CTA computes a 128 x BN tile: one thread issues TMA loads of 128x64
+// (A) and BNx64 (B) BF16 tiles into a ring of up to 4 (as many as the
+// K-blocks) 128-byte-swizzled shared-memory buffers, one thread issues
 // tcgen05.mma (M=128, N=BN, K=16) from shared-memory descriptors into a TMEM
 // accumulator, and the four warps read the accumulator back with
 // tcgen05.ld for the epilogue.  Every wait on an mbarrier is bounded; a
@@ -33,11 +35,12 @@ constexpr long long WAIT_LIMIT = 1LL << 22;
 
 __device__ int g_gemm_err;
 
-template <int BN> struct __align__(1024) GemmSmem {
-    __nv_bfloat16 a[STAGES][BM * BK]; // 16 KB per stage, 1024-byte aligned
-    __nv_bfloat16 b[STAGES][BN * BK];
-    uint64_t full[STAGES], empty[STAGES], done;
-    uint32_t tmem_base;
+// shared memory of one CTA with a ring of `stages` operand buffers:
+// A stages, B stages (each 1024-byte aligned), then the mbarriers
+template <int BN> struct SmemLayout {
+    static constexpr uint32_t a_bytes = BM * BK * 2, b_bytes = BN * BK * 2;
+    __host__ __device__ static uint32_t bars(int stages) { return (uint32_t)stages * (a_bytes + b_bytes); }
+    __host__ __device__ static uint32_t total(int stages) { return bars(stages) + (2 * stages + 2) * 8 + 16; }
 };
 
 struct Epilogue {
@@ -46,7 +49,13 @@ struct Epilogue {
     int M, N, c_bf16;
     float alpha, beta;
     const float *bias;
+    __nv_bfloat16 *aux; // optional second output act(z) in BF16 (same layout as C)
+    int act;            // 0: aux = z, 1: aux = GELU(z)
+    int a_bcast;        // A shared by every batch (loaded at batch coordinate 0)
+    int stages;
 };
+
+__device__ __forceinline__ float act_gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -139,46 +148,52 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 template <int BN>
-__global__ void __launch_bounds__(GEMM_THREADS, 1)
+__global__ void __launch_bounds__(GEMM_THREADS)
     k_gemm_bf16(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int K, Epilogue ep) {
     extern __shared__ uint8_t dsmem[];
-    GemmSmem<BN> &S = *reinterpret_cast<GemmSmem<BN> *>((reinterpret_cast<uintptr_t>(dsmem) + 1023) &
-                                                         ~static_cast<uintptr_t>(1023));
+    typedef SmemLayout<BN> L;
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~static_cast<uintptr_t>(1023));
+    const int stages = ep.stages;
+    uint8_t *sa = base, *sb = base + (size_t)stages * L::a_bytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + L::bars(stages));
+    uint64_t *empty = full + stages, *done = empty + stages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, z = blockIdx.z;
     const int nk = (K + BK - 1) / BK;
     __shared__ int fail;
     if (threadIdx.x == 0) {
         fail = 0;
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&S.full[s], 1);
-            mbar_init(&S.empty[s], 1);
+        for (int s = 0; s < stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
         }
-        mbar_init(&S.done, 1);
+        mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_base)),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"((uint32_t)BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = S.tmem_base;
+    const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
         if (lane == 0) { // TMA producer
             const uint32_t bytes = (uint32_t)(BM + BN) * BK * sizeof(__nv_bfloat16);
+            const int za = ep.a_bcast ? 0 : z;
             for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % STAGES;
-                if (kb >= STAGES && !mbar_wait(&S.empty[s], ((kb / STAGES) - 1) & 1)) {
+                const int s = kb % stages;
+                if (kb >= stages && !mbar_wait(&empty[s], ((kb / stages) - 1) & 1)) {
                     fail = 1;
                     break;
                 }
-                mbar_expect_tx(&S.full[s], bytes);
-                tma_load_3d(S.a[s], &tmA, kb * BK, m0, z, &S.full[s]);
-                tma_load_3d(S.b[s], &tmB, kb * BK, n0, z, &S.full[s]);
+                mbar_expect_tx(&full[s], bytes);
+                tma_load_3d(sa + (size_t)s * L::a_bytes, &tmA, kb * BK, m0, za, &full[s]);
+                tma_load_3d(sb + (size_t)s * L::b_bytes, &tmB, kb * BK, n0, z, &full[s]);
             }
         }
         __syncwarp();
@@ -186,23 +201,24 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (lane == 0) { // MMA issuer
             const uint32_t id = idesc<BN>();
             for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % STAGES;
-                if (!mbar_wait(&S.full[s], (kb / STAGES) & 1)) {
+                const int s = kb % stages;
+                if (!mbar_wait(&full[s], (kb / stages) & 1)) {
                     fail = 1;
                     break;
                 }
                 fence_after();
-                const uint64_t da = sdesc(smem_u32(S.a[s])), db = sdesc(smem_u32(S.b[s]));
+                const uint64_t da = sdesc(smem_u32(sa + (size_t)s * L::a_bytes)),
+                               db = sdesc(smem_u32(sb + (size_t)s * L::b_bytes));
 #pragma unroll
                 for (int k = 0; k < BK / 16; ++k)
                     mma(tmem, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), id, (kb > 0 || k > 0) ? 1u : 0u);
-                mma_commit(&S.empty[s]);
+                mma_commit(&empty[s]);
             }
-            mma_commit(&S.done);
+            mma_commit(done);
         }
         __syncwarp();
     }
-    const bool ok = mbar_wait(&S.done, 0);
+    const bool ok = mbar_wait(done, 0);
     fence_after();
     if (ok && !fail) {
         const int row = m0 + warp * 32 + lane;
@@ -211,30 +227,78 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32];
             tmem_ld32(trow + (uint32_t)c0, v);
-            if (row >= ep.M) continue;
             const int col0 = n0 + c0;
-            if (col0 >= ep.N) continue;
-            if (ep.c_bf16) {
-                __nv_bfloat16 *C = reinterpret_cast<__nv_bfloat16 *>(ep.C) + (long long)z * ep.sC + (long long)row * ep.ldc;
+            if (row >= ep.M || col0 >= ep.N) continue;
+            const long long off = (long long)z * ep.sC + (long long)row * ep.ldc + col0;
+            const bool full32 = col0 + 32 <= ep.N;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int col = col0 + i;
-                    if (col < ep.N) {
-                        float x = ep.alpha * v[i];
-                        if (ep.bias) x += ep.bias[col];
-                        C[col] = __float2bfloat16_rn(x);
+            for (int i = 0; i < 32; ++i) {
+                float x = ep.alpha * v[i];
+                if (ep.bias && col0 + i < ep.N) x += ep.bias[col0 + i];
+                v[i] = x;
+            }
+            if (ep.c_bf16) {
+                __nv_bfloat16 *C = reinterpret_cast<__nv_bfloat16 *>(ep.C) + off;
+                if (full32 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0)) {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 8) {
+                        uint4 w;
+                        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) h[q] = __floats2bfloat162_rn(v[i + 2 * q], v[i + 2 * q + 1]);
+                        *reinterpret_cast<uint4 *>(C + i) = w;
                     }
+                } else {
+                    for (int i = 0; i < 32 && col0 + i < ep.N; ++i) C[i] = __float2bfloat16_rn(v[i]);
                 }
             } else {
-                float *C = reinterpret_cast<float *>(ep.C) + (long long)z * ep.sC + (long long)row * ep.ldc;
+                float *C = reinterpret_cast<float *>(ep.C) + off;
+                if (full32 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0)) {
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int col = col0 + i;
-                    if (col < ep.N) {
-                        float x = ep.alpha * v[i];
-                        if (ep.beta != 0.0f) x += ep.beta * C[col];
-                        if (ep.bias) x += ep.bias[col];
-                        C[col] = x;
+                    for (int i = 0; i < 32; i += 4) {
+                        float4 o = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                        if (ep.beta != 0.0f) {
+                            float4 c = *reinterpret_cast<const float4 *>(C + i);
+                            o.x += ep.beta * c.x;
+                            o.y += ep.beta * c.y;
+                            o.z += ep.beta * c.z;
+                            o.w += ep.beta * c.w;
+                        }
+                        *reinterpret_cast<float4 *>(C + i) = o;
+                        v[i] = o.x;
+                        v[i + 1] = o.y;
+                        v[i + 2] = o.z;
+                        v[i + 3] = o.w;
+                    }
+                } else {
+                    for (int i = 0; i < 32 && col0 + i < ep.N; ++i) {
+                        float x = v[i];
+                        if (ep.beta != 0.0f) x += ep.beta * C[i];
+                        C[i] = x;
+                        v[i] = x;
+                    }
+                }
+                if (ep.aux) {
+                    __nv_bfloat16 *X = ep.aux + off;
+                    if (full32 && ((reinterpret_cast<uintptr_t>(X) & 15) == 0)) {
+#pragma unroll
+                        for (int i = 0; i < 32; i += 8) {
+                            uint4 w;
+                            __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&w);
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) {
+                                float a0 = v[i + 2 * q], a1 = v[i + 2 * q + 1];
+                                if (ep.act) {
+                                    a0 = act_gelu(a0);
+                                    a1 = act_gelu(a1);
+                                }
+                                h[q] = __floats2bfloat162_rn(a0, a1);
+                            }
+                            *reinterpret_cast<uint4 *>(X + i) = w;
+                        }
+                    } else {
+                        for (int i = 0; i < 32 && col0 + i < ep.N; ++i)
+                            X[i] = __float2bfloat16_rn(ep.act ? act_gelu(v[i]) : v[i]);
                     }
                 }
             }
@@ -279,12 +343,14 @@ bool make_map(CUtensorMap *m, const void *p, int K, int rows, int batch, long lo
 }
 
 template <int BN> int launch(const CUtensorMap &ta, const CUtensorMap &tb, int batch, int M, int N, int K,
-                             const Epilogue &ep, cudaStream_t s) {
-    const size_t smem = sizeof(GemmSmem<BN>) + 1024;
+                             Epilogue ep, cudaStream_t s) {
+    const int nk = (K + BK - 1) / BK;
+    ep.stages = nk < STAGES ? nk : STAGES;
+    const size_t smem = SmemLayout<BN>::total(ep.stages) + 1024;
     static bool attr_set = false;
     if (!attr_set) {
-        if (cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(k_gemm_bf16<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(SmemLayout<BN>::total(STAGES) + 1024)) != cudaSuccess)
             return GF_FNO_ERR_CUDA;
         attr_set = true;
     }
@@ -300,18 +366,30 @@ extern "C" {
 int gf_gemm_bf16(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda, long long sA,
                  long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha, float beta,
                  const float *bias, void *stream) {
+    return gf_gemm_bf16_ex(A, B, C, batch, M, N, K, lda, sA, ldb, sB, ldc, sC, c_bf16, alpha, beta, bias, nullptr, 0,
+                           stream);
+}
+
+int gf_gemm_bf16_ex(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda,
+                    long long sA, long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha,
+                    float beta, const float *bias, void *aux, int act, void *stream) {
     if (!A || !B || !C || batch < 1 || M < 1 || N < 1 || K < 1) return GF_FNO_ERR_ARG;
     if (batch > 65535 || (M + BM - 1) / BM > 2147483647LL) return GF_FNO_ERR_ARG;
     // TMA: 16-byte aligned base addresses and row / batch strides
     if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return GF_FNO_ERR_ALIGN;
-    if ((lda * 2) % 16 || (ldb * 2) % 16 || (sA * 2) % 16 || (sB * 2) % 16 || K % 8) return GF_FNO_ERR_ALIGN;
+    const int a_bcast = sA < 0 ? 1 : 0; // sA = -1: one A for every batch
+    if ((lda * 2) % 16 || (ldb * 2) % 16 || ((a_bcast ? 0 : sA) * 2) % 16 || (sB * 2) % 16 || K % 8)
+        return GF_FNO_ERR_ALIGN;
     if (lda < K || ldb < K || ldc < N) return GF_FNO_ERR_ARG;
-    if (c_bf16 && beta != 0.0f) return GF_FNO_ERR_ARG;
+    if (c_bf16 && (beta != 0.0f || aux)) return GF_FNO_ERR_ARG;
+    if (aux && (reinterpret_cast<uintptr_t>(aux) & 15)) return GF_FNO_ERR_ALIGN;
     const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
     CUtensorMap ta, tb;
-    if (!make_map(&ta, A, K, M, batch, lda, sA, BM) || !make_map(&tb, B, K, N, batch, ldb, sB, bn))
+    if (!make_map(&ta, A, K, M, a_bcast ? 1 : batch, lda, a_bcast ? 0 : sA, BM) ||
+        !make_map(&tb, B, K, N, batch, ldb, sB, bn))
         return GF_FNO_ERR_CUDA;
-    Epilogue ep{C, ldc, sC > 0 ? sC : (long long)M * ldc, M, N, c_bf16, alpha, beta, bias};
+    Epilogue ep{C, ldc, sC > 0 ? sC : (long long)M * ldc, M, N, c_bf16, alpha, beta, bias,
+                reinterpret_cast<__nv_bfloat16 *>(aux), act, a_bcast, STAGES};
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     if (bn == 64) return launch<64>(ta, tb, batch, M, N, K, ep, s);
     if (bn == 128) return launch<128>(ta, tb, batch, M, N, K, ep, s);

@@ -63,9 +63,12 @@ __global__ void k_gelu(const float *__restrict__ z, void *__restrict__ a, long l
 }
 
 __global__ void k_gelu_bwd(const float *__restrict__ z, const void *__restrict__ da, int dat, float *__restrict__ dz,
-                           long long n) {
+                           __nv_bfloat16 *__restrict__ dzb, long long n) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dz[i] = ldv(da, i, dat) * gelu_d(z[i]);
+    if (i >= n) return;
+    float g = ldv(da, i, dat) * gelu_d(z[i]);
+    dz[i] = g;
+    if (dzb) dzb[i] = __float2bfloat16_rn(g);
 }
 
 // Forward DFT bookkeeping.  Y[(b, c, kp)][q] holds, for the W-transformed
@@ -174,6 +177,26 @@ __global__ void k_colsum(const float *__restrict__ X, float *__restrict__ out, l
     if (threadIdx.x == 0) out[c] = (accum ? out[c] : 0.0f) + red[0];
 }
 
+// column sums, stage 1: block b sums rows [b*rpb, (b+1)*rpb) of a row-major
+// matrix whose column count divides the block size (coalesced reads; each
+// thread stays on one column), partial[b][c]
+__global__ void k_colsum_part(const float *__restrict__ X, float *__restrict__ part, long long rows, int cols,
+                              long long rpb) {
+    __shared__ float red[TB];
+    const long long r0 = (long long)blockIdx.x * rpb, r1 = min(rows, r0 + rpb);
+    const int per = TB / cols; // rows per pass
+    const int c = threadIdx.x % cols, rr = threadIdx.x / cols;
+    float s = 0.0f;
+    for (long long r = r0 + rr; r < r1; r += per) s += X[r * cols + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < cols) {
+        float t = 0.0f;
+        for (int q = 0; q < per; ++q) t += red[q * cols + threadIdx.x];
+        part[(long long)blockIdx.x * cols + threadIdx.x] = t;
+    }
+}
+
 __global__ void k_sum_batches(const float *__restrict__ src, float *__restrict__ dst, int nb, long long n, int accum) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -197,14 +220,16 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
 // mean-squared error over n values; loss accumulated in FP64, gradient
 // scale * 2 (pred - target) / n written as BF16 for the backward GEMMs
 __global__ void k_mse(const float *__restrict__ pred, const float *__restrict__ target, void *__restrict__ dpred,
-                      int dt, double *__restrict__ loss, long long n, float scale) {
+                      int dt, double *__restrict__ loss, long long n, float scale, const float *__restrict__ w,
+                      long long w_period, int w_len) {
     __shared__ double red[TB];
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0.0;
     if (i < n) {
         float d = pred[i] - target[i];
-        e = (double)d * d;
-        if (dpred) stv(dpred, i, dt, scale * 2.0f * d / (float)n);
+        float wi = w ? w[(i / w_period) % w_len] : 1.0f;
+        e = (double)wi * d * d;
+        if (dpred) stv(dpred, i, dt, scale * 2.0f * wi * d / (float)n);
     }
     red[threadIdx.x] = e;
     __syncthreads();
@@ -330,9 +355,9 @@ int gf_fno_gelu(const float *z, void *a, long long n, int a_bf16, void *stream) 
     FNO_RET(stream);
 }
 
-int gf_fno_gelu_bwd(const float *z, const void *da, int da_bf16, float *dz, long long n, void *stream) {
+int gf_fno_gelu_bwd(const float *z, const void *da, int da_bf16, float *dz, void *dz_bf16, long long n, void *stream) {
     if (!z || !da || !dz || n < 0) return GF_FNO_ERR_ARG;
-    if (n) k_gelu_bwd<<<nblk(n), TB, 0, (cudaStream_t)stream>>>(z, da, da_bf16, dz, n);
+    if (n) k_gelu_bwd<<<nblk(n), TB, 0, (cudaStream_t)stream>>>(z, da, da_bf16, dz, (__nv_bfloat16 *)dz_bf16, n);
     FNO_RET(stream);
 }
 
@@ -366,7 +391,24 @@ int gf_fno_modes_grad(const float *dRm, float *dR, int modes, int C, void *strea
 
 int gf_fno_colsum(const float *X, float *out, long long rows, int cols, int accum, void *stream) {
     if (!X || !out || rows < 1 || cols < 1) return GF_FNO_ERR_ARG;
-    k_colsum<<<(unsigned)cols, TB, 0, (cudaStream_t)stream>>>(X, out, rows, cols, accum);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cols <= TB && TB % cols == 0 && rows >= 4096) {
+        // two stages through a fixed scratch of 1024 partial rows
+        static float *part = nullptr;
+        static int part_cols = 0;
+        const int nb = 1024;
+        if (!part || part_cols < cols) {
+            if (part) cudaFree(part);
+            part = nullptr;
+            if (cudaMalloc(&part, sizeof(float) * nb * TB) != cudaSuccess) return GF_FNO_ERR_CUDA;
+            part_cols = TB;
+        }
+        long long rpb = (rows + nb - 1) / nb;
+        k_colsum_part<<<nb, TB, 0, st>>>(X, part, rows, cols, rpb);
+        k_sum_batches<<<nblk(cols), TB, 0, st>>>(part, out, nb, cols, accum);
+    } else {
+        k_colsum<<<(unsigned)cols, TB, 0, st>>>(X, out, rows, cols, accum);
+    }
     FNO_RET(stream);
 }
 
@@ -387,7 +429,15 @@ int gf_fno_adam(float *p, const float *g, float *m, float *v, long long n, float
 int gf_fno_mse(const float *pred, const float *target, void *dpred, int dpred_bf16, double *loss, long long n,
                float scale, void *stream) {
     if (!pred || !target || !loss || n < 1) return GF_FNO_ERR_ARG;
-    k_mse<<<nblk(n), TB, 0, (cudaStream_t)stream>>>(pred, target, dpred, dpred_bf16, loss, n, scale);
+    k_mse<<<nblk(n), TB, 0, (cudaStream_t)stream>>>(pred, target, dpred, dpred_bf16, loss, n, scale, nullptr, 1, 1);
+    FNO_RET(stream);
+}
+
+int gf_fno_mse_weighted(const float *pred, const float *target, void *dpred, int dpred_bf16, double *loss,
+                        long long n, float scale, const float *w, long long w_period, int w_len, void *stream) {
+    if (!pred || !target || !loss || !w || n < 1 || w_period < 1 || w_len < 1) return GF_FNO_ERR_ARG;
+    k_mse<<<nblk(n), TB, 0, (cudaStream_t)stream>>>(pred, target, dpred, dpred_bf16, loss, n, scale, w, w_period,
+                                                   w_len);
     FNO_RET(stream);
 }
 

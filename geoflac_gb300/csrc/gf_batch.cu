@@ -474,7 +474,20 @@ struct gf_batch {
         cudaGraphExec_t exec;
     };
     std::vector<Graph> graphs;
+    // device copy of the fields gf_batch_inject overwrites (restore point)
+    void *backup = nullptr;
+    std::vector<size_t> backup_off;
 };
+
+namespace {
+// (device pointer, bytes) of every field of member v that injection writes
+std::vector<std::pair<void *, size_t>> injected_fields(const GfMemberView &v) {
+    const size_t N = (size_t)v.d.N, E = (size_t)v.d.E;
+    return {{v.A.vel, 2 * N * sizeof(double)},    {v.A.temp, N * sizeof(double)},
+            {v.A.cord, 2 * N * sizeof(double)},   {v.A.stress0, 16 * E * sizeof(float)},
+            {v.A.aps, E * sizeof(float)},         {v.A.area, 4 * E * sizeof(float)}};
+}
+} // namespace
 
 namespace {
 
@@ -679,6 +692,7 @@ void gf_batch_destroy(gf_batch *b) {
         if (b->d_tiles[k]) cudaFree(b->d_tiles[k]);
     if (b->d_members) cudaFree(b->d_members);
     if (b->d_sync) cudaFree(b->d_sync);
+    if (b->backup) cudaFree(b->backup);
     if (b->s) cudaStreamDestroy(b->s);
     delete b;
 }
@@ -818,6 +832,44 @@ int gf_batch_inject(gf_batch *b, const float *grid, int H, int W) {
         k_inject_elems<<<b->ntile[K_E], T, 0, b->s>>>(g, b->d_tiles[K_E], b->ntile[K_E], ipt, nullptr);
     GB_CK(cudaGetLastError());
     return check_status(b);
+}
+
+int gf_batch_backup(gf_batch *b) {
+    if (!b) return GF_ERR_ARG;
+    for (const GfMemberView &v : b->views) GB_CK(cudaStreamSynchronize(v.s));
+    if (!b->backup) {
+        size_t total = 0;
+        b->backup_off.clear();
+        for (const GfMemberView &v : b->views) {
+            b->backup_off.push_back(total);
+            for (auto &f : injected_fields(v)) total += (f.second + 255) & ~(size_t)255;
+        }
+        GB_CK(cudaMalloc(&b->backup, total));
+    }
+    for (size_t m = 0; m < b->views.size(); ++m) {
+        size_t off = b->backup_off[m];
+        for (auto &f : injected_fields(b->views[m])) {
+            GB_CK(cudaMemcpyAsync((char *)b->backup + off, f.first, f.second, cudaMemcpyDeviceToDevice, b->s));
+            off += (f.second + 255) & ~(size_t)255;
+        }
+    }
+    return GF_OK;
+}
+
+int gf_batch_restore(gf_batch *b, const int *members, int count) {
+    if (!b || (count > 0 && !members)) return GF_ERR_ARG;
+    if (!b->backup) return GF_ERR_ARG;
+    for (int k = 0; k < count; ++k) {
+        int m = members[k];
+        if (m < 0 || m >= (int)b->views.size()) return GF_ERR_ARG;
+        size_t off = b->backup_off[m];
+        for (auto &f : injected_fields(b->views[m])) {
+            GB_CK(cudaMemcpyAsync(f.first, (char *)b->backup + off, f.second, cudaMemcpyDeviceToDevice, b->s));
+            off += (f.second + 255) & ~(size_t)255;
+        }
+    }
+    GB_CK(cudaStreamSynchronize(b->s));
+    return GF_OK;
 }
 
 int gf_batch_force_residual(gf_batch *b, double *residual) {

@@ -39,7 +39,8 @@ def _lib():
         "gf_fno_transpose": [vp, vp, i, ll, i, i, i, vp],
         "gf_fno_cast": [vp, vp, ll, i, i, vp],
         "gf_fno_gelu": [vp, vp, ll, i, vp],
-        "gf_fno_gelu_bwd": [vp, vp, i, vp, ll, vp],
+        "gf_fno_gelu_bwd": [vp, vp, i, vp, vp, ll, vp],
+        "gf_gemm_bf16_ex": [vp, vp, vp, i, i, i, i, ll, ll, ll, ll, ll, ll, i, f, f, vp, vp, i, vp],
         "gf_fno_spec_combine": [vp, vp, i, i, i, i, vp],
         "gf_fno_spec_combine_bwd": [vp, vp, i, i, i, i, vp],
         "gf_fno_expand_modes": [vp, vp, vp, i, i, vp],
@@ -48,6 +49,7 @@ def _lib():
         "gf_fno_sum_batches": [vp, vp, i, ll, i, vp],
         "gf_fno_adam": [vp, vp, vp, vp, ll, f, f, f, f, i, f, vp],
         "gf_fno_mse": [vp, vp, vp, i, vp, ll, f, vp],
+        "gf_fno_mse_weighted": [vp, vp, vp, i, vp, ll, f, vp, ll, i, vp],
         "gf_fno_add": [vp, vp, vp, vp, ll, vp],
         "gf_fno_pack_input": [vp, vp, vp, vp, i, i, i, vp],
         "gf_fno_pack_target": [vp, vp, vp, vp, ll, vp],
@@ -175,14 +177,15 @@ class Fno:
     def s(self):
         return self.torch.cuda.current_stream().cuda_stream
 
-    def gemm(self, A, B, Cout, batch, M, N, K, lda, sA, ldb, sB, ldc, sC, alpha=1.0, beta=0.0, bias=None):
+    def gemm(self, A, B, Cout, batch, M, N, K, lda, sA, ldb, sB, ldc, sC, alpha=1.0, beta=0.0, bias=None,
+             aux=None, act=0):
         c_bf16 = 1 if Cout.dtype == self.torch.bfloat16 else 0
-        _ck(self.lib.gf_gemm_bf16(_p(A), _p(B), _p(Cout), batch, M, N, K, lda, sA, ldb, sB, ldc, sC, c_bf16,
-                                  alpha, beta, _p(bias), self.s), "gemm")
+        _ck(self.lib.gf_gemm_bf16_ex(_p(A), _p(B), _p(Cout), batch, M, N, K, lda, sA, ldb, sB, ldc, sC, c_bf16,
+                                     alpha, beta, _p(bias), _p(aux), act, self.s), "gemm")
 
-    def mm(self, A, Bw, out, M, N, K, beta=0.0, bias=None):
-        """out[M, N] (+)= A[M, K] Bw[N, K]^T (+ bias)."""
-        self.gemm(A, Bw, out, 1, M, N, K, K, 0, K, 0, N, 0, 1.0, beta, bias)
+    def mm(self, A, Bw, out, M, N, K, beta=0.0, bias=None, aux=None, act=0):
+        """out[M, N] (+)= A[M, K] Bw[N, K]^T (+ bias); aux = BF16 out or GELU(out)."""
+        self.gemm(A, Bw, out, 1, M, N, K, K, 0, K, 0, N, 0, 1.0, beta, bias, aux, act)
 
     def tr(self, src, dst, batch, rows, cols):
         _ck(self.lib.gf_fno_transpose(_p(src), _p(dst), batch, rows, cols,
@@ -203,9 +206,9 @@ class Fno:
     def gelu(self, z, out):
         _ck(self.lib.gf_fno_gelu(_p(z), _p(out), z.numel(), int(out.dtype == self.torch.bfloat16), self.s), "gelu")
 
-    def gelu_bwd(self, z, da, dz):
-        _ck(self.lib.gf_fno_gelu_bwd(_p(z), _p(da), int(da.dtype == self.torch.bfloat16), _p(dz), z.numel(),
-                                     self.s), "gelu_bwd")
+    def gelu_bwd(self, z, da, dz, dz_b=None):
+        _ck(self.lib.gf_fno_gelu_bwd(_p(z), _p(da), int(da.dtype == self.torch.bfloat16), _p(dz), _p(dz_b),
+                                     z.numel(), self.s), "gelu_bwd")
 
     def colsum(self, X, out, rows, cols):
         _ck(self.lib.gf_fno_colsum(_p(X), _p(out), rows, cols, 0, self.s), "colsum")
@@ -256,10 +259,9 @@ class Fno:
         self.mm(Vt, self.mat["IH"], Z, B * Cc * m2, 2 * H, 2 * Q)
         Zt = torch.empty((B, H, Cc, 2 * m2), dtype=bf, device="cuda")
         self.tr_pairs(Z, Zt, B, Cc * m2, H)
-        s = torch.empty((B, H, Cc, W), dtype=torch.float32, device="cuda")
-        self.mm(Zt, self.mat["IW"], s, B * H * Cc, W, 2 * m2)
+        # s[b, h] = IW Zt[b, h]^T, channels last: one IW for all (b, h)
         s_cl = torch.empty((B, H, W, Cc), dtype=torch.float32, device="cuda")
-        self.tr(s, s_cl, B * H, Cc, W)
+        self.gemm(self.mat["IW"], Zt, s_cl, B * H, W, Cc, 2 * m2, 2 * m2, -1, 2 * m2, Cc * 2 * m2, Cc, W * Cc)
         if save:
             return s_cl, (U, RmT)
         return s_cl, None
@@ -273,27 +275,24 @@ class Fno:
         wb = {k: self.bf16(self.p[k]) for k in self.p if not k.startswith("R") and not k.endswith("_b")
               and not (k.startswith("b") and k[1:].isdigit())}
         z = torch.empty((M, cfg.C), dtype=torch.float32, device="cuda")
-        self.mm(x.view(M, cfg.cin), wb["lift_w"], z, M, cfg.C, cfg.cin, bias=self.p["lift_b"])
-        v = self.bf16(z)
+        v = torch.empty((M, cfg.C), dtype=bf, device="cuda")
+        self.mm(x.view(M, cfg.cin), wb["lift_w"], z, M, cfg.C, cfg.cin, bias=self.p["lift_b"], aux=v)
         saved = {"x": x, "v": [], "z": [], "spec": [], "wb": wb}
         for l in range(cfg.layers):
             s_cl, sp = self.spectral(v.view(B, cfg.H, cfg.W, cfg.C), l, B, train)
             zl = s_cl.view(M, cfg.C)
-            self.mm(v, wb[f"w{l}"], zl, M, cfg.C, cfg.C, beta=1.0, bias=self.p[f"b{l}"])
+            vn = torch.empty((M, cfg.C), dtype=bf, device="cuda")
+            # z = v W^T + b + S(v); next input GELU(z) (z itself after the last layer)
+            self.mm(v, wb[f"w{l}"], zl, M, cfg.C, cfg.C, beta=1.0, bias=self.p[f"b{l}"], aux=vn,
+                    act=1 if l < cfg.layers - 1 else 0)
             if train:
                 saved["v"].append(v)
                 saved["z"].append(zl)
                 saved["spec"].append(sp)
-            vn = torch.empty((M, cfg.C), dtype=bf, device="cuda")
-            if l < cfg.layers - 1:
-                self.gelu(zl, vn)
-            else:
-                _ck(self.lib.gf_fno_cast(_p(zl), _p(vn), zl.numel(), 0, 1, self.s), "cast")
             v = vn
         zp = torch.empty((M, cfg.P), dtype=torch.float32, device="cuda")
-        self.mm(v, wb["p1_w"], zp, M, cfg.P, cfg.C, bias=self.p["p1_b"])
         hh = torch.empty((M, cfg.P), dtype=bf, device="cuda")
-        self.gelu(zp, hh)
+        self.mm(v, wb["p1_w"], zp, M, cfg.P, cfg.C, bias=self.p["p1_b"], aux=hh, act=1)
         out = torch.empty((M, cfg.cout), dtype=torch.float32, device="cuda")
         self.mm(hh, wb["p2_w"], out, M, cfg.cout, cfg.P, bias=self.p["p2_b"])
         if train:
@@ -359,8 +358,8 @@ class Fno:
         dh = torch.empty((M, cfg.P), dtype=torch.float32, device="cuda")
         self.mm(d2, p2T, dh, M, cfg.P, cfg.cout)
         dzp = torch.empty_like(dh)
-        self.gelu_bwd(sv["zp"], dh, dzp)
-        dzp_b = self.bf16(dzp)
+        dzp_b = torch.empty(dh.shape, dtype=bf, device="cuda")
+        self.gelu_bwd(sv["zp"], dh, dzp, dzp_b)
         self.wgrad(dzp_b, sv["vL"], M, cfg.P, cfg.C, self.g["p1_w"])
         self.colsum(dzp, self.g["p1_b"], M, cfg.P)
         p1T = torch.empty((cfg.C, cfg.P), dtype=bf, device="cuda")
@@ -371,10 +370,11 @@ class Fno:
             zl = sv["z"][l]
             if l < cfg.layers - 1:
                 dz = torch.empty_like(dv)
-                self.gelu_bwd(zl, dv, dz)
+                dz_b = torch.empty(dv.shape, dtype=bf, device="cuda")
+                self.gelu_bwd(zl, dv, dz, dz_b)
             else:
                 dz = dv
-            dz_b = self.bf16(dz)
+                dz_b = self.bf16(dz)
             self.wgrad(dz_b, sv["v"][l], M, cfg.C, cfg.C, self.g[f"w{l}"])
             self.colsum(dz, self.g[f"b{l}"], M, cfg.C)
             dv_spec = self.spectral_bwd(dz.view(B, cfg.H, cfg.W, cfg.C), l, B, sv["spec"][l])
@@ -388,12 +388,17 @@ class Fno:
         self.saved = None
         return self.g
 
-    def loss_grad(self, out, target):
-        """mean-squared error and its BF16 gradient w.r.t. the output"""
+    def loss_grad(self, out, target, weight=None):
+        """mean-squared error (optionally weighted per pixel and channel of one
+        sample, weight [H, W, cout]) and its BF16 gradient w.r.t. the output"""
         torch = self.torch
         loss = torch.zeros(1, dtype=torch.float64, device="cuda")
         dout = torch.empty(out.shape, dtype=torch.bfloat16, device="cuda")
-        _ck(self.lib.gf_fno_mse(_p(out), _p(target), _p(dout), 1, _p(loss), out.numel(), 1.0, self.s), "mse")
+        if weight is None:
+            _ck(self.lib.gf_fno_mse(_p(out), _p(target), _p(dout), 1, _p(loss), out.numel(), 1.0, self.s), "mse")
+        else:
+            _ck(self.lib.gf_fno_mse_weighted(_p(out), _p(target), _p(dout), 1, _p(loss), out.numel(), 1.0,
+                                             _p(weight), 1, weight.numel(), self.s), "mse")
         return loss, dout
 
     def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):

@@ -104,11 +104,15 @@ class Surrogate:
                                        self.cfg.W, self.s), "pack_input")
 
     def train(self, snaps: Snapshots, epochs: int, batch: int = 64, lr: float = 1e-3, seed: int = 0,
-              max_pairs: Optional[int] = None) -> Dict[str, float]:
-        """Adam over all (t, t + interval) pairs, cosine learning rate."""
+              max_pairs: Optional[int] = None, surface_weight: float = 16.0) -> Dict[str, float]:
+        """Adam over all (t, t + interval) pairs, cosine learning rate; the
+        displacement channel of the top grid rows (the topography) is
+        weighted by `surface_weight` in the loss."""
         import torch
 
         cfg = self.cfg
+        wgt = torch.ones((cfg.H, cfg.W, cfg.cout), dtype=torch.float32, device="cuda")
+        wgt[:2, :, 8] = surface_weight
         n, ns = snaps.grids.shape[0], snaps.grids.shape[1]
         pairs = [(m, k) for m in range(n) for k in range(ns - 1)]
         if max_pairs:
@@ -139,7 +143,7 @@ class Surrogate:
                 _ck(self.lib.gf_fno_pack_target(_p(yb), _p(xb), _p(self.norm.stats_d), _p(tgt),
                                                 batch * cfg.H * cfg.W, self.s), "pack_target")
                 out = self.net.forward(inp, train=True)
-                loss, dout = self.net.loss_grad(out, tgt)
+                loss, dout = self.net.loss_grad(out, tgt, wgt)
                 self.net.backward(dout)
                 lr_t = 0.5 * lr * (1.0 + math.cos(math.pi * it / max(steps, 1)))
                 self.net.adam(lr=lr_t)
@@ -213,8 +217,7 @@ def screen(batch: Batch, sur: Surrogate, prms: List[dict], interval: int, tol: f
     H, W = cfg.H, cfg.W
     torch.cuda.synchronize()
     t0 = time.time()
-    for m in batch.members:  # restore point for the members the gate rejects
-        m.download()
+    batch.backup()  # restore point for the members the gate rejects
     t_save = time.time() - t0
     raw = torch.empty((n, H, W, NCH), dtype=torch.float32, device="cuda")
     batch.sample(raw, H, W, CRUST_PHASE)
@@ -230,8 +233,7 @@ def screen(batch: Batch, sur: Surrogate, prms: List[dict], interval: int, tol: f
     out = pred
     if len(fail):
         sub = [batch.members[k] for k in fail]
-        for m in sub:
-            m.upload()
+        batch.restore(fail)
         sb = Batch(sub)
         sb.set_config(**{k: v for k, v in batch.config().items()})
         sb.step(interval)

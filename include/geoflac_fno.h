@@ -26,6 +26,12 @@ extern "C" {
 int gf_gemm_bf16(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda, long long sA,
                  long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha, float beta,
                  const float *bias, void *stream);
+/* The same with two extensions: sA = -1 shares one A among all batches,
+ * and (FP32 C only) aux, if not NULL, receives a BF16 copy of the final C
+ * (act = 0) or of GELU(C) (act = 1) in the same layout. */
+int gf_gemm_bf16_ex(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda,
+                    long long sA, long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha,
+                    float beta, const float *bias, void *aux, int act, void *stream);
 /* GF_FNO_ERR_TIMEOUT if a GEMM kernel gave up a wait since the last call. */
 int gf_gemm_error(void);
 
@@ -34,9 +40,9 @@ int gf_gemm_error(void);
 int gf_fno_transpose(const void *src, void *dst, int batch, long long rows, int cols, int src_bf16, int dst_bf16,
                      void *stream);
 int gf_fno_cast(const void *src, void *dst, long long n, int src_bf16, int dst_bf16, void *stream);
-/* a = GELU(z) (erf form); dz = da * GELU'(z). */
+/* a = GELU(z) (erf form); dz = da * GELU'(z), with an optional BF16 copy. */
 int gf_fno_gelu(const float *z, void *a, long long n, int a_bf16, void *stream);
-int gf_fno_gelu_bwd(const float *z, const void *da, int da_bf16, float *dz, long long n, void *stream);
+int gf_fno_gelu_bwd(const float *z, const void *da, int da_bf16, float *dz, void *dz_bf16, long long n, void *stream);
 /* Complex bookkeeping of the truncated 2-D DFT.  Y[(b, c, kp)][q]: for the
  * W-transformed row kp (kp < m2 real part, kp >= m2 imaginary part of W-mode
  * kp mod m2), cosine (q < Q) and sine (q >= Q) sums over the rows h of the Q
@@ -73,6 +79,9 @@ int gf_fno_gather_rows(const void *src, void *dst, const long long *idx, int nro
                        void *stream);
 /* Prediction back to fields: y = x + mean_d + std_d * pred. */
 int gf_fno_unpack(const float *pred, const float *x, const float *stats_d, float *y, long long points, void *stream);
+/* The same with weights: term i weighted by w[(i / w_period) % w_len]. */
+int gf_fno_mse_weighted(const float *pred, const float *target, void *dpred, int dpred_bf16, double *loss,
+                        long long n, float scale, const float *w, long long w_period, int w_len, void *stream);
 /* out = x + y (y may be NULL), FP32 and/or BF16 outputs. */
 int gf_fno_add(const float *x, const float *y, float *out, void *out_bf16, long long n, void *stream);
 

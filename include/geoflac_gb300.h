@@ -351,6 +351,11 @@ int gf_batch_inject(gf_batch *b, const float *grid, int H, int W);
  * without damping): sum over free nodes of |F| divided by the sum of
  * |gravity| and the magnitudes of the stress-divergence terms. */
 int gf_batch_force_residual(gf_batch *b, double *residual);
+/* Device copy of the fields gf_batch_inject writes, for every member (the
+ * copy is allocated at the first call and kept), and the restore of the
+ * listed members from it. */
+int gf_batch_backup(gf_batch *b);
+int gf_batch_restore(gf_batch *b, const int *members, int count);
 long long gf_batch_elements(gf_batch *b);
 int gf_batch_grid(gf_batch *b);
 

@@ -64,3 +64,23 @@ def test_gemm_rejects_unaligned_strides():
     # K = 12 is not a multiple of 8: the TMA row stride would be 24 bytes
     assert lib.gf_gemm_bf16(A.data_ptr(), A.data_ptr(), out.data_ptr(), 1, 64, 64, 12, 12, 0, 12, 0, 64, 0, 0,
                             1.0, 0.0, None, None) == -3
+
+
+def test_gemm_broadcast_a_and_fused_gelu_copy():
+    """sA = -1 shares A among the batches; aux receives BF16 GELU(C)."""
+    torch = pytest.importorskip("torch")
+    from geoflac_gb300.fno import _lib
+    lib = _lib()
+    A = torch.randn(1, 384, 48).to(torch.bfloat16).cuda()
+    B = torch.randn(37, 64, 48).to(torch.bfloat16).cuda()
+    bias = torch.randn(64).cuda()
+    C0 = torch.randn(37, 384, 64).cuda()
+    out = C0.clone()
+    aux = torch.empty(37, 384, 64, dtype=torch.bfloat16, device="cuda")
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), out.data_ptr(), 37, 384, 64, 48, 48, -1, 48, 64 * 48, 64,
+                               384 * 64, 0, 1.0, 1.0, bias.data_ptr(), aux.data_ptr(), 1, None) == 0
+    torch.cuda.synchronize()
+    ref = torch.matmul(A.float().expand(37, -1, -1), B.float().transpose(1, 2)) + C0 + bias
+    assert (out - ref).abs().max().item() / ref.abs().max().item() <= 2e-3
+    g = torch.nn.functional.gelu(ref)
+    assert (aux.float() - g).abs().max().item() / g.abs().max().item() <= 1e-2
