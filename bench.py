@@ -257,6 +257,11 @@ def run_ours(args):
         print(json.dumps({"profile": args.profile, "steps": args.warmup + args.steps, "launches": g.launches}))
         g.close()
         return
+    if args.only == "surrogate":  # development: the surrogate leg alone
+        args.batch_cfg = dict(threads=256, items_per_thread=2, ctas_per_sm=2, graph_steps=10)
+        print(json.dumps({"metric": METRIC, "partial": "surrogate leg only",
+                          "surrogate": bench_surrogate(args, d)}))
+        return
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     E = 1000 * 300
     res = {}
@@ -434,8 +439,10 @@ def bench_surrogate(args, workdir: str):
            "modes": [cfg.m1, cfg.m2], "layers": cfg.layers, "training_pairs": pairs, "epochs": args.sur_epochs,
            "train_seconds": info["seconds"], "train_loss_first": info["first_loss"],
            "train_loss_final": info["final_loss"], "data_seconds": t_data,
-           "plain_seconds": t_plain, "screen_seconds": res["seconds"], "screen_predict_seconds": res["seconds_predict"],
-           "screen_save_seconds": res["seconds_save"], "rerun_members": len(res["rerun"]),
+           "plain_seconds": t_plain, "screen_seconds": res["seconds"],
+           "screen_breakdown": {k[8:]: v for k, v in res.items() if k.startswith("seconds_")},
+           "rerun_members": len(res["rerun"]), "rerun_detail": res["rerun_detail"],
+           "rerun_elements": [int((fb[k][0].params.nx - 1) * (fb[k][0].params.nz - 1)) for k in res["rerun"]],
            "speedup_vs_plain": t_plain / res["seconds"],
            "gate": {k: v for k, v in cal.items()},
            "rel_err": {k: {"median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)), "max": float(np.max(v))}
@@ -545,12 +552,13 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
-    ap.add_argument("--sur-epochs", type=int, default=20, help="surrogate training epochs (0: skip the surrogate)")
+    ap.add_argument("--sur-epochs", type=int, default=30, help="surrogate training epochs (0: skip the surrogate)")
     ap.add_argument("--sur-snaps", type=int, default=17, help="snapshots per member (pairs = members x (snaps - 1))")
     ap.add_argument("--sur-interval", type=int, default=500, help="steps between snapshots and of the forecast")
     ap.add_argument("--sur-start", type=int, default=1000, help="plain steps of the fresh sweep before the forecast")
     ap.add_argument("--sur-lr", type=float, default=2e-3)
     ap.add_argument("--fno-batch", type=int, default=64, help="batch of the fno profiling run")
+    ap.add_argument("--only", choices=["surrogate"], default=None, help="run one leg only (development)")
     ap.add_argument("--profile", choices=["fp64", "mixed", "batch", "fno"], default=None,
                     help="run warmup+steps steps of one mode and nothing else (for ncu)")
     args = ap.parse_args()

@@ -104,7 +104,7 @@ class Surrogate:
                                        self.cfg.W, self.s), "pack_input")
 
     def train(self, snaps: Snapshots, epochs: int, batch: int = 64, lr: float = 1e-3, seed: int = 0,
-              max_pairs: Optional[int] = None, surface_weight: float = 16.0) -> Dict[str, float]:
+              max_pairs: Optional[int] = None, surface_weight: float = 64.0) -> Dict[str, float]:
         """Adam over all (t, t + interval) pairs, cosine learning rate; the
         displacement channel of the top grid rows (the topography) is
         weighted by `surface_weight` in the loss."""
@@ -220,32 +220,47 @@ def screen(batch: Batch, sur: Surrogate, prms: List[dict], interval: int, tol: f
     batch.backup()  # restore point for the members the gate rejects
     t_save = time.time() - t0
     raw = torch.empty((n, H, W, NCH), dtype=torch.float32, device="cuda")
+    ts = time.time()
     batch.sample(raw, H, W, CRUST_PHASE)
     torch.cuda.synchronize()
     t1 = time.time()
+    t_sample = t1 - ts
     pred = sur.predict(raw, params_array(prms))
     torch.cuda.synchronize()
     t_pred = time.time() - t1
+    ti = time.time()
     batch.inject(pred, H, W)
+    t_inject = time.time() - ti
+    ti = time.time()
     resid = batch.force_residual()
+    t_resid = time.time() - ti
     fail = np.nonzero(resid > tol)[0]
     t2 = time.time()
     out = pred
+    rr = {}
     if len(fail):
         sub = [batch.members[k] for k in fail]
         batch.restore(fail)
         sb = Batch(sub)
         sb.set_config(**{k: v for k, v in batch.config().items()})
+        rr["prepare"] = time.time() - t2
+        stream = torch.cuda.ExternalStream(sb.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
         sb.step(interval)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rr["step_host"] = time.time() - t2 - rr["prepare"]
+        rr["step_gpu"] = e0.elapsed_time(e1) / 1e3
         g = torch.empty((len(sub), H, W, NCH), dtype=torch.float32, device="cuda")
         sb.sample(g, H, W, CRUST_PHASE)
         torch.cuda.synchronize()
-        idx = torch.from_numpy(fail.astype(np.int64)).cuda()
-        out = pred.clone()
-        out[idx] = g
+        for r, k in enumerate(fail):  # plain results replace the rejected forecasts (device copies)
+            out[int(k)].copy_(g[r])
         sb.close()
     torch.cuda.synchronize()
     t_rerun = time.time() - t2
-    return {"fields": out, "raw_t": raw, "residual": resid, "rerun": fail.tolist(),
-            "seconds": time.time() - t0, "seconds_save": t_save, "seconds_predict": t_pred,
+    return {"fields": out, "raw_t": raw, "residual": resid, "rerun": fail.tolist(), "rerun_detail": rr,
+            "seconds": time.time() - t0, "seconds_save": t_save, "seconds_sample": t_sample,
+            "seconds_predict": t_pred, "seconds_inject": t_inject, "seconds_residual": t_resid,
             "seconds_rerun": t_rerun}
