@@ -336,10 +336,19 @@ __global__ void k_inject_nodes(GridArgs g, const int2 *tiles, int ntile, int ipt
             if (n >= m.d.N) continue;
             const int j = (int)(n % m.d.nz), i = (int)(n / m.d.nz);
             const float fx = (float)i * g.W / (m.d.nx - 1) - 0.5f, fy = (float)j * g.H / (m.d.nz - 1) - 0.5f;
-            m.A.vel[n] = grid_at(g, tl.x, fy, fx, 0);
-            m.A.vel[m.d.N + n] = grid_at(g, tl.x, fy, fx, 1);
+            const double vx = grid_at(g, tl.x, fy, fx, 0), vz = grid_at(g, tl.x, fy, fx, 1);
+            const double z = m.z0 + m.rzbo * (double)j / (double)(m.d.nz - 1) + (double)grid_at(g, tl.x, fy, fx, 8);
+            m.A.vel[n] = vx;
+            m.A.vel[m.d.N + n] = vz;
             m.A.temp[n] = grid_at(g, tl.x, fy, fx, 6);
-            m.A.cord[m.d.N + n] = m.z0 + m.rzbo * (double)j / (double)(m.d.nz - 1) + (double)grid_at(g, tl.x, fy, fx, 8);
+            m.A.cord[m.d.N + n] = z;
+            const float hx = (float)vx, hz = (float)vz, hc = (float)z;
+            m.A.vel_hi[n] = hx;
+            m.A.vel_lo[n] = (float)(vx - (double)hx);
+            m.A.vel_hi[m.d.N + n] = hz;
+            m.A.vel_lo[m.d.N + n] = (float)(vz - (double)hz);
+            m.A.cord_hi[m.d.N + n] = hc;
+            m.A.cord_lo[m.d.N + n] = (float)(z - (double)hc);
         }
     }
 }
@@ -485,7 +494,9 @@ std::vector<std::pair<void *, size_t>> injected_fields(const GfMemberView &v) {
     const size_t N = (size_t)v.d.N, E = (size_t)v.d.E;
     return {{v.A.vel, 2 * N * sizeof(double)},    {v.A.temp, N * sizeof(double)},
             {v.A.cord, 2 * N * sizeof(double)},   {v.A.stress0, 16 * E * sizeof(float)},
-            {v.A.aps, E * sizeof(float)},         {v.A.area, 4 * E * sizeof(float)}};
+            {v.A.aps, E * sizeof(float)},         {v.A.area, 4 * E * sizeof(float)},
+            {v.A.cord_hi, 2 * N * sizeof(float)}, {v.A.cord_lo, 2 * N * sizeof(float)},
+            {v.A.vel_hi, 2 * N * sizeof(float)},  {v.A.vel_lo, 2 * N * sizeof(float)}};
 }
 } // namespace
 

@@ -170,6 +170,10 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
     } while (0)
     if (m & GF_F_CORD) T_(xfer(c, L.cord, A.cord, 2 * N, dir));
     if (m & GF_F_VEL) T_(xfer(c, L.vel, A.vel, 2 * N, dir));
+    if (dir && (m & (GF_F_CORD | GF_F_VEL)) && c->mode == GF_MODE_MIXED) {
+        GfLaunch g = launch_of(c);
+        GfKernels<float>::split_nodes(g);
+    }
     if (m & GF_F_TEMP) {
         T_(xfer(c, L.temp, A.temp, N, dir));
         T_(xfer(c, L.temp0, A.temp0, N, dir));
@@ -399,6 +403,7 @@ template <class R> int enqueue_remesh(gf_ctx *c) {
     GfLaunch g = launch_of(c);
     GfRemeshArgs a = remesh_args(c);
     GfRemesh<R>::regrid(g, a, c->rb);
+    GfKernels<R>::split_nodes(g); // new coordinates and interpolated velocities
     if (c->p.incoming_left == 1 || c->p.incoming_right == 1) {
         int rc = sidewall_temps(c);
         if (rc) return rc;
@@ -582,7 +587,13 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &b.d_scalars, 4));
         A_(mesh_templates(c));
     }
-    if (mode == GF_MODE_MIXED) A_(dalloc(c, &c->staging, 16 * E));
+    if (mode == GF_MODE_MIXED) {
+        A_(dalloc(c, &c->staging, 16 * E));
+        A_(dalloc(c, &A.cord_hi, 2 * N));
+        A_(dalloc(c, &A.cord_lo, 2 * N));
+        A_(dalloc(c, &A.vel_hi, 2 * N));
+        A_(dalloc(c, &A.vel_lo, 2 * N));
+    }
     DevParams P;
     fill_params(P, *p);
     A_(cuda_err(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice), "params"));

@@ -70,6 +70,9 @@ struct DevArrays {
     uint8_t *e_flag;                                  // change_phase element flags
     int *m_count, *m_offset;                          // marker2elem scan
     double *cord_old;                                 // remesh
+    // mixed: FP32 hi/lo splits of the FP64 coordinates and velocities
+    // (x = hi + lo), so differences of neighbouring values need no FP64
+    float *cord_hi, *cord_lo, *vel_hi, *vel_lo;
     int *nmarkers;                                    // device marker count
 };
 
@@ -101,6 +104,8 @@ template <class R> struct GfKernels {
     static void stress_out(const GfLaunch &g, double *dst);
     // count_phase_ratio of every element (marker2elem.f90:49)
     static void phase_recount_all(const GfLaunch &g);
+    // refresh the hi/lo splits after the FP64 coordinates / velocities changed
+    static void split_nodes(const GfLaunch &g);
 };
 
 // Remesh event (par.f90:94-110): host-prepared constants, passed by value.

@@ -70,6 +70,52 @@ __device__ __forceinline__ void load_quad(const double *__restrict__ cord, const
     q.y[3] = cord[d.N + n3 + 1];
 }
 
+// Mixed path: coordinates of a quad relative to its node 1, in FP32 from the
+// hi/lo splits (the hi difference of neighbouring nodes is exact, the lo
+// parts carry the rest), and velocities relative to node 1 the same way.
+struct QuadF {
+    float x[4], y[4];
+};
+
+__device__ __forceinline__ float hl_diff(const float *__restrict__ h, const float *__restrict__ l, long long a,
+                                         long long b) {
+    return (h[a] - h[b]) + (l[a] - l[b]);
+}
+
+__device__ __forceinline__ void quad_nodes(const GfDims &d, int j, int i, long long n[4]) {
+    n[0] = gf_node(d, j, i);
+    n[1] = n[0] + 1;
+    n[2] = gf_node(d, j, i + 1);
+    n[3] = n[2] + 1;
+}
+
+__device__ __forceinline__ void load_quad_rel(const DevArrays &A, const GfDims &d, int j, int i, QuadF &q) {
+    long long n[4];
+    quad_nodes(d, j, i, n);
+    const float *xh = A.cord_hi, *xl = A.cord_lo, *yh = A.cord_hi + d.N, *yl = A.cord_lo + d.N;
+    q.x[0] = 0.0f;
+    q.y[0] = 0.0f;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        q.x[k] = hl_diff(xh, xl, n[k], n[0]);
+        q.y[k] = hl_diff(yh, yl, n[k], n[0]);
+    }
+}
+
+__device__ __forceinline__ void load_vel_rel(const DevArrays &A, const GfDims &d, int j, int i, float vx[4],
+                                             float vy[4]) {
+    long long n[4];
+    quad_nodes(d, j, i, n);
+    const float *xh = A.vel_hi, *xl = A.vel_lo, *yh = A.vel_hi + d.N, *yl = A.vel_lo + d.N;
+    vx[0] = 0.0f;
+    vy[0] = 0.0f;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        vx[k] = hl_diff(xh, xl, n[k], n[0]);
+        vy[k] = hl_diff(yh, yl, n[k], n[0]);
+    }
+}
+
 // Shape-function derivatives of the four triangles (fl_rheol.f90:98-132):
 // dx[m][k], dz[m][k] for local vertex m of triangle k.  Coordinate
 // differences are taken in FP64, then rounded to R.
@@ -84,6 +130,19 @@ __device__ __forceinline__ void shape_derivs(const Quad &q, const R ar[4], R dx[
     dz[0][2] = R(x[3] - x[1]) * ar[2]; dz[1][2] = R(x[0] - x[3]) * ar[2]; dz[2][2] = R(x[1] - x[0]) * ar[2];
     dx[0][3] = R(y[3] - y[2]) * ar[3]; dx[1][3] = R(y[2] - y[0]) * ar[3]; dx[2][3] = R(y[0] - y[3]) * ar[3];
     dz[0][3] = R(x[2] - x[3]) * ar[3]; dz[1][3] = R(x[0] - x[2]) * ar[3]; dz[2][3] = R(x[3] - x[0]) * ar[3];
+}
+
+// the same from relative FP32 coordinates (only differences enter)
+__device__ __forceinline__ void shape_derivs_f(const QuadF &q, const float ar[4], float dx[3][4], float dz[3][4]) {
+    const float *x = q.x, *y = q.y;
+    dx[0][0] = (y[1] - y[2]) * ar[0]; dx[1][0] = (y[2] - y[0]) * ar[0]; dx[2][0] = (y[0] - y[1]) * ar[0];
+    dz[0][0] = (x[2] - x[1]) * ar[0]; dz[1][0] = (x[0] - x[2]) * ar[0]; dz[2][0] = (x[1] - x[0]) * ar[0];
+    dx[0][1] = (y[1] - y[3]) * ar[1]; dx[1][1] = (y[3] - y[2]) * ar[1]; dx[2][1] = (y[2] - y[1]) * ar[1];
+    dz[0][1] = (x[3] - x[1]) * ar[1]; dz[1][1] = (x[2] - x[3]) * ar[1]; dz[2][1] = (x[1] - x[2]) * ar[1];
+    dx[0][2] = (y[1] - y[3]) * ar[2]; dx[1][2] = (y[3] - y[0]) * ar[2]; dx[2][2] = (y[0] - y[1]) * ar[2];
+    dz[0][2] = (x[3] - x[1]) * ar[2]; dz[1][2] = (x[0] - x[3]) * ar[2]; dz[2][2] = (x[1] - x[0]) * ar[2];
+    dx[0][3] = (y[3] - y[2]) * ar[3]; dx[1][3] = (y[2] - y[0]) * ar[3]; dx[2][3] = (y[0] - y[3]) * ar[3];
+    dz[0][3] = (x[2] - x[3]) * ar[3]; dz[1][3] = (x[0] - x[2]) * ar[3]; dz[2][3] = (x[3] - x[0]) * ar[3];
 }
 
 // ---------------------------------------------------------------- matprops
@@ -148,17 +207,18 @@ __device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDi
     for (int k = 0; k < P.ninh100; ++k)
         if (i + 1 >= P.w_ix1[k] && i + 1 <= P.w_ix2[k] && j + 1 >= P.w_iy1[k] && j + 1 <= P.w_iy2[k])
             return (float)P.v_min;
-    const double *cord = A.cord, *temp = A.temp;
+    const float *zh = A.cord_hi + d.N;
+    const double *temp = A.temp;
     long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
-    double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
-    double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
-    float tmpr0 = 0.25f * float(temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
-    float tmpr = float(zsurf - zcord) * 1e-3f * 0.3f + tmpr0;
+    float zcord = 0.25f * (zh[n1] + zh[n1 + 1] + zh[n3] + zh[n3 + 1]);
+    float zsurf = 0.50f * (zh[gf_node(d, 0, i)] + zh[gf_node(d, 0, i + 1)]);
+    float tmpr0 = 0.25f * ((float)temp[n1] + (float)temp[n1 + 1] + (float)temp[n3] + (float)temp[n3 + 1]);
+    float tmpr = (zsurf - zcord) * 1e-3f * 0.3f + tmpr0;
     float s11 = 0.25f * (st[gf_s(d, e, 0, 0)] + st[gf_s(d, e, 0, 1)] + st[gf_s(d, e, 0, 2)] + st[gf_s(d, e, 0, 3)]);
     float s22 = 0.25f * (st[gf_s(d, e, 1, 0)] + st[gf_s(d, e, 1, 1)] + st[gf_s(d, e, 1, 2)] + st[gf_s(d, e, 1, 3)]);
     float s33 = 0.25f * (st[gf_s(d, e, 3, 0)] + st[gf_s(d, e, 3, 1)] + st[gf_s(d, e, 3, 2)] + st[gf_s(d, e, 3, 3)]);
     float pres = -(s11 + s22 + s33) / 3.0f + (float)A.p_ref[e]; // stored stresses are deviations from -p_ref
-    float zc = float(zcord);
+    float zc = zcord;
     float deptmpr410 = -101.58f * (tmpr + 273.0f) - 216828.0f;
     float deptmpr660 = 66.55f * (tmpr + 273.0f) - 788494.0f;
     float vmin = (float)P.v_min, vmax = (float)P.v_max;

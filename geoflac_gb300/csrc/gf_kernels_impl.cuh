@@ -31,17 +31,27 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     R *st = (R *)A.stress0;
     const R *area = (const R *)A.area;
 
-    const double *vel = A.vel;
     long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     R vx[4], vy[4];
-    vx[0] = R(vel[n1]); vx[1] = R(vel[n1 + 1]); vx[2] = R(vel[n3]); vx[3] = R(vel[n3 + 1]);
-    vy[0] = R(vel[d.N + n1]); vy[1] = R(vel[d.N + n1 + 1]); vy[2] = R(vel[d.N + n3]); vy[3] = R(vel[d.N + n3 + 1]);
-    Quad q;
-    load_quad(A.cord, d, j, i, q);
     R ar[4];
     for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
     R dx[3][4], dz[3][4], sr[3][4];
-    shape_derivs<R>(q, ar, dx, dz);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // FP32 from the hi/lo splits: coordinates and velocities relative to
+        // the quad's node 1 (each triangle's shape derivatives sum to zero,
+        // so a common velocity offset drops out of the strain rates)
+        load_vel_rel(A, d, j, i, vx, vy);
+        QuadF qf;
+        load_quad_rel(A, d, j, i, qf);
+        shape_derivs_f(qf, ar, dx, dz);
+    } else {
+        const double *vel = A.vel;
+        vx[0] = R(vel[n1]); vx[1] = R(vel[n1 + 1]); vx[2] = R(vel[n3]); vx[3] = R(vel[n3 + 1]);
+        vy[0] = R(vel[d.N + n1]); vy[1] = R(vel[d.N + n1 + 1]); vy[2] = R(vel[d.N + n3]); vy[3] = R(vel[d.N + n3 + 1]);
+        Quad q;
+        load_quad(A.cord, d, j, i, q);
+        shape_derivs<R>(q, ar, dx, dz);
+    }
     // node triplets of triangles A,B,C,D: (1,2,3), (3,2,4), (1,2,4), (1,4,3)
     const int tn[4][3] = {{0, 1, 2}, {2, 1, 3}, {0, 1, 3}, {0, 3, 2}};
 #pragma unroll
@@ -310,13 +320,13 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         for (int qd = 0; qd < 4; ++qd) {
             int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
             long long e = gf_elem(d, je, ie);
-            Quad q;
-            load_quad(A.cord, d, je, ie, q);
+            QuadF q;
+            load_quad_rel(A, d, je, ie, q);
             float ar[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) ar[k] = (float)area[gf_ek(d, e, k)];
             float dx[3][4], dz[3][4];
-            shape_derivs<float>(q, ar, dx, dz);
+            shape_derivs_f(q, ar, dx, dz);
             float dp = float(A.p_ref[e] - pn);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -446,6 +456,13 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     }
     vel[n] = v0;
     vel[d.N + n] = v1;
+    if (sizeof(R) == sizeof(float)) {
+        float h0 = (float)v0, h1 = (float)v1;
+        A.vel_hi[n] = h0;
+        A.vel_lo[n] = (float)(v0 - (double)h0);
+        A.vel_hi[d.N + n] = h1;
+        A.vel_lo[d.N + n] = (float)(v1 - (double)h1);
+    }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
     b_k_node<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -455,7 +472,13 @@ template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const De
 // fl_move (fl_move.f90:3-132)
 __device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d, long long n) {
     if (n >= 2 * d.N) return;
-    A.cord[n] = A.cord[n] + A.vel[n] * C->dt;
+    const double c = A.cord[n] + A.vel[n] * C->dt;
+    A.cord[n] = c;
+    if (A.cord_hi) {
+        const float h = (float)c;
+        A.cord_hi[n] = h;
+        A.cord_lo[n] = (float)(c - (double)h);
+    }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
     b_k_move_cord(C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -467,12 +490,21 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
     elem_ji(d, e, j, i);
     const double dtd = C->dt;
     if (advance_time && e == 0) C->time = C->time + dtd; // par.f90:86, after every reader of time
+    const bool fp32_path = sizeof(R) == sizeof(float);
     Quad q;
-    load_quad(A.cord, d, j, i, q);
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
-    const double *vel = A.vel;
-    double xv[4] = {vel[n1], vel[n1 + 1], vel[n3], vel[n3 + 1]};
-    double yv[4] = {vel[d.N + n1], vel[d.N + n1 + 1], vel[d.N + n3], vel[d.N + n3 + 1]};
+    QuadF qf;
+    double xv[4], yv[4];
+    float rvx[4], rvy[4];
+    if (fp32_path) {
+        load_quad_rel(A, d, j, i, qf);
+        load_vel_rel(A, d, j, i, rvx, rvy);
+    } else {
+        load_quad(A.cord, d, j, i, q);
+        long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+        const double *vel = A.vel;
+        xv[0] = vel[n1]; xv[1] = vel[n1 + 1]; xv[2] = vel[n3]; xv[3] = vel[n3 + 1];
+        yv[0] = vel[d.N + n1]; yv[1] = vel[d.N + n1 + 1]; yv[2] = vel[d.N + n3]; yv[3] = vel[d.N + n3 + 1];
+    }
     R *area = (R *)A.area;
     R *dvol = (R *)A.dvol;
     R *st = (R *)A.stress0;
@@ -498,25 +530,25 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
                         det * dtd;
             dw12 = R(dw);
         } else {
-            // FP32 from edge vectors (FP64 differences): det = B x C with
-            // B = b - a, C = c - a.  dvol = det_new*area_old - 1 is taken as
-            // (det_new - det_old)*area_old with the change of det expanded in
-            // this step's displacements u = vel*dt, which FP32 resolves.
-            float Bx = float(xc[b] - xc[a]), By = float(yc[b] - yc[a]);
-            float Cx = float(xc[c] - xc[a]), Cy = float(yc[c] - yc[a]);
-            float dBx = float((xv[b] - xv[a]) * dtd), dBy = float((yv[b] - yv[a]) * dtd);
-            float dCx = float((xv[c] - xv[a]) * dtd), dCy = float((yv[c] - yv[a]) * dtd);
+            // FP32 from edge vectors of the relative coordinates: det = B x C
+            // with B = b - a, C = c - a.  dvol = det_new*area_old - 1 is taken
+            // as (det_new - det_old)*area_old with the change of det expanded
+            // in this step's displacements u = vel*dt, which FP32 resolves.
+            const float *x = qf.x, *y = qf.y;
+            const float dtf = (float)dtd;
+            float Bx = x[b] - x[a], By = y[b] - y[a];
+            float Cx = x[c] - x[a], Cy = y[c] - y[a];
+            float dBx = (rvx[b] - rvx[a]) * dtf, dBy = (rvy[b] - rvy[a]) * dtf;
+            float dCx = (rvx[c] - rvx[a]) * dtf, dCy = (rvy[c] - rvy[a]) * dtf;
             float Box = Bx - dBx, Boy = By - dBy, Cox = Cx - dCx, Coy = Cy - dCy;
             float ddet = (Box * dCy - Boy * dCx) + (dBx * Coy - dBy * Cox) + (dBx * dCy - dBy * dCx);
             float det = Bx * Cy - By * Cx;
             dvol[gf_ek(d, e, k)] = R(ddet * (float)ar_old);
             ar_new = R(1.0f / det);
             // 0.5 * curl of the velocity over the triangle, times dt
-            float wx = float(xv[a]) * float(xc[c] - xc[b]) + float(xv[b]) * float(xc[a] - xc[c]) +
-                       float(xv[c]) * float(xc[b] - xc[a]);
-            float wy = float(yv[a]) * float(yc[c] - yc[b]) + float(yv[b]) * float(yc[a] - yc[c]) +
-                       float(yv[c]) * float(yc[b] - yc[a]);
-            dw12 = R(0.5f * (wx + wy) / det * float(dtd));
+            float wx = rvx[a] * (x[c] - x[b]) + rvx[b] * (x[a] - x[c]) + rvx[c] * (x[b] - x[a]);
+            float wy = rvy[a] * (y[c] - y[b]) + rvy[b] * (y[a] - y[c]) + rvy[c] * (y[b] - y[a]);
+            dw12 = R(0.5f * (wx + wy) / det * dtf);
         }
         area[gf_ek(d, e, k)] = ar_new;
         neg |= !(ar_new > R(0));
@@ -714,8 +746,8 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     float dissip = (P.ishearh == 1 && P.itherm != 2) ? ((const float *)A.shrheat)[e] : 0.0f;
     float diff = cond_eff / den / cp_eff;
     float src = ((float)A.source[e] + dissip / den) / cp_eff;
-    Quad q;
-    load_quad(A.cord, d, j, i, q);
+    QuadF q;
+    load_quad_rel(A, d, j, i, q);
     const float *area = (const float *)A.area;
     const long long E = d.E;
     const int tv[2][3] = {{0, 1, 2}, {2, 1, 3}};
@@ -723,8 +755,8 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     for (int t = 0; t < 2; ++t) {
         float a = area[gf_ek(d, e, t)];
         const int v1 = tv[t][0], v2 = tv[t][1], v3 = tv[t][2];
-        float dd[3] = {float(q.y[v2] - q.y[v3]) * a, float(q.y[v3] - q.y[v1]) * a, float(q.y[v1] - q.y[v2]) * a};
-        float zz[3] = {float(q.x[v3] - q.x[v2]) * a, float(q.x[v1] - q.x[v3]) * a, float(q.x[v2] - q.x[v1]) * a};
+        float dd[3] = {(q.y[v2] - q.y[v3]) * a, (q.y[v3] - q.y[v1]) * a, (q.y[v1] - q.y[v2]) * a};
+        float zz[3] = {(q.x[v3] - q.x[v2]) * a, (q.x[v1] - q.x[v3]) * a, (q.x[v2] - q.x[v1]) * a};
 #pragma unroll
         for (int m = 0; m < 3; ++m)
 #pragma unroll
@@ -903,7 +935,33 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
     const DevParams &P = *Pp;
     double dl = 1e300, vmax = 0.0, dmax = 0.0;
     unsigned pm = 0;
-    if (t < d.E) {
+    if (t < d.E && sizeof(R) == sizeof(float)) {
+        // mixed: edge lengths and 1/(area*length) in FP32 from the hi/lo
+        // coordinates; the minimum over elements stays FP64
+        long long e = t;
+        int j, i;
+        elem_ji(d, e, j, i);
+        const float *area = (const float *)A.area;
+        QuadF q;
+        load_quad_rel(A, d, j, i, q);
+        auto len = [&](int a, int b) {
+            float ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
+            return sqrtf(ddx * ddx + ddy * ddy);
+        };
+        float a0 = area[gf_ek(d, e, 0)], a1 = area[gf_ek(d, e, 1)], a2 = area[gf_ek(d, e, 2)],
+              a3 = area[gf_ek(d, e, 3)];
+        float l, df = 1e30f;
+        l = len(1, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a2 * l));
+        l = len(3, 1); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a2 * l));
+        l = len(3, 2); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a3 * l));
+        l = len(2, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a3 * l));
+        l = len(3, 0); df = fminf(df, 1.0f / (a2 * l)); df = fminf(df, 1.0f / (a3 * l));
+        l = len(1, 2); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a1 * l));
+        dl = (double)df;
+        int iph = A.iphase[e] - 1;
+        dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
+        pm = 1u << iph;
+    } else if (t < d.E) {
         long long e = t;
         int j, i;
         elem_ji(d, e, j, i);
@@ -1321,6 +1379,26 @@ template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarke
     using namespace gfk;
     GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
     GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 0);
+}
+
+namespace {
+namespace gfk {
+__global__ void k_split(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double v = src[t];
+    const float h = (float)v;
+    hi[t] = h;
+    lo[t] = (float)(v - (double)h);
+}
+} // namespace gfk
+} // namespace
+
+template <class R> void GfKernels<R>::split_nodes(const GfLaunch &g) {
+    using namespace gfk;
+    if (!g.A.cord_hi) return;
+    GF_LAUNCH(k_split, 2 * g.d.N, g.A.cord, g.A.cord_hi, g.A.cord_lo, 2 * g.d.N);
+    GF_LAUNCH(k_split, 2 * g.d.N, g.A.vel, g.A.vel_hi, g.A.vel_lo, 2 * g.d.N);
 }
 
 template <class R> void GfKernels<R>::phase_recount_all(const GfLaunch &g) {
