@@ -112,6 +112,26 @@ void fill_params(DevParams &P, const gf_params &p) {
     P.rho_magma = p.rho_magma; P.weaken_ratio_plastic = p.weaken_ratio_plastic;
     P.weaken_ratio_viscous = p.weaken_ratio_viscous; P.xReyn = p.xReyn; P.strain_inert = p.strain_inert;
     P.dt_scale = p.dt_scale; P.fracm = p.fracm;
+    for (int k = 0; k < GF_MAXPH; ++k) {
+        P.f_bulkm[k] = (float)(p.rl[k] + 2.0 * p.rm[k] / 3.0);
+        P.f_rm[k] = (float)p.rm[k];
+        P.f_fric1[k] = (float)p.fric1[k];
+        P.f_fric2[k] = (float)p.fric2[k];
+        P.f_coh1[k] = (float)p.cohesion1[k];
+        P.f_coh2[k] = (float)p.cohesion2[k];
+        P.f_dil1[k] = (float)p.dilat1[k];
+        P.f_dil2[k] = (float)p.dilat2[k];
+        P.f_pl1[k] = (float)p.plstrain1[k];
+        P.f_pl2[k] = (float)p.plstrain2[k];
+        P.f_cp[k] = (float)p.cp[k];
+        P.f_cond[k] = (float)p.conduct[k];
+        P.f_den[k] = (float)p.den[k];
+        P.f_pln[k] = (float)p.pln[k];
+        P.f_lacoef[k] = p.acoef[k] > 0 ? (float)std::log(0.75 * p.acoef[k]) : 0.0f;
+        P.f_eactiv[k] = (float)p.eactiv[k];
+        P.f_vactiv[k] = (float)p.vactiv[k];
+    }
+    P.f_ten_off = (float)p.ten_off;
 }
 
 GfLaunch launch_of(gf_ctx *c) {

@@ -26,6 +26,13 @@ struct DevParams {
     int w_ix1[GF_MAXINH], w_ix2[GF_MAXINH], w_iy1[GF_MAXINH], w_iy2[GF_MAXINH];
     double g, demf, ten_off, tau_heal, v_min, v_max, t_top, t_bot, bot_bc, pisos, drosub, rzbo, rxbo, vbc,
         fmagma_max, rho_magma, weaken_ratio_plastic, weaken_ratio_viscous, xReyn, strain_inert, dt_scale, fracm;
+    // FP32 copies of the per-phase constants for the mixed kernels
+    // (f_lacoef = log(0.75 * acoef), f_bulkm = rl + 2/3 rm)
+    float f_bulkm[GF_MAXPH], f_rm[GF_MAXPH], f_fric1[GF_MAXPH], f_fric2[GF_MAXPH], f_coh1[GF_MAXPH],
+        f_coh2[GF_MAXPH], f_dil1[GF_MAXPH], f_dil2[GF_MAXPH], f_pl1[GF_MAXPH], f_pl2[GF_MAXPH], f_cp[GF_MAXPH],
+        f_cond[GF_MAXPH], f_den[GF_MAXPH], f_pln[GF_MAXPH], f_lacoef[GF_MAXPH], f_eactiv[GF_MAXPH],
+        f_vactiv[GF_MAXPH];
+    float f_ten_off;
 };
 
 // Scalars the step reads and writes, resident on the device so that a

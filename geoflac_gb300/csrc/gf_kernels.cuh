@@ -233,10 +233,10 @@ __device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDi
     float ev = 0.0f;
     for (int k = 0; k < P.nphase; ++k) {
         float ratio = (float)A.phase_ratio[gf_pr(d, e, k)];
-        if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
-        float n = (float)P.pln[k];
-        float lv = lbase + (1.0f / n - 1.0f) * lsr - (1.0f / n) * logf(0.75f * (float)P.acoef[k]) +
-                   ((float)P.eactiv[k] + (float)P.vactiv[k] * pres) / (n * 8.31448f * (tmpr + 273.0f));
+        if (ratio < 0.01f) continue;
+        float n = P.f_pln[k];
+        float lv = lbase + (1.0f / n - 1.0f) * lsr - (1.0f / n) * P.f_lacoef[k] +
+                   (P.f_eactiv[k] + P.f_vactiv[k] * pres) / (n * 8.31448f * (tmpr + 273.0f));
         lv = fminf(lmax, fmaxf(lmin, lv));
         ev += ratio / expf(lv);
     }
@@ -544,20 +544,30 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
     R pls_curr = aps_e;
     phi = 0; coh = 0; psi = 0; hardn = 0;
     for (int k = 0; k < P.nphase; ++k) {
-        R ratio = R(A.phase_ratio[gf_pr(d, e, k)]);
-        if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
-        R f, c, dd, h;
-        R pl1 = R(P.plstrain1[k]), pl2 = R(P.plstrain2[k]);
+        R ratio, f, c, dd, h, pl1, pl2, f1, f2, c1, c2, d1, d2;
+        if constexpr (sizeof(R) == sizeof(float)) {
+            // phase ratios are k/n with n <= 32 markers: 0.01 separates 0 from the rest in FP32 too
+            ratio = (float)A.phase_ratio[gf_pr(d, e, k)];
+            if (ratio < 0.01f) continue;
+            pl1 = P.f_pl1[k]; pl2 = P.f_pl2[k];
+            f1 = P.f_fric1[k]; f2 = P.f_fric2[k]; c1 = P.f_coh1[k]; c2 = P.f_coh2[k]; d1 = P.f_dil1[k]; d2 = P.f_dil2[k];
+        } else {
+            ratio = R(A.phase_ratio[gf_pr(d, e, k)]);
+            if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
+            pl1 = R(P.plstrain1[k]); pl2 = R(P.plstrain2[k]);
+            f1 = R(P.fric1[k]); f2 = R(P.fric2[k]); c1 = R(P.cohesion1[k]); c2 = R(P.cohesion2[k]);
+            d1 = R(P.dilat1[k]); d2 = R(P.dilat2[k]);
+        }
         if (pls_curr < pl1) {
-            f = R(P.fric1[k]); c = R(P.cohesion1[k]); dd = R(P.dilat1[k]); h = 0;
+            f = f1; c = c1; dd = d1; h = 0;
         } else if (pls_curr < pl2) {
             R dpl = (pls_curr - pl1) / (pl2 - pl1);
-            f = R(P.fric1[k]) + (R(P.fric2[k]) - R(P.fric1[k])) * dpl;
-            dd = R(P.dilat1[k]) + (R(P.dilat2[k]) - R(P.dilat1[k])) * dpl;
-            c = R(P.cohesion1[k]) + (R(P.cohesion2[k]) - R(P.cohesion1[k])) * dpl;
-            h = (R(P.cohesion2[k]) - R(P.cohesion1[k])) / (pl2 - pl1);
+            f = f1 + (f2 - f1) * dpl;
+            dd = d1 + (d2 - d1) * dpl;
+            c = c1 + (c2 - c1) * dpl;
+            h = (c2 - c1) / (pl2 - pl1);
         } else {
-            f = R(P.fric2[k]); c = R(P.cohesion2[k]); dd = R(P.dilat2[k]); h = 0;
+            f = f2; c = c2; dd = d2; h = 0;
         }
         phi = phi + ratio / f;
         coh = coh + ratio / c;

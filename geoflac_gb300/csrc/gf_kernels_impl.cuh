@@ -99,8 +99,14 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 
     int iph = A.iphase[e] - 1;
     int irh = P.irheol[iph];
-    R bulkm = R(P.rl[iph] + 2.0 * P.rm[iph] / 3.0);
-    R rmu = R(P.rm[iph]);
+    R bulkm, rmu;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        bulkm = P.f_bulkm[iph];
+        rmu = P.f_rm[iph];
+    } else {
+        bulkm = R(P.rl[iph] + 2.0 * P.rm[iph] / 3.0);
+        rmu = R(P.rm[iph]);
+    }
     R stherm = R(0.0);
     if (P.istress_therm > 0)
         stherm = R(-P.alfa[iph] * (P.rl[iph] + 2.0 * P.rm[iph] / 3.0) * (A.temp[n1] - A.temp0[n1]));
@@ -119,7 +125,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         vis = visn[e];
     }
     PlasticConsts<R> pc;
-    if (irh == 6 || irh >= 11) pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi, R(P.ten_off));
+    if (irh == 6 || irh >= 11)
+        pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi, sizeof(R) == sizeof(float) ? R(P.f_ten_off) : R(P.ten_off));
     R dike = A.dike_released ? R(A.dike_released[e]) : R(0);
     const R *dvol = (const R *)A.dvol;
     R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
@@ -742,7 +749,7 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     int j, i;
     elem_ji(d, e, j, i);
     int iph = A.iphase[e] - 1;
-    float cp_eff = (float)P.cp[iph], cond_eff = (float)P.conduct[iph], den = (float)P.den[iph];
+    float cp_eff = P.f_cp[iph], cond_eff = P.f_cond[iph], den = P.f_den[iph];
     float dissip = (P.ishearh == 1 && P.itherm != 2) ? ((const float *)A.shrheat)[e] : 0.0f;
     float diff = cond_eff / den / cp_eff;
     float src = ((float)A.source[e] + dissip / den) / cp_eff;
