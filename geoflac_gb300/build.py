@@ -29,6 +29,7 @@ UNITS = [
     ("gf_capi.cu", ["-fmad=false"]),
     ("gf_noalloc.cu", ["-fmad=false"]),
     ("gf_remesh.cu", ["-fmad=false"]),
+    ("gf_io.cu", ["-fmad=false"]),
     ("gf_batch.cu", ["-fmad=true"]),
     ("fno_gemm.cu", ["-fmad=true"]),
     ("fno_ops.cu", ["-fmad=true"]),

@@ -152,6 +152,9 @@ def load_library(path: str = LIB_PATH):
         "gf_set_clock": (_i, [vp, K]),
         "gf_get_clock": (_i, [vp, K]),
         "gf_set_params": (_i, [vp, P]),
+        "gf_get_params": (_i, [vp, P]),
+        "gf_outflac": (_i, [vp, C.c_char_p, _i]), "gf_outmarker": (_i, [vp, C.c_char_p, _i]),
+        "gf_saveflac": (_i, [vp, C.c_char_p]), "gf_rsflac": (_i, [vp, C.c_char_p]),
         "gf_finish_setflac": (_i, [vp]),
         "gf_fl_therm": (_i, [vp]), "gf_change_phase": (_i, [vp]), "gf_fl_rheol": (_i, [vp]),
         "gf_fl_node": (_i, [vp]), "gf_fl_move": (_i, [vp]), "gf_rmasses": (_i, [vp]),

@@ -589,6 +589,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.nmarkers, 1));
     A_(dalloc(c, &c->d_angle, 1));
     A_(dalloc(c, &A.cord_old, 2 * N));
+    A_(dalloc(c, &A.orig, 2 * N));
     {
         GfRemeshBufs &b = c->rb;
         A_(dalloc(c, &b.tx, p->nx));
@@ -656,6 +657,12 @@ int gf_set_params(gf_ctx *c, const gf_params *p) {
     GF_CK(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice));
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
     c->graphs.clear();
+    return GF_OK;
+}
+
+int gf_get_params(gf_ctx *c, gf_params *p) {
+    if (!c || !p) return GF_ERR_ARG;
+    *p = c->p;
     return GF_OK;
 }
 
@@ -764,6 +771,8 @@ int gf_marker2elem(gf_ctx *c) {
 
 int gf_finish_setflac(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
+    // xoriginal = cord(:,:,1), zoriginal = cord(:,:,2) (setflac.f90:54-55)
+    GF_CK(cudaMemcpyAsync(c->A.orig, c->A.cord, sizeof(double) * 2 * c->d.N, cudaMemcpyDeviceToDevice, c->s));
     k_rmasses(c);
     if (c->p.ivis_present == 1) k_init_visc(c);
     k_dt_mass(c);
@@ -806,6 +815,55 @@ int gf_ctx_view(gf_ctx *c, GfMemberView *v) {
     v->rzbo = c->p.rzbo;
     v->g = c->p.g;
     v->s = c->s;
+    v->hp = &c->p;
+    v->L = &c->L;
+    return GF_OK;
+}
+
+} // extern "C"
+namespace {
+template <class R> __global__ void k_fill(R *p, long long n, R v) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+template <class R> void restart_fields(gf_ctx *c) {
+    const long long E = c->d.E, N = c->d.N;
+    auto nb = [](long long n) { return (unsigned)((n + 255) / 256); };
+    k_fill<R><<<nb(E), 256, 0, c->s>>>((R *)c->A.shrheat, E, R(0));
+    k_fill<R><<<nb(E), 256, 0, c->s>>>((R *)c->A.sshrheat, E, R(0));
+    k_fill<R><<<nb(3 * E), 256, 0, c->s>>>((R *)c->A.se2sr, 3 * E, R(1e-16));
+    k_fill<R><<<nb(E), 256, 0, c->s>>>((R *)c->A.e2sr, E, R(1e-16));
+    k_fill<R><<<nb(4 * E), 256, 0, c->s>>>((R *)c->A.dvol, 4 * E, R(0));
+    cudaMemcpyAsync(c->A.temp0, c->A.temp, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->s);
+    c->launches += 5;
+}
+} // namespace
+extern "C" {
+
+int gf_ctx_restart_finish(gf_ctx *c) {
+    if (!c) return GF_ERR_ARG;
+    int rc;
+    GfLaunch g = launch_of(c);
+    if (c->mode == GF_MODE_MIXED) {
+        GfRemesh<float>::init_areas(g);
+        restart_fields<float>(c);
+    } else {
+        GfRemesh<double>::init_areas(g);
+        restart_fields<double>(c);
+    }
+    rc = take_status(c);
+    if (rc) return rc;
+    k_rmasses(c);
+    if (c->p.ivis_present == 1) k_init_visc(c);
+    k_dt_mass(c);
+    rc = take_status(c);
+    if (rc) return rc;
+    DevClock C;
+    GF_CK(cudaMemcpy(&C, c->dC, sizeof C, cudaMemcpyDeviceToHost));
+    C.dtavg = 0.0;
+    GF_CK(cudaMemcpy(c->dC, &C, sizeof C, cudaMemcpyHostToDevice));
+    c->nsrate = -1;
+    drop_graphs(c);
     return GF_OK;
 }
 

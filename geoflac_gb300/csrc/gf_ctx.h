@@ -77,6 +77,7 @@ struct DevArrays {
     uint8_t *e_flag;                                  // change_phase element flags
     int *m_count, *m_offset;                          // marker2elem scan
     double *cord_old;                                 // remesh
+    double *orig; // xoriginal, zoriginal (nz, nx, 2): start-up node positions carried through remeshing
     // mixed: FP32 hi/lo splits of the FP64 coordinates and velocities
     // (x = hi + lo), so differences of neighbouring values need no FP64
     float *cord_hi, *cord_lo, *vel_hi, *vel_lo;

@@ -649,6 +649,8 @@ template <class R> void GfRemesh<R>::regrid(const GfLaunch &g, const GfRemeshArg
     GF_RLAUNCH(k_barcord, d.N, gn, (const double *)A.cord, (const double *)b.pt, b.numtr, b.bc);
     for (int k = 0; k < 2; ++k) interp_plane<double>(g, b, A.vel + k * d.N, d.nz, d.N, 0);
     interp_plane<double>(g, b, A.temp, d.nz, d.N, 0);
+    // xoriginal, zoriginal (remesh.f90:242-243)
+    for (int k = 0; k < 2; ++k) interp_plane<double>(g, b, A.orig + k * d.N, d.nz, d.N, 0);
 }
 
 template <class R> void GfRemesh<R>::init_areas(const GfLaunch &g) {

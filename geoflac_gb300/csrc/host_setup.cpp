@@ -800,6 +800,26 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
     return GF_OK;
 }
 
+// The host part of a restart once the saved fields are in L and marker2elem
+// has refreshed iphase and jmoho (rsflac.f90:117-118,207): check_visc_rheol
+// and init_bc on the restored mesh (the boundary velocities are profiles
+// along the restored side coordinates).
+int gf_host_restart_bc(gf_params *p, gf_layout *L) {
+    gf_clock c{};
+    S s{p, &c, L, GfDims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)}};
+    try {
+        p->ivis_present = 0;
+        for (long long e = 0; e < s.d.E; ++e) {
+            int irh = p->irheol[L->iphase[e] - 1];
+            if (irh == 3 || irh >= 11) p->ivis_present = 1;
+        }
+        init_bc(s);
+    } catch (const Stop &st) {
+        return st.code;
+    }
+    return GF_OK;
+}
+
 // Geotherm of node columns i_first..i_last (0-based) for age zone `zone`
 // (init_geotherm_profile, src/init_temp.f90:127-310), on host arrays in the
 // reference layout: used by the remesh event for material entering through a

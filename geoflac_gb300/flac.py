@@ -46,6 +46,39 @@ class Flac:
         c = capi.setflac_host(p, s)
         return cls(p, c, s, mode)
 
+    @classmethod
+    def restart(cls, inp_path: str, directory: str = ".", mode: str = "fp64", markers_per_side: int = 3,
+                eclogite_rule: int = 0, therm_sweeps: int = 0) -> "Flac":
+        """read_params + rsflac (src/par.f90:28-45) for a restart from the
+        `*.rs` files in `directory`."""
+        p = capi.read_params(inp_path, markers_per_side, eclogite_rule, therm_sweeps)
+        s = HostState(p)
+        c = capi.setflac_host(p, s)
+        g = cls(p, c, s, mode, finish_setflac=False)
+        g.rsflac(directory)
+        return g
+
+    # ---- output and restart files (src/outflac.f90, outmarker.f90,
+    # saveflac.f90, rsflac.f90) ------------------------------------------
+    def outflac(self, directory: str = ".", fresh: bool = False):
+        """Append one float32 frame (`<field>.0`, `_contents.0`)."""
+        check(self.lib.gf_outflac(self.ctx, directory.encode(), 1 if fresh else 0), "outflac")
+
+    def outmarker(self, directory: str = ".", fresh: bool = False):
+        """Write marker1/marker2.NNNNNN.0 and list them in `_markers.0`."""
+        check(self.lib.gf_outmarker(self.ctx, directory.encode(), 1 if fresh else 0), "outmarker")
+
+    def saveflac(self, directory: str = "."):
+        """Write the FP64 restart files (`*.rs`, `_contents.save`)."""
+        check(self.lib.gf_saveflac(self.ctx, directory.encode()), "saveflac")
+        self.download(0)
+
+    def rsflac(self, directory: str = "."):
+        """Restore the state from the restart files in `directory`."""
+        check(self.lib.gf_rsflac(self.ctx, directory.encode()), "rsflac")
+        check(self.lib.gf_get_params(self.ctx, C.byref(self.params)), "gf_get_params")
+        self.download()
+
     # ---- sync points ----------------------------------------------------
     def upload(self, mask: int = capi.F_ALL):
         check(self.lib.gf_upload(self.ctx, mask), "gf_upload")

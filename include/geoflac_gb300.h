@@ -280,6 +280,40 @@ int gf_itest_mesh(gf_ctx *ctx, double *min_angle);
  * marker2elem. */
 int gf_remesh(gf_ctx *ctx);
 
+/* ---- output frames and restart files (drop-in for the reference's I/O) ----
+ * Files go to directory `dir` (NULL or "" = the working directory, as in
+ * the reference) in the reference's binary layouts: gfortran direct-access
+ * records (fixed record length, no record markers, native byte order).
+ * Fields that this library does not model are written as zeros: fmelt,
+ * fmelt2, dtopo, extrusion (surface processes and melting) in frames; dhacc,
+ * extr_acc, q_init, vel_flex_old and the dike_* records in restart files. */
+
+/* outflac (src/outflac.f90:5-431): one float32 frame of the node, element
+ * and surface fields selected by io_flags, appended as record nrec of each
+ * `<field>.0` file and listed in `_contents.0`.  fresh = 1 starts a new
+ * series (the reference's lastout == 1: nrec = 1, `_contents.0` rewritten);
+ * fresh = 0 appends after the last record listed. */
+int gf_outflac(gf_ctx *ctx, const char *dir, int fresh);
+/* outmarker (src/outmarker.f90:1-100): marker1.NNNNNN.0 (x, z in km, age
+ * in Myr, a1, a2 as float32 records) and marker2.NNNNNN.0 (dead, phase,
+ * ntriag as int32 records), listed in `_markers.0`. */
+int gf_outmarker(gf_ctx *ctx, const char *dir, int fresh);
+/* saveflac (src/saveflac.f90:5-172): the FP64 restart files `*.rs`, Amin.rs,
+ * pisos.rs (nyhydro == 2) and `_contents.save`.  Downloads every field into
+ * the host arrays first (the layout must provide them). */
+int gf_saveflac(gf_ctx *ctx, const char *dir);
+/* rsflac (src/rsflac.f90:3-266): reads the restart files of record nrec
+ * named in `_contents.rs` (or, if absent, `_contents.save`) into the host
+ * arrays and the context, rebuilds the element marker lists (stop 999 on a
+ * bad triangle number), then marker2elem, check_visc_rheol, init_areas,
+ * init_bc, the field resets, rmasses, init_visc and dt_mass.  The context
+ * must come from gf_create on the same .inp (sizes, phases, boundary
+ * conditions); its parameters gain the restored Amin, pisos, dxmin, dzmin,
+ * ivis_present and vbc (read them back with gf_get_params). */
+int gf_rsflac(gf_ctx *ctx, const char *dir);
+/* The context's current parameters (the counterpart of gf_set_params). */
+int gf_get_params(gf_ctx *ctx, gf_params *p);
+
 /* Per-subroutine calls wait for their kernels and return the device status
  * (sync = 1, the default: the reference's stop-on-error behaviour).  With
  * sync = 0 they only enqueue work on the context's stream; errors surface at

@@ -1843,6 +1843,30 @@ int or_finish_setflac(gf_params *p, gf_clock *c, gf_layout *L) {
     });
 }
 
+// The tail of rsflac (src/rsflac.f90:197-236) after marker2elem and init_bc:
+// init_areas, temp0 = temp, heating and strain-rate accumulators reset, dvol
+// cleared, rmasses, init_visc, dt_mass, averaging reset
+int or_restart_tail(gf_params *p, gf_clock *c, gf_layout *L) {
+    St s = make(p, c, L);
+    return guard([&] {
+        const long long E = s.d.E, N = s.d.N;
+        init_areas(s);
+        std::memcpy(L->temp0, L->temp, sizeof(double) * (size_t)N);
+        for (long long e = 0; e < E; ++e) {
+            L->shrheat[e] = 0.0;
+            L->sshrheat[e] = 0.0;
+            L->e2sr[e] = 1e-16;
+        }
+        for (long long e = 0; e < 3 * E; ++e) L->se2sr[e] = 1e-16;
+        for (long long e = 0; e < 4 * E; ++e) L->dvol[e] = 0.0;
+        rmasses(s);
+        if (p->ivis_present == 1) init_visc(s);
+        dt_mass(s);
+        c->dtavg = 0;
+        c->nsrate = -1;
+    });
+}
+
 // flac (src/flac.f90:5-91) followed by par.f90:84-87
 int or_flac(gf_params *p, gf_clock *c, gf_layout *L) {
     St s = make(p, c, L);

@@ -31,7 +31,7 @@ def load():
     P, K, L = C.POINTER(GfParams), C.POINTER(GfClock), C.POINTER(GfLayout)
     for name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
                  "init_visc", "marker2elem", "finish_setflac", "flac", "bar2euler", "lpeuler2bar", "remesh",
-                 "remesh_event"):
+                 "remesh_event", "restart_tail"):
         f = getattr(lib, "or_" + name)
         f.restype = C.c_int
         f.argtypes = [P, K, L]
@@ -64,7 +64,7 @@ class Oracle:
     def __getattr__(self, name):
         if name in ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmasses", "dt_mass",
                     "init_visc", "marker2elem", "finish_setflac", "flac", "bar2euler", "lpeuler2bar", "remesh",
-                    "remesh_event"):
+                    "remesh_event", "restart_tail"):
             return lambda: self._call(name)
         raise AttributeError(name)
 
