@@ -3,7 +3,8 @@
 Compiles every translation unit in parallel with nvcc / g++ and links
 ``geoflac_gb300/libgeoflac_gb300.so``.  The FP64 kernels are compiled with
 ``-fmad=false`` (no contraction of a*b+c into one rounding, as in the
-serial reference); the mixed-precision kernels use contraction.  Host C++ is
+serial reference); the mixed-precision kernels use contraction and the
+approximate FP32 division and square root (2 ulp).  Host C++ is
 compiled with ``-ffp-contract=off`` so that x86 and Arm hosts round alike.
 """
 from __future__ import annotations
@@ -25,12 +26,12 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompi
 
 UNITS = [
     ("gf_fp64.cu", ["-fmad=false"]),
-    ("gf_mixed.cu", ["-fmad=true"]),
+    ("gf_mixed.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
     ("gf_capi.cu", ["-fmad=false"]),
     ("gf_noalloc.cu", ["-fmad=false"]),
     ("gf_remesh.cu", ["-fmad=false"]),
     ("gf_io.cu", ["-fmad=false"]),
-    ("gf_batch.cu", ["-fmad=true"]),
+    ("gf_batch.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
     ("fno_gemm.cu", ["-fmad=true"]),
     ("fno_ops.cu", ["-fmad=true"]),
     ("host_inp.cpp", None),

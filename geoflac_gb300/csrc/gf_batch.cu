@@ -340,7 +340,10 @@ __global__ void k_inject_nodes(GridArgs g, const int2 *tiles, int ntile, int ipt
             const double z = m.z0 + m.rzbo * (double)j / (double)(m.d.nz - 1) + (double)grid_at(g, tl.x, fy, fx, 8);
             m.A.vel[n] = vx;
             m.A.vel[m.d.N + n] = vz;
-            m.A.temp[n] = grid_at(g, tl.x, fy, fx, 6);
+            const double tn = grid_at(g, tl.x, fy, fx, 6);
+            m.A.temp[n] = tn;
+            m.A.temp_hi[n] = (float)tn;
+            m.A.temp_lo[n] = (float)(tn - (double)(float)tn);
             m.A.cord[m.d.N + n] = z;
             const float hx = (float)vx, hz = (float)vz, hc = (float)z;
             m.A.vel_hi[n] = hx;
@@ -496,7 +499,8 @@ std::vector<std::pair<void *, size_t>> injected_fields(const GfMemberView &v) {
             {v.A.cord, 2 * N * sizeof(double)},   {v.A.stress0, 16 * E * sizeof(float)},
             {v.A.aps, E * sizeof(float)},         {v.A.area, 4 * E * sizeof(float)},
             {v.A.cord_hi, 2 * N * sizeof(float)}, {v.A.cord_lo, 2 * N * sizeof(float)},
-            {v.A.vel_hi, 2 * N * sizeof(float)},  {v.A.vel_lo, 2 * N * sizeof(float)}};
+            {v.A.vel_hi, 2 * N * sizeof(float)},  {v.A.vel_lo, 2 * N * sizeof(float)},
+            {v.A.temp_hi, N * sizeof(float)},     {v.A.temp_lo, N * sizeof(float)}};
 }
 } // namespace
 
@@ -836,6 +840,7 @@ int gf_batch_sample(gf_batch *b, float *grid, int H, int W, int phase_id) {
 
 int gf_batch_inject(gf_batch *b, const float *grid, int H, int W) {
     if (!b || !grid || H < 2 || W < 2) return GF_ERR_ARG;
+    for (gf_ctx *c : b->members) gf_ctx_invalidate_forces(c);
     GridArgs g{b->d_members, (int)b->members.size(), H, W, 1, nullptr, grid};
     const int T = b->cfg.threads, ipt = b->cfg.items_per_thread;
     if (b->ntile[K_N]) k_inject_nodes<<<b->ntile[K_N], T, 0, b->s>>>(g, b->d_tiles[K_N], b->ntile[K_N], ipt);
@@ -873,6 +878,7 @@ int gf_batch_restore(gf_batch *b, const int *members, int count) {
     for (int k = 0; k < count; ++k) {
         int m = members[k];
         if (m < 0 || m >= (int)b->views.size()) return GF_ERR_ARG;
+        gf_ctx_invalidate_forces(b->members[m]);
         size_t off = b->backup_off[m];
         for (auto &f : injected_fields(b->views[m])) {
             GB_CK(cudaMemcpyAsync(f.first, (char *)b->backup + off, f.second, cudaMemcpyDeviceToDevice, b->s));

@@ -47,6 +47,7 @@ struct gf_ctx {
     std::vector<void *> allocs;
     int sweeps = 0; // cap on the thermal sweeps (0: library cap)
     int sync = 1;
+    int frc_valid = 0; // mixed: e_frc holds the corner forces of the current stresses and mesh
 };
 
 namespace {
@@ -132,6 +133,8 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.f_vactiv[k] = (float)p.vactiv[k];
     }
     P.f_ten_off = (float)p.ten_off;
+    P.f_demf = (float)p.demf;
+    P.f_g = (float)p.g;
 }
 
 GfLaunch launch_of(gf_ctx *c) {
@@ -180,6 +183,7 @@ template <class T> int xfer(gf_ctx *c, T *host, T *dev, long long n, int dir) {
 }
 
 int move_fields(gf_ctx *c, unsigned m, int dir) {
+    if (dir) c->frc_valid = 0;
     const gf_layout &L = c->L;
     DevArrays &A = c->A;
     long long N = c->d.N, E = c->d.E;
@@ -190,10 +194,6 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
     } while (0)
     if (m & GF_F_CORD) T_(xfer(c, L.cord, A.cord, 2 * N, dir));
     if (m & GF_F_VEL) T_(xfer(c, L.vel, A.vel, 2 * N, dir));
-    if (dir && (m & (GF_F_CORD | GF_F_VEL)) && c->mode == GF_MODE_MIXED) {
-        GfLaunch g = launch_of(c);
-        GfKernels<float>::split_nodes(g);
-    }
     if (m & GF_F_TEMP) {
         T_(xfer(c, L.temp, A.temp, N, dir));
         T_(xfer(c, L.temp0, A.temp0, N, dir));
@@ -257,6 +257,10 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.dhacc_correction, A.dhacc_correction, c->p.nx, dir));
     }
 #undef T_
+    if (dir && (m & (GF_F_CORD | GF_F_VEL | GF_F_TEMP)) && c->mode == GF_MODE_MIXED) {
+        GfLaunch g = launch_of(c);
+        GfKernels<float>::split_nodes(g);
+    }
     GF_CK(cudaStreamSynchronize(c->s));
     return GF_OK;
 }
@@ -298,13 +302,20 @@ void k_rheol(gf_ctx *c, int upd, int avg) {
     GfLaunch g = launch_of(c);
     if (c->mode == GF_MODE_MIXED) GfKernels<float>::rheol(g, upd, avg);
     else GfKernels<double>::rheol(g, upd, avg);
+    c->frc_valid = 1;
 }
 void k_node(gf_ctx *c) {
     GfLaunch g = launch_of(c);
-    if (c->mode == GF_MODE_MIXED) GfKernels<float>::node(g);
-    else GfKernels<double>::node(g);
+    if (c->mode == GF_MODE_MIXED) {
+        if (!c->frc_valid) GfKernels<float>::elem_forces(g);
+        c->frc_valid = 1;
+        GfKernels<float>::node(g);
+    } else {
+        GfKernels<double>::node(g);
+    }
 }
 void k_move(gf_ctx *c, int advance_time = 0) {
+    c->frc_valid = 0;
     GfLaunch g = launch_of(c);
     g.advance_time = advance_time;
     if (c->mode == GF_MODE_MIXED) GfKernels<float>::move(g);
@@ -420,14 +431,15 @@ template <class R> void enqueue_marker2elem(gf_ctx *c, const GfLaunch &g, const 
 }
 
 template <class R> int enqueue_remesh(gf_ctx *c) {
+    c->frc_valid = 0;
     GfLaunch g = launch_of(c);
     GfRemeshArgs a = remesh_args(c);
     GfRemesh<R>::regrid(g, a, c->rb);
-    GfKernels<R>::split_nodes(g); // new coordinates and interpolated velocities
     if (c->p.incoming_left == 1 || c->p.incoming_right == 1) {
         int rc = sidewall_temps(c);
         if (rc) return rc;
     }
+    GfKernels<R>::split_nodes(g); // new coordinates, interpolated velocities and temperatures
     if (c->p.ivis_present == 1) GfKernels<R>::init_visc(g);
     GfRemesh<R>::init_areas(g);
     GfKernels<R>::rmasses(g);
@@ -614,6 +626,11 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &A.cord_lo, 2 * N));
         A_(dalloc(c, &A.vel_hi, 2 * N));
         A_(dalloc(c, &A.vel_lo, 2 * N));
+        A_(dalloc(c, &A.pr_hi, E));
+        A_(dalloc(c, &A.pr_lo, E));
+        A_(dalloc(c, &A.e_frc, 16 * E));
+        A_(dalloc(c, &A.temp_hi, N));
+        A_(dalloc(c, &A.temp_lo, N));
     }
     DevParams P;
     fill_params(P, *p);
@@ -869,9 +886,14 @@ int gf_ctx_restart_finish(gf_ctx *c) {
 
 unsigned gf_ctx_signature(const gf_ctx *c) { return step_signature(c); }
 
-void gf_ctx_advance(gf_ctx *c, unsigned sig) { advance_host(c, sig); }
+void gf_ctx_advance(gf_ctx *c, unsigned sig) {
+    c->frc_valid = 0; // the batch step moved the mesh after its own gather
+    advance_host(c, sig);
+}
 
 int gf_ctx_take_status(gf_ctx *c) { return take_status(c); }
+
+void gf_ctx_invalidate_forces(gf_ctx *c) { c->frc_valid = 0; }
 
 int gf_step(gf_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return GF_ERR_ARG;

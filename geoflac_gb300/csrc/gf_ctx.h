@@ -32,7 +32,7 @@ struct DevParams {
         f_coh2[GF_MAXPH], f_dil1[GF_MAXPH], f_dil2[GF_MAXPH], f_pl1[GF_MAXPH], f_pl2[GF_MAXPH], f_cp[GF_MAXPH],
         f_cond[GF_MAXPH], f_den[GF_MAXPH], f_pln[GF_MAXPH], f_lacoef[GF_MAXPH], f_eactiv[GF_MAXPH],
         f_vactiv[GF_MAXPH];
-    float f_ten_off;
+    float f_ten_off, f_demf, f_g;
 };
 
 // Scalars the step reads and writes, resident on the device so that a
@@ -81,6 +81,12 @@ struct DevArrays {
     // mixed: FP32 hi/lo splits of the FP64 coordinates and velocities
     // (x = hi + lo), so differences of neighbouring values need no FP64
     float *cord_hi, *cord_lo, *vel_hi, *vel_lo;
+    float *pr_hi, *pr_lo;     // the same split of p_ref
+    float *temp_hi, *temp_lo; // and of the temperatures
+    // mixed: per-element corner forces for the node gather, [16][E]: for
+    // corner c (0..3) the force of the element's stresses less its own
+    // triangle-1 stress (x, z) and the geometric sums G (x, z)
+    float *e_frc;
     int *nmarkers;                                    // device marker count
 };
 
@@ -100,6 +106,9 @@ template <class R> struct GfKernels {
     static void therm(const GfLaunch &g, int sweeps);
     static void rheol(const GfLaunch &g, int update_visc, int avg_mode);
     static void node(const GfLaunch &g);
+    // mixed: the corner forces of the current stresses (fl_rheol writes them
+    // as it updates the stresses; this recomputes them after other changes)
+    static void elem_forces(const GfLaunch &g);
     static void move(const GfLaunch &g);
     static void rmasses(const GfLaunch &g);
     static void dt_mass(const GfLaunch &g);

@@ -26,6 +26,16 @@ __device__ __forceinline__ double m_sin(double x) { return gfm::sin(x); }
 __device__ __forceinline__ float m_sin(float x) { return sinf(x); }
 __device__ __forceinline__ double m_tan(double x) { return gfm::tan(x); }
 __device__ __forceinline__ float m_tan(float x) { return tanf(x); }
+// sine and tangent of an angle in degrees: FP64 as the reference evaluates
+// them (sin(phi * degrad)); FP32 through sinpi/cospi, whose argument
+// reduction needs no local-memory slow path
+__device__ __forceinline__ double m_sind(double deg) { return gfm::sin(deg * (3.14159265358979323846 / 180.0)); }
+__device__ __forceinline__ float m_sind(float deg) { return sinpif(deg * (1.0f / 180.0f)); }
+__device__ __forceinline__ double m_tand(double deg) { return gfm::tan(deg * (3.14159265358979323846 / 180.0)); }
+__device__ __forceinline__ float m_tand(float deg) {
+    const float x = deg * (1.0f / 180.0f);
+    return sinpif(x) / cospif(x);
+}
 __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
 
@@ -376,20 +386,17 @@ template <class R> struct PlasticConsts {
 
 template <class R>
 __device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh, R phi, R psi, R ten_off) {
-    const R pi = R(3.14159265358979323846);
-    const R degrad = R(3.14159265358979323846 / 180.0);
     const R c4d3 = R(4.0 / 3.0), c2d3 = R(2.0 / 3.0);
-    (void)pi;
     PlasticConsts<R> c;
-    R sphi = m_sin(phi * degrad);
-    R spsi = m_sin(psi * degrad);
+    R sphi = m_sind(phi);
+    R spsi = m_sind(psi);
     c.anphi = (R(1.0) + sphi) / (R(1.0) - sphi);
     c.anpsi = (R(1.0) + spsi) / (R(1.0) - spsi);
     c.amc = R(2.0) * coh * m_sqrt(c.anphi);
     c.e1 = bulkm + c4d3 * rmu;
     c.e2 = bulkm - c2d3 * rmu;
     c.x1 = (c.e1 - c.e2 * c.anpsi + c.e1 * c.anphi * c.anpsi - c.e2 * c.anphi);
-    c.ten_max = (phi == R(0.0)) ? ten_off : fmin(ten_off, coh / (m_tan(phi * degrad)));
+    c.ten_max = (phi == R(0.0)) ? ten_off : fmin(ten_off, coh / m_tand(phi));
     return c;
 }
 

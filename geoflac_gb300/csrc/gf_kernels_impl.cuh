@@ -3,6 +3,11 @@
 
 #include "gf_kernels.cuh"
 
+// resident CTAs per SM the register allocation of k_rheol is sized for
+#ifndef GF_RHEOL_MINB
+#define GF_RHEOL_MINB 2
+#endif
+
 // internal linkage: each precision's translation unit has its own copy
 namespace {
 namespace gfk {
@@ -17,6 +22,43 @@ __device__ __forceinline__ void node_ji(const GfDims &d, long long n, int &j, in
 }
 
 inline unsigned grid_for(long long n) { return (unsigned)((n + GF_THREADS - 1) / GF_THREADS); }
+
+// ======================================================================
+// Mixed path: the element's share of the node forces of fl_node.f90.  For
+// corner c (node 1..4 = (j,i), (j+1,i), (j,i+1), (j+1,i+1)) the three
+// triangles that contain it contribute -0.25/ar * (s . grad N); written as
+//   F_c = -sum_t 0.25/ar_t * ((s_t - s_ref) . grad N_c,t)   (small: stress
+//         variation inside the element, s_ref = triangle 1's stored stress)
+//   G_c =  sum_t 0.25/ar_t * grad N_c,t
+// so that a node sums F_c - (s_ref,e - s_ref,n) . G_c over its elements
+// (sum_e G_c = 0 around an interior node): every FP32 term is a difference.
+// The triangle/vertex tables are fl_node.f90:7-8 for quad 4 - c.
+__device__ __forceinline__ void elem_corner_forces(const float dx[3][4], const float dz[3][4], const float ar[4],
+                                                   const float sn[4][4], float *__restrict__ frc, long long E,
+                                                   long long e) {
+    const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
+    const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int qd = 3 - c;
+        float fx = 0.0f, fy = 0.0f, gx = 0.0f, gz = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int t = kk[qd][k], m = mm[qd][k];
+            const float factor = 0.25f / ar[t];
+            const float ax = factor * dx[m][t], az = factor * dz[m][t];
+            const float sxx = sn[0][t] - sn[0][1], szz = sn[1][t] - sn[1][1], sxz = sn[2][t] - sn[2][1];
+            fx -= sxx * ax + sxz * az;
+            fy -= sxz * ax + szz * az;
+            gx += ax;
+            gz += az;
+        }
+        frc[(4 * c + 0) * E + e] = fx;
+        frc[(4 * c + 1) * E + e] = fy;
+        frc[(4 * c + 2) * E + e] = gx;
+        frc[(4 * c + 3) * E + e] = gz;
+    }
+}
 
 // ======================================================================
 // fl_rheol (fl_rheol.f90:4-389): one thread per element.
@@ -113,7 +155,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     R *aps = (R *)A.aps;
     R aps_e = aps[e];
     // mixed path: stored normal stresses are deviations from -pref
-    const R pref = sizeof(R) == sizeof(float) ? R(A.p_ref[e]) : R(0);
+    R pref = R(0);
+    if constexpr (sizeof(R) == sizeof(float)) pref = A.pr_hi[e]; // == float(p_ref)
     R coh = 0, phi = 0, psi = 0, hardn = 0;
     if (irh == 6 || irh >= 11) pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
     R *visn = (R *)A.visn;
@@ -209,6 +252,16 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = sn[c][k];
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // the node gather's corner forces of the new stresses (the mesh does
+        // not move before fl_node); shape derivatives taken again rather than
+        // kept live through the stress update
+        QuadF q2;
+        load_quad_rel(A, d, j, i, q2);
+        float dx2[3][4], dz2[3][4];
+        shape_derivs_f(q2, ar, dx2, dz2);
+        elem_corner_forces(dx2, dz2, ar, sn, A.e_frc, d.E, e);
+    }
     if (irh == 6 || irh >= 11) {
         R quad_area = ar[0] + ar[1] + ar[2] + ar[3];
         aps_e = aps_e + (depl[0] * ar[0] + depl[1] * ar[1] + depl[2] * ar[2] + depl[3] * ar[3]) / quad_area;
@@ -231,35 +284,54 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         R lambda = bulkm - R(2.0 / 3.0) * rmu, mu = rmu;
         R den_el = R(3.0) * lambda + R(2.0) * mu;
         if (m_abs(den_el) < R(1e-30)) den_el = den_el < R(0) ? R(-1e-30) : R(1e-30);
+        if constexpr (sizeof(R) == sizeof(float)) {
+            // the same elastic-strain differences with one reciprocal and the
+            // stress changes taken first
+            const float lamr = lambda / den_el, inv2mu = 1.0f / (2.0f * mu);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
-            R tr0 = s0v[0][k] + s0v[1][k] + s0v[3][k];
-            R e11a = (s0v[0][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-            R e22a = (s0v[1][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-            R e33a = (s0v[3][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-            R e12a = s0v[2][k] / (R(2.0) * mu);
-            R tr1 = f11 + f22 + f33;
-            R e11b = (f11 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-            R e22b = (f22 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-            R e33b = (f33 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-            R e12b = f12 / (R(2.0) * mu);
-            R d11 = sr[0][k] * dt - (e11b - e11a);
-            R d22 = sr[1][k] * dt - (e22b - e22a);
-            R d12 = sr[2][k] * dt - (e12b - e12a);
-            R d33 = R(0.0) - (e33b - e33a);
-            R a11 = R(0.5) * (s0v[0][k] + f11), a22 = R(0.5) * (s0v[1][k] + f22), a12 = R(0.5) * (s0v[2][k] + f12),
-              a33 = R(0.5) * (s0v[3][k] + f33);
-            R qk = a11 * d11 + a22 * d22 + R(2.0) * a12 * d12 + a33 * d33;
-            if (sizeof(R) == sizeof(float)) qk -= pref * (d11 + d22 + d33); // isotropic reference part
-            qsum = qsum + R(0.25) * qk;
+            for (int k = 0; k < 4; ++k) {
+                float f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
+                float dtr = ((f11 - s0v[0][k]) + (f22 - s0v[1][k])) + (f33 - s0v[3][k]);
+                float d11 = sr[0][k] * dt - ((f11 - s0v[0][k]) - lamr * dtr) * inv2mu;
+                float d22 = sr[1][k] * dt - ((f22 - s0v[1][k]) - lamr * dtr) * inv2mu;
+                float d12 = sr[2][k] * dt - (f12 - s0v[2][k]) * inv2mu;
+                float d33 = -(((f33 - s0v[3][k]) - lamr * dtr) * inv2mu);
+                float a11 = 0.5f * (s0v[0][k] + f11), a22 = 0.5f * (s0v[1][k] + f22),
+                      a12 = 0.5f * (s0v[2][k] + f12), a33 = 0.5f * (s0v[3][k] + f33);
+                float qk = a11 * d11 + a22 * d22 + 2.0f * a12 * d12 + a33 * d33;
+                qk -= pref * (d11 + d22 + d33); // isotropic reference part
+                qsum = qsum + 0.25f * qk;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
+                R tr0 = s0v[0][k] + s0v[1][k] + s0v[3][k];
+                R e11a = (s0v[0][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+                R e22a = (s0v[1][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+                R e33a = (s0v[3][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
+                R e12a = s0v[2][k] / (R(2.0) * mu);
+                R tr1 = f11 + f22 + f33;
+                R e11b = (f11 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+                R e22b = (f22 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+                R e33b = (f33 - (lambda / den_el) * tr1) / (R(2.0) * mu);
+                R e12b = f12 / (R(2.0) * mu);
+                R d11 = sr[0][k] * dt - (e11b - e11a);
+                R d22 = sr[1][k] * dt - (e22b - e22a);
+                R d12 = sr[2][k] * dt - (e12b - e12a);
+                R d33 = R(0.0) - (e33b - e33a);
+                R a11 = R(0.5) * (s0v[0][k] + f11), a22 = R(0.5) * (s0v[1][k] + f22),
+                  a12 = R(0.5) * (s0v[2][k] + f12), a33 = R(0.5) * (s0v[3][k] + f33);
+                R qk = a11 * d11 + a22 * d22 + R(2.0) * a12 * d12 + a33 * d33;
+                qsum = qsum + R(0.25) * qk;
+            }
         }
         shr = shr + qsum;
     }
     sshrheat[e] = shr;
     (void)nloop;
 }
-template <class R> __global__ void __launch_bounds__(GF_THREADS) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
+template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
     b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -299,8 +371,101 @@ __global__ void k_rheol_clock(DevClock *C, int phase) {
 // ======================================================================
 // fl_node (fl_node.f90:3-393): one thread per node, forces gathered from
 // the 4 adjacent quads in the reference's order, no atomics.
-template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long n) {
-    if (n >= d.N) return;
+//
+// Threads are numbered boundary ring first (top row, bottom row, left and
+// right columns), then the interior nodes (column by column, j fastest), so
+// that the boundary nodes, which take the FP64 path with water load and
+// Winkler foundation, run in warps of their own and start first.
+__device__ __forceinline__ long long node_of_slot(const GfDims &d, long long t) {
+    const int nzi = d.nz - 2;
+    if (t < d.nx) return gf_node(d, 0, (int)t);
+    t -= d.nx;
+    if (t < d.nx) return gf_node(d, d.nz - 1, (int)t);
+    t -= d.nx;
+    if (t < nzi) return gf_node(d, 1 + (int)t, 0);
+    t -= nzi;
+    if (t < nzi) return gf_node(d, 1 + (int)t, d.nx - 1);
+    t -= nzi;
+    const int i = (int)(t / nzi);
+    return gf_node(d, 1 + (int)(t - (long long)i * nzi), 1 + i);
+}
+
+// (hi, lo) + b in FP32 pairs: two-sum of hi and b, then renormalised
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float b) {
+    const float s = hi + b;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (b - bb);
+    const float l = lo + err;
+    hi = s + l;
+    lo = l - (hi - s);
+}
+
+// Mixed path, interior node.  Stored normal stresses are deviations from
+// the element's reference pressure p_ref.  The node sums its four elements'
+// corner forces (elem_corner_forces, written by fl_rheol) with the
+// reference-stress differences to one neighbouring triangle (sigma_n) and the
+// p_ref differences, all small, so FP32 resolves the net force.  Damping and
+// the velocity increment are FP32; the velocity is carried as its hi/lo FP32
+// pair and written back to the FP64 array as hi + lo.
+__device__ __forceinline__ void node_interior_f(const DevParams &P, const DevClock *__restrict__ C, DevArrays &A,
+                                                const GfDims &d, long long n, int j, int i) {
+    const float *st = (const float *)A.stress0;
+    const float *frc = A.e_frc;
+    const long long E = d.E;
+    const long long en = gf_elem(d, j - 1, i - 1);
+    const float nxx = st[gf_s(d, en, 0, 1)], nzz = st[gf_s(d, en, 1, 1)], nxz = st[gf_s(d, en, 2, 1)];
+    float fx0 = 0.0f, fy0 = 0.0f;
+#pragma unroll
+    for (int qd = 0; qd < 4; ++qd) {
+        const int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+        const long long e = gf_elem(d, je, ie);
+        const int c = 3 - qd; // this node's corner of element e
+        const float dp = hl_diff(A.pr_hi, A.pr_lo, e, en);
+        const float rxx = (st[gf_s(d, e, 0, 1)] - nxx) - dp;
+        const float rzz = (st[gf_s(d, e, 1, 1)] - nzz) - dp;
+        const float rxz = st[gf_s(d, e, 2, 1)] - nxz;
+        const float gx = frc[(4 * c + 2) * E + e], gz = frc[(4 * c + 3) * E + e];
+        fx0 += frc[(4 * c + 0) * E + e] - (rxx * gx + rxz * gz);
+        fy0 += frc[(4 * c + 1) * E + e] - (rxz * gx + rzz * gz);
+    }
+    float f0 = fx0;
+    float f1 = fy0 - (float)(A.rmass[n] * P.g);
+    const float dtf = (float)C->dt;
+    float drat = dtf / (float)C->dt_elastic;
+    if (drat < 1.0f) drat = 1.0f;
+    float h0 = A.vel_hi[n], l0 = A.vel_lo[n], h1 = A.vel_hi[d.N + n], l1 = A.vel_lo[d.N + n];
+    const int c0 = A.ncod[n], c1 = A.ncod[d.N + n];
+    if ((c0 & 1) != 1 && fabsf(h0) > 1.0e-13f) f0 = f0 - P.f_demf * copysignf(fabsf(f0), h0);
+    if ((c1 & 2) != 2 && fabsf(h1) > 1.0e-13f) f1 = f1 - P.f_demf * copysignf(fabsf(f1), h1);
+    const float s = dtf / ((float)A.amass[n] * drat * drat);
+    double v0, v1;
+    if (c0 == 1) {
+        v0 = A.bc[n];
+        h0 = (float)v0;
+        l0 = (float)(v0 - (double)h0);
+    } else {
+        ff_add(h0, l0, s * f0);
+        v0 = (double)h0 + (double)l0;
+    }
+    if (c1 == 1) {
+        v1 = A.bc[d.N + n];
+        h1 = (float)v1;
+        l1 = (float)(v1 - (double)h1);
+    } else {
+        ff_add(h1, l1, s * f1);
+        v1 = (double)h1 + (double)l1;
+    }
+    A.vel[n] = v0;
+    A.vel[d.N + n] = v1;
+    A.vel_hi[n] = h0;
+    A.vel_lo[n] = l0;
+    A.vel_hi[d.N + n] = h1;
+    A.vel_lo[d.N + n] = l1;
+}
+
+template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long slot) {
+    if (slot >= d.N) return;
+    const long long n = node_of_slot(d, slot);
     const DevParams &P = *Pp;
     int j, i;
     node_ji(d, n, j, i);
@@ -312,43 +477,13 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
     double f0, f1;
     const bool interior = j > 0 && j < nz - 1 && i > 0 && i < nx - 1;
-    if (sizeof(R) == sizeof(float) && interior) {
-        // Mixed path.  Stored normal stresses are deviations from the
-        // element's reference pressure p_ref.  Around an interior node the
-        // triangle edges close, so subtracting one neighbouring triangle's
-        // stress (sigma_n) from every term leaves the force unchanged in
-        // exact arithmetic while the FP32 terms become small differences.
-        const long long en = gf_elem(d, j - 1, i - 1);
-        const float nxx = (float)st[gf_s(d, en, 0, 1)], nzz = (float)st[gf_s(d, en, 1, 1)],
-                    nxz = (float)st[gf_s(d, en, 2, 1)];
-        const double pn = A.p_ref[en];
-        float fx0 = 0.0f, fy0 = 0.0f;
-#pragma unroll
-        for (int qd = 0; qd < 4; ++qd) {
-            int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
-            long long e = gf_elem(d, je, ie);
-            QuadF q;
-            load_quad_rel(A, d, je, ie, q);
-            float ar[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) ar[k] = (float)area[gf_ek(d, e, k)];
-            float dx[3][4], dz[3][4];
-            shape_derivs_f(q, ar, dx, dz);
-            float dp = float(A.p_ref[e] - pn);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                int t = kk[qd][k], m = mm[qd][k];
-                float factor = 0.25f / ar[t];
-                float sxx = ((float)st[gf_s(d, e, 0, t)] - nxx) - dp;
-                float szz = ((float)st[gf_s(d, e, 1, t)] - nzz) - dp;
-                float sxz = (float)st[gf_s(d, e, 2, t)] - nxz;
-                fx0 -= factor * (sxx * dx[m][t] + sxz * dz[m][t]);
-                fy0 -= factor * (sxz * dx[m][t] + szz * dz[m][t]);
-            }
+    if constexpr (sizeof(R) == sizeof(float)) {
+        if (interior) {
+            node_interior_f(P, C, A, d, n, j, i);
+            return;
         }
-        f0 = (double)fx0;
-        f1 = (double)fy0 - A.rmass[n] * P.g;
-    } else {
+    }
+    {
         // FP64 path (and boundary nodes of the mixed path, from total stresses)
         const bool dev = sizeof(R) == sizeof(float);
         R fx0 = R(0.0), fy0 = R(0.0);
@@ -692,8 +827,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict
 // Temperature after the boundary conditions of fl_therm.f90:573-598 (top
 // row t_top, bottom row bot_bc or the flux condition, then the side columns
 // copied from their inner neighbours), read from the swept values `src`.
-__device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevArrays &A, const GfDims &d,
-                                                 const double *__restrict__ src, int j, int i) {
+template <class Src>
+__device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevArrays &A, const GfDims &d, Src src, int j,
+                                                 int i) {
     const int nx = d.nx, nz = d.nz;
     int ii = (i == 0 || nx == 2) ? 1 : (i == nx - 1 ? nx - 2 : i);
     if (j == 0) return P.t_top;
@@ -702,11 +838,11 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
         if (P.itemp_bc == 2) {
             int ie = ii < nx - 2 ? ii : nx - 2;
             double cond_eff = P.conduct[A.iphase[gf_elem(d, nz - 2, ie)] - 1];
-            return src[gf_node(d, nz - 2, ii)] +
+            return src(gf_node(d, nz - 2, ii)) +
                    P.bot_bc * (A.cord[d.N + gf_node(d, nz - 2, ii)] - A.cord[d.N + gf_node(d, nz - 1, ii)]) / cond_eff;
         }
     }
-    return src[gf_node(d, j, ii)];
+    return src(gf_node(d, j, ii));
 }
 
 // temp0 = temp (fl_therm.f90:46-48); temp = converged iterate with the
@@ -729,7 +865,7 @@ __device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp
     const double *src = (k & 1) ? b1 : b0;
     int j, i;
     node_ji(d, n, j, i);
-    double t = therm_bc_value(*Pp, A, d, src, j, i);
+    double t = therm_bc_value(*Pp, A, d, [src](long long m) { return src[m]; }, j, i);
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
 }
@@ -780,21 +916,21 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__
 }
 
 // sweep 0 (final = 0): dT0 = increment with old values; sweep 1 (final = 1):
-// upstream neighbours use T + dT0, then the BCs are applied.
+// upstream neighbours use T + dT0, and tnew = T + dT1 (FP64) is written.
+// The temperature differences come from the hi/lo FP32 split of T.
 __device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
     const int nx = d.nx, nz = d.nz;
     const long long E = d.E;
-    const double *T = A.temp;
-    const double Ts = T[n];
+    const float *th = A.temp_hi, *tl = A.temp_lo;
     float rhs = 0.0f, area_n = 0.0f;
     auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
     // temperature difference to the updated node; upstream nodes carry the
     // increment of sweep 0 in the final sweep
     auto dT = [&](long long m, bool up) {
-        float v = float(T[m] - Ts);
+        float v = hl_diff(th, tl, m, n);
         if (up && final_sweep) v += d0[m];
         return v;
     };
@@ -823,19 +959,24 @@ __device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ 
     if (!final_sweep)
         d0[n] = inc;
     else
-        tnew[n] = Ts + (double)inc;
+        tnew[n] = A.temp[n] + (double)inc;
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep) {
     b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// temp0 = temp; temp = tnew with the boundary conditions (which read tnew
+// at neighbours, never the temp being overwritten), and its split
 __device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
-    double t = therm_bc_value(*Pp, A, d, tnew, j, i);
+    const double t = therm_bc_value(*Pp, A, d, [tnew](long long m) { return tnew[m]; }, j, i);
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
+    const float h = (float)t;
+    A.temp_hi[n] = h;
+    A.temp_lo[n] = (float)(t - (double)h);
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew) {
     b_k_therm_apply32(Pp, A, d, tnew, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -1342,6 +1483,36 @@ template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, 
     }
 }
 
+namespace {
+namespace gfk {
+__global__ void __launch_bounds__(GF_THREADS) k_elem_forces(DevArrays A, GfDims d) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    int j, i;
+    elem_ji(d, e, j, i);
+    const float *st = (const float *)A.stress0;
+    const float *area = (const float *)A.area;
+    float ar[4], sn[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ar[k] = area[gf_ek(d, e, k)];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) sn[c][k] = st[gf_s(d, e, c, k)];
+    }
+    QuadF q;
+    load_quad_rel(A, d, j, i, q);
+    float dx[3][4], dz[3][4];
+    shape_derivs_f(q, ar, dx, dz);
+    elem_corner_forces(dx, dz, ar, sn, A.e_frc, d.E, e);
+}
+} // namespace gfk
+} // namespace
+
+template <class R> void GfKernels<R>::elem_forces(const GfLaunch &g) {
+    using namespace gfk;
+    if (sizeof(R) == sizeof(float)) GF_LAUNCH(k_elem_forces, g.d.E, g.A, g.d);
+}
+
 template <class R> void GfKernels<R>::node(const GfLaunch &g) {
     using namespace gfk;
     GF_LAUNCH(k_node<R>, g.d.N, g.P, g.C, g.A, g.d);
@@ -1406,6 +1577,8 @@ template <class R> void GfKernels<R>::split_nodes(const GfLaunch &g) {
     if (!g.A.cord_hi) return;
     GF_LAUNCH(k_split, 2 * g.d.N, g.A.cord, g.A.cord_hi, g.A.cord_lo, 2 * g.d.N);
     GF_LAUNCH(k_split, 2 * g.d.N, g.A.vel, g.A.vel_hi, g.A.vel_lo, 2 * g.d.N);
+    if (g.A.pr_hi) GF_LAUNCH(k_split, g.d.E, g.A.p_ref, g.A.pr_hi, g.A.pr_lo, g.d.E);
+    if (g.A.temp_hi) GF_LAUNCH(k_split, g.d.N, g.A.temp, g.A.temp_hi, g.A.temp_lo, g.d.N);
 }
 
 template <class R> void GfKernels<R>::phase_recount_all(const GfLaunch &g) {
@@ -1466,6 +1639,7 @@ template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_out(co
 template <class R> void GfKernels<R>::stress_in(const GfLaunch &g, const double *src) {
     using namespace gfk;
     GF_LAUNCH(k_stress_in<R>, g.d.E, src, (R *)g.A.stress0, g.A.p_ref, g.d);
+    if (g.A.pr_hi) GF_LAUNCH(k_split, g.d.E, g.A.p_ref, g.A.pr_hi, g.A.pr_lo, g.d.E);
 }
 
 template <class R> void GfKernels<R>::stress_out(const GfLaunch &g, double *dst) {

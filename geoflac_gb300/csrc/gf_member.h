@@ -22,6 +22,8 @@ int gf_ctx_view(gf_ctx *c, GfMemberView *v);
 unsigned gf_ctx_signature(const gf_ctx *c);
 void gf_ctx_advance(gf_ctx *c, unsigned sig); // host bookkeeping after one step
 int gf_ctx_take_status(gf_ctx *c);
+// the member's stresses or mesh were changed outside its own calls
+void gf_ctx_invalidate_forces(gf_ctx *c);
 // the device-side part of rsflac.f90:197-236 once the restart files are
 // uploaded and marker2elem has run: init_areas, temp0 = temp, heating and
 // strain-rate accumulators reset, rmasses, init_visc, dt_mass, dtavg /
