@@ -144,7 +144,7 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
     if (sig & 1u) {
         if (sig & 2u) { // change_phase
             for_tiles(a, K_M, sm, cur, [&](const BatchMember &m, long long i) {
-                b_k_phase_markers(m.P, m.A, m.d, m.nmarkers, i);
+                b_k_phase_markers32(m.P, m.A, m.d, m.nmarkers, i);
             });
             GF_SYNC();
             for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
@@ -187,7 +187,7 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
             for_members(a, [&](const BatchMember &m) { b_k_frac_fix<R>(m.P, m.C, m.A, m.d); });
             GF_SYNC();
             for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
-                b_k_node_gather_tri(m.A.e_tri, m.A.rmass, m.d, i);
+                b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.rmass, m.d, i);
             });
             GF_SYNC();
         }
@@ -206,7 +206,7 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
             GF_SYNC();
             for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
                 if (m.idt_scale != 0)
-                    b_k_node_gather_tri(m.A.e_tri, m.A.amass, m.d, i);
+                    b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.amass, m.d, i);
                 else if (i < m.d.N)
                     m.A.amass[i] = m.A.rmass[i];
             });

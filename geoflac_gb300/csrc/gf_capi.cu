@@ -134,6 +134,13 @@ void fill_params(DevParams &P, const gf_params &p) {
     }
     P.f_ten_off = (float)p.ten_off;
     P.f_demf = (float)p.demf;
+    for (int k = 0; k < GF_MAXPH; ++k) {
+        P.f_alfa[k] = (float)p.alfa[k];
+        P.f_beta[k] = (float)p.beta[k];
+        P.diffu[k] = (p.den[k] != 0.0 && p.cp[k] != 0.0) ? p.conduct[k] / p.den[k] / p.cp[k] : 0.0;
+    }
+    P.f_fmagma_max = (float)p.fmagma_max;
+    P.f_rho_magma = (float)p.rho_magma;
     P.f_g = (float)p.g;
 }
 

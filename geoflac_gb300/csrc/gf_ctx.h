@@ -33,6 +33,8 @@ struct DevParams {
         f_cond[GF_MAXPH], f_den[GF_MAXPH], f_pln[GF_MAXPH], f_lacoef[GF_MAXPH], f_eactiv[GF_MAXPH],
         f_vactiv[GF_MAXPH];
     float f_ten_off, f_demf, f_g;
+    float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
+    double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:108)
 };
 
 // Scalars the step reads and writes, resident on the device so that a

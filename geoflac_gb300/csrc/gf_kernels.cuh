@@ -321,6 +321,57 @@ __device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims 
     return ed;
 }
 
+// Eff_dens in FP32 for the mixed path (same formula as eff_dens; depths from
+// the hi parts of the coordinates, the pressure from the stored deviations
+// plus p_ref, temperatures from the hi/lo split).
+__device__ float eff_dens_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+                              int *wrote_frac, float *frac_val) {
+    const float den_ramp_dist = 30e3f, amp410 = 0.05f, amp660 = 0.085f;
+    const float *zh = A.cord_hi + d.N, *th = A.temp_hi;
+    const float *st = (const float *)A.stress0;
+    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    float zcord = 0.25f * (zh[n1] + zh[n1 + 1] + zh[n3] + zh[n3 + 1]);
+    float tmpr0 = 0.25f * (th[n1] + th[n1 + 1] + th[n3] + th[n3 + 1]);
+    float zsurf = 0.50f * (zh[gf_node(d, 0, i)] + zh[gf_node(d, 0, i + 1)]);
+    float tmpr = (zsurf - zcord) * 1e-3f * 0.3f + tmpr0;
+    int iph = A.iphase[e];
+    float deptmpr410 = -101.58f * (tmpr + 273.0f) - 216828.0f;
+    float den_amp = 1.0f;
+    *wrote_frac = 0;
+    if (deptmpr410 > zcord) {
+        float f = fminf(1.0f, fmaxf(0.0f, (deptmpr410 - zcord) / den_ramp_dist));
+        *wrote_frac = 1;
+        *frac_val = f;
+        den_amp = 1.0f + amp410 * f;
+    }
+    float deptmpr660 = 66.55f * (tmpr + 273.0f) - 788494.0f;
+    if (deptmpr660 > zcord) {
+        float f = fminf(1.0f, fmaxf(0.0f, (deptmpr660 - zcord) / den_ramp_dist));
+        *wrote_frac = 1;
+        *frac_val = f;
+        den_amp = 1.05f + amp660 * f;
+    }
+    float press = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) press = press - (st[gf_s(d, e, 0, k)] + st[gf_s(d, e, 1, k)] + st[gf_s(d, e, 3, k)]);
+    press = press / 12.0f + A.pr_hi[e];
+    float ed = 0.0f;
+    for (int k = 0; k < P.nphase; ++k) {
+        float ratio = (float)A.phase_ratio[gf_pr(d, e, k)];
+        if (ratio < 0.01f) continue;
+        float dens = P.f_den[k] * (1.0f - P.f_alfa[k] * tmpr + P.f_beta[k] * press);
+        press = dens * P.f_g * zcord;
+        dens = P.f_den[k] * (1.0f - P.f_alfa[k] * tmpr + P.f_beta[k] * press);
+        ed = ed + ratio * dens;
+    }
+    if (iph == 4 || iph == 8 || iph == 9 || iph == 16 || iph == 18) ed = ed * den_amp;
+    if (A.fmagma) {
+        float fma = fminf((float)(A.fmagma[e] + A.fmagma2[e]), P.f_fmagma_max);
+        ed = ed - fma * (ed - P.f_rho_magma);
+    }
+    return ed;
+}
+
 // ---------------------------------------------------------------- rheology
 
 template <class R>

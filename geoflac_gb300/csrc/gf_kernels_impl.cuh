@@ -990,15 +990,26 @@ template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams
     int j, i;
     elem_ji(d, e, j, i);
     int wrote = 0;
-    double fval = 0.0;
-    double dens = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
-    A.e_dens[e] = dens;
-    // each triangle's share c1d12/area*dens (rmasses.f90:271-287), computed
-    // once here with the reference's operations and gathered per node
     const R *area = (const R *)A.area;
-    const double c1d12 = 1.0 / 12.0;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // mixed: FP32 density and FP32 triangle shares
+        float fval = 0.0f;
+        const float dens = eff_dens_f32(*Pp, A, d, j, i, e, &wrote, &fval);
+        A.e_dens[e] = (double)dens;
+        float *tri = (float *)A.e_tri;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 / (double)area[gf_ek(d, e, k)] * dens;
+        for (int k = 0; k < 4; ++k) tri[k * d.E + e] = (1.0f / 12.0f) / area[gf_ek(d, e, k)] * dens;
+    } else {
+        double fval = 0.0;
+        double dens = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
+        A.e_dens[e] = dens;
+        // each triangle's share c1d12/area*dens (rmasses.f90:271-287),
+        // computed once here with the reference's operations and gathered
+        // per node
+        const double c1d12 = 1.0 / 12.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 / (double)area[gf_ek(d, e, k)] * dens;
+    }
     if (wrote) {
         // serial position of this element in the coloured sweep
         int ib = i & 1, jb = j & 1;
@@ -1050,11 +1061,14 @@ __device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3},
 // dt_mass.f90:74-81), then each element's triangles containing the node in
 // the order A, B, C, D.  Every element in a node's neighbourhood has a
 // different colour, so this is the serial order of the coloured scatter.
-__device__ __forceinline__ void b_k_node_gather_tri(const double *__restrict__ tri, double *__restrict__ out, GfDims d, long long n) {
+// T = double: FP64 shares summed in the reference's order; T = float: the
+// mixed path's FP32 shares
+template <class T>
+__device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d, long long n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
-    double acc = 0.0;
+    T acc = T(0);
     int ord[4];
     // the node is vertex 4 of quad (j-1,i-1), 2 of (j-1,i), 3 of (j,i-1), 1 of (j,i)
     int je_[4] = {j - 1, j - 1, j, j}, ie_[4] = {i - 1, i, i - 1, i}, lv[4] = {3, 1, 2, 0};
@@ -1071,10 +1085,11 @@ __device__ __forceinline__ void b_k_node_gather_tri(const double *__restrict__ t
 #pragma unroll
             for (int t = 0; t < 3; ++t) acc = acc + tri[c_vtx_tris[lv[q]][t] * d.E + e];
         }
-    out[n] = acc;
+    out[n] = (double)acc;
 }
-__global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const double *__restrict__ tri, double *__restrict__ out, GfDims d) {
-    b_k_node_gather_tri(tri, out, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+template <class T>
+__global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d) {
+    b_k_node_gather_tri<T>(tri, out, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
@@ -1083,66 +1098,84 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
     const DevParams &P = *Pp;
     double dl = 1e300, vmax = 0.0, dmax = 0.0;
     unsigned pm = 0;
-    if (t < d.E && sizeof(R) == sizeof(float)) {
+    if constexpr (sizeof(R) == sizeof(float)) {
         // mixed: edge lengths and 1/(area*length) in FP32 from the hi/lo
-        // coordinates; the minimum over elements stays FP64
-        long long e = t;
-        int j, i;
-        elem_ji(d, e, j, i);
-        const float *area = (const float *)A.area;
-        QuadF q;
-        load_quad_rel(A, d, j, i, q);
-        auto len = [&](int a, int b) {
-            float ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
-            return sqrtf(ddx * ddx + ddy * ddy);
-        };
-        float a0 = area[gf_ek(d, e, 0)], a1 = area[gf_ek(d, e, 1)], a2 = area[gf_ek(d, e, 2)],
-              a3 = area[gf_ek(d, e, 3)];
-        float l, df = 1e30f;
-        l = len(1, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a2 * l));
-        l = len(3, 1); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a2 * l));
-        l = len(3, 2); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a3 * l));
-        l = len(2, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a3 * l));
-        l = len(3, 0); df = fminf(df, 1.0f / (a2 * l)); df = fminf(df, 1.0f / (a3 * l));
-        l = len(1, 2); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a1 * l));
-        dl = (double)df;
-        int iph = A.iphase[e] - 1;
-        dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
-        pm = 1u << iph;
-    } else if (t < d.E) {
-        long long e = t;
-        int j, i;
-        elem_ji(d, e, j, i);
-        const R *area = (const R *)A.area;
-        Quad q;
-        load_quad(A.cord, d, j, i, q);
-        auto len = [&](int a, int b) {
-            double ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
-            return sqrt(ddx * ddx + ddy * ddy);
-        };
-        double a0 = (double)area[gf_ek(d, e, 0)], a1 = (double)area[gf_ek(d, e, 1)], a2 = (double)area[gf_ek(d, e, 2)],
-               a3 = (double)area[gf_ek(d, e, 3)];
-        double l;
-        l = len(1, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a2 * l));
-        l = len(3, 1); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a2 * l));
-        l = len(3, 2); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-        l = len(2, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-        l = len(3, 0); dl = fmin(dl, 1.0 / (a2 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-        l = len(1, 2); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a1 * l));
-        int iph = A.iphase[e] - 1;
-        dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
-        pm = 1u << iph;
-    }
-    if (t < d.N) vmax = fmax(fabs(A.vel[t]), fabs(A.vel[d.N + t]));
-    dl = warp_min(dl);
-    vmax = warp_max(vmax);
-    dmax = warp_max(dmax);
-    for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
-    if ((threadIdx.x & 31) == 0) {
-        atomic_min_pos(&C->r_dlmin, dl);
-        atomic_max_pos(&C->r_velmax, vmax);
-        atomic_max_pos(&C->r_diffmax, dmax);
-        atomicOr(&C->phase_mask, pm);
+        // coordinates, |vel| from the hi parts; the warp minima and maxima of
+        // these FP32 values convert to FP64 exactly, and the minimum over
+        // elements is taken on their FP64 values
+        float df = 1e30f, vf = 0.0f;
+        if (t < d.E) {
+            long long e = t;
+            int j, i;
+            elem_ji(d, e, j, i);
+            const float *area = (const float *)A.area;
+            QuadF q;
+            load_quad_rel(A, d, j, i, q);
+            auto len = [&](int a, int b) {
+                float ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
+                return sqrtf(ddx * ddx + ddy * ddy);
+            };
+            float a0 = area[gf_ek(d, e, 0)], a1 = area[gf_ek(d, e, 1)], a2 = area[gf_ek(d, e, 2)],
+                  a3 = area[gf_ek(d, e, 3)];
+            float l;
+            l = len(1, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a2 * l));
+            l = len(3, 1); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a2 * l));
+            l = len(3, 2); df = fminf(df, 1.0f / (a1 * l)); df = fminf(df, 1.0f / (a3 * l));
+            l = len(2, 0); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a3 * l));
+            l = len(3, 0); df = fminf(df, 1.0f / (a2 * l)); df = fminf(df, 1.0f / (a3 * l));
+            l = len(1, 2); df = fminf(df, 1.0f / (a0 * l)); df = fminf(df, 1.0f / (a1 * l));
+            pm = 1u << (A.iphase[e] - 1);
+        }
+        if (t < d.N) vf = fmaxf(fabsf(A.vel_hi[t]), fabsf(A.vel_hi[d.N + t]));
+        df = warp_min(df);
+        vf = warp_max(vf);
+        for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
+        if ((threadIdx.x & 31) == 0) {
+            atomic_min_pos(&C->r_dlmin, df < 1e30f ? (double)df : 1e300);
+            atomic_max_pos(&C->r_velmax, (double)vf);
+            // the largest diffusivity of the phases present (dt_mass.f90:108)
+            for (int k = 0; k < P.nphase; ++k)
+                if (pm & (1u << k)) dmax = fmax(dmax, P.diffu[k]);
+            atomic_max_pos(&C->r_diffmax, dmax);
+            atomicOr(&C->phase_mask, pm);
+        }
+        return;
+    } else {
+        if (t < d.E) {
+            long long e = t;
+            int j, i;
+            elem_ji(d, e, j, i);
+            const R *area = (const R *)A.area;
+            Quad q;
+            load_quad(A.cord, d, j, i, q);
+            auto len = [&](int a, int b) {
+                double ddx = q.x[a] - q.x[b], ddy = q.y[a] - q.y[b];
+                return sqrt(ddx * ddx + ddy * ddy);
+            };
+            double a0 = (double)area[gf_ek(d, e, 0)], a1 = (double)area[gf_ek(d, e, 1)],
+                   a2 = (double)area[gf_ek(d, e, 2)], a3 = (double)area[gf_ek(d, e, 3)];
+            double l;
+            l = len(1, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a2 * l));
+            l = len(3, 1); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a2 * l));
+            l = len(3, 2); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+            l = len(2, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+            l = len(3, 0); dl = fmin(dl, 1.0 / (a2 * l)); dl = fmin(dl, 1.0 / (a3 * l));
+            l = len(1, 2); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a1 * l));
+            int iph = A.iphase[e] - 1;
+            dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
+            pm = 1u << iph;
+        }
+        if (t < d.N) vmax = fmax(fabs(A.vel[t]), fabs(A.vel[d.N + t]));
+        dl = warp_min(dl);
+        vmax = warp_max(vmax);
+        dmax = warp_max(dmax);
+        for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
+        if ((threadIdx.x & 31) == 0) {
+            atomic_min_pos(&C->r_dlmin, dl);
+            atomic_max_pos(&C->r_velmax, vmax);
+            atomic_max_pos(&C->r_diffmax, dmax);
+            atomicOr(&C->phase_mask, pm);
+        }
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
@@ -1212,8 +1245,15 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
         double rho_inert2 = (P.xReyn * P.v_min) / (vel_max * fabs(P.rzbo));
         if (rho_inert > rho_inert2) rho_inert = rho_inert2;
     }
+    if constexpr (sizeof(R) == sizeof(float)) {
+        const float r = (float)(c1d12 * rho_inert);
+        float *tri = (float *)A.e_tri;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
+        for (int k = 0; k < 4; ++k) tri[k * d.E + e] = r / area[gf_ek(d, e, k)];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
+    }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
     b_k_elem_am3<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -1348,6 +1388,117 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
 }
 __global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
     b_k_phase_markers(Pp, A, d, nmarkers, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// The same rules in FP32 for the mixed path: the marker's depth below the
+// surface from coordinate differences of the hi/lo splits, its temperature
+// from the hi parts.  Decisions within FP32 rounding of a threshold may
+// differ from the FP64 path.
+__device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, long long kk) {
+    if (kk >= nmarkers) return;
+    if (A.mark_dead[kk] == 0) return;
+    const DevParams &P = *Pp;
+    const int nz = d.nz;
+    int n = A.mark_ntriag[kk];
+    int k = (n - 1) % 2 + 1;
+    int j = ((n - k) / 2) % (nz - 1);
+    int i = (n - k) / 2 / (nz - 1);
+    const float a1 = (float)A.mark_a1[kk], a2 = (float)A.mark_a2[kk], a3 = 1.0f - a1 - a2;
+    long long p1, p2, p3;
+    if (k == 1) {
+        p1 = gf_node(d, j, i); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j, i + 1);
+    } else {
+        p1 = gf_node(d, j, i + 1); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j + 1, i + 1);
+    }
+    const float *zh = A.cord_hi + d.N, *zl = A.cord_lo + d.N, *th = A.temp_hi;
+    const long long s0 = gf_node(d, 0, i), s1 = gf_node(d, 0, i + 1);
+    // depth = 0.5 * (z_s0 + z_s1) - sum a_k z_pk, as differences to z_s0
+    const float ds1 = hl_diff(zh, zl, s1, s0);
+    const float y1 = hl_diff(zh, zl, p1, s0), y2 = hl_diff(zh, zl, p2, s0), y3 = hl_diff(zh, zl, p3, s0);
+    const float depth = 0.5f * ds1 - (y1 * a1 + y2 * a2 + y3 * a3);
+    if (depth > 200e3f) return;
+    const float tmpr = th[p1] * a1 + th[p2] * a2 + th[p3] * a3;
+    int iph = A.mark_phase[kk];
+    long long e = gf_elem(d, j, i);
+    const float rho_g = 3000.0f * P.f_g;
+    long long total = (long long)P.nphase * d.E;
+    auto pr = [&](long long eb, int ph1) {
+        long long off = (long long)(ph1 - 1) + (long long)P.nphase * eb;
+        return (off < 0 || off >= total) ? 0.0 : A.phase_ratio[off];
+    };
+    int newph = 0;
+    switch (iph) {
+    case 4: case 8: {
+        if (depth > 150e3f) break;
+        float trpres = 2.1e9f + (7.5e9f - 2.1e9f) * (tmpr - 730.0f) / (500.0f - 730.0f);
+        float trpres2 = 2.1e9f + (0.6e9f - 2.1e9f) * (tmpr - 730.0f) / (670.0f - 730.0f);
+        float press = rho_g * depth;
+        float pg = fabsf(press * 1e-9f);
+        float solidus = -5.02f * (pg * pg) + 1.32e2f * pg + 1.09e3f + 35.0f;
+        if (press < trpres && press > trpres2) {
+            int jb0 = min(j + 2, nz - 1), jb1 = min(j + 1 + P.nelem_serp, nz - 1);
+            for (int jb = jb0; jb <= jb1; ++jb) {
+                long long eb = gf_elem(d, jb - 1, i);
+                if (pr(eb, 3) > 0.8 || pr(eb, 7) > 0.8 || pr(eb, 1) > 0.8 || pr(eb, 11) > 0.8) {
+                    newph = 9;
+                    break;
+                }
+            }
+        } else if (tmpr >= solidus + 35.0f) {
+            newph = 18;
+        }
+        break;
+    }
+    case 10: case 3: case 7: {
+        float press = rho_g * depth;
+        if (P.eclogite_rule == 1) {
+            if (tmpr >= 600.0f && press >= 1.5e9f) newph = 13;
+        } else {
+            float trpres = -0.3e9f + 2.2e6f * tmpr;
+            float trpres2 = 20.1e9f - 0.0375e9f * tmpr;
+            if (!(tmpr < 400.0f || depth < 20e3f || press < trpres || press < trpres2)) newph = 13;
+        }
+        break;
+    }
+    case 9: {
+        float trpres = 2.1e9f + (7.5e9f - 2.1e9f) * (tmpr - 730.0f) / (500.0f - 730.0f);
+        float trpres2 = 2.1e9f + (0.2e9f - 2.1e9f) * (tmpr - 730.0f) / (650.0f - 730.0f);
+        float press = rho_g * depth;
+        if (!(tmpr < 550.0f || (press < trpres && press > trpres2))) newph = 4;
+        break;
+    }
+    case 1:
+        if (!(tmpr < 80.0f && depth < 2e3f)) newph = 11;
+        break;
+    case 11:
+        if (!(tmpr < 250.0f && depth < 7e3f)) newph = 17;
+        break;
+    case 17: {
+        float trpres = 0.88e9f - (0.88e9f - 0.704e9f) * (710.8f - tmpr) / (710.8f - 662.3f);
+        if (!(rho_g * depth < trpres)) newph = 5;
+        break;
+    }
+    case 5: {
+        float trpres = 0.0f - (0.0f - 1.2e9f) * (500.0f - tmpr) / (500.0f - 600.0f);
+        if (!(rho_g * depth > trpres)) newph = 19;
+        break;
+    }
+    case 16: {
+        float dd = depth - 62e3f;
+        float trtmpr = 880.0f - 35e-9f * (dd * dd);
+        if (!(tmpr < trtmpr)) newph = 4;
+        break;
+    }
+    default:
+        break;
+    }
+    if (newph) {
+        A.e_flag[e] = 1;
+        A.mark_phase[kk] = (int8_t)newph;
+    }
+}
+__global__ void __launch_bounds__(GF_THREADS) k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
+    b_k_phase_markers32(Pp, A, d, nmarkers, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // count_phase_ratio (marker_data.f90:140-172) for flagged elements + aps
@@ -1529,7 +1680,7 @@ template <class R> void GfKernels<R>::rmasses(const GfLaunch &g) {
     GF_LAUNCH(k_elem_dens<R>, g.d.E, g.P, g.C, g.A, g.d);
     k_frac_fix<R><<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d);
     ++*g.launches;
-    GF_LAUNCH(k_node_gather_tri, g.d.N, g.A.e_tri, g.A.rmass, g.d);
+    GF_LAUNCH(k_node_gather_tri<R>, g.d.N, (const R *)g.A.e_tri, g.A.rmass, g.d);
 }
 
 template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
@@ -1544,7 +1695,7 @@ template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
         cudaMemcpyAsync(g.A.amass, g.A.rmass, sizeof(double) * g.d.N, cudaMemcpyDeviceToDevice, g.s);
     } else {
         GF_LAUNCH(k_elem_am3<R>, g.d.E, g.P, g.C, g.A, g.d);
-        GF_LAUNCH(k_node_gather_tri, g.d.N, g.A.e_tri, g.A.amass, g.d);
+        GF_LAUNCH(k_node_gather_tri<R>, g.d.N, (const R *)g.A.e_tri, g.A.amass, g.d);
     }
 }
 
@@ -1555,7 +1706,10 @@ template <class R> void GfKernels<R>::init_visc(const GfLaunch &g) {
 
 template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarkers) {
     using namespace gfk;
-    GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
+    if (sizeof(R) == sizeof(float))
+        GF_LAUNCH(k_phase_markers32, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
+    else
+        GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
     GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 0);
 }
 
