@@ -3,9 +3,12 @@
 
 #include "gf_kernels.cuh"
 
-// resident CTAs per SM the register allocation of k_rheol is sized for
+// resident CTAs per SM the register allocation of k_rheol is sized for:
+// 1 for FP64 (no spills; the kernel is bound by the FP64 pipe), 3 for the
+// mixed path (80 registers; its few spills cost less than the occupancy
+// they buy)
 #ifndef GF_RHEOL_MINB
-#define GF_RHEOL_MINB 2
+#define GF_RHEOL_MINB (sizeof(R) == sizeof(float) ? 3 : 1)
 #endif
 
 // internal linkage: each precision's translation unit has its own copy
@@ -483,11 +486,46 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
             return;
         }
     }
-    {
-        // FP64 path (and boundary nodes of the mixed path, from total stresses)
-        const bool dev = sizeof(R) == sizeof(float);
-        R fx0 = R(0.0), fy0 = R(0.0);
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // Mixed path, boundary node: the elements' corner forces plus their
+        // total reference stress (triangle-1 stress less p_ref) against the
+        // corner geometry G_c, in FP64 from the node coordinates:
+        // 0.25/ar * grad N = 0.25 * (y_u - y_v, x_v - x_u) for the edge (u, v)
+        // that shape_derivs uses for vertex m of triangle t.
+        const int uv[4][3][2] = {{{1, 2}, {2, 0}, {0, 1}}, {{1, 3}, {3, 2}, {2, 1}},
+                                 {{1, 3}, {3, 0}, {0, 1}}, {{3, 2}, {2, 0}, {0, 3}}};
+        const float *frc = A.e_frc;
+        const double *cx = A.cord, *cy = A.cord + d.N;
         double gx = 0.0, gy = 0.0;
+#pragma unroll
+        for (int qd = 0; qd < 4; ++qd) {
+            int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+            if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
+            const long long e = gf_elem(d, je, ie);
+            const int c = 3 - qd;
+            long long nn[4];
+            quad_nodes(d, je, ie, nn);
+            double Gx = 0.0, Gz = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int t = kk[qd][k], m = mm[qd][k];
+                const long long u = nn[uv[t][m][0]], v = nn[uv[t][m][1]];
+                Gx += cy[u] - cy[v];
+                Gz += cx[v] - cx[u];
+            }
+            Gx *= 0.25;
+            Gz *= 0.25;
+            const double pe = A.p_ref[e];
+            const double rxx = (double)st[gf_s(d, e, 0, 1)] - pe, rzz = (double)st[gf_s(d, e, 1, 1)] - pe,
+                         rxz = (double)st[gf_s(d, e, 2, 1)];
+            gx += (double)frc[(4 * c + 0) * d.E + e] - (rxx * Gx + rxz * Gz);
+            gy += (double)frc[(4 * c + 1) * d.E + e] - (rxz * Gx + rzz * Gz);
+        }
+        f0 = gx;
+        f1 = gy - A.rmass[n] * P.g;
+    } else {
+        // FP64 path: the reference's gather from the four quads
+        R fx0 = R(0.0), fy0 = R(0.0);
 #pragma unroll
         for (int qd = 0; qd < 4; ++qd) {
             int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
@@ -498,37 +536,21 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
             R ar[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
-            if (!dev) {
-                R dx[3][4], dz[3][4];
-                shape_derivs<R>(q, ar, dx, dz);
+            R dx[3][4], dz[3][4];
+            shape_derivs<R>(q, ar, dx, dz);
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    int t = kk[qd][k], m = mm[qd][k];
-                    R factor = R(0.25) / ar[t];
-                    R sxx = st[gf_s(d, e, 0, t)], szz = st[gf_s(d, e, 1, t)], sxz = st[gf_s(d, e, 2, t)];
-                    R fx = factor * (sxx * dx[m][t] + sxz * dz[m][t]);
-                    R fy = factor * (sxz * dx[m][t] + szz * dz[m][t]);
-                    fx0 = fx0 - fx;
-                    fy0 = fy0 - fy;
-                }
-            } else {
-                double ard[4] = {(double)ar[0], (double)ar[1], (double)ar[2], (double)ar[3]};
-                double dx[3][4], dz[3][4];
-                shape_derivs<double>(q, ard, dx, dz);
-                double pe = A.p_ref[e];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    int t = kk[qd][k], m = mm[qd][k];
-                    double factor = 0.25 / ard[t];
-                    double sxx = (double)st[gf_s(d, e, 0, t)] - pe, szz = (double)st[gf_s(d, e, 1, t)] - pe,
-                           sxz = (double)st[gf_s(d, e, 2, t)];
-                    gx -= factor * (sxx * dx[m][t] + sxz * dz[m][t]);
-                    gy -= factor * (sxz * dx[m][t] + szz * dz[m][t]);
-                }
+            for (int k = 0; k < 3; ++k) {
+                int t = kk[qd][k], m = mm[qd][k];
+                R factor = R(0.25) / ar[t];
+                R sxx = st[gf_s(d, e, 0, t)], szz = st[gf_s(d, e, 1, t)], sxz = st[gf_s(d, e, 2, t)];
+                R fx = factor * (sxx * dx[m][t] + sxz * dz[m][t]);
+                R fy = factor * (sxz * dx[m][t] + szz * dz[m][t]);
+                fx0 = fx0 - fx;
+                fy0 = fy0 - fy;
             }
         }
-        f0 = dev ? gx : (double)fx0;
-        f1 = (dev ? gy : (double)fy0) - A.rmass[n] * P.g;
+        f0 = (double)fx0;
+        f1 = (double)fy0 - A.rmass[n] * P.g;
     }
     const double *cord = A.cord;
     if (P.nyhydro > 0 && j == 0) { // water load on the surface
