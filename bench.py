@@ -287,6 +287,23 @@ def run_ours(args):
     for f in ("vel", "cord", "temp", "stress0", "aps"):
         a, b = res["mixed"]["g"].state[f], fp["g"].state[f]
         mixed_err[f] = float(abs(a - b).max() / max(abs(b).max(), 1e-300))
+    # the model's own sensitivity: the FP64 run from an initial stress
+    # perturbed by a relative 1e-7 (FP32 rounding), same steps
+    import numpy as np
+
+    from geoflac_gb300 import capi as _capi
+
+    gp = _make_model(inp, "fp64")
+    st = gp.download(_capi.F_STRESS)["stress0"]
+    st[...] = st * (1.0 + 1e-7 * np.random.default_rng(7).standard_normal(st.shape))
+    gp.upload(_capi.F_STRESS)
+    gp.step(args.warmup + args.steps)
+    gp.download()
+    perturbed_err = {}
+    for f in ("vel", "cord", "temp", "stress0", "aps"):
+        a, b = gp.state[f], fp["g"].state[f]
+        perturbed_err[f] = float(abs(a - b).max() / max(abs(b).max(), 1e-300))
+    gp.close()
     value = ws * E * args.steps / fp["t"]
     mixed_value = ws * E * args.steps / res["mixed"]["t"]
     # dominant kernel: fl_rheol (k_rheol), timed alone
@@ -309,7 +326,8 @@ def run_ours(args):
                    "l2": "512 MiB buffer written between timed steps"},
         "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
                   "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes",
-                  "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup},
+                  "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup,
+                  "fp64_perturbed_1e-7_rel_err": perturbed_err},
         "therm_sweeps_fp64": fp["g"].clock.therm_sweeps,
         "e2e": {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,
@@ -385,10 +403,11 @@ def bench_batch(args, workdir: str, local: int):
 
 
 def bench_surrogate(args, workdir: str):
-    """Surrogate leg: snapshots of a 256-member sweep from the ensemble
-    driver, FNO training (the library's tcgen05 kernels), then screening of
-    a fresh 256-member sweep over `interval` steps against the plain
-    ensemble step of the same members (timed on the same GPU)."""
+    """Surrogate leg: snapshots of a training sweep (2048 members, 5
+    snapshots each) from the ensemble driver, FNO training (the library's
+    tcgen05 kernels), then screening of a fresh 256-member sweep over
+    `interval` steps against the plain ensemble step of the same members
+    (timed on the same GPU)."""
     import numpy as np
     import torch
 
@@ -398,8 +417,9 @@ def bench_surrogate(args, workdir: str):
 
     cfg = FnoConfig()
     n, interval = args.members, args.sur_interval
+    nt = args.sur_train_members
     t0 = time.time()
-    tr = ensemble(n, workdir)
+    tr = ensemble(nt, workdir)
     tb = Batch([m for m, _ in tr])
     tb.set_config(**args.batch_cfg)
     snaps = S.generate(tb, [p for _, p in tr], n_snap=args.sur_snaps, interval=interval, H=cfg.H, W=cfg.W)
@@ -407,7 +427,7 @@ def bench_surrogate(args, workdir: str):
     t_data = time.time() - t0
     sur = S.Surrogate(cfg, S.Normaliser.fit(snaps), seed=0)
     info = sur.train(snaps, epochs=args.sur_epochs, batch=64, lr=args.sur_lr)
-    pairs = n * (args.sur_snaps - 1)
+    pairs = nt * (args.sur_snaps - 1)
     del snaps
     tb.close()
     for m, _ in tr:
@@ -435,7 +455,8 @@ def bench_surrogate(args, workdir: str):
     torch.cuda.synchronize()
     res = S.screen(bb, sur, [p for _, p in fb], interval, cal["tol"])
     err = S.rel_errors(res["fields"], truth, res["raw_t"])
-    out = {"members": n, "interval_steps": interval, "grid": [cfg.H, cfg.W], "width": cfg.C,
+    out = {"members": n, "training_members": nt, "snapshots_per_member": args.sur_snaps,
+           "interval_steps": interval, "grid": [cfg.H, cfg.W], "width": cfg.C,
            "modes": [cfg.m1, cfg.m2], "layers": cfg.layers, "training_pairs": pairs, "epochs": args.sur_epochs,
            "train_seconds": info["seconds"], "train_loss_first": info["first_loss"],
            "train_loss_final": info["final_loss"], "data_seconds": t_data,
@@ -552,8 +573,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
-    ap.add_argument("--sur-epochs", type=int, default=30, help="surrogate training epochs (0: skip the surrogate)")
-    ap.add_argument("--sur-snaps", type=int, default=17, help="snapshots per member (pairs = members x (snaps - 1))")
+    ap.add_argument("--sur-epochs", type=int, default=20, help="surrogate training epochs (0: skip the surrogate)")
+    ap.add_argument("--sur-train-members", type=int, default=2048, help="members of the training sweep")
+    ap.add_argument("--sur-snaps", type=int, default=5,
+                    help="snapshots per training member (pairs = members x (snaps - 1))")
     ap.add_argument("--sur-interval", type=int, default=500, help="steps between snapshots and of the forecast")
     ap.add_argument("--sur-start", type=int, default=1000, help="plain steps of the fresh sweep before the forecast")
     ap.add_argument("--sur-lr", type=float, default=2e-3)

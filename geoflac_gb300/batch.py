@@ -95,10 +95,16 @@ def ensemble(n: int, workdir: str, seed: int = inpgen.ENSEMBLE_SEED, mode: str =
              scale: Optional[tuple] = None) -> List[tuple]:
     """n sweep members as (Flac, sampled parameters), .inp files written to
     workdir (9 markers per element)."""
-    out = []
-    for k in range(n):
+    from concurrent.futures import ThreadPoolExecutor
+
+    def host(k):
         m, prm = inpgen.ensemble_member(k, seed, scale or (80, 25, 400, 120))
         path = m.write(os.path.join(workdir, f"member_{k:04d}.inp"))
-        p, c, s = new_state(path)
-        out.append((Flac(p, c, s, mode), prm))
-    return out
+        return new_state(path), prm
+
+    # the host start-up (read_params + setflac) of the members runs in
+    # parallel (the library calls release the interpreter lock); the
+    # device contexts are then created in member order
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        states = list(ex.map(host, range(n)))
+    return [(Flac(p, c, s, mode), prm) for (p, c, s), prm in states]

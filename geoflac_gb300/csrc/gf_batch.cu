@@ -542,7 +542,7 @@ int build_tables(gf_batch *b) {
     GB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     GB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, c.threads, 0));
     if (occ < 1) return GF_ERR_UNSUPPORTED;
-    b->grid = sms * std::min(occ, c.ctas_per_sm);
+    const int full_grid = sms * std::min(occ, c.ctas_per_sm);
     const long long tile = (long long)c.threads * c.items_per_thread;
     for (int kind = 0; kind < K_KINDS; ++kind) {
         std::vector<int2> t;
@@ -561,6 +561,11 @@ int build_tables(gf_batch *b) {
             GB_CK(cudaMemcpy(b->d_tiles[kind], t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice));
         }
     }
+    // a small batch (e.g. a few members rerun after screening) runs on no
+    // more CTAs than it has element or node tiles: its grid barriers then
+    // involve few CTAs
+    const int work = std::max(1, std::max(b->ntile[K_E], b->ntile[K_N]));
+    b->grid = std::min(full_grid, work);
     drop_graphs(b);
     return GF_OK;
 }
