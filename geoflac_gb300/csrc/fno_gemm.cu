@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(GEMM_THREADS)
                 if (ep.bias && col0 + i < ep.N) x += ep.bias[col0 + i];
                 v[i] = x;
             }
-            if (ep.c_bf16) {
+            if (ep.c_bf16 == 1) {
                 __nv_bfloat16 *C = reinterpret_cast<__nv_bfloat16 *>(ep.C) + off;
                 if (full32 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0)) {
 #pragma unroll
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(GEMM_THREADS)
                             o.z += ep.beta * c.z;
                             o.w += ep.beta * c.w;
                         }
-                        *reinterpret_cast<float4 *>(C + i) = o;
+                        if (ep.c_bf16 != 2) *reinterpret_cast<float4 *>(C + i) = o;
                         v[i] = o.x;
                         v[i + 1] = o.y;
                         v[i + 2] = o.z;
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(GEMM_THREADS)
                     for (int i = 0; i < 32 && col0 + i < ep.N; ++i) {
                         float x = v[i];
                         if (ep.beta != 0.0f) x += ep.beta * C[i];
-                        C[i] = x;
+                        if (ep.c_bf16 != 2) C[i] = x;
                         v[i] = x;
                     }
                 }
@@ -373,7 +373,8 @@ int gf_gemm_bf16(const void *A, const void *B, void *C, int batch, int M, int N,
 int gf_gemm_bf16_ex(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda,
                     long long sA, long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha,
                     float beta, const float *bias, void *aux, int act, void *stream) {
-    if (!A || !B || !C || batch < 1 || M < 1 || N < 1 || K < 1) return GF_FNO_ERR_ARG;
+    if (!A || !B || (!C && !(c_bf16 == 2 && beta == 0.0f)) || batch < 1 || M < 1 || N < 1 || K < 1)
+        return GF_FNO_ERR_ARG;
     if (batch > 65535 || (M + BM - 1) / BM > 2147483647LL) return GF_FNO_ERR_ARG;
     // TMA: 16-byte aligned base addresses and row / batch strides
     if ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) return GF_FNO_ERR_ALIGN;
@@ -381,7 +382,9 @@ int gf_gemm_bf16_ex(const void *A, const void *B, void *C, int batch, int M, int
     if ((lda * 2) % 16 || (ldb * 2) % 16 || ((a_bcast ? 0 : sA) * 2) % 16 || (sB * 2) % 16 || K % 8)
         return GF_FNO_ERR_ALIGN;
     if (lda < K || ldb < K || ldc < N) return GF_FNO_ERR_ARG;
-    if (c_bf16 && (beta != 0.0f || aux)) return GF_FNO_ERR_ARG;
+    if (c_bf16 == 1 && (beta != 0.0f || aux)) return GF_FNO_ERR_ARG;
+    if (c_bf16 == 2 && !aux) return GF_FNO_ERR_ARG; // nothing would be stored
+    if (c_bf16 < 0 || c_bf16 > 2) return GF_FNO_ERR_ARG;
     if (aux && (reinterpret_cast<uintptr_t>(aux) & 15)) return GF_FNO_ERR_ALIGN;
     const int bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
     CUtensorMap ta, tb;

@@ -178,14 +178,19 @@ class Fno:
         return self.torch.cuda.current_stream().cuda_stream
 
     def gemm(self, A, B, Cout, batch, M, N, K, lda, sA, ldb, sB, ldc, sC, alpha=1.0, beta=0.0, bias=None,
-             aux=None, act=0):
-        c_bf16 = 1 if Cout.dtype == self.torch.bfloat16 else 0
+             aux=None, act=0, keep_c=True):
+        """keep_c=False (with aux): the FP32 C is only read (beta) or absent
+        (Cout None), and only the BF16 activation is written."""
+        if not keep_c:
+            c_bf16 = 2
+        else:
+            c_bf16 = 1 if Cout.dtype == self.torch.bfloat16 else 0
         _ck(self.lib.gf_gemm_bf16_ex(_p(A), _p(B), _p(Cout), batch, M, N, K, lda, sA, ldb, sB, ldc, sC, c_bf16,
                                      alpha, beta, _p(bias), _p(aux), act, self.s), "gemm")
 
-    def mm(self, A, Bw, out, M, N, K, beta=0.0, bias=None, aux=None, act=0):
+    def mm(self, A, Bw, out, M, N, K, beta=0.0, bias=None, aux=None, act=0, keep_c=True):
         """out[M, N] (+)= A[M, K] Bw[N, K]^T (+ bias); aux = BF16 out or GELU(out)."""
-        self.gemm(A, Bw, out, 1, M, N, K, K, 0, K, 0, N, 0, 1.0, beta, bias, aux, act)
+        self.gemm(A, Bw, out, 1, M, N, K, K, 0, K, 0, N, 0, 1.0, beta, bias, aux, act, keep_c)
 
     def tr(self, src, dst, batch, rows, cols):
         _ck(self.lib.gf_fno_transpose(_p(src), _p(dst), batch, rows, cols,
@@ -274,9 +279,11 @@ class Fno:
         bf = torch.bfloat16
         wb = {k: self.bf16(self.p[k]) for k in self.p if not k.startswith("R") and not k.endswith("_b")
               and not (k.startswith("b") and k[1:].isdigit())}
-        z = torch.empty((M, cfg.C), dtype=torch.float32, device="cuda")
+        # inference keeps only the BF16 activations (no FP32 copies of the
+        # pre-activations, which only the backward pass reads)
+        z = torch.empty((M, cfg.C), dtype=torch.float32, device="cuda") if train else None
         v = torch.empty((M, cfg.C), dtype=bf, device="cuda")
-        self.mm(x.view(M, cfg.cin), wb["lift_w"], z, M, cfg.C, cfg.cin, bias=self.p["lift_b"], aux=v)
+        self.mm(x.view(M, cfg.cin), wb["lift_w"], z, M, cfg.C, cfg.cin, bias=self.p["lift_b"], aux=v, keep_c=train)
         saved = {"x": x, "v": [], "z": [], "spec": [], "wb": wb}
         for l in range(cfg.layers):
             s_cl, sp = self.spectral(v.view(B, cfg.H, cfg.W, cfg.C), l, B, train)
@@ -284,15 +291,15 @@ class Fno:
             vn = torch.empty((M, cfg.C), dtype=bf, device="cuda")
             # z = v W^T + b + S(v); next input GELU(z) (z itself after the last layer)
             self.mm(v, wb[f"w{l}"], zl, M, cfg.C, cfg.C, beta=1.0, bias=self.p[f"b{l}"], aux=vn,
-                    act=1 if l < cfg.layers - 1 else 0)
+                    act=1 if l < cfg.layers - 1 else 0, keep_c=train)
             if train:
                 saved["v"].append(v)
                 saved["z"].append(zl)
                 saved["spec"].append(sp)
             v = vn
-        zp = torch.empty((M, cfg.P), dtype=torch.float32, device="cuda")
+        zp = torch.empty((M, cfg.P), dtype=torch.float32, device="cuda") if train else None
         hh = torch.empty((M, cfg.P), dtype=bf, device="cuda")
-        self.mm(v, wb["p1_w"], zp, M, cfg.P, cfg.C, bias=self.p["p1_b"], aux=hh, act=1)
+        self.mm(v, wb["p1_w"], zp, M, cfg.P, cfg.C, bias=self.p["p1_b"], aux=hh, act=1, keep_c=train)
         out = torch.empty((M, cfg.cout), dtype=torch.float32, device="cuda")
         self.mm(hh, wb["p2_w"], out, M, cfg.cout, cfg.P, bias=self.p["p2_b"])
         if train:

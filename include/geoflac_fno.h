@@ -26,9 +26,12 @@ extern "C" {
 int gf_gemm_bf16(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda, long long sA,
                  long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha, float beta,
                  const float *bias, void *stream);
-/* The same with two extensions: sA = -1 shares one A among all batches,
- * and (FP32 C only) aux, if not NULL, receives a BF16 copy of the final C
- * (act = 0) or of GELU(C) (act = 1) in the same layout. */
+/* The same with three extensions: sA = -1 shares one A among all batches;
+ * (FP32 C only) aux, if not NULL, receives a BF16 copy of the final C
+ * (act = 0) or of GELU(C) (act = 1) in the same layout; and c_bf16 = 2
+ * (with aux) leaves C unwritten: C is then only read, for beta != 0, or
+ * may be NULL with beta = 0 (inference, where only the BF16 activation
+ * is kept). */
 int gf_gemm_bf16_ex(const void *A, const void *B, void *C, int batch, int M, int N, int K, long long lda,
                     long long sA, long long ldb, long long sB, long long ldc, long long sC, int c_bf16, float alpha,
                     float beta, const float *bias, void *aux, int act, void *stream);

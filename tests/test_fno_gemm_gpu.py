@@ -84,3 +84,38 @@ def test_gemm_broadcast_a_and_fused_gelu_copy():
     assert (out - ref).abs().max().item() / ref.abs().max().item() <= 2e-3
     g = torch.nn.functional.gelu(ref)
     assert (aux.float() - g).abs().max().item() / g.abs().max().item() <= 1e-2
+
+
+def test_gemm_aux_only_output():
+    """c_bf16 = 2: C is read for beta (or absent with beta = 0) and left
+    unwritten; aux carries the same BF16 GELU(C) as the full call."""
+    torch = pytest.importorskip("torch")
+    from geoflac_gb300.fno import _lib
+    lib = _lib()
+    A = torch.randn(1, 1000, 64).to(torch.bfloat16).cuda()
+    B = torch.randn(1, 64, 64).to(torch.bfloat16).cuda()
+    bias = torch.randn(64).cuda()
+    C0 = torch.randn(1, 1000, 64).cuda()
+    full, part = C0.clone(), C0.clone()
+    aux_full = torch.empty(1, 1000, 64, dtype=torch.bfloat16, device="cuda")
+    aux_part = torch.empty_like(aux_full)
+    args = (1, 1000, 64, 64, 64, 0, 64, 0, 64, 0)
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), full.data_ptr(), *args, 0, 1.0, 1.0, bias.data_ptr(),
+                               aux_full.data_ptr(), 1, None) == 0
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), part.data_ptr(), *args, 2, 1.0, 1.0, bias.data_ptr(),
+                               aux_part.data_ptr(), 1, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(part, C0)  # read, not written
+    assert torch.equal(aux_part, aux_full)
+    # beta = 0 with no C at all
+    aux0 = torch.empty_like(aux_full)
+    ref0 = torch.empty(1, 1000, 64, device="cuda")
+    aux_ref = torch.empty_like(aux_full)
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), None, *args, 2, 1.0, 0.0, bias.data_ptr(),
+                               aux0.data_ptr(), 1, None) == 0
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), ref0.data_ptr(), *args, 0, 1.0, 0.0, bias.data_ptr(),
+                               aux_ref.data_ptr(), 1, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(aux0, aux_ref)
+    # aux-only without aux stores nothing: rejected
+    assert lib.gf_gemm_bf16_ex(A.data_ptr(), B.data_ptr(), None, *args, 2, 1.0, 0.0, None, None, 0, None) == -2
