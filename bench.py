@@ -313,6 +313,14 @@ def run_ours(args):
     alg = bytes_model.rheol_bytes_per_element(g.params.nphase, "fp64") * E
     achieved = alg / t_rheol / 1e9
     traffic = _ncu_traffic("k_rheol_fp64")
+    # the mixed path's dominant kernel (k_rheol<float>), timed alone
+    gm = res["mixed"]["g"]
+    t_rheol_m = _time_kernel(gm, "fl_rheol", 10, flush)
+    alg_m = bytes_model.rheol_bytes_per_element(gm.params.nphase, "mixed") * E
+    mixed_roofline = {"bound": "hbm", "kernel": "k_rheol (fl_rheol, mixed)", "achieved": alg_m / t_rheol_m / 1e9,
+                      "peak": peak, "unit": "GB/s", "frac": alg_m / t_rheol_m / 1e9 / peak, "peak_kind": peak_kind,
+                      "traffic": _ncu_traffic("k_rheol_mixed"), "avg_launch_s": t_rheol_m,
+                      "algorithmic_bytes_per_launch": alg_m}
     # e2e through the per-subroutine C-ABI (drop-in path)
     e2e_steps = max(5, min(args.steps, 20))
     e2e_wall, h2d, d2h = _time_e2e(g, e2e_steps)
@@ -327,7 +335,7 @@ def run_ours(args):
         "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
                   "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes",
                   "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup,
-                  "fp64_perturbed_1e-7_rel_err": perturbed_err},
+                  "fp64_perturbed_1e-7_rel_err": perturbed_err, "roofline": mixed_roofline},
         "therm_sweeps_fp64": fp["g"].clock.therm_sweeps,
         "e2e": {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps,

@@ -41,5 +41,12 @@ def rheol_bytes_per_element(nphase: int = 2, mode: str = "fp64", n_over_e: float
              + 3 * r + 3 * r + r + r + r  # se2sr, strain, sshrheat, aps, visn
              + 4 + 8 * nphase)        # iphase, phase_ratio
     writes = 16 * r + 3 * r + 3 * r + r + r  # stress0, se2sr, strain, sshrheat, aps
-    node = 32 * n_over_e  # cord + vel (x,z), FP64
+    if mode == "fp64":
+        node = 32 * n_over_e  # cord + vel (x,z), FP64
+    else:
+        # hi/lo FP32 pairs of cord and vel; the corner forces of the node
+        # gather (16 FP32 per element) and the FP32 p_ref split are written
+        node = 32 * n_over_e
+        reads += 4        # p_ref (hi part)
+        writes += 16 * 4  # corner forces
     return reads + writes + node
