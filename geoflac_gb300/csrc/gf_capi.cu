@@ -33,6 +33,10 @@ struct gf_ctx {
     int mode;
     GfDims d;
     cudaStream_t s = nullptr;
+    // mixed: second stream and fork/join events for the thermal sweeps that
+    // run beside fl_rheol / fl_node
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     DevParams *dP = nullptr;
     DevClock *dC = nullptr;
     DevArrays A{};
@@ -472,7 +476,28 @@ unsigned step_signature(const gf_ctx *c) {
 
 // Enqueue one step (flac.f90:5-91 + par.f90:84-87) for a signature.
 void enqueue_step(gf_ctx *c, unsigned sig) {
-    k_therm(c);
+    // Mixed path: on steps where fl_rheol and fl_node read nothing that the
+    // thermal update writes (no viscosity update, no change_phase, no
+    // thermal stress, no Winkler foundation, whose pressure reads the new
+    // temperatures), the two thermal sweeps and the boundary pass run on a
+    // second stream beside them.  The coefficient pass comes first (it reads
+    // the shear heating that fl_rheol's averaging rewrites) and the streams
+    // join before fl_move, which changes the mesh the sweeps' boundary pass
+    // may read.
+    const bool fork = c->mode == GF_MODE_MIXED && c->s2 && (sig & 1u) && !(sig & 2u) && !(sig & 4u) &&
+                      c->p.istress_therm == 0 && c->p.nyhydro == 0;
+    if (fork) {
+        GfLaunch g = launch_of(c);
+        GfKernels<float>::therm_prep(g);
+        cudaEventRecord(c->ev_fork, c->s);
+        cudaStreamWaitEvent(c->s2, c->ev_fork, 0);
+        GfLaunch g2 = g;
+        g2.s = c->s2;
+        GfKernels<float>::therm_sweeps(g2);
+        cudaEventRecord(c->ev_join, c->s2);
+    } else {
+        k_therm(c);
+    }
     // par.f90:86 adds the dt that dt_mass may have just changed, so time
     // advances inside fl_move's kernel only on steps without dt_mass
     bool folded = false;
@@ -481,6 +506,7 @@ void enqueue_step(gf_ctx *c, unsigned sig) {
         int avg = (sig & (8u << 8)) ? 2 : ((sig & (4u << 8)) ? 1 : 0);
         k_rheol(c, (sig & 4u) ? 1 : 0, avg);
         k_node(c);
+        if (fork) cudaStreamWaitEvent(c->s, c->ev_join, 0);
         if (c->p.movegrid != 0) {
             folded = !(sig & 32u);
             k_move(c, folded ? 1 : 0);
@@ -560,6 +586,11 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         }                                                                                                              \
     } while (0)
     A_(cuda_err(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking), "cudaStreamCreate"));
+    if (mode == GF_MODE_MIXED) {
+        A_(cuda_err(cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking), "cudaStreamCreate"));
+        A_(cuda_err(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate"));
+        A_(cuda_err(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "cudaEventCreate"));
+    }
     A_(dalloc(c, &c->dP, 1));
     A_(dalloc(c, &c->dC, 1));
     DevArrays &A = c->A;
@@ -656,6 +687,12 @@ void gf_destroy(gf_ctx *c) {
     if (c->s) cudaStreamSynchronize(c->s);
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
     for (void *p : c->allocs) cudaFree(p);
+    if (c->s2) {
+        cudaStreamSynchronize(c->s2);
+        cudaStreamDestroy(c->s2);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->s) cudaStreamDestroy(c->s);
     delete c;
 }

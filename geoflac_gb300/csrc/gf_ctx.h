@@ -106,6 +106,10 @@ struct GfLaunch {
 // Launchers, one set per precision (template instantiated in its own TU).
 template <class R> struct GfKernels {
     static void therm(const GfLaunch &g, int sweeps);
+    // mixed: the coefficient pass and the two sweeps + boundary pass of
+    // therm, for steps that run the sweeps beside fl_rheol / fl_node
+    static void therm_prep(const GfLaunch &g);
+    static void therm_sweeps(const GfLaunch &g);
     static void rheol(const GfLaunch &g, int update_visc, int avg_mode);
     static void node(const GfLaunch &g);
     // mixed: the corner forces of the current stresses (fl_rheol writes them

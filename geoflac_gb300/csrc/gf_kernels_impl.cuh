@@ -1623,15 +1623,26 @@ template <class R> __global__ void k_convert_back(const R *__restrict__ src, dou
         }                                                                                                              \
     } while (0)
 
+template <class R> void GfKernels<R>::therm_prep(const GfLaunch &g) {
+    using namespace gfk;
+    if (sizeof(R) == sizeof(float)) GF_LAUNCH(k_therm_prep32, g.d.E, g.P, g.A, g.d, (float *)g.A.t_coef);
+}
+
+template <class R> void GfKernels<R>::therm_sweeps(const GfLaunch &g) {
+    using namespace gfk;
+    if (sizeof(R) != sizeof(float)) return;
+    const float *tc = (const float *)g.A.t_coef;
+    float *d0 = (float *)g.A.t_delta0;
+    GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 0);
+    GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 1);
+    GF_LAUNCH(k_therm_apply32, g.d.N, g.P, g.A, g.d, g.A.t_delta1);
+}
+
 template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float)) {
-        float *tc = (float *)g.A.t_coef;
-        float *d0 = (float *)g.A.t_delta0;
-        GF_LAUNCH(k_therm_prep32, g.d.E, g.P, g.A, g.d, tc);
-        GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 0);
-        GF_LAUNCH(k_therm_sweep32, g.d.N, g.P, g.C, g.A, g.d, tc, d0, g.A.t_delta1, 1);
-        GF_LAUNCH(k_therm_apply32, g.d.N, g.P, g.A, g.d, g.A.t_delta1);
+        therm_prep(g);
+        therm_sweeps(g);
         return;
     }
     int kmax = sweeps > 0 ? (sweeps < GF_THERM_KMAX ? sweeps : GF_THERM_KMAX) : GF_THERM_KMAX;
