@@ -55,7 +55,8 @@ struct BatchArgs {
     int ntile[K_KINDS];
     BatchSync *sync;
     unsigned sig;
-    int ipt; // items per thread
+    int ipt;   // items per thread
+    int merge; // every member allows the thermal sweeps beside fl_rheol / fl_node
 };
 
 // Bounded grid barrier (generation counter).  Returns false if any CTA gave
@@ -114,6 +115,55 @@ template <class F> __device__ void for_members(const BatchArgs &a, F &&f) {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < a.nmembers; m += gridDim.x * blockDim.x) f(a.members[m]);
 }
 
+// rmasses, dt_mass and par.f90's time advance after fl_move (shared by both
+// schedules of k_batch_step)
+template <class R> __device__ __forceinline__ void mech_tail(const BatchArgs &a, BatchMember &sm, int &cur, unsigned sig) {
+    using namespace gfk;
+#define GF_SYNC()                                                                                                      \
+    do {                                                                                                               \
+        if (!grid_sync(a.sync)) return;                                                                                \
+    } while (0)
+    const int dtm = (sig & 32u) ? 1 : 0;
+    if (sig & 16u) { // rmasses
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_elem_dens<R>(m.P, m.C, m.A, m.d, i);
+        });
+        GF_SYNC();
+        for_members(a, [&](const BatchMember &m) { b_k_frac_fix<R>(m.P, m.C, m.A, m.d); });
+        GF_SYNC();
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.rmass, m.d, i);
+        });
+        GF_SYNC();
+    }
+    if (dtm) { // dt_mass
+        for_members(a, [&](const BatchMember &m) { b_k_dt_reset(m.C); });
+        GF_SYNC();
+        for_tiles(a, K_EN, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_dt_reduce<R>(m.P, m.C, m.A, m.d, i);
+        });
+        GF_SYNC();
+        for_members(a, [&](const BatchMember &m) { b_k_dt_scalars(m.P, m.C); });
+        GF_SYNC();
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.idt_scale != 0) b_k_elem_am3<R>(m.P, m.C, m.A, m.d, i);
+        });
+        GF_SYNC();
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.idt_scale != 0)
+                b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.amass, m.d, i);
+            else if (i < m.d.N)
+                m.A.amass[i] = m.A.rmass[i];
+        });
+        GF_SYNC();
+    }
+    // par.f90:86: time advanced inside fl_move on steps without dt_mass
+    for_members(a, [&](const BatchMember &m) {
+        if (!m.movegrid || dtm) m.C->time = m.C->time + m.C->dt;
+    });
+#undef GF_SYNC
+}
+
 // One FLAC step (flac.f90:5-91, mixed precision) of every member.
 template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(BatchArgs a) {
     using namespace gfk;
@@ -130,6 +180,45 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
         b_k_therm_prep32(m.P, m.A, m.d, (float *)m.A.t_coef, i);
     });
     GF_SYNC();
+    // Steps whose fl_rheol / fl_node read nothing the thermal update writes
+    // (no viscosity update, no change_phase; every member without thermal
+    // stress, Winkler foundation or flux bottom condition): the sweeps share
+    // phases with fl_rheol, fl_node and the coordinate update, which saves
+    // three grid barriers and lets CTAs go on to the next kind of tile.
+    if (a.merge && (sig & 1u) && !(sig & 2u) && !(sig & 4u)) {
+        const int avg = (sig & (8u << 8)) ? 2 : ((sig & (4u << 8)) ? 1 : 0);
+        const int dtm = (sig & 32u) ? 1 : 0;
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_therm_sweep32(m.P, m.C, m.A, m.d, (const float *)m.A.t_coef, (float *)m.A.t_delta0, m.A.t_delta1,
+                              0, i);
+        });
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) { b_k_rheol<R>(m.P, m.C, m.A, m.d, 0, 0, i); });
+        GF_SYNC();
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_therm_sweep32(m.P, m.C, m.A, m.d, (const float *)m.A.t_coef, (float *)m.A.t_delta0, m.A.t_delta1,
+                              1, i);
+        });
+        if (avg > 0)
+            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+                b_k_rheol_avg<R>(m.C, m.A, m.d, avg == 2 ? 1 : 0, i);
+            });
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) { b_k_node<R>(m.P, m.C, m.A, m.d, i); });
+        GF_SYNC();
+        for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
+            b_k_therm_apply32(m.P, m.A, m.d, m.A.t_delta1, i);
+        });
+        if (avg == 2) for_members(a, [&](const BatchMember &m) { b_k_rheol_clock(m.C, 1); });
+        for_tiles(a, K_N2, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.movegrid) b_k_move_cord(m.C, m.A, m.d, i);
+        });
+        GF_SYNC();
+        for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
+            if (m.movegrid) b_k_move_elem<R>(m.C, m.A, m.d, dtm ? 0 : 1, i);
+        });
+        GF_SYNC();
+        mech_tail<R>(a, sm, cur, sig);
+        return;
+    }
     for (int sweep = 0; sweep < 2; ++sweep) {
         for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
             b_k_therm_sweep32(m.P, m.C, m.A, m.d, (const float *)m.A.t_coef, (float *)m.A.t_delta0, m.A.t_delta1,
@@ -179,43 +268,7 @@ template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(B
             if (m.movegrid) b_k_move_elem<R>(m.C, m.A, m.d, dtm ? 0 : 1, i);
         });
         GF_SYNC();
-        if (sig & 16u) { // rmasses
-            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
-                b_k_elem_dens<R>(m.P, m.C, m.A, m.d, i);
-            });
-            GF_SYNC();
-            for_members(a, [&](const BatchMember &m) { b_k_frac_fix<R>(m.P, m.C, m.A, m.d); });
-            GF_SYNC();
-            for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
-                b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.rmass, m.d, i);
-            });
-            GF_SYNC();
-        }
-        if (dtm) { // dt_mass
-            for_members(a, [&](const BatchMember &m) { b_k_dt_reset(m.C); });
-            GF_SYNC();
-            for_tiles(a, K_EN, sm, cur, [&](const BatchMember &m, long long i) {
-                b_k_dt_reduce<R>(m.P, m.C, m.A, m.d, i);
-            });
-            GF_SYNC();
-            for_members(a, [&](const BatchMember &m) { b_k_dt_scalars(m.P, m.C); });
-            GF_SYNC();
-            for_tiles(a, K_E, sm, cur, [&](const BatchMember &m, long long i) {
-                if (m.idt_scale != 0) b_k_elem_am3<R>(m.P, m.C, m.A, m.d, i);
-            });
-            GF_SYNC();
-            for_tiles(a, K_N, sm, cur, [&](const BatchMember &m, long long i) {
-                if (m.idt_scale != 0)
-                    b_k_node_gather_tri<R>((const R *)m.A.e_tri, m.A.amass, m.d, i);
-                else if (i < m.d.N)
-                    m.A.amass[i] = m.A.rmass[i];
-            });
-            GF_SYNC();
-        }
-        // par.f90:86: time advanced inside fl_move on steps without dt_mass
-        for_members(a, [&](const BatchMember &m) {
-            if (!m.movegrid || dtm) m.C->time = m.C->time + m.C->dt;
-        });
+        mech_tail<R>(a, sm, cur, sig);
     } else {
         for_members(a, [&](const BatchMember &m) { m.C->time = m.C->time + m.C->dt; });
     }
@@ -480,6 +533,7 @@ struct gf_batch {
     gf_batch_config cfg{256, 2, 1, 10};
     double g = 10.0; // gravity of the members (one value; checked at creation)
     int grid = 0;
+    int merge = 0;
     long long elements = 0;
     struct Graph {
         std::vector<unsigned> sigs;
@@ -601,6 +655,7 @@ BatchArgs args_of(const gf_batch *b, unsigned sig) {
     a.sync = b->d_sync;
     a.sig = sig;
     a.ipt = b->cfg.items_per_thread;
+    a.merge = b->merge;
     return a;
 }
 
@@ -647,9 +702,12 @@ std::vector<unsigned> next_sigs(gf_batch *b, int n, std::vector<int> &nl, std::v
 }
 
 int refresh_views(gf_batch *b) {
+    b->merge = 1;
     for (size_t m = 0; m < b->members.size(); ++m) {
         int rc = gf_ctx_view(b->members[m], &b->views[m]);
         if (rc) return rc;
+        const gf_params &p = *b->views[m].hp;
+        if (p.istress_therm != 0 || p.nyhydro != 0 || p.itemp_bc == 2) b->merge = 0;
     }
     return GF_OK;
 }
