@@ -165,7 +165,10 @@ template <class R> __device__ __forceinline__ void mech_tail(const BatchArgs &a,
 }
 
 // One FLAC step (flac.f90:5-91, mixed precision) of every member.
-template <int THREADS> __global__ void __launch_bounds__(THREADS) k_batch_step(BatchArgs a) {
+// MINB: resident CTAs per SM the register allocation is sized for (the whole
+// step is one kernel, so its register count is that of its heaviest phase;
+// a cap trades spills in fl_rheol for occupancy in every phase)
+template <int THREADS, int MINB> __global__ void __launch_bounds__(THREADS, MINB) k_batch_step(BatchArgs a) {
     using namespace gfk;
     typedef float R;
     __shared__ BatchMember sm;
@@ -511,11 +514,18 @@ __global__ void k_force_residual(const BatchMember *members, const int2 *tiles, 
 
 typedef void (*BatchKernel)(BatchArgs);
 
-BatchKernel kernel_for(int threads) {
+// the kernel for a CTA width and residency: register-capped builds where
+// compiled, else the uncapped one
+BatchKernel kernel_for(int threads, int cps) {
     switch (threads) {
-    case 128: return k_batch_step<128>;
-    case 256: return k_batch_step<256>;
-    case 512: return k_batch_step<512>;
+    case 128: return k_batch_step<128, 1>;
+    case 256:
+        if (cps == 2) return k_batch_step<256, 2>;
+        if (cps >= 3) return k_batch_step<256, 3>;
+        return k_batch_step<256, 1>;
+    case 512:
+        if (cps >= 2) return k_batch_step<512, 2>;
+        return k_batch_step<512, 1>;
     default: return nullptr;
     }
 }
@@ -589,7 +599,7 @@ long long kind_count(const GfMemberView &v, int kind) {
 // tile tables and the co-resident grid for the current configuration
 int build_tables(gf_batch *b) {
     const gf_batch_config &c = b->cfg;
-    BatchKernel k = kernel_for(c.threads);
+    BatchKernel k = kernel_for(c.threads, c.ctas_per_sm);
     if (!k || c.items_per_thread < 1 || c.items_per_thread > 64 || c.ctas_per_sm < 1) return GF_ERR_ARG;
     int dev = 0, sms = 0, occ = 0;
     GB_CK(cudaGetDevice(&dev));
@@ -671,7 +681,7 @@ int launch_step(gf_batch *b, unsigned sig) {
     attr[0].val.cooperative = 1;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    GB_CK(cudaLaunchKernelEx(&lc, kernel_for(b->cfg.threads), a));
+    GB_CK(cudaLaunchKernelEx(&lc, kernel_for(b->cfg.threads, b->cfg.ctas_per_sm), a));
     return GF_OK;
 }
 
@@ -857,10 +867,11 @@ int gf_batch_tune(gf_batch *b, int trial_steps, gf_batch_config *best, double *b
     const int ipts[4] = {1, 2, 4, 8};
     int rc = GF_OK;
     for (int t : threads) {
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(t), t, 0);
         for (int ipt : ipts)
-            for (int cps = 1; cps <= std::min(occ, 4); ++cps) {
+            for (int cps = 1; cps <= 4; ++cps) {
+                int occ = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel_for(t, cps), t, 0);
+                if (occ < cps) continue;
                 gf_batch_config c{t, ipt, cps, 0}; // direct launches: no capture inside the timing
                 b->cfg = c;
                 if (build_tables(b)) continue;

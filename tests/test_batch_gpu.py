@@ -3,9 +3,9 @@ the same models stepped one by one, through the C-ABI.
 
 The batch runs the single-model device code per element and node.  Within
 one compiled batch kernel the result of a member does not depend on the
-company it keeps or on the tile depth and residency: those are compared to
-the last bit.  Between differently compiled kernels (the single-model
-kernels, or batch kernels built for another CTA width) the FP32 fields can
+company it keeps or on the tile depth: those are compared to the last bit.
+Between differently compiled kernels (the single-model kernels, or batch
+kernels built for another CTA width or register cap) the FP32 fields can
 differ by FMA contraction; those are compared after 25 steps at rounding
 level: coordinates and temperatures 1e-10, stresses and velocities 1e-5 of
 the field's largest value, plastic strain 1e-6, integer fields exact.
@@ -93,8 +93,9 @@ def test_batch_member_independent_of_company(workdir):
 
 
 def test_batch_shapes_agree(workdir):
-    """Tile depth and residency leave the states unchanged to the bit; other
-    CTA widths (separately compiled kernels) agree at rounding level."""
+    """Tile depth leaves the states unchanged to the bit; other CTA widths
+    and residencies (separately compiled kernels: the residency selects a
+    register-capped build) agree at rounding level."""
     ref = _members(workdir, 4, tag="r")
     rb = Batch(ref)
     rb.set_config(threads=256, items_per_thread=1, ctas_per_sm=1, graph_steps=0)
@@ -105,7 +106,7 @@ def test_batch_shapes_agree(workdir):
         b.set_config(threads=threads, items_per_thread=ipt, ctas_per_sm=cps, graph_steps=0)
         b.step(12)
         for k in range(4):
-            if threads == 256:
+            if threads == 256 and cps == 1:
                 _assert_same(ms[k], ref[k], f"shape {threads}x{ipt}x{cps} member {k}")
             else:
                 _assert_close(ms[k], ref[k], f"shape {threads}x{ipt}x{cps} member {k}")
