@@ -804,7 +804,20 @@ __device__ __forceinline__ void b_k_therm_sweep(DevClock *__restrict__ C, DevArr
     if (k > 0 && C->therm_flags[k - 1] == 0) return; // converged one sweep ago
     long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool changed = false;
-    if (n < d.N) {
+    // A node's sweep-k value depends on sweep k-1 only through its upstream
+    // neighbours (j-1,i), (j,i-1), (j+1,i-1); if none of them changed in
+    // sweep k-1 its value is the one it had (the same inputs give the same
+    // result), and the FP64 evaluation is skipped.
+    bool recompute = true;
+    if (n < d.N && k > 0) {
+        int j, i;
+        node_ji(d, n, j, i);
+        const uint8_t *prev = A.t_chg + (long long)((k - 1) & 1) * d.N;
+        recompute = (j != 0 && prev[gf_node(d, j - 1, i)]) || (i != 0 && prev[gf_node(d, j, i - 1)]) ||
+                    (i != 0 && j != d.nz - 1 && prev[gf_node(d, j + 1, i - 1)]);
+        if (!recompute) Tout[n] = Tup[n];
+    }
+    if (n < d.N && recompute) {
         int j, i;
         node_ji(d, n, j, i);
         const int nx = d.nx, nz = d.nz;
@@ -840,6 +853,7 @@ __device__ __forceinline__ void b_k_therm_sweep(DevClock *__restrict__ C, DevArr
         Tout[n] = tn;
         changed = (tn != Tup[n]);
     }
+    if (n < d.N) A.t_chg[(long long)(k & 1) * d.N + n] = changed ? 1 : 0;
     if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ tc, const double *__restrict__ Tup, double *__restrict__ Tout, int k) {
