@@ -499,8 +499,9 @@ def profile_extra(args, workdir: str):
 
         ms = ensemble(args.members, workdir)
         b = Batch([m for m, _ in ms])
-        # the autotuner's choice on the 256-member sweep
-        b.set_config(threads=256, items_per_thread=8, ctas_per_sm=3, graph_steps=0)
+        # the autotuner's build on the 256-member sweep (256 threads, 3 CTAs
+        # per SM); 2 items per thread so that a small sweep fills the grid
+        b.set_config(threads=256, items_per_thread=2, ctas_per_sm=3, graph_steps=0)
         b.step(args.warmup + args.steps)
         torch.cuda.synchronize()
         print(json.dumps({"profile": "batch", "members": args.members, "elements": b.elements,
