@@ -242,7 +242,11 @@ def screen(batch: Batch, sur: Surrogate, prms: List[dict], interval: int, tol: f
         sub = [batch.members[k] for k in fail]
         batch.restore(fail)
         sb = Batch(sub)
-        sb.set_config(**{k: v for k, v in batch.config().items()})
+        # the parent's CTA build with one item per thread: a few members
+        # then still spread over every SM
+        cfg_sub = dict(batch.config())
+        cfg_sub["items_per_thread"] = 1
+        sb.set_config(**cfg_sub)
         rr["prepare"] = time.time() - t2
         stream = torch.cuda.ExternalStream(sb.stream)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
