@@ -119,6 +119,7 @@ LAYOUT_FIELDS = [
     ("mark_a1", _pd), ("mark_a2", _pd), ("mark_age", _pd),
     ("mark_dead", _pi8), ("mark_phase", _pi8), ("mark_ntriag", _pi),
     ("mark_id_elem", _pi), ("nmark_elem", _pi),
+    ("dhacc", _pd), ("extr_acc", _pd), ("dtopo", _pd),
 ]
 
 
@@ -251,6 +252,8 @@ class HostState:
         A["phase_ratio"] = np.zeros((nph, nz - 1, nx - 1), **f8)
         A["jmoho"] = np.zeros(nx, dtype=np.int32)
         A["dhacc_correction"] = np.zeros(nx, dtype=np.float64)
+        for k in ("dhacc", "extr_acc", "dtopo"):
+            A[k] = np.zeros(nx, dtype=np.float64)
         M = self.max_markers
         A["mark_a1"] = np.zeros(M)
         A["mark_a2"] = np.zeros(M)

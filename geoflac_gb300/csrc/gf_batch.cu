@@ -718,6 +718,9 @@ int refresh_views(gf_batch *b) {
         if (rc) return rc;
         const gf_params &p = *b->views[m].hp;
         if (p.istress_therm != 0 || p.nyhydro != 0 || p.itemp_bc == 2) b->merge = 0;
+        // surface processes (diff_topo / resurface) are not part of the
+        // ensemble step
+        if (p.topo_kappa > 0.0) return GF_ERR_UNSUPPORTED;
     }
     return GF_OK;
 }

@@ -144,6 +144,8 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.diffu[k] = (p.den[k] != 0.0 && p.cp[k] != 0.0) ? p.conduct[k] / p.den[k] / p.cp[k] : 0.0;
     }
     P.f_fmagma_max = (float)p.fmagma_max;
+    P.topo_kappa = p.topo_kappa;
+    for (int k = 0; k < GF_MAXPH; ++k) P.erodibility[k] = p.erodibility[k];
     P.f_rho_magma = (float)p.rho_magma;
     P.f_g = (float)p.g;
 }
@@ -266,6 +268,9 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.mark_id_elem, A.mark_id_elem, (long long)GF_MAX_MARKERS_PER_ELEM * E, dir));
         T_(xfer(c, L.nmark_elem, A.nmark_elem, E, dir));
         T_(xfer(c, L.dhacc_correction, A.dhacc_correction, c->p.nx, dir));
+        T_(xfer(c, L.dhacc, A.dhacc, c->p.nx, dir));
+        T_(xfer(c, L.extr_acc, A.extr_acc, c->p.nx, dir));
+        T_(xfer(c, L.dtopo, A.dtopo, c->p.nx, dir));
     }
 #undef T_
     if (dir && (m & (GF_F_CORD | GF_F_VEL | GF_F_TEMP)) && c->mode == GF_MODE_MIXED) {
@@ -325,12 +330,21 @@ void k_node(gf_ctx *c) {
         GfKernels<double>::node(g);
     }
 }
+// fl_move (fl_move.f90:4-132): the coordinate update, diff_topo (with
+// resurface every ifreq_avgsr steps) when topo_kappa > 0, then areas, dvol
+// and the rotation of stress and strain
+template <class R> void move_step(gf_ctx *c, const GfLaunch &g) {
+    GfKernels<R>::move_cord(g);
+    if (c->p.topo_kappa > 0.0)
+        GfRemesh<R>::diff_topo(g, c->nloop % c->p.ifreq_avgsr == 0 ? 1 : 0, c->nloop, (int)c->L.max_markers);
+    GfKernels<R>::move_elem(g);
+}
 void k_move(gf_ctx *c, int advance_time = 0) {
     c->frc_valid = 0;
     GfLaunch g = launch_of(c);
     g.advance_time = advance_time;
-    if (c->mode == GF_MODE_MIXED) GfKernels<float>::move(g);
-    else GfKernels<double>::move(g);
+    if (c->mode == GF_MODE_MIXED) move_step<float>(c, g);
+    else move_step<double>(c, g);
 }
 void k_rmasses(gf_ctx *c) {
     GfLaunch g = launch_of(c);
@@ -470,6 +484,8 @@ unsigned step_signature(const gf_ctx *c) {
         if (c->nsrate == p.ifreq_avgsr) sig |= 8u << 8;
         else if (c->nsrate == -1) sig |= 4u << 8;
         if (c->nloop % p.ifreq_imasses == 0) sig |= 32u;
+        // resurface: its random seeds use nloop, so such steps run uncaptured
+        if (p.movegrid != 0 && p.topo_kappa > 0.0 && c->nloop % p.ifreq_avgsr == 0) sig |= 64u;
     }
     return sig;
 }
@@ -562,7 +578,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     *out = nullptr;
     if (mode != GF_MODE_FP64 && mode != GF_MODE_MIXED) return GF_ERR_ARG;
     if (L->nx != p->nx || L->nz != p->nz || L->nphase != p->nphase || p->nx < 2 || p->nz < 2) return GF_ERR_ARG;
-    if (p->nystressbc != 0 || p->itype_melting != 0 || p->topo_kappa > 0.0) return GF_ERR_UNSUPPORTED;
+    if (p->nystressbc != 0 || p->itype_melting != 0) return GF_ERR_UNSUPPORTED;
     if (p->nphase > 32) return GF_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -603,6 +619,9 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.bc, 2 * N));
     A_(dalloc(c, &A.ncod, 2 * N));
     A_(dalloc(c, &A.dhacc_correction, p->nx));
+    A_(dalloc(c, &A.dhacc, p->nx));
+    A_(dalloc(c, &A.extr_acc, p->nx));
+    A_(dalloc(c, &A.dtopo, p->nx));
     A_(ralloc(c, &A.stress0, 16 * E));
     A_(ralloc(c, &A.area, 4 * E));
     A_(ralloc(c, &A.dvol, 4 * E));
@@ -791,10 +810,18 @@ int gf_fl_node(gf_ctx *c) {
     return call_status(c);
 }
 
+static int sync_markers_after_resurface(gf_ctx *c);
+
 int gf_fl_move(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
     if (c->p.movegrid == 0) return GF_OK;
+    const bool resurf = c->p.topo_kappa > 0.0 && c->nloop % c->p.ifreq_avgsr == 0;
+    if (resurf) GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
     k_move(c);
+    if (resurf) {
+        int rc = sync_markers_after_resurface(c);
+        if (rc) return rc;
+    }
     return call_status(c);
 }
 
@@ -851,7 +878,12 @@ int gf_finish_setflac(gf_ctx *c) {
 int gf_flac(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
     unsigned sig = step_signature(c);
+    if (sig & 64u) GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
     enqueue_step(c, sig);
+    if (sig & 64u) {
+        int rc = sync_markers_after_resurface(c);
+        if (rc) return rc;
+    }
     advance_host(c, sig);
     return call_status(c);
 }
@@ -940,12 +972,33 @@ int gf_ctx_take_status(gf_ctx *c) { return take_status(c); }
 
 void gf_ctx_invalidate_forces(gf_ctx *c) { c->frc_valid = 0; }
 
+// After a step with resurface: the device marker count is the current one
+// (resurface adds markers); graphs whose change_phase launch covers an older
+// count are dropped.
+static int sync_markers_after_resurface(gf_ctx *c) {
+    int nm = c->nmarkers;
+    GF_CK(cudaMemcpyAsync(&nm, c->A.nmarkers, sizeof(int), cudaMemcpyDeviceToHost, c->s));
+    GF_CK(cudaStreamSynchronize(c->s));
+    if (nm != c->nmarkers) {
+        c->nmarkers = nm;
+        drop_graphs(c);
+    }
+    return GF_OK;
+}
+
 int gf_step(gf_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return GF_ERR_ARG;
     for (int k = 0; k < nsteps; ++k) {
         unsigned sig = step_signature(c);
-        int rc = run_graph(c, sig);
-        if (rc) return rc;
+        if (sig & 64u) { // resurface: uncaptured (its seeds use nloop)
+            GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
+            enqueue_step(c, sig);
+            int rc = sync_markers_after_resurface(c);
+            if (rc) return rc;
+        } else {
+            int rc = run_graph(c, sig);
+            if (rc) return rc;
+        }
         advance_host(c, sig);
     }
     return take_status(c);
@@ -961,7 +1014,36 @@ int gf_itest_mesh(gf_ctx *c, double *min_angle) {
     GF_CK(cudaMemcpyAsync(&a, c->d_angle, sizeof a, cudaMemcpyDeviceToHost, c->s));
     GF_CK(cudaStreamSynchronize(c->s));
     if (min_angle) *min_angle = a;
-    c->need_remeshing = (a <= c->p.angle_rem) ? 1 : 0;
+    // rem_test.f90:23-66: shortening (code 2), surface topography change
+    // (code 3), before the angle (code 1)
+    const gf_params &p = c->p;
+    const int nx = p.nx;
+    const long long N = c->d.N;
+    int need = 0;
+    if (p.mode_rem == 11 || p.mode_rem == 3) {
+        double x0 = 0.0, xn = 0.0;
+        GF_CK(cudaMemcpy(&x0, c->A.cord + gf_node(c->d, 0, 0), sizeof(double), cudaMemcpyDeviceToHost));
+        GF_CK(cudaMemcpy(&xn, c->A.cord + gf_node(c->d, 0, nx - 1), sizeof(double), cudaMemcpyDeviceToHost));
+        double testcr = p.dx_rem * p.rxbo / (nx - 1);
+        double shortening = std::fabs(xn - x0 - p.rxbo);
+        if (shortening > testcr) need = 2;
+    }
+    const double arc_extrusion_rate = 1.0 - p.ratio_mantle_mzone;
+    if (need == 0 && (p.topo_kappa > 0 || arc_extrusion_rate > 0)) {
+        std::vector<double> dh(nx), ex(nx);
+        double z00 = 0.0, z10 = 0.0;
+        GF_CK(cudaMemcpy(dh.data(), c->A.dhacc, sizeof(double) * nx, cudaMemcpyDeviceToHost));
+        GF_CK(cudaMemcpy(ex.data(), c->A.extr_acc, sizeof(double) * nx, cudaMemcpyDeviceToHost));
+        GF_CK(cudaMemcpy(&z00, c->A.cord + N + gf_node(c->d, 0, 0), sizeof(double), cudaMemcpyDeviceToHost));
+        GF_CK(cudaMemcpy(&z10, c->A.cord + N + gf_node(c->d, 1, 0), sizeof(double), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nx - 1; ++i) {
+            double testcr = (z00 - z10) * 0.3333;
+            double topochanges = std::fabs(dh[i]) + ex[i];
+            if (topochanges > testcr) need = 3;
+        }
+    }
+    if (need == 0 && a <= p.angle_rem) need = 1;
+    c->need_remeshing = need;
     return GF_OK;
 }
 

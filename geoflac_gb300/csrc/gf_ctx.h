@@ -35,6 +35,7 @@ struct DevParams {
     float f_ten_off, f_demf, f_g;
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
     double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:108)
+    double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)
 };
 
 // Scalars the step reads and writes, resident on the device so that a
@@ -60,6 +61,7 @@ struct DevArrays {
     double *cord, *vel, *temp, *temp0, *amass, *rmass, *bc;
     int *ncod;
     double *dhacc_correction;
+    double *dhacc, *extr_acc, *dtopo; // surface processes (nx each)
     // element fields stored as R
     void *stress0, *area, *dvol, *strain, *se2sr, *aps, *visn, *e2sr, *shrheat, *sshrheat;
     // element fields always FP64
@@ -117,6 +119,9 @@ template <class R> struct GfKernels {
     // as it updates the stresses; this recomputes them after other changes)
     static void elem_forces(const GfLaunch &g);
     static void move(const GfLaunch &g);
+    // fl_move in two parts, for diff_topo between them
+    static void move_cord(const GfLaunch &g);
+    static void move_elem(const GfLaunch &g);
     static void rmasses(const GfLaunch &g);
     static void dt_mass(const GfLaunch &g);
     static void init_visc(const GfLaunch &g);
@@ -166,5 +171,7 @@ template <class R> struct GfRemesh {
     static void rebin_markers(const GfLaunch &g, const GfRemeshArgs &a, const GfRemeshBufs &b);
     static void top_up_markers(const GfLaunch &g, const GfRemeshArgs &a, const GfRemeshBufs &b);
     static void jmoho(const GfLaunch &g);
+    // diff_topo (and resurface when `resurface`) after the coordinate update
+    static void diff_topo(const GfLaunch &g, int resurface, int nloop, int max_markers);
 };
 

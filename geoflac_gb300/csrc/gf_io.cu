@@ -127,7 +127,9 @@ __global__ void k_frame_line(const DevParams *__restrict__ Pp, DevArrays A, GfDi
     double cond = Pp->conduct[A.iphase[gf_elem(d, 0, ii)] - 1];
     f.lf[LF_HFL * nx + i] = (float)(cond * dtmpr / dl);
     f.lf[LF_TOPO * nx + i] = (float)(A.cord[N + gf_node(d, 0, i)] / 1000);
-    f.lf[LF_DTOPO * nx + i] = 0.0f; // surface processes are not modelled
+    // dtopo in mm/yr (outflac.f90:410-412); extrusion needs the magma
+    // sub-model and stays zero
+    f.lf[LF_DTOPO * nx + i] = (float)(A.dtopo[i] / f.dt * 1000 * GF_SEC_YEAR);
     f.lf[LF_EXTR * nx + i] = 0.0f;
 }
 
@@ -424,10 +426,10 @@ int gf_saveflac(gf_ctx *ctx, const char *dir) {
         return write_record(dir, name, 1, a ? a : zeros.data(), (size_t)n * 8, (size_t)n * 8);
     };
     IO_CK(w8("cord.rs", L.cord, 2 * N));
-    // surface-process and flexure accumulators are not modelled: zero records
-    IO_CK(w8("dhacc.rs", nullptr, nx - 1));
+    // surface accumulators; the flexure ones are not modelled: zero records
+    IO_CK(w8("dhacc.rs", L.dhacc, nx - 1));
     IO_CK(w8("dhacc_corr.rs", L.dhacc_correction, nx));
-    IO_CK(w8("extr_acc.rs", nullptr, nx - 1));
+    IO_CK(w8("extr_acc.rs", L.extr_acc, nx - 1));
     IO_CK(w8("q_init.rs", nullptr, nx));
     IO_CK(w8("vel_flex_old.rs", nullptr, nx));
     IO_CK(w8("vel.rs", L.vel, 2 * N));
@@ -495,7 +497,9 @@ int gf_rsflac(gf_ctx *ctx, const char *dir) {
     };
     std::vector<double> orig((size_t)2 * N);
     IO_CK(r8("cord.rs", L.cord, 2 * N));
+    IO_CK(r8("dhacc.rs", L.dhacc, nx - 1));
     IO_CK(r8("dhacc_corr.rs", L.dhacc_correction, nx));
+    IO_CK(r8("extr_acc.rs", L.extr_acc, nx - 1));
     IO_CK(r8("vel.rs", L.vel, 2 * N));
     IO_CK(r8("strain.rs", L.strain, 3 * E));
     IO_CK(r8("stress.rs", L.stress0, 16 * E));

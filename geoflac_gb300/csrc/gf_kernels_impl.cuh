@@ -676,6 +676,12 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
     const int nd1[4] = {0, 2, 0, 0}, nd2[4] = {1, 1, 1, 3}, nd3[4] = {2, 3, 3, 2};
     bool neg = false;
     const bool fp32 = sizeof(R) == sizeof(float);
+    // the surface nodes also moved by diff_topo's dtopo (zero without it)
+    float tz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (fp32 && j == 0) {
+        tz[0] = (float)A.dtopo[i];
+        tz[2] = (float)A.dtopo[i + 1];
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int a = nd1[k], b = nd2[k], c = nd3[k];
@@ -702,8 +708,8 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
             const float dtf = (float)dtd;
             float Bx = x[b] - x[a], By = y[b] - y[a];
             float Cx = x[c] - x[a], Cy = y[c] - y[a];
-            float dBx = (rvx[b] - rvx[a]) * dtf, dBy = (rvy[b] - rvy[a]) * dtf;
-            float dCx = (rvx[c] - rvx[a]) * dtf, dCy = (rvy[c] - rvy[a]) * dtf;
+            float dBx = (rvx[b] - rvx[a]) * dtf, dBy = (rvy[b] - rvy[a]) * dtf + (tz[b] - tz[a]);
+            float dCx = (rvx[c] - rvx[a]) * dtf, dCy = (rvy[c] - rvy[a]) * dtf + (tz[c] - tz[a]);
             float Box = Bx - dBx, Boy = By - dBy, Cox = Cx - dCx, Coy = Cy - dCy;
             float ddet = (Box * dCy - Boy * dCx) + (dBx * Coy - dBy * Cox) + (dBx * dCy - dBy * dCx);
             float det = Bx * Cy - By * Cx;
@@ -1716,10 +1722,17 @@ template <class R> void GfKernels<R>::node(const GfLaunch &g) {
     GF_LAUNCH(k_node<R>, g.d.N, g.P, g.C, g.A, g.d);
 }
 
-template <class R> void GfKernels<R>::move(const GfLaunch &g) {
+template <class R> void GfKernels<R>::move_cord(const GfLaunch &g) {
     using namespace gfk;
     GF_LAUNCH(k_move_cord, 2 * g.d.N, g.C, g.A, g.d);
+}
+template <class R> void GfKernels<R>::move_elem(const GfLaunch &g) {
+    using namespace gfk;
     GF_LAUNCH(k_move_elem<R>, g.d.E, g.C, g.A, g.d, g.advance_time);
+}
+template <class R> void GfKernels<R>::move(const GfLaunch &g) {
+    move_cord(g);
+    move_elem(g);
 }
 
 template <class R> void GfKernels<R>::rmasses(const GfLaunch &g) {

@@ -597,6 +597,207 @@ __global__ void k_jmoho(DevArrays A, GfDims d) {
     A.jmoho[i] = jm;
 }
 
+// ---------------------------------------------------------------- surface processes
+// diff_topo (fl_move.f90:138-315) on the moved surface, one CTA: the
+// diffusion increment of every interior surface node from the positions
+// before any of them changes, the edge copies, the limit to half the top
+// element's thickness, the accumulators, then the new heights (and their
+// hi/lo split in the mixed path).  The magma blocks add zero without melt.
+__global__ void __launch_bounds__(1024) k_diff_topo(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
+                                                    GfDims d) {
+    const DevParams &P = *Pp;
+    const int nx = d.nx;
+    const double dt = C->dt;
+    double *cord = A.cord, *dtopo = A.dtopo;
+    for (int i = 1 + threadIdx.x; i < nx - 1; i += blockDim.x) {
+        double snder = (P.topo_kappa * (CY(cord, d, 0, i + 1) - CY(cord, d, 0, i)) / (CX(cord, d, 0, i + 1) - CX(cord, d, 0, i)) -
+                        P.topo_kappa * (CY(cord, d, 0, i) - CY(cord, d, 0, i - 1)) / (CX(cord, d, 0, i) - CX(cord, d, 0, i - 1))) /
+                       (CX(cord, d, 0, i + 1) - CX(cord, d, 0, i - 1));
+        if (snder < 0) {
+            int iph = A.iphase[gf_elem(d, 0, i)];
+            snder = snder * P.erodibility[iph - 1];
+        }
+        dtopo[i] = dt * snder;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        dtopo[0] = dtopo[1];
+        dtopo[nx - 1] = dtopo[nx - 2];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const double lim = 0.5 * (CY(cord, d, 0, i) - CY(cord, d, 1, i));
+        const double v = lim < dtopo[i] ? lim : dtopo[i];
+        dtopo[i] = v;
+        A.dhacc_correction[i] = A.dhacc_correction[i] + v;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nx - 1; i += blockDim.x) A.dhacc[i] = A.dhacc[i] + 0.5 * (dtopo[i] + dtopo[i + 1]);
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const long long n = d.N + gf_node(d, 0, i);
+        const double z = cord[n] + dtopo[i];
+        cord[n] = z;
+        if (A.cord_hi) {
+            const float h = (float)z;
+            A.cord_hi[n] = h;
+            A.cord_lo[n] = (float)(z - (double)h);
+        }
+    }
+}
+
+// count_phase_ratio (marker_data.f90:140-172) of one element
+__device__ void count_phase_ratio1(const DevParams &P, DevClock *C, DevArrays &A, const GfDims &d, long long e) {
+    int nm = A.nmark_elem[e];
+    if (nm == 0) {
+        set_status(C, 134, (int)e);
+        return;
+    }
+    int cnt[GF_MAXPH + 1];
+    for (int k = 0; k <= GF_MAXPH; ++k) cnt[k] = 0;
+    for (int m = 0; m < nm; ++m) {
+        int iph = A.mark_phase[A.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + m] - 1];
+        if (iph >= 1 && iph <= GF_MAXPH) cnt[iph] += 1;
+    }
+    int best = 0, iph = 1;
+    for (int k = 1; k <= P.nphase; ++k) {
+        A.phase_ratio[gf_pr(d, e, k - 1)] = cnt[k] / (nm * 1.0);
+        if (cnt[k] > best) {
+            best = cnt[k];
+            iph = k;
+        }
+    }
+    A.iphase[e] = iph;
+}
+
+// add_marker (marker_data.f90:41-104) at (x, y) in element (j, i): 1 when
+// added, 0 when outside the element, -1 when the element or the marker
+// arrays are full
+__device__ int add_marker1(DevArrays &A, const GfDims &d, double x, double y, int iph, double age, int j, int i,
+                           int max_markers) {
+    double b1, b2;
+    int ntr;
+    if (!check_inside(A.cord, d, x, y, b1, b2, ntr, i, j)) return 0;
+    const long long e = gf_elem(d, j, i);
+    const int kk = *A.nmarkers + 1, nm = A.nmark_elem[e] + 1;
+    if (nm > GF_MAX_MARKERS_PER_ELEM || kk > max_markers) return -1;
+    *A.nmarkers = kk;
+    A.nmark_elem[e] = nm;
+    A.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + nm - 1] = kk;
+    A.mark_dead[kk - 1] = 1;
+    A.mark_a1[kk - 1] = b1;
+    A.mark_a2[kk - 1] = b2;
+    A.mark_age[kk - 1] = age;
+    A.mark_ntriag[kk - 1] = ntr;
+    A.mark_phase[kk - 1] = (int8_t)iph;
+    return 1;
+}
+
+// resurface (fl_move.f90:320-426), serial over the surface elements as in
+// the reference (markers are numbered in element order): erosion past
+// thickness / markers removes the element's topmost marker, deposition adds
+// a sediment marker (phase ksed1 = 1) by add_marker_at_top
+// (fl_move.f90:429-472, stop 134 after 100 misses)
+__global__ void k_resurface(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d, int nloop,
+                            int max_markers) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const DevParams &P = *Pp;
+    const int nx = d.nx, M = GF_MAX_MARKERS_PER_ELEM;
+    const double *c = A.cord;
+    const double time = C->time;
+    for (int i = 0; i < nx - 1; ++i) {
+        double elz = 0.5 * (CY(c, d, 0, i) - CY(c, d, 1, i) + CY(c, d, 0, i + 1) - CY(c, d, 1, i + 1));
+        double chgtopo = A.dhacc[i];
+        const long long e = gf_elem(d, 0, i);
+        int kinc = A.nmark_elem[e];
+        int ichanged = 0;
+        if (-chgtopo * kinc >= elz && kinc > 1) {
+            double ymax = -1e30;
+            int kmax = 0;
+            for (int k = 1; k <= kinc; ++k) {
+                int n = A.mark_id_elem[e * M + k - 1];
+                int m = A.mark_ntriag[n - 1];
+                int kk = (m - 1) % 2 + 1;
+                int jj = ((m - kk) / 2) % (d.nz - 1);
+                int ii = (m - kk) / 2 / (d.nz - 1);
+                double ba1 = A.mark_a1[n - 1], ba2 = A.mark_a2[n - 1];
+                double ba3 = 1.0 - ba1 - ba2;
+                int i1, i2, i3, j1, j2, j3;
+                if (kk == 1) {
+                    i1 = ii; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj;
+                } else {
+                    i1 = ii + 1; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj + 1;
+                }
+                double y = CY(c, d, j1, i1) * ba1 + CY(c, d, j2, i2) * ba2 + CY(c, d, j3, i3) * ba3;
+                if (ymax < y) {
+                    ymax = y;
+                    kmax = k;
+                }
+            }
+            if (kmax != 0) {
+                int nmax = A.mark_id_elem[e * M + kmax - 1];
+                A.mark_id_elem[e * M + kmax - 1] = A.mark_id_elem[e * M + kinc - 1];
+                A.mark_id_elem[e * M + kinc - 1] = 0;
+                A.mark_dead[nmax - 1] = 0;
+                A.nmark_elem[e] = A.nmark_elem[e] - 1;
+            }
+            A.dhacc[i] = 0.0;
+            ichanged = 1;
+        }
+        if (chgtopo * kinc >= elz && kinc != M) {
+            // add_marker_at_top(i, 0.1, time, nloop, ksed1)
+            int iseed = nloop + (i + 1), icount = 0;
+            while (true) {
+                double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
+                double x1 = CX(c, d, 0, i) * (1 - r1) + CX(c, d, 0, i + 1) * r1;
+                double y1 = CY(c, d, 0, i) * (1 - r1) + CY(c, d, 0, i + 1) * r1;
+                double x2 = CX(c, d, 1, i) * (1 - r1) + CX(c, d, 1, i + 1) * r1;
+                double y2 = CY(c, d, 1, i) * (1 - r1) + CY(c, d, 1, i + 1) * r1;
+                r2 = r2 * 0.1;
+                double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
+                int inc = add_marker1(A, d, xx, yy, 1, time, 0, i, max_markers);
+                if (inc == 1 || inc == -1) break;
+                if (++icount > 100) {
+                    set_status(C, 134, (int)e);
+                    return;
+                }
+            }
+            A.dhacc[i] = 0.0;
+            ichanged = 1;
+        }
+        if (ichanged == 1) count_phase_ratio1(P, C, A, d, e);
+    }
+}
+
+// the surface accumulators length-weighted onto the new surface elements
+// (remesh.f90:20-53), one thread, the reference's walk; cordo = the mesh
+// before regridding, scratch = 2 (nx - 1) doubles
+__global__ void k_surface_acc_remesh(DevArrays A, GfDims d, double *scratch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int nx = d.nx;
+    const double *c = A.cord, *co = A.cord_old;
+    double *dhnew = scratch, *extnew = scratch + (nx - 1);
+    for (int k = 0; k < nx - 1; ++k) dhnew[k] = extnew[k] = 0.0;
+    int i = 0, ii = 0;
+    double xl = CX(c, d, 0, 0), xr;
+    while ((i > ii ? i : ii) < nx - 1) {
+        const double xo = CX(co, d, 0, ii + 1), xn = CX(c, d, 0, i + 1);
+        xr = xo < xn ? xo : xn;
+        if (xl < xr) {
+            dhnew[i] = dhnew[i] + A.dhacc[ii] * (xr - xl);
+            extnew[i] = extnew[i] + A.extr_acc[ii] * (xr - xl);
+        }
+        if (xr == xo)
+            ii = ii + 1;
+        else
+            i = i + 1;
+        if ((i > ii ? i : ii) < nx - 1) xl = xr;
+    }
+    for (int k = 0; k < nx - 1; ++k) {
+        A.dhacc[k] = dhnew[k] / (CX(c, d, 0, k + 1) - CX(c, d, 0, k));
+        A.extr_acc[k] = extnew[k] / (CX(c, d, 0, k + 1) - CX(c, d, 0, k));
+    }
+}
+
 } // namespace gfr
 } // namespace
 
@@ -626,6 +827,8 @@ template <class R> void GfRemesh<R>::regrid(const GfLaunch &g, const GfRemeshArg
     cudaMemcpyAsync(A.cord_old, A.cord, sizeof(double) * 2 * d.N, cudaMemcpyDeviceToDevice, g.s);
     GF_RLAUNCH(k_regrid_x, d.N, A, d, a, b.tx);
     GF_RLAUNCH(k_regrid_z, (long long)d.nx, A, d, a, b.tz);
+    k_surface_acc_remesh<<<1, 1, 0, g.s>>>(A, d, b.plane);
+    ++*g.launches;
     // element-wise fields on the element-centre grid (remesh.f90:57-127)
     int nzt = d.nz - 1, nxt = d.nx - 1;
     GF_RLAUNCH(k_centres, d.E, A, d, b.cold, b.cnew);
@@ -687,6 +890,16 @@ template <class R> void GfRemesh<R>::top_up_markers(const GfLaunch &g, const GfR
 template <class R> void GfRemesh<R>::jmoho(const GfLaunch &g) {
     using namespace gfr;
     if (g.A.jmoho) GF_RLAUNCH(k_jmoho, (long long)(g.d.nx - 1), g.A, g.d);
+}
+
+template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface, int nloop, int max_markers) {
+    using namespace gfr;
+    k_diff_topo<<<1, 1024, 0, g.s>>>(g.P, g.C, g.A, g.d);
+    ++*g.launches;
+    if (resurface) {
+        k_resurface<<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d, nloop, max_markers);
+        ++*g.launches;
+    }
 }
 
 template struct GfRemesh<double>;

@@ -131,6 +131,9 @@ void init_cord(S &s) {
     p.dzmin = dzmin;
     if (s.L->dhacc_correction)
         for (int i = 0; i < nx; ++i) s.L->dhacc_correction[i] = 0.0;
+    for (double *a : {s.L->dhacc, s.L->extr_acc, s.L->dtopo})
+        if (a)
+            for (int i = 0; i < nx; ++i) a[i] = 0.0;
 }
 
 // init_phase (src/init_phase.f90:5-53); element ranges are 1-based.

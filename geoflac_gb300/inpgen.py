@@ -129,6 +129,7 @@ class Model:
     i_rey: int = 1
     xReyn: float = 5.0
     ifreq: int = 10
+    topo_kappa: float = 0.0  # surface diffusion (diff_topo); 0 = off
     frac: float = 0.45
     fracm: float = 0.5
     demf: float = 0.8
@@ -214,7 +215,7 @@ class Model:
         c("; dx_rem")
         c("1.3")
         c("; topography diffusion: topo_kappa, fac_kappa")
-        c("0.0  0.0")
+        c(f"{_fmt(self.topo_kappa)}  0.0")
         c("; ---- process control")
         c(f"{self.idt_scale}")
         c(f"{_fmt(self.dt_scale)},{_fmt(self.strain_inert)}")

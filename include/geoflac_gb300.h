@@ -81,7 +81,7 @@ extern "C" {
 #define GF_F_PHASE (1u << 9) /* iphase and phase_ratio */
 #define GF_F_RATE (1u << 10) /* e2sr, se2sr, shrheat, sshrheat, temp0, source */
 #define GF_F_BC (1u << 11)   /* bc and ncod */
-#define GF_F_MARKERS (1u << 12)
+#define GF_F_MARKERS (1u << 12) /* markers, dhacc_correction, dhacc, extr_acc, dtopo */
 #define GF_F_ALL 0xffffffffu
 
 /* Every value of the .inp file, in the order src/read_params.f90:3-348
@@ -198,6 +198,11 @@ typedef struct gf_layout {
     int *mark_ntriag;
     int *mark_id_elem; /* (32, nz-1, nx-1) */
     int *nmark_elem;   /* (nz-1, nx-1) */
+    /* surface processes (diff_topo, fl_move.f90:138-315), nx entries each:
+     * accumulated topography change per surface element (dhacc, nx-1 used)
+     * and arc extrusion (extr_acc, nx-1 used; stays zero without the magma
+     * sub-model), and the last step's topography change per surface node */
+    double *dhacc, *extr_acc, *dtopo;
 } gf_layout;
 
 typedef struct gf_ctx gf_ctx;

@@ -688,6 +688,120 @@ void fl_node(St &s) {
 // --------------------------------------------------------------------------
 // fl_move (src/fl_move.f90:3-132)
 
+void count_phase_ratio(St &s, int j, int i);
+int add_marker(St &s, double x, double y, int iph, double age, int j, int i);
+
+// add_marker_at_top (fl_move.f90:429-472): a marker of phase kph at a
+// random point of the top element of column i, in the upper dz_ratio of it;
+// stop 134 after 100 misses
+void add_marker_at_top(St &s, int i, double dz_ratio, double time, int loop, int kph) {
+    int iseed = loop + (i + 1);
+    int icount = 0;
+    while (true) {
+        double r1 = gf_myrandom(iseed);
+        double r2 = gf_myrandom(iseed);
+        double x1 = s.cord(0, i, 0) * (1 - r1) + s.cord(0, i + 1, 0) * r1;
+        double y1 = s.cord(0, i, 1) * (1 - r1) + s.cord(0, i + 1, 1) * r1;
+        double x2 = s.cord(1, i, 0) * (1 - r1) + s.cord(1, i + 1, 0) * r1;
+        double y2 = s.cord(1, i, 1) * (1 - r1) + s.cord(1, i + 1, 1) * r1;
+        r2 = r2 * dz_ratio;
+        double xx = x1 * (1 - r2) + x2 * r2;
+        double yy = y1 * (1 - r2) + y2 * r2;
+        int inc = add_marker(s, xx, yy, kph, time, 0, i);
+        if (inc == 1 || inc == -1) break;
+        icount = icount + 1;
+        if (icount > 100) throw Stop{134};
+    }
+}
+
+// resurface (fl_move.f90:320-426), serial over the surface elements: an
+// element whose accumulated erosion exceeds its thickness / markers loses its
+// topmost marker, one whose deposition does gains a sediment marker (phase
+// ksed1 = 1); the arc-extrusion branch needs extr_acc, which stays zero
+// without the magma sub-model
+void resurface(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const int nx = p.nx, M = GF_MAX_MARKERS_PER_ELEM;
+    for (int i = 0; i < nx - 1; ++i) {
+        double elz = 0.5 * (s.cord(0, i, 1) - s.cord(1, i, 1) + s.cord(0, i + 1, 1) - s.cord(1, i + 1, 1));
+        double chgtopo = L.dhacc[i];
+        long long e = s.e(0, i);
+        int kinc = L.nmark_elem[e];
+        int ichanged = 0;
+        if (-chgtopo * kinc >= elz && kinc > 1) {
+            double ymax = -1e30;
+            int kmax = 0;
+            for (int k = 1; k <= kinc; ++k) {
+                int n = L.mark_id_elem[e * M + k - 1];
+                int m = L.mark_ntriag[n - 1];
+                int kk = (m - 1) % 2 + 1;
+                int jj = ((m - kk) / 2) % (p.nz - 1);
+                int ii = (m - kk) / 2 / (p.nz - 1);
+                double ba1 = L.mark_a1[n - 1], ba2 = L.mark_a2[n - 1];
+                double ba3 = 1.0 - ba1 - ba2;
+                int i1, i2, i3, j1, j2, j3;
+                if (kk == 1) {
+                    i1 = ii; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj;
+                } else {
+                    i1 = ii + 1; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj + 1;
+                }
+                double y = s.cord(j1, i1, 1) * ba1 + s.cord(j2, i2, 1) * ba2 + s.cord(j3, i3, 1) * ba3;
+                if (ymax < y) {
+                    ymax = y;
+                    kmax = k;
+                }
+            }
+            if (kmax != 0) {
+                int nmax = L.mark_id_elem[e * M + kmax - 1];
+                L.mark_id_elem[e * M + kmax - 1] = L.mark_id_elem[e * M + kinc - 1];
+                L.mark_id_elem[e * M + kinc - 1] = 0;
+                L.mark_dead[nmax - 1] = 0;
+                L.nmark_elem[e] = L.nmark_elem[e] - 1;
+            }
+            L.dhacc[i] = 0.0;
+            ichanged = 1;
+        }
+        if (chgtopo * kinc >= elz && kinc != M) {
+            add_marker_at_top(s, i, 0.1, s.c->time, s.c->nloop, 1);
+            L.dhacc[i] = 0.0;
+            ichanged = 1;
+        }
+        if (ichanged == 1) count_phase_ratio(s, 0, i);
+    }
+}
+
+// diff_topo (fl_move.f90:138-315): diffusion of the surface with topo_kappa
+// and the erodibility of the surface phase where it erodes, limited to half
+// the top element's thickness; accumulates dhacc_correction and dhacc;
+// resurface every ifreq_avgsr steps.  The magma blocks (arc extrusion, MOR
+// crust) add zero without melt and are left out.
+void diff_topo(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const int nx = p.nx;
+    const double dt = s.c->dt;
+    std::vector<double> dtopo(nx, 0.0);
+    for (int i = 1; i < nx - 1; ++i) {
+        double snder = (p.topo_kappa * (s.cord(0, i + 1, 1) - s.cord(0, i, 1)) / (s.cord(0, i + 1, 0) - s.cord(0, i, 0)) -
+                        p.topo_kappa * (s.cord(0, i, 1) - s.cord(0, i - 1, 1)) / (s.cord(0, i, 0) - s.cord(0, i - 1, 0))) /
+                       (s.cord(0, i + 1, 0) - s.cord(0, i - 1, 0));
+        if (snder < 0) {
+            int iph = L.iphase[s.e(0, i)];
+            snder = snder * p.erodibility[iph - 1];
+        }
+        dtopo[i] = dt * snder;
+    }
+    dtopo[0] = dtopo[1];
+    dtopo[nx - 1] = dtopo[nx - 2];
+    for (int i = 0; i < nx; ++i) dtopo[i] = std::min(dtopo[i], 0.5 * (s.cord(0, i, 1) - s.cord(1, i, 1)));
+    for (int i = 0; i < nx; ++i) L.dhacc_correction[i] = L.dhacc_correction[i] + dtopo[i];
+    for (int i = 0; i < nx - 1; ++i) L.dhacc[i] = L.dhacc[i] + 0.5 * (dtopo[i] + dtopo[i + 1]);
+    for (int i = 0; i < nx; ++i) s.cordr(0, i, 1) = s.cord(0, i, 1) + dtopo[i];
+    for (int i = 0; i < nx; ++i) L.dtopo[i] = dtopo[i];
+    if (s.c->nloop % p.ifreq_avgsr == 0) resurface(s);
+}
+
 void fl_move(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
@@ -698,7 +812,7 @@ void fl_move(St &s) {
         L.cord[n] = L.cord[n] + L.vel[n] * dt;
         L.cord[s.d.N + n] = L.cord[s.d.N + n] + L.vel[s.d.N + n] * dt;
     }
-    if (p.topo_kappa > 0.0) throw Stop{GF_ERR_UNSUPPORTED};
+    if (p.topo_kappa > 0.0) diff_topo(s);
     static const int nd1[4] = {1, 3, 1, 1}, nd2[4] = {2, 2, 2, 4}, nd3[4] = {3, 4, 4, 3};
     int err = 0;
 #pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
@@ -1704,6 +1818,29 @@ void remesh(St &s) {
     size_t N = (size_t)s.d.N, E = (size_t)s.d.E;
     std::vector<double> cordo(L.cord, L.cord + 2 * N);
     rem_cord(s, cordo);
+    // surface accumulators, length-weighted onto the new surface elements
+    // (remesh.f90:20-53)
+    if (L.dhacc && L.extr_acc) {
+        std::vector<double> dhnew(nx - 1, 0.0), extnew(nx - 1, 0.0);
+        int i = 0, ii = 0;
+        double xl = s.cord(0, i, 0), xr;
+        while (std::max(i, ii) < nx - 1) {
+            xr = std::min(cordo[gf_n2(s.d, 0, ii + 1, 0)], s.cord(0, i + 1, 0));
+            if (xl < xr) {
+                dhnew[i] = dhnew[i] + L.dhacc[ii] * (xr - xl);
+                extnew[i] = extnew[i] + L.extr_acc[ii] * (xr - xl);
+            }
+            if (xr == cordo[gf_n2(s.d, 0, ii + 1, 0)])
+                ii = ii + 1;
+            else
+                i = i + 1;
+            if (std::max(i, ii) < nx - 1) xl = xr;
+        }
+        for (int k = 0; k < nx - 1; ++k) {
+            L.dhacc[k] = dhnew[k] / (s.cord(0, k + 1, 0) - s.cord(0, k, 0));
+            L.extr_acc[k] = extnew[k] / (s.cord(0, k + 1, 0) - s.cord(0, k, 0));
+        }
+    }
     // element fields: barycentric interpolation between element centres
     int nzt = nz - 1, nxt = nx - 1;
     std::vector<double> cold(2 * E), cnew(2 * E);
@@ -1893,11 +2030,29 @@ int or_step(gf_params *p, gf_clock *c, gf_layout *L, int nsteps) {
     return 0;
 }
 
+// itest_mesh (rem_test.f90:9-139): shortening (mode_rem 3 / 11, code 2),
+// surface topography change (code 3), then the smallest angle (code 1); the
+// angle is returned in every case
 int or_itest_mesh(gf_params *p, gf_clock *c, gf_layout *L, double *angle) {
     St s = make(p, c, L);
+    int need = 0;
+    const int nx = p->nx;
+    if (p->mode_rem == 11 || p->mode_rem == 3) {
+        double testcr = p->dx_rem * p->rxbo / (nx - 1);
+        double shortening = std::fabs(s.cord(0, nx - 1, 0) - s.cord(0, 0, 0) - p->rxbo);
+        if (shortening > testcr) need = 2;
+    }
+    const double arc_extrusion_rate = 1.0 - p->ratio_mantle_mzone;
+    if (need == 0 && (p->topo_kappa > 0 || arc_extrusion_rate > 0) && L->dhacc && L->extr_acc)
+        for (int i = 0; i < nx - 1; ++i) {
+            double testcr = (s.cord(0, 0, 1) - s.cord(1, 0, 1)) * 0.3333;
+            double topochanges = std::fabs(L->dhacc[i]) + L->extr_acc[i];
+            if (topochanges > testcr) need = 3;
+        }
     double a = min_angle(s);
     if (angle) *angle = a;
-    c->need_remeshing = (a <= p->angle_rem) ? 1 : 0;
+    if (need == 0 && a <= p->angle_rem) need = 1;
+    c->need_remeshing = need;
     return 0;
 }
 
