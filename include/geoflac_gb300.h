@@ -290,8 +290,8 @@ int gf_remesh(gf_ctx *ctx);
  * the reference) in the reference's binary layouts: gfortran direct-access
  * records (fixed record length, no record markers, native byte order).
  * Fields that this library does not model are written as zeros: fmelt,
- * fmelt2, dtopo, extrusion (surface processes and melting) in frames; dhacc,
- * extr_acc, q_init, vel_flex_old and the dike_* records in restart files. */
+ * fmelt2, extrusion (melting) in frames; q_init, vel_flex_old (flexure) and
+ * the dike_* records in restart files. */
 
 /* outflac (src/outflac.f90:5-431): one float32 frame of the node, element
  * and surface fields selected by io_flags, appended as record nrec of each
