@@ -120,6 +120,7 @@ LAYOUT_FIELDS = [
     ("mark_dead", _pi8), ("mark_phase", _pi8), ("mark_ntriag", _pi),
     ("mark_id_elem", _pi), ("nmark_elem", _pi),
     ("dhacc", _pd), ("extr_acc", _pd), ("dtopo", _pd),
+    ("orig", _pd), ("q_init", _pd), ("vel_flex_old", _pd),
 ]
 
 
@@ -252,8 +253,9 @@ class HostState:
         A["phase_ratio"] = np.zeros((nph, nz - 1, nx - 1), **f8)
         A["jmoho"] = np.zeros(nx, dtype=np.int32)
         A["dhacc_correction"] = np.zeros(nx, dtype=np.float64)
-        for k in ("dhacc", "extr_acc", "dtopo"):
+        for k in ("dhacc", "extr_acc", "dtopo", "q_init", "vel_flex_old"):
             A[k] = np.zeros(nx, dtype=np.float64)
+        A["orig"] = np.zeros((nz, nx, 2), **f8)
         M = self.max_markers
         A["mark_a1"] = np.zeros(M)
         A["mark_a2"] = np.zeros(M)

@@ -271,6 +271,9 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.dhacc, A.dhacc, c->p.nx, dir));
         T_(xfer(c, L.extr_acc, A.extr_acc, c->p.nx, dir));
         T_(xfer(c, L.dtopo, A.dtopo, c->p.nx, dir));
+        T_(xfer(c, L.orig, A.orig, 2 * N, dir));
+        T_(xfer(c, L.q_init, A.q_init, c->p.nx, dir));
+        T_(xfer(c, L.vel_flex_old, A.vel_flex_old, c->p.nx, dir));
     }
 #undef T_
     if (dir && (m & (GF_F_CORD | GF_F_VEL | GF_F_TEMP)) && c->mode == GF_MODE_MIXED) {
@@ -335,6 +338,11 @@ void k_node(gf_ctx *c) {
 // and the rotation of stress and strain
 template <class R> void move_step(gf_ctx *c, const GfLaunch &g) {
     GfKernels<R>::move_cord(g);
+    for (int b = 0; b < c->p.nofbc; ++b) // fl_flexure: the first nbc 200 on the bottom
+        if (c->p.nbc[b] == 200 && c->p.nofside[b] == 2) {
+            GfRemesh<R>::flexure(g, c->p.bca[b], c->p.bcb[b]);
+            break;
+        }
     if (c->p.topo_kappa > 0.0)
         GfRemesh<R>::diff_topo(g, c->nloop % c->p.ifreq_avgsr == 0 ? 1 : 0, c->nloop, (int)c->L.max_markers);
     GfKernels<R>::move_elem(g);
@@ -579,6 +587,9 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     if (mode != GF_MODE_FP64 && mode != GF_MODE_MIXED) return GF_ERR_ARG;
     if (L->nx != p->nx || L->nz != p->nz || L->nphase != p->nphase || p->nx < 2 || p->nz < 2) return GF_ERR_ARG;
     if (p->nystressbc != 0 || p->itype_melting != 0) return GF_ERR_UNSUPPORTED;
+    // the flexural bottom (nbc 200) runs in FP64 contexts only
+    for (int b = 0; b < p->nofbc; ++b)
+        if (mode == GF_MODE_MIXED && p->nbc[b] == 200 && p->nofside[b] == 2) return GF_ERR_UNSUPPORTED;
     if (p->nphase > 32) return GF_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -622,6 +633,9 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.dhacc, p->nx));
     A_(dalloc(c, &A.extr_acc, p->nx));
     A_(dalloc(c, &A.dtopo, p->nx));
+    A_(dalloc(c, &A.q_init, p->nx));
+    A_(dalloc(c, &A.vel_flex_old, p->nx));
+    A_(dalloc(c, &A.flex, (size_t)12 * p->nx));
     A_(ralloc(c, &A.stress0, 16 * E));
     A_(ralloc(c, &A.area, 4 * E));
     A_(ralloc(c, &A.dvol, 4 * E));
@@ -861,7 +875,9 @@ int gf_marker2elem(gf_ctx *c) {
 int gf_finish_setflac(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
     // xoriginal = cord(:,:,1), zoriginal = cord(:,:,2) (setflac.f90:54-55)
-    GF_CK(cudaMemcpyAsync(c->A.orig, c->A.cord, sizeof(double) * 2 * c->d.N, cudaMemcpyDeviceToDevice, c->s));
+    // (when the host layout does not provide the start-up positions)
+    if (!c->L.orig)
+        GF_CK(cudaMemcpyAsync(c->A.orig, c->A.cord, sizeof(double) * 2 * c->d.N, cudaMemcpyDeviceToDevice, c->s));
     k_rmasses(c);
     if (c->p.ivis_present == 1) k_init_visc(c);
     k_dt_mass(c);

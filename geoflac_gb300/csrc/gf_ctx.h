@@ -62,6 +62,8 @@ struct DevArrays {
     int *ncod;
     double *dhacc_correction;
     double *dhacc, *extr_acc, *dtopo; // surface processes (nx each)
+    double *q_init, *vel_flex_old;    // flexural bottom (nx each)
+    double *flex;                     // flexure scratch (12 nx)
     // element fields stored as R
     void *stress0, *area, *dvol, *strain, *se2sr, *aps, *visn, *e2sr, *shrheat, *sshrheat;
     // element fields always FP64
@@ -173,5 +175,7 @@ template <class R> struct GfRemesh {
     static void jmoho(const GfLaunch &g);
     // diff_topo (and resurface when `resurface`) after the coordinate update
     static void diff_topo(const GfLaunch &g, int resurface, int nloop, int max_markers);
+    // fl_flexure (nbc 200 on the bottom): plate thickness Te, fluid density rho_m
+    static void flexure(const GfLaunch &g, double Te, double rho_m);
 };
 

@@ -426,12 +426,12 @@ int gf_saveflac(gf_ctx *ctx, const char *dir) {
         return write_record(dir, name, 1, a ? a : zeros.data(), (size_t)n * 8, (size_t)n * 8);
     };
     IO_CK(w8("cord.rs", L.cord, 2 * N));
-    // surface accumulators; the flexure ones are not modelled: zero records
+    // surface and flexure accumulators
     IO_CK(w8("dhacc.rs", L.dhacc, nx - 1));
     IO_CK(w8("dhacc_corr.rs", L.dhacc_correction, nx));
     IO_CK(w8("extr_acc.rs", L.extr_acc, nx - 1));
-    IO_CK(w8("q_init.rs", nullptr, nx));
-    IO_CK(w8("vel_flex_old.rs", nullptr, nx));
+    IO_CK(w8("q_init.rs", L.q_init, nx));
+    IO_CK(w8("vel_flex_old.rs", L.vel_flex_old, nx));
     IO_CK(w8("vel.rs", L.vel, 2 * N));
     IO_CK(w8("strain.rs", L.strain, 3 * E));
     IO_CK(w8("stress.rs", L.stress0, 16 * E));
@@ -508,6 +508,9 @@ int gf_rsflac(gf_ctx *ctx, const char *dir) {
     // zoriginal.rs into xoriginal)
     IO_CK(r8("xoriginal.rs", orig.data(), N));
     IO_CK(r8("zoriginal.rs", orig.data() + N, N));
+    if (L.orig) std::memcpy(L.orig, orig.data(), sizeof(double) * 2 * N);
+    IO_CK(r8("q_init.rs", L.q_init, nx));
+    IO_CK(r8("vel_flex_old.rs", L.vel_flex_old, nx));
     IO_CK(read_record(dir, "phase.rs", nrec, L.iphase, (size_t)E * 4, (size_t)E * 8));
     for (long long e = 0; e < E; ++e)
         if (L.iphase[e] < 1 || L.iphase[e] > p.nphase) return GF_ERR_PARSE;

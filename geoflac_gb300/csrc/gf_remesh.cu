@@ -768,6 +768,148 @@ __global__ void k_resurface(const DevParams *__restrict__ Pp, DevClock *C, DevAr
     }
 }
 
+// fl_flexure (fl_flexure.f90:1-189), one CTA: column weights (with the last
+// Eff_dens write of `frac` in the reference's serial order), q_init on the
+// first call, the plate's rigidity, the block tridiagonal solve on one thread
+// (the reference's forward sweep and back substitution), then the new bottom
+// heights and the flexure velocity of every column.  Scratch: 12 nx doubles.
+template <class R>
+__global__ void __launch_bounds__(1024) k_flexure(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d,
+                                                  double Te, double rho_m) {
+    const DevParams &P = *Pp;
+    const int nx = d.nx, nz = d.nz;
+    const long long N = d.N;
+    const double g = P.g;
+    double *q = A.flex, *Load = A.flex + nx, *dx = A.flex + 2 * nx, *D = A.flex + 3 * nx;
+    double *cp = A.flex + 4 * nx, *rp = A.flex + 8 * nx, *u = A.flex + 10 * nx;
+    __shared__ long long s_pos[1024];
+    __shared__ double s_val[1024];
+    long long mypos = -1;
+    double myval = 0.0;
+    bool zero = true;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        long long pos = (long long)i * (2 * nz + 4); // Eff_dens calls of column i, in order
+        auto ED = [&](int j, int ie) {
+            int w = 0;
+            double f = 0.0;
+            double r = gfk::eff_dens<R>(P, A, d, j, ie, gf_elem(d, j, ie), &w, &f);
+            if (w) {
+                mypos = pos;
+                myval = f;
+            }
+            ++pos;
+            return r;
+        };
+        double qi = 0.0;
+        for (int j = 0; j < nz - 1; ++j) {
+            double rho;
+            if (i == 0) {
+                rho = ED(j, 0);
+            } else if (i == nx - 1) {
+                rho = ED(j, nx - 2);
+            } else {
+                double r1 = ED(j, i - 1), r2 = ED(j, i);
+                rho = 0.5 * (r1 + r2);
+            }
+            double dz = CY(A.cord, d, j, i) - CY(A.cord, d, j + 1, i);
+            qi = qi + rho * g * dz;
+        }
+        double rho_b;
+        if (i == 0) {
+            rho_b = ED(nz - 2, 0);
+        } else if (i == nx - 1) {
+            rho_b = ED(nz - 2, nx - 2);
+        } else {
+            double r1 = ED(nz - 2, i - 1), r2 = ED(nz - 2, i);
+            rho_b = 0.5 * (r1 + r2);
+        }
+        qi = qi - rho_b * g * (A.orig[N + gf_node(d, nz - 1, i)] - CY(A.cord, d, nz - 1, i));
+        q[i] = qi;
+        zero = zero && A.q_init[i] == 0.0;
+    }
+    s_pos[threadIdx.x] = mypos;
+    s_val[threadIdx.x] = myval;
+    const bool all_zero = __syncthreads_and(zero ? 1 : 0) != 0;
+    if (threadIdx.x == 0) {
+        long long best = -1;
+        double v = 0.0;
+        for (int t = 0; t < (int)blockDim.x; ++t)
+            if (s_pos[t] > best) {
+                best = s_pos[t];
+                v = s_val[t];
+            }
+        if (best >= 0) C->frac = v;
+    }
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        if (all_zero) A.q_init[i] = q[i];
+        Load[i] = q[i] - A.q_init[i];
+        if (i < nx - 1) {
+            double v = CX(A.cord, d, nz - 1, i + 1) - CX(A.cord, d, nz - 1, i);
+            dx[i] = v <= 0.0 ? 1.0 : v;
+        }
+        int iph = i < nx - 1 ? A.iphase[gf_elem(d, nz - 2, i)] : A.iphase[gf_elem(d, nz - 2, nx - 2)];
+        if (iph < 1 || iph > P.nphase) iph = 1;
+        double lambda = P.rl[iph - 1], mu = P.rm[iph - 1], E, nu;
+        if (lambda + mu > 0.0) {
+            E = mu * (3.0 * lambda + 2.0 * mu) / (lambda + mu);
+            nu = lambda / (2.0 * (lambda + mu));
+        } else {
+            E = 1.0e11;
+            nu = 0.25;
+        }
+        if (nu >= 1.0 || nu <= -1.0) nu = 0.25;
+        double Di = (E * (Te * Te * Te)) / (12.0 * (1.0 - (nu * nu)));
+        D[i] = Di <= 0.0 ? 1.0e15 : Di;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double rg = rho_m * g;
+        cp[0] = cp[1] = cp[2] = cp[3] = 0.0;
+        rp[0] = 0.0;
+        rp[1] = rg > 0.0 ? Load[0] / rg : 0.0;
+        for (int i = 1; i < nx - 1; ++i) {
+            double a_i = 2.0 / (dx[i - 1] * (dx[i] + dx[i - 1]));
+            double c_i = 2.0 / (dx[i] * (dx[i] + dx[i - 1]));
+            double b_i = -(a_i + c_i);
+            double d11 = b_i - a_i * cp[4 * (i - 1) + 0];
+            double d12 = -rho_m * g - a_i * cp[4 * (i - 1) + 1];
+            double d21 = 1.0 / D[i] - a_i * cp[4 * (i - 1) + 2];
+            double d22 = b_i - a_i * cp[4 * (i - 1) + 3];
+            double det = d11 * d22 - d12 * d21;
+            if (fabs(det) < 1e-30) det = copysign(1e-30, det);
+            double i11 = d22 / det, i12 = -d12 / det, i21 = -d21 / det, i22 = d11 / det;
+            cp[4 * i + 0] = i11 * c_i;
+            cp[4 * i + 1] = i12 * c_i;
+            cp[4 * i + 2] = i21 * c_i;
+            cp[4 * i + 3] = i22 * c_i;
+            double t1 = -Load[i] - a_i * rp[2 * (i - 1)], t2 = 0.0 - a_i * rp[2 * (i - 1) + 1];
+            rp[2 * i] = i11 * t1 + i12 * t2;
+            rp[2 * i + 1] = i21 * t1 + i22 * t2;
+        }
+        u[2 * (nx - 1)] = 0.0;
+        u[2 * (nx - 1) + 1] = rg > 0.0 ? Load[nx - 1] / rg : 0.0;
+        for (int i = nx - 2; i >= 0; --i) {
+            u[2 * i] = rp[2 * i] - (cp[4 * i + 0] * u[2 * (i + 1)] + cp[4 * i + 1] * u[2 * (i + 1) + 1]);
+            u[2 * i + 1] = rp[2 * i + 1] - (cp[4 * i + 2] * u[2 * (i + 1)] + cp[4 * i + 3] * u[2 * (i + 1) + 1]);
+        }
+    }
+    __syncthreads();
+    const double dt = C->dt;
+    double *vz = A.vel + N;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const double vfo = A.vel_flex_old[i];
+        for (int j = 0; j < nz - 1; ++j) vz[gf_node(d, j, i)] = vz[gf_node(d, j, i)] - vfo;
+        const long long nb = N + gf_node(d, nz - 1, i);
+        const double cord_old_z = A.cord[nb];
+        A.cord[nb] = A.orig[nb] - u[2 * i + 1];
+        double vel_flex = 0.0;
+        if (dt > 0.0) vel_flex = (A.cord[nb] - cord_old_z) / dt;
+        for (int j = 0; j < nz - 1; ++j) vz[gf_node(d, j, i)] = vz[gf_node(d, j, i)] + vel_flex;
+        vz[gf_node(d, nz - 1, i)] = vel_flex;
+        A.vel_flex_old[i] = vel_flex;
+    }
+}
+
 // the surface accumulators length-weighted onto the new surface elements
 // (remesh.f90:20-53), one thread, the reference's walk; cordo = the mesh
 // before regridding, scratch = 2 (nx - 1) doubles
@@ -890,6 +1032,12 @@ template <class R> void GfRemesh<R>::top_up_markers(const GfLaunch &g, const GfR
 template <class R> void GfRemesh<R>::jmoho(const GfLaunch &g) {
     using namespace gfr;
     if (g.A.jmoho) GF_RLAUNCH(k_jmoho, (long long)(g.d.nx - 1), g.A, g.d);
+}
+
+template <class R> void GfRemesh<R>::flexure(const GfLaunch &g, double Te, double rho_m) {
+    using namespace gfr;
+    k_flexure<R><<<1, 1024, 0, g.s>>>(g.P, g.C, g.A, g.d, Te, rho_m);
+    ++*g.launches;
 }
 
 template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface, int nloop, int max_markers) {

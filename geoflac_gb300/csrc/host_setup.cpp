@@ -131,7 +131,7 @@ void init_cord(S &s) {
     p.dzmin = dzmin;
     if (s.L->dhacc_correction)
         for (int i = 0; i < nx; ++i) s.L->dhacc_correction[i] = 0.0;
-    for (double *a : {s.L->dhacc, s.L->extr_acc, s.L->dtopo})
+    for (double *a : {s.L->dhacc, s.L->extr_acc, s.L->dtopo, s.L->q_init, s.L->vel_flex_old})
         if (a)
             for (int i = 0; i < nx; ++i) a[i] = 0.0;
 }
@@ -782,6 +782,7 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
         init_bc(s);
         // field defaults (setflac.f90:53-66)
         if (L->temp0) std::memcpy(L->temp0, L->temp, sizeof(double) * N);
+        if (L->orig) std::memcpy(L->orig, L->cord, sizeof(double) * 2 * N);
         for (size_t e = 0; e < E; ++e) {
             if (L->shrheat) L->shrheat[e] = 0.0;
             if (L->sshrheat) L->sshrheat[e] = 0.0;

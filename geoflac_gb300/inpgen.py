@@ -62,8 +62,9 @@ class BC:
     side: int  # 1 left, 2 bottom, 3 right, 4 top
     n1: int
     n2: int
-    nbc: int  # 10 vx, 1 vz
+    nbc: int  # 10 vx, 1 vz, 200 flexural bottom
     a: float
+    b: float = 0.0  # second coefficient (nbc 200: the fluid's density)
 
 
 @dataclass
@@ -158,7 +159,7 @@ class Model:
         c("; side  nbc1 nbc2 nbc  a b c d e f g h i")
         for b in self.bcs:
             nbc = "01" if b.nbc == 1 else str(b.nbc)
-            c(f"{b.side} {b.n1} {b.n2} {nbc} {_fmt(b.a)} 0 0 0 0 0 0 0 0")
+            c(f"{b.side} {b.n1} {b.n2} {nbc} {_fmt(b.a)} {_fmt(b.b)} 0 0 0 0 0 0 0")
         c("; hydrostatic pressure: nyhydro, pisos, iphsub, drosub, damp_vis")
         c(f"{self.nyhydro} {_fmt(self.pisos)} {self.iphsub} {_fmt(self.drosub)} 0.0")
         c("; gravity")

@@ -81,7 +81,9 @@ extern "C" {
 #define GF_F_PHASE (1u << 9) /* iphase and phase_ratio */
 #define GF_F_RATE (1u << 10) /* e2sr, se2sr, shrheat, sshrheat, temp0, source */
 #define GF_F_BC (1u << 11)   /* bc and ncod */
-#define GF_F_MARKERS (1u << 12) /* markers, dhacc_correction, dhacc, extr_acc, dtopo */
+#define GF_F_MARKERS (1u << 12) /* markers, and the surface and bottom accumulators:
+                                   dhacc_correction, dhacc, extr_acc, dtopo, orig,
+                                   q_init, vel_flex_old */
 #define GF_F_ALL 0xffffffffu
 
 /* Every value of the .inp file, in the order src/read_params.f90:3-348
@@ -203,6 +205,10 @@ typedef struct gf_layout {
      * and arc extrusion (extr_acc, nx-1 used; stays zero without the magma
      * sub-model), and the last step's topography change per surface node */
     double *dhacc, *extr_acc, *dtopo;
+    /* start-up node positions carried through remeshing (xoriginal,
+     * zoriginal: (nz, nx, 2), the reference's arrays.f90:12) and the
+     * flexural bottom's state (fl_flexure.f90: q_init, vel_flex_old; nx) */
+    double *orig, *q_init, *vel_flex_old;
 } gf_layout;
 
 typedef struct gf_ctx gf_ctx;

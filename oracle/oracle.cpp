@@ -802,6 +802,126 @@ void diff_topo(St &s) {
     if (s.c->nloop % p.ifreq_avgsr == 0) resurface(s);
 }
 
+// fl_flexure (fl_flexure.f90:1-189) with get_column_weights (:192-231) and
+// solve_block_tridiagonal (:234-294): the bottom of a model with the
+// flexural boundary condition (nbc 200 on side 2) follows an elastic plate of
+// thickness bca on a fluid of density bcb, loaded by the change of the
+// columns' weight; the plate's deflection rate is added to the columns'
+// vertical velocities
+void fl_flexure(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int bc_idx = -1;
+    for (int b = 0; b < p.nofbc; ++b)
+        if (p.nbc[b] == 200 && p.nofside[b] == 2) {
+            bc_idx = b;
+            break;
+        }
+    if (bc_idx < 0) return;
+    const int nx = p.nx, nz = p.nz;
+    const double Te = p.bca[bc_idx], rho_m = p.bcb[bc_idx], g = p.g;
+    const long long N = s.d.N;
+    auto ED = [&](int j, int i) { return eff_dens(s, j, i, &s.c->frac); };
+    std::vector<double> q(nx), Load(nx), x(nx), dx(nx), D(nx);
+    for (int i = 0; i < nx; ++i) { // get_column_weights
+        q[i] = 0.0;
+        for (int j = 0; j < nz - 1; ++j) {
+            double rho;
+            if (i == 0)
+                rho = ED(j, 0);
+            else if (i == nx - 1)
+                rho = ED(j, nx - 2);
+            else {
+                double r1 = ED(j, i - 1), r2 = ED(j, i); // left operand first
+                rho = 0.5 * (r1 + r2);
+            }
+            double dz = s.cord(j, i, 1) - s.cord(j + 1, i, 1);
+            q[i] = q[i] + rho * g * dz;
+        }
+        double rho_b;
+        if (i == 0)
+            rho_b = ED(nz - 2, 0);
+        else if (i == nx - 1)
+            rho_b = ED(nz - 2, nx - 2);
+        else {
+            double r1 = ED(nz - 2, i - 1), r2 = ED(nz - 2, i);
+            rho_b = 0.5 * (r1 + r2);
+        }
+        q[i] = q[i] - rho_b * g * (L.orig[N + gf_node(s.d, nz - 1, i)] - s.cord(nz - 1, i, 1));
+    }
+    bool all_zero = true;
+    for (int i = 0; i < nx; ++i) all_zero = all_zero && L.q_init[i] == 0.0;
+    if (all_zero)
+        for (int i = 0; i < nx; ++i) L.q_init[i] = q[i];
+    for (int i = 0; i < nx; ++i) Load[i] = q[i] - L.q_init[i];
+    for (int i = 0; i < nx; ++i) x[i] = s.cord(nz - 1, i, 0);
+    for (int i = 0; i < nx - 1; ++i) {
+        dx[i] = x[i + 1] - x[i];
+        if (dx[i] <= 0.0) dx[i] = 1.0;
+    }
+    for (int i = 0; i < nx; ++i) {
+        int iph = i < nx - 1 ? L.iphase[s.e(nz - 2, i)] : L.iphase[s.e(nz - 2, nx - 2)];
+        if (iph < 1 || iph > p.nphase) iph = 1;
+        double lambda = p.rl[iph - 1], mu = p.rm[iph - 1], E, nu;
+        if (lambda + mu > 0.0) {
+            E = mu * (3.0 * lambda + 2.0 * mu) / (lambda + mu);
+            nu = lambda / (2.0 * (lambda + mu));
+        } else {
+            E = 1.0e11;
+            nu = 0.25;
+        }
+        if (nu >= 1.0 || nu <= -1.0) nu = 0.25;
+        D[i] = (E * (Te * Te * Te)) / (12.0 * (1.0 - (nu * nu)));
+        if (D[i] <= 0.0) D[i] = 1.0e15;
+    }
+    // block tridiagonal system (2x2 blocks; the a and c blocks are diagonal)
+    // solved by the forward sweep and back substitution of the reference
+    std::vector<double> cp(4 * nx), rp(2 * nx), u(2 * nx);
+    auto W = [&](double load) { return rho_m * g > 0.0 ? load / (rho_m * g) : 0.0; };
+    // i = 0: B = I, C = 0, r = (0, w_winkler_1)
+    cp[0] = cp[1] = cp[2] = cp[3] = 0.0;
+    rp[0] = 0.0;
+    rp[1] = W(Load[0]);
+    for (int i = 1; i < nx - 1; ++i) {
+        double a_i = 2.0 / (dx[i - 1] * (dx[i] + dx[i - 1]));
+        double c_i = 2.0 / (dx[i] * (dx[i] + dx[i - 1]));
+        double b_i = -(a_i + c_i);
+        double b11 = b_i, b12 = -rho_m * g, b21 = 1.0 / D[i], b22 = b_i;
+        double r1 = -Load[i], r2 = 0.0;
+        double d11 = b11 - a_i * cp[4 * (i - 1) + 0];
+        double d12 = b12 - a_i * cp[4 * (i - 1) + 1];
+        double d21 = b21 - a_i * cp[4 * (i - 1) + 2];
+        double d22 = b22 - a_i * cp[4 * (i - 1) + 3];
+        double det = d11 * d22 - d12 * d21;
+        if (std::fabs(det) < 1e-30) det = std::copysign(1e-30, det);
+        double i11 = d22 / det, i12 = -d12 / det, i21 = -d21 / det, i22 = d11 / det;
+        cp[4 * i + 0] = i11 * c_i;
+        cp[4 * i + 1] = i12 * c_i;
+        cp[4 * i + 2] = i21 * c_i;
+        cp[4 * i + 3] = i22 * c_i;
+        double t1 = r1 - a_i * rp[2 * (i - 1)], t2 = r2 - a_i * rp[2 * (i - 1) + 1];
+        rp[2 * i] = i11 * t1 + i12 * t2;
+        rp[2 * i + 1] = i21 * t1 + i22 * t2;
+    }
+    u[2 * (nx - 1)] = 0.0;
+    u[2 * (nx - 1) + 1] = W(Load[nx - 1]);
+    for (int i = nx - 2; i >= 0; --i) {
+        u[2 * i] = rp[2 * i] - (cp[4 * i + 0] * u[2 * (i + 1)] + cp[4 * i + 1] * u[2 * (i + 1) + 1]);
+        u[2 * i + 1] = rp[2 * i + 1] - (cp[4 * i + 2] * u[2 * (i + 1)] + cp[4 * i + 3] * u[2 * (i + 1) + 1]);
+    }
+    const double dt = s.c->dt;
+    for (int i = 0; i < nx; ++i) {
+        for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] - L.vel_flex_old[i];
+        double cord_old_z = s.cord(nz - 1, i, 1);
+        s.cordr(nz - 1, i, 1) = L.orig[N + gf_node(s.d, nz - 1, i)] - u[2 * i + 1];
+        double vel_flex = 0.0;
+        if (dt > 0.0) vel_flex = (s.cord(nz - 1, i, 1) - cord_old_z) / dt;
+        for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] + vel_flex;
+        L.vel[N + gf_node(s.d, nz - 1, i)] = vel_flex;
+        L.vel_flex_old[i] = vel_flex;
+    }
+}
+
 void fl_move(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
@@ -812,6 +932,7 @@ void fl_move(St &s) {
         L.cord[n] = L.cord[n] + L.vel[n] * dt;
         L.cord[s.d.N + n] = L.cord[s.d.N + n] + L.vel[s.d.N + n] * dt;
     }
+    fl_flexure(s);
     if (p.topo_kappa > 0.0) diff_topo(s);
     static const int nd1[4] = {1, 3, 1, 1}, nd2[4] = {2, 2, 2, 4}, nd3[4] = {3, 4, 4, 3};
     int err = 0;
@@ -1905,6 +2026,10 @@ void remesh(St &s) {
     Interp rn = rem_barcord(coldn, cnewn, nz, nx);
     for (int k = 0; k < 2; ++k) rem_interpolate(rn, L.vel + (size_t)k * N);
     rem_interpolate(rn, L.temp);
+    if (L.orig) { // xoriginal, zoriginal (remesh.f90:242-243)
+        rem_interpolate(rn, L.orig);
+        rem_interpolate(rn, L.orig + N);
+    }
     // side-wall geotherms for incoming material (sidewalltemp, init_temp.f90:313-353)
     if (p.incoming_left == 1) {
         for (int i = 0; i <= idist; ++i) geotherm_column(s, 0, i, p.age_1[0], p.tp1[0], p.tp2[0]);

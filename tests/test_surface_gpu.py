@@ -136,3 +136,45 @@ def test_batch_rejects_surface_processes(workdir):
         Batch([gpu])
     assert e.value.code == -5
     gpu.close()
+
+
+def _flex_model(workdir, tag, mode="fp64"):
+    """The 60x20 model on a flexural bottom (nbc 200: 20 km elastic plate on
+    a 3300 kg/m3 fluid) instead of the free-slip base, with a surface relief
+    whose load the plate carries."""
+    m = inpgen.config1()
+    m.bcs = [b for b in m.bcs if b.side != 2] + [inpgen.BC(2, 1, m.nex + 1, 200, 20e3, 3300.0)]
+    p, c, s = new_state(m.write(str(workdir / f"flex_{tag}.inp")))
+    x = s["cord"][0, :, 0]
+    s["cord"][0, :, 1] += 300.0 * np.exp(-((x - 150e3) / 30e3) ** 2)
+    _init_areas(s)
+    return p, c, s
+
+
+def test_flexure_matches_oracle(workdir):
+    p, c, s = _flex_model(workdir, "a")
+    assert p.nbc[[b for b in range(p.nofbc) if p.nofside[b] == 2][0]] == 200
+    p2, c2, s2 = clone(p, c, s)
+    orc = Oracle(p2, c2, s2)
+    orc.finish_setflac()
+    gpu = Flac(p, c, s, "fp64")
+    gpu.step(60)
+    orc.step(60)
+    extra = ("q_init", "vel_flex_old", "orig")
+    gpu.download()
+    diffs, bad = compare_states(gpu.state, orc.s, FLOAT_FIELDS + EXTRA_FLOATS + extra, INT_FIELDS)
+    assert not bad, f"integer fields differ: {bad}"
+    worst = max(diffs, key=diffs.get)
+    assert diffs[worst] <= TOL, f"{worst} differs by {diffs[worst]:.3e}"
+    # the plate moved the bottom off its start-up depth
+    bottom = orc.s["cord"][-1, :, 1]
+    assert np.abs(bottom - orc.s["orig"][-1, :, 1]).max() > 0
+    assert np.abs(orc.s["q_init"]).max() > 0
+    gpu.close()
+
+
+def test_flexure_rejected_in_mixed_contexts(workdir):
+    p, c, s = _flex_model(workdir, "m")
+    with pytest.raises(capi.GfError) as e:
+        Flac(p, c, s, "mixed")
+    assert e.value.code == -5
