@@ -120,7 +120,7 @@ LAYOUT_FIELDS = [
     ("mark_dead", _pi8), ("mark_phase", _pi8), ("mark_ntriag", _pi),
     ("mark_id_elem", _pi), ("nmark_elem", _pi),
     ("dhacc", _pd), ("extr_acc", _pd), ("dtopo", _pd),
-    ("orig", _pd), ("q_init", _pd), ("vel_flex_old", _pd),
+    ("xoriginal", _pd), ("zoriginal", _pd), ("q_init", _pd), ("vel_flex_old", _pd),
 ]
 
 
@@ -255,7 +255,10 @@ class HostState:
         A["dhacc_correction"] = np.zeros(nx, dtype=np.float64)
         for k in ("dhacc", "extr_acc", "dtopo", "q_init", "vel_flex_old"):
             A[k] = np.zeros(nx, dtype=np.float64)
+        # xoriginal, zoriginal as the two planes of one (nz, nx, 2) array
         A["orig"] = np.zeros((nz, nx, 2), **f8)
+        A["xoriginal"] = A["orig"][:, :, 0]
+        A["zoriginal"] = A["orig"][:, :, 1]
         M = self.max_markers
         A["mark_a1"] = np.zeros(M)
         A["mark_a2"] = np.zeros(M)
@@ -289,7 +292,8 @@ class HostState:
 
     def copy_from(self, other: "HostState"):
         for k, v in other.arrays.items():
-            self.arrays[k][...] = v
+            if k not in ("xoriginal", "zoriginal"):  # views of "orig"
+                self.arrays[k][...] = v
 
     def snapshot(self):
         return {k: v.copy() for k, v in self.arrays.items()}

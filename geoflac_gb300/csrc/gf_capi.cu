@@ -271,7 +271,8 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.dhacc, A.dhacc, c->p.nx, dir));
         T_(xfer(c, L.extr_acc, A.extr_acc, c->p.nx, dir));
         T_(xfer(c, L.dtopo, A.dtopo, c->p.nx, dir));
-        T_(xfer(c, L.orig, A.orig, 2 * N, dir));
+        T_(xfer(c, L.xoriginal, A.orig, N, dir));
+        T_(xfer(c, L.zoriginal, A.orig + N, N, dir));
         T_(xfer(c, L.q_init, A.q_init, c->p.nx, dir));
         T_(xfer(c, L.vel_flex_old, A.vel_flex_old, c->p.nx, dir));
     }
@@ -876,7 +877,7 @@ int gf_finish_setflac(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
     // xoriginal = cord(:,:,1), zoriginal = cord(:,:,2) (setflac.f90:54-55)
     // (when the host layout does not provide the start-up positions)
-    if (!c->L.orig)
+    if (!c->L.xoriginal || !c->L.zoriginal)
         GF_CK(cudaMemcpyAsync(c->A.orig, c->A.cord, sizeof(double) * 2 * c->d.N, cudaMemcpyDeviceToDevice, c->s));
     k_rmasses(c);
     if (c->p.ivis_present == 1) k_init_visc(c);

@@ -508,7 +508,8 @@ int gf_rsflac(gf_ctx *ctx, const char *dir) {
     // zoriginal.rs into xoriginal)
     IO_CK(r8("xoriginal.rs", orig.data(), N));
     IO_CK(r8("zoriginal.rs", orig.data() + N, N));
-    if (L.orig) std::memcpy(L.orig, orig.data(), sizeof(double) * 2 * N);
+    if (L.xoriginal) std::memcpy(L.xoriginal, orig.data(), sizeof(double) * N);
+    if (L.zoriginal) std::memcpy(L.zoriginal, orig.data() + N, sizeof(double) * N);
     IO_CK(r8("q_init.rs", L.q_init, nx));
     IO_CK(r8("vel_flex_old.rs", L.vel_flex_old, nx));
     IO_CK(read_record(dir, "phase.rs", nrec, L.iphase, (size_t)E * 4, (size_t)E * 8));

@@ -782,7 +782,8 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
         init_bc(s);
         // field defaults (setflac.f90:53-66)
         if (L->temp0) std::memcpy(L->temp0, L->temp, sizeof(double) * N);
-        if (L->orig) std::memcpy(L->orig, L->cord, sizeof(double) * 2 * N);
+        if (L->xoriginal) std::memcpy(L->xoriginal, L->cord, sizeof(double) * N);
+        if (L->zoriginal) std::memcpy(L->zoriginal, L->cord + N, sizeof(double) * N);
         for (size_t e = 0; e < E; ++e) {
             if (L->shrheat) L->shrheat[e] = 0.0;
             if (L->sshrheat) L->sshrheat[e] = 0.0;

@@ -82,8 +82,8 @@ extern "C" {
 #define GF_F_RATE (1u << 10) /* e2sr, se2sr, shrheat, sshrheat, temp0, source */
 #define GF_F_BC (1u << 11)   /* bc and ncod */
 #define GF_F_MARKERS (1u << 12) /* markers, and the surface and bottom accumulators:
-                                   dhacc_correction, dhacc, extr_acc, dtopo, orig,
-                                   q_init, vel_flex_old */
+                                   dhacc_correction, dhacc, extr_acc, dtopo,
+                                   xoriginal, zoriginal, q_init, vel_flex_old */
 #define GF_F_ALL 0xffffffffu
 
 /* Every value of the .inp file, in the order src/read_params.f90:3-348
@@ -206,9 +206,9 @@ typedef struct gf_layout {
      * sub-model), and the last step's topography change per surface node */
     double *dhacc, *extr_acc, *dtopo;
     /* start-up node positions carried through remeshing (xoriginal,
-     * zoriginal: (nz, nx, 2), the reference's arrays.f90:12) and the
-     * flexural bottom's state (fl_flexure.f90: q_init, vel_flex_old; nx) */
-    double *orig, *q_init, *vel_flex_old;
+     * zoriginal: (nz, nx) each, arrays.f90:12) and the flexural bottom's
+     * state (fl_flexure.f90: q_init, vel_flex_old; nx each) */
+    double *xoriginal, *zoriginal, *q_init, *vel_flex_old;
 } gf_layout;
 
 typedef struct gf_ctx gf_ctx;

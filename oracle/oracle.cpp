@@ -847,7 +847,7 @@ void fl_flexure(St &s) {
             double r1 = ED(nz - 2, i - 1), r2 = ED(nz - 2, i);
             rho_b = 0.5 * (r1 + r2);
         }
-        q[i] = q[i] - rho_b * g * (L.orig[N + gf_node(s.d, nz - 1, i)] - s.cord(nz - 1, i, 1));
+        q[i] = q[i] - rho_b * g * (L.zoriginal[gf_node(s.d, nz - 1, i)] - s.cord(nz - 1, i, 1));
     }
     bool all_zero = true;
     for (int i = 0; i < nx; ++i) all_zero = all_zero && L.q_init[i] == 0.0;
@@ -913,7 +913,7 @@ void fl_flexure(St &s) {
     for (int i = 0; i < nx; ++i) {
         for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] - L.vel_flex_old[i];
         double cord_old_z = s.cord(nz - 1, i, 1);
-        s.cordr(nz - 1, i, 1) = L.orig[N + gf_node(s.d, nz - 1, i)] - u[2 * i + 1];
+        s.cordr(nz - 1, i, 1) = L.zoriginal[gf_node(s.d, nz - 1, i)] - u[2 * i + 1];
         double vel_flex = 0.0;
         if (dt > 0.0) vel_flex = (s.cord(nz - 1, i, 1) - cord_old_z) / dt;
         for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] + vel_flex;
@@ -2026,10 +2026,8 @@ void remesh(St &s) {
     Interp rn = rem_barcord(coldn, cnewn, nz, nx);
     for (int k = 0; k < 2; ++k) rem_interpolate(rn, L.vel + (size_t)k * N);
     rem_interpolate(rn, L.temp);
-    if (L.orig) { // xoriginal, zoriginal (remesh.f90:242-243)
-        rem_interpolate(rn, L.orig);
-        rem_interpolate(rn, L.orig + N);
-    }
+    if (L.xoriginal) rem_interpolate(rn, L.xoriginal); // remesh.f90:242-243
+    if (L.zoriginal) rem_interpolate(rn, L.zoriginal);
     // side-wall geotherms for incoming material (sidewalltemp, init_temp.f90:313-353)
     if (p.incoming_left == 1) {
         for (int i = 0; i <= idist; ++i) geotherm_column(s, 0, i, p.age_1[0], p.tp1[0], p.tp2[0]);
