@@ -44,6 +44,29 @@ def _dist():
     return ws, rank, local
 
 
+def _max_over_ranks(x: float, device: str) -> float:
+    """The largest value of x over the ranks of the process group (x itself
+    without one)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _replica_throughput(units_per_rank: float, t_rank: float, device: str):
+    """Whole-job throughput of N independent replicas: all ranks' units over
+    the slowest rank's time.  Returns (value, slowest time)."""
+    import torch.distributed as dist
+
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = _max_over_ranks(t_rank, device)
+    return ws * units_per_rank / t, t
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling during the timed region."""
 
@@ -273,10 +296,7 @@ def run_ours(args):
             torch.cuda.synchronize()
             dev_t, launches, wall = _time_device(g, args.steps, args.warmup, flush)
             torch.cuda.synchronize()
-        t = torch.tensor([dev_t], dtype=torch.float64, device="cuda")
-        if ws > 1:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_t = float(t.item())
+        dev_t = _max_over_ranks(dev_t, "cuda")
         res[mode] = dict(g=g, t=dev_t, launches=launches, clocks=cs.summary(), wall=wall)
     fp = res["fp64"]
     # both modes advanced the same number of steps from the same state:
@@ -385,18 +405,24 @@ def bench_batch(args, workdir: str, local: int):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
     with ClockSampler(local) as cs:
         e0.record(stream)
         b.step(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
     E = b.elements
+    # N replicas of the sweep (one per GPU): all ranks' element-steps over
+    # the slowest rank's time
+    value, t = _replica_throughput(E * args.steps, e0.elapsed_time(e1) / 1e3, "cuda")
     nodes = sum(m.params.nx * m.params.nz for m in models)
     bpe = bytes_model.step_bytes_per_element("mixed", nphase=models[0].params.nphase, n_over_e=nodes / E)
     peak, peak_kind = _peaks()
     achieved = bpe * E * args.steps / t / 1e9
-    out = {"value": E * args.steps / t, "unit": "element-steps/s", "members": len(models), "elements": E,
+    out = {"value": value, "unit": "element-steps/s", "members": len(models), "elements": E,
            "nodes": nodes, "ms_per_step": 1e3 * t / args.steps, "steps": args.steps, "dtype": "f32 element fields / f64 nodes",
            "config": {k: v for k, v in tuned.items() if k != "ms_per_step"}, "grid_ctas": b.grid,
            "gpu_launches": args.steps,
