@@ -142,6 +142,22 @@ def _ncu_traffic(kernel: str):
     return None
 
 
+def _ncu_pipe(kernel: str):
+    """(pipe, fraction of its peak) of `kernel` from the committed ncu summary,
+    if any: the compute bound of a kernel that HBM does not bound."""
+    path = os.path.join(ROOT, "profiles", "pipes.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == kernel:
+            try:
+                return {"pipe": parts[1], "frac_of_peak": float(parts[2]), "source": "ncu (profiles/)"}
+            except ValueError:
+                return None
+    return None
+
+
 def _make_model(inp: str, mode: str):
     import torch
 
@@ -363,7 +379,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "k_rheol (fl_rheol, FP64)", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic, "avg_launch_s": t_rheol,
-                     "algorithmic_bytes_per_launch": alg},
+                     "algorithmic_bytes_per_launch": alg, "compute": _ncu_pipe("k_rheol_fp64")},
         "gpu_launches": fp["launches"],
         "clocks": fp["clocks"],
     }
