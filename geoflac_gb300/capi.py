@@ -121,6 +121,8 @@ LAYOUT_FIELDS = [
     ("mark_id_elem", _pi), ("nmark_elem", _pi),
     ("dhacc", _pd), ("extr_acc", _pd), ("dtopo", _pd),
     ("xoriginal", _pd), ("zoriginal", _pd), ("q_init", _pd), ("vel_flex_old", _pd),
+    ("fmelt", _pd), ("fmelt2", _pd), ("dike_backlog", _pd), ("dike_marker_vol", _pd),
+    ("mor_marker_vol", _pd), ("extrusion", _pd),
 ]
 
 
@@ -228,7 +230,7 @@ class HostState:
     NODE2 = ("cord", "vel", "bc")
     NODE1 = ("temp", "temp0", "amass", "rmass")
     ELEM1 = ("aps", "visn", "e2sr", "source", "shrheat", "sshrheat", "fmagma", "fmagma2",
-             "dike_released")
+             "dike_released", "fmelt", "fmelt2", "dike_backlog", "dike_marker_vol", "mor_marker_vol")
 
     def __init__(self, p: GfParams):
         nx, nz, nph = p.nx, p.nz, p.nphase
@@ -253,7 +255,7 @@ class HostState:
         A["phase_ratio"] = np.zeros((nph, nz - 1, nx - 1), **f8)
         A["jmoho"] = np.zeros(nx, dtype=np.int32)
         A["dhacc_correction"] = np.zeros(nx, dtype=np.float64)
-        for k in ("dhacc", "extr_acc", "dtopo", "q_init", "vel_flex_old"):
+        for k in ("dhacc", "extr_acc", "dtopo", "q_init", "vel_flex_old", "extrusion"):
             A[k] = np.zeros(nx, dtype=np.float64)
         # xoriginal, zoriginal as the two planes of one (nz, nx, 2) array
         A["orig"] = np.zeros((nz, nx, 2), **f8)

@@ -148,6 +148,10 @@ void fill_params(DevParams &P, const gf_params &p) {
     for (int k = 0; k < GF_MAXPH; ++k) P.erodibility[k] = p.erodibility[k];
     P.f_rho_magma = (float)p.rho_magma;
     P.f_g = (float)p.g;
+    P.prod_magma = p.prod_magma; P.prod_magma2 = p.prod_magma2; P.angle_mzone = p.angle_mzone;
+    P.ratio_mantle_mzone = p.ratio_mantle_mzone; P.ratio_crust_mzone = p.ratio_crust_mzone;
+    P.latent_heat_magma = p.latent_heat_magma; P.lambda_freeze = p.lambda_freeze;
+    P.lambda_freeze_tdep = p.lambda_freeze_tdep; P.dxmin = p.dxmin; P.Amin = p.Amin; P.nelem_dike = p.nelem_dike;
 }
 
 GfLaunch launch_of(gf_ctx *c) {
@@ -158,6 +162,7 @@ GfLaunch launch_of(gf_ctx *c) {
     g.d = c->d;
     g.s = c->s;
     g.launches = &c->launches;
+    g.arc_rate = 1.0 - c->p.ratio_mantle_mzone - c->p.ratio_crust_mzone;
     g.idt_scale = c->p.idt_scale;
     g.advance_time = 0;
     return g;
@@ -256,6 +261,13 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.fmagma, A.fmagma, E, dir));
         T_(xfer(c, L.fmagma2, A.fmagma2, E, dir));
         T_(xfer(c, L.dike_released, A.dike_released, E, dir));
+        if (A.dike_backlog) { // magma sub-model
+            T_(xfer(c, L.fmelt, A.fmelt, E, dir));
+            T_(xfer(c, L.fmelt2, A.fmelt2, E, dir));
+            T_(xfer(c, L.dike_backlog, A.dike_backlog, E, dir));
+            T_(xfer(c, L.dike_marker_vol, A.dike_marker_vol, E, dir));
+            T_(xfer(c, L.mor_marker_vol, A.mor_marker_vol, E, dir));
+        }
     }
     if (m & GF_F_MARKERS) {
         long long M = L.max_markers;
@@ -275,6 +287,7 @@ int move_fields(gf_ctx *c, unsigned m, int dir) {
         T_(xfer(c, L.zoriginal, A.orig + N, N, dir));
         T_(xfer(c, L.q_init, A.q_init, c->p.nx, dir));
         T_(xfer(c, L.vel_flex_old, A.vel_flex_old, c->p.nx, dir));
+        if (A.extrusion) T_(xfer(c, L.extrusion, A.extrusion, c->p.nx, dir));
     }
 #undef T_
     if (dir && (m & (GF_F_CORD | GF_F_VEL | GF_F_TEMP)) && c->mode == GF_MODE_MIXED) {
@@ -315,8 +328,17 @@ __global__ void k_clock_advance(DevClock *C) { C->time = C->time + C->dt; }
 // ---- dispatch on precision
 void k_therm(gf_ctx *c) {
     GfLaunch g = launch_of(c);
-    if (c->mode == GF_MODE_MIXED) GfKernels<float>::therm(g, c->sweeps);
-    else GfKernels<double>::therm(g, c->sweeps);
+    if (c->mode == GF_MODE_MIXED) {
+        GfKernels<float>::therm(g, c->sweeps);
+    } else if (c->p.itype_melting == 1) {
+        // temp0 = temp, then the magma sub-model changes temp before the
+        // diffusion (fl_therm.f90:46-391)
+        cudaMemcpyAsync(c->A.temp0, c->A.temp, sizeof(double) * c->d.N, cudaMemcpyDeviceToDevice, c->s);
+        GfMagma::therm(g, (int)c->L.max_markers);
+        GfKernels<double>::therm(g, c->sweeps, 1);
+    } else {
+        GfKernels<double>::therm(g, c->sweeps);
+    }
 }
 void k_rheol(gf_ctx *c, int upd, int avg) {
     GfLaunch g = launch_of(c);
@@ -374,6 +396,7 @@ void k_change_phase(gf_ctx *c) {
     GfLaunch g = launch_of(c);
     if (c->mode == GF_MODE_MIXED) GfKernels<float>::change_phase(g, c->nmarkers);
     else GfKernels<double>::change_phase(g, c->nmarkers);
+    if (c->p.itype_melting == 1) GfMagma::melting(g);
 }
 
 // The launch sequence of one `flac` call depends only on these flags.
@@ -493,8 +516,11 @@ unsigned step_signature(const gf_ctx *c) {
         if (c->nsrate == p.ifreq_avgsr) sig |= 8u << 8;
         else if (c->nsrate == -1) sig |= 4u << 8;
         if (c->nloop % p.ifreq_imasses == 0) sig |= 32u;
-        // resurface: its random seeds use nloop, so such steps run uncaptured
+        // resurface: its random seeds use nloop, so such steps run uncaptured;
+        // so do all steps of the magma sub-model, whose fl_therm may add
+        // markers
         if (p.movegrid != 0 && p.topo_kappa > 0.0 && c->nloop % p.ifreq_avgsr == 0) sig |= 64u;
+        if (p.itype_melting == 1) sig |= 64u;
     }
     return sig;
 }
@@ -587,7 +613,9 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     *out = nullptr;
     if (mode != GF_MODE_FP64 && mode != GF_MODE_MIXED) return GF_ERR_ARG;
     if (L->nx != p->nx || L->nz != p->nz || L->nphase != p->nphase || p->nx < 2 || p->nz < 2) return GF_ERR_ARG;
-    if (p->nystressbc != 0 || p->itype_melting != 0) return GF_ERR_UNSUPPORTED;
+    if (p->nystressbc != 0) return GF_ERR_UNSUPPORTED;
+    // the magma sub-model runs in FP64 contexts only
+    if (p->itype_melting != 0 && (p->itype_melting != 1 || mode == GF_MODE_MIXED)) return GF_ERR_UNSUPPORTED;
     // the flexural bottom (nbc 200) runs in FP64 contexts only
     for (int b = 0; b < p->nofbc; ++b)
         if (mode == GF_MODE_MIXED && p->nbc[b] == 200 && p->nofside[b] == 2) return GF_ERR_UNSUPPORTED;
@@ -675,6 +703,24 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &c->d_angle, 1));
     A_(dalloc(c, &A.cord_old, 2 * N));
     A_(dalloc(c, &A.orig, 2 * N));
+    if (p->itype_melting == 1) {
+        A_(dalloc(c, &A.fmelt, E));
+        A_(dalloc(c, &A.fmelt2, E));
+        A_(dalloc(c, &A.dike_added, E));
+        A_(dalloc(c, &A.dike_backlog, E));
+        A_(dalloc(c, &A.dike_marker_vol, E));
+        A_(dalloc(c, &A.mor_marker_vol, E));
+        A_(dalloc(c, &A.extrusion, p->nx));
+        A_(dalloc(c, &A.mg_e, E));
+        A_(dalloc(c, &A.mg_src, (size_t)GF_MG_SRC_W * E));
+        A_(dalloc(c, &A.mg_s, 16));
+        A_(dalloc(c, &A.mg_c, p->nx));
+        A_(dalloc(c, &A.mg_list, E));
+        A_(dalloc(c, &A.mg_blk, E / 1024 + 2));
+        A_(dalloc(c, &A.mg_i, 16));
+        A_(dalloc(c, &A.mg_col, 2 * p->nx));
+        A_(dalloc(c, &A.mg_mask, E));
+    }
     {
         GfRemeshBufs &b = c->rb;
         A_(dalloc(c, &b.tx, p->nx));
@@ -797,9 +843,17 @@ int gf_get_clock(gf_ctx *c, gf_clock *k) {
 
 // One reference subroutine per entry point; each waits for its kernels and
 // returns the device status (the reference's stop code where it would stop).
+static int sync_markers_after_resurface(gf_ctx *c);
+
 int gf_fl_therm(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
+    const bool magma = c->mode == GF_MODE_FP64 && c->p.itype_melting == 1; // may add markers
+    if (magma) GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
     k_therm(c);
+    if (magma) {
+        int rc = sync_markers_after_resurface(c);
+        if (rc) return rc;
+    }
     return call_status(c);
 }
 
@@ -824,8 +878,6 @@ int gf_fl_node(gf_ctx *c) {
     k_node(c);
     return call_status(c);
 }
-
-static int sync_markers_after_resurface(gf_ctx *c);
 
 int gf_fl_move(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
@@ -989,9 +1041,9 @@ int gf_ctx_take_status(gf_ctx *c) { return take_status(c); }
 
 void gf_ctx_invalidate_forces(gf_ctx *c) { c->frc_valid = 0; }
 
-// After a step with resurface: the device marker count is the current one
-// (resurface adds markers); graphs whose change_phase launch covers an older
-// count are dropped.
+// After a step with resurface or the magma sub-model: the device marker
+// count is the current one (both add markers); graphs whose change_phase
+// launch covers an older count are dropped.
 static int sync_markers_after_resurface(gf_ctx *c) {
     int nm = c->nmarkers;
     GF_CK(cudaMemcpyAsync(&nm, c->A.nmarkers, sizeof(int), cudaMemcpyDeviceToHost, c->s));

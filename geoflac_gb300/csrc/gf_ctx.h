@@ -36,6 +36,10 @@ struct DevParams {
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
     double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:108)
     double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)
+    // magma sub-model (itype_melting = 1)
+    double prod_magma, prod_magma2, angle_mzone, ratio_mantle_mzone, ratio_crust_mzone, latent_heat_magma,
+        lambda_freeze, lambda_freeze_tdep, dxmin, Amin;
+    int nelem_dike;
 };
 
 // Scalars the step reads and writes, resident on the device so that a
@@ -95,7 +99,18 @@ struct DevArrays {
     // triangle-1 stress (x, z) and the geometric sums G (x, z)
     float *e_frc;
     int *nmarkers;                                    // device marker count
+    // magma sub-model (allocated when itype_melting = 1): melt fractions,
+    // dike / MOR accumulators (E each), the last arc extrusion (nx), and
+    // scratch: per-element values (E), per-source terms (GF_MG_SRC_W x E),
+    // zone scalars, per-column values (nx), ordered element lists (E) with
+    // their block counts, element masks (E)
+    double *fmelt, *fmelt2, *dike_added, *dike_backlog, *dike_marker_vol, *mor_marker_vol, *extrusion;
+    double *mg_e, *mg_src, *mg_s, *mg_c;
+    int *mg_list, *mg_blk, *mg_i, *mg_col;
+    uint8_t *mg_mask;
 };
+
+#define GF_MG_SRC_W 12 // doubles per migration source
 
 struct GfLaunch {
     const DevParams *P;
@@ -106,11 +121,13 @@ struct GfLaunch {
     long long *launches;
     int idt_scale;   // host copy of the mass-scaling mode (selects launches)
     int advance_time; // fold par.f90's time += dt into the step's last kernel
+    double arc_rate;  // arc extrusion rate 1 - ratio_mantle_mzone - ratio_crust_mzone (diff_topo)
 };
 
 // Launchers, one set per precision (template instantiated in its own TU).
 template <class R> struct GfKernels {
-    static void therm(const GfLaunch &g, int sweeps);
+    // keep_temp0: temp0 was taken before the magma sub-model changed temp
+    static void therm(const GfLaunch &g, int sweeps, int keep_temp0 = 0);
     // mixed: the coefficient pass and the two sweeps + boundary pass of
     // therm, for steps that run the sweeps beside fl_rheol / fl_node
     static void therm_prep(const GfLaunch &g);
@@ -163,6 +180,14 @@ struct GfRemeshBufs {
     int *m_slot;         // markers grouped by element
     int *e_count, *e_offset, *e_fill; // per element (e_offset has E + 1)
     int *d_scalars;      // [0] scan total
+};
+
+// Magma sub-model (itype_melting = 1, FP64 contexts): melting after
+// change_phase's recount (change_phase.f90:264-483) and fl_therm's magma
+// part between temp0 = temp and the diffusion (fl_therm.f90:56-391).
+struct GfMagma {
+    static void melting(const GfLaunch &g);
+    static void therm(const GfLaunch &g, int max_markers);
 };
 
 template <class R> struct GfRemesh {

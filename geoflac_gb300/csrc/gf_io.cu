@@ -93,8 +93,8 @@ __global__ void k_frame_elems(const DevParams *__restrict__ Pp, DevArrays A, GfD
                          T[gf_node(d, j + 1, i + 1)]));
     put(EF_VISC, log10((double)((const R *)A.visn)[e]));
     put(EF_SRC, A.source[e]);
-    put(EF_FMELT, 0.0); // melting is not modelled on this path
-    put(EF_FMELT2, 0.0);
+    put(EF_FMELT, A.fmelt ? A.fmelt[e] : 0.0);
+    put(EF_FMELT2, A.fmelt2 ? A.fmelt2[e] : 0.0);
     put(EF_FMAGMA, A.fmagma ? A.fmagma[e] : 0.0);
     put(EF_FMAGMA2, A.fmagma2 ? A.fmagma2[e] : 0.0);
     const int iph = A.iphase[e];
@@ -127,10 +127,10 @@ __global__ void k_frame_line(const DevParams *__restrict__ Pp, DevArrays A, GfDi
     double cond = Pp->conduct[A.iphase[gf_elem(d, 0, ii)] - 1];
     f.lf[LF_HFL * nx + i] = (float)(cond * dtmpr / dl);
     f.lf[LF_TOPO * nx + i] = (float)(A.cord[N + gf_node(d, 0, i)] / 1000);
-    // dtopo in mm/yr (outflac.f90:410-412); extrusion needs the magma
-    // sub-model and stays zero
+    // dtopo in mm/yr (outflac.f90:410-412); the last arc extrusion
+    // (zero without the magma sub-model)
     f.lf[LF_DTOPO * nx + i] = (float)(A.dtopo[i] / f.dt * 1000 * GF_SEC_YEAR);
-    f.lf[LF_EXTR * nx + i] = 0.0f;
+    f.lf[LF_EXTR * nx + i] = A.extrusion ? (float)A.extrusion[i] : 0.0f;
 }
 
 // marker positions (marker2xy, bar2euler.f90:86-120) and the output records
@@ -444,9 +444,9 @@ int gf_saveflac(gf_ctx *ctx, const char *dir) {
     IO_CK(w8("fmagma.rs", L.fmagma, E));
     IO_CK(w8("fmagma2.rs", L.fmagma2, E));
     IO_CK(w8("source.rs", L.source, E));
-    IO_CK(w8("dike_backlog.rs", nullptr, E)); // dike intrusion is not modelled
-    IO_CK(w8("dike_marker_vol.rs", nullptr, E));
-    IO_CK(w8("mor_marker_vol.rs", nullptr, E));
+    IO_CK(w8("dike_backlog.rs", L.dike_backlog, E));
+    IO_CK(w8("dike_marker_vol.rs", L.dike_marker_vol, E));
+    IO_CK(w8("mor_marker_vol.rs", L.mor_marker_vol, E));
     std::snprintf(line, sizeof line, " %.17E\n", p.Amin);
     IO_CK(append_line(dir, "Amin.rs", 1, line));
     if (p.nyhydro == 2) { // read back by rsflac.f90:189-193
@@ -519,6 +519,12 @@ int gf_rsflac(gf_ctx *ctx, const char *dir) {
     IO_CK(r8("fmagma.rs", L.fmagma, E));
     IO_CK(r8("fmagma2.rs", L.fmagma2, E));
     IO_CK(r8("source.rs", L.source, E));
+    IO_CK(r8("dike_backlog.rs", L.dike_backlog, E));
+    IO_CK(r8("dike_marker_vol.rs", L.dike_marker_vol, E));
+    IO_CK(r8("mor_marker_vol.rs", L.mor_marker_vol, E));
+    // melt fractions restart at zero (rsflac.f90:239-240)
+    for (double *a : {L.fmelt, L.fmelt2})
+        if (a) std::memset(a, 0, sizeof(double) * (size_t)E);
     f = std::fopen(path_of(dir, "Amin.rs").c_str(), "r");
     if (!f) return GF_ERR_IO;
     got = std::fscanf(f, "%lf", &p.Amin);

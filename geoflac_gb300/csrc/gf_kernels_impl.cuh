@@ -889,7 +889,7 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
 
 // temp0 = temp (fl_therm.f90:46-48); temp = converged iterate with the
 // boundary conditions applied.
-__device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax) {
+__device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax, int keep_temp0) {
     int kc = kmax;
     for (int k = 0; k < kmax; ++k)
         if (C->therm_flags[k] == 0) {
@@ -908,11 +908,11 @@ __device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp
     int j, i;
     node_ji(d, n, j, i);
     double t = therm_bc_value(*Pp, A, d, [src](long long m) { return src[m]; }, j, i);
-    A.temp0[n] = A.temp[n];
+    if (!keep_temp0) A.temp0[n] = A.temp[n];
     A.temp[n] = t;
 }
-__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax) {
-    b_k_therm_apply(Pp, C, A, d, b0, b1, kmax);
+__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax, int keep_temp0) {
+    b_k_therm_apply(Pp, C, A, d, b0, b1, kmax, keep_temp0);
 }
 
 // ---- mixed precision: FP32 coefficients, two sweeps.
@@ -1658,7 +1658,7 @@ template <class R> void GfKernels<R>::therm_sweeps(const GfLaunch &g) {
     GF_LAUNCH(k_therm_apply32, g.d.N, g.P, g.A, g.d, g.A.t_delta1);
 }
 
-template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps) {
+template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int keep_temp0) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float)) {
         therm_prep(g);
@@ -1672,7 +1672,7 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps) {
         const double *up = k == 0 ? g.A.temp : bufs[(k - 1) & 1];
         GF_LAUNCH(k_therm_sweep, g.d.N, g.C, g.A, g.d, g.A.t_coef, up, bufs[k & 1], k);
     }
-    GF_LAUNCH(k_therm_apply, g.d.N, g.P, g.C, g.A, g.d, bufs[0], bufs[1], kmax);
+    GF_LAUNCH(k_therm_apply, g.d.N, g.P, g.C, g.A, g.d, bufs[0], bufs[1], kmax, keep_temp0);
 }
 
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {

@@ -1,0 +1,754 @@
+// Magma sub-model on the device (itype_melting = 1, FP64 contexts):
+// melting after change_phase's phase recount (src/change_phase.f90:264-483),
+// fl_therm's magma part (src/fl_therm.f90:56-391) and the magma blocks of
+// diff_topo (src/fl_move.f90:213-302).  Included by gf_remesh.cu inside its
+// kernel namespace (it shares check_inside, add_marker1 and
+// count_phase_ratio1 with the surface processes); compiled without FMA
+// contraction.
+//
+// The reference runs these loops serially (or with OpenMP atomics, whose
+// order varies from run to run); this file reproduces the serial order:
+//  * element-to-node sums become per-node gathers in serial element order;
+//  * the melting loops cool an element's corners in place, so later
+//    elements see earlier ones' cooling: the elements that can melt at all
+//    (above their solidus at the start; temperatures only fall in these
+//    loops) are listed in serial order and one thread walks the list;
+//  * the weighted sums of the MOR melting zone are taken by one warp, terms
+//    computed in parallel and added in order;
+//  * migration scatters many sources into many targets: each target walks
+//    the ordered source list (only the sources whose reach covers its
+//    column), inserting the reference's per-element clamp at its own serial
+//    position;
+//  * new markers are numbered in serial order by one thread walking the
+//    list of elements that receive any.
+
+constexpr int MG_SED1 = 1, MG_OCEAN1 = 3, MG_MANT1 = 4, MG_SCHIST = 5, MG_OCEAN2 = 7, MG_MANT2 = 8, MG_SERP = 9,
+              MG_OCEANDRY = 10, MG_SED2 = 11, MG_ECLG = 13, MG_ARC1 = 14, MG_HYDMANT = 16, MG_METASED = 17;
+constexpr double MG_W_BARRIER = 1.0e-4;
+constexpr int MG_CB = 1024; // elements per block of the ordered compaction
+
+// zone scalars (mg_s) and integer slots (mg_i)
+enum { MS_VALID = 0, MS_XC, MS_ZC, MS_ZSURF, MS_H2, MS_TANL, MS_TANR, MS_TANM, MS_WSUM };
+enum { MI_COUNT = 0, MI_FOUND, MI_IC, MI_JC, MI_IHWL, MI_IHWR, MI_IHW };
+// per-source terms (mg_src, GF_MG_SRC_W doubles per source)
+enum { SR_E = 0, SR_FLAGS, SR_TERM_C, SR_II0, SR_II1, SR_TERM_M, SR_XMELT, SR_ZMELT, SR_J1, SR_I1, SR_TERM_R };
+
+// (j, i) of element e = i (nz-1) + j and of node n = i nz + j
+__device__ __forceinline__ void mg_eji(const GfDims &d, long long e, int &j, int &i) {
+    i = (int)(e / (d.nz - 1));
+    j = (int)(e - (long long)i * (d.nz - 1));
+}
+__device__ __forceinline__ void mg_nji(const GfDims &d, long long n, int &j, int &i) {
+    i = (int)(n / d.nz);
+    j = (int)(n - (long long)i * d.nz);
+}
+__device__ __forceinline__ double mg_min(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double mg_max(double a, double b) { return b > a ? b : a; }
+// ceiling() of a ratio that may be huge, held to +-2^29 (beyond every loop
+// bound it feeds)
+__device__ __forceinline__ int mg_ceil(double x) {
+    double c = ceil(x);
+    if (!(c < 536870912.0)) return 536870912;
+    if (c < -536870912.0) return -536870912;
+    return (int)c;
+}
+// phase_ratio(iph, e) with the reference's flat-memory reads for a phase id
+// above nphase (the next element's entries; zero past the array)
+__device__ __forceinline__ double mg_pr(const DevArrays &A, const GfDims &d, long long e, int iph1) {
+    const long long off = (long long)(iph1 - 1) + (long long)d.nphase * e;
+    if (off < 0 || off >= (long long)d.nphase * d.E) return 0.0;
+    return A.phase_ratio[off];
+}
+__device__ __forceinline__ double mg_T(const DevArrays &A, const GfDims &d, int j, int i) {
+    return A.temp[gf_node(d, j, i)];
+}
+__device__ __forceinline__ double mg_tmpr(const DevArrays &A, const GfDims &d, int j, int i) {
+    return 0.25 * (mg_T(A, d, j, i) + mg_T(A, d, j, i + 1) + mg_T(A, d, j + 1, i) + mg_T(A, d, j + 1, i + 1));
+}
+__device__ __forceinline__ double mg_depth(const DevArrays &A, const GfDims &d, int j, int i) {
+    const double *c = A.cord;
+    double yy = 0.25 * (CY(c, d, j, i) + CY(c, d, j, i + 1) + CY(c, d, j + 1, i) + CY(c, d, j + 1, i + 1));
+    return 0.5 * (CY(c, d, 0, i) + CY(c, d, 0, i + 1)) - yy;
+}
+__device__ __forceinline__ double mg_pmelt(const DevParams &P, int kph, double over, double span) {
+    if (P.latent_heat_magma > 0.0) return mg_min(P.cp[kph - 1] * over / P.latent_heat_magma, 0.1);
+    return mg_min(over / span * 0.1, 0.1);
+}
+__device__ __forceinline__ void mg_cool(DevArrays &A, const GfDims &d, int j, int i, double dt_melt) {
+    double *T = A.temp;
+    T[gf_node(d, j, i)] = T[gf_node(d, j, i)] - dt_melt;
+    T[gf_node(d, j, i + 1)] = T[gf_node(d, j, i + 1)] - dt_melt;
+    T[gf_node(d, j + 1, i)] = T[gf_node(d, j + 1, i)] - dt_melt;
+    T[gf_node(d, j + 1, i + 1)] = T[gf_node(d, j + 1, i + 1)] - dt_melt;
+}
+// the four solidi (Katz 2003 hydrous mantle, Nichols 1994 sediments,
+// Gutscher 2000 basalt / eclogite, Grove 2009 water-saturated mantle)
+__device__ __forceinline__ double sol_mantle(const DevParams &P, double depth) {
+    double press = fabs(3000.0 * P.g * depth * 1e-9);
+    return -5.02 * (press * press) + 1.32e2 * press + 1.09e3;
+}
+__device__ __forceinline__ double sol_sed(double depth) {
+    return mg_max(680 + 0.6e-3 * (depth - 140e3), 930 - 313 * (1 - gfm::exp(-depth / 7e3)));
+}
+__device__ __forceinline__ double sol_basalt(double depth) {
+    double press = 3000 * 10 * depth / 1e9;
+    if (press < 1.0) return 1050.0 - 420.0 * (1.0 - gfm::exp(-press * 3.3));
+    if (press > 2.7) return (press + 14.0) * 43.0;
+    return 630.0 + 13.0 * (press * press);
+}
+__device__ __forceinline__ double sol_wet(double depth) {
+    if (depth > 80e3) return 800;
+    return 800 + (double)6.2e-8f * ((depth - 80e3) * (depth - 80e3));
+}
+__device__ __forceinline__ double tpr_mantle(const DevArrays &A, const GfDims &d, long long e) {
+    return mg_pr(A, d, e, MG_MANT1) + mg_pr(A, d, e, MG_MANT2);
+}
+__device__ __forceinline__ double tpr_sed(const DevArrays &A, const GfDims &d, long long e) {
+    return mg_pr(A, d, e, MG_SED1) + mg_pr(A, d, e, MG_SED2) + mg_pr(A, d, e, MG_METASED) + mg_pr(A, d, e, MG_SCHIST);
+}
+__device__ __forceinline__ double tpr_basalt(const DevArrays &A, const GfDims &d, long long e) {
+    return mg_pr(A, d, e, MG_OCEAN1) + mg_pr(A, d, e, MG_OCEAN2) + mg_pr(A, d, e, MG_OCEANDRY) + mg_pr(A, d, e, MG_ECLG);
+}
+
+// ---------------------------------------------------------------- ordered compaction
+// Which elements a list holds.
+enum { MG_PRED_MASK = 0, MG_PRED_W = 1, MG_PRED_SRC = 2 };
+__device__ __forceinline__ bool mg_pred(int mode, const DevArrays &A, const GfDims &d, long long e) {
+    if (mode == MG_PRED_MASK) return A.mg_mask[e] != 0;
+    if (mode == MG_PRED_W) return A.fmelt2[e] > MG_W_BARRIER;
+    // migration sources: melting below the column's Moho, or MOR melt with
+    // a valid melting zone
+    int j, i;
+    mg_eji(d, e, j, i);
+    if (j + 1 > A.jmoho[i] && A.fmelt[e] > 0) return true;
+    return A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0;
+}
+// block b counts its MG_CB elements
+__global__ void __launch_bounds__(MG_CB) k_mg_count(DevArrays A, GfDims d, int mode) {
+    const long long e = (long long)blockIdx.x * MG_CB + threadIdx.x;
+    const int v = (e < d.E && mg_pred(mode, A, d, e)) ? 1 : 0;
+    const int c = __syncthreads_count(v);
+    if (threadIdx.x == 0) A.mg_blk[blockIdx.x] = c;
+}
+// block b writes its elements after those of blocks 0..b-1; the last block
+// stores the total in mg_i[MI_COUNT]
+__global__ void __launch_bounds__(MG_CB) k_mg_write(DevArrays A, GfDims d, int mode) {
+    __shared__ int red[32];
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int part = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += MG_CB) part += A.mg_blk[b];
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) red[w] = part;
+    __syncthreads();
+    int base = 0;
+    for (int k = 0; k < MG_CB / 32; ++k) base += red[k];
+    const long long e = (long long)blockIdx.x * MG_CB + threadIdx.x;
+    const bool v = e < d.E && mg_pred(mode, A, d, e);
+    const unsigned bal = __ballot_sync(0xffffffffu, v);
+    if (lane == 0) wsum[w] = __popc(bal);
+    __syncthreads();
+    int off = base;
+    for (int k = 0; k < w; ++k) off += wsum[k];
+    off += __popc(bal & ((1u << lane) - 1u));
+    if (v) A.mg_list[off] = (int)e;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        int tot = base;
+        for (int k = 0; k < MG_CB / 32; ++k) tot += wsum[k];
+        A.mg_i[MI_COUNT] = tot;
+    }
+}
+
+// ---------------------------------------------------------------- melting (change_phase)
+// per column: the deepest serpentinite / chlorite element above the
+// melting depth (flux melting starts there; -1: none), or fl_therm's
+// topmost non-sediment row (1-based) for the dikes
+__global__ void k_mg_cols(DevArrays A, GfDims d, int mode) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.nx - 1) return;
+    if (mode == 0) {
+        int js = -1;
+        for (int j = d.nz - 2; j >= 0; --j) {
+            const long long e = gf_elem(d, j, i);
+            if (mg_pr(A, d, e, MG_SERP) + mg_pr(A, d, e, MG_HYDMANT) > 0.6 && CY(A.cord, d, j, i) > -200e3) {
+                js = j;
+                break;
+            }
+        }
+        A.mg_col[i] = js;
+    } else {
+        const int jm = A.jmoho[i] < d.nz - 1 ? A.jmoho[i] : d.nz - 1;
+        int jtop = 1;
+        while (jtop < jm) {
+            const int iph = A.iphase[gf_elem(d, jtop - 1, i)];
+            if (iph != MG_SED1 && iph != MG_SED2) break;
+            ++jtop;
+        }
+        A.mg_col[d.nx + i] = jtop;
+    }
+}
+
+// zero the melt fractions; mark the elements above a solidus at the start
+// (bit 0 mantle, 1 sediments, 2 basalt, 3 flux melting)
+__global__ void __launch_bounds__(GF_THREADS) k_melt_flags(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const DevParams &P = *Pp;
+    int j, i;
+    mg_eji(d, e, j, i);
+    A.fmelt[e] = 0.0;
+    A.fmelt2[e] = 0.0;
+    const double z = CY(A.cord, d, j, i);
+    const double tmpr = mg_tmpr(A, d, j, i), depth = mg_depth(A, d, j, i);
+    unsigned m = 0;
+    if (tpr_mantle(A, d, e) > 0.6 && z > -150e3 && tmpr > sol_mantle(P, depth)) m |= 1u;
+    if (tpr_sed(A, d, e) > 0.6 && z > -200e3 && tmpr > sol_sed(depth)) m |= 2u;
+    if (tpr_basalt(A, d, e) > 0.6 && z > -200e3 && tmpr > sol_basalt(depth)) m |= 4u;
+    const int js = A.mg_col[i];
+    if (js >= 0 && j <= js && tmpr > sol_wet(depth)) m |= 8u;
+    A.mg_mask[e] = (uint8_t)m;
+}
+
+// the four melting loops over the listed elements, in the reference's order
+__global__ void k_melt_serial(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const DevParams &P = *Pp;
+    const int n = A.mg_i[MI_COUNT];
+    const int *list = A.mg_list;
+    int j, i;
+    for (int k = 0; k < n; ++k) { // hydrous mantle
+        const long long e = list[k];
+        if (!(A.mg_mask[e] & 1u)) continue;
+        mg_eji(d, e, j, i);
+        const double tpr = tpr_mantle(A, d, e), tmpr = mg_tmpr(A, d, j, i);
+        const double sol = sol_mantle(P, mg_depth(A, d, j, i));
+        if (tmpr > sol) {
+            A.fmelt2[e] = mg_pmelt(P, MG_MANT1, tmpr - sol, 35.0) * tpr;
+            mg_cool(A, d, j, i, tmpr - sol);
+        }
+    }
+    for (int k = 0; k < n; ++k) { // sediments
+        const long long e = list[k];
+        if (!(A.mg_mask[e] & 2u)) continue;
+        mg_eji(d, e, j, i);
+        const double tpr = tpr_sed(A, d, e), tmpr = mg_tmpr(A, d, j, i);
+        const double sol = sol_sed(mg_depth(A, d, j, i));
+        if (tmpr > sol) {
+            A.fmelt[e] = mg_pmelt(P, MG_SED2, tmpr - sol, 50.0) * tpr;
+            mg_cool(A, d, j, i, tmpr - sol);
+        }
+    }
+    for (int k = 0; k < n; ++k) { // basalt and eclogite
+        const long long e = list[k];
+        if (!(A.mg_mask[e] & 4u)) continue;
+        mg_eji(d, e, j, i);
+        const double tpr = tpr_basalt(A, d, e), tmpr = mg_tmpr(A, d, j, i);
+        const double sol = sol_basalt(mg_depth(A, d, j, i));
+        if (tmpr > sol) {
+            A.fmelt[e] = A.fmelt[e] + mg_pmelt(P, MG_OCEAN1, tmpr - sol, 20.0) * tpr;
+            mg_cool(A, d, j, i, tmpr - sol);
+        }
+    }
+    // flux melting: columns in order, each upwards from its start row (the
+    // list holds a column's elements contiguously, top to bottom)
+    for (int k = 0; k < n;) {
+        const int col = (int)(list[k] / (d.nz - 1));
+        int kend = k;
+        while (kend < n && (int)(list[kend] / (d.nz - 1)) == col) ++kend;
+        for (int kk = kend - 1; kk >= k; --kk) {
+            const long long e = list[kk];
+            if (!(A.mg_mask[e] & 8u)) continue;
+            mg_eji(d, e, j, i);
+            const double tmpr = mg_tmpr(A, d, j, i), sol = sol_wet(mg_depth(A, d, j, i));
+            if (tmpr > sol) {
+                A.fmelt[e] = A.fmelt[e] + mg_pmelt(P, MG_MANT1, tmpr - sol, 50.0) *
+                                              (mg_pr(A, d, e, MG_MANT1) + mg_pr(A, d, e, MG_MANT2) + mg_pr(A, d, e, MG_SERP));
+                mg_cool(A, d, j, i, tmpr - sol);
+            }
+        }
+        k = kend;
+    }
+}
+
+// ---------------------------------------------------------------- fl_therm's magma part
+// freezing of both pools (temperature from temp0); the latent heat of the
+// element's four corners kept for the node pass
+__global__ void __launch_bounds__(GF_THREADS) k_mg_freeze(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
+                                                          GfDims d) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const DevParams &P = *Pp;
+    const double dt = C->dt;
+    int j, i;
+    mg_eji(d, e, j, i);
+    const double *T0 = A.temp0;
+    const double cp_eff = P.cp[A.iphase[e] - 1];
+    const double tmpr = 0.25 * (T0[gf_node(d, j, i)] + T0[gf_node(d, j + 1, i)] + T0[gf_node(d, j, i + 1)] +
+                                T0[gf_node(d, j + 1, i + 1)]);
+    const double fr_lambda = P.lambda_freeze * gfm::exp(-P.lambda_freeze_tdep * (tmpr - P.t_top));
+    const double f1 = A.fmagma[e], f2 = A.fmagma2[e];
+    const double d1 = mg_min(f1, f1 * dt * fr_lambda), d2 = mg_min(f2, f2 * dt * fr_lambda);
+    A.fmagma[e] = f1 - d1;
+    A.fmagma2[e] = f2 - d2;
+    A.mg_e[e] = d1 * P.latent_heat_magma / cp_eff / 4 + d2 * P.latent_heat_magma / cp_eff / 4;
+}
+// each node adds its elements' latent heat in serial element order, then
+// temp = min(temp, t_bot)
+__global__ void __launch_bounds__(GF_THREADS) k_mg_freeze_nodes(const DevParams *__restrict__ Pp, DevArrays A,
+                                                                GfDims d) {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= d.N) return;
+    int J, I;
+    mg_nji(d, n, J, I);
+    const int nx = d.nx, nz = d.nz;
+    double t = A.temp[n];
+    if (J > 0 && I > 0) t = t + A.mg_e[gf_elem(d, J - 1, I - 1)];
+    if (J < nz - 1 && I > 0) t = t + A.mg_e[gf_elem(d, J, I - 1)];
+    if (J > 0 && I < nx - 1) t = t + A.mg_e[gf_elem(d, J - 1, I)];
+    if (J < nz - 1 && I < nx - 1) t = t + A.mg_e[gf_elem(d, J, I)];
+    A.temp[n] = mg_min(t, Pp->t_bot);
+}
+
+// element centre of the quad with the reference's corner order
+// (j,i), (j,i+1), (j+1,i), (j+1,i+1)
+__device__ __forceinline__ double mg_cx(const double *c, const GfDims &d, int j, int i) {
+    return 0.25 * (CX(c, d, j, i) + CX(c, d, j, i + 1) + CX(c, d, j + 1, i) + CX(c, d, j + 1, i + 1));
+}
+__device__ __forceinline__ double mg_cz(const double *c, const GfDims &d, int j, int i) {
+    return 0.25 * (CY(c, d, j, i) + CY(c, d, j, i + 1) + CY(c, d, j + 1, i) + CY(c, d, j + 1, i + 1));
+}
+
+// fmelt2-weighted centre of the MOR melting zone (one warp: terms in
+// parallel, sums in serial order); also the mantle cone's tan and width
+__global__ void k_mg_zone1(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    const DevParams &P = *Pp;
+    const int n = A.mg_i[MI_COUNT];
+    double xs = 0, zs = 0, ws = 0;
+    for (int base = 0; base < n; base += 32) {
+        double tx = 0, tz = 0, tw = 0;
+        if (base + lane < n) {
+            const long long e = A.mg_list[base + lane];
+            int j, i;
+            mg_eji(d, e, j, i);
+            tw = A.fmelt2[e];
+            tx = mg_cx(A.cord, d, j, i) * tw;
+            tz = mg_cz(A.cord, d, j, i) * tw;
+        }
+        const int m = n - base < 32 ? n - base : 32;
+        for (int k = 0; k < m; ++k) {
+            xs = xs + __shfl_sync(0xffffffffu, tx, k);
+            zs = zs + __shfl_sync(0xffffffffu, tz, k);
+            ws = ws + __shfl_sync(0xffffffffu, tw, k);
+        }
+    }
+    if (lane == 0) {
+        const double tan_m = gfm::tan(0.5 * P.angle_mzone * 3.14159265358979323846 / 180.0);
+        A.mg_s[MS_TANM] = tan_m;
+        A.mg_i[MI_IHW] = mg_ceil(tan_m * 200e3 / P.dxmin);
+        A.mg_s[MS_WSUM] = ws;
+        A.mg_s[MS_VALID] = 0.0;
+        A.mg_i[MI_FOUND] = 0x7fffffff;
+        if (ws > 0.0) {
+            A.mg_s[MS_XC] = xs / ws;
+            A.mg_s[MS_ZC] = zs / ws;
+        }
+    }
+}
+// the first element (serial order) holding the centre
+__global__ void __launch_bounds__(GF_THREADS) k_mg_find(DevArrays A, GfDims d) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E || !(A.mg_s[MS_WSUM] > 0.0)) return;
+    int j, i;
+    mg_eji(d, e, j, i);
+    const double xc = A.mg_s[MS_XC], zc = A.mg_s[MS_ZC];
+    const double *c = A.cord;
+    if (CX(c, d, j, i) <= xc && CX(c, d, j, i + 1) >= xc && CY(c, d, j, i) >= zc && CY(c, d, j + 1, i) <= zc)
+        atomicMin(&A.mg_i[MI_FOUND], (int)e);
+}
+// widths on either side of the centre and the zone's cone (one warp)
+__global__ void k_mg_zone2(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int found = A.mg_i[MI_FOUND];
+    if (found == 0x7fffffff) return;
+    const int lane = threadIdx.x;
+    const DevParams &P = *Pp;
+    const int n = A.mg_i[MI_COUNT];
+    const double xc = A.mg_s[MS_XC];
+    double xl = 0, xr = 0, wl = 0, wr = 0;
+    for (int base = 0; base < n; base += 32) {
+        double tl = 0, tr = 0, w = 0, x = 0;
+        if (base + lane < n) {
+            const long long e = A.mg_list[base + lane];
+            int j, i;
+            mg_eji(d, e, j, i);
+            w = A.fmelt2[e];
+            x = mg_cx(A.cord, d, j, i);
+            tl = (xc - x) * (xc - x) * w;
+            tr = (x - xc) * (x - xc) * w;
+        }
+        const int m = n - base < 32 ? n - base : 32;
+        for (int k = 0; k < m; ++k) {
+            const double xk = __shfl_sync(0xffffffffu, x, k), wk = __shfl_sync(0xffffffffu, w, k);
+            const double lk = __shfl_sync(0xffffffffu, tl, k), rk = __shfl_sync(0xffffffffu, tr, k);
+            if (xk < xc) {
+                xl = xl + lk;
+                wl = wl + wk;
+            } else if (xk > xc) {
+                xr = xr + rk;
+                wr = wr + wk;
+            }
+        }
+    }
+    if (lane == 0) {
+        int jc, ic;
+        mg_eji(d, found, jc, ic);
+        xl = 1.8 * sqrt(xl / wl);
+        xr = 1.8 * sqrt(xr / wr);
+        if (xl < P.dxmin) xl = P.dxmin;
+        if (xr < P.dxmin) xr = P.dxmin;
+        if (xl != xl) xl = P.dxmin;
+        if (xr != xr) xr = P.dxmin;
+        const double z_surf = 0.5 * (CY(A.cord, d, 0, ic) + CY(A.cord, d, 0, ic + 1));
+        const double h2 = z_surf - A.mg_s[MS_ZC];
+        const double tl = xl / h2, tr = xr / h2;
+        A.mg_s[MS_ZSURF] = z_surf;
+        A.mg_s[MS_H2] = h2;
+        A.mg_s[MS_TANL] = tl;
+        A.mg_s[MS_TANR] = tr;
+        A.mg_i[MI_IC] = ic;
+        A.mg_i[MI_JC] = jc;
+        A.mg_i[MI_IHWL] = mg_ceil(tl * 150e3 / P.dxmin);
+        A.mg_i[MI_IHWR] = mg_ceil(tr * 150e3 / P.dxmin);
+        A.mg_s[MS_VALID] = 1.0;
+    }
+}
+
+// the terms each listed migration source adds
+__global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
+                                                       GfDims d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.mg_i[MI_COUNT]) return;
+    const DevParams &P = *Pp;
+    const double dt = C->dt;
+    const long long e = A.mg_list[k];
+    int j, i;
+    mg_eji(d, e, j, i);
+    const int nx = d.nx, i1 = i + 1, j1 = j + 1;
+    const int jm = A.jmoho[i] < 1 ? 1 : (A.jmoho[i] > d.nz - 1 ? d.nz - 1 : A.jmoho[i]); // a valid row
+    const double *c = A.cord;
+    const double area0 = ((const double *)A.area)[gf_ek(d, e, 0)], area1 = ((const double *)A.area)[gf_ek(d, e, 1)];
+    const double quad_area = 0.5 / area0 + 0.5 / area1;
+    double *s = A.mg_src + (long long)k * GF_MG_SRC_W;
+    unsigned flags = 0;
+    s[SR_E] = (double)e;
+    s[SR_J1] = j1;
+    s[SR_I1] = i1;
+    if (j1 > jm && A.fmelt[e] > 0) {
+        flags |= 1u;
+        const double fm = A.fmelt[e];
+        double area_ratio = (CY(c, d, 0, i) + CY(c, d, 0, i + 1) - CY(c, d, jm - 1, i) - CY(c, d, jm - 1, i + 1)) /
+                            (CY(c, d, j, i) + CY(c, d, j, i + 1) - CY(c, d, j + 1, i) - CY(c, d, j + 1, i + 1));
+        const int nd = P.nelem_dike;
+        const int ihalf = (nd - 1) / 2 > 0 ? (nd - 1) / 2 : 0, nd1 = nd > 1 ? nd : 1;
+        int ii_start = i1 - ihalf > 1 ? i1 - ihalf : 1;
+        int ii_end = ii_start + nd1 - 1 < nx - 1 ? ii_start + nd1 - 1 : nx - 1;
+        ii_start = ii_end - nd1 + 1 > 1 ? ii_end - nd1 + 1 : 1;
+        const int ncol = ii_end - ii_start + 1;
+        s[SR_TERM_C] = fm * P.ratio_crust_mzone * area_ratio * P.prod_magma * dt / ncol;
+        s[SR_II0] = ii_start;
+        s[SR_II1] = ii_end;
+        const double z_moho = 0.5 * (CY(c, d, jm - 1, i) + CY(c, d, jm - 1, i + 1));
+        const double z_melt = 0.5 * (CY(c, d, j + 1, i) + CY(c, d, j + 1, i + 1));
+        const double x_melt = 0.5 * (CX(c, d, j + 1, i) + CX(c, d, j + 1, i + 1));
+        const double h = z_moho - z_melt;
+        area_ratio = h * h * A.mg_s[MS_TANM] / quad_area;
+        s[SR_TERM_M] = fm * P.ratio_mantle_mzone * area_ratio * P.prod_magma * dt;
+        s[SR_XMELT] = x_melt;
+        s[SR_ZMELT] = z_melt;
+    }
+    if (A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0) {
+        flags |= 2u;
+        const double h2 = A.mg_s[MS_H2];
+        const double area_ratio =
+            0.5 * (h2 * h2 * A.mg_s[MS_TANL] / quad_area + h2 * h2 * A.mg_s[MS_TANR] / quad_area);
+        s[SR_TERM_R] = A.fmelt2[e] * area_ratio * P.prod_magma2 * dt;
+    }
+    s[SR_FLAGS] = flags;
+}
+
+// first position of the ordered source list whose element is >= e
+__device__ __forceinline__ int mg_lower(const int *list, int n, long long e) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (list[mid] < e) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// every element as a migration target: the adds of the sources that reach
+// it, in serial order, with its own clamp to fmagma_max at its place in
+// that order; dike_added and the MOR marker volume alongside
+__global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.E) return;
+    const DevParams &P = *Pp;
+    const int nx = d.nx, nz = d.nz;
+    int jt, it;
+    mg_eji(d, t, jt, it);
+    const int jt1 = jt + 1, it1 = it + 1;
+    const double *c = A.cord;
+    const double x = 0.5 * (CX(c, d, jt, it) + CX(c, d, jt, it + 1));
+    const double z = 0.5 * (CY(c, d, jt, it) + CY(c, d, jt, it + 1));
+    const int jm_t = A.jmoho[it], jtop_t = A.mg_col[nx + it];
+    const bool crust_row = jt1 >= jtop_t && jt1 <= jm_t;
+    const int n = A.mg_i[MI_COUNT];
+    const int ihw = A.mg_i[MI_IHW];
+    const double tan_m = A.mg_s[MS_TANM];
+    // the MOR zone above the melting centre
+    bool mor = false;
+    double xc = 0, z_surf = 0, tl = 0, tr = 0;
+    if (A.mg_s[MS_VALID] != 0.0) {
+        const int ic1 = A.mg_i[MI_IC] + 1, jc1 = A.mg_i[MI_JC] + 1;
+        const int lo = ic1 - A.mg_i[MI_IHWL] > 1 ? ic1 - A.mg_i[MI_IHWL] : 1;
+        const int hi = ic1 + A.mg_i[MI_IHWR] < nx - 1 ? ic1 + A.mg_i[MI_IHWR] : nx - 1;
+        mor = it1 >= lo && it1 <= hi && jt1 <= jc1;
+        xc = A.mg_s[MS_XC];
+        z_surf = A.mg_s[MS_ZSURF];
+        tl = A.mg_s[MS_TANL];
+        tr = A.mg_s[MS_TANR];
+    }
+    // sources whose dikes or mantle cone can reach this column: columns
+    // within max(nelem_dike, cone half width) (every source when the
+    // element is in the MOR zone)
+    int k0 = 0, k1 = n;
+    if (!mor) {
+        const int reach = (P.nelem_dike > ihw ? P.nelem_dike : ihw) + 1;
+        const long long clo = it - reach < 0 ? 0 : it - reach;
+        const long long chi = it + reach + 1 > nx - 1 ? nx - 1 : it + reach + 1;
+        k0 = mg_lower(A.mg_list, n, clo * (nz - 1));
+        k1 = mg_lower(A.mg_list, n, chi * (nz - 1));
+    }
+    const double fmax = P.fmagma_max;
+    double f = A.fmagma[t], f2 = A.fmagma2[t], da = 0.0, mv = A.mor_marker_vol[t];
+    bool clamped = false;
+    for (int k = k0; k < k1; ++k) {
+        const double *s = A.mg_src + (long long)k * GF_MG_SRC_W;
+        const long long es = (long long)s[SR_E];
+        if (!clamped && es > t) {
+            f = mg_min(f, fmax);
+            f2 = mg_min(f2, fmax);
+            clamped = true;
+        }
+        const unsigned flags = (unsigned)s[SR_FLAGS];
+        if (flags & 1u) {
+            if (crust_row && it1 >= (int)s[SR_II0] && it1 <= (int)s[SR_II1]) {
+                f = f + s[SR_TERM_C];
+                da = da + s[SR_TERM_C];
+            }
+            const int i1s = (int)s[SR_I1];
+            const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
+            if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= (int)s[SR_J1] &&
+                fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
+                f = f + s[SR_TERM_M];
+        }
+        if ((flags & 2u) && mor) {
+            if (x < xc && fabs(xc - x) <= tl * (z_surf - z)) {
+                f2 = f2 + s[SR_TERM_R];
+                mv = mv + s[SR_TERM_R];
+            }
+            if (x >= xc && fabs(x - xc) <= tr * (z_surf - z)) {
+                f2 = f2 + s[SR_TERM_R];
+                mv = mv + s[SR_TERM_R];
+            }
+        }
+        if (es == t) {
+            f = mg_min(f, fmax);
+            f2 = mg_min(f2, fmax);
+            clamped = true;
+        }
+    }
+    if (!clamped) {
+        f = mg_min(f, fmax);
+        f2 = mg_min(f2, fmax);
+    }
+    A.fmagma[t] = f;
+    A.fmagma2[t] = f2;
+    A.dike_added[t] = da;
+    A.mor_marker_vol[t] = mv;
+}
+
+// rate-capped dike release; mark the elements that receive new markers
+__global__ void __launch_bounds__(GF_THREADS) k_mg_release(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= d.E) return;
+    const DevParams &P = *Pp;
+    const double *area = (const double *)A.area;
+    const double elem_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
+    const double pending = A.dike_added[e] * elem_area + A.dike_backlog[e];
+    const double released = mg_min(pending, 1.0e-4 * P.Amin);
+    A.dike_backlog[e] = pending - released;
+    A.dike_released[e] = released / elem_area;
+    const double dmv = A.dike_marker_vol[e] + released;
+    A.dike_marker_vol[e] = dmv;
+    const int kinc = A.nmark_elem[e];
+    bool add = false;
+    if (kinc > 0 && kinc < GF_MAX_MARKERS_PER_ELEM) {
+        const double unit = elem_area / kinc;
+        // the MOR test with the count before any arc markers is exact when
+        // no arc marker comes first and a superset otherwise
+        add = dmv >= unit || A.mor_marker_vol[e] >= unit;
+    }
+    A.mg_mask[e] = add ? 1 : 0;
+}
+// new arc (karc1) and oceanic-crust (kocean1) markers at the centres of the
+// listed elements, numbered in serial order
+__global__ void k_mg_markers(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d, int max_markers) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const DevParams &P = *Pp;
+    const int n = A.mg_i[MI_COUNT];
+    const double *area = (const double *)A.area;
+    const double time = C->time;
+    for (int k = 0; k < n; ++k) {
+        const long long e = A.mg_list[k];
+        int j, i;
+        mg_eji(d, e, j, i);
+        const double elem_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
+        for (int path = 0; path < 2; ++path) {
+            double *vol = path == 0 ? &A.dike_marker_vol[e] : &A.mor_marker_vol[e];
+            const int kinc = A.nmark_elem[e];
+            if (kinc > 0 && kinc < GF_MAX_MARKERS_PER_ELEM) {
+                const double unit = elem_area / kinc;
+                if (*vol >= unit) {
+                    const int room = GF_MAX_MARKERS_PER_ELEM - kinc, want = mg_ceil(*vol / unit);
+                    const int n_to_add = want < room ? want : room;
+                    const double *c = A.cord;
+                    const double xc = 0.25 * (CX(c, d, j, i) + CX(c, d, j + 1, i) + CX(c, d, j, i + 1) + CX(c, d, j + 1, i + 1));
+                    const double yc = 0.25 * (CY(c, d, j, i) + CY(c, d, j + 1, i) + CY(c, d, j, i + 1) + CY(c, d, j + 1, i + 1));
+                    for (int m = 0; m < n_to_add; ++m)
+                        add_marker1(A, d, xc, yc, path == 0 ? MG_ARC1 : MG_OCEAN1, time, j, i, max_markers);
+                    *vol = 0.0;
+                    count_phase_ratio1(P, C, A, d, e);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- diff_topo's magma blocks
+// arc extrusion of each inner column (fl_move.f90:213-237)
+__global__ void __launch_bounds__(GF_THREADS) k_arc_cols(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
+                                                         GfDims d, double rate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i >= d.nx - 2) return;
+    const DevParams &P = *Pp;
+    const double *area = (const double *)A.area;
+    double totalmelt = 0;
+    for (int j = 0; j < d.nz - 1; ++j) {
+        const long long e = gf_elem(d, j, i);
+        const double quad_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
+        totalmelt = totalmelt + quad_area * A.fmelt[e];
+    }
+    const double *c = A.cord;
+    const double ext = rate * C->dt * totalmelt * P.prod_magma /
+                       (CX(c, d, 0, i + 1) - CX(c, d, 0, i) +
+                        0.5 * (CX(c, d, 0, i) - CX(c, d, 0, i - 1) + CX(c, d, 0, i + 2) - CX(c, d, 0, i + 1)));
+    A.extrusion[i] = ext;
+    A.extr_acc[i] = A.extr_acc[i] + ext;
+    A.dhacc[i] = A.dhacc[i] + ext;
+}
+// each surface node takes the extrusion of the column on its left, then of
+// the one on its right (serial column order)
+__global__ void k_arc_nodes(DevArrays A, GfDims d) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= d.nx) return;
+    const long long nz_ = d.N + gf_node(d, 0, I);
+    double hc = A.dhacc_correction[I], z = A.cord[nz_];
+    if (I - 1 >= 1 && I - 1 < d.nx - 2) {
+        hc = hc + A.extrusion[I - 1];
+        z = z + A.extrusion[I - 1];
+    }
+    if (I >= 1 && I < d.nx - 2) {
+        hc = hc + A.extrusion[I];
+        z = z + A.extrusion[I];
+    }
+    A.dhacc_correction[I] = hc;
+    A.cord[nz_] = z;
+}
+// the MOR pool of each inner column: its volume, the erupted fraction
+// taken from the pool, and the height it would form (fl_move.f90:247-264)
+__global__ void __launch_bounds__(GF_THREADS) k_mor_cols(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
+                                                         GfDims d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (i >= d.nx - 2) return;
+    const DevParams &P = *Pp;
+    const double dt = C->dt;
+    const double *area = (const double *)A.area;
+    double total_melt = 0;
+    for (int j = 0; j < d.nz - 1; ++j) {
+        const long long e = gf_elem(d, j, i);
+        const double quad_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
+        const double f2 = A.fmagma2[e];
+        total_melt = total_melt + quad_area * f2;
+        A.fmagma2[e] = f2 - mg_min(f2, f2 * P.prod_magma2 * dt);
+    }
+    A.mg_c[i] = dt * total_melt * P.prod_magma2 / (CX(A.cord, d, 0, i + 1) - CX(A.cord, d, 0, i));
+}
+// newphase2marker (remesh.f90:495-520) on rows j1..j2, columns i1..i2 (1-based)
+__device__ void mg_newphase(DevArrays &A, const GfDims &d, int j1, int j2, int i1, int i2, int iph) {
+    const long long total = (long long)d.nphase * d.E;
+    for (int i = i1; i <= i2; ++i)
+        for (int j = j1; j <= j2; ++j) {
+            const long long e = gf_elem(d, j - 1, i - 1);
+            for (int n = 0; n < A.nmark_elem[e]; ++n)
+                A.mark_phase[A.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + n] - 1] = (int8_t)iph;
+            A.iphase[e] = iph;
+            for (int k = 0; k < d.nphase; ++k) A.phase_ratio[gf_pr(d, e, k)] = 0.0;
+            const long long off = (long long)(iph - 1) + (long long)d.nphase * e;
+            if (off < total) A.phase_ratio[off] = 1.0;
+        }
+}
+// the columns with MOR magma in serial order (one warp finds them, its first
+// lane walks them): rows of new oceanic crust, and the remainder onto the
+// column's two surface nodes, which the next column reads
+__global__ void k_mor_chain(DevArrays A, GfDims d) {
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x, nx = d.nx, nz = d.nz;
+    double *c = A.cord;
+    for (int base = 1; base < nx - 2; base += 32) {
+        const int ii = base + lane;
+        const bool act = ii < nx - 2 && A.mg_c[ii] != 0.0;
+        unsigned bal = __ballot_sync(0xffffffffu, act);
+        if (lane == 0)
+            while (bal) {
+                const int i = base + __ffs(bal) - 1;
+                bal &= bal - 1;
+                const double eh = A.mg_c[i];
+                double ele_height = 0, quotient = 0, remainder = 0;
+                int j_oc = 1;
+                for (int j = 0; j < nz - 1; ++j) {
+                    ele_height = ele_height + fabs(0.5 * (CY(c, d, j + 1, i + 1) + CY(c, d, j + 1, i)) -
+                                                   0.5 * (CY(c, d, j, i + 1) + CY(c, d, j, i)));
+                    quotient = eh / ele_height;
+                    remainder = fmod(eh, ele_height);
+                    if (quotient >= 0.0 && quotient < 2.0) {
+                        j_oc = j + 1;
+                        break;
+                    }
+                }
+                for (int j = 1; j <= nz - 1; ++j)
+                    if (A.iphase[gf_elem(d, j - 1, i)] != MG_OCEAN1 && quotient >= 1) {
+                        const int j2 = j + j_oc - 1 < nz - 1 ? j + j_oc - 1 : nz - 1;
+                        mg_newphase(A, d, j, j2, i + 1, i + 1, MG_OCEAN1);
+                        break;
+                    }
+                A.extr_acc[i] = A.extr_acc[i] + remainder / 2;
+                c[d.N + gf_node(d, 0, i)] = c[d.N + gf_node(d, 0, i)] + remainder / 2;
+                c[d.N + gf_node(d, 0, i + 1)] = c[d.N + gf_node(d, 0, i + 1)] + remainder / 2;
+            }
+        __syncwarp();
+    }
+}

@@ -695,8 +695,9 @@ __device__ int add_marker1(DevArrays &A, const GfDims &d, double x, double y, in
 // resurface (fl_move.f90:320-426), serial over the surface elements as in
 // the reference (markers are numbered in element order): erosion past
 // thickness / markers removes the element's topmost marker, deposition adds
-// a sediment marker (phase ksed1 = 1) by add_marker_at_top
-// (fl_move.f90:429-472, stop 134 after 100 misses)
+// a sediment marker (phase ksed1 = 1) and accumulated extrusion arc markers
+// (phase kocean1), by add_marker_at_top (fl_move.f90:429-472, stop 134
+// after 100 misses)
 __global__ void k_resurface(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d, int nloop,
                             int max_markers) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -762,6 +763,35 @@ __global__ void k_resurface(const DevParams *__restrict__ Pp, DevClock *C, DevAr
                 }
             }
             A.dhacc[i] = 0.0;
+            ichanged = 1;
+        }
+        // volcanic extrusion: arc markers (phase kocean1) in the upper part
+        // of the element, add_marker_at_top with seeds nloop + i + ii
+        // (fl_move.f90:403-416)
+        const double chgtopo2 = A.extr_acc[i];
+        if (chgtopo2 * kinc >= elz && kinc != M) {
+            const double q = ceil(chgtopo2 / elz * kinc);
+            const int n_to_add = q < (double)(M - kinc) ? (int)q : M - kinc;
+            const double dz_ratio = 1.0 < chgtopo2 / elz ? 1.0 : chgtopo2 / elz;
+            for (int ii = 1; ii <= n_to_add; ++ii) {
+                int iseed = nloop + (i + 1) + ii + (i + 1), icount = 0;
+                while (true) {
+                    double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
+                    double x1 = CX(c, d, 0, i) * (1 - r1) + CX(c, d, 0, i + 1) * r1;
+                    double y1 = CY(c, d, 0, i) * (1 - r1) + CY(c, d, 0, i + 1) * r1;
+                    double x2 = CX(c, d, 1, i) * (1 - r1) + CX(c, d, 1, i + 1) * r1;
+                    double y2 = CY(c, d, 1, i) * (1 - r1) + CY(c, d, 1, i + 1) * r1;
+                    r2 = r2 * dz_ratio;
+                    double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
+                    int inc = add_marker1(A, d, xx, yy, 3, time, 0, i, max_markers);
+                    if (inc == 1 || inc == -1) break;
+                    if (++icount > 100) {
+                        set_status(C, 134, (int)e);
+                        return;
+                    }
+                }
+            }
+            A.extr_acc[i] = 0.0;
             ichanged = 1;
         }
         if (ichanged == 1) count_phase_ratio1(P, C, A, d, e);
@@ -940,6 +970,8 @@ __global__ void k_surface_acc_remesh(DevArrays A, GfDims d, double *scratch) {
     }
 }
 
+#include "gf_magma.cuh"
+
 } // namespace gfr
 } // namespace
 
@@ -982,6 +1014,9 @@ template <class R> void GfRemesh<R>::regrid(const GfLaunch &g, const GfRemeshArg
     if (sizeof(R) == sizeof(float)) interp_plane<double>(g, b, A.p_ref, nzt, d.E, 0);
     for (int k = 0; k < 3; ++k) interp_plane<R>(g, b, (R *)A.strain + k * d.E, nzt, d.E, 0);
     interp_plane<R>(g, b, (R *)A.aps, nzt, d.E, 1);
+    if (A.dike_backlog) // magma pools and dike / MOR accumulators (remesh.f90:106-115)
+        for (double *f : {A.fmagma, A.fmagma2, A.dike_backlog, A.dike_marker_vol, A.mor_marker_vol})
+            interp_plane<double>(g, b, f, nzt, d.E, 0);
     if (a.incoming_left == 1 || a.incoming_right == 1) {
         k_incoming<R><<<1, GF_THREADS, 0, g.s>>>(g.C, A, d, a);
         ++*g.launches;
@@ -1044,6 +1079,16 @@ template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface,
     using namespace gfr;
     k_diff_topo<<<1, 1024, 0, g.s>>>(g.P, g.C, g.A, g.d);
     ++*g.launches;
+    if (g.A.dike_backlog && g.d.nx > 3) { // magma sub-model: arc extrusion and MOR crust
+        const long long ncol = g.d.nx - 3;
+        if (g.arc_rate > 0) {
+            GF_RLAUNCH(k_arc_cols, ncol, g.P, g.C, g.A, g.d, g.arc_rate);
+            GF_RLAUNCH(k_arc_nodes, (long long)g.d.nx, g.A, g.d);
+        }
+        GF_RLAUNCH(k_mor_cols, ncol, g.P, g.C, g.A, g.d);
+        k_mor_chain<<<1, 32, 0, g.s>>>(g.A, g.d);
+        ++*g.launches;
+    }
     if (resurface) {
         k_resurface<<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d, nloop, max_markers);
         ++*g.launches;
@@ -1052,3 +1097,42 @@ template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface,
 
 template struct GfRemesh<double>;
 template struct GfRemesh<float>;
+
+// ---------------------------------------------------------------- magma sub-model
+namespace {
+void mg_compact(const GfLaunch &g, int mode) {
+    const unsigned nb = (unsigned)((g.d.E + gfr::MG_CB - 1) / gfr::MG_CB);
+    gfr::k_mg_count<<<nb, gfr::MG_CB, 0, g.s>>>(g.A, g.d, mode);
+    gfr::k_mg_write<<<nb, gfr::MG_CB, 0, g.s>>>(g.A, g.d, mode);
+    *g.launches += 2;
+}
+} // namespace
+
+void GfMagma::melting(const GfLaunch &g) {
+    using namespace gfr;
+    GF_RLAUNCH(k_mg_cols, (long long)(g.d.nx - 1), g.A, g.d, 0);
+    GF_RLAUNCH(k_melt_flags, g.d.E, g.P, g.A, g.d);
+    mg_compact(g, MG_PRED_MASK);
+    k_melt_serial<<<1, 1, 0, g.s>>>(g.P, g.A, g.d);
+    ++*g.launches;
+}
+
+void GfMagma::therm(const GfLaunch &g, int max_markers) {
+    using namespace gfr;
+    const GfDims &d = g.d;
+    GF_RLAUNCH(k_mg_freeze, d.E, g.P, g.C, g.A, d);
+    GF_RLAUNCH(k_mg_freeze_nodes, d.N, g.P, g.A, d);
+    mg_compact(g, MG_PRED_W);
+    k_mg_zone1<<<1, 32, 0, g.s>>>(g.P, g.A, d);
+    GF_RLAUNCH(k_mg_find, d.E, g.A, d);
+    k_mg_zone2<<<1, 32, 0, g.s>>>(g.P, g.A, d);
+    *g.launches += 2;
+    GF_RLAUNCH(k_mg_cols, (long long)(d.nx - 1), g.A, d, 1);
+    mg_compact(g, MG_PRED_SRC);
+    GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, g.A, d);
+    GF_RLAUNCH(k_mg_migrate, d.E, g.P, g.A, d);
+    GF_RLAUNCH(k_mg_release, d.E, g.P, g.A, d);
+    mg_compact(g, MG_PRED_MASK);
+    k_mg_markers<<<1, 1, 0, g.s>>>(g.P, g.C, g.A, d, max_markers);
+    ++*g.launches;
+}

@@ -790,11 +790,16 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
             if (L->fmagma) L->fmagma[e] = 0.0;
             if (L->fmagma2) L->fmagma2[e] = 0.0;
             if (L->dike_released) L->dike_released[e] = 0.0;
+            // melt fractions and dike / MOR accumulators (setflac.f90:60-63,
+            // arrays.f90:124-128)
+            for (double *f : {L->fmelt, L->fmelt2, L->dike_backlog, L->dike_marker_vol, L->mor_marker_vol})
+                if (f) f[e] = 0.0;
             if (L->e2sr) L->e2sr[e] = 1e-16;
             if (L->visn) L->visn[e] = 0.0;
         }
         if (L->se2sr)
             for (size_t e = 0; e < 3 * E; ++e) L->se2sr[e] = 1e-16;
+        if (L->extrusion) std::memset(L->extrusion, 0, sizeof(double) * p->nx);
         if (L->amass) std::memset(L->amass, 0, sizeof(double) * N);
         if (L->rmass) std::memset(L->rmass, 0, sizeof(double) * N);
         c->dtavg = 0.0;

@@ -131,6 +131,21 @@ class Model:
     xReyn: float = 5.0
     ifreq: int = 10
     topo_kappa: float = 0.0  # surface diffusion (diff_topo); 0 = off
+    # magma sub-model (read_params.f90:243-255); itype_melting 0 = off
+    itype_melting: int = 0
+    nelem_dike: int = 1
+    prod_magma: float = 2e-15
+    prod_magma2: float = 0.0
+    rho_magma: float = 2700.0
+    angle_mzone: float = 30.0
+    fmagma_max: float = 0.1
+    ratio_mantle_mzone: float = 0.1
+    ratio_crust_mzone: float = 0.1
+    latent_heat_magma: float = 420000.0
+    lambda_freeze: float = 1e-13
+    lambda_freeze_tdep: float = 0.002
+    weaken_ratio_plastic: float = 1.0
+    weaken_ratio_viscous: float = 1.0
     frac: float = 0.45
     fracm: float = 0.5
     demf: float = 0.8
@@ -204,13 +219,15 @@ class Model:
         c("; viscosity limits: v_min, v_max, ivis_shape, efoldc")
         c(f"{_fmt(self.v_min)}, {_fmt(self.v_max)}, 2, 500.0")
         c("; magma: itype_melting, nelem_serp, nelem_dike, prod_magma, prod_magma2, rho_magma")
-        c("0, 2, 1, 2e-15, 0.0, 2700.0")
+        c(f"{self.itype_melting}, 2, {self.nelem_dike}, {_fmt(self.prod_magma)}, {_fmt(self.prod_magma2)}, "
+          f"{_fmt(self.rho_magma)}")
         c("; angle_mzone, fmagma_max, ratio_mantle_mzone, ratio_crust_mzone")
-        c("30.0, 0.1, 0.1, 0.1")
+        c(f"{_fmt(self.angle_mzone)}, {_fmt(self.fmagma_max)}, {_fmt(self.ratio_mantle_mzone)}, "
+          f"{_fmt(self.ratio_crust_mzone)}")
         c("; latent_heat_magma, lambda_freeze, lambda_freeze_tdep")
-        c("420000.0, 1e-13, 0.002")
+        c(f"{_fmt(self.latent_heat_magma)}, {_fmt(self.lambda_freeze)}, {_fmt(self.lambda_freeze_tdep)}")
         c("; weaken_ratio_plastic, weaken_ratio_viscous")
-        c("1.0, 1.0")
+        c(f"{_fmt(self.weaken_ratio_plastic)}, {_fmt(self.weaken_ratio_viscous)}")
         c("; ---- remeshing: ny_rem, mode_rem, ntest_rem, angle_rem")
         c(f"{self.ny_rem}  {self.mode_rem}  {self.ntest_rem}  {_fmt(self.angle_rem)}")
         c("; dx_rem")
@@ -360,9 +377,28 @@ def config3_small() -> Model:
     return config3(60, 15)
 
 
+def magma_arc(nex: int = 60, nez: int = 15) -> Model:
+    """config3 with all 19 phase ids of the reference's special rules, the
+    magma sub-model on (itype_melting 1: melting, dikes, mantle percolation,
+    the MOR pool with eruption) and surface diffusion (which carries the
+    arc-extrusion and MOR-crust blocks).  The melting itself is set up by
+    the caller (temperatures, subducted phases)."""
+    m = config3(nex, nez)
+    m.phases = m.phases + [crust() for _ in range(19 - len(m.phases))]
+    m.phases[13] = crust(den=2800.0)  # 14: arc crust
+    m.phases[15] = mantle()  # 16: hydrated mantle
+    m.phases[17] = mantle()  # 18: dry mantle
+    m.itype_melting = 1
+    m.nelem_dike = 3
+    m.prod_magma = 2e-13
+    m.prod_magma2 = 1e-11
+    m.topo_kappa = 1e-6
+    return m
+
+
 CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config3_small": config3_small,
            "elastic_bar": elastic_bar, "maxwell_column": maxwell_column,
-           "plastic_bar": plastic_bar}
+           "plastic_bar": plastic_bar, "magma_arc": magma_arc}
 
 
 # ---------------------------------------------------------------- ensembles

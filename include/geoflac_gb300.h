@@ -209,6 +209,12 @@ typedef struct gf_layout {
      * zoriginal: (nz, nx) each, arrays.f90:12) and the flexural bottom's
      * state (fl_flexure.f90: q_init, vel_flex_old; nx each) */
     double *xoriginal, *zoriginal, *q_init, *vel_flex_old;
+    /* magma sub-model (itype_melting = 1): the melt fractions of the last
+     * change_phase (change_phase.f90:264-483), the dike-intrusion backlog and
+     * marker-volume accumulators and the MOR marker-volume accumulator
+     * (fl_therm.f90:330-391), (nz-1, nx-1) each; the last arc-extrusion
+     * height per surface element (fl_move.f90:213-237; nx, nx-1 used) */
+    double *fmelt, *fmelt2, *dike_backlog, *dike_marker_vol, *mor_marker_vol, *extrusion;
 } gf_layout;
 
 typedef struct gf_ctx gf_ctx;
@@ -295,9 +301,8 @@ int gf_remesh(gf_ctx *ctx);
  * Files go to directory `dir` (NULL or "" = the working directory, as in
  * the reference) in the reference's binary layouts: gfortran direct-access
  * records (fixed record length, no record markers, native byte order).
- * Fields that this library does not model are written as zeros: fmelt,
- * fmelt2, extrusion (melting) in frames; q_init, vel_flex_old (flexure) and
- * the dike_* records in restart files. */
+ * Every field of the reference's frames and restart files is written from
+ * the model's state (the magma fields stay zero unless itype_melting = 1). */
 
 /* outflac (src/outflac.f90:5-431): one float32 frame of the node, element
  * and surface fields selected by io_flags, appended as record nrec of each

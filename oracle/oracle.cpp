@@ -690,6 +690,23 @@ void fl_node(St &s) {
 
 void count_phase_ratio(St &s, int j, int i);
 int add_marker(St &s, double x, double y, int iph, double age, int j, int i);
+void newphase2marker(St &s, int j1, int j2, int i1, int i2, int iph);
+
+// phase ids with special rules (phases.f90)
+constexpr int K_SED1 = 1, K_OCEAN1 = 3, K_MANT1 = 4, K_SCHIST = 5, K_OCEAN2 = 7, K_MANT2 = 8, K_SERP = 9,
+              K_OCEANDRY = 10, K_SED2 = 11, K_ECLG = 13, K_ARC1 = 14, K_HYDMANT = 16, K_METASED = 17;
+
+// Fortran MIN / MAX of two reals as gfortran evaluates them for ordered values
+inline double fmin2(double a, double b) { return b < a ? b : a; }
+inline double fmax2(double a, double b) { return b > a ? b : a; }
+// ceiling() of a ratio that may be huge, held to +-2^29 (beyond every loop
+// bound it feeds)
+inline int ceil_int(double x) {
+    double c = std::ceil(x);
+    if (!(c < 536870912.0)) return 536870912;
+    if (c < -536870912.0) return -536870912;
+    return (int)c;
+}
 
 // add_marker_at_top (fl_move.f90:429-472): a marker of phase kph at a
 // random point of the top element of column i, in the upper dz_ratio of it;
@@ -717,8 +734,8 @@ void add_marker_at_top(St &s, int i, double dz_ratio, double time, int loop, int
 // resurface (fl_move.f90:320-426), serial over the surface elements: an
 // element whose accumulated erosion exceeds its thickness / markers loses its
 // topmost marker, one whose deposition does gains a sediment marker (phase
-// ksed1 = 1); the arc-extrusion branch needs extr_acc, which stays zero
-// without the magma sub-model
+// ksed1 = 1), one whose accumulated extrusion does gains arc markers
+// (phase kocean1)
 void resurface(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
@@ -767,6 +784,17 @@ void resurface(St &s) {
             L.dhacc[i] = 0.0;
             ichanged = 1;
         }
+        // volcanic extrusion: arc markers (phase kocean1) in the upper
+        // part of the element (fl_move.f90:403-416)
+        double chgtopo2 = L.extr_acc ? L.extr_acc[i] : 0.0;
+        if (chgtopo2 * kinc >= elz && kinc != M) {
+            int n_to_add = std::min(ceil_int(chgtopo2 / elz * kinc), M - kinc);
+            double dz_ratio = fmin2(chgtopo2 / elz, 1.0);
+            for (int ii = 1; ii <= n_to_add; ++ii)
+                add_marker_at_top(s, i, dz_ratio, s.c->time, s.c->nloop + (i + 1) + ii, K_OCEAN1);
+            L.extr_acc[i] = 0;
+            ichanged = 1;
+        }
         if (ichanged == 1) count_phase_ratio(s, 0, i);
     }
 }
@@ -774,8 +802,8 @@ void resurface(St &s) {
 // diff_topo (fl_move.f90:138-315): diffusion of the surface with topo_kappa
 // and the erodibility of the surface phase where it erodes, limited to half
 // the top element's thickness; accumulates dhacc_correction and dhacc;
-// resurface every ifreq_avgsr steps.  The magma blocks (arc extrusion, MOR
-// crust) add zero without melt and are left out.
+// then arc extrusion and MOR crust from the magma pools (zero without melt);
+// resurface every ifreq_avgsr steps.
 void diff_topo(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
@@ -798,6 +826,64 @@ void diff_topo(St &s) {
     for (int i = 0; i < nx; ++i) L.dhacc_correction[i] = L.dhacc_correction[i] + dtopo[i];
     for (int i = 0; i < nx - 1; ++i) L.dhacc[i] = L.dhacc[i] + 0.5 * (dtopo[i] + dtopo[i + 1]);
     for (int i = 0; i < nx; ++i) s.cordr(0, i, 1) = s.cord(0, i, 1) + dtopo[i];
+    const int nz = p.nz;
+    // arc extrusion (fl_move.f90:213-237): the melt of each inner column
+    // erupts as a layer over the column and half its neighbours
+    const double arc_extrusion_rate = 1.0 - p.ratio_mantle_mzone - p.ratio_crust_mzone;
+    if (arc_extrusion_rate > 0 && L.fmelt && L.extrusion) {
+        for (int i = 1; i < nx - 2; ++i) {
+            double totalmelt = 0;
+            for (int j = 0; j < nz - 1; ++j) {
+                long long e = s.e(j, i);
+                double quad_area = 0.5 / s.area(e, 0) + 0.5 / s.area(e, 1);
+                totalmelt = totalmelt + quad_area * L.fmelt[e];
+            }
+            double ext = arc_extrusion_rate * dt * totalmelt * p.prod_magma /
+                         (s.cord(0, i + 1, 0) - s.cord(0, i, 0) +
+                          0.5 * (s.cord(0, i, 0) - s.cord(0, i - 1, 0) + s.cord(0, i + 2, 0) - s.cord(0, i + 1, 0)));
+            L.extrusion[i] = ext;
+            L.extr_acc[i] = L.extr_acc[i] + ext;
+            L.dhacc_correction[i] = L.dhacc_correction[i] + ext;
+            L.dhacc_correction[i + 1] = L.dhacc_correction[i + 1] + ext;
+            L.dhacc[i] = L.dhacc[i] + ext;
+            s.cordr(0, i, 1) = s.cord(0, i, 1) + ext;
+            s.cordr(0, i + 1, 1) = s.cord(0, i + 1, 1) + ext;
+        }
+    }
+    // new oceanic crust from the MOR magma pool fmagma2 (fl_move.f90:243-302)
+    for (int i = 1; i < nx - 2 && L.fmagma2; ++i) {
+        double total_melt = 0;
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            double quad_area = 0.5 / s.area(e, 0) + 0.5 / s.area(e, 1);
+            total_melt = total_melt + quad_area * L.fmagma2[e];
+            double delta = fmin2(L.fmagma2[e], L.fmagma2[e] * p.prod_magma2 * dt);
+            L.fmagma2[e] = L.fmagma2[e] - delta;
+        }
+        double extrusion_height = dt * total_melt * p.prod_magma2 / (s.cord(0, i + 1, 0) - s.cord(0, i, 0));
+        double ele_height = 0, quotient = 0, remainder = 0;
+        int j_oc = 1;
+        for (int j = 0; j < nz - 1; ++j) {
+            ele_height = ele_height + std::fabs(0.5 * (s.cord(j + 1, i + 1, 1) + s.cord(j + 1, i, 1)) -
+                                                0.5 * (s.cord(j, i + 1, 1) + s.cord(j, i, 1)));
+            quotient = extrusion_height / ele_height;
+            remainder = std::fmod(extrusion_height, ele_height);
+            if (quotient >= 0.0 && quotient < 2.0) {
+                j_oc = j + 1;
+                break;
+            }
+        }
+        for (int j = 1; j <= nz - 1; ++j) {
+            int iph = L.iphase[s.e(j - 1, i)];
+            if (iph != K_OCEAN1 && quotient >= 1) {
+                newphase2marker(s, j, std::min(nz - 1, j + j_oc - 1), i + 1, i + 1, K_OCEAN1);
+                break;
+            }
+        }
+        L.extr_acc[i] = L.extr_acc[i] + remainder / 2;
+        s.cordr(0, i, 1) = s.cord(0, i, 1) + remainder / 2;
+        s.cordr(0, i + 1, 1) = s.cord(0, i + 1, 1) + remainder / 2;
+    }
     for (int i = 0; i < nx; ++i) L.dtopo[i] = dtopo[i];
     if (s.c->nloop % p.ifreq_avgsr == 0) resurface(s);
 }
@@ -1128,16 +1214,211 @@ void init_visc(St &s) {
 }
 
 // --------------------------------------------------------------------------
-// fl_therm (src/fl_therm.f90:393-598); the magma sub-model (itype_melting=1,
-// fl_therm.f90:56-391) is not part of this path.
+// fl_therm's magma sub-model (fl_therm.f90:56-391, itype_melting = 1), run
+// after temp0 = temp and before the diffusion: freezing of the magma pools
+// with its latent heat, the centre and widths of the MOR melting zone,
+// migration of the melt (dikes through the crust, percolation through the
+// mantle wedge, the MOR pool), then the rate-capped dike release and new
+// arc / oceanic-crust markers.  Serial order (i outer, j inner) throughout:
+// the reference's atomics and reductions taken in that order.
+
+void therm_magma(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const int nx = p.nx, nz = p.nz, M = GF_MAX_MARKERS_PER_ELEM;
+    const double dt = s.c->dt;
+    auto X = [&](int j, int i) { return s.cord(j, i, 0); };
+    auto Z = [&](int j, int i) { return s.cord(j, i, 1); };
+    auto T = [&](int j, int i) -> double & { return L.temp[gf_node(s.d, j, i)]; };
+    auto T0 = [&](int j, int i) { return L.temp0[gf_node(s.d, j, i)]; };
+    const double tan_mzone = gfm::tan(0.5 * p.angle_mzone * 3.14159265358979323846 / 180.0);
+    const int ihw = ceil_int(tan_mzone * 200e3 / p.dxmin);
+    const double w_barrier = 1.0e-4;
+
+    // freezing: dM = min(M, M dt lambda(T)), latent heat to the 4 corners
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            double cp_eff = p.cp[L.iphase[e] - 1];
+            double tmpr = 0.25 * (T0(j, i) + T0(j + 1, i) + T0(j, i + 1) + T0(j + 1, i + 1));
+            double fr_lambda = p.lambda_freeze * gfm::exp(-p.lambda_freeze_tdep * (tmpr - p.t_top));
+            double d1 = fmin2(L.fmagma[e], L.fmagma[e] * dt * fr_lambda);
+            double d2 = fmin2(L.fmagma2[e], L.fmagma2[e] * dt * fr_lambda);
+            L.fmagma[e] = L.fmagma[e] - d1;
+            L.fmagma2[e] = L.fmagma2[e] - d2;
+            double dT = d1 * p.latent_heat_magma / cp_eff / 4 + d2 * p.latent_heat_magma / cp_eff / 4;
+            T(j, i) = T(j, i) + dT;
+            T(j, i + 1) = T(j, i + 1) + dT;
+            T(j + 1, i) = T(j + 1, i) + dT;
+            T(j + 1, i + 1) = T(j + 1, i + 1) + dT;
+        }
+    for (long long n = 0; n < s.d.N; ++n) L.temp[n] = fmin2(L.temp[n], p.t_bot);
+
+    // MOR melting zone: fmelt2-weighted centre, the element holding it,
+    // then the weighted widths on either side
+    double x_sum = 0, z_sum = 0, w_sum = 0;
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            double w = L.fmelt2[s.e(j, i)];
+            if (w > w_barrier) {
+                x_sum = x_sum + 0.25 * (X(j, i) + X(j, i + 1) + X(j + 1, i) + X(j + 1, i + 1)) * w;
+                z_sum = z_sum + 0.25 * (Z(j, i) + Z(j, i + 1) + Z(j + 1, i) + Z(j + 1, i + 1)) * w;
+                w_sum = w_sum + w;
+            }
+        }
+    bool valid = false;
+    int ic = 0, jc = 0; // 0-based element of the centre
+    double x_center = 0, z_center = 0, z_surf = 0, h2 = 0, tan_l = 0, tan_r = 0;
+    int ihw_l = 0, ihw_r = 0;
+    if (w_sum > 0.0) {
+        x_center = x_sum / w_sum;
+        z_center = z_sum / w_sum;
+        for (int i = 0; i < nx - 1 && !valid; ++i)
+            for (int j = 0; j < nz - 1; ++j)
+                if (X(j, i) <= x_center && X(j, i + 1) >= x_center && Z(j, i) >= z_center && Z(j + 1, i) <= z_center) {
+                    ic = i;
+                    jc = j;
+                    valid = true;
+                    break;
+                }
+    }
+    if (valid) {
+        double xl = 0, xr = 0, wl = 0, wr = 0;
+        for (int i = 0; i < nx - 1; ++i)
+            for (int j = 0; j < nz - 1; ++j) {
+                double w = L.fmelt2[s.e(j, i)];
+                double x = 0.25 * (X(j, i) + X(j, i + 1) + X(j + 1, i) + X(j + 1, i + 1));
+                if (w > w_barrier && x < x_center) {
+                    xl = xl + (x_center - x) * (x_center - x) * w;
+                    wl = wl + w;
+                } else if (w > w_barrier && x > x_center) {
+                    xr = xr + (x - x_center) * (x - x_center) * w;
+                    wr = wr + w;
+                }
+            }
+        xl = 1.8 * std::sqrt(xl / wl);
+        xr = 1.8 * std::sqrt(xr / wr);
+        if (xl < p.dxmin) xl = p.dxmin;
+        if (xr < p.dxmin) xr = p.dxmin;
+        if (xl != xl) xl = p.dxmin;
+        if (xr != xr) xr = p.dxmin;
+        z_surf = 0.5 * (Z(0, ic) + Z(0, ic + 1));
+        h2 = z_surf - z_center;
+        tan_l = xl / h2;
+        tan_r = xr / h2;
+        ihw_l = ceil_int(tan_l * 150e3 / p.dxmin);
+        ihw_r = ceil_int(tan_r * 150e3 / p.dxmin);
+    }
+
+    // migration (1-based column / row numbers as in the reference)
+    std::vector<double> dike_added(s.d.E, 0.0);
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            const int i1 = i + 1, j1 = j + 1, jm = L.jmoho[i];
+            double quad_area = 0.5 / s.area(e, 0) + 0.5 / s.area(e, 1);
+            if (j1 > jm && L.fmelt[e] > 0) {
+                // crust: dikes over nelem_dike columns, from the topmost
+                // non-sediment element down to the Moho
+                double area_ratio = (Z(0, i) + Z(0, i + 1) - Z(jm - 1, i) - Z(jm - 1, i + 1)) /
+                                    (Z(j, i) + Z(j, i + 1) - Z(j + 1, i) - Z(j + 1, i + 1));
+                const int nd = p.nelem_dike;
+                int ihalf = std::max(0, (nd - 1) / 2);
+                int ii_start = std::max(1, i1 - ihalf);
+                int ii_end = std::min(nx - 1, ii_start + std::max(1, nd) - 1);
+                ii_start = std::max(1, ii_end - std::max(1, nd) + 1);
+                int ncol = ii_end - ii_start + 1;
+                for (int ii = ii_start; ii <= ii_end; ++ii) {
+                    int jtop = 1;
+                    while (jtop < L.jmoho[ii - 1] &&
+                           (L.iphase[s.e(jtop - 1, ii - 1)] == K_SED1 || L.iphase[s.e(jtop - 1, ii - 1)] == K_SED2))
+                        ++jtop;
+                    for (int jj = jtop; jj <= L.jmoho[ii - 1]; ++jj) {
+                        long long t = s.e(jj - 1, ii - 1);
+                        L.fmagma[t] = L.fmagma[t] + L.fmelt[e] * p.ratio_crust_mzone * area_ratio * p.prod_magma * dt / ncol;
+                        dike_added[t] = dike_added[t] + L.fmelt[e] * p.ratio_crust_mzone * area_ratio * p.prod_magma * dt / ncol;
+                    }
+                }
+                // mantle: percolation upwards within the cone of half
+                // angle angle_mzone / 2 above the melting element
+                double z_moho = 0.5 * (Z(jm - 1, i) + Z(jm - 1, i + 1));
+                double z_melt = 0.5 * (Z(j + 1, i) + Z(j + 1, i + 1));
+                double x_melt = 0.5 * (X(j + 1, i) + X(j + 1, i + 1));
+                double h = z_moho - z_melt;
+                area_ratio = h * h * tan_mzone / quad_area;
+                for (int ii = std::max(1, i1 - ihw); ii <= std::min(nx - 1, i1 + ihw); ++ii)
+                    for (int jj = L.jmoho[ii - 1] + 1; jj <= j1; ++jj) {
+                        double x = 0.5 * (X(jj - 1, ii - 1) + X(jj - 1, ii));
+                        double z = 0.5 * (Z(jj - 1, ii - 1) + Z(jj - 1, ii));
+                        if (std::fabs(x - x_melt) <= tan_mzone * (z - z_melt)) {
+                            long long t = s.e(jj - 1, ii - 1);
+                            L.fmagma[t] = L.fmagma[t] + L.fmelt[e] * p.ratio_mantle_mzone * area_ratio * p.prod_magma * dt;
+                        }
+                    }
+            }
+            if (L.fmelt2[e] > 0 && valid) {
+                // MOR melt: into the zone above the melting centre
+                double area_ratio = 0.5 * (h2 * h2 * tan_l / quad_area + h2 * h2 * tan_r / quad_area);
+                for (int ii = std::max(1, ic + 1 - ihw_l); ii <= std::min(nx - 1, ic + 1 + ihw_r); ++ii)
+                    for (int jj = 1; jj <= jc + 1; ++jj) {
+                        double x = 0.5 * (X(jj - 1, ii - 1) + X(jj - 1, ii));
+                        double z = 0.5 * (Z(jj - 1, ii - 1) + Z(jj - 1, ii));
+                        long long t = s.e(jj - 1, ii - 1);
+                        if (x < x_center && std::fabs(x_center - x) <= tan_l * (z_surf - z)) {
+                            L.fmagma2[t] = L.fmagma2[t] + L.fmelt2[e] * area_ratio * p.prod_magma2 * dt;
+                            L.mor_marker_vol[t] = L.mor_marker_vol[t] + L.fmelt2[e] * area_ratio * p.prod_magma2 * dt;
+                        }
+                        if (x >= x_center && std::fabs(x - x_center) <= tan_r * (z_surf - z)) {
+                            L.fmagma2[t] = L.fmagma2[t] + L.fmelt2[e] * area_ratio * p.prod_magma2 * dt;
+                            L.mor_marker_vol[t] = L.mor_marker_vol[t] + L.fmelt2[e] * area_ratio * p.prod_magma2 * dt;
+                        }
+                    }
+            }
+            L.fmagma[e] = fmin2(L.fmagma[e], p.fmagma_max);
+            L.fmagma2[e] = fmin2(L.fmagma2[e], p.fmagma_max);
+        }
+
+    // dike release, capped at 1e-4 Amin per step, and new markers at the
+    // element centre once a marker's share of the element has accumulated
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            double elem_area = 0.5 / s.area(e, 0) + 0.5 / s.area(e, 1);
+            double pending = dike_added[e] * elem_area + L.dike_backlog[e];
+            double released = fmin2(pending, 1.0e-4 * p.Amin);
+            L.dike_backlog[e] = pending - released;
+            L.dike_released[e] = released / elem_area;
+            L.dike_marker_vol[e] = L.dike_marker_vol[e] + released;
+            for (int path = 0; path < 2; ++path) {
+                double &vol = path == 0 ? L.dike_marker_vol[e] : L.mor_marker_vol[e];
+                int kinc = L.nmark_elem[e];
+                if (kinc > 0 && kinc < M) {
+                    double unit = elem_area / kinc;
+                    if (vol >= unit) {
+                        int n_to_add = std::min(ceil_int(vol / unit), M - kinc);
+                        double xc = 0.25 * (X(j, i) + X(j + 1, i) + X(j, i + 1) + X(j + 1, i + 1));
+                        double yc = 0.25 * (Z(j, i) + Z(j + 1, i) + Z(j, i + 1) + Z(j + 1, i + 1));
+                        for (int k = 0; k < n_to_add; ++k)
+                            add_marker(s, xc, yc, path == 0 ? K_ARC1 : K_OCEAN1, s.c->time, j, i);
+                        vol = 0.0;
+                        count_phase_ratio(s, j, i);
+                    }
+                }
+            }
+        }
+}
+
+// --------------------------------------------------------------------------
+// fl_therm (src/fl_therm.f90:4-598): temp0 = temp, the magma sub-model when
+// itype_melting = 1, then the explicit diffusion and the boundary values.
 
 void fl_therm(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
     double dt = s.c->dt;
     int nx = p.nx, nz = p.nz;
-    if (p.itype_melting == 1) throw Stop{GF_ERR_UNSUPPORTED};
     std::memcpy(L.temp0, L.temp, sizeof(double) * (size_t)s.d.N);
+    if (p.itype_melting == 1) therm_magma(s);
     std::vector<double> diff(s.d.E), src(s.d.E);
 #pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
     for (int i = 0; i < nx - 1; ++i)
@@ -1346,7 +1627,114 @@ void marker2elem(St &s) {
         }
 }
 
-// change_phase (src/change_phase.f90:35-262); melting (:264+) not on this path.
+// --------------------------------------------------------------------------
+// Melting (change_phase.f90:264-483, itype_melting = 1): hydrous mantle
+// (fmelt2, Katz 2003 solidus), sediments (Nichols 1994), basalt / eclogite
+// (Gutscher 2000) and flux melting above serpentinite or chlorite
+// (Grove 2009 water-saturated solidus) into fmelt.  A melting element's
+// corners are cooled back to the solidus, in place and in serial order, so
+// each element sees its predecessors' cooling.
+
+void melting(St &s) {
+    const gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const int nx = p.nx, nz = p.nz;
+    auto Z = [&](int j, int i) { return s.cord(j, i, 1); };
+    auto T = [&](int j, int i) -> double & { return L.temp[gf_node(s.d, j, i)]; };
+    auto tmpr_of = [&](int j, int i) { return 0.25 * (T(j, i) + T(j, i + 1) + T(j + 1, i) + T(j + 1, i + 1)); };
+    auto depth_of = [&](int j, int i) {
+        double yy = 0.25 * (Z(j, i) + Z(j, i + 1) + Z(j + 1, i) + Z(j + 1, i + 1));
+        return 0.5 * (Z(0, i) + Z(0, i + 1)) - yy;
+    };
+    auto cool = [&](int j, int i, double dt_melt) {
+        T(j, i) = T(j, i) - dt_melt;
+        T(j, i + 1) = T(j, i + 1) - dt_melt;
+        T(j + 1, i) = T(j + 1, i) - dt_melt;
+        T(j + 1, i + 1) = T(j + 1, i + 1) - dt_melt;
+    };
+    auto pmelt_of = [&](int kph, double over, double span) {
+        if (p.latent_heat_magma > 0.0) return fmin2(p.cp[kph - 1] * over / p.latent_heat_magma, 0.1);
+        return fmin2(over / span * 0.1, 0.1);
+    };
+    // hydrous mantle
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            L.fmelt2[e] = 0;
+            double tpr = s.pr(e, K_MANT1) + s.pr(e, K_MANT2);
+            if (tpr > 0.6 && Z(j, i) > -150e3) {
+                double tmpr = tmpr_of(j, i), depth = depth_of(j, i);
+                double press = std::fabs(3000.0 * p.g * depth * 1e-9);
+                double solidus = -5.02 * (press * press) + 1.32e2 * press + 1.09e3;
+                if (tmpr > solidus) {
+                    L.fmelt2[e] = pmelt_of(K_MANT1, tmpr - solidus, 35.0) * tpr;
+                    cool(j, i, tmpr - solidus);
+                }
+            }
+        }
+    // sediments
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            L.fmelt[e] = 0;
+            double tpr = s.pr(e, K_SED1) + s.pr(e, K_SED2) + s.pr(e, K_METASED) + s.pr(e, K_SCHIST);
+            if (tpr > 0.6 && Z(j, i) > -200e3) {
+                double tmpr = tmpr_of(j, i), depth = depth_of(j, i);
+                double solidus = fmax2(680 + 0.6e-3 * (depth - 140e3), 930 - 313 * (1 - gfm::exp(-depth / 7e3)));
+                if (tmpr > solidus) {
+                    L.fmelt[e] = pmelt_of(K_SED2, tmpr - solidus, 50.0) * tpr;
+                    cool(j, i, tmpr - solidus);
+                }
+            }
+        }
+    // basalt and eclogite
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = 0; j < nz - 1; ++j) {
+            long long e = s.e(j, i);
+            double tpr = s.pr(e, K_OCEAN1) + s.pr(e, K_OCEAN2) + s.pr(e, K_OCEANDRY) + s.pr(e, K_ECLG);
+            if (tpr > 0.6 && Z(j, i) > -200e3) {
+                double tmpr = tmpr_of(j, i), depth = depth_of(j, i);
+                double press = 3000 * 10 * depth / 1e9;
+                double solidus;
+                if (press < 1.0)
+                    solidus = 1050.0 - 420.0 * (1.0 - gfm::exp(-press * 3.3));
+                else if (press > 2.7)
+                    solidus = (press + 14.0) * 43.0;
+                else
+                    solidus = 630.0 + 13.0 * (press * press);
+                if (tmpr > solidus) {
+                    L.fmelt[e] = L.fmelt[e] + pmelt_of(K_OCEAN1, tmpr - solidus, 20.0) * tpr;
+                    cool(j, i, tmpr - solidus);
+                }
+            }
+        }
+    // flux melting: above the deepest serpentinite / chlorite element of
+    // each column
+    for (int i = 0; i < nx - 1; ++i)
+        for (int j = nz - 2; j >= 0; --j) {
+            long long e = s.e(j, i);
+            if (s.pr(e, K_SERP) + s.pr(e, K_HYDMANT) > 0.6 && Z(j, i) > -200e3) {
+                for (int jj = j; jj >= 0; --jj) {
+                    long long t = s.e(jj, i);
+                    double tmpr = tmpr_of(jj, i), depth = depth_of(jj, i);
+                    double solidus;
+                    if (depth > 80e3)
+                        solidus = 800;
+                    else
+                        solidus = 800 + (double)6.2e-8f * ((depth - 80e3) * (depth - 80e3));
+                    if (tmpr > solidus) {
+                        L.fmelt[t] = L.fmelt[t] + pmelt_of(K_MANT1, tmpr - solidus, 50.0) *
+                                                      (s.pr(t, K_MANT1) + s.pr(t, K_MANT2) + s.pr(t, K_SERP));
+                        cool(jj, i, tmpr - solidus);
+                    }
+                }
+                break;
+            }
+        }
+}
+
+// change_phase (src/change_phase.f90:35-262), then melting when
+// itype_melting = 1.
 void change_phase(St &s) {
     const gf_params &p = *s.p;
     gf_layout &L = *s.L;
@@ -1468,6 +1856,7 @@ void change_phase(St &s) {
             L.aps[e] = std::max(a0 - a0 / (double)(float)kinc, 0.0);
         }
     if (err) throw Stop{err};
+    if (p.itype_melting == 1) melting(s);
 }
 
 // --------------------------------------------------------------------------
@@ -1981,6 +2370,8 @@ void remesh(St &s) {
     rem_interpolate(r, L.aps);
     for (size_t e = 0; e < E; ++e)
         if (L.aps[e] < 0.0) L.aps[e] = 0.0;
+    if (p.itype_melting == 1) // remesh.f90:106-115
+        for (double *f : {L.fmagma, L.fmagma2, L.dike_backlog, L.dike_marker_vol, L.mor_marker_vol}) rem_interpolate(r, f);
     // material entering through the side walls (remesh.f90:129-194)
     const int idist = 2;
     int ju = 1, jl = 1;
