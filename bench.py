@@ -285,7 +285,7 @@ def run_ours(args):
 
     d = tempfile.mkdtemp(prefix="gfbench")
     inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
-    if args.profile in ("fno", "batch"):
+    if args.profile in ("fno", "batch", "magma"):
         profile_extra(args, d)
         return
     if args.profile:
@@ -536,6 +536,8 @@ def profile_extra(args, workdir: str):
     import numpy as np
     import torch
 
+    if args.profile == "magma":
+        return profile_magma(args, workdir)
     if args.profile == "batch":
         from geoflac_gb300.batch import Batch, ensemble
 
@@ -564,6 +566,71 @@ def profile_extra(args, workdir: str):
         net.adam(lr=1e-4)
     torch.cuda.synchronize()
     print(json.dumps({"profile": "fno", "steps": args.warmup + args.steps, "loss": loss.item()}))
+
+
+def _seed_melting(p, s):
+    """Melting set-up of the arc model, by fractions of the mesh: a hot
+    mantle column (MOR melt), subducted basalt / sediment below the Moho
+    (arc melt), serpentinite under hot mantle (flux melting)."""
+    import numpy as np
+
+    nz1, nx1 = p.nz - 1, p.nx - 1
+    r = lambda f: int(round(f * nz1))
+    c = lambda f: int(round(f * nx1))
+    T = s["temp"]
+    T[r(2 / 15):r(5 / 15), c(8 / 60):c(17 / 60)] = 1500.0
+    ids, nm, ph = s["mark_id_elem"], s["nmark_elem"], s["mark_phase"]
+    touched = []
+    for i in range(c(34 / 60), c(38 / 60)):
+        for j in range(r(3 / 15), r(5 / 15)):
+            ph[ids[:nm[j, i], j, i] - 1] = 3 if i % 2 else 11
+            touched.append((j, i))
+    T[r(3 / 15):r(6 / 15), c(34 / 60):c(39 / 60)] = 1100.0
+    j0, i0 = r(6 / 15), c(45 / 60)
+    ph[ids[:nm[j0, i0], j0, i0] - 1] = 9
+    touched.append((j0, i0))
+    T[r(3 / 15):r(7 / 15), i0:i0 + 2] = 1000.0
+    for j, i in touched:  # count_phase_ratio of the changed elements
+        cnt = np.bincount(ph[ids[:nm[j, i], j, i] - 1], minlength=p.nphase + 1)[1:p.nphase + 1]
+        s["phase_ratio"][:, j, i] = cnt / nm[j, i]
+        s["iphase"][j, i] = int(np.argmax(cnt)) + 1
+
+
+def profile_magma(args, workdir: str):
+    """The magma sub-model's cost: FP64 steps of the 600x150 arc model with
+    melting seeded, itype_melting 1 against the same model with 0."""
+    import torch
+
+    from geoflac_gb300 import clone, inpgen, new_state
+    from geoflac_gb300.flac import Flac
+
+    m = inpgen.magma_arc(600, 150)
+    # production rates of the reference's defaults: the test model's faster
+    # MOR eruption lifts 2 km surface elements past their neighbours
+    m.prod_magma, m.prod_magma2 = 2e-15, 1e-13
+    p, c, s = new_state(m.write(os.path.join(workdir, "magma_arc.inp")))
+    _seed_melting(p, s)
+    p0, c0, s0 = clone(p, c, s)
+    p0.itype_melting = 0
+    out = {"profile": "magma", "model": "magma_arc 600x150 (config3 with 19 phases, itype_melting 1, "
+                                        "prod_magma 2e-15, prod_magma2 1e-13)",
+           "elements": (p.nx - 1) * (p.nz - 1), "steps": args.steps}
+    for tag, (pp, cc, ss) in (("plain", (p0, c0, s0)), ("magma", (p, c, s))):
+        g = Flac(pp, cc, ss, "fp64")
+        g.step(args.warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.step(args.steps)
+        g.status()
+        torch.cuda.synchronize()
+        out[f"ms_per_step_{tag}"] = (time.perf_counter() - t0) * 1e3 / args.steps
+        st = g.download()
+        out[f"melting_elements_{tag}"] = int(((st["fmelt"] > 0) | (st["fmelt2"] > 0)).sum())
+        out[f"magma_elements_{tag}"] = int(((st["fmagma"] > 0) | (st["fmagma2"] > 0)).sum())
+        out[f"markers_{tag}"] = int(g.clock.nmarkers)
+        g.close()
+    out["overhead"] = out["ms_per_step_magma"] / out["ms_per_step_plain"]
+    print(json.dumps(out))
 
 
 def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
@@ -634,7 +701,7 @@ def main():
     ap.add_argument("--sur-lr", type=float, default=2e-3)
     ap.add_argument("--fno-batch", type=int, default=64, help="batch of the fno profiling run")
     ap.add_argument("--only", choices=["surrogate"], default=None, help="run one leg only (development)")
-    ap.add_argument("--profile", choices=["fp64", "mixed", "batch", "fno"], default=None,
+    ap.add_argument("--profile", choices=["fp64", "mixed", "batch", "fno", "magma"], default=None,
                     help="run warmup+steps steps of one mode and nothing else (for ncu)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

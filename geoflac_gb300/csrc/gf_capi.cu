@@ -713,11 +713,13 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &A.extrusion, p->nx));
         A_(dalloc(c, &A.mg_e, E));
         A_(dalloc(c, &A.mg_src, (size_t)GF_MG_SRC_W * E));
+        A_(dalloc(c, &A.mg_src2, (size_t)GF_MG_SRC_W * E));
+        A_(dalloc(c, &A.mg_list2, E));
         A_(dalloc(c, &A.mg_s, 16));
         A_(dalloc(c, &A.mg_c, p->nx));
         A_(dalloc(c, &A.mg_list, E));
         A_(dalloc(c, &A.mg_blk, E / 1024 + 2));
-        A_(dalloc(c, &A.mg_i, 16));
+        A_(dalloc(c, &A.mg_i, 32));
         A_(dalloc(c, &A.mg_col, 2 * p->nx));
         A_(dalloc(c, &A.mg_mask, E));
     }

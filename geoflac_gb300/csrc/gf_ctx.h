@@ -101,16 +101,16 @@ struct DevArrays {
     int *nmarkers;                                    // device marker count
     // magma sub-model (allocated when itype_melting = 1): melt fractions,
     // dike / MOR accumulators (E each), the last arc extrusion (nx), and
-    // scratch: per-element values (E), per-source terms (GF_MG_SRC_W x E),
-    // zone scalars, per-column values (nx), ordered element lists (E) with
-    // their block counts, element masks (E)
+    // scratch: per-element values (E), per-source / per-candidate records
+    // (GF_MG_SRC_W x E, two lists), zone scalars, per-column values (nx),
+    // ordered element lists (E, two) with their block counts, element masks (E)
     double *fmelt, *fmelt2, *dike_added, *dike_backlog, *dike_marker_vol, *mor_marker_vol, *extrusion;
-    double *mg_e, *mg_src, *mg_s, *mg_c;
-    int *mg_list, *mg_blk, *mg_i, *mg_col;
+    double *mg_e, *mg_src, *mg_src2, *mg_s, *mg_c;
+    int *mg_list, *mg_list2, *mg_blk, *mg_i, *mg_col;
     uint8_t *mg_mask;
 };
 
-#define GF_MG_SRC_W 12 // doubles per migration source
+#define GF_MG_SRC_W 16 // doubles per migration source / melting candidate
 
 struct GfLaunch {
     const DevParams *P;

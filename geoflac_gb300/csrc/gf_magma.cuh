@@ -29,9 +29,13 @@ constexpr int MG_CB = 1024; // elements per block of the ordered compaction
 
 // zone scalars (mg_s) and integer slots (mg_i)
 enum { MS_VALID = 0, MS_XC, MS_ZC, MS_ZSURF, MS_H2, MS_TANL, MS_TANR, MS_TANM, MS_WSUM };
-enum { MI_COUNT = 0, MI_FOUND, MI_IC, MI_JC, MI_IHWL, MI_IHWR, MI_IHW };
+enum { MI_COUNT = 0, MI_FOUND, MI_IC, MI_JC, MI_IHWL, MI_IHWR, MI_IHW, MI_COUNT2, MI_MAXJ };
 // per-source terms (mg_src, GF_MG_SRC_W doubles per source)
 enum { SR_E = 0, SR_FLAGS, SR_TERM_C, SR_II0, SR_II1, SR_TERM_M, SR_XMELT, SR_ZMELT, SR_J1, SR_I1, SR_TERM_R };
+// per-candidate record of the melting walk (mg_src): element, loop mask,
+// corner nodes (j,i), (j,i+1), (j+1,i), (j+1,i+1), then the phase sum and
+// solidus of each loop (mantle, sediments, basalt, flux)
+enum { MR_E = 0, MR_MASK, MR_N00, MR_N01, MR_N10, MR_N11, MR_TPR };
 
 // (j, i) of element e = i (nz-1) + j and of node n = i nz + j
 __device__ __forceinline__ void mg_eji(const GfDims &d, long long e, int &j, int &i) {
@@ -112,16 +116,16 @@ __device__ __forceinline__ double tpr_basalt(const DevArrays &A, const GfDims &d
 
 // ---------------------------------------------------------------- ordered compaction
 // Which elements a list holds.
-enum { MG_PRED_MASK = 0, MG_PRED_W = 1, MG_PRED_SRC = 2 };
+enum { MG_PRED_MASK = 0, MG_PRED_W = 1, MG_PRED_SRC = 2, MG_PRED_ARC = 3 };
 __device__ __forceinline__ bool mg_pred(int mode, const DevArrays &A, const GfDims &d, long long e) {
     if (mode == MG_PRED_MASK) return A.mg_mask[e] != 0;
     if (mode == MG_PRED_W) return A.fmelt2[e] > MG_W_BARRIER;
-    // migration sources: melting below the column's Moho, or MOR melt with
-    // a valid melting zone
+    // migration sources: melting below the column's Moho (dikes and the
+    // mantle cone: ARC), or also MOR melt with a valid melting zone (SRC)
     int j, i;
     mg_eji(d, e, j, i);
     if (j + 1 > A.jmoho[i] && A.fmelt[e] > 0) return true;
-    return A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0;
+    return mode == MG_PRED_SRC && A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0;
 }
 // block b counts its MG_CB elements
 __global__ void __launch_bounds__(MG_CB) k_mg_count(DevArrays A, GfDims d, int mode) {
@@ -131,8 +135,8 @@ __global__ void __launch_bounds__(MG_CB) k_mg_count(DevArrays A, GfDims d, int m
     if (threadIdx.x == 0) A.mg_blk[blockIdx.x] = c;
 }
 // block b writes its elements after those of blocks 0..b-1; the last block
-// stores the total in mg_i[MI_COUNT]
-__global__ void __launch_bounds__(MG_CB) k_mg_write(DevArrays A, GfDims d, int mode) {
+// stores the total in *count
+__global__ void __launch_bounds__(MG_CB) k_mg_write(DevArrays A, GfDims d, int mode, int *list, int *count) {
     __shared__ int red[32];
     __shared__ int wsum[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -151,11 +155,11 @@ __global__ void __launch_bounds__(MG_CB) k_mg_write(DevArrays A, GfDims d, int m
     int off = base;
     for (int k = 0; k < w; ++k) off += wsum[k];
     off += __popc(bal & ((1u << lane) - 1u));
-    if (v) A.mg_list[off] = (int)e;
+    if (v) list[off] = (int)e;
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
         int tot = base;
         for (int k = 0; k < MG_CB / 32; ++k) tot += wsum[k];
-        A.mg_i[MI_COUNT] = tot;
+        *count = tot;
     }
 }
 
@@ -209,62 +213,80 @@ __global__ void __launch_bounds__(GF_THREADS) k_melt_flags(const DevParams *__re
     A.mg_mask[e] = (uint8_t)m;
 }
 
+// the static part of each listed candidate: corner nodes, and per loop the
+// phase sum and the solidus (depth and phases do not change while melting)
+__global__ void __launch_bounds__(GF_THREADS) k_melt_prep(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.mg_i[MI_COUNT]) return;
+    const DevParams &P = *Pp;
+    const long long e = A.mg_list[k];
+    int j, i;
+    mg_eji(d, e, j, i);
+    double *r = A.mg_src + (long long)k * GF_MG_SRC_W;
+    const double depth = mg_depth(A, d, j, i);
+    r[MR_E] = (double)e;
+    r[MR_MASK] = A.mg_mask[e];
+    r[MR_N00] = (double)gf_node(d, j, i);
+    r[MR_N01] = (double)gf_node(d, j, i + 1);
+    r[MR_N10] = (double)gf_node(d, j + 1, i);
+    r[MR_N11] = (double)gf_node(d, j + 1, i + 1);
+    r[MR_TPR + 0] = tpr_mantle(A, d, e);
+    r[MR_TPR + 1] = sol_mantle(P, depth);
+    r[MR_TPR + 2] = tpr_sed(A, d, e);
+    r[MR_TPR + 3] = sol_sed(depth);
+    r[MR_TPR + 4] = tpr_basalt(A, d, e);
+    r[MR_TPR + 5] = sol_basalt(depth);
+    r[MR_TPR + 6] = mg_pr(A, d, e, MG_MANT1) + mg_pr(A, d, e, MG_MANT2) + mg_pr(A, d, e, MG_SERP);
+    r[MR_TPR + 7] = sol_wet(depth);
+}
+
+// one candidate of melting loop `loop`: the element's mean temperature from
+// the current corner values, melt and cooling when above the solidus
+__device__ __forceinline__ void melt_one(const DevParams &P, double *__restrict__ T, double *__restrict__ fmelt,
+                                         double *__restrict__ fmelt2, const double *__restrict__ r, int loop) {
+    const long long n00 = (long long)r[MR_N00], n01 = (long long)r[MR_N01], n10 = (long long)r[MR_N10],
+                    n11 = (long long)r[MR_N11];
+    const double tmpr = 0.25 * (T[n00] + T[n01] + T[n10] + T[n11]);
+    const double sol = r[MR_TPR + 2 * loop + 1];
+    if (!(tmpr > sol)) return;
+    const long long e = (long long)r[MR_E];
+    const double over = tmpr - sol;
+    if (loop == 0) {
+        fmelt2[e] = mg_pmelt(P, MG_MANT1, over, 35.0) * r[MR_TPR];
+    } else if (loop == 1) {
+        fmelt[e] = mg_pmelt(P, MG_SED2, over, 50.0) * r[MR_TPR + 2];
+    } else if (loop == 2) {
+        fmelt[e] = fmelt[e] + mg_pmelt(P, MG_OCEAN1, over, 20.0) * r[MR_TPR + 4];
+    } else {
+        fmelt[e] = fmelt[e] + mg_pmelt(P, MG_MANT1, over, 50.0) * r[MR_TPR + 6];
+    }
+    T[n00] = T[n00] - over;
+    T[n01] = T[n01] - over;
+    T[n10] = T[n10] - over;
+    T[n11] = T[n11] - over;
+}
+
 // the four melting loops over the listed elements, in the reference's order
 __global__ void k_melt_serial(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const DevParams &P = *Pp;
     const int n = A.mg_i[MI_COUNT];
-    const int *list = A.mg_list;
-    int j, i;
-    for (int k = 0; k < n; ++k) { // hydrous mantle
-        const long long e = list[k];
-        if (!(A.mg_mask[e] & 1u)) continue;
-        mg_eji(d, e, j, i);
-        const double tpr = tpr_mantle(A, d, e), tmpr = mg_tmpr(A, d, j, i);
-        const double sol = sol_mantle(P, mg_depth(A, d, j, i));
-        if (tmpr > sol) {
-            A.fmelt2[e] = mg_pmelt(P, MG_MANT1, tmpr - sol, 35.0) * tpr;
-            mg_cool(A, d, j, i, tmpr - sol);
+    const double *__restrict__ rec = A.mg_src;
+    double *__restrict__ T = A.temp;
+    for (int loop = 0; loop < 3; ++loop) // hydrous mantle, sediments, basalt / eclogite
+        for (int k = 0; k < n; ++k) {
+            const double *r = rec + (long long)k * GF_MG_SRC_W;
+            if ((unsigned)r[MR_MASK] & (1u << loop)) melt_one(P, T, A.fmelt, A.fmelt2, r, loop);
         }
-    }
-    for (int k = 0; k < n; ++k) { // sediments
-        const long long e = list[k];
-        if (!(A.mg_mask[e] & 2u)) continue;
-        mg_eji(d, e, j, i);
-        const double tpr = tpr_sed(A, d, e), tmpr = mg_tmpr(A, d, j, i);
-        const double sol = sol_sed(mg_depth(A, d, j, i));
-        if (tmpr > sol) {
-            A.fmelt[e] = mg_pmelt(P, MG_SED2, tmpr - sol, 50.0) * tpr;
-            mg_cool(A, d, j, i, tmpr - sol);
-        }
-    }
-    for (int k = 0; k < n; ++k) { // basalt and eclogite
-        const long long e = list[k];
-        if (!(A.mg_mask[e] & 4u)) continue;
-        mg_eji(d, e, j, i);
-        const double tpr = tpr_basalt(A, d, e), tmpr = mg_tmpr(A, d, j, i);
-        const double sol = sol_basalt(mg_depth(A, d, j, i));
-        if (tmpr > sol) {
-            A.fmelt[e] = A.fmelt[e] + mg_pmelt(P, MG_OCEAN1, tmpr - sol, 20.0) * tpr;
-            mg_cool(A, d, j, i, tmpr - sol);
-        }
-    }
     // flux melting: columns in order, each upwards from its start row (the
     // list holds a column's elements contiguously, top to bottom)
     for (int k = 0; k < n;) {
-        const int col = (int)(list[k] / (d.nz - 1));
+        const long long col = (long long)rec[(long long)k * GF_MG_SRC_W + MR_E] / (d.nz - 1);
         int kend = k;
-        while (kend < n && (int)(list[kend] / (d.nz - 1)) == col) ++kend;
+        while (kend < n && (long long)rec[(long long)kend * GF_MG_SRC_W + MR_E] / (d.nz - 1) == col) ++kend;
         for (int kk = kend - 1; kk >= k; --kk) {
-            const long long e = list[kk];
-            if (!(A.mg_mask[e] & 8u)) continue;
-            mg_eji(d, e, j, i);
-            const double tmpr = mg_tmpr(A, d, j, i), sol = sol_wet(mg_depth(A, d, j, i));
-            if (tmpr > sol) {
-                A.fmelt[e] = A.fmelt[e] + mg_pmelt(P, MG_MANT1, tmpr - sol, 50.0) *
-                                              (mg_pr(A, d, e, MG_MANT1) + mg_pr(A, d, e, MG_MANT2) + mg_pr(A, d, e, MG_SERP));
-                mg_cool(A, d, j, i, tmpr - sol);
-            }
+            const double *r = rec + (long long)kk * GF_MG_SRC_W;
+            if ((unsigned)r[MR_MASK] & 8u) melt_one(P, T, A.fmelt, A.fmelt2, r, 3);
         }
         k = kend;
     }
@@ -318,38 +340,43 @@ __device__ __forceinline__ double mg_cz(const double *c, const GfDims &d, int j,
     return 0.25 * (CY(c, d, j, i) + CY(c, d, j, i + 1) + CY(c, d, j + 1, i) + CY(c, d, j + 1, i + 1));
 }
 
-// fmelt2-weighted centre of the MOR melting zone (one warp: terms in
-// parallel, sums in serial order); also the mantle cone's tan and width
-__global__ void k_mg_zone1(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
+// fmelt2-weighted centre of the MOR melting zone (one CTA: terms in
+// parallel into shared memory, sums by one thread in serial order); also
+// the mantle cone's tan and width
+__global__ void __launch_bounds__(MG_CB) k_mg_zone1(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    __shared__ double sx[MG_CB], sz[MG_CB], sw[MG_CB];
     const DevParams &P = *Pp;
     const int n = A.mg_i[MI_COUNT];
     double xs = 0, zs = 0, ws = 0;
-    for (int base = 0; base < n; base += 32) {
-        double tx = 0, tz = 0, tw = 0;
-        if (base + lane < n) {
-            const long long e = A.mg_list[base + lane];
+    for (int base = 0; base < n; base += MG_CB) {
+        if (base + (int)threadIdx.x < n) {
+            const long long e = A.mg_list[base + threadIdx.x];
             int j, i;
             mg_eji(d, e, j, i);
-            tw = A.fmelt2[e];
-            tx = mg_cx(A.cord, d, j, i) * tw;
-            tz = mg_cz(A.cord, d, j, i) * tw;
+            const double w = A.fmelt2[e];
+            sx[threadIdx.x] = mg_cx(A.cord, d, j, i) * w;
+            sz[threadIdx.x] = mg_cz(A.cord, d, j, i) * w;
+            sw[threadIdx.x] = w;
         }
-        const int m = n - base < 32 ? n - base : 32;
-        for (int k = 0; k < m; ++k) {
-            xs = xs + __shfl_sync(0xffffffffu, tx, k);
-            zs = zs + __shfl_sync(0xffffffffu, tz, k);
-            ws = ws + __shfl_sync(0xffffffffu, tw, k);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int m = n - base < MG_CB ? n - base : MG_CB;
+            for (int k = 0; k < m; ++k) {
+                xs = xs + sx[k];
+                zs = zs + sz[k];
+                ws = ws + sw[k];
+            }
         }
+        __syncthreads();
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         const double tan_m = gfm::tan(0.5 * P.angle_mzone * 3.14159265358979323846 / 180.0);
         A.mg_s[MS_TANM] = tan_m;
         A.mg_i[MI_IHW] = mg_ceil(tan_m * 200e3 / P.dxmin);
         A.mg_s[MS_WSUM] = ws;
         A.mg_s[MS_VALID] = 0.0;
         A.mg_i[MI_FOUND] = 0x7fffffff;
+        A.mg_i[MI_MAXJ] = 0;
         if (ws > 0.0) {
             A.mg_s[MS_XC] = xs / ws;
             A.mg_s[MS_ZC] = zs / ws;
@@ -367,41 +394,42 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_find(DevArrays A, GfDims d) {
     if (CX(c, d, j, i) <= xc && CX(c, d, j, i + 1) >= xc && CY(c, d, j, i) >= zc && CY(c, d, j + 1, i) <= zc)
         atomicMin(&A.mg_i[MI_FOUND], (int)e);
 }
-// widths on either side of the centre and the zone's cone (one warp)
-__global__ void k_mg_zone2(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+// widths on either side of the centre and the zone's cone (one CTA as above)
+__global__ void __launch_bounds__(MG_CB) k_mg_zone2(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    __shared__ double sx[MG_CB], sw[MG_CB], sl[MG_CB], sr[MG_CB];
     const int found = A.mg_i[MI_FOUND];
     if (found == 0x7fffffff) return;
-    const int lane = threadIdx.x;
     const DevParams &P = *Pp;
     const int n = A.mg_i[MI_COUNT];
     const double xc = A.mg_s[MS_XC];
     double xl = 0, xr = 0, wl = 0, wr = 0;
-    for (int base = 0; base < n; base += 32) {
-        double tl = 0, tr = 0, w = 0, x = 0;
-        if (base + lane < n) {
-            const long long e = A.mg_list[base + lane];
+    for (int base = 0; base < n; base += MG_CB) {
+        if (base + (int)threadIdx.x < n) {
+            const long long e = A.mg_list[base + threadIdx.x];
             int j, i;
             mg_eji(d, e, j, i);
-            w = A.fmelt2[e];
-            x = mg_cx(A.cord, d, j, i);
-            tl = (xc - x) * (xc - x) * w;
-            tr = (x - xc) * (x - xc) * w;
+            const double w = A.fmelt2[e], x = mg_cx(A.cord, d, j, i);
+            sx[threadIdx.x] = x;
+            sw[threadIdx.x] = w;
+            sl[threadIdx.x] = (xc - x) * (xc - x) * w;
+            sr[threadIdx.x] = (x - xc) * (x - xc) * w;
         }
-        const int m = n - base < 32 ? n - base : 32;
-        for (int k = 0; k < m; ++k) {
-            const double xk = __shfl_sync(0xffffffffu, x, k), wk = __shfl_sync(0xffffffffu, w, k);
-            const double lk = __shfl_sync(0xffffffffu, tl, k), rk = __shfl_sync(0xffffffffu, tr, k);
-            if (xk < xc) {
-                xl = xl + lk;
-                wl = wl + wk;
-            } else if (xk > xc) {
-                xr = xr + rk;
-                wr = wr + wk;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int m = n - base < MG_CB ? n - base : MG_CB;
+            for (int k = 0; k < m; ++k) {
+                if (sx[k] < xc) {
+                    xl = xl + sl[k];
+                    wl = wl + sw[k];
+                } else if (sx[k] > xc) {
+                    xr = xr + sr[k];
+                    wr = wr + sw[k];
+                }
             }
         }
+        __syncthreads();
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         int jc, ic;
         mg_eji(d, found, jc, ic);
         xl = 1.8 * sqrt(xl / wl);
@@ -427,12 +455,12 @@ __global__ void k_mg_zone2(const DevParams *__restrict__ Pp, DevArrays A, GfDims
 
 // the terms each listed migration source adds
 __global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
-                                                       GfDims d) {
+                                                       GfDims d, const int *list, const int *count, double *out) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= A.mg_i[MI_COUNT]) return;
+    if (k >= *count) return;
     const DevParams &P = *Pp;
     const double dt = C->dt;
-    const long long e = A.mg_list[k];
+    const long long e = list[k];
     int j, i;
     mg_eji(d, e, j, i);
     const int nx = d.nx, i1 = i + 1, j1 = j + 1;
@@ -440,13 +468,14 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restri
     const double *c = A.cord;
     const double area0 = ((const double *)A.area)[gf_ek(d, e, 0)], area1 = ((const double *)A.area)[gf_ek(d, e, 1)];
     const double quad_area = 0.5 / area0 + 0.5 / area1;
-    double *s = A.mg_src + (long long)k * GF_MG_SRC_W;
+    double *s = out + (long long)k * GF_MG_SRC_W;
     unsigned flags = 0;
     s[SR_E] = (double)e;
     s[SR_J1] = j1;
     s[SR_I1] = i1;
     if (j1 > jm && A.fmelt[e] > 0) {
         flags |= 1u;
+        atomicMax(&A.mg_i[MI_MAXJ], j1);
         const double fm = A.fmelt[e];
         double area_ratio = (CY(c, d, 0, i) + CY(c, d, 0, i + 1) - CY(c, d, jm - 1, i) - CY(c, d, jm - 1, i + 1)) /
                             (CY(c, d, j, i) + CY(c, d, j, i + 1) - CY(c, d, j + 1, i) - CY(c, d, j + 1, i + 1));
@@ -505,7 +534,6 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
     const double z = 0.5 * (CY(c, d, jt, it) + CY(c, d, jt, it + 1));
     const int jm_t = A.jmoho[it], jtop_t = A.mg_col[nx + it];
     const bool crust_row = jt1 >= jtop_t && jt1 <= jm_t;
-    const int n = A.mg_i[MI_COUNT];
     const int ihw = A.mg_i[MI_IHW];
     const double tan_m = A.mg_s[MS_TANM];
     // the MOR zone above the melting centre
@@ -521,22 +549,32 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
         tl = A.mg_s[MS_TANL];
         tr = A.mg_s[MS_TANR];
     }
-    // sources whose dikes or mantle cone can reach this column: columns
-    // within max(nelem_dike, cone half width) (every source when the
-    // element is in the MOR zone)
-    int k0 = 0, k1 = n;
+    // an element in the MOR zone walks every source; any other only the
+    // dike / mantle-cone sources in columns within max(nelem_dike, cone
+    // half width), and none when it lies below its Moho and below every
+    // such source
+    const int *list = A.mg_list;
+    const double *src = A.mg_src;
+    int k0 = 0, k1 = A.mg_i[MI_COUNT];
     if (!mor) {
+        list = A.mg_list2;
+        src = A.mg_src2;
+        const int n = A.mg_i[MI_COUNT2];
         const int reach = (P.nelem_dike > ihw ? P.nelem_dike : ihw) + 1;
         const long long clo = it - reach < 0 ? 0 : it - reach;
         const long long chi = it + reach + 1 > nx - 1 ? nx - 1 : it + reach + 1;
-        k0 = mg_lower(A.mg_list, n, clo * (nz - 1));
-        k1 = mg_lower(A.mg_list, n, chi * (nz - 1));
+        if (jt1 > jm_t && jt1 > A.mg_i[MI_MAXJ]) {
+            k0 = k1 = 0;
+        } else {
+            k0 = mg_lower(list, n, clo * (nz - 1));
+            k1 = mg_lower(list, n, chi * (nz - 1));
+        }
     }
     const double fmax = P.fmagma_max;
     double f = A.fmagma[t], f2 = A.fmagma2[t], da = 0.0, mv = A.mor_marker_vol[t];
     bool clamped = false;
     for (int k = k0; k < k1; ++k) {
-        const double *s = A.mg_src + (long long)k * GF_MG_SRC_W;
+        const double *s = src + (long long)k * GF_MG_SRC_W;
         const long long es = (long long)s[SR_E];
         if (!clamped && es > t) {
             f = mg_min(f, fmax);
@@ -639,19 +677,32 @@ __global__ void k_mg_markers(const DevParams *__restrict__ Pp, DevClock *C, DevA
 }
 
 // ---------------------------------------------------------------- diff_topo's magma blocks
-// arc extrusion of each inner column (fl_move.f90:213-237)
+// the area-weighted column sum of f (rows in order): one warp, each lane
+// one row of every 32, every lane adding the same terms in row order
+__device__ __forceinline__ double mg_col_sum(const DevArrays &A, const GfDims &d, int i, const double *f, int lane) {
+    const double *area = (const double *)A.area;
+    double tot = 0;
+    for (int j0 = 0; j0 < d.nz - 1; j0 += 32) {
+        const int j = j0 + lane;
+        double term = 0;
+        if (j < d.nz - 1) {
+            const long long e = gf_elem(d, j, i);
+            const double quad_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
+            term = quad_area * f[e];
+        }
+        const int m = d.nz - 1 - j0 < 32 ? d.nz - 1 - j0 : 32;
+        for (int k = 0; k < m; ++k) tot = tot + __shfl_sync(0xffffffffu, term, k);
+    }
+    return tot;
+}
+// arc extrusion of each inner column (fl_move.f90:213-237), one warp per column
 __global__ void __launch_bounds__(GF_THREADS) k_arc_cols(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
                                                          GfDims d, double rate) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1, lane = threadIdx.x & 31;
     if (i >= d.nx - 2) return;
     const DevParams &P = *Pp;
-    const double *area = (const double *)A.area;
-    double totalmelt = 0;
-    for (int j = 0; j < d.nz - 1; ++j) {
-        const long long e = gf_elem(d, j, i);
-        const double quad_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
-        totalmelt = totalmelt + quad_area * A.fmelt[e];
-    }
+    const double totalmelt = mg_col_sum(A, d, i, A.fmelt, lane);
+    if (lane != 0) return;
     const double *c = A.cord;
     const double ext = rate * C->dt * totalmelt * P.prod_magma /
                        (CX(c, d, 0, i + 1) - CX(c, d, 0, i) +
@@ -679,23 +730,21 @@ __global__ void k_arc_nodes(DevArrays A, GfDims d) {
     A.cord[nz_] = z;
 }
 // the MOR pool of each inner column: its volume, the erupted fraction
-// taken from the pool, and the height it would form (fl_move.f90:247-264)
+// taken from the pool, and the height it would form (fl_move.f90:247-264);
+// one warp per column
 __global__ void __launch_bounds__(GF_THREADS) k_mor_cols(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A,
                                                          GfDims d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) + 1, lane = threadIdx.x & 31;
     if (i >= d.nx - 2) return;
     const DevParams &P = *Pp;
     const double dt = C->dt;
-    const double *area = (const double *)A.area;
-    double total_melt = 0;
-    for (int j = 0; j < d.nz - 1; ++j) {
+    const double total_melt = mg_col_sum(A, d, i, A.fmagma2, lane);
+    for (int j = lane; j < d.nz - 1; j += 32) {
         const long long e = gf_elem(d, j, i);
-        const double quad_area = 0.5 / area[gf_ek(d, e, 0)] + 0.5 / area[gf_ek(d, e, 1)];
         const double f2 = A.fmagma2[e];
-        total_melt = total_melt + quad_area * f2;
         A.fmagma2[e] = f2 - mg_min(f2, f2 * P.prod_magma2 * dt);
     }
-    A.mg_c[i] = dt * total_melt * P.prod_magma2 / (CX(A.cord, d, 0, i + 1) - CX(A.cord, d, 0, i));
+    if (lane == 0) A.mg_c[i] = dt * total_melt * P.prod_magma2 / (CX(A.cord, d, 0, i + 1) - CX(A.cord, d, 0, i));
 }
 // newphase2marker (remesh.f90:495-520) on rows j1..j2, columns i1..i2 (1-based)
 __device__ void mg_newphase(DevArrays &A, const GfDims &d, int j1, int j2, int i1, int i2, int iph) {
@@ -711,43 +760,67 @@ __device__ void mg_newphase(DevArrays &A, const GfDims &d, int j1, int j2, int i
             if (off < total) A.phase_ratio[off] = 1.0;
         }
 }
-// the columns with MOR magma in serial order (one warp finds them, its first
-// lane walks them): rows of new oceanic crust, and the remainder onto the
-// column's two surface nodes, which the next column reads
+// the columns with MOR magma in serial order: one warp loads 32 columns'
+// erupted heights and surface / second-row heights, its first lane walks the
+// active ones, converting rows to oceanic crust (newphase2marker) when the
+// erupted height reaches an element's, and adding the remainder to the
+// column's two surface nodes; the left node of the next column is the one
+// this column just raised
 __global__ void k_mor_chain(DevArrays A, GfDims d) {
+    __shared__ double s_eh[32], s_z0[32], s_z0n[32], s_z1[32], s_z1n[32], s_ea[32];
     if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     const int lane = threadIdx.x, nx = d.nx, nz = d.nz;
     double *c = A.cord;
+    const long long N = d.N;
+    int last = -1;       // the last column processed
+    double last_z = 0.0; // its right surface node's new height
     for (int base = 1; base < nx - 2; base += 32) {
         const int ii = base + lane;
-        const bool act = ii < nx - 2 && A.mg_c[ii] != 0.0;
-        unsigned bal = __ballot_sync(0xffffffffu, act);
+        const bool in = ii < nx - 2;
+        const double eh = in ? A.mg_c[ii] : 0.0;
+        if (in) {
+            s_eh[lane] = eh;
+            s_z0[lane] = CY(c, d, 0, ii);
+            s_z0n[lane] = CY(c, d, 0, ii + 1);
+            s_z1[lane] = CY(c, d, 1, ii);
+            s_z1n[lane] = CY(c, d, 1, ii + 1);
+            s_ea[lane] = A.extr_acc[ii];
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, in && eh != 0.0);
+        __syncwarp();
         if (lane == 0)
             while (bal) {
-                const int i = base + __ffs(bal) - 1;
+                const int l = __ffs(bal) - 1, i = base + l;
                 bal &= bal - 1;
-                const double eh = A.mg_c[i];
-                double ele_height = 0, quotient = 0, remainder = 0;
+                const double h = s_eh[l];
+                const double z0 = (last == i - 1) ? last_z : s_z0[l], z0n = s_z0n[l];
+                double ele_height = fabs(0.5 * (s_z1n[l] + s_z1[l]) - 0.5 * (z0n + z0));
+                double quotient = h / ele_height, remainder = fmod(h, ele_height);
                 int j_oc = 1;
-                for (int j = 0; j < nz - 1; ++j) {
-                    ele_height = ele_height + fabs(0.5 * (CY(c, d, j + 1, i + 1) + CY(c, d, j + 1, i)) -
-                                                   0.5 * (CY(c, d, j, i + 1) + CY(c, d, j, i)));
-                    quotient = eh / ele_height;
-                    remainder = fmod(eh, ele_height);
-                    if (quotient >= 0.0 && quotient < 2.0) {
-                        j_oc = j + 1;
-                        break;
+                if (!(quotient >= 0.0 && quotient < 2.0)) {
+                    for (int j = 1; j < nz - 1; ++j) {
+                        ele_height = ele_height + fabs(0.5 * (CY(c, d, j + 1, i + 1) + CY(c, d, j + 1, i)) -
+                                                       0.5 * (CY(c, d, j, i + 1) + CY(c, d, j, i)));
+                        quotient = h / ele_height;
+                        remainder = fmod(h, ele_height);
+                        if (quotient >= 0.0 && quotient < 2.0) {
+                            j_oc = j + 1;
+                            break;
+                        }
                     }
                 }
-                for (int j = 1; j <= nz - 1; ++j)
-                    if (A.iphase[gf_elem(d, j - 1, i)] != MG_OCEAN1 && quotient >= 1) {
-                        const int j2 = j + j_oc - 1 < nz - 1 ? j + j_oc - 1 : nz - 1;
-                        mg_newphase(A, d, j, j2, i + 1, i + 1, MG_OCEAN1);
-                        break;
-                    }
-                A.extr_acc[i] = A.extr_acc[i] + remainder / 2;
-                c[d.N + gf_node(d, 0, i)] = c[d.N + gf_node(d, 0, i)] + remainder / 2;
-                c[d.N + gf_node(d, 0, i + 1)] = c[d.N + gf_node(d, 0, i + 1)] + remainder / 2;
+                if (quotient >= 1)
+                    for (int j = 1; j <= nz - 1; ++j)
+                        if (A.iphase[gf_elem(d, j - 1, i)] != MG_OCEAN1) {
+                            const int j2 = j + j_oc - 1 < nz - 1 ? j + j_oc - 1 : nz - 1;
+                            mg_newphase(A, d, j, j2, i + 1, i + 1, MG_OCEAN1);
+                            break;
+                        }
+                A.extr_acc[i] = s_ea[l] + remainder / 2;
+                c[N + gf_node(d, 0, i)] = z0 + remainder / 2;
+                last_z = z0n + remainder / 2;
+                c[N + gf_node(d, 0, i + 1)] = last_z;
+                last = i;
             }
         __syncwarp();
     }

@@ -1082,10 +1082,10 @@ template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface,
     if (g.A.dike_backlog && g.d.nx > 3) { // magma sub-model: arc extrusion and MOR crust
         const long long ncol = g.d.nx - 3;
         if (g.arc_rate > 0) {
-            GF_RLAUNCH(k_arc_cols, ncol, g.P, g.C, g.A, g.d, g.arc_rate);
+            GF_RLAUNCH(k_arc_cols, 32 * ncol, g.P, g.C, g.A, g.d, g.arc_rate); // one warp per column
             GF_RLAUNCH(k_arc_nodes, (long long)g.d.nx, g.A, g.d);
         }
-        GF_RLAUNCH(k_mor_cols, ncol, g.P, g.C, g.A, g.d);
+        GF_RLAUNCH(k_mor_cols, 32 * ncol, g.P, g.C, g.A, g.d);
         k_mor_chain<<<1, 32, 0, g.s>>>(g.A, g.d);
         ++*g.launches;
     }
@@ -1100,39 +1100,46 @@ template struct GfRemesh<float>;
 
 // ---------------------------------------------------------------- magma sub-model
 namespace {
-void mg_compact(const GfLaunch &g, int mode) {
+// the elements of `mode` in serial order into list, their number into *count
+void mg_compact(const GfLaunch &g, int mode, int *list, int *count) {
     const unsigned nb = (unsigned)((g.d.E + gfr::MG_CB - 1) / gfr::MG_CB);
     gfr::k_mg_count<<<nb, gfr::MG_CB, 0, g.s>>>(g.A, g.d, mode);
-    gfr::k_mg_write<<<nb, gfr::MG_CB, 0, g.s>>>(g.A, g.d, mode);
+    gfr::k_mg_write<<<nb, gfr::MG_CB, 0, g.s>>>(g.A, g.d, mode, list, count);
     *g.launches += 2;
 }
 } // namespace
 
 void GfMagma::melting(const GfLaunch &g) {
     using namespace gfr;
-    GF_RLAUNCH(k_mg_cols, (long long)(g.d.nx - 1), g.A, g.d, 0);
-    GF_RLAUNCH(k_melt_flags, g.d.E, g.P, g.A, g.d);
-    mg_compact(g, MG_PRED_MASK);
-    k_melt_serial<<<1, 1, 0, g.s>>>(g.P, g.A, g.d);
+    const DevArrays &A = g.A;
+    GF_RLAUNCH(k_mg_cols, (long long)(g.d.nx - 1), A, g.d, 0);
+    GF_RLAUNCH(k_melt_flags, g.d.E, g.P, A, g.d);
+    mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
+    GF_RLAUNCH(k_melt_prep, g.d.E, g.P, A, g.d);
+    k_melt_serial<<<1, 1, 0, g.s>>>(g.P, A, g.d);
     ++*g.launches;
 }
 
 void GfMagma::therm(const GfLaunch &g, int max_markers) {
     using namespace gfr;
     const GfDims &d = g.d;
-    GF_RLAUNCH(k_mg_freeze, d.E, g.P, g.C, g.A, d);
-    GF_RLAUNCH(k_mg_freeze_nodes, d.N, g.P, g.A, d);
-    mg_compact(g, MG_PRED_W);
-    k_mg_zone1<<<1, 32, 0, g.s>>>(g.P, g.A, d);
-    GF_RLAUNCH(k_mg_find, d.E, g.A, d);
-    k_mg_zone2<<<1, 32, 0, g.s>>>(g.P, g.A, d);
+    const DevArrays &A = g.A;
+    GF_RLAUNCH(k_mg_freeze, d.E, g.P, g.C, A, d);
+    GF_RLAUNCH(k_mg_freeze_nodes, d.N, g.P, A, d);
+    mg_compact(g, MG_PRED_W, A.mg_list, A.mg_i + MI_COUNT);
+    k_mg_zone1<<<1, MG_CB, 0, g.s>>>(g.P, A, d);
+    GF_RLAUNCH(k_mg_find, d.E, A, d);
+    k_mg_zone2<<<1, MG_CB, 0, g.s>>>(g.P, A, d);
     *g.launches += 2;
-    GF_RLAUNCH(k_mg_cols, (long long)(d.nx - 1), g.A, d, 1);
-    mg_compact(g, MG_PRED_SRC);
-    GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, g.A, d);
-    GF_RLAUNCH(k_mg_migrate, d.E, g.P, g.A, d);
-    GF_RLAUNCH(k_mg_release, d.E, g.P, g.A, d);
-    mg_compact(g, MG_PRED_MASK);
-    k_mg_markers<<<1, 1, 0, g.s>>>(g.P, g.C, g.A, d, max_markers);
+    GF_RLAUNCH(k_mg_cols, (long long)(d.nx - 1), A, d, 1);
+    // every source (for the MOR zone) and the dike / mantle-cone sources
+    mg_compact(g, MG_PRED_SRC, A.mg_list, A.mg_i + MI_COUNT);
+    GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list, (const int *)(A.mg_i + MI_COUNT), A.mg_src);
+    mg_compact(g, MG_PRED_ARC, A.mg_list2, A.mg_i + MI_COUNT2);
+    GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list2, (const int *)(A.mg_i + MI_COUNT2), A.mg_src2);
+    GF_RLAUNCH(k_mg_migrate, d.E, g.P, A, d);
+    GF_RLAUNCH(k_mg_release, d.E, g.P, A, d);
+    mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
+    k_mg_markers<<<1, 1, 0, g.s>>>(g.P, g.C, A, d, max_markers);
     ++*g.launches;
 }
