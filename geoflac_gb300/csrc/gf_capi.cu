@@ -516,11 +516,8 @@ unsigned step_signature(const gf_ctx *c) {
         if (c->nsrate == p.ifreq_avgsr) sig |= 8u << 8;
         else if (c->nsrate == -1) sig |= 4u << 8;
         if (c->nloop % p.ifreq_imasses == 0) sig |= 32u;
-        // resurface: its random seeds use nloop, so such steps run uncaptured;
-        // so do all steps of the magma sub-model, whose fl_therm may add
-        // markers
+        // resurface: its random seeds use nloop, so such steps run uncaptured
         if (p.movegrid != 0 && p.topo_kappa > 0.0 && c->nloop % p.ifreq_avgsr == 0) sig |= 64u;
-        if (p.itype_melting == 1) sig |= 64u;
     }
     return sig;
 }
@@ -715,6 +712,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &A.mg_src, (size_t)GF_MG_SRC_W * E));
         A_(dalloc(c, &A.mg_src2, (size_t)GF_MG_SRC_W * E));
         A_(dalloc(c, &A.mg_list2, E));
+        A_(dalloc(c, &A.mg_order, 5 * E));
         A_(dalloc(c, &A.mg_s, 16));
         A_(dalloc(c, &A.mg_c, p->nx));
         A_(dalloc(c, &A.mg_list, E));
@@ -949,9 +947,12 @@ int gf_finish_setflac(gf_ctx *c) {
 int gf_flac(gf_ctx *c) {
     if (!c) return GF_ERR_ARG;
     unsigned sig = step_signature(c);
-    if (sig & 64u) GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
+    // the magma sub-model's fl_therm may add markers: the host count is
+    // re-read after every call, so that it is current for the next one
+    const bool resync = (sig & 64u) || (c->mode == GF_MODE_FP64 && c->p.itype_melting == 1);
+    if (resync) GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
     enqueue_step(c, sig);
-    if (sig & 64u) {
+    if (resync) {
         int rc = sync_markers_after_resurface(c);
         if (rc) return rc;
     }
@@ -1059,8 +1060,19 @@ static int sync_markers_after_resurface(gf_ctx *c) {
 
 int gf_step(gf_ctx *c, int nsteps) {
     if (!c || nsteps < 0) return GF_ERR_ARG;
+    // The magma sub-model's fl_therm may add markers on any step (device
+    // count).  Its steps are graph-replayed too; the host copy of the count
+    // is brought up to date before a step that uses it (change_phase's
+    // launch, a resurface step) and at the end.
+    const bool magma = c->mode == GF_MODE_FP64 && c->p.itype_melting == 1;
+    if (magma) // the host count is current between calls
+        GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
     for (int k = 0; k < nsteps; ++k) {
         unsigned sig = step_signature(c);
+        if (magma && (sig & (2u | 64u))) {
+            int rc = sync_markers_after_resurface(c);
+            if (rc) return rc;
+        }
         if (sig & 64u) { // resurface: uncaptured (its seeds use nloop)
             GF_CK(cudaMemcpyAsync(c->A.nmarkers, &c->nmarkers, sizeof(int), cudaMemcpyHostToDevice, c->s));
             enqueue_step(c, sig);
@@ -1071,6 +1083,10 @@ int gf_step(gf_ctx *c, int nsteps) {
             if (rc) return rc;
         }
         advance_host(c, sig);
+    }
+    if (magma) {
+        int rc = sync_markers_after_resurface(c);
+        if (rc) return rc;
     }
     return take_status(c);
 }

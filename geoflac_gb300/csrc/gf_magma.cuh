@@ -29,9 +29,13 @@ constexpr int MG_CB = 1024; // elements per block of the ordered compaction
 
 // zone scalars (mg_s) and integer slots (mg_i)
 enum { MS_VALID = 0, MS_XC, MS_ZC, MS_ZSURF, MS_H2, MS_TANL, MS_TANR, MS_TANM, MS_WSUM };
-enum { MI_COUNT = 0, MI_FOUND, MI_IC, MI_JC, MI_IHWL, MI_IHWR, MI_IHW, MI_COUNT2, MI_MAXJ };
+enum { MI_COUNT = 0, MI_FOUND, MI_IC, MI_JC, MI_IHWL, MI_IHWR, MI_IHW, MI_COUNT2, MI_MAXJ, MI_P0 };
 // per-source terms (mg_src, GF_MG_SRC_W doubles per source)
 enum { SR_E = 0, SR_FLAGS, SR_TERM_C, SR_II0, SR_II1, SR_TERM_M, SR_XMELT, SR_ZMELT, SR_J1, SR_I1, SR_TERM_R };
+// Integer entries of the records are stored bit for bit (mg_pack / mg_int):
+// a conversion from double would run on the FP64 pipe in every inner loop.
+__device__ __forceinline__ double mg_pack(long long v) { return __longlong_as_double(v); }
+__device__ __forceinline__ long long mg_int(double v) { return __double_as_longlong(v); }
 // per-candidate record of the melting walk (mg_src): element, loop mask,
 // corner nodes (j,i), (j,i+1), (j+1,i), (j+1,i+1), then the phase sum and
 // solidus of each loop (mantle, sediments, basalt, flux)
@@ -224,12 +228,12 @@ __global__ void __launch_bounds__(GF_THREADS) k_melt_prep(const DevParams *__res
     mg_eji(d, e, j, i);
     double *r = A.mg_src + (long long)k * GF_MG_SRC_W;
     const double depth = mg_depth(A, d, j, i);
-    r[MR_E] = (double)e;
-    r[MR_MASK] = A.mg_mask[e];
-    r[MR_N00] = (double)gf_node(d, j, i);
-    r[MR_N01] = (double)gf_node(d, j, i + 1);
-    r[MR_N10] = (double)gf_node(d, j + 1, i);
-    r[MR_N11] = (double)gf_node(d, j + 1, i + 1);
+    r[MR_E] = mg_pack(e);
+    r[MR_MASK] = mg_pack(A.mg_mask[e]);
+    r[MR_N00] = mg_pack(gf_node(d, j, i));
+    r[MR_N01] = mg_pack(gf_node(d, j, i + 1));
+    r[MR_N10] = mg_pack(gf_node(d, j + 1, i));
+    r[MR_N11] = mg_pack(gf_node(d, j + 1, i + 1));
     r[MR_TPR + 0] = tpr_mantle(A, d, e);
     r[MR_TPR + 1] = sol_mantle(P, depth);
     r[MR_TPR + 2] = tpr_sed(A, d, e);
@@ -240,56 +244,132 @@ __global__ void __launch_bounds__(GF_THREADS) k_melt_prep(const DevParams *__res
     r[MR_TPR + 7] = sol_wet(depth);
 }
 
-// one candidate of melting loop `loop`: the element's mean temperature from
-// the current corner values, melt and cooling when above the solidus
-__device__ __forceinline__ void melt_one(const DevParams &P, double *__restrict__ T, double *__restrict__ fmelt,
-                                         double *__restrict__ fmelt2, const double *__restrict__ r, int loop) {
-    const long long n00 = (long long)r[MR_N00], n01 = (long long)r[MR_N01], n10 = (long long)r[MR_N10],
-                    n11 = (long long)r[MR_N11];
-    const double tmpr = 0.25 * (T[n00] + T[n01] + T[n10] + T[n11]);
-    const double sol = r[MR_TPR + 2 * loop + 1];
-    if (!(tmpr > sol)) return;
-    const long long e = (long long)r[MR_E];
-    const double over = tmpr - sol;
-    if (loop == 0) {
-        fmelt2[e] = mg_pmelt(P, MG_MANT1, over, 35.0) * r[MR_TPR];
-    } else if (loop == 1) {
-        fmelt[e] = mg_pmelt(P, MG_SED2, over, 50.0) * r[MR_TPR + 2];
-    } else if (loop == 2) {
-        fmelt[e] = fmelt[e] + mg_pmelt(P, MG_OCEAN1, over, 20.0) * r[MR_TPR + 4];
-    } else {
-        fmelt[e] = fmelt[e] + mg_pmelt(P, MG_MANT1, over, 50.0) * r[MR_TPR + 6];
+// each melting loop's candidates in processing order (one CTA): positions
+// in the candidate list with the loop's bit, in list order; the flux loop
+// then column by column, each column's run reversed (upwards).  Slot
+// loop * E of mg_order, the flux order at 4 E; counts in mg_i[MI_P0 + loop].
+__global__ void __launch_bounds__(MG_CB) k_melt_order(DevArrays A, GfDims d) {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    const int n = A.mg_i[MI_COUNT];
+    const double *rec = A.mg_src;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int loop = 0; loop < 4; ++loop) {
+        int *out = A.mg_order + (long long)loop * d.E;
+        if (threadIdx.x == 0) carry = 0;
+        __syncthreads();
+        for (int base = 0; base < n; base += MG_CB) {
+            const int k = base + threadIdx.x;
+            const bool v = k < n && (mg_int(rec[(long long)k * GF_MG_SRC_W + MR_MASK]) & (1LL << loop));
+            const unsigned bal = __ballot_sync(0xffffffffu, v);
+            if (lane == 0) wsum[w] = __popc(bal);
+            __syncthreads();
+            int off = carry;
+            for (int q = 0; q < w; ++q) off += wsum[q];
+            off += __popc(bal & ((1u << lane) - 1u));
+            if (v) out[off] = k;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int t = 0;
+                for (int q = 0; q < MG_CB / 32; ++q) t += wsum[q];
+                carry += t;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) A.mg_i[MI_P0 + loop] = carry;
+        __syncthreads();
     }
-    T[n00] = T[n00] - over;
-    T[n01] = T[n01] - over;
-    T[n10] = T[n10] - over;
-    T[n11] = T[n11] - over;
+    const int n3 = A.mg_i[MI_P0 + 3];
+    const int *o3 = A.mg_order + 3 * d.E;
+    int *o4 = A.mg_order + 4 * d.E;
+    const long long nz1 = d.nz - 1;
+    auto elem = [&](int p) { return mg_int(rec[(long long)o3[p] * GF_MG_SRC_W + MR_E]); };
+    for (int p = threadIdx.x; p < n3; p += MG_CB) {
+        const long long col = elem(p) / nz1;
+        int lo = 0, hi = n3; // first entry of the column
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (elem(mid) < col * nz1) lo = mid + 1;
+            else hi = mid;
+        }
+        const int gs = lo;
+        hi = n3; // first entry past the column
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (elem(mid) < (col + 1) * nz1) lo = mid + 1;
+            else hi = mid;
+        }
+        o4[gs + (lo - 1 - p)] = o3[p];
+    }
 }
 
-// the four melting loops over the listed elements, in the reference's order
+// melting loop `loop` over its candidates in processing order, one thread:
+// the next candidate's corner temperatures are loaded while the current one
+// is processed, then patched where the current one cooled a shared corner
+__device__ void melt_walk(const DevParams &P, double *__restrict__ T, double *__restrict__ fmelt,
+                          double *__restrict__ fmelt2, const double *__restrict__ rec, const int *__restrict__ order,
+                          int cnt, int loop) {
+    if (cnt <= 0) return;
+    const double *r = rec + (long long)order[0] * GF_MG_SRC_W;
+    long long n[4], m[4];
+    double t[4], u[4];
+    for (int q = 0; q < 4; ++q) {
+        n[q] = mg_int(r[MR_N00 + q]);
+        t[q] = T[n[q]];
+    }
+    long long e = mg_int(r[MR_E]);
+    double fm = (loop >= 2) ? fmelt[e] : 0.0;
+    for (int k = 0; k < cnt; ++k) {
+        const double *rn = r;
+        long long en = 0;
+        double fmn = 0.0;
+        if (k + 1 < cnt) {
+            rn = rec + (long long)order[k + 1] * GF_MG_SRC_W;
+            for (int q = 0; q < 4; ++q) {
+                m[q] = mg_int(rn[MR_N00 + q]);
+                u[q] = T[m[q]];
+            }
+            en = mg_int(rn[MR_E]);
+            if (loop >= 2) fmn = fmelt[en];
+        }
+        const double tmpr = 0.25 * (t[0] + t[1] + t[2] + t[3]);
+        const double sol = r[MR_TPR + 2 * loop + 1];
+        if (tmpr > sol) {
+            const double over = tmpr - sol;
+            if (loop == 0) {
+                fmelt2[e] = mg_pmelt(P, MG_MANT1, over, 35.0) * r[MR_TPR];
+            } else if (loop == 1) {
+                fmelt[e] = mg_pmelt(P, MG_SED2, over, 50.0) * r[MR_TPR + 2];
+            } else if (loop == 2) {
+                fmelt[e] = fm + mg_pmelt(P, MG_OCEAN1, over, 20.0) * r[MR_TPR + 4];
+            } else {
+                fmelt[e] = fm + mg_pmelt(P, MG_MANT1, over, 50.0) * r[MR_TPR + 6];
+            }
+            for (int q = 0; q < 4; ++q) {
+                t[q] = t[q] - over;
+                T[n[q]] = t[q];
+            }
+            if (k + 1 < cnt)
+                for (int q = 0; q < 4; ++q)
+                    for (int c = 0; c < 4; ++c)
+                        if (m[q] == n[c]) u[q] = t[c];
+        }
+        r = rn;
+        e = en;
+        fm = fmn;
+        for (int q = 0; q < 4; ++q) {
+            n[q] = m[q];
+            t[q] = u[q];
+        }
+    }
+}
+
+// the four melting loops, in the reference's order
 __global__ void k_melt_serial(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const DevParams &P = *Pp;
-    const int n = A.mg_i[MI_COUNT];
-    const double *__restrict__ rec = A.mg_src;
-    double *__restrict__ T = A.temp;
-    for (int loop = 0; loop < 3; ++loop) // hydrous mantle, sediments, basalt / eclogite
-        for (int k = 0; k < n; ++k) {
-            const double *r = rec + (long long)k * GF_MG_SRC_W;
-            if ((unsigned)r[MR_MASK] & (1u << loop)) melt_one(P, T, A.fmelt, A.fmelt2, r, loop);
-        }
-    // flux melting: columns in order, each upwards from its start row (the
-    // list holds a column's elements contiguously, top to bottom)
-    for (int k = 0; k < n;) {
-        const long long col = (long long)rec[(long long)k * GF_MG_SRC_W + MR_E] / (d.nz - 1);
-        int kend = k;
-        while (kend < n && (long long)rec[(long long)kend * GF_MG_SRC_W + MR_E] / (d.nz - 1) == col) ++kend;
-        for (int kk = kend - 1; kk >= k; --kk) {
-            const double *r = rec + (long long)kk * GF_MG_SRC_W;
-            if ((unsigned)r[MR_MASK] & 8u) melt_one(P, T, A.fmelt, A.fmelt2, r, 3);
-        }
-        k = kend;
-    }
+    for (int loop = 0; loop < 4; ++loop)
+        melt_walk(*Pp, A.temp, A.fmelt, A.fmelt2, A.mg_src, A.mg_order + (long long)(loop == 3 ? 4 : loop) * d.E,
+                  A.mg_i[MI_P0 + loop], loop);
 }
 
 // ---------------------------------------------------------------- fl_therm's magma part
@@ -470,9 +550,9 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restri
     const double quad_area = 0.5 / area0 + 0.5 / area1;
     double *s = out + (long long)k * GF_MG_SRC_W;
     unsigned flags = 0;
-    s[SR_E] = (double)e;
-    s[SR_J1] = j1;
-    s[SR_I1] = i1;
+    s[SR_E] = mg_pack(e);
+    s[SR_J1] = mg_pack(j1);
+    s[SR_I1] = mg_pack(i1);
     if (j1 > jm && A.fmelt[e] > 0) {
         flags |= 1u;
         atomicMax(&A.mg_i[MI_MAXJ], j1);
@@ -486,8 +566,8 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restri
         ii_start = ii_end - nd1 + 1 > 1 ? ii_end - nd1 + 1 : 1;
         const int ncol = ii_end - ii_start + 1;
         s[SR_TERM_C] = fm * P.ratio_crust_mzone * area_ratio * P.prod_magma * dt / ncol;
-        s[SR_II0] = ii_start;
-        s[SR_II1] = ii_end;
+        s[SR_II0] = mg_pack(ii_start);
+        s[SR_II1] = mg_pack(ii_end);
         const double z_moho = 0.5 * (CY(c, d, jm - 1, i) + CY(c, d, jm - 1, i + 1));
         const double z_melt = 0.5 * (CY(c, d, j + 1, i) + CY(c, d, j + 1, i + 1));
         const double x_melt = 0.5 * (CX(c, d, j + 1, i) + CX(c, d, j + 1, i + 1));
@@ -504,7 +584,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_src(const DevParams *__restri
             0.5 * (h2 * h2 * A.mg_s[MS_TANL] / quad_area + h2 * h2 * A.mg_s[MS_TANR] / quad_area);
         s[SR_TERM_R] = A.fmelt2[e] * area_ratio * P.prod_magma2 * dt;
     }
-    s[SR_FLAGS] = flags;
+    s[SR_FLAGS] = mg_pack(flags);
 }
 
 // first position of the ordered source list whose element is >= e
@@ -537,17 +617,17 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
     const int ihw = A.mg_i[MI_IHW];
     const double tan_m = A.mg_s[MS_TANM];
     // the MOR zone above the melting centre
-    bool mor = false;
-    double xc = 0, z_surf = 0, tl = 0, tr = 0;
+    bool mor = false, mor_l = false, mor_r = false;
     if (A.mg_s[MS_VALID] != 0.0) {
         const int ic1 = A.mg_i[MI_IC] + 1, jc1 = A.mg_i[MI_JC] + 1;
         const int lo = ic1 - A.mg_i[MI_IHWL] > 1 ? ic1 - A.mg_i[MI_IHWL] : 1;
         const int hi = ic1 + A.mg_i[MI_IHWR] < nx - 1 ? ic1 + A.mg_i[MI_IHWR] : nx - 1;
         mor = it1 >= lo && it1 <= hi && jt1 <= jc1;
-        xc = A.mg_s[MS_XC];
-        z_surf = A.mg_s[MS_ZSURF];
-        tl = A.mg_s[MS_TANL];
-        tr = A.mg_s[MS_TANR];
+        // which side of the zone's cone the element lies in (the same for
+        // every source)
+        const double xc = A.mg_s[MS_XC], z_surf = A.mg_s[MS_ZSURF];
+        mor_l = mor && x < xc && fabs(xc - x) <= A.mg_s[MS_TANL] * (z_surf - z);
+        mor_r = mor && x >= xc && fabs(x - xc) <= A.mg_s[MS_TANR] * (z_surf - z);
     }
     // an element in the MOR zone walks every source; any other only the
     // dike / mantle-cone sources in columns within max(nelem_dike, cone
@@ -575,33 +655,27 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
     bool clamped = false;
     for (int k = k0; k < k1; ++k) {
         const double *s = src + (long long)k * GF_MG_SRC_W;
-        const long long es = (long long)s[SR_E];
+        const long long es = mg_int(s[SR_E]);
         if (!clamped && es > t) {
             f = mg_min(f, fmax);
             f2 = mg_min(f2, fmax);
             clamped = true;
         }
-        const unsigned flags = (unsigned)s[SR_FLAGS];
-        if (flags & 1u) {
-            if (crust_row && it1 >= (int)s[SR_II0] && it1 <= (int)s[SR_II1]) {
+        const long long flags = mg_int(s[SR_FLAGS]);
+        if (flags & 1) {
+            if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) {
                 f = f + s[SR_TERM_C];
                 da = da + s[SR_TERM_C];
             }
-            const int i1s = (int)s[SR_I1];
+            const int i1s = (int)mg_int(s[SR_I1]);
             const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
-            if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= (int)s[SR_J1] &&
+            if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= mg_int(s[SR_J1]) &&
                 fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
                 f = f + s[SR_TERM_M];
         }
-        if ((flags & 2u) && mor) {
-            if (x < xc && fabs(xc - x) <= tl * (z_surf - z)) {
-                f2 = f2 + s[SR_TERM_R];
-                mv = mv + s[SR_TERM_R];
-            }
-            if (x >= xc && fabs(x - xc) <= tr * (z_surf - z)) {
-                f2 = f2 + s[SR_TERM_R];
-                mv = mv + s[SR_TERM_R];
-            }
+        if ((flags & 2) && (mor_l || mor_r)) {
+            f2 = f2 + s[SR_TERM_R];
+            mv = mv + s[SR_TERM_R];
         }
         if (es == t) {
             f = mg_min(f, fmax);

@@ -1116,8 +1116,9 @@ void GfMagma::melting(const GfLaunch &g) {
     GF_RLAUNCH(k_melt_flags, g.d.E, g.P, A, g.d);
     mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
     GF_RLAUNCH(k_melt_prep, g.d.E, g.P, A, g.d);
+    k_melt_order<<<1, MG_CB, 0, g.s>>>(A, g.d);
     k_melt_serial<<<1, 1, 0, g.s>>>(g.P, A, g.d);
-    ++*g.launches;
+    *g.launches += 2;
 }
 
 void GfMagma::therm(const GfLaunch &g, int max_markers) {
