@@ -439,17 +439,23 @@ __global__ void __launch_bounds__(MG_CB) k_mg_zone1(const DevParams *__restrict_
             sw[threadIdx.x] = w;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            const int m = n - base < MG_CB ? n - base : MG_CB;
-            for (int k = 0; k < m; ++k) {
-                xs = xs + sx[k];
-                zs = zs + sz[k];
-                ws = ws + sw[k];
-            }
-        }
+        // the three sums by the first lanes of warps 0-2 (on different SM
+        // sub-partitions, whose FP64 pipes then run side by side)
+        const int m = n - base < MG_CB ? n - base : MG_CB;
+        if (threadIdx.x == 0)
+            for (int k = 0; k < m; ++k) xs = xs + sx[k];
+        else if (threadIdx.x == 32)
+            for (int k = 0; k < m; ++k) zs = zs + sz[k];
+        else if (threadIdx.x == 64)
+            for (int k = 0; k < m; ++k) ws = ws + sw[k];
         __syncthreads();
     }
+    if (threadIdx.x == 32) sx[0] = zs;
+    if (threadIdx.x == 64) sx[1] = ws;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        zs = sx[0];
+        ws = sx[1];
         const double tan_m = gfm::tan(0.5 * P.angle_mzone * 3.14159265358979323846 / 180.0);
         A.mg_s[MS_TANM] = tan_m;
         A.mg_i[MI_IHW] = mg_ceil(tan_m * 200e3 / P.dxmin);
@@ -495,21 +501,31 @@ __global__ void __launch_bounds__(MG_CB) k_mg_zone2(const DevParams *__restrict_
             sr[threadIdx.x] = (x - xc) * (x - xc) * w;
         }
         __syncthreads();
+        // the four sums by the first lanes of warps 0-3
+        const int m = n - base < MG_CB ? n - base : MG_CB;
         if (threadIdx.x == 0) {
-            const int m = n - base < MG_CB ? n - base : MG_CB;
-            for (int k = 0; k < m; ++k) {
-                if (sx[k] < xc) {
-                    xl = xl + sl[k];
-                    wl = wl + sw[k];
-                } else if (sx[k] > xc) {
-                    xr = xr + sr[k];
-                    wr = wr + sw[k];
-                }
-            }
+            for (int k = 0; k < m; ++k)
+                if (sx[k] < xc) xl = xl + sl[k];
+        } else if (threadIdx.x == 32) {
+            for (int k = 0; k < m; ++k)
+                if (sx[k] < xc) wl = wl + sw[k];
+        } else if (threadIdx.x == 64) {
+            for (int k = 0; k < m; ++k)
+                if (sx[k] > xc) xr = xr + sr[k];
+        } else if (threadIdx.x == 96) {
+            for (int k = 0; k < m; ++k)
+                if (sx[k] > xc) wr = wr + sw[k];
         }
         __syncthreads();
     }
+    if (threadIdx.x == 32) sl[0] = wl;
+    if (threadIdx.x == 64) sl[1] = xr;
+    if (threadIdx.x == 96) sl[2] = wr;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        wl = sl[0];
+        xr = sl[1];
+        wr = sl[2];
         int jc, ic;
         mg_eji(d, found, jc, ic);
         xl = 1.8 * sqrt(xl / wl);
@@ -600,9 +616,15 @@ __device__ __forceinline__ int mg_lower(const int *list, int n, long long e) {
 
 // every element as a migration target: the adds of the sources that reach
 // it, in serial order, with its own clamp to fmagma_max at its place in
-// that order; dike_added and the MOR marker volume alongside
+// that order; dike_added and the MOR marker volume alongside.  Two threads
+// per element in alternate warps (which sit on different SM
+// sub-partitions): one carries fmagma and fmagma2, the other dike_added and
+// the MOR marker volume, so that each thread's chain of FP64 adds is half
+// as long.
 __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int part = (int)((gid >> 5) & 1);
+    const long long t = ((gid >> 6) << 5) + (gid & 31);
     if (t >= d.E) return;
     const DevParams &P = *Pp;
     const int nx = d.nx, nz = d.nz;
@@ -651,46 +673,52 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
         }
     }
     const double fmax = P.fmagma_max;
-    double f = A.fmagma[t], f2 = A.fmagma2[t], da = 0.0, mv = A.mor_marker_vol[t];
-    bool clamped = false;
-    for (int k = k0; k < k1; ++k) {
-        const double *s = src + (long long)k * GF_MG_SRC_W;
-        const long long es = mg_int(s[SR_E]);
-        if (!clamped && es > t) {
-            f = mg_min(f, fmax);
-            f2 = mg_min(f2, fmax);
-            clamped = true;
-        }
-        const long long flags = mg_int(s[SR_FLAGS]);
-        if (flags & 1) {
-            if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) {
-                f = f + s[SR_TERM_C];
-                da = da + s[SR_TERM_C];
+    const bool mor_in = mor_l || mor_r;
+    if (part == 0) { // fmagma, fmagma2 with the clamp
+        double f = A.fmagma[t], f2 = A.fmagma2[t];
+        bool clamped = false;
+        for (int k = k0; k < k1; ++k) {
+            const double *s = src + (long long)k * GF_MG_SRC_W;
+            const long long es = mg_int(s[SR_E]);
+            if (!clamped && es > t) {
+                f = mg_min(f, fmax);
+                f2 = mg_min(f2, fmax);
+                clamped = true;
             }
-            const int i1s = (int)mg_int(s[SR_I1]);
-            const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
-            if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= mg_int(s[SR_J1]) &&
-                fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
-                f = f + s[SR_TERM_M];
+            const long long flags = mg_int(s[SR_FLAGS]);
+            if (flags & 1) {
+                if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) f = f + s[SR_TERM_C];
+                const int i1s = (int)mg_int(s[SR_I1]);
+                const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
+                if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= mg_int(s[SR_J1]) &&
+                    fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
+                    f = f + s[SR_TERM_M];
+            }
+            if ((flags & 2) && mor_in) f2 = f2 + s[SR_TERM_R];
+            if (es == t) {
+                f = mg_min(f, fmax);
+                f2 = mg_min(f2, fmax);
+                clamped = true;
+            }
         }
-        if ((flags & 2) && (mor_l || mor_r)) {
-            f2 = f2 + s[SR_TERM_R];
-            mv = mv + s[SR_TERM_R];
-        }
-        if (es == t) {
+        if (!clamped) {
             f = mg_min(f, fmax);
             f2 = mg_min(f2, fmax);
-            clamped = true;
         }
+        A.fmagma[t] = f;
+        A.fmagma2[t] = f2;
+    } else { // dike_added, MOR marker volume (no clamp)
+        double da = 0.0, mv = A.mor_marker_vol[t];
+        for (int k = k0; k < k1; ++k) {
+            const double *s = src + (long long)k * GF_MG_SRC_W;
+            const long long flags = mg_int(s[SR_FLAGS]);
+            if ((flags & 1) && crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1]))
+                da = da + s[SR_TERM_C];
+            if ((flags & 2) && mor_in) mv = mv + s[SR_TERM_R];
+        }
+        A.dike_added[t] = da;
+        A.mor_marker_vol[t] = mv;
     }
-    if (!clamped) {
-        f = mg_min(f, fmax);
-        f2 = mg_min(f2, fmax);
-    }
-    A.fmagma[t] = f;
-    A.fmagma2[t] = f2;
-    A.dike_added[t] = da;
-    A.mor_marker_vol[t] = mv;
 }
 
 // rate-capped dike release; mark the elements that receive new markers

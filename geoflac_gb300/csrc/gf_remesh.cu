@@ -692,109 +692,131 @@ __device__ int add_marker1(DevArrays &A, const GfDims &d, double x, double y, in
     return 1;
 }
 
-// resurface (fl_move.f90:320-426), serial over the surface elements as in
-// the reference (markers are numbered in element order): erosion past
-// thickness / markers removes the element's topmost marker, deposition adds
-// a sediment marker (phase ksed1 = 1) and accumulated extrusion arc markers
-// (phase kocean1), by add_marker_at_top (fl_move.f90:429-472, stop 134
-// after 100 misses)
-__global__ void k_resurface(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d, int nloop,
-                            int max_markers) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const DevParams &P = *Pp;
+// add_marker_at_top (fl_move.f90:429-472): a marker of phase kph at a random
+// point in the upper dz_ratio of the top element of column i (seed loop +
+// i + 1); false after 100 misses (stop 134)
+__device__ bool add_marker_at_top1(DevArrays &A, const GfDims &d, int i, double dz_ratio, double time, int loop,
+                                   int kph, int max_markers) {
+    const double *c = A.cord;
+    int iseed = loop + (i + 1), icount = 0;
+    while (true) {
+        double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
+        double x1 = CX(c, d, 0, i) * (1 - r1) + CX(c, d, 0, i + 1) * r1;
+        double y1 = CY(c, d, 0, i) * (1 - r1) + CY(c, d, 0, i + 1) * r1;
+        double x2 = CX(c, d, 1, i) * (1 - r1) + CX(c, d, 1, i + 1) * r1;
+        double y2 = CY(c, d, 1, i) * (1 - r1) + CY(c, d, 1, i + 1) * r1;
+        r2 = r2 * dz_ratio;
+        double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
+        int inc = add_marker1(A, d, xx, yy, kph, time, 0, i, max_markers);
+        if (inc == 1 || inc == -1) return true;
+        if (++icount > 100) return false;
+    }
+}
+
+// resurface (fl_move.f90:320-426), in two passes that give the serial
+// loop's result.  Per surface element: an element whose accumulated erosion
+// passes thickness / markers loses its topmost marker (its own marker list
+// only, so all elements at once); then, in element order (the markers'
+// numbering), deposition adds a sediment marker (ksed1) and accumulated
+// extrusion arc markers (kocean1) by add_marker_at_top.  The conditions use
+// the element's marker count from before its erosion, as the reference.
+// Work flags and counts go to the flexure scratch (free after fl_flexure).
+__global__ void __launch_bounds__(GF_THREADS) k_resurface_erode(const DevParams *__restrict__ Pp, DevClock *C,
+                                                                DevArrays A, GfDims d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nx = d.nx, M = GF_MAX_MARKERS_PER_ELEM;
+    if (i >= nx - 1) return;
+    const double *c = A.cord;
+    int *rs = (int *)A.flex;
+    const double elz = 0.5 * (CY(c, d, 0, i) - CY(c, d, 1, i) + CY(c, d, 0, i + 1) - CY(c, d, 1, i + 1));
+    const double chgtopo = A.dhacc[i];
+    const long long e = gf_elem(d, 0, i);
+    const int kinc = A.nmark_elem[e];
+    int work = 0;
+    if (-chgtopo * kinc >= elz && kinc > 1) {
+        double ymax = -1e30;
+        int kmax = 0;
+        for (int k = 1; k <= kinc; ++k) {
+            int n = A.mark_id_elem[e * M + k - 1];
+            int m = A.mark_ntriag[n - 1];
+            int kk = (m - 1) % 2 + 1;
+            int jj = ((m - kk) / 2) % (d.nz - 1);
+            int ii = (m - kk) / 2 / (d.nz - 1);
+            double ba1 = A.mark_a1[n - 1], ba2 = A.mark_a2[n - 1];
+            double ba3 = 1.0 - ba1 - ba2;
+            int i1, i2, i3, j1, j2, j3;
+            if (kk == 1) {
+                i1 = ii; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj;
+            } else {
+                i1 = ii + 1; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj + 1;
+            }
+            double y = CY(c, d, j1, i1) * ba1 + CY(c, d, j2, i2) * ba2 + CY(c, d, j3, i3) * ba3;
+            if (ymax < y) {
+                ymax = y;
+                kmax = k;
+            }
+        }
+        if (kmax != 0) {
+            int nmax = A.mark_id_elem[e * M + kmax - 1];
+            A.mark_id_elem[e * M + kmax - 1] = A.mark_id_elem[e * M + kinc - 1];
+            A.mark_id_elem[e * M + kinc - 1] = 0;
+            A.mark_dead[nmax - 1] = 0;
+            A.nmark_elem[e] = A.nmark_elem[e] - 1;
+        }
+        A.dhacc[i] = 0.0;
+        work |= 4;
+    }
+    if (chgtopo * kinc >= elz && kinc != M) work |= 1;
+    if (A.extr_acc[i] * kinc >= elz && kinc != M) work |= 2;
+    rs[i] = work;
+    rs[nx + i] = kinc;
+    if (work == 4) count_phase_ratio1(*Pp, C, A, d, e);
+}
+// the additions, one warp: 32 columns' flags at a time, the first lane adds
+// in column order
+__global__ void k_resurface_add(const DevParams *__restrict__ Pp, DevClock *C, DevArrays A, GfDims d, int nloop,
+                                int max_markers) {
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const DevParams &P = *Pp;
+    const int nx = d.nx, M = GF_MAX_MARKERS_PER_ELEM, lane = threadIdx.x;
+    const int *rs = (const int *)A.flex;
     const double *c = A.cord;
     const double time = C->time;
-    for (int i = 0; i < nx - 1; ++i) {
-        double elz = 0.5 * (CY(c, d, 0, i) - CY(c, d, 1, i) + CY(c, d, 0, i + 1) - CY(c, d, 1, i + 1));
-        double chgtopo = A.dhacc[i];
-        const long long e = gf_elem(d, 0, i);
-        int kinc = A.nmark_elem[e];
-        int ichanged = 0;
-        if (-chgtopo * kinc >= elz && kinc > 1) {
-            double ymax = -1e30;
-            int kmax = 0;
-            for (int k = 1; k <= kinc; ++k) {
-                int n = A.mark_id_elem[e * M + k - 1];
-                int m = A.mark_ntriag[n - 1];
-                int kk = (m - 1) % 2 + 1;
-                int jj = ((m - kk) / 2) % (d.nz - 1);
-                int ii = (m - kk) / 2 / (d.nz - 1);
-                double ba1 = A.mark_a1[n - 1], ba2 = A.mark_a2[n - 1];
-                double ba3 = 1.0 - ba1 - ba2;
-                int i1, i2, i3, j1, j2, j3;
-                if (kk == 1) {
-                    i1 = ii; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj;
-                } else {
-                    i1 = ii + 1; i2 = ii; i3 = ii + 1; j1 = jj; j2 = jj + 1; j3 = jj + 1;
-                }
-                double y = CY(c, d, j1, i1) * ba1 + CY(c, d, j2, i2) * ba2 + CY(c, d, j3, i3) * ba3;
-                if (ymax < y) {
-                    ymax = y;
-                    kmax = k;
-                }
-            }
-            if (kmax != 0) {
-                int nmax = A.mark_id_elem[e * M + kmax - 1];
-                A.mark_id_elem[e * M + kmax - 1] = A.mark_id_elem[e * M + kinc - 1];
-                A.mark_id_elem[e * M + kinc - 1] = 0;
-                A.mark_dead[nmax - 1] = 0;
-                A.nmark_elem[e] = A.nmark_elem[e] - 1;
-            }
-            A.dhacc[i] = 0.0;
-            ichanged = 1;
-        }
-        if (chgtopo * kinc >= elz && kinc != M) {
-            // add_marker_at_top(i, 0.1, time, nloop, ksed1)
-            int iseed = nloop + (i + 1), icount = 0;
-            while (true) {
-                double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
-                double x1 = CX(c, d, 0, i) * (1 - r1) + CX(c, d, 0, i + 1) * r1;
-                double y1 = CY(c, d, 0, i) * (1 - r1) + CY(c, d, 0, i + 1) * r1;
-                double x2 = CX(c, d, 1, i) * (1 - r1) + CX(c, d, 1, i + 1) * r1;
-                double y2 = CY(c, d, 1, i) * (1 - r1) + CY(c, d, 1, i + 1) * r1;
-                r2 = r2 * 0.1;
-                double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
-                int inc = add_marker1(A, d, xx, yy, 1, time, 0, i, max_markers);
-                if (inc == 1 || inc == -1) break;
-                if (++icount > 100) {
-                    set_status(C, 134, (int)e);
-                    return;
-                }
-            }
-            A.dhacc[i] = 0.0;
-            ichanged = 1;
-        }
-        // volcanic extrusion: arc markers (phase kocean1) in the upper part
-        // of the element, add_marker_at_top with seeds nloop + i + ii
-        // (fl_move.f90:403-416)
-        const double chgtopo2 = A.extr_acc[i];
-        if (chgtopo2 * kinc >= elz && kinc != M) {
-            const double q = ceil(chgtopo2 / elz * kinc);
-            const int n_to_add = q < (double)(M - kinc) ? (int)q : M - kinc;
-            const double dz_ratio = 1.0 < chgtopo2 / elz ? 1.0 : chgtopo2 / elz;
-            for (int ii = 1; ii <= n_to_add; ++ii) {
-                int iseed = nloop + (i + 1) + ii + (i + 1), icount = 0;
-                while (true) {
-                    double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
-                    double x1 = CX(c, d, 0, i) * (1 - r1) + CX(c, d, 0, i + 1) * r1;
-                    double y1 = CY(c, d, 0, i) * (1 - r1) + CY(c, d, 0, i + 1) * r1;
-                    double x2 = CX(c, d, 1, i) * (1 - r1) + CX(c, d, 1, i + 1) * r1;
-                    double y2 = CY(c, d, 1, i) * (1 - r1) + CY(c, d, 1, i + 1) * r1;
-                    r2 = r2 * dz_ratio;
-                    double xx = x1 * (1 - r2) + x2 * r2, yy = y1 * (1 - r2) + y2 * r2;
-                    int inc = add_marker1(A, d, xx, yy, 3, time, 0, i, max_markers);
-                    if (inc == 1 || inc == -1) break;
-                    if (++icount > 100) {
+    bool failed = false;
+    for (int base = 0; base < nx - 1 && !failed; base += 32) {
+        const int ii = base + lane;
+        unsigned bal = __ballot_sync(0xffffffffu, ii < nx - 1 && (rs[ii] & 3));
+        if (lane == 0)
+            while (bal && !failed) {
+                const int i = base + __ffs(bal) - 1;
+                bal &= bal - 1;
+                const int work = rs[i], kinc = rs[nx + i];
+                const long long e = gf_elem(d, 0, i);
+                const double elz = 0.5 * (CY(c, d, 0, i) - CY(c, d, 1, i) + CY(c, d, 0, i + 1) - CY(c, d, 1, i + 1));
+                if (work & 1) { // sedimentation (ksed1)
+                    if (!add_marker_at_top1(A, d, i, 0.1, time, nloop, 1, max_markers)) {
                         set_status(C, 134, (int)e);
-                        return;
+                        failed = true;
+                        break;
                     }
+                    A.dhacc[i] = 0.0;
                 }
+                if (work & 2) { // volcanic extrusion: arc markers, seeds nloop + i + ii (fl_move.f90:403-416)
+                    const double chgtopo2 = A.extr_acc[i];
+                    const double q = ceil(chgtopo2 / elz * kinc);
+                    const int n_to_add = q < (double)(M - kinc) ? (int)q : M - kinc;
+                    const double dz_ratio = 1.0 < chgtopo2 / elz ? 1.0 : chgtopo2 / elz;
+                    for (int k = 1; k <= n_to_add && !failed; ++k)
+                        if (!add_marker_at_top1(A, d, i, dz_ratio, time, nloop + (i + 1) + k, 3, max_markers)) {
+                            set_status(C, 134, (int)e);
+                            failed = true;
+                        }
+                    if (failed) break;
+                    A.extr_acc[i] = 0.0;
+                }
+                count_phase_ratio1(P, C, A, d, e);
             }
-            A.extr_acc[i] = 0.0;
-            ichanged = 1;
-        }
-        if (ichanged == 1) count_phase_ratio1(P, C, A, d, e);
+        failed = __shfl_sync(0xffffffffu, failed, 0);
     }
 }
 
@@ -1090,7 +1112,8 @@ template <class R> void GfRemesh<R>::diff_topo(const GfLaunch &g, int resurface,
         ++*g.launches;
     }
     if (resurface) {
-        k_resurface<<<1, 1, 0, g.s>>>(g.P, g.C, g.A, g.d, nloop, max_markers);
+        GF_RLAUNCH(k_resurface_erode, (long long)(g.d.nx - 1), g.P, g.C, g.A, g.d);
+        k_resurface_add<<<1, 32, 0, g.s>>>(g.P, g.C, g.A, g.d, nloop, max_markers);
         ++*g.launches;
     }
 }
@@ -1138,7 +1161,7 @@ void GfMagma::therm(const GfLaunch &g, int max_markers) {
     GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list, (const int *)(A.mg_i + MI_COUNT), A.mg_src);
     mg_compact(g, MG_PRED_ARC, A.mg_list2, A.mg_i + MI_COUNT2);
     GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list2, (const int *)(A.mg_i + MI_COUNT2), A.mg_src2);
-    GF_RLAUNCH(k_mg_migrate, d.E, g.P, A, d);
+    GF_RLAUNCH(k_mg_migrate, 2 * ((d.E + 31) / 32) * 32, g.P, A, d); // two threads per element
     GF_RLAUNCH(k_mg_release, d.E, g.P, A, d);
     mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
     k_mg_markers<<<1, 1, 0, g.s>>>(g.P, g.C, A, d, max_markers);
