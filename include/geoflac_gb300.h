@@ -240,7 +240,10 @@ int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L);
 /* ---- device context ---- */
 
 /* Create a device context mirroring L.  mode is GF_MODE_FP64 or
- * GF_MODE_MIXED.  Allocates all device storage; nothing is copied yet. */
+ * GF_MODE_MIXED.  Allocates all device storage; nothing is copied yet.
+ * GF_ERR_UNSUPPORTED: applied stress boundary conditions (nystressbc = 1),
+ * and, in GF_MODE_MIXED, the magma sub-model (itype_melting = 1) and the
+ * flexural bottom (nbc 200 on side 2). */
 int gf_create(gf_ctx **ctx, const gf_params *p, const gf_layout *L, int mode);
 void gf_destroy(gf_ctx *ctx);
 int gf_upload(gf_ctx *ctx, unsigned field_mask);
