@@ -110,9 +110,9 @@ def test_magma_steps_match_oracle(workdir):
     gpu.close()
 
 
-def test_magma_per_subroutine_and_remesh(workdir):
+def test_magma_flac_calls_and_remesh(workdir):
     gpu, orc = _pair(workdir, "b")
-    for _ in range(11):  # drop-in per-subroutine calls, melting at nloop 0 and 10
+    for _ in range(11):  # gf_flac calls (one step each), melting at nloop 0 and 10
         gpu.flac()
         orc.flac()
     _compare(gpu, orc, "11 flac calls")
@@ -122,6 +122,36 @@ def test_magma_per_subroutine_and_remesh(workdir):
     gpu.step(10)
     orc.step(10)
     _compare(gpu, orc, "after remesh")
+    gpu.close()
+
+
+def test_magma_drop_in_subroutines(workdir):
+    """The reference's flac.f90 order through the per-subroutine entry points
+    (fl_therm with the magma part, change_phase with melting, fl_rheol,
+    fl_node, fl_move with the magma blocks of diff_topo, rmasses, dt_mass),
+    the caller advancing nloop and time as par.f90 does."""
+    gpu, orc = _pair(workdir, "d")
+    p = orc.p
+    for _ in range(12):
+        nl = orc.c.nloop
+        calls = ["fl_therm"]
+        if nl % p.ifreq_rmasses == 0:
+            calls.append("change_phase")
+        calls += ["fl_rheol", "fl_node", "fl_move"]
+        if nl % p.ifreq_rmasses == 0:
+            calls.append("rmasses")
+        if nl % p.ifreq_imasses == 0:
+            calls.append("dt_mass")
+        for f in calls:
+            getattr(orc, f)()
+            getattr(gpu, f)()
+        orc.c.nloop += 1
+        orc.c.time += orc.c.dt
+        gpu.download(0)
+        gpu.clock.nloop += 1
+        gpu.clock.time += gpu.clock.dt
+        gpu.upload(0)
+    _compare(gpu, orc, "12 drop-in steps")
     gpu.close()
 
 
