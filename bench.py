@@ -34,7 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "element-steps/s on 1 GB300: FP64 vs mixed vs batched; surrogate sweep speedup @err"
-WORKLOAD = "config2: two-phase extension, 1000x300 quads (300,000 elements, 301,301 nodes), 1000 km x 300 km"
+WORKLOAD = "extension_1000x300: two-phase extension, 1000x300 quads (300,000 elements, 301,301 nodes), 1000 km x 300 km"
 
 
 def _dist():
@@ -284,7 +284,7 @@ def run_ours(args):
     from geoflac_gb300 import bytes_model, inpgen
 
     d = tempfile.mkdtemp(prefix="gfbench")
-    inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    inp = inpgen.extension_1000x300().write(os.path.join(d, "extension_1000x300.inp"))
     if args.profile in ("fno", "batch", "magma"):
         profile_extra(args, d)
         return
@@ -612,7 +612,7 @@ def profile_magma(args, workdir: str):
     _seed_melting(p, s)
     p0, c0, s0 = clone(p, c, s)
     p0.itype_melting = 0
-    out = {"profile": "magma", "model": "magma_arc 600x150 (config3 with 19 phases, itype_melting 1, "
+    out = {"profile": "magma", "model": "magma_arc 600x150 (convergence with 19 phases, itype_melting 1, "
                                         "prod_magma 2e-15, prod_magma2 1e-13)",
            "elements": (p.nx - 1) * (p.nz - 1), "steps": args.steps}
     for tag, (pp, cc, ss) in (("plain", (p0, c0, s0)), ("magma", (p, c, s))):
@@ -660,7 +660,7 @@ def run_reference(args):
     from oracle.oracle import Oracle
 
     d = tempfile.mkdtemp(prefix="gfbench")
-    inp = inpgen.config2().write(os.path.join(d, "config2.inp"))
+    inp = inpgen.extension_1000x300().write(os.path.join(d, "extension_1000x300.inp"))
     n = os.cpu_count() or 1
     p, c, s = new_state(inp)
     o = Oracle(p, c, s, threads=n)

@@ -5,10 +5,10 @@ The file layout is the reference's positional format read by
 ``src/read_params.f90:3-348`` (one READ per non-comment line, ``;`` starts a
 comment line).  The workloads are seeded synthetic models:
 
-* ``config1``  -- two-phase extension, 60x20 quads, 300 km x 100 km (CPU-sized)
-* ``config2``  -- the same physics at 1000x300 quads, 1000 km x 300 km,
+* ``extension_60x20``  -- two-phase extension, 60x20 quads, 300 km x 100 km (CPU-sized)
+* ``extension_1000x300``  -- the same physics at 1000x300 quads, 1000 km x 300 km,
                   remeshing when a triangle angle falls below 10 degrees
-* ``config3``  -- ocean-continent convergence, 600x150 quads, 1200 km x 300 km,
+* ``convergence``  -- ocean-continent convergence, 600x150 quads, 1200 km x 300 km,
                   Winkler foundation, basalt -> eclogite
 * ``elastic_bar``, ``maxwell_column``, ``plastic_bar`` -- the analytic
   known-answer set-ups described by the reference's tutorials 01-03
@@ -304,15 +304,15 @@ def two_phase_extension(nex: int, nez: int, width: float, depth: float,
     return m
 
 
-def config1() -> Model:
+def extension_60x20() -> Model:
     return two_phase_extension(60, 20, 300e3, 100e3)
 
 
-def config2() -> Model:
+def extension_1000x300() -> Model:
     return two_phase_extension(1000, 300, 1000e3, 300e3, ny_rem=1)
 
 
-def config3(nex: int = 600, nez: int = 150) -> Model:
+def convergence(nex: int = 600, nez: int = 150) -> Model:
     """Ocean-continent convergence: 60-Myr half-space cooling oceanic plate
     (7 km basalt, 1 km weak sediment) on the left, 35 km continental crust on
     the right, left wall pushing at 5 cm/yr, Winkler foundation."""
@@ -372,18 +372,19 @@ def plastic_bar() -> Model:
                  phases=ph, v_min=1e19, ntest_rem=100)
 
 
-def config3_small() -> Model:
-    """config3's physics on a 60x15 mesh (CPU-sized parity case)."""
-    return config3(60, 15)
+def convergence_60x15() -> Model:
+    """The ocean-continent convergence model on a 60x15 mesh (CPU-sized
+    parity case)."""
+    return convergence(60, 15)
 
 
 def magma_arc(nex: int = 60, nez: int = 15) -> Model:
-    """config3 with all 19 phase ids of the reference's special rules, the
-    magma sub-model on (itype_melting 1: melting, dikes, mantle percolation,
+    """The convergence model with all 19 phase ids of the reference's
+    special rules, the magma sub-model on (itype_melting 1: melting, dikes, mantle percolation,
     the MOR pool with eruption) and surface diffusion (which carries the
     arc-extrusion and MOR-crust blocks).  The melting itself is set up by
     the caller (temperatures, subducted phases)."""
-    m = config3(nex, nez)
+    m = convergence(nex, nez)
     m.phases = m.phases + [crust() for _ in range(19 - len(m.phases))]
     m.phases[13] = crust(den=2800.0)  # 14: arc crust
     m.phases[15] = mantle()  # 16: hydrated mantle
@@ -396,7 +397,7 @@ def magma_arc(nex: int = 60, nez: int = 15) -> Model:
     return m
 
 
-CONFIGS = {"config1": config1, "config2": config2, "config3": config3, "config3_small": config3_small,
+CONFIGS = {"extension_60x20": extension_60x20, "extension_1000x300": extension_1000x300, "convergence_600x150": convergence, "convergence_60x15": convergence_60x15,
            "elastic_bar": elastic_bar, "maxwell_column": maxwell_column,
            "plastic_bar": plastic_bar, "magma_arc": magma_arc}
 

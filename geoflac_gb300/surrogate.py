@@ -10,7 +10,7 @@
    member, write the prediction into the member's mesh (gf_batch_inject)
    and gate it with the force-imbalance residual of the injected state
    (gf_batch_force_residual).  Members above the tolerance are restored and
-   advanced by the plain FLAC step; the plain step stays the judge.
+   advanced by the plain FLAC step; the plain step stays the arbiter of the error.
 """
 from __future__ import annotations
 

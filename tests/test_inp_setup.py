@@ -27,7 +27,7 @@ def test_generated_configs_round_trip(workdir):
 def test_list_directed_forms(workdir):
     """Repeat counts, D exponents, trailing remarks and values continued on
     the next line, as Fortran list-directed input allows."""
-    txt = inpgen.config1().text().splitlines()
+    txt = inpgen.extension_60x20().text().splitlines()
     # the viscosity line "v_min, v_max, 2, 500.0" -> D exponent, split across lines
     i = next(k for k, s in enumerate(txt) if s.startswith("1e+20") or s.startswith("100000000000000000000"))
     txt[i] = "1.0D20,"
@@ -59,7 +59,7 @@ def test_reference_inputs_parse():
 
 
 def test_setflac_host_state(workdir):
-    m = inpgen.config1()
+    m = inpgen.extension_60x20()
     p, c, s = new_state(m.write(str(workdir / "c1.inp")))
     nex, nez = m.nex, m.nez
     # uniform mesh
@@ -112,7 +112,7 @@ def test_marker_lcg_matches_published_recurrence():
 def test_winkler_pisos(workdir):
     """nyhydro = 2: pisos is the lithostatic pressure at the base of the last
     column (init_stress.f90:400-403)."""
-    p, c, s = new_state(inpgen.config3_small().write(str(workdir / "c3.inp")))
+    p, c, s = new_state(inpgen.convergence_60x15().write(str(workdir / "c3.inp")))
     rho_g_h = 0.0
     assert p.pisos > 0
     col = s["stress0"][:, -1, 1, 0]

@@ -116,7 +116,7 @@ def _model(workdir, name, mode, **kw):
 
 @pytest.mark.parametrize("mode,tol", [("fp64", 1e-6), ("mixed", 1e-5)])
 def test_outflac_frame_matches_state(workdir, mode, tol):
-    _, g = _model(workdir, "config1", mode)
+    _, g = _model(workdir, "extension_60x20", mode)
     for k in range(19):
         g.params.io_flags[k] = 1
     g.set_params()
@@ -187,7 +187,7 @@ def test_outflac_frame_matches_state(workdir, mode, tol):
 
 
 def test_outmarker_matches_markers(workdir):
-    _, g = _model(workdir, "config3_small", "fp64")
+    _, g = _model(workdir, "convergence_60x15", "fp64")
     g.step(400)
     g.remesh()  # a remesh adds markers and kills some
     g.step(20)
@@ -273,7 +273,7 @@ def _read_restart(d, p, s):
 
 
 def test_saveflac_rsflac_round_trip_matches_oracle(workdir):
-    inp, g1 = _model(workdir, "config3_small", "fp64")
+    inp, g1 = _model(workdir, "convergence_60x15", "fp64")
     g1.step(400)
     g1.remesh()
     g1.step(30)
@@ -328,7 +328,7 @@ def test_saveflac_rsflac_round_trip_matches_oracle(workdir):
 
 
 def test_rsflac_mixed_and_bad_files(workdir):
-    inp, g1 = _model(workdir, "config1", "mixed")
+    inp, g1 = _model(workdir, "extension_60x20", "mixed")
     g1.step(100)
     d = str(workdir / "restart_mixed")
     os.makedirs(d, exist_ok=True)

@@ -58,7 +58,7 @@ def _report(name, data):
             json.dump(data, f, indent=1)
 
 
-@pytest.mark.parametrize("name", ["config1", "config3_small"])
+@pytest.mark.parametrize("name", ["extension_60x20", "convergence_60x15"])
 def test_mixed_short_horizon(workdir, name):
     """10 steps: FP32 rounding has not yet been amplified."""
     a, b = _pair(workdir, name)
@@ -74,7 +74,7 @@ def test_mixed_short_horizon(workdir, name):
     b.close()
 
 
-@pytest.mark.parametrize("name", ["config1", "config3_small"])
+@pytest.mark.parametrize("name", ["extension_60x20", "convergence_60x15"])
 def test_mixed_long_run_observables(workdir, name):
     """500 steps: mean stresses, total plastic strain and topography, each
     within a fixed bound or, where the model itself is that sensitive,

@@ -1,6 +1,6 @@
 """Pins the oracle to the reference's analytic known answers
 (examples/tutorial01-03 of the reference): the oracle must reproduce the
-physics those tutorials verify before it can judge the CUDA kernels.
+physics those tutorials verify before it can check the CUDA kernels.
 
 * elastic bar in plane strain: E_eff = 4 mu (lambda+mu)/(lambda+2 mu) = 80 GPa
 * Maxwell column under constant strain rate: sigma_xx(t) =

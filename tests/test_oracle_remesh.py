@@ -8,7 +8,7 @@ from oracle.oracle import Oracle
 
 
 def test_remesh_event_invariants(workdir):
-    inp = inpgen.CONFIGS["config3_small"]().write(str(workdir / "c3s_rm.inp"))
+    inp = inpgen.CONFIGS["convergence_60x15"]().write(str(workdir / "c3s_rm.inp"))
     p, c, s = new_state(inp)
     assert p.incoming_left == 1
     o = Oracle(p, c, s, threads=2)

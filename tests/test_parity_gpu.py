@@ -43,7 +43,7 @@ def _assert_close(gpu, orc, tol=TOL, where=""):
     return diffs
 
 
-@pytest.mark.parametrize("name", ["config1", "config3_small"])
+@pytest.mark.parametrize("name", ["extension_60x20", "convergence_60x15"])
 def test_setflac_parity(workdir, name):
     gpu, orc = _pair(workdir, name)
     _assert_close(gpu, orc, where="setflac")
@@ -54,7 +54,7 @@ def test_setflac_parity(workdir, name):
 def test_each_routine_matches_oracle(workdir, routine):
     """Advance 37 steps with the oracle, give both the same state, then run
     one reference subroutine on each side and compare every field."""
-    gpu, orc = _pair(workdir, "config3_small")
+    gpu, orc = _pair(workdir, "convergence_60x15")
     orc.step(37)
     gpu.state.copy_from(orc.s)
     C = gpu.clock
@@ -69,7 +69,7 @@ def test_each_routine_matches_oracle(workdir, routine):
     gpu.close()
 
 
-@pytest.mark.parametrize("name,steps", [("config1", 1000), ("config3_small", 600)])
+@pytest.mark.parametrize("name,steps", [("extension_60x20", 1000), ("convergence_60x15", 600)])
 def test_steps_match_oracle(workdir, name, steps):
     """The full step (flac.f90) over many steps: captured-graph driver vs
     the serial oracle, checked every 100 steps."""
@@ -86,8 +86,8 @@ def test_steps_match_oracle(workdir, name, steps):
 
 def test_graph_step_equals_flac_calls(workdir):
     """gf_step(n) (graph replay) and n gf_flac calls give identical bits."""
-    a, _ = _pair(workdir, "config1")
-    b, _ = _pair(workdir, "config1")
+    a, _ = _pair(workdir, "extension_60x20")
+    b, _ = _pair(workdir, "extension_60x20")
     a.step(25)
     for _ in range(25):
         b.flac()
@@ -103,7 +103,7 @@ def test_thermal_fixed_point_is_exact(workdir):
     """The in-place (Gauss-Seidel) thermal update of fl_therm.f90 is
     reproduced bit for bit: the sweeps reach their fixed point well below
     the cap, and the temperatures equal the serial oracle's exactly."""
-    gpu, orc = _pair(workdir, "config1")
+    gpu, orc = _pair(workdir, "extension_60x20")
     for _ in range(30):
         orc.fl_therm()
         gpu.fl_therm()
@@ -116,7 +116,7 @@ def test_thermal_fixed_point_is_exact(workdir):
 
 def test_thermal_sweep_cap_reports_unconverged(workdir):
     """A cap below the number of sweeps needed is reported, not hidden."""
-    inp = inpgen.config1().write(str(workdir / "c1cap.inp"))
+    inp = inpgen.extension_60x20().write(str(workdir / "c1cap.inp"))
     p, c, s = new_state(inp, therm_sweeps=1)
     g = Flac(p, c, s, "fp64")
     g.fl_therm()
@@ -128,7 +128,7 @@ def test_thermal_sweep_cap_reports_unconverged(workdir):
 def test_maxwell_stop_code(workdir):
     """A viscosity far below the Maxwell limit makes the reference stop with
     code 22 (rh_maxwell.f90:58-62); the GPU path returns the same code."""
-    gpu, orc = _pair(workdir, "config1")
+    gpu, orc = _pair(workdir, "extension_60x20")
     gpu.download()
     gpu.state["visn"][...] = 1e10
     gpu.upload(capi.F_VISN)
@@ -148,7 +148,7 @@ def test_maxwell_stop_code(workdir):
 def test_negative_area_stop_code(workdir):
     """Velocities that fold an element make fl_move stop with code 40
     (fl_move.f90:110-126) on both sides."""
-    gpu, orc = _pair(workdir, "config1")
+    gpu, orc = _pair(workdir, "extension_60x20")
     gpu.download()
     v = gpu.state["vel"]
     v[...] = 0.0

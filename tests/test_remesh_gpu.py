@@ -47,8 +47,8 @@ def _compare(gpu, orc, tol, where):
     return diffs
 
 
-@pytest.mark.parametrize("name,mps,steps", [("config3_small", 3, 400), ("config3_small", 2, 600),
-                                            ("config1", 3, 300)])
+@pytest.mark.parametrize("name,mps,steps", [("convergence_60x15", 3, 400), ("convergence_60x15", 2, 600),
+                                            ("extension_60x20", 3, 300)])
 def test_remesh_event_matches_oracle(workdir, name, mps, steps):
     gpu, orc = _pair(workdir, name, markers_per_side=mps)
     gpu.step(steps)
@@ -67,7 +67,7 @@ def test_remesh_event_matches_oracle(workdir, name, mps, steps):
 
 def test_marker2elem_top_up_matches_oracle(workdir):
     """marker2elem alone on a state whose elements hold 4 markers each."""
-    gpu, orc = _pair(workdir, "config1", markers_per_side=2)
+    gpu, orc = _pair(workdir, "extension_60x20", markers_per_side=2)
     gpu.step(20)
     orc.step(20)
     gpu.download()  # the clock (nloop seeds the marker positions)
@@ -84,7 +84,7 @@ def test_marker2elem_top_up_matches_oracle(workdir):
 def test_run_loop_remeshes_like_the_oracle(workdir):
     """par.f90's loop: ntest_rem steps, itest_mesh, remesh when the smallest
     angle falls below angle_rem (raised here so that events happen)."""
-    gpu, orc = _pair(workdir, "config3_small")
+    gpu, orc = _pair(workdir, "convergence_60x15")
     for pr in (gpu.params, orc.p):
         pr.ny_rem = 1
         pr.ntest_rem = 100
@@ -104,7 +104,7 @@ def test_run_loop_remeshes_like_the_oracle(workdir):
 
 
 def test_mixed_remesh_keeps_marker_bookkeeping(workdir):
-    gpu, _ = _pair(workdir, "config3_small", mode="mixed")
+    gpu, _ = _pair(workdir, "convergence_60x15", mode="mixed")
     gpu.step(400)
     gpu.remesh()
     gpu.step(50)

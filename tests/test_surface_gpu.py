@@ -40,7 +40,7 @@ def _init_areas(s):
 
 
 def _setup(workdir, tag, mode="fp64"):
-    m = inpgen.config1()
+    m = inpgen.extension_60x20()
     m.topo_kappa = 2e-5
     p, c, s = new_state(m.write(str(workdir / f"surf_{tag}.inp")))
     for k in range(p.nphase):
@@ -142,7 +142,7 @@ def _flex_model(workdir, tag, mode="fp64"):
     """The 60x20 model on a flexural bottom (nbc 200: 20 km elastic plate on
     a 3300 kg/m3 fluid) instead of the free-slip base, with a surface relief
     whose load the plate carries."""
-    m = inpgen.config1()
+    m = inpgen.extension_60x20()
     m.bcs = [b for b in m.bcs if b.side != 2] + [inpgen.BC(2, 1, m.nex + 1, 200, 20e3, 3300.0)]
     p, c, s = new_state(m.write(str(workdir / f"flex_{tag}.inp")))
     x = s["cord"][0, :, 0]

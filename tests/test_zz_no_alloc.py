@@ -25,7 +25,7 @@ def _entry():
     return f
 
 
-@pytest.mark.parametrize("name,steps", [("config1", 300), ("config3_small", 600)])
+@pytest.mark.parametrize("name,steps", [("extension_60x20", 300), ("convergence_60x15", 600)])
 def test_min_angle_noalloc_matches_itest_mesh(workdir, name, steps):
     torch = pytest.importorskip("torch")
     f = _entry()
