@@ -120,16 +120,16 @@ __device__ __forceinline__ double tpr_basalt(const DevArrays &A, const GfDims &d
 
 // ---------------------------------------------------------------- ordered compaction
 // Which elements a list holds.
-enum { MG_PRED_MASK = 0, MG_PRED_W = 1, MG_PRED_SRC = 2, MG_PRED_ARC = 3 };
+enum { MG_PRED_MASK = 0, MG_PRED_W = 1, MG_PRED_MOR = 2, MG_PRED_ARC = 3 };
 __device__ __forceinline__ bool mg_pred(int mode, const DevArrays &A, const GfDims &d, long long e) {
     if (mode == MG_PRED_MASK) return A.mg_mask[e] != 0;
     if (mode == MG_PRED_W) return A.fmelt2[e] > MG_W_BARRIER;
-    // migration sources: melting below the column's Moho (dikes and the
-    // mantle cone: ARC), or also MOR melt with a valid melting zone (SRC)
+    // migration sources: MOR melt with a valid melting zone (MOR), melting
+    // below the column's Moho (dikes and the mantle cone: ARC)
+    if (mode == MG_PRED_MOR) return A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0;
     int j, i;
     mg_eji(d, e, j, i);
-    if (j + 1 > A.jmoho[i] && A.fmelt[e] > 0) return true;
-    return mode == MG_PRED_SRC && A.fmelt2[e] > 0 && A.mg_s[MS_VALID] != 0.0;
+    return j + 1 > A.jmoho[i] && A.fmelt[e] > 0;
 }
 // block b counts its MG_CB elements
 __global__ void __launch_bounds__(MG_CB) k_mg_count(DevArrays A, GfDims d, int mode) {
@@ -616,21 +616,68 @@ __device__ __forceinline__ int mg_lower(const int *list, int n, long long e) {
 
 // every element as a migration target: the adds of the sources that reach
 // it, in serial order, with its own clamp to fmagma_max at its place in
-// that order; dike_added and the MOR marker volume alongside.  Two threads
-// per element in alternate warps (which sit on different SM
-// sub-partitions): one carries fmagma and fmagma2, the other dike_added and
-// the MOR marker volume, so that each thread's chain of FP64 adds is half
-// as long.
+// that order.  fmagma takes only dike / mantle-cone adds and fmagma2 only
+// MOR adds, so each is accumulated over its own ordered source list; four
+// threads per element in consecutive warps (different SM sub-partitions,
+// whose FP64 pipes run side by side) carry fmagma, fmagma2, dike_added and
+// the MOR marker volume.
 __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int part = (int)((gid >> 5) & 1);
-    const long long t = ((gid >> 6) << 5) + (gid & 31);
+    const int part = (int)((gid >> 5) & 3);
+    const long long t = ((gid >> 7) << 5) + (gid & 31);
     if (t >= d.E) return;
     const DevParams &P = *Pp;
     const int nx = d.nx, nz = d.nz;
     int jt, it;
     mg_eji(d, t, jt, it);
     const int jt1 = jt + 1, it1 = it + 1;
+    const double fmax = P.fmagma_max;
+    if (part == 1 || part == 3) { // MOR pool: fmagma2 (clamped) and the MOR marker volume
+        bool in = false;
+        if (A.mg_s[MS_VALID] != 0.0) {
+            const int ic1 = A.mg_i[MI_IC] + 1, jc1 = A.mg_i[MI_JC] + 1;
+            const int lo = ic1 - A.mg_i[MI_IHWL] > 1 ? ic1 - A.mg_i[MI_IHWL] : 1;
+            const int hi = ic1 + A.mg_i[MI_IHWR] < nx - 1 ? ic1 + A.mg_i[MI_IHWR] : nx - 1;
+            if (it1 >= lo && it1 <= hi && jt1 <= jc1) {
+                // which side of the zone's cone the element lies in
+                const double *c = A.cord;
+                const double x = 0.5 * (CX(c, d, jt, it) + CX(c, d, jt, it + 1));
+                const double z = 0.5 * (CY(c, d, jt, it) + CY(c, d, jt, it + 1));
+                const double xc = A.mg_s[MS_XC], z_surf = A.mg_s[MS_ZSURF];
+                in = (x < xc && fabs(xc - x) <= A.mg_s[MS_TANL] * (z_surf - z)) ||
+                     (x >= xc && fabs(x - xc) <= A.mg_s[MS_TANR] * (z_surf - z));
+            }
+        }
+        const int n = in ? A.mg_i[MI_COUNT] : 0;
+        const double *src = A.mg_src;
+        if (part == 1) {
+            double f2 = A.fmagma2[t];
+            bool clamped = false;
+            for (int k = 0; k < n; ++k) {
+                const double *s = src + (long long)k * GF_MG_SRC_W;
+                const long long es = mg_int(s[SR_E]);
+                if (!clamped && es > t) {
+                    f2 = mg_min(f2, fmax);
+                    clamped = true;
+                }
+                f2 = f2 + s[SR_TERM_R];
+                if (es == t) {
+                    f2 = mg_min(f2, fmax);
+                    clamped = true;
+                }
+            }
+            if (!clamped) f2 = mg_min(f2, fmax);
+            A.fmagma2[t] = f2;
+        } else {
+            double mv = A.mor_marker_vol[t];
+            for (int k = 0; k < n; ++k) mv = mv + src[(long long)k * GF_MG_SRC_W + SR_TERM_R];
+            A.mor_marker_vol[t] = mv;
+        }
+        return;
+    }
+    // dikes and the mantle cone: fmagma (clamped) and dike_added, over the
+    // sources in columns within max(nelem_dike, cone half width), none
+    // when the element lies below its Moho and below every source
     const double *c = A.cord;
     const double x = 0.5 * (CX(c, d, jt, it) + CX(c, d, jt, it + 1));
     const double z = 0.5 * (CY(c, d, jt, it) + CY(c, d, jt, it + 1));
@@ -638,86 +685,47 @@ __global__ void __launch_bounds__(GF_THREADS) k_mg_migrate(const DevParams *__re
     const bool crust_row = jt1 >= jtop_t && jt1 <= jm_t;
     const int ihw = A.mg_i[MI_IHW];
     const double tan_m = A.mg_s[MS_TANM];
-    // the MOR zone above the melting centre
-    bool mor = false, mor_l = false, mor_r = false;
-    if (A.mg_s[MS_VALID] != 0.0) {
-        const int ic1 = A.mg_i[MI_IC] + 1, jc1 = A.mg_i[MI_JC] + 1;
-        const int lo = ic1 - A.mg_i[MI_IHWL] > 1 ? ic1 - A.mg_i[MI_IHWL] : 1;
-        const int hi = ic1 + A.mg_i[MI_IHWR] < nx - 1 ? ic1 + A.mg_i[MI_IHWR] : nx - 1;
-        mor = it1 >= lo && it1 <= hi && jt1 <= jc1;
-        // which side of the zone's cone the element lies in (the same for
-        // every source)
-        const double xc = A.mg_s[MS_XC], z_surf = A.mg_s[MS_ZSURF];
-        mor_l = mor && x < xc && fabs(xc - x) <= A.mg_s[MS_TANL] * (z_surf - z);
-        mor_r = mor && x >= xc && fabs(x - xc) <= A.mg_s[MS_TANR] * (z_surf - z);
-    }
-    // an element in the MOR zone walks every source; any other only the
-    // dike / mantle-cone sources in columns within max(nelem_dike, cone
-    // half width), and none when it lies below its Moho and below every
-    // such source
-    const int *list = A.mg_list;
-    const double *src = A.mg_src;
-    int k0 = 0, k1 = A.mg_i[MI_COUNT];
-    if (!mor) {
-        list = A.mg_list2;
-        src = A.mg_src2;
+    const int *list = A.mg_list2;
+    const double *src = A.mg_src2;
+    int k0 = 0, k1 = 0;
+    if (!(jt1 > jm_t && jt1 > A.mg_i[MI_MAXJ])) {
         const int n = A.mg_i[MI_COUNT2];
         const int reach = (P.nelem_dike > ihw ? P.nelem_dike : ihw) + 1;
         const long long clo = it - reach < 0 ? 0 : it - reach;
         const long long chi = it + reach + 1 > nx - 1 ? nx - 1 : it + reach + 1;
-        if (jt1 > jm_t && jt1 > A.mg_i[MI_MAXJ]) {
-            k0 = k1 = 0;
-        } else {
-            k0 = mg_lower(list, n, clo * (nz - 1));
-            k1 = mg_lower(list, n, chi * (nz - 1));
-        }
+        k0 = mg_lower(list, n, clo * (nz - 1));
+        k1 = mg_lower(list, n, chi * (nz - 1));
     }
-    const double fmax = P.fmagma_max;
-    const bool mor_in = mor_l || mor_r;
-    if (part == 0) { // fmagma, fmagma2 with the clamp
-        double f = A.fmagma[t], f2 = A.fmagma2[t];
+    if (part == 0) {
+        double f = A.fmagma[t];
         bool clamped = false;
         for (int k = k0; k < k1; ++k) {
             const double *s = src + (long long)k * GF_MG_SRC_W;
             const long long es = mg_int(s[SR_E]);
             if (!clamped && es > t) {
                 f = mg_min(f, fmax);
-                f2 = mg_min(f2, fmax);
                 clamped = true;
             }
-            const long long flags = mg_int(s[SR_FLAGS]);
-            if (flags & 1) {
-                if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) f = f + s[SR_TERM_C];
-                const int i1s = (int)mg_int(s[SR_I1]);
-                const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
-                if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= mg_int(s[SR_J1]) &&
-                    fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
-                    f = f + s[SR_TERM_M];
-            }
-            if ((flags & 2) && mor_in) f2 = f2 + s[SR_TERM_R];
+            if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) f = f + s[SR_TERM_C];
+            const int i1s = (int)mg_int(s[SR_I1]);
+            const int lo = i1s - ihw > 1 ? i1s - ihw : 1, hi = i1s + ihw < nx - 1 ? i1s + ihw : nx - 1;
+            if (it1 >= lo && it1 <= hi && jt1 >= jm_t + 1 && jt1 <= mg_int(s[SR_J1]) &&
+                fabs(x - s[SR_XMELT]) <= tan_m * (z - s[SR_ZMELT]))
+                f = f + s[SR_TERM_M];
             if (es == t) {
                 f = mg_min(f, fmax);
-                f2 = mg_min(f2, fmax);
                 clamped = true;
             }
         }
-        if (!clamped) {
-            f = mg_min(f, fmax);
-            f2 = mg_min(f2, fmax);
-        }
+        if (!clamped) f = mg_min(f, fmax);
         A.fmagma[t] = f;
-        A.fmagma2[t] = f2;
-    } else { // dike_added, MOR marker volume (no clamp)
-        double da = 0.0, mv = A.mor_marker_vol[t];
+    } else {
+        double da = 0.0;
         for (int k = k0; k < k1; ++k) {
             const double *s = src + (long long)k * GF_MG_SRC_W;
-            const long long flags = mg_int(s[SR_FLAGS]);
-            if ((flags & 1) && crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1]))
-                da = da + s[SR_TERM_C];
-            if ((flags & 2) && mor_in) mv = mv + s[SR_TERM_R];
+            if (crust_row && it1 >= mg_int(s[SR_II0]) && it1 <= mg_int(s[SR_II1])) da = da + s[SR_TERM_C];
         }
         A.dike_added[t] = da;
-        A.mor_marker_vol[t] = mv;
     }
 }
 

@@ -1156,12 +1156,12 @@ void GfMagma::therm(const GfLaunch &g, int max_markers) {
     k_mg_zone2<<<1, MG_CB, 0, g.s>>>(g.P, A, d);
     *g.launches += 2;
     GF_RLAUNCH(k_mg_cols, (long long)(d.nx - 1), A, d, 1);
-    // every source (for the MOR zone) and the dike / mantle-cone sources
-    mg_compact(g, MG_PRED_SRC, A.mg_list, A.mg_i + MI_COUNT);
+    // the MOR sources and the dike / mantle-cone sources, each in serial order
+    mg_compact(g, MG_PRED_MOR, A.mg_list, A.mg_i + MI_COUNT);
     GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list, (const int *)(A.mg_i + MI_COUNT), A.mg_src);
     mg_compact(g, MG_PRED_ARC, A.mg_list2, A.mg_i + MI_COUNT2);
     GF_RLAUNCH(k_mg_src, d.E, g.P, g.C, A, d, (const int *)A.mg_list2, (const int *)(A.mg_i + MI_COUNT2), A.mg_src2);
-    GF_RLAUNCH(k_mg_migrate, 2 * ((d.E + 31) / 32) * 32, g.P, A, d); // two threads per element
+    GF_RLAUNCH(k_mg_migrate, 4 * ((d.E + 31) / 32) * 32, g.P, A, d); // four threads per element
     GF_RLAUNCH(k_mg_release, d.E, g.P, A, d);
     mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
     k_mg_markers<<<1, 1, 0, g.s>>>(g.P, g.C, A, d, max_markers);
