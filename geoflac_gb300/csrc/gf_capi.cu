@@ -712,7 +712,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &A.mg_src, (size_t)GF_MG_SRC_W * E));
         A_(dalloc(c, &A.mg_src2, (size_t)GF_MG_SRC_W * E));
         A_(dalloc(c, &A.mg_list2, E));
-        A_(dalloc(c, &A.mg_order, 5 * E));
+        A_(dalloc(c, &A.mg_order, 6 * E));
         A_(dalloc(c, &A.mg_s, 16));
         A_(dalloc(c, &A.mg_c, p->nx));
         A_(dalloc(c, &A.mg_list, E));

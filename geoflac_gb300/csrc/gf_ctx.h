@@ -107,7 +107,7 @@ struct DevArrays {
     double *fmelt, *fmelt2, *dike_added, *dike_backlog, *dike_marker_vol, *mor_marker_vol, *extrusion;
     double *mg_e, *mg_src, *mg_src2, *mg_s, *mg_c;
     int *mg_list, *mg_list2, *mg_blk, *mg_i, *mg_col;
-    int *mg_order; // melting walk order per loop (5 E)
+    int *mg_order; // melting walk order per loop, flux order, level-sorted candidates (6 E)
     uint8_t *mg_mask;
 };
 

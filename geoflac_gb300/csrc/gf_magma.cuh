@@ -364,12 +364,99 @@ __device__ void melt_walk(const DevParams &P, double *__restrict__ T, double *__
     }
 }
 
-// the four melting loops, in the reference's order
-__global__ void k_melt_serial(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int loop = 0; loop < 4; ++loop)
-        melt_walk(*Pp, A.temp, A.fmelt, A.fmelt2, A.mg_src, A.mg_order + (long long)(loop == 3 ? 4 : loop) * d.E,
-                  A.mg_i[MI_P0 + loop], loop);
+// one candidate of melting loop `loop` from the current corner temperatures
+__device__ __forceinline__ void melt_one(const DevParams &P, double *__restrict__ T, double *__restrict__ fmelt,
+                                         double *__restrict__ fmelt2, const double *__restrict__ r, int loop) {
+    long long n[4];
+    double t[4];
+    for (int q = 0; q < 4; ++q) {
+        n[q] = mg_int(r[MR_N00 + q]);
+        t[q] = T[n[q]];
+    }
+    const double tmpr = 0.25 * (t[0] + t[1] + t[2] + t[3]);
+    const double sol = r[MR_TPR + 2 * loop + 1];
+    if (!(tmpr > sol)) return;
+    const long long e = mg_int(r[MR_E]);
+    const double over = tmpr - sol;
+    if (loop == 0) fmelt2[e] = mg_pmelt(P, MG_MANT1, over, 35.0) * r[MR_TPR];
+    else if (loop == 1) fmelt[e] = mg_pmelt(P, MG_SED2, over, 50.0) * r[MR_TPR + 2];
+    else if (loop == 2) fmelt[e] = fmelt[e] + mg_pmelt(P, MG_OCEAN1, over, 20.0) * r[MR_TPR + 4];
+    else fmelt[e] = fmelt[e] + mg_pmelt(P, MG_MANT1, over, 50.0) * r[MR_TPR + 6];
+    for (int q = 0; q < 4; ++q) T[n[q]] = t[q] - over;
+}
+
+// The four melting loops, in the reference's order, by one CTA.  In a
+// loop's serial order (columns ascending; rows downwards, or upwards for
+// flux melting) an element depends on the earlier elements that share one of
+// its corners: (j-1,i), (j-1,i-1), (j,i-1), (j+1,i-1) (rows mirrored for the
+// flux loop).  Level 2i + j (2i - j for the flux loop) puts every such
+// predecessor on a lower level, and elements of one level share no corner,
+// so the levels run one after another, the elements of a level at once:
+// the serial result, bit for bit.  Above MG_LEVELS levels, or for a short
+// list, one thread walks the list instead.
+constexpr int MG_LEVELS = 4096;
+__global__ void __launch_bounds__(MG_CB) k_melt_serial(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    __shared__ int start[MG_LEVELS + 1];
+    __shared__ int fill[MG_LEVELS];
+    __shared__ int psum[MG_CB];
+    const DevParams &P = *Pp;
+    const long long nz1 = d.nz - 1;
+    const int nlev = 2 * d.nx + d.nz;
+    int *lvl = A.mg_order + 5 * d.E; // candidates sorted by level
+    for (int loop = 0; loop < 4; ++loop) {
+        const int *order = A.mg_order + (long long)(loop == 3 ? 4 : loop) * d.E;
+        const int cnt = A.mg_i[MI_P0 + loop];
+        if (cnt == 0) continue;
+        if (nlev > MG_LEVELS || cnt < 64) { // a short list: the walk is cheaper than the level sort
+            if (threadIdx.x == 0) melt_walk(P, A.temp, A.fmelt, A.fmelt2, A.mg_src, order, cnt, loop);
+            __syncthreads();
+            continue;
+        }
+        auto level = [&](int k) {
+            const long long e = mg_int(A.mg_src[(long long)order[k] * GF_MG_SRC_W + MR_E]);
+            const int i = (int)(e / nz1), j = (int)(e - (long long)i * nz1);
+            return loop < 3 ? 2 * i + j : 2 * i - j + d.nz;
+        };
+        for (int l = threadIdx.x; l < nlev; l += MG_CB) fill[l] = 0;
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += MG_CB) atomicAdd(&fill[level(k)], 1);
+        __syncthreads();
+        // exclusive scan of the level counts: each thread a contiguous run
+        const int per = (nlev + MG_CB - 1) / MG_CB, l0 = threadIdx.x * per;
+        int sum = 0;
+        for (int l = l0; l < l0 + per && l < nlev; ++l) sum += fill[l];
+        psum[threadIdx.x] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0;
+            for (int q = 0; q < MG_CB; ++q) {
+                const int v = psum[q];
+                psum[q] = acc;
+                acc += v;
+            }
+        }
+        __syncthreads();
+        int acc = psum[threadIdx.x];
+        for (int l = l0; l < l0 + per && l < nlev; ++l) {
+            start[l] = acc;
+            acc += fill[l];
+            fill[l] = 0;
+        }
+        if (threadIdx.x == MG_CB - 1) start[nlev] = cnt;
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += MG_CB) {
+            const int l = level(k);
+            lvl[start[l] + atomicAdd(&fill[l], 1)] = order[k];
+        }
+        __syncthreads();
+        for (int l = 0; l < nlev; ++l) {
+            const int s0 = start[l], s1 = start[l + 1];
+            if (s0 == s1) continue;
+            for (int k = s0 + (int)threadIdx.x; k < s1; k += MG_CB)
+                melt_one(P, A.temp, A.fmelt, A.fmelt2, A.mg_src + (long long)lvl[k] * GF_MG_SRC_W, loop);
+            __syncthreads();
+        }
+    }
 }
 
 // ---------------------------------------------------------------- fl_therm's magma part

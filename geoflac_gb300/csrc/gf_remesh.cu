@@ -1140,7 +1140,7 @@ void GfMagma::melting(const GfLaunch &g) {
     mg_compact(g, MG_PRED_MASK, A.mg_list, A.mg_i + MI_COUNT);
     GF_RLAUNCH(k_melt_prep, g.d.E, g.P, A, g.d);
     k_melt_order<<<1, MG_CB, 0, g.s>>>(A, g.d);
-    k_melt_serial<<<1, 1, 0, g.s>>>(g.P, A, g.d);
+    k_melt_serial<<<1, MG_CB, 0, g.s>>>(g.P, A, g.d);
     *g.launches += 2;
 }
 
