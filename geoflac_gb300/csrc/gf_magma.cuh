@@ -12,13 +12,16 @@
 //  * the melting loops cool an element's corners in place, so later
 //    elements see earlier ones' cooling: the elements that can melt at all
 //    (above their solidus at the start; temperatures only fall in these
-//    loops) are listed in serial order and one thread walks the list;
-//  * the weighted sums of the MOR melting zone are taken by one warp, terms
-//    computed in parallel and added in order;
+//    loops) are listed in serial order and run by corner-dependency levels
+//    (elements of one level share no corner), or walked by one thread when
+//    the list is short;
+//  * the weighted sums of the MOR melting zone are taken in serial order,
+//    terms computed in parallel, each sum by its own warp;
 //  * migration scatters many sources into many targets: each target walks
-//    the ordered source list (only the sources whose reach covers its
-//    column), inserting the reference's per-element clamp at its own serial
-//    position;
+//    the ordered lists of the sources that can reach it (dike / cone sources
+//    in its column window, MOR sources in the MOR cone), inserting the
+//    reference's per-element clamp at its own serial position, one warp per
+//    accumulated field;
 //  * new markers are numbered in serial order by one thread walking the
 //    list of elements that receive any.
 
