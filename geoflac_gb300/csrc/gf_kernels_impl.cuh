@@ -65,7 +65,9 @@ __device__ __forceinline__ void elem_corner_forces(const float dx[3][4], const f
 
 // ======================================================================
 // fl_rheol (fl_rheol.f90:4-389): one thread per element.
-template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e) {
+// tc / tv: the coordinates' and velocities' hi/lo planes in a shared-memory
+// tile (mixed path; null: read the global arrays)
+template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e, const NodePlanes *tc = nullptr, const NodePlanes *tv = nullptr) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -85,9 +87,14 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         // FP32 from the hi/lo splits: coordinates and velocities relative to
         // the quad's node 1 (each triangle's shape derivatives sum to zero,
         // so a common velocity offset drops out of the strain rates)
-        load_vel_rel(A, d, j, i, vx, vy);
         QuadF qf;
-        load_quad_rel(A, d, j, i, qf);
+        if (tv) {
+            load_rel(*tv, d, j, i, vx, vy);
+            load_rel(*tc, d, j, i, qf.x, qf.y);
+        } else {
+            load_vel_rel(A, d, j, i, vx, vy);
+            load_quad_rel(A, d, j, i, qf);
+        }
         shape_derivs_f(qf, ar, dx, dz);
     } else {
         const double *vel = A.vel;
@@ -260,7 +267,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         // not move before fl_node); shape derivatives taken again rather than
         // kept live through the stress update
         QuadF q2;
-        load_quad_rel(A, d, j, i, q2);
+        if (tc) load_rel(*tc, d, j, i, q2.x, q2.y);
+        else load_quad_rel(A, d, j, i, q2);
         float dx2[3][4], dz2[3][4];
         shape_derivs_f(q2, ar, dx2, dz2);
         elem_corner_forces(dx2, dz2, ar, sn, A.e_frc, d.E, e);
@@ -336,6 +344,73 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
     b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Mixed path: fl_rheol with the corner nodes from a shared-memory tile.  A
+// CTA's GF_THREADS consecutive elements use one contiguous range of nodes
+// (their columns and the next), the same range in each of the 8 hi/lo
+// planes (coordinates and velocities, x and z); one thread copies the 8
+// ranges with bulk asynchronous copies (each from the 16-byte boundary at or
+// below the first node, a multiple of 16 bytes long; the planes are padded
+// on the device for the rounding) onto an mbarrier, and every thread then
+// reads its corners from shared memory.  Results equal k_rheol's bit for
+// bit.  `cap`: floats per plane in shared memory.
+__device__ __forceinline__ uint32_t rt_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__global__ void __launch_bounds__(GF_THREADS, 3) k_rheol_tile(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int cap) {
+    extern __shared__ __align__(16) float rt_sm[];
+    __shared__ __align__(8) uint64_t rt_bar;
+    const long long e0 = (long long)blockIdx.x * GF_THREADS;
+    const long long e1 = e0 + GF_THREADS - 1 < d.E - 1 ? e0 + GF_THREADS - 1 : d.E - 1;
+    int j0, i0, j1, i1;
+    elem_ji(d, e0, j0, i0);
+    elem_ji(d, e1, j1, i1);
+    const long long nlo = gf_node(d, j0, i0), nhi = gf_node(d, j1 + 1, i1 + 1);
+    const float *src[8] = {A.cord_hi, A.cord_lo, A.cord_hi + d.N, A.cord_lo + d.N,
+                           A.vel_hi,  A.vel_lo,  A.vel_hi + d.N,  A.vel_lo + d.N};
+    int shift[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) shift[q] = (int)((reinterpret_cast<uintptr_t>(src[q] + nlo) & 15u) >> 2);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar)), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        uint32_t total = 0, bytes[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            bytes[q] = (uint32_t)((shift[q] + (int)(nhi - nlo + 1) + 3) & ~3) * 4u;
+            total += bytes[q];
+        }
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rt_smem(&rt_bar)), "r"(total)
+                     : "memory");
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(rt_smem(rt_sm + q * cap)),
+                         "l"(reinterpret_cast<uint64_t>(src[q] + nlo - shift[q])), "r"(bytes[q]),
+                         "r"(rt_smem(&rt_bar))
+                         : "memory");
+    }
+    __syncthreads();
+    bool ok = false;
+    for (long long it = 0; it < (1LL << 22) && !ok; ++it) {
+        uint32_t r;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(r)
+                     : "r"(rt_smem(&rt_bar)), "r"(0)
+                     : "memory");
+        ok = r != 0;
+    }
+    if (!ok) { // the copies never completed: report, no compute on stale data
+        if (threadIdx.x == 0) set_status(C, GF_ERR_TIMEOUT, (int)e0);
+        return;
+    }
+    const NodePlanes tc{rt_sm + 0 * cap + shift[0], rt_sm + 1 * cap + shift[1], rt_sm + 2 * cap + shift[2],
+                        rt_sm + 3 * cap + shift[3], nlo};
+    const NodePlanes tv{rt_sm + 4 * cap + shift[4], rt_sm + 5 * cap + shift[5], rt_sm + 6 * cap + shift[6],
+                        rt_sm + 7 * cap + shift[7], nlo};
+    b_k_rheol<float>(Pp, C, A, d, update_visc, 0, e0 + threadIdx.x, &tc, &tv);
 }
 
 // Periodic time averaging (fl_rheol.f90:393-421); mode 1 resets the sums.
@@ -1677,7 +1752,14 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int k
 
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {
     using namespace gfk;
-    GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
+    if (sizeof(R) == sizeof(float) && g.rheol_tile_cap > 0) {
+        const size_t smem = (size_t)8 * g.rheol_tile_cap * sizeof(float);
+        k_rheol_tile<<<gfk::grid_for(g.d.E), GF_THREADS, smem, g.s>>>(g.P, g.C, g.A, g.d, update_visc,
+                                                                    g.rheol_tile_cap);
+        ++*g.launches;
+    } else {
+        GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
+    }
     if (avg_mode > 0) {
         GF_LAUNCH(k_rheol_avg<R>, g.d.E, g.C, g.A, g.d, avg_mode == 2 ? 1 : 0);
         if (avg_mode == 2) {
