@@ -763,7 +763,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
                 rmax = std::max(rmax, ((i1 + 1) * c->d.nz + j1 + 1) - (i0 * c->d.nz + j0) + 1);
             }
             const long long cap = (rmax + 3 + 3) & ~3LL;
-            if (8 * cap * (long long)sizeof(float) <= 48 * 1024) c->rheol_tile_cap = (int)cap;
+            if (2 * 8 * cap * (long long)sizeof(float) <= 48 * 1024) c->rheol_tile_cap = (int)cap;
         }
         A_(dalloc(c, &A.pr_hi, E));
         A_(dalloc(c, &A.pr_lo, E));

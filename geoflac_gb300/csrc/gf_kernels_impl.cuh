@@ -346,74 +346,105 @@ template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) 
     b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// Mixed path: fl_rheol with the corner nodes from a shared-memory tile.  A
-// CTA's GF_THREADS consecutive elements use one contiguous range of nodes
+// Mixed path: fl_rheol with the corner nodes from shared-memory tiles.  A
+// tile of GF_THREADS consecutive elements uses one contiguous range of nodes
 // (their columns and the next), the same range in each of the 8 hi/lo
-// planes (coordinates and velocities, x and z); one thread copies the 8
-// ranges with bulk asynchronous copies (each from the 16-byte boundary at or
-// below the first node, a multiple of 16 bytes long; the planes are padded
-// on the device for the rounding) onto an mbarrier, and every thread then
-// reads its corners from shared memory.  Results equal k_rheol's bit for
-// bit.  `cap`: floats per plane in shared memory.
+// planes (coordinates and velocities, x and z).  Persistent CTAs walk the
+// tiles with two buffers: one thread copies the next tile's 8 ranges with
+// bulk asynchronous copies (each from the 16-byte boundary at or below the
+// first node, a multiple of 16 bytes long; the planes are padded on the
+// device for the rounding) onto that buffer's mbarrier while every thread
+// works on the current tile, reading its corners from shared memory.
+// Results equal k_rheol's bit for bit.  `cap`: floats per plane.
 __device__ __forceinline__ uint32_t rt_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__global__ void __launch_bounds__(GF_THREADS, 3) k_rheol_tile(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int cap) {
-    extern __shared__ __align__(16) float rt_sm[];
-    __shared__ __align__(8) uint64_t rt_bar;
-    const long long e0 = (long long)blockIdx.x * GF_THREADS;
+struct RtTile {
+    long long nlo, nhi;
+    int shift[8];
+};
+__device__ __forceinline__ RtTile rt_tile(const DevArrays &A, const GfDims &d, long long tile, const float *const src[8]) {
+    RtTile t;
+    const long long e0 = tile * GF_THREADS;
     const long long e1 = e0 + GF_THREADS - 1 < d.E - 1 ? e0 + GF_THREADS - 1 : d.E - 1;
     int j0, i0, j1, i1;
     elem_ji(d, e0, j0, i0);
     elem_ji(d, e1, j1, i1);
-    const long long nlo = gf_node(d, j0, i0), nhi = gf_node(d, j1 + 1, i1 + 1);
-    const float *src[8] = {A.cord_hi, A.cord_lo, A.cord_hi + d.N, A.cord_lo + d.N,
-                           A.vel_hi,  A.vel_lo,  A.vel_hi + d.N,  A.vel_lo + d.N};
-    int shift[8];
+    t.nlo = gf_node(d, j0, i0);
+    t.nhi = gf_node(d, j1 + 1, i1 + 1);
 #pragma unroll
-    for (int q = 0; q < 8; ++q) shift[q] = (int)((reinterpret_cast<uintptr_t>(src[q] + nlo) & 15u) >> 2);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar)), "r"(1));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        uint32_t total = 0, bytes[8];
+    for (int q = 0; q < 8; ++q) t.shift[q] = (int)((reinterpret_cast<uintptr_t>(src[q] + t.nlo) & 15u) >> 2);
+    return t;
+}
+// one thread: the 8 bulk copies of a tile into buffer `buf`
+__device__ __forceinline__ void rt_issue(const RtTile &t, const float *const src[8], float *buf, int cap, uint64_t *bar) {
+    uint32_t total = 0, bytes[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            bytes[q] = (uint32_t)((shift[q] + (int)(nhi - nlo + 1) + 3) & ~3) * 4u;
-            total += bytes[q];
-        }
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rt_smem(&rt_bar)), "r"(total)
-                     : "memory");
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(rt_smem(rt_sm + q * cap)),
-                         "l"(reinterpret_cast<uint64_t>(src[q] + nlo - shift[q])), "r"(bytes[q]),
-                         "r"(rt_smem(&rt_bar))
-                         : "memory");
+    for (int q = 0; q < 8; ++q) {
+        bytes[q] = (uint32_t)((t.shift[q] + (int)(t.nhi - t.nlo + 1) + 3) & ~3) * 4u;
+        total += bytes[q];
     }
-    __syncthreads();
-    bool ok = false;
-    for (long long it = 0; it < (1LL << 22) && !ok; ++it) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); // earlier reads of buf before the copies' writes
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rt_smem(bar)), "r"(total) : "memory");
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(rt_smem(buf + q * cap)), "l"(reinterpret_cast<uint64_t>(src[q] + t.nlo - t.shift[q])),
+                     "r"(bytes[q]), "r"(rt_smem(bar))
+                     : "memory");
+}
+__device__ __forceinline__ bool rt_wait(uint64_t *bar, uint32_t parity) {
+    for (long long it = 0; it < (1LL << 22); ++it) {
         uint32_t r;
         asm volatile("{\n\t.reg .pred p;\n\t"
                      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}"
                      : "=r"(r)
-                     : "r"(rt_smem(&rt_bar)), "r"(0)
+                     : "r"(rt_smem(bar)), "r"(parity)
                      : "memory");
-        ok = r != 0;
+        if (r) return true;
     }
-    if (!ok) { // the copies never completed: report, no compute on stale data
-        if (threadIdx.x == 0) set_status(C, GF_ERR_TIMEOUT, (int)e0);
-        return;
+    return false;
+}
+__global__ void __launch_bounds__(GF_THREADS, 3) k_rheol_tile(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int cap) {
+    extern __shared__ __align__(16) float rt_sm[];
+    __shared__ __align__(8) uint64_t rt_bar[2];
+    const long long ntile = (d.E + GF_THREADS - 1) / GF_THREADS;
+    if ((long long)blockIdx.x >= ntile) return;
+    const float *const src[8] = {A.cord_hi, A.cord_lo, A.cord_hi + d.N, A.cord_lo + d.N,
+                                 A.vel_hi,  A.vel_lo,  A.vel_hi + d.N,  A.vel_lo + d.N};
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar[0])), "r"(1));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar[1])), "r"(1));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        rt_issue(rt_tile(A, d, blockIdx.x, src), src, rt_sm, cap, &rt_bar[0]);
     }
-    const NodePlanes tc{rt_sm + 0 * cap + shift[0], rt_sm + 1 * cap + shift[1], rt_sm + 2 * cap + shift[2],
-                        rt_sm + 3 * cap + shift[3], nlo};
-    const NodePlanes tv{rt_sm + 4 * cap + shift[4], rt_sm + 5 * cap + shift[5], rt_sm + 6 * cap + shift[6],
-                        rt_sm + 7 * cap + shift[7], nlo};
-    b_k_rheol<float>(Pp, C, A, d, update_visc, 0, e0 + threadIdx.x, &tc, &tv);
+    __syncthreads();
+    int k = 0;
+    for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x, ++k) {
+        const int b = k & 1;
+        const long long next = tile + gridDim.x;
+        // the other buffer was read by every thread before the last barrier
+        if (threadIdx.x == 0 && next < ntile)
+            rt_issue(rt_tile(A, d, next, src), src, rt_sm + (b ^ 1) * 8 * cap, cap, &rt_bar[b ^ 1]);
+        const RtTile t = rt_tile(A, d, tile, src);
+        if (!rt_wait(&rt_bar[b], (uint32_t)((k >> 1) & 1))) { // the copies never completed
+            if (threadIdx.x == 0) {
+                set_status(C, GF_ERR_TIMEOUT, (int)(tile * GF_THREADS));
+                if (next < ntile) rt_wait(&rt_bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1)); // the next tile's copies
+            }
+            return;
+        }
+        const float *buf = rt_sm + b * 8 * cap;
+        const NodePlanes tc{buf + 0 * cap + t.shift[0], buf + 1 * cap + t.shift[1], buf + 2 * cap + t.shift[2],
+                            buf + 3 * cap + t.shift[3], t.nlo};
+        const NodePlanes tv{buf + 4 * cap + t.shift[4], buf + 5 * cap + t.shift[5], buf + 6 * cap + t.shift[6],
+                            buf + 7 * cap + t.shift[7], t.nlo};
+        b_k_rheol<float>(Pp, C, A, d, update_visc, 0, tile * GF_THREADS + threadIdx.x, &tc, &tv);
+        __syncthreads();
+    }
+    // every copy was waited for: `next` is issued only when it is the next
+    // iteration's tile
 }
 
-// Periodic time averaging (fl_rheol.f90:393-421); mode 1 resets the sums.
 template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset, long long e) {
     if (e >= d.E) return;
     R *se2sr = (R *)A.se2sr;
@@ -1753,9 +1784,17 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int k
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float) && g.rheol_tile_cap > 0) {
-        const size_t smem = (size_t)8 * g.rheol_tile_cap * sizeof(float);
-        k_rheol_tile<<<gfk::grid_for(g.d.E), GF_THREADS, smem, g.s>>>(g.P, g.C, g.A, g.d, update_visc,
-                                                                    g.rheol_tile_cap);
+        const size_t smem = (size_t)2 * 8 * g.rheol_tile_cap * sizeof(float); // two buffers
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (sms <= 0) sms = 1;
+        }
+        const long long ntile = (g.d.E + GF_THREADS - 1) / GF_THREADS;
+        const unsigned grid = (unsigned)(ntile < 3LL * sms ? ntile : 3LL * sms);
+        k_rheol_tile<<<grid, GF_THREADS, smem, g.s>>>(g.P, g.C, g.A, g.d, update_visc, g.rheol_tile_cap);
         ++*g.launches;
     } else {
         GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
