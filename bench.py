@@ -34,7 +34,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "element-steps/s on 1 GB300: FP64 vs mixed vs batched; surrogate sweep speedup @err"
-WORKLOAD = "extension_1000x300: two-phase extension, 1000x300 quads (300,000 elements, 301,301 nodes), 1000 km x 300 km"
+WORKLOAD = ("extension_1000x300: two-phase extension, 1000x300 quads (300,000 elements, 301,301 nodes), "
+            "1000 km x 300 km, 25 markers per element")
+MARKERS_PER_SIDE = 5  # 5 x 5 = 25 markers per element
+
+
+def bench_config(ws: int) -> dict:
+    """The `config` object of both arms' JSON lines (the same workload)."""
+    return {"workload": WORKLOAD, "mode": "fp64", "elements": 1000 * 300, "nodes": 1001 * 301,
+            "markers_per_element": MARKERS_PER_SIDE ** 2, "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 between timed steps (512 MiB buffer written; host arm: n/a)"}
 
 
 def _dist():
@@ -164,7 +173,7 @@ def _make_model(inp: str, mode: str):
     from geoflac_gb300 import new_state
     from geoflac_gb300.flac import Flac
 
-    p, c, s = new_state(inp)
+    p, c, s = new_state(inp, markers_per_side=MARKERS_PER_SIDE)
     bufs = []
 
     def pinned(nbytes):
@@ -365,9 +374,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * fp["t"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .inp model)",
-        "config": {"workload": WORKLOAD, "mode": "fp64", "elements": E, "nodes": 1001 * 301,
-                   "markers_per_element": 9, "parallelism": f"replicas x{ws}",
-                   "l2": "512 MiB buffer written between timed steps"},
+        "config": bench_config(ws),
         "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
                   "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes",
                   "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup,
@@ -640,7 +647,7 @@ def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
     from oracle.oracle import Oracle
 
     n = threads or os.cpu_count() or 1
-    p, c, s = new_state(inp)
+    p, c, s = new_state(inp, markers_per_side=MARKERS_PER_SIDE)
     o = Oracle(p, c, s, threads=n)
     o.finish_setflac()
     o.step(1)
@@ -662,7 +669,7 @@ def run_reference(args):
     d = tempfile.mkdtemp(prefix="gfbench")
     inp = inpgen.extension_1000x300().write(os.path.join(d, "extension_1000x300.inp"))
     n = os.cpu_count() or 1
-    p, c, s = new_state(inp)
+    p, c, s = new_state(inp, markers_per_side=MARKERS_PER_SIDE)
     o = Oracle(p, c, s, threads=n)
     o.finish_setflac()
     o.step(args.warmup)
@@ -676,7 +683,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded .inp model)",
-        "config": {"workload": WORKLOAD, "mode": "fp64", "elements": E},
+        "config": bench_config(ws),
         "cpu_baseline": {"value": v, "unit": "element-steps/s", "cores": n, "kind": "port",
                          "sample": f"{args.steps} full FLAC steps of the 1000x300 mesh, {n} OpenMP threads"},
         "e2e": {"value": v, "unit": "element-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -52,7 +52,6 @@ struct gf_ctx {
     int sweeps = 0; // cap on the thermal sweeps (0: library cap)
     int sync = 1;
     int frc_valid = 0; // mixed: e_frc holds the corner forces of the current stresses and mesh
-    int rheol_tile_cap = 0; // mixed: node-plane floats of the tiled fl_rheol (0: untiled)
 };
 
 namespace {
@@ -166,7 +165,6 @@ GfLaunch launch_of(gf_ctx *c) {
     g.arc_rate = 1.0 - c->p.ratio_mantle_mzone - c->p.ratio_crust_mzone;
     g.idt_scale = c->p.idt_scale;
     g.advance_time = 0;
-    g.rheol_tile_cap = c->rheol_tile_cap;
     return g;
 }
 
@@ -743,28 +741,10 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     }
     if (mode == GF_MODE_MIXED) {
         A_(dalloc(c, &c->staging, 16 * E));
-        // 8 floats of padding: the tiled fl_rheol copies whole 16-byte
-        // blocks, up to 3 floats past a plane's last node
-        A_(dalloc(c, &A.cord_hi, 2 * N + 8));
-        A_(dalloc(c, &A.cord_lo, 2 * N + 8));
-        A_(dalloc(c, &A.vel_hi, 2 * N + 8));
-        A_(dalloc(c, &A.vel_lo, 2 * N + 8));
-        // GEOFLAC_RHEOL_TILE=1 selects the tiled fl_rheol (corner nodes
-        // staged in shared memory; slower than the untiled kernel on GB300,
-        // whose loads all stay in flight at once): its node range per CTA
-        // (GF_THREADS consecutive elements), rounded for the 16-byte copies
-        const char *tile_env = std::getenv("GEOFLAC_RHEOL_TILE");
-        if (tile_env && tile_env[0] == '1') {
-            long long rmax = 0;
-            for (long long e0 = 0; e0 < E; e0 += GF_THREADS) {
-                const long long e1 = std::min(E - 1, e0 + GF_THREADS - 1);
-                const long long i0 = e0 / (c->d.nz - 1), j0 = e0 - i0 * (c->d.nz - 1);
-                const long long i1 = e1 / (c->d.nz - 1), j1 = e1 - i1 * (c->d.nz - 1);
-                rmax = std::max(rmax, ((i1 + 1) * c->d.nz + j1 + 1) - (i0 * c->d.nz + j0) + 1);
-            }
-            const long long cap = (rmax + 3 + 3) & ~3LL;
-            if (2 * 8 * cap * (long long)sizeof(float) <= 48 * 1024) c->rheol_tile_cap = (int)cap;
-        }
+        A_(dalloc(c, &A.cord_hi, 2 * N));
+        A_(dalloc(c, &A.cord_lo, 2 * N));
+        A_(dalloc(c, &A.vel_hi, 2 * N));
+        A_(dalloc(c, &A.vel_lo, 2 * N));
         A_(dalloc(c, &A.pr_hi, E));
         A_(dalloc(c, &A.pr_lo, E));
         A_(dalloc(c, &A.e_frc, 16 * E));

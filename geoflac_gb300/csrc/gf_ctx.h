@@ -123,7 +123,6 @@ struct GfLaunch {
     int idt_scale;   // host copy of the mass-scaling mode (selects launches)
     int advance_time; // fold par.f90's time += dt into the step's last kernel
     double arc_rate;  // arc extrusion rate 1 - ratio_mantle_mzone - ratio_crust_mzone (diff_topo)
-    int rheol_tile_cap; // mixed: floats per node plane of k_rheol_tile's shared-memory tile (0: k_rheol)
 };
 
 // Launchers, one set per precision (template instantiated in its own TU).

@@ -99,28 +99,6 @@ __device__ __forceinline__ void quad_nodes(const GfDims &d, int j, int i, long l
     n[3] = n[2] + 1;
 }
 
-// The four hi/lo planes of a split node field (x and z) and the node index
-// that maps to entry 0 (0 for the global arrays; the first node of a
-// shared-memory tile).
-struct NodePlanes {
-    const float *xh, *xl, *yh, *yl;
-    long long off;
-};
-
-__device__ __forceinline__ void load_rel(const NodePlanes &p, const GfDims &d, int j, int i, float x[4], float y[4]) {
-    long long n[4];
-    quad_nodes(d, j, i, n);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) n[k] -= p.off;
-    x[0] = 0.0f;
-    y[0] = 0.0f;
-#pragma unroll
-    for (int k = 1; k < 4; ++k) {
-        x[k] = hl_diff(p.xh, p.xl, n[k], n[0]);
-        y[k] = hl_diff(p.yh, p.yl, n[k], n[0]);
-    }
-}
-
 __device__ __forceinline__ void load_quad_rel(const DevArrays &A, const GfDims &d, int j, int i, QuadF &q) {
     long long n[4];
     quad_nodes(d, j, i, n);

@@ -65,9 +65,7 @@ __device__ __forceinline__ void elem_corner_forces(const float dx[3][4], const f
 
 // ======================================================================
 // fl_rheol (fl_rheol.f90:4-389): one thread per element.
-// tc / tv: the coordinates' and velocities' hi/lo planes in a shared-memory
-// tile (mixed path; null: read the global arrays)
-template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e, const NodePlanes *tc = nullptr, const NodePlanes *tv = nullptr) {
+template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -88,13 +86,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         // the quad's node 1 (each triangle's shape derivatives sum to zero,
         // so a common velocity offset drops out of the strain rates)
         QuadF qf;
-        if (tv) {
-            load_rel(*tv, d, j, i, vx, vy);
-            load_rel(*tc, d, j, i, qf.x, qf.y);
-        } else {
-            load_vel_rel(A, d, j, i, vx, vy);
-            load_quad_rel(A, d, j, i, qf);
-        }
+        load_vel_rel(A, d, j, i, vx, vy);
+        load_quad_rel(A, d, j, i, qf);
         shape_derivs_f(qf, ar, dx, dz);
     } else {
         const double *vel = A.vel;
@@ -267,8 +260,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         // not move before fl_node); shape derivatives taken again rather than
         // kept live through the stress update
         QuadF q2;
-        if (tc) load_rel(*tc, d, j, i, q2.x, q2.y);
-        else load_quad_rel(A, d, j, i, q2);
+        load_quad_rel(A, d, j, i, q2);
         float dx2[3][4], dz2[3][4];
         shape_derivs_f(q2, ar, dx2, dz2);
         elem_corner_forces(dx2, dz2, ar, sn, A.e_frc, d.E, e);
@@ -344,105 +336,6 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
     b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-// Mixed path: fl_rheol with the corner nodes from shared-memory tiles.  A
-// tile of GF_THREADS consecutive elements uses one contiguous range of nodes
-// (their columns and the next), the same range in each of the 8 hi/lo
-// planes (coordinates and velocities, x and z).  Persistent CTAs walk the
-// tiles with two buffers: one thread copies the next tile's 8 ranges with
-// bulk asynchronous copies (each from the 16-byte boundary at or below the
-// first node, a multiple of 16 bytes long; the planes are padded on the
-// device for the rounding) onto that buffer's mbarrier while every thread
-// works on the current tile, reading its corners from shared memory.
-// Results equal k_rheol's bit for bit.  `cap`: floats per plane.
-__device__ __forceinline__ uint32_t rt_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-struct RtTile {
-    long long nlo, nhi;
-    int shift[8];
-};
-__device__ __forceinline__ RtTile rt_tile(const DevArrays &A, const GfDims &d, long long tile, const float *const src[8]) {
-    RtTile t;
-    const long long e0 = tile * GF_THREADS;
-    const long long e1 = e0 + GF_THREADS - 1 < d.E - 1 ? e0 + GF_THREADS - 1 : d.E - 1;
-    int j0, i0, j1, i1;
-    elem_ji(d, e0, j0, i0);
-    elem_ji(d, e1, j1, i1);
-    t.nlo = gf_node(d, j0, i0);
-    t.nhi = gf_node(d, j1 + 1, i1 + 1);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) t.shift[q] = (int)((reinterpret_cast<uintptr_t>(src[q] + t.nlo) & 15u) >> 2);
-    return t;
-}
-// one thread: the 8 bulk copies of a tile into buffer `buf`
-__device__ __forceinline__ void rt_issue(const RtTile &t, const float *const src[8], float *buf, int cap, uint64_t *bar) {
-    uint32_t total = 0, bytes[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        bytes[q] = (uint32_t)((t.shift[q] + (int)(t.nhi - t.nlo + 1) + 3) & ~3) * 4u;
-        total += bytes[q];
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); // earlier reads of buf before the copies' writes
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rt_smem(bar)), "r"(total) : "memory");
-#pragma unroll
-    for (int q = 0; q < 8; ++q)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(rt_smem(buf + q * cap)), "l"(reinterpret_cast<uint64_t>(src[q] + t.nlo - t.shift[q])),
-                     "r"(bytes[q]), "r"(rt_smem(bar))
-                     : "memory");
-}
-__device__ __forceinline__ bool rt_wait(uint64_t *bar, uint32_t parity) {
-    for (long long it = 0; it < (1LL << 22); ++it) {
-        uint32_t r;
-        asm volatile("{\n\t.reg .pred p;\n\t"
-                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(r)
-                     : "r"(rt_smem(bar)), "r"(parity)
-                     : "memory");
-        if (r) return true;
-    }
-    return false;
-}
-__global__ void __launch_bounds__(GF_THREADS, 3) k_rheol_tile(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int cap) {
-    extern __shared__ __align__(16) float rt_sm[];
-    __shared__ __align__(8) uint64_t rt_bar[2];
-    const long long ntile = (d.E + GF_THREADS - 1) / GF_THREADS;
-    if ((long long)blockIdx.x >= ntile) return;
-    const float *const src[8] = {A.cord_hi, A.cord_lo, A.cord_hi + d.N, A.cord_lo + d.N,
-                                 A.vel_hi,  A.vel_lo,  A.vel_hi + d.N,  A.vel_lo + d.N};
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar[0])), "r"(1));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(rt_smem(&rt_bar[1])), "r"(1));
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        rt_issue(rt_tile(A, d, blockIdx.x, src), src, rt_sm, cap, &rt_bar[0]);
-    }
-    __syncthreads();
-    int k = 0;
-    for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x, ++k) {
-        const int b = k & 1;
-        const long long next = tile + gridDim.x;
-        // the other buffer was read by every thread before the last barrier
-        if (threadIdx.x == 0 && next < ntile)
-            rt_issue(rt_tile(A, d, next, src), src, rt_sm + (b ^ 1) * 8 * cap, cap, &rt_bar[b ^ 1]);
-        const RtTile t = rt_tile(A, d, tile, src);
-        if (!rt_wait(&rt_bar[b], (uint32_t)((k >> 1) & 1))) { // the copies never completed
-            if (threadIdx.x == 0) {
-                set_status(C, GF_ERR_TIMEOUT, (int)(tile * GF_THREADS));
-                if (next < ntile) rt_wait(&rt_bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1)); // the next tile's copies
-            }
-            return;
-        }
-        const float *buf = rt_sm + b * 8 * cap;
-        const NodePlanes tc{buf + 0 * cap + t.shift[0], buf + 1 * cap + t.shift[1], buf + 2 * cap + t.shift[2],
-                            buf + 3 * cap + t.shift[3], t.nlo};
-        const NodePlanes tv{buf + 4 * cap + t.shift[4], buf + 5 * cap + t.shift[5], buf + 6 * cap + t.shift[6],
-                            buf + 7 * cap + t.shift[7], t.nlo};
-        b_k_rheol<float>(Pp, C, A, d, update_visc, 0, tile * GF_THREADS + threadIdx.x, &tc, &tv);
-        __syncthreads();
-    }
-    // every copy was waited for: `next` is issued only when it is the next
-    // iteration's tile
 }
 
 template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset, long long e) {
@@ -1783,22 +1676,7 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int k
 
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {
     using namespace gfk;
-    if (sizeof(R) == sizeof(float) && g.rheol_tile_cap > 0) {
-        const size_t smem = (size_t)2 * 8 * g.rheol_tile_cap * sizeof(float); // two buffers
-        static int sms = 0;
-        if (sms == 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (sms <= 0) sms = 1;
-        }
-        const long long ntile = (g.d.E + GF_THREADS - 1) / GF_THREADS;
-        const unsigned grid = (unsigned)(ntile < 3LL * sms ? ntile : 3LL * sms);
-        k_rheol_tile<<<grid, GF_THREADS, smem, g.s>>>(g.P, g.C, g.A, g.d, update_visc, g.rheol_tile_cap);
-        ++*g.launches;
-    } else {
-        GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
-    }
+    GF_LAUNCH(k_rheol<R>, g.d.E, g.P, g.C, g.A, g.d, update_visc, 0);
     if (avg_mode > 0) {
         GF_LAUNCH(k_rheol_avg<R>, g.d.E, g.C, g.A, g.d, avg_mode == 2 ? 1 : 0);
         if (avg_mode == 2) {

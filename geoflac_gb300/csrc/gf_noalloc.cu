@@ -12,20 +12,28 @@
 // to a fixed array compiled into this library instead of context memory.
 //
 // The array g_min_angle_scratch below is that scratch (65,792 bytes):
-//   bytes   0..3    completion ticket (unsigned int) -- must be zero when a
-//                   launch starts; the module loads it as zero and the last
-//                   block of every launch sets it back to zero
-//   bytes   8..15   the result (double), overwritten by every call
+//   bytes   0..3    completion ticket (unsigned int)
+//   bytes   8..15   the result (double)
 //   bytes 256..     one partial minimum per block, overwritten by every call
-// Every call shares it: two calls in flight at the same time on one device
-// (different streams or host threads) corrupt each other's ticket, partials
-// and result.  Callers serialise them (one stream, or wait between calls).
+// Before each launch the call clears the ticket and sets the result to a NaN
+// (two cudaMemsetAsync on the caller's stream; they allocate nothing), and
+// the last block of the launch writes the minimum there.  A result that is
+// still NaN after the launch (the last block never ran) is an error, never a
+// stale angle.  Every call shares the array: two calls in flight at the same
+// time on one device (different streams or host threads) corrupt each
+// other's ticket, partials and result.  Callers serialise them (one stream,
+// or wait between calls).
 //
-// Its device address is looked up once per device, on the first call made
-// while that device is current; make that first call before any stream
-// capture begins.
+// The array's device address is looked up once per CUDA context (a module
+// loaded into a caller-made driver context has its own copy of the array),
+// on the first call made while that context is current.  Each call ends with
+// a cudaStreamSynchronize and a copy into host memory, so it cannot be made
+// while its stream is being captured into a graph.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <math.h>
 
 #include <mutex>
 
@@ -35,7 +43,7 @@
 #define GF_MA_THREADS 256
 #define GF_MA_MAX_BLOCKS 8192 // at most 8192 * 256 = 2,097,152 elements
 #define GF_MA_HEADER 32       // doubles ahead of the partials (256 bytes)
-#define GF_MA_MAX_DEVICES 64
+#define GF_MA_MAX_SLOTS 64     // contexts whose scratch address is cached
 
 static __device__ __align__(256) double g_min_angle_scratch[GF_MA_HEADER + GF_MA_MAX_BLOCKS];
 
@@ -107,20 +115,53 @@ __global__ void __launch_bounds__(GF_MA_THREADS) k_min_angle_scratch(const doubl
 }
 
 std::mutex g_setup_mu;
-double *g_scratch_ptr[GF_MA_MAX_DEVICES] = {};
+struct ScratchSlot {
+    CUcontext ctx;
+    int dev;
+    double *ptr;
+};
+ScratchSlot g_slots[GF_MA_MAX_SLOTS] = {};
+int g_nslots = 0;
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+bool g_ctx_fn_looked_up = false;
 
-// Device address of the scratch array on the current device (looked up once).
-int scratch_of_current_device(double **out) {
+// Current driver context (nullptr when the driver entry point is unavailable:
+// the cache is then keyed by the device alone).  Caller holds g_setup_mu.
+CUcontext current_context() {
+    if (!g_ctx_fn_looked_up) {
+        g_ctx_fn_looked_up = true;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+    }
+    CUcontext c = nullptr;
+    if (g_ctx_get_current && g_ctx_get_current(&c) != CUDA_SUCCESS) c = nullptr;
+    return c;
+}
+
+// Device address of the scratch array in the current context (looked up
+// once per context with cudaGetSymbolAddress).
+int scratch_of_current_context(double **out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return GF_ERR_CUDA;
-    if (dev < 0 || dev >= GF_MA_MAX_DEVICES) return GF_ERR_ARG;
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        double *ptr = nullptr;
-        if (cudaGetSymbolAddress((void **)&ptr, g_min_angle_scratch) != cudaSuccess || !ptr) return GF_ERR_CUDA;
-        g_scratch_ptr[dev] = ptr;
-    }
-    *out = g_scratch_ptr[dev];
+    CUcontext ctx = current_context();
+    for (int k = 0; k < g_nslots; ++k)
+        if (g_slots[k].ctx == ctx && g_slots[k].dev == dev) {
+            *out = g_slots[k].ptr;
+            return GF_OK;
+        }
+    if (g_nslots == GF_MA_MAX_SLOTS) return GF_ERR_LIMIT;
+    double *ptr = nullptr;
+    if (cudaGetSymbolAddress((void **)&ptr, g_min_angle_scratch) != cudaSuccess || !ptr) return GF_ERR_CUDA;
+    // the lookup may have made the runtime's primary context current (no
+    // context was current before it): key the address on the context now set
+    ctx = current_context();
+    g_slots[g_nslots++] = ScratchSlot{ctx, dev, ptr};
+    *out = ptr;
     return GF_OK;
 }
 
@@ -132,15 +173,20 @@ extern "C" int gf_min_angle_noalloc(const double *d_cord, int nx, int nz, void *
     long long blocks = (E + GF_MA_THREADS - 1) / GF_MA_THREADS;
     if (blocks > GF_MA_MAX_BLOCKS) return GF_ERR_LIMIT;
     double *scratch = nullptr;
-    int rc = scratch_of_current_device(&scratch);
+    int rc = scratch_of_current_context(&scratch);
     if (rc != GF_OK) return rc;
     GfDims d{nx, nz, 0, (long long)nx * nz, E};
     cudaStream_t s = (cudaStream_t)stream;
+    // ticket = 0 and result = NaN (all bits set) before the launch, so that
+    // neither an earlier aborted launch nor the previous call's result leaks
+    if (cudaMemsetAsync(scratch, 0, sizeof(double), s) != cudaSuccess) return GF_ERR_CUDA;
+    if (cudaMemsetAsync(scratch + 1, 0xff, sizeof(double), s) != cudaSuccess) return GF_ERR_CUDA;
     k_min_angle_scratch<<<(unsigned)blocks, GF_MA_THREADS, 0, s>>>(d_cord, d, scratch);
     if (cudaGetLastError() != cudaSuccess) return GF_ERR_CUDA;
     double a = 0.0;
     if (cudaMemcpyAsync(&a, scratch + 1, sizeof a, cudaMemcpyDeviceToHost, s) != cudaSuccess) return GF_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return GF_ERR_CUDA;
+    if (isnan(a)) return GF_ERR_CUDA; // the launch ended before its last block folded the partials
     *min_angle = a;
     return GF_OK;
 }

@@ -369,8 +369,11 @@ void init_marker(S &s) {
                 double ry = gf_myrandom(iseed);
                 rx = 0.5 - rx;
                 ry = 0.5 - ry;
-                double ddx = dx * rx / 3;
-                double ddy = dy * ry / 3;
+                // the reference's jitter is a third of the element (one
+                // point spacing for its 3 x 3 pattern); m x m points keep it
+                // at one spacing, dx / m
+                double ddx = dx * rx / ms;
+                double ddy = dy * ry / ms;
                 double xx = px[l] + ddx;
                 double yy = py[l] + ddy;
                 for (int n = 0; n < p.nzone_age; ++n) {

@@ -357,10 +357,15 @@ const char *gf_strerror(int code);
  * that runtime and cudaFree stalls the whole device.  Allocates nothing: its
  * scratch is a fixed 65,792-byte array inside this library, so at most
  * 2,097,152 elements ((nx-1)*(nz-1)); larger meshes return GF_ERR_LIMIT.
- * The first call on each device looks up that array's address: make it
- * before any stream capture begins.  All calls share the array, so calls
- * must not overlap in time on one device (serialise them on one stream).
- * Runs on `stream` (a cudaStream_t; NULL = default stream) and waits for it.
+ * The first call in each CUDA context looks up that array's address (a
+ * caller-made driver context holds its own copy of the array).  All calls
+ * share the array, so calls must not overlap in time on one device
+ * (serialise them on one stream); each call clears the array's completion
+ * ticket and result before its launch and returns GF_ERR_CUDA, not a stale
+ * angle, if the launch did not finish the result.  Runs on `stream` (a
+ * cudaStream_t; NULL = default stream) and synchronises it, copying the
+ * result into host memory: it cannot be called while that stream is being
+ * captured into a CUDA graph.
  * No reference counterpart (itest_mesh works on the host's module arrays). */
 int gf_min_angle_noalloc(const double *d_cord, int nx, int nz, void *stream, double *min_angle);
 

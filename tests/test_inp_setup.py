@@ -98,24 +98,109 @@ def test_setflac_host_state(workdir):
     assert np.allclose(s["area"], 1.0 / (5e3 * 5e3))
 
 
-def test_marker_lcg_matches_published_recurrence():
-    """myrandom_mod.f90: iseed = mod(8121*iseed + 28411, 134456)."""
-    seeds = []
-    k = 0
-    for _ in range(5):
-        k = (8121 * (k % 134456) + 28411) % 134456
-        seeds.append(k / 134456)
-    assert seeds[0] == 28411 / 134456
-    assert all(0 <= v < 1 for v in seeds)
+def _myrandom(seed):
+    """myrandom_mod.f90:9-19: iseed = mod(8121*mod(iseed,134456) + 28411, 134456), r = iseed/134456."""
+    seed = seed % 134456
+    seed = (8121 * seed + 28411) % 134456
+    return seed, seed / 134456
 
 
-def test_winkler_pisos(workdir):
-    """nyhydro = 2: pisos is the lithostatic pressure at the base of the last
-    column (init_stress.f90:400-403)."""
+def _marker_xy(s, ids):
+    """marker2xy (bar2euler.f90:73-117) in numpy: positions of markers `ids`
+    (1-based) from their triangle and barycentric coordinates."""
+    cord = s["cord"]
+    nz1 = cord.shape[0] - 1
+    n = s["mark_ntriag"][ids - 1].astype(np.int64)
+    k = (n - 1) % 2 + 1
+    jj = ((n - k) // 2) % nz1
+    ii = (n - k) // 2 // nz1
+    a1, a2 = s["mark_a1"][ids - 1], s["mark_a2"][ids - 1]
+    a3 = 1.0 - a1 - a2
+    i1 = np.where(k == 1, ii, ii + 1)
+    j2, i2 = jj + 1, ii
+    j3 = np.where(k == 1, jj, jj + 1)
+    i3 = ii + 1
+    x = cord[jj, i1, 0] * a1 + cord[j2, i2, 0] * a2 + cord[j3, i3, 0] * a3
+    y = cord[jj, i1, 1] * a1 + cord[j2, i2, 1] * a2 + cord[j3, i3, 1] * a3
+    return x, y
+
+
+@pytest.mark.parametrize("ms", [3, 5])
+def test_marker_positions_follow_the_lcg_chain(workdir, ms):
+    """init_marker.f90:30-128 restated in numpy for the first mesh column:
+    the serial LCG chain (seed += i + j per element, two draws per point),
+    the point pattern (the reference's 1/6-1/2-5/6 weights for 3 x 3; the
+    same construction at (2m+1)/(2 ms) for ms x ms) and a jitter of one point
+    spacing; the product's start-up markers sit at these positions, in this
+    order, with the layer phase of their depth."""
+    m = inpgen.extension_60x20()
+    p, c, s = new_state(m.write(str(workdir / f"lcg{ms}.inp")), markers_per_side=ms)
+    cord = s["cord"]
+    if ms == 3:
+        w1 = np.array([0.1666666666666666666666, 0.5, 0.8333333333333333333333])
+        w0 = np.array([0.8333333333333333333333, 0.5, 0.1666666666666666666666])
+    else:
+        w1 = (2.0 * np.arange(ms) + 1.0) / (2.0 * ms)
+        w0 = 1.0 - w1
+    seed = 0
+    i = 0
+    for j in range(p.nz - 1):
+        ax = cord[j, i, 0] * w0 + cord[j + 1, i, 0] * w1
+        ay = cord[j, i, 1] * w0 + cord[j + 1, i, 1] * w1
+        bx = cord[j, i + 1, 0] * w0 + cord[j + 1, i + 1, 0] * w1
+        by = cord[j, i + 1, 1] * w0 + cord[j + 1, i + 1, 1] * w1
+        px = (ax[:, None] * w0[None, :] + bx[:, None] * w1[None, :]).ravel()
+        py = (ay[:, None] * w0[None, :] + by[:, None] * w1[None, :]).ravel()
+        dx = cord[j, i + 1, 0] - cord[j, i, 0]
+        dy = cord[j + 1, i, 1] - cord[j, i, 1]
+        seed = seed + (i + 1) + (j + 1)
+        xs, ys = [], []
+        for q in range(ms * ms):
+            seed, rx = _myrandom(seed)
+            seed, ry = _myrandom(seed)
+            xs.append(px[q] + dx * (0.5 - rx) / ms)
+            ys.append(py[q] + dy * (0.5 - ry) / ms)
+        ids = s["mark_id_elem"][:ms * ms, j, i]
+        assert s["nmark_elem"][j, i] == ms * ms
+        x, y = _marker_xy(s, ids)
+        assert np.allclose(x, xs, rtol=0, atol=1e-6) and np.allclose(y, ys, rtol=0, atol=1e-6), (j, i)
+        # crust above 30 km depth, mantle below (the age zone's layer)
+        expect_ph = np.where(np.array(ys) * -1e-3 < 30.0, 2, 4)
+        assert np.array_equal(s["mark_phase"][ids - 1], expect_ph)
+    # the draws are the recurrence's: the first is 8121 * 2 + 28411
+    assert _myrandom(2) == ((8121 * 2 + 28411) % 134456, ((8121 * 2 + 28411) % 134456) / 134456)
+
+
+def test_hydrostatic_prestress_and_winkler_pisos(workdir):
+    """init_stress.f90:16-51 restated in numpy from the start-up mesh,
+    phases and temperatures: every column's pressure at each element centre
+    (oceanic columns under 8 km of water) is the element's -sxx = -szz = -syy,
+    and with nyhydro = 2 pisos is the pressure at the base of the last column."""
     p, c, s = new_state(inpgen.convergence_60x15().write(str(workdir / "c3.inp")))
-    rho_g_h = 0.0
-    assert p.pisos > 0
-    col = s["stress0"][:, -1, 1, 0]
-    # pisos exceeds the pressure at the centre of the deepest element
-    assert p.pisos > -col[-1]
-    assert rho_g_h == 0.0
+    assert p.nyhydro == 2
+    cord, temp, iph = s["cord"], s["temp"], s["iphase"]
+    den = np.array([p.den[k] for k in range(p.nphase)])
+    alfa = np.array([p.alfa[k] for k in range(p.nphase)])
+    beta = np.array([p.beta[k] for k in range(p.nphase)])
+    st = s["stress0"]
+    pisos = 0.0
+    for i in range(p.nx - 1):
+        rogh = -1030.0 * p.g * 8.0e3 if iph[0, i] in (3, 7) else 0.0
+        for j in range(p.nz - 1):
+            ph = iph[j, i] - 1
+            tmpr = 0.25 * (temp[j, i] + temp[j + 1, i] + temp[j, i + 1] + temp[j + 1, i + 1])
+            densT = den[ph] * (1 - alfa[ph] * tmpr)
+            dh = 0.5 * ((cord[j, i, 1] - cord[j + 1, i, 1]) + (cord[j, i + 1, 1] - cord[j + 1, i + 1, 1]))
+            dPT = densT * p.g * dh
+            dP = dPT * (1 - beta[ph] * rogh) / (1 + beta[ph] / 2 * dPT)
+            press = rogh + 0.5 * dP
+            for k in range(4):
+                assert st[j, i, 0, k] == pytest.approx(-press, rel=1e-13)
+                assert st[j, i, 1, k] == pytest.approx(-press, rel=1e-13)
+                assert st[j, i, 2, k] == 0.0
+                assert st[j, i, 3, k] == pytest.approx(-press, rel=1e-13)
+            rogh = rogh + dP
+        if i == p.nx - 2:
+            pisos = rogh + p.extra_pres
+    assert pisos > 0
+    assert p.pisos == pytest.approx(pisos, rel=1e-13)

@@ -100,25 +100,3 @@ def test_mixed_long_run_observables(workdir, name):
         assert err[k] <= max(bound, 3.0 * sens[k]), (k, err, sens)
     for g in (a, b, c):
         g.close()
-
-
-@pytest.mark.parametrize("name", ["extension_60x20", "convergence_60x15"])
-def test_tiled_rheology_equals_untiled(workdir, monkeypatch, name):
-    """fl_rheol with the corner nodes staged in shared memory by bulk copies
-    (k_rheol_tile, GEOFLAC_RHEOL_TILE=1) gives the untiled kernel's results
-    bit for bit; the tiles of 256 elements span several columns on these
-    meshes."""
-    inp = inpgen.CONFIGS[name]().write(str(workdir / f"{name}_tile.inp"))
-    p, c, s = new_state(inp)
-    p2, c2, s2 = clone(p, c, s)
-    monkeypatch.setenv("GEOFLAC_RHEOL_TILE", "1")
-    tiled = Flac(p, c, s, "mixed")
-    monkeypatch.delenv("GEOFLAC_RHEOL_TILE")
-    plain = Flac(p2, c2, s2, "mixed")
-    tiled.step(40)
-    plain.step(40)
-    a, b = tiled.download(), plain.download()
-    for f in ("cord", "vel", "temp", "stress0", "aps", "strain", "se2sr", "sshrheat", "visn"):
-        assert np.array_equal(a[f], b[f]), f
-    tiled.close()
-    plain.close()

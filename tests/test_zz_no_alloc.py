@@ -55,3 +55,55 @@ def test_min_angle_noalloc_rejects_oversize_mesh():
     assert f(d.data_ptr(), 2050, 1025, None, C.byref(out)) == GF_ERR_LIMIT
     assert f(d.data_ptr(), 3001, 3001, None, C.byref(out)) == GF_ERR_LIMIT
     assert out.value == -1.0
+
+
+def _expected_min_angle(x, y):
+    """The smallest angle of the four overlaid triangles of every quad
+    (src/rem_test.f90:77-118) in numpy, in the kernel's order of operations:
+    the angles at the second and third vertex from acos, the first as 180
+    minus both, each quad's minimum clamped at zero."""
+    q = [(x[:-1, :-1], y[:-1, :-1]), (x[1:, :-1], y[1:, :-1]), (x[:-1, 1:], y[:-1, 1:]), (x[1:, 1:], y[1:, 1:])]
+    raddeg = 180.0 / np.pi
+    amin = np.full(x[:-1, :-1].shape, 180.0)
+    for tv in ((0, 1, 2), (1, 3, 2), (0, 1, 3), (0, 3, 2)):
+        v = (tv[0], tv[1], tv[2], tv[0])
+        ang = [None, None, None]
+        for k in (1, 2):
+            xa, ya = q[v[k + 1]][0] - q[v[k]][0], q[v[k + 1]][1] - q[v[k]][1]
+            xb, yb = q[v[k - 1]][0] - q[v[k]][0], q[v[k - 1]][1] - q[v[k]][1]
+            la, lb = np.sqrt(xa * xa + ya * ya), np.sqrt(xb * xb + yb * yb)
+            ang[k] = raddeg * np.arccos((xa * xb + ya * yb) / (la * lb))
+        ang[0] = 180.0 - ang[1] - ang[2]
+        amin = np.minimum(amin, np.minimum(ang[0], np.minimum(ang[1], ang[2])))
+    return float(np.maximum(amin, 0.0).min())
+
+
+def test_min_angle_noalloc_largest_mesh_allocates_nothing():
+    """The largest accepted mesh, 2049 x 1025 nodes (2,097,152 elements, all
+    8,192 blocks of partial minima), with jittered nodes and one node pulled
+    towards its neighbour to set a known smallest angle: the result equals
+    numpy's, on two calls in a row, and the device's free memory is the same
+    before and after them."""
+    torch = pytest.importorskip("torch")
+    f = _entry()
+    nx, nz = 2049, 1025
+    rng = np.random.default_rng(11)
+    xs, zs = np.meshgrid(np.arange(nx) * 1000.0, np.arange(nz) * -800.0)  # (nz, nx)
+    x = xs + rng.uniform(-60.0, 60.0, xs.shape)
+    y = zs + rng.uniform(-60.0, 60.0, zs.shape)
+    x[700, 1500] += 600.0  # a sliver near node (700, 1500)
+    expect = _expected_min_angle(x, y)
+    cord = np.stack([x, y], axis=-1)  # (nz, nx, 2); Fortran order = depth fastest
+    d_cord = torch.from_numpy(cord.transpose(2, 1, 0).copy().ravel()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    out = C.c_double(-1.0)
+    assert f(d_cord.data_ptr(), nx, nz, stream, C.byref(out)) == 0  # first call: module and address set-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        out = C.c_double(-1.0)
+        assert f(d_cord.data_ptr(), nx, nz, stream, C.byref(out)) == 0
+        assert abs(out.value - expect) <= TOL * expect, (out.value, expect)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert 0.0 < expect < 30.0
