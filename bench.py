@@ -643,8 +643,7 @@ def profile_magma(args, workdir: str):
 def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
     """The oracle (OpenMP FP64 restatement of the reference's loops) on the
     host cores, on a bounded sample of the same workload."""
-    from geoflac_gb300 import new_state
-    from oracle.oracle import Oracle
+    from oracle.oracle import Oracle, new_state
 
     n = threads or os.cpu_count() or 1
     p, c, s = new_state(inp, markers_per_side=MARKERS_PER_SIDE)
@@ -663,8 +662,8 @@ def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
         return
-    from geoflac_gb300 import inpgen, new_state
-    from oracle.oracle import Oracle
+    from geoflac_gb300 import inpgen
+    from oracle.oracle import Oracle, new_state
 
     d = tempfile.mkdtemp(prefix="gfbench")
     inp = inpgen.extension_1000x300().write(os.path.join(d, "extension_1000x300.inp"))

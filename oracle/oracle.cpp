@@ -7,10 +7,15 @@
 // kernels; with OpenMP threads (loops parallelised where the reference has
 // `!$OMP do`) it is the timed host baseline.
 //
-// It works on the same state as the product (gf_params / gf_clock /
-// gf_layout from include/geoflac_gb300.h, the reference's column-major array
-// layout) so that a test can take one initial state, advance it with both
-// and compare every field.
+// It builds its own initial state from the .inp file (read_params and the
+// setflac chain, restated below) and works on the reference's column-major
+// array layout through the interface structures of include/geoflac_gb300.h
+// (gf_params / gf_clock / gf_layout), so that a test can start the library
+// and the oracle from the same file, advance both and compare every field.
+// The one piece of code it shares with the library is the deterministic
+// FP64 exp/log/pow/sin/tan of geoflac_gb300/csrc/gf_math.h, which the tests
+// check against the C library (and or_set_libm switches the oracle's
+// transcendentals to the C library's, to measure how far that moves a run).
 //
 // Parity pinning: the reference cannot be compiled in this environment (no
 // Fortran compiler), and it commits no golden outputs.  The oracle is pinned
@@ -22,17 +27,55 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <deque>
+#include <string>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
 
 #include "../include/geoflac_gb300.h"
-#include "../geoflac_gb300/csrc/gf_index.h"
 #include "../geoflac_gb300/csrc/gf_math.h"
 
 namespace {
+
+// Index helpers of the reference's column-major layout (src/arrays.f90),
+// 0-based: node (j,i) is cord(j+1,i+1,:), element (j,i) is
+// stress0(j+1,i+1,:,:); the depth index j runs fastest.
+struct ODims {
+    int nx, nz, nphase;
+    long long N; // nodes
+    long long E; // elements
+};
+inline long long o_node(const ODims &d, int j, int i) { return (long long)i * d.nz + j; }
+inline long long o_elem(const ODims &d, int j, int i) { return (long long)i * (d.nz - 1) + j; }
+// cord(j,i,k), vel, bc, ncod: plane k (0 x, 1 z) of nz*nx values
+inline long long o_n2(const ODims &d, int j, int i, int k) { return k * d.N + o_node(d, j, i); }
+// stress0(j,i,c,k): component c (sxx, szz, sxz, syy) of triangle k
+inline long long o_s(const ODims &d, long long e, int c, int k) { return (long long)(c + 4 * k) * d.E + e; }
+// area(j,i,k), dvol, strain, se2sr: plane k of E values
+inline long long o_ek(const ODims &d, long long e, int k) { return (long long)k * d.E + e; }
+// phase_ratio(ph,j,i): the phase index runs fastest
+inline long long o_pr(const ODims &d, long long e, int ph) { return e * d.nphase + ph; }
+
+// myrandom (src/myrandom_mod.f90:9-19): r in [0,1), the seed updated
+inline double o_myrandom(int &iseed) {
+    iseed = iseed % 134456;
+    iseed = (8121 * iseed + 28411) % 134456;
+    return (iseed * 1.0) / 134456;
+}
+
+// Transcendentals of the step: the deterministic FP64 implementation the
+// library's kernels use (gf_math.h, so that both sides round alike), or,
+// after or_set_libm(1), the C library's (to measure how far the choice
+// moves a run; the library's kernels always use gf_math.h).
+bool g_libm = false;
+inline double o_exp(double x) { return g_libm ? std::exp(x) : gfm::exp(x); }
+inline double o_pow(double x, double y) { return g_libm ? std::pow(x, y) : gfm::pow(x, y); }
+inline double o_sin(double x) { return g_libm ? std::sin(x) : gfm::sin(x); }
+inline double o_tan(double x) { return g_libm ? std::tan(x) : gfm::tan(x); }
 
 int g_threads = 1;
 
@@ -44,14 +87,14 @@ struct St {
     gf_params *p;
     gf_clock *c;
     gf_layout *L;
-    GfDims d;
-    double cord(int j, int i, int k) const { return L->cord[gf_n2(d, j, i, k)]; }
-    double &cordr(int j, int i, int k) { return L->cord[gf_n2(d, j, i, k)]; }
-    double vel(int j, int i, int k) const { return L->vel[gf_n2(d, j, i, k)]; }
-    double &temp(int j, int i) { return L->temp[gf_node(d, j, i)]; }
-    long long e(int j, int i) const { return gf_elem(d, j, i); }
-    double area(long long e, int k) const { return L->area[gf_ek(d, e, k)]; }
-    double &st(long long e, int c, int k) { return L->stress0[gf_s(d, e, c, k)]; }
+    ODims d;
+    double cord(int j, int i, int k) const { return L->cord[o_n2(d, j, i, k)]; }
+    double &cordr(int j, int i, int k) { return L->cord[o_n2(d, j, i, k)]; }
+    double vel(int j, int i, int k) const { return L->vel[o_n2(d, j, i, k)]; }
+    double &temp(int j, int i) { return L->temp[o_node(d, j, i)]; }
+    long long e(int j, int i) const { return o_elem(d, j, i); }
+    double area(long long e, int k) const { return L->area[o_ek(d, e, k)]; }
+    double &st(long long e, int c, int k) { return L->stress0[o_s(d, e, c, k)]; }
     // phase_ratio(iph, e) with the reference's flat-memory semantics for a
     // phase id above nphase (read the neighbouring entries, 0 past the end)
     double pr(long long e, int iph1) const {
@@ -63,7 +106,7 @@ struct St {
 };
 
 St make(gf_params *p, gf_clock *c, gf_layout *L) {
-    return St{p, c, L, GfDims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)}};
+    return St{p, c, L, ODims{p->nx, p->nz, p->nphase, (long long)p->nx * p->nz, (long long)(p->nx - 1) * (p->nz - 1)}};
 }
 
 // --------------------------------------------------------------------------
@@ -76,8 +119,8 @@ double eff_dens(St &s, int j, int i, double *frac_slot) {
     double adi_grad = 3e-1, den_ramp_dist = 30e3, amp410 = 0.05, amp660 = 0.085;
     long long e = s.e(j, i);
     double zcord = 0.25 * (s.cord(j, i, 1) + s.cord(j + 1, i, 1) + s.cord(j, i + 1, 1) + s.cord(j + 1, i + 1, 1));
-    double tmpr0 = 0.25 * (s.L->temp[gf_node(s.d, j, i)] + s.L->temp[gf_node(s.d, j + 1, i)] +
-                           s.L->temp[gf_node(s.d, j, i + 1)] + s.L->temp[gf_node(s.d, j + 1, i + 1)]);
+    double tmpr0 = 0.25 * (s.L->temp[o_node(s.d, j, i)] + s.L->temp[o_node(s.d, j + 1, i)] +
+                           s.L->temp[o_node(s.d, j, i + 1)] + s.L->temp[o_node(s.d, j + 1, i + 1)]);
     double zsurf = 0.50 * (s.cord(0, i, 1) + s.cord(0, i + 1, 1));
     double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
     int iph = s.L->iphase[e];
@@ -102,11 +145,11 @@ double eff_dens(St &s, int j, int i, double *frac_slot) {
     }
     double press = 0;
     for (int k = 0; k < 4; ++k)
-        press = press - (s.L->stress0[gf_s(s.d, e, 0, k)] + s.L->stress0[gf_s(s.d, e, 1, k)] + s.L->stress0[gf_s(s.d, e, 3, k)]);
+        press = press - (s.L->stress0[o_s(s.d, e, 0, k)] + s.L->stress0[o_s(s.d, e, 1, k)] + s.L->stress0[o_s(s.d, e, 3, k)]);
     press = press / 12;
     double ed = 0.0;
     for (int k = 0; k < p.nphase; ++k) {
-        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        double ratio = s.L->phase_ratio[o_pr(s.d, e, k)];
         if (ratio < 0.01) continue;
         double dens = p.den[k] * (1 - p.alfa[k] * tmpr + p.beta[k] * press);
         press = dens * p.g * zcord;
@@ -129,8 +172,8 @@ double eff_visc(St &s, int j, int i) {
     long long e = s.e(j, i);
     double adi_grad = 3e-1, r = 8.31448;
     double zcord = 0.25 * (s.cord(j, i, 1) + s.cord(j + 1, i, 1) + s.cord(j, i + 1, 1) + s.cord(j + 1, i + 1, 1));
-    double tmpr0 = 0.25 * (s.L->temp[gf_node(s.d, j, i)] + s.L->temp[gf_node(s.d, j + 1, i)] +
-                           s.L->temp[gf_node(s.d, j, i + 1)] + s.L->temp[gf_node(s.d, j + 1, i + 1)]);
+    double tmpr0 = 0.25 * (s.L->temp[o_node(s.d, j, i)] + s.L->temp[o_node(s.d, j + 1, i)] +
+                           s.L->temp[o_node(s.d, j, i + 1)] + s.L->temp[o_node(s.d, j + 1, i + 1)]);
     double zsurf = 0.50 * (s.cord(0, i, 1) + s.cord(0, i + 1, 1));
     double tmpr = (zsurf - zcord) * 1e-3 * adi_grad + tmpr0;
     double s11 = 0.25 * (s.st(e, 0, 0) + s.st(e, 0, 1) + s.st(e, 0, 2) + s.st(e, 0, 3));
@@ -141,22 +184,22 @@ double eff_visc(St &s, int j, int i) {
     double deptmpr660 = 66.55 * (tmpr + 273.0) - 788494.0;
     double ev;
     if (zcord < deptmpr660) {
-        ev = 1e22 * gfm::exp(-0.0115 * (tmpr - p.t_bot));
+        ev = 1e22 * o_exp(-0.0115 * (tmpr - p.t_bot));
         return std::min(p.v_max, std::max(p.v_min, ev));
     } else if (zcord < deptmpr410) {
-        ev = 1e21 * gfm::exp(-0.0115 * (tmpr - p.t_bot));
+        ev = 1e21 * o_exp(-0.0115 * (tmpr - p.t_bot));
         return std::min(p.v_max, std::max(p.v_min, ev));
     }
     double srat = s.L->e2sr[e];
     if (srat == 0) srat = p.vbc / p.rxbo;
     ev = 0.0;
     for (int k = 0; k < p.nphase; ++k) {
-        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        double ratio = s.L->phase_ratio[o_pr(s.d, e, k)];
         if (ratio < 0.01) continue;
         double pw = 1.0 / p.pln[k] - 1.0;
         double pw1 = -1.0 / p.pln[k];
-        double vis = 0.25 * gfm::pow(srat, pw) * gfm::pow(0.75 * p.acoef[k], pw1) *
-                     gfm::exp((p.eactiv[k] + p.vactiv[k] * pres) / (p.pln[k] * r * (tmpr + 273.0))) * 1e6;
+        double vis = 0.25 * o_pow(srat, pw) * o_pow(0.75 * p.acoef[k], pw1) *
+                     o_exp((p.eactiv[k] + p.vactiv[k] * pres) / (p.pln[k] * r * (tmpr + 273.0))) * 1e6;
         if (vis < p.v_min) vis = p.v_min;
         if (vis > p.v_max) vis = p.v_max;
         ev = ev + ratio / vis;
@@ -164,7 +207,7 @@ double eff_visc(St &s, int j, int i) {
     ev = 1 / ev;
     double fm = (s.L->fmagma ? s.L->fmagma[e] : 0.0) + (s.L->fmagma2 ? s.L->fmagma2[e] : 0.0);
     double fma = std::min(fm, p.fmagma_max);
-    if (p.itype_melting == 1) ev = ev * gfm::exp(p.weaken_ratio_viscous * fma / p.fmagma_max);
+    if (p.itype_melting == 1) ev = ev * o_exp(p.weaken_ratio_viscous * fma / p.fmagma_max);
     return std::min(p.v_max, std::max(p.v_min, ev));
 }
 
@@ -227,15 +270,15 @@ void plastic(double bulkm, double rmu, double coh, double phi, double psi, doubl
     const double degrad = pi / 180.0;
     const double c4d3 = 4.0 / 3.0, c2d3 = 2.0 / 3.0;
     depls = 0.0;
-    double sphi = gfm::sin(phi * degrad);
-    double spsi = gfm::sin(psi * degrad);
+    double sphi = o_sin(phi * degrad);
+    double spsi = o_sin(psi * degrad);
     double anphi = (1.0 + sphi) / (1.0 - sphi);
     double anpsi = (1.0 + spsi) / (1.0 - spsi);
     double amc = 2.0 * coh * std::sqrt(anphi);
     double e1 = bulkm + c4d3 * rmu;
     double e2 = bulkm - c2d3 * rmu;
     double x1 = (e1 - e2 * anpsi + e1 * anphi * anpsi - e2 * anphi);
-    double ten_max = (phi == 0.0) ? ten_off : std::min(ten_off, coh / (gfm::tan(phi * degrad)));
+    double ten_max = (phi == 0.0) ? ten_off : std::min(ten_off, coh / (o_tan(phi * degrad)));
     double s11i = s11 + (de22 + de33) * e2 + de11 * e1;
     double s22i = s22 + (de11 + de33) * e2 + de22 * e1;
     double s12i = s12 + de12 * 2.0 * rmu;
@@ -314,7 +357,7 @@ void pre_plast(St &s, long long e, double &coh, double &phi, double &psi, double
     double pls_curr = s.L->aps[e];
     phi = 0; coh = 0; psi = 0; hardn = 0;
     for (int k = 0; k < p.nphase; ++k) {
-        double ratio = s.L->phase_ratio[gf_pr(s.d, e, k)];
+        double ratio = s.L->phase_ratio[o_pr(s.d, e, k)];
         if (ratio < 0.01) continue;
         double f, c, d, h;
         if (pls_curr < p.plstrain1[k]) {
@@ -394,9 +437,9 @@ void fl_rheol_elem(St &s, int j, int i, double dt) {
     double srII = 0.5 * std::sqrt((s11 - s22) * (s11 - s22) + 4.0 * s12 * s12);
     double srI = 0.5 * (s11 + s22);
     double srs2 = (s11 - srI) * (s11 - srI) + (s22 - srI) * (s22 - srI) + 2.0 * s12 * s12;
-    L.se2sr[gf_ek(s.d, e, 0)] = L.se2sr[gf_ek(s.d, e, 0)] + s11 * dt;
-    L.se2sr[gf_ek(s.d, e, 1)] = L.se2sr[gf_ek(s.d, e, 1)] + s22 * dt;
-    L.se2sr[gf_ek(s.d, e, 2)] = L.se2sr[gf_ek(s.d, e, 2)] + s12 * dt;
+    L.se2sr[o_ek(s.d, e, 0)] = L.se2sr[o_ek(s.d, e, 0)] + s11 * dt;
+    L.se2sr[o_ek(s.d, e, 1)] = L.se2sr[o_ek(s.d, e, 1)] + s22 * dt;
+    L.se2sr[o_ek(s.d, e, 2)] = L.se2sr[o_ek(s.d, e, 2)] + s12 * dt;
     s11 = 0.25 * (s.st(e, 0, 0) + s.st(e, 0, 1) + s.st(e, 0, 2) + s.st(e, 0, 3));
     s22 = 0.25 * (s.st(e, 1, 0) + s.st(e, 1, 1) + s.st(e, 1, 2) + s.st(e, 1, 3));
     s12 = 0.25 * (s.st(e, 2, 0) + s.st(e, 2, 1) + s.st(e, 2, 2) + s.st(e, 2, 3));
@@ -408,7 +451,7 @@ void fl_rheol_elem(St &s, int j, int i, double dt) {
     double bulkm = p.rl[iph] + 2.0 * p.rm[iph] / 3.0;
     double rmu = p.rm[iph];
     double stherm = 0.0;
-    if (p.istress_therm > 0) stherm = -p.alfa[iph] * bulkm * (L.temp[gf_node(s.d, j, i)] - L.temp0[gf_node(s.d, j, i)]);
+    if (p.istress_therm > 0) stherm = -p.alfa[iph] * bulkm * (L.temp[o_node(s.d, j, i)] - L.temp0[o_node(s.d, j, i)]);
     double coh = 0, phi = 0, psi = 0, hardn = 0;
     if (irh == 6 || irh >= 11) pre_plast(s, e, coh, phi, psi, hardn);
     if (irh == 3 || irh >= 11) {
@@ -423,7 +466,7 @@ void fl_rheol_elem(St &s, int j, int i, double dt) {
     double dike = L.dike_released ? L.dike_released[e] : 0.0;
     for (int k = 0; k < 4; ++k) {
         double de11 = sr[0][k] * dt, de22 = sr[1][k] * dt, de12 = sr[2][k] * dt, de33 = 0.0;
-        double dv = L.dvol[gf_ek(s.d, e, k)] - dike;
+        double dv = L.dvol[o_ek(s.d, e, k)] - dike;
         s11p[k] = s.st(e, 0, k) + stherm;
         s22p[k] = s.st(e, 1, k) + stherm;
         s12p[k] = s.st(e, 2, k);
@@ -488,9 +531,9 @@ void fl_rheol_elem(St &s, int j, int i, double dt) {
     }
     // the reference accumulates the element-averaged *stress* here
     // (s11/s22/s12 were reassigned at fl_rheol.f90:181-183)
-    L.strain[gf_ek(s.d, e, 0)] = L.strain[gf_ek(s.d, e, 0)] + s11 * dt;
-    L.strain[gf_ek(s.d, e, 1)] = L.strain[gf_ek(s.d, e, 1)] + s22 * dt;
-    L.strain[gf_ek(s.d, e, 2)] = L.strain[gf_ek(s.d, e, 2)] + s12 * dt;
+    L.strain[o_ek(s.d, e, 0)] = L.strain[o_ek(s.d, e, 0)] + s11 * dt;
+    L.strain[o_ek(s.d, e, 1)] = L.strain[o_ek(s.d, e, 1)] + s22 * dt;
+    L.strain[o_ek(s.d, e, 2)] = L.strain[o_ek(s.d, e, 2)] + s12 * dt;
     if (p.ishearh == 1) {
         double q = 0.0;
         for (int k = 0; k < 4; ++k) {
@@ -542,13 +585,13 @@ void fl_rheol(St &s) {
     if (c.nsrate == p.ifreq_avgsr || c.nsrate == -1) {
         bool reset = c.nsrate == p.ifreq_avgsr;
         for (long long e = 0; e < s.d.E; ++e) {
-            double a = L.se2sr[gf_ek(s.d, e, 0)], b = L.se2sr[gf_ek(s.d, e, 1)], q = L.se2sr[gf_ek(s.d, e, 2)];
+            double a = L.se2sr[o_ek(s.d, e, 0)], b = L.se2sr[o_ek(s.d, e, 1)], q = L.se2sr[o_ek(s.d, e, 2)];
             L.e2sr[e] = (0.5 * std::sqrt((a - b) * (a - b) + 4.0 * q * q)) / c.dtavg;
             L.shrheat[e] = L.sshrheat[e] / c.dtavg;
             if (reset) {
-                L.se2sr[gf_ek(s.d, e, 0)] = 0.0;
-                L.se2sr[gf_ek(s.d, e, 1)] = 0.0;
-                L.se2sr[gf_ek(s.d, e, 2)] = 0.0;
+                L.se2sr[o_ek(s.d, e, 0)] = 0.0;
+                L.se2sr[o_ek(s.d, e, 1)] = 0.0;
+                L.se2sr[o_ek(s.d, e, 2)] = 0.0;
                 L.sshrheat[e] = 0.0;
             }
         }
@@ -601,15 +644,15 @@ void fl_node(St &s) {
                 for (int k = 0; k < 3; ++k) {
                     int t = kk[q][k] - 1, m = mm[q][k] - 1;
                     double factor = 0.25 / ar[t];
-                    double fx = factor * (L.stress0[gf_s(s.d, e, 0, t)] * dx[m][t] + L.stress0[gf_s(s.d, e, 2, t)] * dz[m][t]);
-                    double fy = factor * (L.stress0[gf_s(s.d, e, 2, t)] * dx[m][t] + L.stress0[gf_s(s.d, e, 1, t)] * dz[m][t]);
+                    double fx = factor * (L.stress0[o_s(s.d, e, 0, t)] * dx[m][t] + L.stress0[o_s(s.d, e, 2, t)] * dz[m][t]);
+                    double fy = factor * (L.stress0[o_s(s.d, e, 2, t)] * dx[m][t] + L.stress0[o_s(s.d, e, 1, t)] * dz[m][t]);
                     fx0 = fx0 - fx;
                     fy0 = fy0 - fy;
                 }
             }
-            fy0 = fy0 - L.rmass[gf_node(s.d, j, i)] * p.g;
-            force[gf_n2(s.d, j, i, 0)] = fx0;
-            force[gf_n2(s.d, j, i, 1)] = fy0;
+            fy0 = fy0 - L.rmass[o_node(s.d, j, i)] * p.g;
+            force[o_n2(s.d, j, i, 0)] = fx0;
+            force[o_n2(s.d, j, i, 1)] = fy0;
         }
     if (p.nyhydro > 0) {
         for (int i = 0; i < nx; ++i) {
@@ -628,8 +671,8 @@ void fl_node(St &s) {
                     dlxr = s.cord(0, i + 1, 0) - s.cord(0, i, 0);
                     dlyr = s.cord(0, i + 1, 1) - s.cord(0, i, 1);
                 }
-                double &f0 = force[gf_n2(s.d, 0, i, 0)];
-                double &f1 = force[gf_n2(s.d, 0, i, 1)];
+                double &f0 = force[o_n2(s.d, 0, i, 0)];
+                double &f1 = force[o_n2(s.d, 0, i, 1)];
                 f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
                 f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
             }
@@ -638,7 +681,7 @@ void fl_node(St &s) {
         for (int i = 0; i < nx; ++i) {
             double p_est = p.pisos + 0.5 * (p.den[ips] + p.drosub) * p.g * (s.cord(nz - 1, i, 1) - p.rzbo);
             double rosubg = p.g * (p.den[ips] + p.drosub) *
-                            (1 - p.alfa[ips] * L.temp[gf_node(s.d, nz - 1, i)] + p.beta[ips] * p_est);
+                            (1 - p.alfa[ips] * L.temp[o_node(s.d, nz - 1, i)] + p.beta[ips] * p_est);
             double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
             if (i > 0) {
                 pl = p.pisos - rosubg * ((s.cord(nz - 1, i - 1, 1) + s.cord(nz - 1, i, 1)) / 2.0 - p.rzbo);
@@ -650,8 +693,8 @@ void fl_node(St &s) {
                 dlxr = s.cord(nz - 1, i + 1, 0) - s.cord(nz - 1, i, 0);
                 dlyr = s.cord(nz - 1, i + 1, 1) - s.cord(nz - 1, i, 1);
             }
-            double &f0 = force[gf_n2(s.d, nz - 1, i, 0)];
-            double &f1 = force[gf_n2(s.d, nz - 1, i, 1)];
+            double &f0 = force[o_n2(s.d, nz - 1, i, 0)];
+            double &f1 = force[o_n2(s.d, nz - 1, i, 1)];
             f0 = f0 - 0.5 * pl * dlyl - 0.5 * pr * dlyr;
             f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
         }
@@ -659,12 +702,12 @@ void fl_node(St &s) {
 #pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
     for (int i = 0; i < nx; ++i)
         for (int j = 0; j < nz; ++j) {
-            long long n0 = gf_n2(s.d, j, i, 0), n1 = gf_n2(s.d, j, i, 1);
+            long long n0 = o_n2(s.d, j, i, 0), n1 = o_n2(s.d, j, i, 1);
             double f0 = force[n0], f1 = force[n1];
             int c0 = L.ncod[n0], c1 = L.ncod[n1];
             if ((c0 & 1) != 1 && std::fabs(L.vel[n0]) > 1.0e-13) f0 = f0 - p.demf * std::copysign(std::fabs(f0), L.vel[n0]);
             if ((c1 & 2) != 2 && std::fabs(L.vel[n1]) > 1.0e-13) f1 = f1 - p.demf * std::copysign(std::fabs(f1), L.vel[n1]);
-            double am = L.amass[gf_node(s.d, j, i)];
+            double am = L.amass[o_node(s.d, j, i)];
             if (c0 == 1)
                 L.vel[n0] = L.bc[n0];
             else
@@ -676,11 +719,11 @@ void fl_node(St &s) {
         }
     if (p.i_prestress == 1 && c.time < 600e3 * GF_SEC_YEAR) {
         for (int k = 0; k < 2; ++k)
-            for (int i = 0; i < nx; ++i) L.vel[gf_n2(s.d, nz - 1, i, k)] = 0.0;
+            for (int i = 0; i < nx; ++i) L.vel[o_n2(s.d, nz - 1, i, k)] = 0.0;
         for (int k = 0; k < 2; ++k)
             for (int j = 0; j < nz; ++j) {
-                L.vel[gf_n2(s.d, j, 0, k)] = 0.0;
-                L.vel[gf_n2(s.d, j, nx - 1, k)] = 0.0;
+                L.vel[o_n2(s.d, j, 0, k)] = 0.0;
+                L.vel[o_n2(s.d, j, nx - 1, k)] = 0.0;
             }
     }
 }
@@ -715,8 +758,8 @@ void add_marker_at_top(St &s, int i, double dz_ratio, double time, int loop, int
     int iseed = loop + (i + 1);
     int icount = 0;
     while (true) {
-        double r1 = gf_myrandom(iseed);
-        double r2 = gf_myrandom(iseed);
+        double r1 = o_myrandom(iseed);
+        double r2 = o_myrandom(iseed);
         double x1 = s.cord(0, i, 0) * (1 - r1) + s.cord(0, i + 1, 0) * r1;
         double y1 = s.cord(0, i, 1) * (1 - r1) + s.cord(0, i + 1, 1) * r1;
         double x2 = s.cord(1, i, 0) * (1 - r1) + s.cord(1, i + 1, 0) * r1;
@@ -933,7 +976,7 @@ void fl_flexure(St &s) {
             double r1 = ED(nz - 2, i - 1), r2 = ED(nz - 2, i);
             rho_b = 0.5 * (r1 + r2);
         }
-        q[i] = q[i] - rho_b * g * (L.zoriginal[gf_node(s.d, nz - 1, i)] - s.cord(nz - 1, i, 1));
+        q[i] = q[i] - rho_b * g * (L.zoriginal[o_node(s.d, nz - 1, i)] - s.cord(nz - 1, i, 1));
     }
     bool all_zero = true;
     for (int i = 0; i < nx; ++i) all_zero = all_zero && L.q_init[i] == 0.0;
@@ -997,13 +1040,13 @@ void fl_flexure(St &s) {
     }
     const double dt = s.c->dt;
     for (int i = 0; i < nx; ++i) {
-        for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] - L.vel_flex_old[i];
+        for (int j = 0; j < nz - 1; ++j) L.vel[N + o_node(s.d, j, i)] = L.vel[N + o_node(s.d, j, i)] - L.vel_flex_old[i];
         double cord_old_z = s.cord(nz - 1, i, 1);
-        s.cordr(nz - 1, i, 1) = L.zoriginal[gf_node(s.d, nz - 1, i)] - u[2 * i + 1];
+        s.cordr(nz - 1, i, 1) = L.zoriginal[o_node(s.d, nz - 1, i)] - u[2 * i + 1];
         double vel_flex = 0.0;
         if (dt > 0.0) vel_flex = (s.cord(nz - 1, i, 1) - cord_old_z) / dt;
-        for (int j = 0; j < nz - 1; ++j) L.vel[N + gf_node(s.d, j, i)] = L.vel[N + gf_node(s.d, j, i)] + vel_flex;
-        L.vel[N + gf_node(s.d, nz - 1, i)] = vel_flex;
+        for (int j = 0; j < nz - 1; ++j) L.vel[N + o_node(s.d, j, i)] = L.vel[N + o_node(s.d, j, i)] + vel_flex;
+        L.vel[N + o_node(s.d, nz - 1, i)] = vel_flex;
         L.vel_flex_old[i] = vel_flex;
     }
 }
@@ -1034,8 +1077,8 @@ void fl_move(St &s) {
             for (int k = 0; k < 4; ++k) {
                 int a = nd1[k] - 1, b = nd2[k] - 1, cc = nd3[k] - 1;
                 double det = ((xc[b] * yc[cc] - yc[b] * xc[cc]) - (xc[a] * yc[cc] - yc[a] * xc[cc])) + (xc[a] * yc[b] - yc[a] * xc[b]);
-                L.dvol[gf_ek(s.d, e, k)] = det * L.area[gf_ek(s.d, e, k)] - 1.0;
-                L.area[gf_ek(s.d, e, k)] = 1.0 / det;
+                L.dvol[o_ek(s.d, e, k)] = det * L.area[o_ek(s.d, e, k)] - 1.0;
+                L.area[o_ek(s.d, e, k)] = 1.0 / det;
                 double dw12 = 0.5 * (xv[a] * (xc[cc] - xc[b]) + xv[b] * (xc[a] - xc[cc]) + xv[cc] * (xc[b] - xc[a]) +
                                      yv[a] * (yc[cc] - yc[b]) + yv[b] * (yc[a] - yc[cc]) + yv[cc] * (yc[b] - yc[a])) /
                               det * dt;
@@ -1044,14 +1087,14 @@ void fl_move(St &s) {
                 s.st(e, 1, k) = s22 - s12 * 2 * dw12;
                 s.st(e, 2, k) = s12 + dw12 * (s22 - s11);
                 if (k == 0) {
-                    double e11 = L.strain[gf_ek(s.d, e, 0)], e22 = L.strain[gf_ek(s.d, e, 1)], e12 = L.strain[gf_ek(s.d, e, 2)];
-                    L.strain[gf_ek(s.d, e, 0)] = e11 + e12 * 2 * dw12;
-                    L.strain[gf_ek(s.d, e, 1)] = e22 - e12 * 2 * dw12;
-                    L.strain[gf_ek(s.d, e, 2)] = e12 + dw12 * (e22 - e11);
+                    double e11 = L.strain[o_ek(s.d, e, 0)], e22 = L.strain[o_ek(s.d, e, 1)], e12 = L.strain[o_ek(s.d, e, 2)];
+                    L.strain[o_ek(s.d, e, 0)] = e11 + e12 * 2 * dw12;
+                    L.strain[o_ek(s.d, e, 1)] = e22 - e12 * 2 * dw12;
+                    L.strain[o_ek(s.d, e, 2)] = e12 + dw12 * (e22 - e11);
                 }
             }
             for (int k = 0; k < 4; ++k)
-                if (L.area[gf_ek(s.d, e, k)] <= 0) neg = true;
+                if (L.area[o_ek(s.d, e, k)] <= 0) neg = true;
             if (neg) {
 #pragma omp critical
                 err = 40;
@@ -1079,8 +1122,8 @@ void rmasses(St &s) {
                     long long e = s.e(j, i);
                     double a0 = s.area(e, 0), a1 = s.area(e, 1), a2 = s.area(e, 2), a3 = s.area(e, 3);
                     double *rm = L.rmass;
-                    long long n11 = gf_node(s.d, j, i), n21 = gf_node(s.d, j + 1, i), n12 = gf_node(s.d, j, i + 1),
-                              n22 = gf_node(s.d, j + 1, i + 1);
+                    long long n11 = o_node(s.d, j, i), n21 = o_node(s.d, j + 1, i), n12 = o_node(s.d, j, i + 1),
+                              n22 = o_node(s.d, j + 1, i + 1);
                     rm[n11] = rm[n11] + c1d12 / a0 * dens;
                     rm[n21] = rm[n21] + c1d12 / a0 * dens;
                     rm[n12] = rm[n12] + c1d12 / a0 * dens;
@@ -1170,8 +1213,8 @@ void dt_mass(St &s) {
                     }
                     if (p.idt_scale > 0) {
                         double *am = L.amass;
-                        long long n11 = gf_node(s.d, j, i), n21 = gf_node(s.d, j + 1, i), n12 = gf_node(s.d, j, i + 1),
-                                  n22 = gf_node(s.d, j + 1, i + 1);
+                        long long n11 = o_node(s.d, j, i), n21 = o_node(s.d, j + 1, i), n12 = o_node(s.d, j, i + 1),
+                                  n22 = o_node(s.d, j + 1, i + 1);
                         double am3 = c1d12 * rho_inert / s.area(e, 0);
                         am[n11] = am[n11] + am3; am[n21] = am[n21] + am3; am[n12] = am[n12] + am3;
                         am3 = c1d12 * rho_inert / s.area(e, 1);
@@ -1229,9 +1272,9 @@ void therm_magma(St &s) {
     const double dt = s.c->dt;
     auto X = [&](int j, int i) { return s.cord(j, i, 0); };
     auto Z = [&](int j, int i) { return s.cord(j, i, 1); };
-    auto T = [&](int j, int i) -> double & { return L.temp[gf_node(s.d, j, i)]; };
-    auto T0 = [&](int j, int i) { return L.temp0[gf_node(s.d, j, i)]; };
-    const double tan_mzone = gfm::tan(0.5 * p.angle_mzone * 3.14159265358979323846 / 180.0);
+    auto T = [&](int j, int i) -> double & { return L.temp[o_node(s.d, j, i)]; };
+    auto T0 = [&](int j, int i) { return L.temp0[o_node(s.d, j, i)]; };
+    const double tan_mzone = o_tan(0.5 * p.angle_mzone * 3.14159265358979323846 / 180.0);
     const int ihw = ceil_int(tan_mzone * 200e3 / p.dxmin);
     const double w_barrier = 1.0e-4;
 
@@ -1241,7 +1284,7 @@ void therm_magma(St &s) {
             long long e = s.e(j, i);
             double cp_eff = p.cp[L.iphase[e] - 1];
             double tmpr = 0.25 * (T0(j, i) + T0(j + 1, i) + T0(j, i + 1) + T0(j + 1, i + 1));
-            double fr_lambda = p.lambda_freeze * gfm::exp(-p.lambda_freeze_tdep * (tmpr - p.t_top));
+            double fr_lambda = p.lambda_freeze * o_exp(-p.lambda_freeze_tdep * (tmpr - p.t_top));
             double d1 = fmin2(L.fmagma[e], L.fmagma[e] * dt * fr_lambda);
             double d2 = fmin2(L.fmagma2[e], L.fmagma2[e] * dt * fr_lambda);
             L.fmagma[e] = L.fmagma[e] - d1;
@@ -1430,8 +1473,8 @@ void fl_therm(St &s) {
             diff[e] = cond_eff / p.den[iph] / cp_eff;
             src[e] = (L.source[e] + dissip / p.den[iph]) / cp_eff;
         }
-    auto C = [&](int j, int i, int k) { return L.cord[gf_n2(s.d, j, i, k)]; };
-    auto T = [&](int j, int i) { return L.temp[gf_node(s.d, j, i)]; };
+    auto C = [&](int j, int i, int k) { return L.cord[o_n2(s.d, j, i, k)]; };
+    auto T = [&](int j, int i) { return L.temp[o_node(s.d, j, i)]; };
     // in place, lexicographic (i outer, j inner): a Gauss-Seidel sweep
 #pragma omp parallel for num_threads(g_threads) if (g_threads > 1)
     for (int i = 0; i < nx; ++i)
@@ -1503,21 +1546,21 @@ void fl_therm(St &s) {
                       0.5 * diff[e] * inv_area *
                           (T(j, i) * (d1 * d1 + z1 * z1) + T(j + 1, i) * (d2 * d1 + z2 * z1) + T(j, i + 1) * (d3 * d1 + z3 * z1));
             }
-            L.temp[gf_node(s.d, j, i)] = T(j, i) + rhs * dt / area_n;
+            L.temp[o_node(s.d, j, i)] = T(j, i) + rhs * dt / area_n;
         }
     for (int i = 0; i < nx; ++i) {
-        L.temp[gf_node(s.d, 0, i)] = p.t_top;
+        L.temp[o_node(s.d, 0, i)] = p.t_top;
         if (p.itemp_bc == 1)
-            L.temp[gf_node(s.d, nz - 1, i)] = p.bot_bc;
+            L.temp[o_node(s.d, nz - 1, i)] = p.bot_bc;
         else if (p.itemp_bc == 2) {
             int ie = std::min(i, nx - 2);
             double cond_eff = p.conduct[L.iphase[s.e(nz - 2, ie)] - 1];
-            L.temp[gf_node(s.d, nz - 1, i)] = T(nz - 2, i) + p.bot_bc * (C(nz - 2, i, 1) - C(nz - 1, i, 1)) / cond_eff;
+            L.temp[o_node(s.d, nz - 1, i)] = T(nz - 2, i) + p.bot_bc * (C(nz - 2, i, 1) - C(nz - 1, i, 1)) / cond_eff;
         }
     }
     for (int j = 0; j < nz; ++j) {
-        L.temp[gf_node(s.d, j, 0)] = T(j, 1);
-        L.temp[gf_node(s.d, j, nx - 1)] = T(j, nx - 2);
+        L.temp[o_node(s.d, j, 0)] = T(j, 1);
+        L.temp[o_node(s.d, j, nx - 1)] = T(j, nx - 2);
     }
 }
 
@@ -1535,7 +1578,7 @@ void count_phase_ratio(St &s, int j, int i) {
         int iph = L.mark_phase[kk - 1];
         if (iph >= 1 && iph <= GF_MAXPH) cnt[iph] += 1;
     }
-    for (int k = 1; k <= s.p->nphase; ++k) L.phase_ratio[gf_pr(s.d, e, k - 1)] = cnt[k] / (nm * 1.0);
+    for (int k = 1; k <= s.p->nphase; ++k) L.phase_ratio[o_pr(s.d, e, k - 1)] = cnt[k] / (nm * 1.0);
     int iph = 1, best = 0;
     for (int k = 1; k <= s.p->nphase; ++k)
         if (cnt[k] > best) {
@@ -1598,7 +1641,7 @@ void marker2elem(St &s) {
             int kinc = L.nmark_elem[s.e(j, i)];
             int icount = 0;
             while (kinc <= 4) {
-                double r1 = gf_myrandom(iseed), r2 = gf_myrandom(iseed);
+                double r1 = o_myrandom(iseed), r2 = o_myrandom(iseed);
                 double x1 = s.cord(j, i, 0) * (1 - r1) + s.cord(j, i + 1, 0) * r1;
                 double y1 = s.cord(j, i, 1) * (1 - r1) + s.cord(j, i + 1, 1) * r1;
                 double x2 = s.cord(j + 1, i, 0) * (1 - r1) + s.cord(j + 1, i + 1, 0) * r1;
@@ -1640,7 +1683,7 @@ void melting(St &s) {
     gf_layout &L = *s.L;
     const int nx = p.nx, nz = p.nz;
     auto Z = [&](int j, int i) { return s.cord(j, i, 1); };
-    auto T = [&](int j, int i) -> double & { return L.temp[gf_node(s.d, j, i)]; };
+    auto T = [&](int j, int i) -> double & { return L.temp[o_node(s.d, j, i)]; };
     auto tmpr_of = [&](int j, int i) { return 0.25 * (T(j, i) + T(j, i + 1) + T(j + 1, i) + T(j + 1, i + 1)); };
     auto depth_of = [&](int j, int i) {
         double yy = 0.25 * (Z(j, i) + Z(j, i + 1) + Z(j + 1, i) + Z(j + 1, i + 1));
@@ -1680,7 +1723,7 @@ void melting(St &s) {
             double tpr = s.pr(e, K_SED1) + s.pr(e, K_SED2) + s.pr(e, K_METASED) + s.pr(e, K_SCHIST);
             if (tpr > 0.6 && Z(j, i) > -200e3) {
                 double tmpr = tmpr_of(j, i), depth = depth_of(j, i);
-                double solidus = fmax2(680 + 0.6e-3 * (depth - 140e3), 930 - 313 * (1 - gfm::exp(-depth / 7e3)));
+                double solidus = fmax2(680 + 0.6e-3 * (depth - 140e3), 930 - 313 * (1 - o_exp(-depth / 7e3)));
                 if (tmpr > solidus) {
                     L.fmelt[e] = pmelt_of(K_SED2, tmpr - solidus, 50.0) * tpr;
                     cool(j, i, tmpr - solidus);
@@ -1697,7 +1740,7 @@ void melting(St &s) {
                 double press = 3000 * 10 * depth / 1e9;
                 double solidus;
                 if (press < 1.0)
-                    solidus = 1050.0 - 420.0 * (1.0 - gfm::exp(-press * 3.3));
+                    solidus = 1050.0 - 420.0 * (1.0 - o_exp(-press * 3.3));
                 else if (press > 2.7)
                     solidus = (press + 14.0) * 43.0;
                 else
@@ -1752,7 +1795,7 @@ void change_phase(St &s) {
         int i = (n - k) / 2 / (nz - 1);
         double a1 = L.mark_a1[kk], a2 = L.mark_a2[kk];
         double yy, tmpr;
-        auto Tn = [&](int jj, int ii) { return L.temp[gf_node(s.d, jj, ii)]; };
+        auto Tn = [&](int jj, int ii) { return L.temp[o_node(s.d, jj, ii)]; };
         if (k == 1) {
             yy = s.cord(j, i, 1) * a1 + s.cord(j + 1, i, 1) * a2 + s.cord(j, i + 1, 1) * (1 - a1 - a2);
             tmpr = Tn(j, i) * a1 + Tn(j + 1, i) * a2 + Tn(j, i + 1) * (1 - a1 - a2);
@@ -1941,7 +1984,7 @@ void geotherm_column(St &s, int n, int i, double age_1n, double tp1n, double tp2
     int nz = p.nz, nx = p.nx;
     const double pi = 3.14159265358979323846;
     double t_top = p.t_top, t_bot = p.t_bot;
-    auto T = [&](int j) -> double & { return L.temp[gf_node(s.d, j, i)]; };
+    auto T = [&](int j) -> double & { return L.temp[o_node(s.d, j, i)]; };
     auto Y = [&](int j) { return s.cord(j, i, 1); };
     int ic = p.ictherm[n];
     if (ic == 1) {
@@ -2115,7 +2158,7 @@ void rem_cord(St &s, const std::vector<double> &cordo) {
     const gf_params &p = *s.p;
     int nx = p.nx, nz = p.nz;
     std::vector<double> st(std::max(nx, nz) + 2);
-    auto CO = [&](int j, int i, int k) { return cordo[gf_n2(s.d, j, i, k)]; };
+    auto CO = [&](int j, int i, int k) { return cordo[o_n2(s.d, j, i, k)]; };
     for (int j = 0; j < nz; ++j) {
         double xl = 0, xr = 0;
         if (p.mode_rem == 1) {
@@ -2297,8 +2340,8 @@ void newphase2marker(St &s, int j1, int j2, int i1, int i2, int iph) {
             long long e = s.e(j - 1, i - 1);
             for (int n = 0; n < L.nmark_elem[e]; ++n) L.mark_phase[L.mark_id_elem[e * GF_MAX_MARKERS_PER_ELEM + n] - 1] = (int8_t)iph;
             L.iphase[e] = iph;
-            for (int k = 0; k < s.p->nphase; ++k) L.phase_ratio[gf_pr(s.d, e, k)] = 0.0;
-            L.phase_ratio[gf_pr(s.d, e, iph - 1)] = 1.0;
+            for (int k = 0; k < s.p->nphase; ++k) L.phase_ratio[o_pr(s.d, e, k)] = 0.0;
+            L.phase_ratio[o_pr(s.d, e, iph - 1)] = 1.0;
         }
 }
 
@@ -2310,12 +2353,12 @@ void init_areas(St &s) {
             double x3 = s.cord(j, i + 1, 0), y3 = s.cord(j, i + 1, 1), x4 = s.cord(j + 1, i + 1, 0), y4 = s.cord(j + 1, i + 1, 1);
             long long e = s.e(j, i);
             double *a = s.L->area;
-            a[gf_ek(s.d, e, 0)] = 1.0 / (((x2 * y3 - y2 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y2 - y1 * x2));
-            a[gf_ek(s.d, e, 1)] = 1.0 / (((x2 * y4 - y2 * x4) - (x3 * y4 - y3 * x4)) + (x3 * y2 - y3 * x2));
-            a[gf_ek(s.d, e, 2)] = 1.0 / (((x2 * y4 - y2 * x4) - (x1 * y4 - y1 * x4)) + (x1 * y2 - y1 * x2));
-            a[gf_ek(s.d, e, 3)] = 1.0 / (((x4 * y3 - y4 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y4 - y1 * x4));
+            a[o_ek(s.d, e, 0)] = 1.0 / (((x2 * y3 - y2 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y2 - y1 * x2));
+            a[o_ek(s.d, e, 1)] = 1.0 / (((x2 * y4 - y2 * x4) - (x3 * y4 - y3 * x4)) + (x3 * y2 - y3 * x2));
+            a[o_ek(s.d, e, 2)] = 1.0 / (((x2 * y4 - y2 * x4) - (x1 * y4 - y1 * x4)) + (x1 * y2 - y1 * x2));
+            a[o_ek(s.d, e, 3)] = 1.0 / (((x4 * y3 - y4 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y4 - y1 * x4));
             for (int k = 0; k < 4; ++k)
-                if (a[gf_ek(s.d, e, k)] < 0) throw Stop{41};
+                if (a[o_ek(s.d, e, k)] < 0) throw Stop{41};
         }
 }
 
@@ -2335,12 +2378,12 @@ void remesh(St &s) {
         int i = 0, ii = 0;
         double xl = s.cord(0, i, 0), xr;
         while (std::max(i, ii) < nx - 1) {
-            xr = std::min(cordo[gf_n2(s.d, 0, ii + 1, 0)], s.cord(0, i + 1, 0));
+            xr = std::min(cordo[o_n2(s.d, 0, ii + 1, 0)], s.cord(0, i + 1, 0));
             if (xl < xr) {
                 dhnew[i] = dhnew[i] + L.dhacc[ii] * (xr - xl);
                 extnew[i] = extnew[i] + L.extr_acc[ii] * (xr - xl);
             }
-            if (xr == cordo[gf_n2(s.d, 0, ii + 1, 0)])
+            if (xr == cordo[o_n2(s.d, 0, ii + 1, 0)])
                 ii = ii + 1;
             else
                 i = i + 1;
@@ -2354,7 +2397,7 @@ void remesh(St &s) {
     // element fields: barycentric interpolation between element centres
     int nzt = nz - 1, nxt = nx - 1;
     std::vector<double> cold(2 * E), cnew(2 * E);
-    auto CO = [&](int j, int i, int k) { return cordo[gf_n2(s.d, j, i, k)]; };
+    auto CO = [&](int j, int i, int k) { return cordo[o_n2(s.d, j, i, k)]; };
     for (int i = 0; i < nxt; ++i)
         for (int j = 0; j < nzt; ++j) {
             size_t q = (size_t)i * nzt + j;
@@ -2446,6 +2489,744 @@ void remesh_event(St &s) {
         for (int i = 0; i < s.p->nx; ++i) s.L->dhacc_correction[i] = 0.0;
 }
 
+// --------------------------------------------------------------------------
+// Start-up: read_params (src/read_params.f90:3-373) and the setflac chain
+// (src/setflac.f90:4-89: init_cord, init_phase, init_marker,
+// check_visc_rheol, init_areas, init_temp, init_stress, init_bc).  The
+// oracle builds its own initial state from the .inp file with these, so
+// that nothing of the product's host code enters a comparison.
+
+// Fortran list-directed input over the lines of an .inp file.  A READ
+// starts at the current record and takes values from as many records as it
+// needs; what is left of its last record is dropped.  Values are separated
+// by commas, blanks or the end of a record; two commas in a row give a null
+// value (the item keeps its value), r*v repeats v r times, r* gives r nulls,
+// a slash ends the READ.
+struct ParseErr {
+    int line;
+};
+
+class ListInput {
+  public:
+    explicit ListInput(std::vector<std::string> lines) : rec_(lines) {}
+    // AdvanceToNextInputLine (read_params.f90:351-373): skip records whose
+    // first character is ';'
+    void advance() {
+        while (cur_ < rec_.size() && !rec_[cur_].empty() && rec_[cur_][0] == ';') ++cur_;
+        if (cur_ >= rec_.size()) throw ParseErr{(int)cur_ + 1};
+    }
+    void begin() {
+        q_.clear();
+        slash_ = false;
+        used_ = false;
+    }
+    // end of a READ statement: continue after its last record
+    void end() {
+        if (used_ || q_.empty()) ++cur_;
+        q_.clear();
+    }
+    // an empty READ: skips one record
+    void skip() {
+        if (cur_ >= rec_.size()) throw ParseErr{(int)cur_ + 1};
+        ++cur_;
+    }
+    bool next(std::string &v) { // false: null value (item unchanged)
+        if (slash_) return false;
+        while (q_.empty()) {
+            if (used_) ++cur_;
+            if (cur_ >= rec_.size()) throw ParseErr{(int)cur_ + 1};
+            split(rec_[cur_]);
+            used_ = true;
+        }
+        Tok t = q_.front();
+        q_.pop_front();
+        if (t.kind == 2) {
+            slash_ = true;
+            q_.clear();
+            return false;
+        }
+        if (t.kind == 1) return false;
+        v = t.s;
+        return true;
+    }
+    void i(int &x) {
+        std::string v;
+        if (!next(v)) return;
+        char *e = nullptr;
+        long r = std::strtol(v.c_str(), &e, 10);
+        if (e == v.c_str() || *e) throw ParseErr{(int)cur_ + 1};
+        x = (int)r;
+    }
+    void d(double &x) {
+        std::string v;
+        if (!next(v)) return;
+        for (char &c : v)
+            if (c == 'd' || c == 'D') c = 'e';
+        char *e = nullptr;
+        double r = std::strtod(v.c_str(), &e);
+        if (e == v.c_str() || *e) throw ParseErr{(int)cur_ + 1};
+        x = r;
+    }
+    void str(char *dst, size_t n) {
+        std::string v;
+        if (!next(v)) return;
+        std::snprintf(dst, n, "%s", v.c_str());
+    }
+    int line() const { return (int)cur_ + 1; }
+
+  private:
+    struct Tok {
+        int kind; // 0 value, 1 null, 2 slash
+        std::string s;
+    };
+    void split(const std::string &r) {
+        size_t k = 0, n = r.size();
+        bool want = true; // a comma now gives a null value
+        while (k < n) {
+            char c = r[k];
+            if (c == ' ' || c == '\t' || c == '\r') {
+                ++k;
+                continue;
+            }
+            if (c == ',') {
+                if (want) q_.push_back({1, ""});
+                want = true;
+                ++k;
+                continue;
+            }
+            if (c == '/') {
+                q_.push_back({2, ""});
+                return;
+            }
+            std::string t;
+            if (c == '\'' || c == '"') {
+                char qc = c;
+                ++k;
+                while (k < n && r[k] != qc) t += r[k++];
+                ++k;
+                q_.push_back({0, t});
+                want = false;
+                continue;
+            }
+            while (k < n && r[k] != ' ' && r[k] != '\t' && r[k] != ',' && r[k] != '/' && r[k] != '\r') t += r[k++];
+            size_t star = t.find('*');
+            if (star != std::string::npos && star > 0 &&
+                t.find_first_not_of("0123456789") == star) { // r*v or r*
+                int reps = std::atoi(t.substr(0, star).c_str());
+                std::string v = t.substr(star + 1);
+                for (int m = 0; m < reps; ++m) q_.push_back(v.empty() ? Tok{1, ""} : Tok{0, v});
+            } else {
+                q_.push_back({0, t});
+            }
+            want = false;
+        }
+    }
+    std::vector<std::string> rec_;
+    size_t cur_ = 0;
+    std::deque<Tok> q_;
+    bool slash_ = false, used_ = false;
+};
+
+const double O_SEC_YEAR = 3.1558e7; // src/params.f90 sec_year
+
+// read_params (src/read_params.f90:3-348), in its order
+int read_params(const char *path, gf_params *p) {
+    std::FILE *f = std::fopen(path, "r");
+    if (!f) return GF_ERR_IO;
+    std::vector<std::string> lines;
+    std::string cur;
+    for (int ch; (ch = std::fgetc(f)) != EOF;) {
+        if (ch == '\n') {
+            lines.push_back(cur);
+            cur.clear();
+        } else {
+            cur += (char)ch;
+        }
+    }
+    if (!cur.empty()) lines.push_back(cur);
+    std::fclose(f);
+    // options with no .inp counterpart survive the read
+    int mps = p->markers_per_side, ecl = p->eclogite_rule, tsw = p->therm_sweeps;
+    std::memset(p, 0, sizeof *p);
+    p->markers_per_side = mps;
+    p->eclogite_rule = ecl;
+    p->therm_sweeps = tsw;
+    ListInput r(lines);
+    auto rd = [&](auto &&body) {
+        r.advance();
+        r.begin();
+        body();
+        r.end();
+    };
+    try {
+        rd([&] { r.i(p->nx); r.i(p->nz); });
+        p->nx += 1;
+        p->nz += 1;
+        rd([&] { r.d(p->x0); r.d(p->z0); });
+        rd([&] { r.d(p->rxbo); r.d(p->rzbo); });
+        rd([&] { r.i(p->ircoord); r.str(p->coordfile, sizeof p->coordfile); });
+        if (p->ircoord > 0) {
+            rd([&] { r.i(p->nzonx); });
+            if (p->nzonx != 0) return GF_ERR_PARSE;
+            rd([&] { r.i(p->nzony); });
+            if (p->nzony != 0) return GF_ERR_PARSE;
+        } else {
+            rd([&] { r.i(p->nzonx); });
+            if (p->nzonx == 0) {
+                p->nzonx = 1;
+                p->nelz_x[0] = p->nx - 1;
+                p->sizez_x[0] = 1.0;
+            } else {
+                if (p->nzonx < 0 || p->nzonx > GF_MAXZONE) return GF_ERR_PARSE;
+                for (int k = 0; k < p->nzonx; ++k) rd([&] { r.i(p->nelz_x[k]); r.d(p->sizez_x[k]); });
+            }
+            rd([&] { r.i(p->nzony); });
+            if (p->nzony == 0) {
+                p->nzony = 1;
+                p->nelz_y[0] = p->nz - 1;
+                p->sizez_y[0] = 1.0;
+            } else {
+                if (p->nzony < 0 || p->nzony > GF_MAXZONE) return GF_ERR_PARSE;
+                for (int k = 0; k < p->nzony; ++k) {
+                    p->sizez_y[k] = 1.0;
+                    rd([&] { r.i(p->nelz_y[k]); r.d(p->sizez_y[k]); });
+                }
+            }
+        }
+        // mechanical conditions
+        rd([&] { r.i(p->nystressbc); r.i(p->nydrsides); });
+        rd([&] { r.i(p->nofbc); });
+        if (p->nofbc < 0 || p->nofbc > GF_MAXBC) return GF_ERR_PARSE;
+        r.advance();
+        for (int k = 0; k < p->nofbc; ++k) { // one READ per condition, no comment lines between
+            r.begin();
+            r.i(p->nofside[k]); r.i(p->nbc1[k]); r.i(p->nbc2[k]); r.i(p->nbc[k]);
+            r.d(p->bca[k]); r.d(p->bcb[k]); r.d(p->bcc[k]); r.d(p->bcd[k]); r.d(p->bce[k]);
+            r.d(p->bcf[k]); r.d(p->bcg[k]); r.d(p->bch[k]); r.d(p->bci[k]);
+            r.end();
+        }
+        r.advance();
+        rd([&] { r.i(p->nyhydro); r.d(p->pisos); r.i(p->iphsub); r.d(p->drosub); r.d(p->damp_vis); });
+        rd([&] { r.d(p->g); });
+        // thermal conditions
+        rd([&] { r.i(p->i_prestress); });
+        rd([&] { r.d(p->extra_pres); });
+        rd([&] { r.i(p->itherm); });
+        rd([&] { r.i(p->istress_therm); });
+        rd([&] { r.i(p->ishearh); });
+        rd([&] { r.d(p->t_top); });
+        rd([&] { r.d(p->t_bot); });
+        rd([&] { r.d(p->hs); r.d(p->hr); });
+        rd([&] { r.i(p->itemp_bc); r.d(p->bot_bc); });
+        if (p->itemp_bc == 2) p->bot_bc = p->bot_bc / 1000;
+        rd([&] { r.i(p->irtemp); });
+        r.advance();
+        if (p->irtemp > 0) {
+            r.begin();
+            r.str(p->tempfile, sizeof p->tempfile);
+            r.end();
+        } else {
+            r.skip();
+        }
+        rd([&] { r.i(p->nzone_age); });
+        if (p->nzone_age < 0 || p->nzone_age > GF_MAXZONE_AGE) return GF_ERR_PARSE;
+        r.advance();
+        for (int n = 0; n < p->nzone_age; ++n) {
+            r.begin();
+            r.i(p->ictherm[n]); r.d(p->age_1[n]); r.d(p->tp1[n]); r.d(p->tp2[n]); r.i(p->ixtb1[n]); r.i(p->ixtb2[n]);
+            r.end();
+            r.advance();
+            r.begin();
+            r.i(p->nph_layer[n]);
+            if (p->nph_layer[n] < 1 || p->nph_layer[n] > GF_MAXZONE_LAYER) return GF_ERR_PARSE;
+            for (int m = 0; m < p->nph_layer[n] - 1; ++m) r.d(p->hc[n][m]);
+            r.end();
+            r.begin();
+            for (int m = 0; m < p->nph_layer[n]; ++m) r.i(p->iph_col[n][m]);
+            r.end();
+        }
+        // smooth transitions between age zones (read_params.f90:168-186)
+        for (int n = 0; n < p->nzone_age - 1; ++n) {
+            p->iph_col_trans[n] = 0;
+            if (p->ixtb2[n] == -1) {
+                p->iph_col_trans[n] = 1;
+                p->ixtb2[n] = p->ixtb2[n + 1];
+                p->ixtb1[n + 1] = p->ixtb1[n];
+            }
+        }
+        // rheology
+        rd([&] { r.i(p->nphase); });
+        if (p->nphase < 1 || p->nphase > GF_MAXPH) return GF_ERR_PARSE;
+        for (int k = 0; k < p->nphase; ++k)
+            rd([&] {
+                r.i(p->irheol[k]); r.d(p->visc[k]); r.d(p->den[k]); r.d(p->alfa[k]); r.d(p->beta[k]);
+                r.d(p->pln[k]); r.d(p->acoef[k]); r.d(p->eactiv[k]); r.d(p->vactiv[k]); r.d(p->rl[k]);
+                r.d(p->rm[k]); r.d(p->plstrain1[k]); r.d(p->plstrain2[k]); r.d(p->fric1[k]); r.d(p->fric2[k]);
+                r.d(p->cohesion1[k]); r.d(p->cohesion2[k]); r.d(p->dilat1[k]); r.d(p->dilat2[k]);
+                r.d(p->conduct[k]); r.d(p->cp[k]); r.d(p->ts[k]); r.d(p->tl[k]); r.d(p->tk[k]);
+                r.d(p->erodibility[k]);
+            });
+        rd([&] { r.i(p->irphase); });
+        r.advance();
+        if (p->irphase > 0) {
+            r.begin();
+            r.str(p->phasefile, sizeof p->phasefile);
+            r.end();
+        } else {
+            r.skip();
+        }
+        rd([&] { r.i(p->inhom); });
+        if (p->inhom < 0 || p->inhom > GF_MAXINH) return GF_ERR_PARSE; // stop 26
+        for (int k = 0; k < p->inhom; ++k)
+            rd([&] {
+                r.i(p->ix1[k]); r.i(p->ix2[k]); r.i(p->iy1[k]); r.i(p->iy2[k]); r.i(p->inphase[k]);
+                r.i(p->igeom[k]); r.d(p->xinitaps[k]);
+            });
+        rd([&] { r.d(p->ten_off); });
+        rd([&] { r.d(p->tau_heal); });
+        rd([&] { r.d(p->v_min); r.d(p->v_max); r.i(p->ivis_shape); r.d(p->efoldc); });
+        rd([&] {
+            r.i(p->itype_melting); r.i(p->nelem_serp); r.i(p->nelem_dike); r.d(p->prod_magma); r.d(p->prod_magma2);
+            r.d(p->rho_magma);
+        });
+        rd([&] { r.d(p->angle_mzone); r.d(p->fmagma_max); r.d(p->ratio_mantle_mzone); r.d(p->ratio_crust_mzone); });
+        rd([&] { r.d(p->latent_heat_magma); r.d(p->lambda_freeze); r.d(p->lambda_freeze_tdep); });
+        rd([&] { r.d(p->weaken_ratio_plastic); r.d(p->weaken_ratio_viscous); });
+        p->weaken_ratio_viscous = std::log(p->weaken_ratio_viscous);
+        // remeshing
+        rd([&] { r.i(p->ny_rem); r.i(p->mode_rem); r.i(p->ntest_rem); r.d(p->angle_rem); });
+        if (p->mode_rem != 1 && p->mode_rem != 11 && p->mode_rem != 3 && p->mode_rem != 4) return GF_ERR_PARSE;
+        rd([&] { r.d(p->dx_rem); });
+        rd([&] { r.d(p->topo_kappa); r.d(p->fac_kappa); });
+        // process control
+        rd([&] { r.i(p->idt_scale); });
+        rd([&] { r.d(p->dt_scale); r.d(p->strain_inert); });
+        rd([&] { r.i(p->i_rey); r.d(p->xReyn); });
+        rd([&] { r.i(p->ifreq_rmasses); });
+        rd([&] { r.i(p->ifreq_imasses); });
+        rd([&] { r.i(p->ifreq_visc); });
+        rd([&] { r.i(p->ifreq_avgsr); });
+        if (p->ifreq_rmasses <= 0 || p->ifreq_imasses <= 0 || p->ifreq_visc <= 0 || p->ifreq_avgsr <= 0)
+            return GF_ERR_PARSE;
+        if (p->ntest_rem % p->ifreq_rmasses + p->ntest_rem % p->ifreq_imasses + p->ntest_rem % p->ifreq_visc +
+                p->ntest_rem % p->ifreq_avgsr != 0)
+            return GF_ERR_PARSE;
+        rd([&] { r.d(p->frac); r.d(p->fracm); });
+        rd([&] { r.i(p->movegrid); r.i(p->ndim); });
+        rd([&] { r.d(p->demf); r.i(p->mix_strain); r.i(p->mix_stress); });
+        // output
+        rd([&] { r.d(p->time_max); });
+        p->time_max = p->time_max * 1000 * O_SEC_YEAR;
+        rd([&] { r.d(p->dtout_screen); });
+        p->dtout_screen = p->dtout_screen * 1000 * O_SEC_YEAR;
+        rd([&] { r.d(p->dtout_file); });
+        p->dtout_file = p->dtout_file * 1000 * O_SEC_YEAR;
+        rd([&] {
+            for (int k = 0; k < 19; ++k) r.i(p->io_flags[k]);
+        });
+        rd([&] { r.i(p->lastout); });
+        rd([&] { r.d(p->dtsave_file); });
+        p->dtsave_file = p->dtsave_file * 1000 * O_SEC_YEAR;
+        rd([&] { r.i(p->lastsave); });
+    } catch (const ParseErr &) {
+        return GF_ERR_PARSE;
+    }
+    if (p->nx < 2 || p->nz < 2) return GF_ERR_PARSE;
+    return GF_OK;
+}
+
+// init_cord (src/init_cord.f90:5-93) for a mesh from the zone lists
+void init_cord(St &s) {
+    gf_params &p = *s.p;
+    int nx = p.nx, nz = p.nz;
+    if (p.ircoord > 0) throw Stop{GF_ERR_UNSUPPORTED};
+    // test_grid (init_cord.f90:97-137)
+    int sx = 0, sz = 0;
+    for (int k = 0; k < p.nzonx; ++k) sx += p.nelz_x[k];
+    for (int k = 0; k < p.nzony; ++k) sz += p.nelz_y[k];
+    if (p.nzonx != 0 && p.nzonx % 2 == 0) throw Stop{16};
+    if (sx != nx - 1) throw Stop{17};
+    if (p.nzony != 0 && p.nzony % 2 == 0) throw Stop{18};
+    if (sz != nz - 1) throw Stop{19};
+    std::vector<double> rm(nx + nz);
+    mesh1(p.x0, p.x0 + p.rxbo, rm.data(), nx, p.nzonx, p.nelz_x, p.sizez_x);
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) s.cordr(j, i, 0) = rm[i];
+    mesh1(p.z0, p.z0 + p.rzbo, rm.data(), nz, p.nzony, p.nelz_y, p.sizez_y);
+    for (int j = 0; j < nz; ++j)
+        for (int i = 0; i < nx; ++i) s.cordr(j, i, 1) = rm[j];
+    // surface relief of igeom 20 (table) and 21 (trapezoid), 1-based columns
+    for (int n = 0; n < p.inhom; ++n) {
+        double amp = p.xinitaps[n];
+        if (p.igeom[n] == 20) {
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) s.cordr(0, i - 1, 1) += amp;
+        } else if (p.igeom[n] == 21) {
+            for (int i = p.ix1[n]; i <= p.ix2[n] - 1; ++i)
+                s.cordr(0, i - 1, 1) += amp * (double)(float)(i - p.ix1[n]) / (p.ix2[n] - p.ix1[n]);
+            for (int i = p.ix2[n]; i <= p.iy1[n]; ++i) s.cordr(0, i - 1, 1) += amp;
+            for (int i = p.iy1[n] + 1; i <= p.iy2[n]; ++i)
+                s.cordr(0, i - 1, 1) += amp * (double)(float)(p.iy2[n] - i) / (p.iy2[n] - p.iy1[n]);
+        }
+    }
+    // every column re-spaced from its top to its bottom
+    for (int i = 0; i < nx; ++i) {
+        mesh1(s.cord(0, i, 1), s.cord(nz - 1, i, 1), rm.data(), nz, p.nzony, p.nelz_y, p.sizez_y);
+        for (int j = 0; j < nz; ++j) s.cordr(j, i, 1) = rm[j];
+    }
+    double dxmin = 1e300, dzmin = 1e300;
+    for (int i = 1; i < nx; ++i) dxmin = std::min(dxmin, s.cord(0, i, 0) - s.cord(0, i - 1, 0));
+    for (int j = 0; j < nz - 1; ++j) dzmin = std::min(dzmin, s.cord(j, 0, 1) - s.cord(j + 1, 0, 1));
+    p.dxmin = dxmin;
+    p.dzmin = dzmin;
+    gf_layout &L = *s.L;
+    for (int i = 0; i < nx; ++i) {
+        if (L.dhacc_correction) L.dhacc_correction[i] = 0.0;
+        if (L.dhacc) L.dhacc[i] = 0.0;
+        if (L.extr_acc) L.extr_acc[i] = 0.0;
+    }
+}
+
+// real(4) arithmetic of the reference's inclined zones: nint / floor /
+// ceiling of float(iy2-iy1)/float(ix2-ix1)*(j-ix1)
+inline float o_slope(int ix1, int ix2, int iy1, int iy2, int j) {
+    float a = (float)(iy2 - iy1) / (float)(ix2 - ix1);
+    return a * (float)(j - ix1);
+}
+inline int o_nint(float v) { return (int)(v < 0 ? -std::floor(-v + 0.5f) : std::floor(v + 0.5f)); }
+
+// init_phase (src/init_phase.f90:5-50): inclusions on the element phases
+// and plastic strain (1-based element ranges)
+void init_phase(St &s) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    if (p.irphase > 0) throw Stop{GF_ERR_UNSUPPORTED};
+    auto E = [&](int j, int i) { return s.e(j - 1, i - 1); };
+    for (int n = 0; n < p.inhom; ++n) {
+        if (p.igeom[n] == 0)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i)
+                for (int j = p.iy1[n]; j <= p.iy2[n]; ++j) {
+                    if (p.inphase[n] > 0) L.iphase[E(j, i)] = p.inphase[n];
+                    L.aps[E(j, i)] = p.xinitaps[n];
+                }
+        if (p.igeom[n] == 3)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                int j = o_nint(o_slope(p.ix1[n], p.ix2[n], p.iy1[n], p.iy2[n], i)) + p.iy1[n];
+                if (p.inphase[n] > 0) L.iphase[E(j, i)] = p.inphase[n];
+            }
+        if (p.igeom[n] == 4)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                float t = o_slope(p.ix1[n], p.ix2[n], p.iy1[n], p.iy2[n], i);
+                int j1 = (int)std::floor(t) + p.iy1[n], j2 = (int)std::ceil(t) + p.iy1[n];
+                for (int j = j1; j <= j2; ++j) {
+                    L.aps[E(j, i)] = p.xinitaps[n];
+                    if (p.inphase[n] > 0) L.iphase[E(j, i)] = p.inphase[n];
+                }
+            }
+    }
+}
+
+// init_marker (src/init_marker.f90:1-164): ms x ms points per element on
+// the reference's construction (3 x 3: the 1/6, 1/2, 5/6 weights along both
+// edges), each moved by up to half a point spacing with two draws of the
+// serial LCG chain, its phase from the age zone's layers at its depth; then
+// the inclusions and marker2elem.  ms other than 3 has no reference
+// counterpart; its points sit at (2m+1)/(2 ms) and move by up to half of
+// their spacing dx/ms.
+void init_marker(St &s) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    const int ms = p.markers_per_side > 0 ? p.markers_per_side : 3;
+    std::memset(L.mark_id_elem, 0, sizeof(int) * (size_t)s.d.E * GF_MAX_MARKERS_PER_ELEM);
+    std::memset(L.nmark_elem, 0, sizeof(int) * (size_t)s.d.E);
+    s.c->nmarkers = 0;
+    std::vector<double> wa(ms), wb(ms); // weights of an edge's first and second node
+    if (ms == 3) {
+        const double half = 0.5, onesixth = 0.1666666666666666666666, fivesixth = 0.8333333333333333333333;
+        wa[0] = fivesixth, wb[0] = onesixth;
+        wa[1] = half, wb[1] = half;
+        wa[2] = onesixth, wb[2] = fivesixth;
+    } else {
+        for (int m = 0; m < ms; ++m) {
+            wb[m] = (2.0 * m + 1.0) / (2.0 * ms);
+            wa[m] = 1.0 - wb[m];
+        }
+    }
+    std::vector<double> ax(ms), az(ms), bx(ms), bz(ms), ptx(ms * ms), ptz(ms * ms);
+    int iseed = 0;
+    for (int i = 1; i <= nx - 1; ++i)
+        for (int j = 1; j <= nz - 1; ++j) {
+            // a: points along the element's left edge, b: its right edge
+            for (int m = 0; m < ms; ++m) {
+                ax[m] = s.cord(j - 1, i - 1, 0) * wa[m] + s.cord(j, i - 1, 0) * wb[m];
+                az[m] = s.cord(j - 1, i - 1, 1) * wa[m] + s.cord(j, i - 1, 1) * wb[m];
+                bx[m] = s.cord(j - 1, i, 0) * wa[m] + s.cord(j, i, 0) * wb[m];
+                bz[m] = s.cord(j - 1, i, 1) * wa[m] + s.cord(j, i, 1) * wb[m];
+            }
+            for (int m = 0; m < ms; ++m)
+                for (int q = 0; q < ms; ++q) {
+                    ptx[m * ms + q] = ax[m] * wa[q] + bx[m] * wb[q];
+                    ptz[m * ms + q] = az[m] * wa[q] + bz[m] * wb[q];
+                }
+            double dx = s.cord(j - 1, i, 0) - s.cord(j - 1, i - 1, 0);
+            double dy = s.cord(j, i - 1, 1) - s.cord(j - 1, i - 1, 1);
+            iseed = iseed + i + j;
+            int l = 1, tries = 0;
+            while (l <= ms * ms) {
+                int kph = L.iphase[s.e(j - 1, i - 1)];
+                double rx = o_myrandom(iseed);
+                double ry = o_myrandom(iseed);
+                rx = 0.5 - rx;
+                ry = 0.5 - ry;
+                double ddx = dx * rx / ms;
+                double ddy = dy * ry / ms;
+                double xx = ptx[l - 1] + ddx;
+                double yy = ptz[l - 1] + ddy;
+                for (int n = 1; n <= p.nzone_age; ++n) {
+                    if (i < p.ixtb1[n - 1] || i > p.ixtb2[n - 1]) continue;
+                    if (n != 1 && p.iph_col_trans[n - 2] == 1) continue;
+                    int nl = p.nph_layer[n - 1];
+                    double hhc[GF_MAXZONE_LAYER];
+                    for (int m = 1; m <= nl - 1; ++m) hhc[m - 1] = p.hc[n - 1][m - 1];
+                    if (p.iph_col_trans[n - 1] == 1) {
+                        int i1 = p.ixtb1[n - 1], i2 = p.ixtb2[n - 1];
+                        double rr = (s.cord(0, i - 1, 0) - s.cord(0, i1 - 1, 0)) / (s.cord(0, i2 - 1, 0) - s.cord(0, i1 - 1, 0));
+                        for (int m = 1; m <= nl - 1; ++m)
+                            hhc[m - 1] = p.hc[n - 1][m - 1] + (p.hc[n][m - 1] - p.hc[n - 1][m - 1]) * rr;
+                    }
+                    double yyy = yy * (-1e-3);
+                    int m = 1;
+                    while (m <= nl - 1 && !(yyy < hhc[m - 1])) ++m; // the Fortran DO leaves m = nl
+                    kph = p.iph_col[n - 1][m - 1];
+                }
+                int inc = add_marker(s, xx, yy, kph, 0.0, j - 1, i - 1);
+                if (++tries > 1000 * ms * ms) throw Stop{133};
+                if (inc <= 0) continue;
+                l = l + 1;
+            }
+        }
+    for (int n = 0; n < p.inhom; ++n) {
+        if (p.inphase[n] < 0) continue;
+        if (p.igeom[n] == 0) newphase2marker(s, p.iy1[n], p.iy2[n], p.ix1[n], p.ix2[n], p.inphase[n]);
+        if (p.igeom[n] == 3)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                int k = o_nint(o_slope(p.ix1[n], p.ix2[n], p.iy1[n], p.iy2[n], i)) + p.iy1[n];
+                newphase2marker(s, k, k, i, i, p.inphase[n]);
+            }
+        if (p.igeom[n] == 4)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                float t = o_slope(p.ix1[n], p.ix2[n], p.iy1[n], p.iy2[n], i);
+                newphase2marker(s, (int)std::floor(t) + p.iy1[n], (int)std::ceil(t) + p.iy1[n], i, i, p.inphase[n]);
+            }
+    }
+    marker2elem(s);
+}
+
+// init_temp (src/init_temp.f90:3-124): the age zones' geotherms, radiogenic
+// sources by depth, Gaussian perturbations (igeom 11, 13, 14)
+void init_temp(St &s) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    if (p.irtemp > 0) throw Stop{GF_ERR_UNSUPPORTED};
+    for (int n = 1; n <= p.nzone_age; ++n) {
+        if (n != 1 && p.iph_col_trans[n - 2] == 1) continue;
+        for (int i = p.ixtb1[n - 1]; i <= p.ixtb2[n - 1]; ++i) {
+            double age = p.age_1[n - 1], t1 = p.tp1[n - 1], t2 = p.tp2[n - 1];
+            if (p.iph_col_trans[n - 1] == 1) {
+                int i1 = p.ixtb1[n - 1], i2 = p.ixtb2[n - 1];
+                double ratio = (s.cord(0, i - 1, 0) - s.cord(0, i1 - 1, 0)) / (s.cord(0, i2 - 1, 0) - s.cord(0, i1 - 1, 0));
+                age = p.age_1[n - 1] + (p.age_1[n] - p.age_1[n - 1]) * ratio;
+                t1 = p.tp1[n - 1] + (p.tp1[n] - p.tp1[n - 1]) * ratio;
+                t2 = p.tp2[n - 1] + (p.tp2[n] - p.tp2[n - 1]) * ratio;
+            }
+            geotherm_column(s, n - 1, i - 1, age, t1, t2);
+        }
+    }
+    for (int j = 0; j < nz - 1; ++j) {
+        double y = -(s.cord(j + 1, 0, 1) + s.cord(j, 0, 1)) / 2 / 1000;
+        double v = p.hs * std::exp(-y / p.hr);
+        for (int i = 0; i < nx - 1; ++i) L.source[s.e(j, i)] = v;
+    }
+    auto T = [&](int j, int i) -> double & { return L.temp[o_node(s.d, j - 1, i - 1)]; };
+    for (int n = 0; n < p.inhom; ++n) {
+        int g = p.igeom[n];
+        if (g != 11 && g != 13 && g != 14) continue;
+        int ixc = (p.ix1[n] + p.ix2[n]) / 2, iwidth = p.ix2[n] - p.ix1[n];
+        double amp = p.xinitaps[n];
+        auto pert_of = [&](int i) {
+            double t = (double)(float)(i - ixc) / (0.25 * (double)(float)iwidth);
+            return amp * std::exp(-(t * t));
+        };
+        if (g == 11)
+            for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                double pert = pert_of(i);
+                for (int k = p.iy1[n]; k <= p.iy2[n]; ++k) {
+                    double pert2 = 1.0 * (k - p.iy1[n]) / (p.iy2[n] - p.iy1[n]);
+                    T(k, i) = std::min(p.t_bot, T(k, i) + pert * pert2);
+                }
+            }
+        else
+            for (int k = p.iy1[n]; k <= p.iy2[n]; ++k) {
+                int kk = k - p.iy1[n];
+                for (int i = p.ix1[n]; i <= p.ix2[n]; ++i) {
+                    int ic = g == 13 ? i + kk : i - kk;
+                    T(k, ic) = std::max(p.t_top, std::min(p.t_bot, T(k, ic) + pert_of(i)));
+                }
+            }
+    }
+}
+
+// init_stress (src/init_stress.f90:5-60): hydrostatic prestress per column
+// (oceanic columns under 8 km of water), pisos for the Winkler foundation
+void init_stress(St &s) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    p.pisos = 0.0;
+    for (int i = 1; i <= nx - 1; ++i) {
+        int top = L.iphase[s.e(0, i - 1)];
+        double rogh = (top == 3 || top == 7) ? -1030.0 * p.g * 8.0e3 : 0.0; // kocean1, kocean2
+        for (int j = 1; j <= nz - 1; ++j) {
+            long long e = s.e(j - 1, i - 1);
+            int iph = L.iphase[e] - 1;
+            double tmpr = 0.25 * (s.temp(j - 1, i - 1) + s.temp(j, i - 1) + s.temp(j - 1, i) + s.temp(j, i));
+            double densT = p.den[iph] * (1 - p.alfa[iph] * tmpr);
+            double dh1 = s.cord(j - 1, i - 1, 1) - s.cord(j, i - 1, 1);
+            double dh2 = s.cord(j - 1, i, 1) - s.cord(j, i, 1);
+            double dh = 0.5 * (dh1 + dh2);
+            double dPT = densT * p.g * dh;
+            double dP = dPT * (1 - p.beta[iph] * rogh) / (1 + p.beta[iph] / 2 * dPT);
+            double press = rogh + 0.5 * dP;
+            for (int k = 0; k < 4; ++k) {
+                s.st(e, 0, k) = -press;
+                s.st(e, 1, k) = -press;
+                s.st(e, 2, k) = 0.0;
+                s.st(e, 3, k) = -press;
+            }
+            rogh = rogh + dP;
+        }
+        if (i == nx - 1 && p.nyhydro == 2) p.pisos = rogh + p.extra_pres;
+    }
+}
+
+// velbc (src/init_bc.f90:284-339) at node (j,i) (0-based) for condition n
+void velbc(St &s, int n, int j, int i, double x) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    const double pi2 = 2.0 * 3.14159;
+    double fun = p.bca[n] + p.bcb[n] * x + p.bcc[n] * x * x +
+                 (p.bcd[n] * std::cos(pi2 * p.bce[n] * x) + p.bcf[n] * std::sin(pi2 * p.bcg[n] * x)) *
+                     std::exp(-((x - p.bci[n]) * p.bch[n]) * ((x - p.bci[n]) * p.bch[n]));
+    long long kx = o_n2(s.d, j, i, 0), kz = o_n2(s.d, j, i, 1);
+    if (p.nbc[n] == 10) {
+        L.ncod[kx] = 1;
+        if (std::fabs(L.bc[kx]) > 0.0) fun = L.bc[kx];
+        L.bc[kx] = fun;
+    }
+    if (p.nbc[n] == 1 || p.nbc[n] == 200) {
+        L.ncod[kz] = 1;
+        L.bc[kz] = p.nbc[n] == 200 ? 0.0 : fun;
+    }
+}
+
+// init_bc (src/init_bc.f90:4-221) for velocity conditions on the four
+// sides (stress conditions and the mid-domain side 5 are not restated) and
+// vbcal (:385-409)
+void init_bc(St &s) {
+    gf_params &p = *s.p;
+    gf_layout &L = *s.L;
+    int nx = p.nx, nz = p.nz;
+    std::memset(L.bc, 0, sizeof(double) * 2 * (size_t)s.d.N);
+    std::memset(L.ncod, 0, sizeof(int) * 2 * (size_t)s.d.N);
+    p.incoming_left = 0;
+    p.incoming_right = 0;
+    for (int n = 0; n < p.nofbc; ++n) {
+        int t = p.nbc[n], side = p.nofside[n];
+        if (t == 2 || t == 20 || t == 40 || side == 5) throw Stop{GF_ERR_UNSUPPORTED};
+        int ndbc = p.nbc2[n] - p.nbc1[n] + 1;
+        bool vel = t == 1 || t == 10 || t == 30 || (side == 2 && t == 200);
+        // coordinate along the side, scaled to [0,1] over the condition's range
+        auto along = [&](int k) -> double { // k: 1-based node along the side
+            if (side == 1) return s.cord(k - 1, 0, 1);
+            if (side == 3) return s.cord(k - 1, nx - 1, 1);
+            if (side == 2) return s.cord(nz - 1, k - 1, 0);
+            return s.cord(0, k - 1, 0);
+        };
+        double x1 = along(p.nbc1[n]), x2 = along(p.nbc2[n]);
+        for (int m = 1; m <= ndbc; ++m) {
+            int numbp = m + p.nbc1[n] - 1;
+            double x = (along(numbp) - x1) / (x2 - x1);
+            if (vel) {
+                if (side == 1) velbc(s, n, numbp - 1, 0, x);
+                if (side == 2) velbc(s, n, nz - 1, numbp - 1, x);
+                if (side == 3) velbc(s, n, numbp - 1, nx - 1, x);
+                if (side == 4) velbc(s, n, 0, numbp - 1, x);
+            }
+            if (side == 1 && (t == 1 || t == 10) && p.bca[n] > 0) p.incoming_left = 1;
+            if (side == 3 && (t == 1 || t == 10) && p.bca[n] < 0) p.incoming_right = 1;
+        }
+    }
+    p.nopbmax = 0;
+    double vbc = 0.0;
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j)
+            for (int k = 0; k < 2; ++k) {
+                int c = L.ncod[o_n2(s.d, j, i, k)];
+                if (c == 1 || c == 10 || c == 30) vbc = std::max(vbc, std::fabs(L.bc[o_n2(s.d, j, i, k)]));
+            }
+    if (vbc == 0.0) vbc = 1.0e-10;
+    p.vbc = vbc;
+}
+
+// setflac (src/setflac.f90:4-66): the start-up state up to (not including)
+// rmasses / init_visc / dt_mass, which or_finish_setflac runs
+void setflac(St &s) {
+    gf_params &p = *s.p;
+    gf_clock &c = *s.c;
+    gf_layout &L = *s.L;
+    size_t N = (size_t)s.d.N, E = (size_t)s.d.E;
+    std::memset(&c, 0, sizeof c);
+    c.nloop = 0;
+    c.time = 0.0;
+    c.frac = p.frac;
+    init_cord(s);
+    std::fill(L.aps, L.aps + E, 0.0);
+    std::fill(L.vel, L.vel + 2 * N, 0.0);
+    std::fill(L.dvol, L.dvol + 4 * E, 0.0);
+    std::fill(L.strain, L.strain + 3 * E, 0.0);
+    init_phase(s);
+    init_marker(s);
+    // check_visc_rheol (src/init_phase.f90:56-72)
+    p.ivis_present = 0;
+    for (size_t e = 0; e < E; ++e) {
+        int irh = p.irheol[L.iphase[e] - 1];
+        if (irh == 3 || irh >= 11) p.ivis_present = 1;
+    }
+    init_areas(s);
+    double amin = 1e300;
+    for (size_t e = 0; e < E; ++e) amin = std::min(amin, 0.5 / L.area[e] + 0.5 / L.area[E + e]);
+    p.Amin = amin;
+    init_temp(s);
+    init_stress(s);
+    init_bc(s);
+    std::copy(L.temp, L.temp + N, L.temp0);
+    if (L.xoriginal) std::copy(L.cord, L.cord + N, L.xoriginal);
+    if (L.zoriginal) std::copy(L.cord + N, L.cord + 2 * N, L.zoriginal);
+    for (double *f : {L.shrheat, L.sshrheat, L.fmagma, L.fmagma2, L.dike_released, L.fmelt, L.fmelt2, L.dike_backlog,
+                      L.dike_marker_vol, L.mor_marker_vol, L.visn})
+        if (f) std::fill(f, f + E, 0.0);
+    std::fill(L.e2sr, L.e2sr + E, 1e-16);
+    std::fill(L.se2sr, L.se2sr + 3 * E, 1e-16);
+    if (L.dtopo) std::fill(L.dtopo, L.dtopo + p.nx, 0.0);
+    if (L.extrusion) std::fill(L.extrusion, L.extrusion + p.nx, 0.0);
+    if (L.q_init) std::fill(L.q_init, L.q_init + p.nx, 0.0);
+    std::fill(L.amass, L.amass + N, 0.0);
+    std::fill(L.rmass, L.rmass + N, 0.0);
+    c.dtavg = 0.0;
+    c.nsrate = -1;
+}
+
 template <class F> int guard(F &&f) {
     try {
         f();
@@ -2458,6 +3239,25 @@ template <class F> int guard(F &&f) {
 } // namespace
 
 extern "C" {
+
+// 1: the oracle's exp/pow/sin/tan from the C library; 0: from gf_math.h
+void or_set_libm(int on) { g_libm = on != 0; }
+
+// Batch evaluation of gf_math.h's functions (fn 0 exp, 1 log, 2 pow, 3 sin,
+// 4 cos, 5 tan) for the accuracy test against the C library; y only for pow
+void or_gfm(int fn, const double *x, const double *y, double *out, long long n) {
+    for (long long k = 0; k < n; ++k) {
+        double v = x[k];
+        switch (fn) {
+        case 0: out[k] = gfm::exp(v); break;
+        case 1: out[k] = gfm::log(v); break;
+        case 2: out[k] = gfm::pow(v, y[k]); break;
+        case 3: out[k] = gfm::sin(v); break;
+        case 4: out[k] = gfm::cos(v); break;
+        default: out[k] = gfm::tan(v); break;
+        }
+    }
+}
 
 void or_set_threads(int n) { g_threads = n > 0 ? n : 1; }
 int or_get_threads(void) { return g_threads; }
@@ -2481,6 +3281,20 @@ OR_ENTRY(bar2euler, bar2euler(s))
 OR_ENTRY(lpeuler2bar, lpeuler2bar(s))
 OR_ENTRY(remesh, remesh(s))
 OR_ENTRY(remesh_event, remesh_event(s))
+
+// read_params (src/read_params.f90:3-348) into *p; markers_per_side,
+// eclogite_rule and therm_sweeps keep the caller's values
+int or_read_params(const char *path, gf_params *p) {
+    if (!path || !p) return GF_ERR_ARG;
+    return read_params(path, p);
+}
+
+// setflac (src/setflac.f90:4-66) on the caller's host arrays
+int or_setflac(gf_params *p, gf_clock *c, gf_layout *L) {
+    if (!p || !c || !L || L->nx != p->nx || L->nz != p->nz || L->nphase != p->nphase) return GF_ERR_ARG;
+    St s = make(p, c, L);
+    return guard([&] { setflac(s); });
+}
 
 // rmasses, init_visc, dt_mass and the averaging reset of setflac.f90:71-81
 int or_finish_setflac(gf_params *p, gf_clock *c, gf_layout *L) {

@@ -39,10 +39,44 @@ def load():
     lib.or_step.argtypes = [P, K, L, C.c_int]
     lib.or_itest_mesh.restype = C.c_int
     lib.or_itest_mesh.argtypes = [P, K, L, C.POINTER(C.c_double)]
+    lib.or_read_params.restype = C.c_int
+    lib.or_read_params.argtypes = [C.c_char_p, P]
+    lib.or_setflac.restype = C.c_int
+    lib.or_setflac.argtypes = [P, K, L]
     lib.or_set_threads.argtypes = [C.c_int]
     lib.or_set_threads.restype = None
     _lib = lib
     return lib
+
+
+def read_params(path: str, markers_per_side: int = 3, eclogite_rule: int = 0,
+                therm_sweeps: int = 0) -> GfParams:
+    """The oracle's own read_params of an .inp file."""
+    lib = load()
+    p = GfParams()
+    p.markers_per_side = markers_per_side
+    p.eclogite_rule = eclogite_rule
+    p.therm_sweeps = therm_sweeps
+    rc = lib.or_read_params(path.encode(), C.byref(p))
+    if rc:
+        raise RuntimeError(f"oracle read_params({path}): status {rc}")
+    return p
+
+
+def new_state(path: str, markers_per_side: int = 3, eclogite_rule: int = 0, therm_sweeps: int = 0):
+    """Start-up state (params, clock, host arrays) built by the oracle alone:
+    its read_params and setflac chain (init_cord .. init_bc), without the
+    product's library.  or_finish_setflac (Oracle.finish_setflac) completes
+    it with rmasses, init_visc and dt_mass."""
+    from geoflac_gb300.capi import HostState
+
+    p = read_params(path, markers_per_side, eclogite_rule, therm_sweeps)
+    s = HostState(p)
+    c = GfClock()
+    rc = load().or_setflac(C.byref(p), C.byref(c), C.byref(s.layout))
+    if rc:
+        raise RuntimeError(f"oracle setflac: status {rc}")
+    return p, c, s
 
 
 class Oracle:

@@ -26,3 +26,11 @@ def compare_states(gpu, ref, fields=FLOAT_FIELDS, ints=INT_FIELDS):
         out[f] = rel_diff(gpu[f], ref[f])
     bad_ints = [f for f in ints if not np.array_equal(gpu[f], ref[f])]
     return out, bad_ints
+
+
+def oracle_state(path: str, **kw):
+    """The oracle's own start-up state of an .inp file (its read_params and
+    setflac chain; nothing of the product's host code)."""
+    from oracle.oracle import new_state as oracle_new_state
+
+    return oracle_new_state(path, **kw)

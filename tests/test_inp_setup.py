@@ -204,3 +204,45 @@ def test_hydrostatic_prestress_and_winkler_pisos(workdir):
             pisos = rogh + p.extra_pres
     assert pisos > 0
     assert p.pisos == pytest.approx(pisos, rel=1e-13)
+
+
+def _struct_diff(a, b):
+    """Fields of two ctypes structures whose bytes differ."""
+    import ctypes as C
+
+    out = []
+    for name, _ in a._fields_:
+        f = getattr(type(a), name)
+        if C.string_at(C.addressof(a) + f.offset, f.size) != C.string_at(C.addressof(b) + f.offset, f.size):
+            out.append(name)
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(inpgen.CONFIGS))
+@pytest.mark.parametrize("ms", [3, 5])
+def test_oracle_startup_equals_library_startup(workdir, name, ms):
+    """The oracle builds its initial state on its own (read_params and the
+    setflac chain restated from the Fortran: init_cord, init_phase,
+    init_marker with its serial LCG chain, check_visc_rheol, init_areas,
+    init_temp, init_stress, init_bc, vbcal); the library's host start-up
+    gives the same parameters, clock and arrays bit for bit."""
+    from oracle.oracle import new_state as oracle_new_state
+
+    path = inpgen.CONFIGS[name]().write(str(workdir / f"st_{name}_{ms}.inp"))
+    p1, c1, s1 = new_state(path, markers_per_side=ms)
+    p2, c2, s2 = oracle_new_state(path, markers_per_side=ms)
+    assert _struct_diff(p1, p2) == []
+    assert _struct_diff(c1, c2) == []
+    bad = [k for k in s1.arrays if not np.array_equal(s1.arrays[k], s2.arrays[k])]
+    assert bad == []
+    assert c2.nmarkers == ms * ms * (p2.nx - 1) * (p2.nz - 1)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference inputs not mounted")
+def test_oracle_reads_reference_inputs_like_the_library():
+    from oracle.oracle import read_params as oracle_read_params
+
+    files = sorted(glob.glob(f"{REF}/benchmark/*.inp") + glob.glob(f"{REF}/examples/**/*.inp", recursive=True))
+    assert files
+    for f in files:
+        assert _struct_diff(capi.read_params(f), oracle_read_params(f)) == [], f

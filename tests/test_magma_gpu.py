@@ -17,11 +17,11 @@ steps 0, 10, 20, 30)."""
 import numpy as np
 import pytest
 
-from geoflac_gb300 import capi, clone, inpgen, new_state
+from geoflac_gb300 import capi, inpgen, new_state
 from geoflac_gb300.flac import Flac
 from oracle.oracle import Oracle
 
-from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states
+from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states, oracle_state
 
 pytestmark = pytest.mark.gpu
 
@@ -47,9 +47,11 @@ def _set_phase(s, j, i, ph):
     s["mark_phase"][ids - 1] = ph
 
 
-def magma_state(workdir, tag):
+def magma_state(workdir, tag, make=new_state):
+    """The seeded arc model; `make` builds the start-up state (the
+    library's new_state, or the oracle's own for the oracle side)."""
     m = inpgen.magma_arc()
-    p, c, s = new_state(m.write(str(workdir / f"magma_{tag}.inp")))
+    p, c, s = make(m.write(str(workdir / f"magma_{tag}.inp")))
     T = s["temp"]
     T[2:5, 8:17] = 1500.0  # hot mantle: MOR melt (Katz solidus ~1300 C at 60 km)
     for i in range(34, 38):  # subducted basalt / sediment below the Moho
@@ -76,7 +78,7 @@ def magma_state(workdir, tag):
 
 def _pair(workdir, tag):
     p, c, s = magma_state(workdir, tag)
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = magma_state(workdir, tag + "_o", make=oracle_state)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     return Flac(p, c, s, "fp64"), orc

@@ -16,8 +16,8 @@ import math
 import numpy as np
 import pytest
 
-from geoflac_gb300 import clone, inpgen, new_state
-from oracle.oracle import Oracle
+from geoflac_gb300 import clone, inpgen
+from oracle.oracle import Oracle, new_state
 
 from .test_magma_gpu import _set_phase, recount
 

@@ -12,8 +12,8 @@ import math
 import numpy as np
 import pytest
 
-from geoflac_gb300 import capi, inpgen, new_state
-from oracle.oracle import Oracle
+from geoflac_gb300 import capi, inpgen
+from oracle.oracle import Oracle, new_state
 
 SEC_YEAR = capi.SEC_YEAR
 

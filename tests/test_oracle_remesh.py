@@ -3,8 +3,8 @@ lpeuler2bar -> marker2elem, src/par.f90:89-108) on a deformed convergent
 model: the regridded mesh, the marker bookkeeping and the phase ratios."""
 import numpy as np
 
-from geoflac_gb300 import inpgen, new_state
-from oracle.oracle import Oracle
+from geoflac_gb300 import inpgen
+from oracle.oracle import Oracle, new_state
 
 
 def test_remesh_event_invariants(workdir):

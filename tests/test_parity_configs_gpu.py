@@ -14,11 +14,11 @@ counts) bit-exact.
 import numpy as np
 import pytest
 
-from geoflac_gb300 import clone, inpgen, new_state
+from geoflac_gb300 import inpgen, new_state
 from geoflac_gb300.flac import Flac
 from oracle.oracle import Oracle
 
-from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states
+from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states, oracle_state
 
 pytestmark = pytest.mark.gpu
 
@@ -50,7 +50,7 @@ def test_extension_1000x300_25_markers_with_remesh(workdir):
     # 25 markers in every element, each inside its own element at start-up
     assert c.nmarkers == 25 * E
     assert np.all(s["nmark_elem"] == 25)
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = oracle_state(inp, markers_per_side=5)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     gpu = Flac(p, c, s, "fp64")
@@ -95,7 +95,8 @@ def test_eclogite_rule_matches_oracle(workdir, rule):
     p, c, s = new_state(inp, eclogite_rule=rule)
     assert p.eclogite_rule == rule
     _seed_basalt(p, s)
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = oracle_state(inp, eclogite_rule=rule)
+    _seed_basalt(p2, s2)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     gpu = Flac(p, c, s, "fp64")

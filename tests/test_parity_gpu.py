@@ -8,11 +8,11 @@ fields (iphase, marker element/triangle indices, phase counts) bit-exact.
 import numpy as np
 import pytest
 
-from geoflac_gb300 import capi, clone, inpgen, new_state
+from geoflac_gb300 import capi, inpgen, new_state
 from geoflac_gb300.flac import Flac
 from oracle.oracle import Oracle
 
-from ._util import compare_states, rel_diff
+from ._util import compare_states, oracle_state, rel_diff
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +23,7 @@ ROUTINES = ("fl_therm", "change_phase", "fl_rheol", "fl_node", "fl_move", "rmass
 def _pair(workdir, name, mode="fp64", **kw):
     inp = inpgen.CONFIGS[name]().write(str(workdir / f"{name}.inp"))
     p, c, s = new_state(inp, **kw)
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = oracle_state(inp, **kw)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     gpu = Flac(p, c, s, mode)
@@ -45,6 +45,9 @@ def _assert_close(gpu, orc, tol=TOL, where=""):
 
 @pytest.mark.parametrize("name", ["extension_60x20", "convergence_60x15"])
 def test_setflac_parity(workdir, name):
+    """The library's start-up state finished on the device (rmasses,
+    init_visc, dt_mass) against the oracle's own read_params, setflac chain
+    and finish."""
     gpu, orc = _pair(workdir, name)
     _assert_close(gpu, orc, where="setflac")
     gpu.close()

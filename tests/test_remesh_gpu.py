@@ -10,11 +10,11 @@ for 50 steps after the event within the step parity tolerance 1e-10.
 import numpy as np
 import pytest
 
-from geoflac_gb300 import clone, inpgen, new_state
+from geoflac_gb300 import inpgen, new_state
 from geoflac_gb300.flac import Flac
 from oracle.oracle import Oracle
 
-from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states
+from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states, oracle_state
 
 pytestmark = pytest.mark.gpu
 
@@ -27,7 +27,7 @@ EXTRA_INTS = ("jmoho",)
 def _pair(workdir, name, mode="fp64", **kw):
     inp = inpgen.CONFIGS[name]().write(str(workdir / f"{name}_rm.inp"))
     p, c, s = new_state(inp, **kw)
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = oracle_state(inp, **kw)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     return Flac(p, c, s, mode), orc

@@ -13,11 +13,11 @@ largest magnitude (FP64 path, 60 steps).
 import numpy as np
 import pytest
 
-from geoflac_gb300 import capi, clone, inpgen, new_state
+from geoflac_gb300 import capi, inpgen, new_state
 from geoflac_gb300.flac import Flac
 from oracle.oracle import Oracle
 
-from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states
+from ._util import FLOAT_FIELDS, INT_FIELDS, compare_states, oracle_state
 
 pytestmark = pytest.mark.gpu
 
@@ -39,10 +39,11 @@ def _init_areas(s):
     a[:, :, 3] = 1.0 / (((x4 * y3 - y4 * x3) - (x1 * y3 - y1 * x3)) + (x1 * y4 - y1 * x4))
 
 
-def _setup(workdir, tag, mode="fp64"):
-    m = inpgen.extension_60x20()
-    m.topo_kappa = 2e-5
-    p, c, s = new_state(m.write(str(workdir / f"surf_{tag}.inp")))
+def _surface_state(path, make):
+    """The 60x20 model with a surface relief and accumulated surface
+    changes; `make` builds the start-up state (the library's or the
+    oracle's own)."""
+    p, c, s = make(path)
     for k in range(p.nphase):
         p.erodibility[k] = 0.5 + 0.25 * k
     x = s["cord"][0, :, 0]
@@ -56,7 +57,15 @@ def _setup(workdir, tag, mode="fp64"):
     dh[3:-3:7] = -1.5 * elz[3:-3:7] / kinc[3:-3:7]
     dh[6:-3:7] = 1.5 * elz[6:-3:7] / kinc[6:-3:7]
     s["dhacc"][...] = dh
-    p2, c2, s2 = clone(p, c, s)
+    return p, c, s
+
+
+def _setup(workdir, tag, mode="fp64"):
+    m = inpgen.extension_60x20()
+    m.topo_kappa = 2e-5
+    path = m.write(str(workdir / f"surf_{tag}.inp"))
+    p, c, s = _surface_state(path, new_state)
+    p2, c2, s2 = _surface_state(path, oracle_state)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     return Flac(p, c, s, mode), orc
@@ -138,13 +147,13 @@ def test_batch_rejects_surface_processes(workdir):
     gpu.close()
 
 
-def _flex_model(workdir, tag, mode="fp64"):
+def _flex_model(workdir, tag, mode="fp64", make=new_state):
     """The 60x20 model on a flexural bottom (nbc 200: 20 km elastic plate on
     a 3300 kg/m3 fluid) instead of the free-slip base, with a surface relief
-    whose load the plate carries."""
+    whose load the plate carries; `make` builds the start-up state."""
     m = inpgen.extension_60x20()
     m.bcs = [b for b in m.bcs if b.side != 2] + [inpgen.BC(2, 1, m.nex + 1, 200, 20e3, 3300.0)]
-    p, c, s = new_state(m.write(str(workdir / f"flex_{tag}.inp")))
+    p, c, s = make(m.write(str(workdir / f"flex_{tag}.inp")))
     x = s["cord"][0, :, 0]
     s["cord"][0, :, 1] += 300.0 * np.exp(-((x - 150e3) / 30e3) ** 2)
     _init_areas(s)
@@ -154,7 +163,7 @@ def _flex_model(workdir, tag, mode="fp64"):
 def test_flexure_matches_oracle(workdir):
     p, c, s = _flex_model(workdir, "a")
     assert p.nbc[[b for b in range(p.nofbc) if p.nofside[b] == 2][0]] == 200
-    p2, c2, s2 = clone(p, c, s)
+    p2, c2, s2 = _flex_model(workdir, "a_o", make=oracle_state)
     orc = Oracle(p2, c2, s2)
     orc.finish_setflac()
     gpu = Flac(p, c, s, "fp64")
