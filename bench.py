@@ -370,41 +370,148 @@ def run_ours(args):
     e2e_steps = max(5, min(args.steps, 20))
     e2e_wall, h2d, d2h = _time_e2e(g, e2e_steps)
     e2e_value = ws * E * e2e_steps / e2e_wall
+    e2e = {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "steps": e2e_steps,
+           "path": "per-subroutine C-ABI calls, clock scalars in/out, cord+vel to host every step"}
+    roofline = {"bound": "hbm", "kernel": "k_rheol (fl_rheol, FP64)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "avg_launch_s": t_rheol, "algorithmic_bytes_per_launch": alg, "compute": _ncu_pipe("k_rheol_fp64")}
+    for r in res.values():
+        r["g"].close()
+    err10 = mixed_error_steps(inp, 10)
+    detail = {"mixed_rel_err_vs_fp64": mixed_err, "mixed_err_after_steps": args.steps + args.warmup,
+              "mixed_rel_err_vs_fp64_10_steps": err10, "fp64_perturbed_1e-7_rel_err": perturbed_err,
+              "mixed_roofline": mixed_roofline, "e2e": e2e, "roofline": roofline,
+              "therm_sweeps_fp64": fp["g"].clock.therm_sweeps, "clocks_mixed": res["mixed"]["clocks"]}
     out = {
         "metric": METRIC, "value": value, "unit": "element-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * fp["t"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .inp model)",
         "config": bench_config(ws),
-        "mixed": {"value": mixed_value, "ms_per_step": 1e3 * res["mixed"]["t"] / args.steps,
-                  "speedup_vs_fp64": mixed_value / value, "dtype": "f32 element fields / f64 nodes",
-                  "rel_err_vs_fp64": mixed_err, "err_after_steps": args.steps + args.warmup,
-                  "fp64_perturbed_1e-7_rel_err": perturbed_err, "roofline": mixed_roofline},
-        "therm_sweeps_fp64": fp["g"].clock.therm_sweeps,
-        "e2e": {"value": e2e_value, "unit": "element-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
-                "path": "per-subroutine C-ABI calls, clock scalars in/out, cord+vel to host every step"},
-        "roofline": {"bound": "hbm", "kernel": "k_rheol (fl_rheol, FP64)", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic, "avg_launch_s": t_rheol,
-                     "algorithmic_bytes_per_launch": alg, "compute": _ncu_pipe("k_rheol_fp64")},
+        "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
+        "roofline": {k: _r(roofline[k]) for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
         "gpu_launches": fp["launches"],
-        "clocks": fp["clocks"],
+        "clocks": {k: fp["clocks"].get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+        "mixed": {"value": _r(mixed_value), "ms_per_step": _r(1e3 * res["mixed"]["t"] / args.steps),
+                  "speedup_vs_fp64": _r(mixed_value / value),
+                  "vel_rel_err_vs_fp64": {"10_steps": _r(err10["vel"]), f"{args.steps + args.warmup}_steps":
+                                          _r(mixed_err["vel"])},
+                  "fp64_own_vel_change_1e-7": _r(perturbed_err["vel"]),
+                  "roofline_frac": _r(mixed_roofline["frac"])},
     }
-    for r in res.values():
-        r["g"].close()
     if args.members > 0:
-        out["batched"] = bench_batch(args, d, local)
-        out["batched"]["surrogate"] = None
+        bt = bench_batch(args, d, local)
+        detail["batched"] = dict(bt)
+        out["batched"] = {"value": _r(bt["value"]), "ms_per_step": _r(bt["ms_per_step"]), "members": bt["members"],
+                          "elements": bt["elements"], "roofline_frac": _r(bt["roofline"]["frac"]),
+                          "config": bt["config"]}
         if args.sur_epochs > 0:
-            args.batch_cfg = {k: v for k, v in out["batched"]["config"].items()}
-            out["batched"]["surrogate"] = bench_surrogate(args, d)
+            args.batch_cfg = {k: v for k, v in bt["config"].items()}
+            sg = bench_surrogate(args, d)
+            detail["surrogate"] = sg
+            out["surrogate"] = {"speedup_vs_plain": _r(sg["speedup_vs_plain"]),
+                                "screen_s": _r(sg["screen_seconds"]), "plain_s": _r(sg["plain_seconds"]),
+                                "rerun_members": sg["rerun_members"],
+                                "rel_err": {k: {q: _r(v) for q, v in sg["rel_err"][k].items()}
+                                            for k in ("topography", "plastic_strain")},
+                                "members_over_2pct": sg["members_over_2pct"]}
+    if args.c3_steps > 0:
+        c3 = bench_config3(args, d)
+        detail["config3"] = c3
+        out["config3"] = {k: c3[k] for k in ("steps", "ms_per_step_fp64", "ms_per_step_mixed", "rel_err_vs_fp64",
+                                             "fp64_own_change_1e-7", "status")}
     if rank == 0 and ws == 1 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(inp, steps=args.cpu_steps)
+        cb = cpu_baselines(inp, args)
+        detail["cpu_baselines"] = cb
+        out["cpu_baseline"] = dict(cb["extension_1000x300"]["all_cores"])
+        out["cpu_baseline"]["value_1_thread"] = _r(cb["extension_1000x300"]["1_thread"]["value"])
+        out["cpu_baseline"]["extension_60x20"] = {k: _r(v["value"]) for k, v in cb["extension_60x20"].items()}
     if rank == 0:
+        # details first (an earlier line), the compact record last
+        print(json.dumps({"detail": detail}))
         print(json.dumps(out))
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def _r(x, digits=4):
+    """Round floats to `digits` significant digits for the compact record."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}")
+    return x
+
+
+def _field_errors(a, b, fields=("vel", "cord", "temp", "stress0", "aps")):
+    """max |a - b| / max |b| per field"""
+    return {f: float(abs(a[f] - b[f]).max() / max(abs(b[f]).max(), 1e-300)) for f in fields}
+
+
+def mixed_error_steps(inp: str, steps: int):
+    """Per-field error of the mixed path against the FP64 path, both advanced
+    `steps` steps from the same start-up state of the bench's model."""
+    a, b = _make_model(inp, "fp64"), _make_model(inp, "mixed")
+    a.step(steps)
+    b.step(steps)
+    err = _field_errors(b.download(), a.download())
+    a.close()
+    b.close()
+    return err
+
+
+def bench_config3(args, workdir: str):
+    """The convergent workload (600x150 quads, 1200 km x 300 km: 60-Myr
+    oceanic plate with basalt and weak sediment, continental plate, left wall
+    at 5 cm/yr, Winkler base, basalt -> eclogite above 600 C and 1.5 GPa)
+    advanced `--c3-steps` steps in FP64 and in mixed precision from the same
+    start; per-field error of the mixed run against the FP64 run, beside the
+    FP64 run's own change when its initial stresses are perturbed by a
+    relative 1e-7 (FP32 rounding size)."""
+    import numpy as np
+    import torch
+
+    from geoflac_gb300 import inpgen, new_state
+    from geoflac_gb300.flac import Flac
+
+    inp = inpgen.convergence(600, 150).write(os.path.join(workdir, "convergence_600x150.inp"))
+    steps = args.c3_steps
+    fields = ("vel", "cord", "temp", "stress0", "aps")
+    states, times, status = {}, {}, "ok"
+    for tag, mode, perturb in (("fp64", "fp64", False), ("mixed", "mixed", False), ("fp64_pert", "fp64", True)):
+        p, c, s = new_state(inp, eclogite_rule=1)
+        if perturb:
+            st = s["stress0"]
+            st[...] = st * (1.0 + 1e-7 * np.random.default_rng(7).standard_normal(st.shape))
+        g = Flac(p, c, s, mode)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            g.step(steps)
+            g.status()
+        except Exception as e:  # a stop code of the reference (e.g. 40: negative area)
+            status = f"{tag}: {e}"
+        torch.cuda.synchronize()
+        times[tag] = (time.perf_counter() - t0) / steps
+        st = g.download()
+        states[tag] = {f: st[f].copy() for f in fields}
+        states[tag]["topography"] = st["cord"][0, :, 1].copy()
+        states[tag]["iphase"] = st["iphase"].copy()
+        states[tag]["nloop"] = g.clock.nloop
+        states[tag]["eclogite_markers"] = int(np.count_nonzero(st["mark_phase"][:g.clock.nmarkers] == 13))
+        g.close()
+
+    def errs(a, b):
+        e = _field_errors(a, b, fields + ("topography",))
+        e["iphase_differs"] = float(np.mean(a["iphase"] != b["iphase"]))
+        return {k: _r(v) for k, v in e.items()}
+
+    return {"workload": "convergence_600x150 (90,000 elements, eclogite at 600 C / 1.5 GPa, Winkler base)",
+            "steps": steps, "status": status, "ms_per_step_fp64": _r(1e3 * times["fp64"]),
+            "ms_per_step_mixed": _r(1e3 * times["mixed"]),
+            "rel_err_vs_fp64": errs(states["mixed"], states["fp64"]),
+            "fp64_own_change_1e-7": errs(states["fp64_pert"], states["fp64"]),
+            "eclogite_markers": {k: v["eclogite_markers"] for k, v in states.items()},
+            "nloop": {k: v["nloop"] for k, v in states.items()}}
 
 
 def bench_batch(args, workdir: str, local: int):
@@ -524,7 +631,8 @@ def bench_surrogate(args, workdir: str):
            "speedup_vs_plain": t_plain / res["seconds"],
            "gate": {k: v for k, v in cal.items()},
            "rel_err": {k: {"median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)), "max": float(np.max(v))}
-                       for k, v in err.items()}}
+                       for k, v in err.items()},
+           "members_over_2pct": {k: int(np.count_nonzero(err[k] > 0.02)) for k in ("topography", "plastic_strain")}}
     for b in (ba, bb):
         b.close()
     for m, _ in fa + fb:
@@ -640,25 +748,47 @@ def profile_magma(args, workdir: str):
     print(json.dumps(out))
 
 
-def cpu_baseline(inp: str, steps: int = 4, threads: int = 0):
-    """The oracle (OpenMP FP64 restatement of the reference's loops) on the
-    host cores, on a bounded sample of the same workload."""
+def _oracle_rate(inp: str, steps: int, threads: int):
+    """Element-steps/s of the oracle (the FP64 restatement of the reference's
+    loops, OpenMP where the reference has `!$OMP do`) on `threads` host
+    threads over `steps` steps after one untimed step, from its own start-up."""
     from oracle.oracle import Oracle, new_state
 
-    n = threads or os.cpu_count() or 1
     p, c, s = new_state(inp, markers_per_side=MARKERS_PER_SIDE)
-    o = Oracle(p, c, s, threads=n)
+    o = Oracle(p, c, s, threads=threads)
     o.finish_setflac()
     o.step(1)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
-    E = (p.nx - 1) * (p.nz - 1)
-    return {"value": E * steps / dt, "unit": "element-steps/s", "cores": n, "kind": "port",
-            "sample": f"{steps} full FLAC steps of the 1000x300 mesh ({E} elements), {n} OpenMP threads"}
+    return (p.nx - 1) * (p.nz - 1) * steps / dt, dt
+
+
+def cpu_baselines(inp: str, args):
+    """The host baseline on 1 thread and on all cores, on the bench's
+    1000x300 model (bounded samples: `--cpu-steps` steps on all cores,
+    a quarter of that, at least 2, on one thread) and on the 60x20 model of
+    the same physics (its full 2000 steps)."""
+    from geoflac_gb300 import inpgen
+
+    n = os.cpu_count() or 1
+    out = {}
+    small = inpgen.extension_60x20().write(os.path.join(os.path.dirname(inp), "extension_60x20.inp"))
+    for name, path, st_all, st_one in (("extension_1000x300", inp, args.cpu_steps, max(2, args.cpu_steps // 4)),
+                                       ("extension_60x20", small, 2000, 2000)):
+        out[name] = {}
+        for tag, threads, steps in (("1_thread", 1, st_one), ("all_cores", n, st_all)):
+            v, dt = _oracle_rate(path, steps, threads)
+            out[name][tag] = {"value": _r(v), "unit": "element-steps/s", "cores": threads, "kind": "port",
+                              "sample": f"{steps} FLAC steps of {name}, {threads} OpenMP thread(s), {dt:.1f} s"}
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the FP64 restatement of the
+    reference's loops; the Fortran reference cannot be built on these
+    machines) from its own start-up state, on all host cores, with the same
+    config as the GPU arm."""
     ws, rank, local = _dist()
     if rank != 0:
         return
@@ -695,7 +825,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=40, help="host baseline sample on all cores (1000x300 steps)")
+    ap.add_argument("--c3-steps", type=int, default=15000, help="steps of the convergent 600x150 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
     ap.add_argument("--sur-epochs", type=int, default=20, help="surrogate training epochs (0: skip the surrogate)")
