@@ -59,35 +59,18 @@ struct BatchArgs {
     int merge; // every member allows the thermal sweeps beside fl_rheol / fl_node
 };
 
-// Bounded grid barrier (generation counter).  Returns false if any CTA gave
+// Bounded grid barrier (gf_grid_barrier: arrivals, generation counter,
+// error flag -- BatchSync has that layout).  Returns false if any CTA gave
 // up waiting; the kernel then returns at once.
-__device__ bool grid_sync(BatchSync *s) {
-    __shared__ int bad;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *vgen = &s->gen;
-        unsigned g = *vgen;
-        __threadfence();
-        unsigned arrived = atomicAdd(&s->count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&s->count, 0u);
-            __threadfence();
-            atomicAdd(&s->gen, 1u);
-        } else {
-            long long it = 0;
-            while (*vgen == g) {
-                if (++it > (1LL << 24)) {
-                    atomicExch(&s->err, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        bad = *(volatile int *)&s->err;
-    }
-    __syncthreads();
-    return bad == 0;
+__device__ bool grid_sync(BatchSync *s) { return gfk::gf_grid_barrier(reinterpret_cast<unsigned *>(s), 1LL << 24); }
+
+// Check of the bounded barrier: CTA `absent` of a two-CTA co-resident launch
+// never arrives; the other waits at most `limit` polls and leaves with the
+// error flag set (absent = -1: both arrive and pass).
+__global__ void k_barrier_probe(unsigned *bar, int absent, long long limit, int *passed) {
+    if ((int)blockIdx.x == absent) return;
+    bool ok = gfk::gf_grid_barrier(bar, limit);
+    if (threadIdx.x == 0) passed[blockIdx.x] = ok ? 1 : 0;
 }
 
 // All tiles of one item kind, a contiguous run per CTA; the member record is
@@ -983,6 +966,35 @@ int gf_batch_force_residual(gf_batch *b, double *residual) {
     GB_CK(e);
     for (int m = 0; m < n; ++m) residual[m] = h[2 * m] / (h[2 * m + 1] > 0 ? h[2 * m + 1] : 1.0);
     return GF_OK;
+}
+
+int gf_grid_barrier_selftest(int absent_cta, long long limit, int *passed) {
+    if (!passed || absent_cta < -1 || absent_cta > 1 || limit < 1) return GF_ERR_ARG;
+    unsigned *bar = nullptr;
+    int *d_passed = nullptr;
+    GB_CK(cudaMalloc(&bar, 4 * sizeof(unsigned)));
+    cudaError_t e = cudaMalloc(&d_passed, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(bar, 0, 4 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(d_passed, 0xff, 2 * sizeof(int));
+    unsigned err = 0;
+    if (e == cudaSuccess) {
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(2);
+        lc.blockDim = dim3(32);
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        e = cudaLaunchKernelEx(&lc, k_barrier_probe, bar, absent_cta, limit, d_passed);
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(passed, d_passed, 2 * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&err, bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(bar);
+    cudaFree(d_passed);
+    GB_CK(e);
+    return err ? GF_ERR_TIMEOUT : GF_OK;
 }
 
 } // extern "C"

@@ -42,6 +42,7 @@ struct gf_ctx {
     DevArrays A{};
     double *staging = nullptr; // FP64 staging for mixed-mode conversions
     double *d_angle = nullptr;
+    unsigned *therm_bar = nullptr; // grid barrier of the FP64 thermal sweeps
     GfRemeshBufs rb{};         // remesh scratch
     double ar_x = 0, ar_z = 0; // mesh1 zone-pattern totals
     // host mirrors of the host-controlled scalars
@@ -165,6 +166,7 @@ GfLaunch launch_of(gf_ctx *c) {
     g.arc_rate = 1.0 - c->p.ratio_mantle_mzone - c->p.ratio_crust_mzone;
     g.idt_scale = c->p.idt_scale;
     g.advance_time = 0;
+    g.therm_bar = c->therm_bar;
     return g;
 }
 
@@ -691,6 +693,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.t_delta1, N));
     A_(dalloc(c, &A.t_coef, (size_t)18 * E));
     A_(dalloc(c, &A.t_chg, 2 * N));
+    A_(dalloc(c, &c->therm_bar, 4));
     A_(dalloc(c, &A.e_dens, E));
     A_(dalloc(c, &A.e_tri, 4 * E));
     A_(dalloc(c, &A.p_ref, E));

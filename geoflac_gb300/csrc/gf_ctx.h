@@ -123,6 +123,7 @@ struct GfLaunch {
     int idt_scale;   // host copy of the mass-scaling mode (selects launches)
     int advance_time; // fold par.f90's time += dt into the step's last kernel
     double arc_rate;  // arc extrusion rate 1 - ratio_mantle_mzone - ratio_crust_mzone (diff_topo)
+    unsigned *therm_bar; // grid barrier of the FP64 thermal sweeps (arrivals, generation, error flag)
 };
 
 // Launchers, one set per precision (template instantiated in its own TU).

@@ -803,68 +803,6 @@ template <class R> __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(co
     b_k_therm_prep<R>(Pp, C, A, d, tc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// One sweep.  Tup holds the current iterate (Told for sweep 0); self and
-// downstream values always come from Told (A.temp).
-__device__ __forceinline__ void b_k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ tc, const double *__restrict__ Tup, double *__restrict__ Tout, int k) {
-    if (k > 0 && C->therm_flags[k - 1] == 0) return; // converged one sweep ago
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    bool changed = false;
-    // A node's sweep-k value depends on sweep k-1 only through its upstream
-    // neighbours (j-1,i), (j,i-1), (j+1,i-1); if none of them changed in
-    // sweep k-1 its value is the one it had (the same inputs give the same
-    // result), and the FP64 evaluation is skipped.
-    bool recompute = true;
-    if (n < d.N && k > 0) {
-        int j, i;
-        node_ji(d, n, j, i);
-        const uint8_t *prev = A.t_chg + (long long)((k - 1) & 1) * d.N;
-        recompute = (j != 0 && prev[gf_node(d, j - 1, i)]) || (i != 0 && prev[gf_node(d, j, i - 1)]) ||
-                    (i != 0 && j != d.nz - 1 && prev[gf_node(d, j + 1, i - 1)]);
-        if (!recompute) Tout[n] = Tup[n];
-    }
-    if (n < d.N && recompute) {
-        int j, i;
-        node_ji(d, n, j, i);
-        const int nx = d.nx, nz = d.nz;
-        const long long E = d.E;
-        const double *T = A.temp;
-        double rhs = 0.0, area_n = 0.0;
-        auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
-        // triangle t of element e; vs = local index of the updated node; the
-        // three (local vertex, temperature) terms in the reference's order
-        auto tri = [&](long long e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
-            double ra = tc[(12 + t) * E + e];
-            area_n = area_n + ra;
-            const double *K = tc + (long long)t * 6 * E + e;
-            rhs = rhs + tc[(16 + t) * E + e] -
-                  tc[(14 + t) * E + e] * (T0 * K[kidx(v0, vs) * E] + T1 * K[kidx(v1, vs) * E] + T2 * K[kidx(v2, vs) * E]);
-        };
-        double Ts = T[n];
-        if (j != 0 && i != 0) // element (j-1,i-1), triangle B: vertices (j-1,i), (j,i-1), node
-            tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, Tup[Nd(j - 1, i)], 1, Tup[Nd(j, i - 1)], 2, Ts);
-        if (j != 0 && i != nx - 1) { // element (j-1,i), triangles A and B
-            long long e = gf_elem(d, j - 1, i);
-            tri(e, 0, 1, 0, Tup[Nd(j - 1, i)], 1, Ts, 2, T[Nd(j - 1, i + 1)]);
-            tri(e, 1, 1, 0, T[Nd(j - 1, i + 1)], 1, Ts, 2, T[Nd(j, i + 1)]);
-        }
-        if (j != nz - 1 && i != 0) { // element (j,i-1), triangles A and B
-            long long e = gf_elem(d, j, i - 1);
-            tri(e, 0, 2, 0, Tup[Nd(j, i - 1)], 1, Tup[Nd(j + 1, i - 1)], 2, Ts);
-            tri(e, 1, 0, 0, Ts, 1, Tup[Nd(j + 1, i - 1)], 2, T[Nd(j + 1, i)]);
-        }
-        if (j != nz - 1 && i != nx - 1) // element (j,i), triangle A
-            tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
-        double tn = Ts + rhs * C->dt / area_n;
-        Tout[n] = tn;
-        changed = (tn != Tup[n]);
-    }
-    if (n < d.N) A.t_chg[(long long)(k & 1) * d.N + n] = changed ? 1 : 0;
-    if (__any_sync(0xffffffffu, changed) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
-}
-__global__ void __launch_bounds__(GF_THREADS) k_therm_sweep(DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ tc, const double *__restrict__ Tup, double *__restrict__ Tout, int k) {
-    b_k_therm_sweep(C, A, d, tc, Tup, Tout, k);
-}
-
 // Temperature after the boundary conditions of fl_therm.f90:573-598 (top
 // row t_top, bottom row bot_bc or the flux condition, then the side columns
 // copied from their inner neighbours), read from the swept values `src`.
@@ -886,32 +824,142 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
     return src(gf_node(d, j, ii));
 }
 
-// temp0 = temp (fl_therm.f90:46-48); temp = converged iterate with the
-// boundary conditions applied.
-__device__ __forceinline__ void b_k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax, int keep_temp0) {
-    int kc = kmax;
-    for (int k = 0; k < kmax; ++k)
-        if (C->therm_flags[k] == 0) {
+// One node of sweep k.  Tup holds the current iterate (Told for sweep 0);
+// self and downstream values always come from Told (A.temp).  Returns
+// whether the node's value changed.  The iterates and the change flags are
+// written by other CTAs of the same (persistent) launch, so their loads
+// bypass L1 (__ldcg).
+__device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double dt, const double *__restrict__ tc,
+                                                 const double *Tup, double *Tout, int k, long long n) {
+    int j, i;
+    node_ji(d, n, j, i);
+    // A node's sweep-k value depends on sweep k-1 only through its upstream
+    // neighbours (j-1,i), (j,i-1), (j+1,i-1); if none of them changed in
+    // sweep k-1 its value is the one it had (the same inputs give the same
+    // result), and the FP64 evaluation is skipped.
+    if (k > 0) {
+        const uint8_t *prev = A.t_chg + (long long)((k - 1) & 1) * d.N;
+        bool recompute = (j != 0 && __ldcg(prev + gf_node(d, j - 1, i))) ||
+                         (i != 0 && __ldcg(prev + gf_node(d, j, i - 1))) ||
+                         (i != 0 && j != d.nz - 1 && __ldcg(prev + gf_node(d, j + 1, i - 1)));
+        if (!recompute) {
+            Tout[n] = __ldcg(Tup + n);
+            return false;
+        }
+    }
+    const int nx = d.nx, nz = d.nz;
+    const long long E = d.E;
+    const double *T = A.temp;
+    double rhs = 0.0, area_n = 0.0;
+    auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
+    auto U = [&](int jj, int ii) { return __ldcg(Tup + Nd(jj, ii)); };
+    // triangle t of element e; vs = local index of the updated node; the
+    // three (local vertex, temperature) terms in the reference's order
+    auto tri = [&](long long e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
+        double ra = tc[(12 + t) * E + e];
+        area_n = area_n + ra;
+        const double *K = tc + (long long)t * 6 * E + e;
+        rhs = rhs + tc[(16 + t) * E + e] -
+              tc[(14 + t) * E + e] * (T0 * K[kidx(v0, vs) * E] + T1 * K[kidx(v1, vs) * E] + T2 * K[kidx(v2, vs) * E]);
+    };
+    double Ts = T[n];
+    if (j != 0 && i != 0) // element (j-1,i-1), triangle B: vertices (j-1,i), (j,i-1), node
+        tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, U(j - 1, i), 1, U(j, i - 1), 2, Ts);
+    if (j != 0 && i != nx - 1) { // element (j-1,i), triangles A and B
+        long long e = gf_elem(d, j - 1, i);
+        tri(e, 0, 1, 0, U(j - 1, i), 1, Ts, 2, T[Nd(j - 1, i + 1)]);
+        tri(e, 1, 1, 0, T[Nd(j - 1, i + 1)], 1, Ts, 2, T[Nd(j, i + 1)]);
+    }
+    if (j != nz - 1 && i != 0) { // element (j,i-1), triangles A and B
+        long long e = gf_elem(d, j, i - 1);
+        tri(e, 0, 2, 0, U(j, i - 1), 1, U(j + 1, i - 1), 2, Ts);
+        tri(e, 1, 0, 0, Ts, 1, U(j + 1, i - 1), 2, T[Nd(j + 1, i)]);
+    }
+    if (j != nz - 1 && i != nx - 1) // element (j,i), triangle A
+        tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
+    double tn = Ts + rhs * dt / area_n;
+    Tout[n] = tn;
+    return tn != __ldcg(Tup + n);
+}
+
+// Bounded grid barrier of a co-resident (cooperative) launch: generation
+// counter in bar[1], arrivals in bar[0], error flag in bar[2].  A CTA that
+// waits longer than `limit` polls sets the flag; every CTA returns false
+// once the flag is set.
+__device__ bool gf_grid_barrier(unsigned *bar, long long limit) {
+    __shared__ int bad;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        unsigned g0 = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == g0) {
+                if (++it > limit) {
+                    atomicExch(bar + 2, 1u);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        bad = *(volatile unsigned *)(bar + 2) != 0u;
+    }
+    __syncthreads();
+    return !bad;
+}
+
+// The FP64 thermal update after k_therm_prep, in one co-resident launch:
+// sweeps until one changes nothing (at most kmax; grid barrier between
+// sweeps, every CTA reads the same flag after it), then the boundary
+// conditions and temp0 = temp (fl_therm.f90:46-48, 573-598) from the last
+// sweep's buffer.  Node n is always handled by the same thread.
+__global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
+                                                            DevArrays A, GfDims d, const double *__restrict__ tc,
+                                                            double *b0, double *b1, int kmax, int keep_temp0,
+                                                            unsigned *bar) {
+    const long long stride = (long long)gridDim.x * blockDim.x; // a multiple of 32
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long npad = (d.N + 31) / 32 * 32; // equal trip counts within a warp (the vote)
+    const double dt = C->dt;
+    int kc = kmax; // the first sweep that changed nothing
+    for (int k = 0; k < kmax; ++k) {
+        const double *up = k == 0 ? A.temp : ((k - 1) & 1 ? b1 : b0);
+        double *out = (k & 1) ? b1 : b0;
+        bool any = false;
+        for (long long n = gt; n < npad; n += stride) {
+            bool changed = n < d.N && therm_sweep_node(A, d, dt, tc, up, out, k, n);
+            if (n < d.N) A.t_chg[(long long)(k & 1) * d.N + n] = changed ? 1 : 0;
+            any = any || changed;
+        }
+        if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
+        if (!gf_grid_barrier(bar, 1LL << 24)) {
+            if (gt == 0) set_status(C, GF_ERR_TIMEOUT, k);
+            return;
+        }
+        if (*(volatile int *)&C->therm_flags[k] == 0) {
             kc = k;
             break;
         }
-    long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n == 0) {
+    }
+    if (gt == 0) {
         C->therm_sweeps_used = kc + 1;
         if (kc == kmax) C->therm_unconverged += 1;
     }
-    if (n >= d.N) return;
-    // sweep kc (or the last one) wrote buffer kc & 1
-    int k = kc < kmax ? kc : kmax - 1;
-    const double *src = (k & 1) ? b1 : b0;
-    int j, i;
-    node_ji(d, n, j, i);
-    double t = therm_bc_value(*Pp, A, d, [src](long long m) { return src[m]; }, j, i);
-    if (!keep_temp0) A.temp0[n] = A.temp[n];
-    A.temp[n] = t;
-}
-__global__ void __launch_bounds__(GF_THREADS) k_therm_apply(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const double *__restrict__ b0, const double *__restrict__ b1, int kmax, int keep_temp0) {
-    b_k_therm_apply(Pp, C, A, d, b0, b1, kmax, keep_temp0);
+    const double *src = ((kc < kmax ? kc : kmax - 1) & 1) ? b1 : b0;
+    for (long long n = gt; n < d.N; n += stride) {
+        int j, i;
+        node_ji(d, n, j, i);
+        double t = therm_bc_value(*Pp, A, d, [src](long long m) { return __ldcg(src + m); }, j, i);
+        if (!keep_temp0) A.temp0[n] = A.temp[n];
+        A.temp[n] = t;
+    }
 }
 
 // ---- mixed precision: FP32 coefficients, two sweeps.
@@ -1666,12 +1714,34 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int k
     }
     int kmax = sweeps > 0 ? (sweeps < GF_THERM_KMAX ? sweeps : GF_THERM_KMAX) : GF_THERM_KMAX;
     GF_LAUNCH(k_therm_prep<R>, g.d.E, g.P, g.C, g.A, g.d, g.A.t_coef);
-    double *bufs[2] = {g.A.t_delta0, g.A.t_delta1};
-    for (int k = 0; k < kmax; ++k) {
-        const double *up = k == 0 ? g.A.temp : bufs[(k - 1) & 1];
-        GF_LAUNCH(k_therm_sweep, g.d.N, g.C, g.A, g.d, g.A.t_coef, up, bufs[k & 1], k);
+    // the sweeps and the boundary pass: one co-resident launch
+    static int occ[64] = {0}, sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    dev = dev & 63;
+    if (occ[dev] == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[dev], k_therm_sweeps, GF_THREADS, 0);
+        cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+        if (occ[dev] <= 0) occ[dev] = 1;
     }
-    GF_LAUNCH(k_therm_apply, g.d.N, g.P, g.C, g.A, g.d, bufs[0], bufs[1], kmax, keep_temp0);
+    const long long need = (g.d.N + GF_THREADS - 1) / GF_THREADS;
+    const long long cap = (long long)occ[dev] * sms[dev];
+    // arrivals and the error flag start at zero in every launch (the
+    // generation counter only has to change)
+    cudaMemsetAsync(g.therm_bar, 0, sizeof(unsigned), g.s);
+    cudaMemsetAsync(g.therm_bar + 2, 0, sizeof(unsigned), g.s);
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)(need < cap ? need : cap));
+    lc.blockDim = dim3(GF_THREADS);
+    lc.stream = g.s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, k_therm_sweeps, g.P, g.C, g.A, g.d, (const double *)g.A.t_coef, g.A.t_delta0,
+                       g.A.t_delta1, kmax, keep_temp0, g.therm_bar);
+    ++*g.launches;
 }
 
 template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, int avg_mode) {

@@ -416,6 +416,15 @@ int gf_batch_backup(gf_batch *b);
 int gf_batch_restore(gf_batch *b, const int *members, int count);
 long long gf_batch_elements(gf_batch *b);
 int gf_batch_grid(gf_batch *b);
+/* Check of the bounded grid barrier that separates the phases of the
+ * persistent kernels (the ensemble step, the FP64 thermal sweeps): a
+ * two-CTA co-resident launch in which CTA `absent_cta` (0 or 1) never
+ * arrives, so the other gives up after `limit` polls (about 64 ns each) and
+ * the call returns GF_ERR_TIMEOUT with the device still usable; absent_cta
+ * = -1 lets both arrive (GF_OK).  passed[k] = 1 if CTA k left the barrier
+ * normally, 0 if it gave up, -1 if it never reached it.  No reference
+ * counterpart. */
+int gf_grid_barrier_selftest(int absent_cta, long long limit, int *passed);
 
 /* sizeof(gf_params), sizeof(gf_clock), sizeof(gf_layout) for which = 0, 1, 2:
  * lets a binding (ctypes, cgo, ISO_C_BINDING) check its struct mirrors.
