@@ -825,7 +825,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=40, help="host baseline sample on all cores (1000x300 steps)")
+    ap.add_argument("--cpu-steps", type=int, default=400, help="host baseline sample on all cores (1000x300 steps)")
     ap.add_argument("--c3-steps", type=int, default=15000, help="steps of the convergent 600x150 leg (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=256, help="ensemble size of the batched leg (0: skip)")
