@@ -138,6 +138,7 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.f_vactiv[k] = (float)p.vactiv[k];
     }
     P.f_ten_off = (float)p.ten_off;
+    P.f_tau_heal = (float)p.tau_heal;
     P.f_demf = (float)p.demf;
     for (int k = 0; k < GF_MAXPH; ++k) {
         P.f_alfa[k] = (float)p.alfa[k];

@@ -8,6 +8,7 @@
 #include "gf_index.h"
 
 #define GF_THREADS 256
+#define GF_THREADS_MAX 512 // the largest CTA of any kernel (the ensemble step's)
 #define GF_THERM_KMAX 24 // cap on the thermal fixed-point sweeps per fl_therm
 
 // Read-only model constants the kernels use (copied once per context into
@@ -32,7 +33,7 @@ struct DevParams {
         f_coh2[GF_MAXPH], f_dil1[GF_MAXPH], f_dil2[GF_MAXPH], f_pl1[GF_MAXPH], f_pl2[GF_MAXPH], f_cp[GF_MAXPH],
         f_cond[GF_MAXPH], f_den[GF_MAXPH], f_pln[GF_MAXPH], f_lacoef[GF_MAXPH], f_eactiv[GF_MAXPH],
         f_vactiv[GF_MAXPH];
-    float f_ten_off, f_demf, f_g;
+    float f_ten_off, f_demf, f_g, f_tau_heal;
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
     double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:108)
     double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)

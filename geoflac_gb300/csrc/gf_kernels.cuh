@@ -80,6 +80,46 @@ __device__ __forceinline__ void load_quad(const double *__restrict__ cord, const
     q.y[3] = cord[d.N + n3 + 1];
 }
 
+// Conversions between FP64 and FP32 on the integer pipe (mixed path).  On
+// GB300 the FP64 pipe runs at 1/64 of the FP32 rate and the conversion
+// instructions between the two formats issue to it; a mixed kernel that
+// converts a few values per item is bound by that pipe.  These give the
+// conversion instructions' results with integer operations:
+//   gf_d2f: round to nearest even for finite values whose float is normal
+//           (smaller magnitudes give a signed zero, larger an infinity);
+//   gf_f2d: exact (float subnormals give a signed zero).
+__device__ __forceinline__ float gf_d2f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127; // float exponent
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    // mantissa bits 51..29 kept (20 from hi, 3 from lo), 28..0 dropped
+    unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu, half = 0x10000000u;
+    m += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(sign + ((unsigned)e << 23) + m); // a carry out of m raises the exponent
+}
+__device__ __forceinline__ double gf_f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    if (e == 0u) return __longlong_as_double((long long)((unsigned long long)sign << 32));
+    const unsigned ed = (e == 255u) ? 0x7ffu : e - 127u + 1023u;
+    const unsigned hi = sign | (ed << 20) | (m >> 3);
+    return __longlong_as_double((long long)(((unsigned long long)hi << 32) | ((unsigned long long)(m & 7u) << 29)));
+}
+// x = hi + lo with hi = float(x): the hi/lo split of the mixed path
+__device__ __forceinline__ void gf_split(double x, float &h, float &l) {
+    h = gf_d2f(x);
+    l = gf_d2f(x - gf_f2d(h));
+}
+// an FP64 input in the kernel's precision R (FP64 kernels keep it as it is)
+template <class R> __device__ __forceinline__ R gf_to(double x) {
+    if constexpr (sizeof(R) == sizeof(float)) return gf_d2f(x);
+    else return x;
+}
+
 // Mixed path: coordinates of a quad relative to its node 1, in FP32 from the
 // hi/lo splits (the hi difference of neighbouring nodes is exact, the lo
 // parts carry the rest), and velocities relative to node 1 the same way.
@@ -605,7 +645,7 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
         R ratio, f, c, dd, h, pl1, pl2, f1, f2, c1, c2, d1, d2;
         if constexpr (sizeof(R) == sizeof(float)) {
             // phase ratios are k/n with n <= 32 markers: 0.01 separates 0 from the rest in FP32 too
-            ratio = (float)A.phase_ratio[gf_pr(d, e, k)];
+            ratio = gf_d2f(A.phase_ratio[gf_pr(d, e, k)]);
             if (ratio < 0.01f) continue;
             pl1 = P.f_pl1[k]; pl2 = P.f_pl2[k];
             f1 = P.f_fric1[k]; f2 = P.f_fric2[k]; c1 = P.f_coh1[k]; c2 = P.f_coh2[k]; d1 = P.f_dil1[k]; d2 = P.f_dil2[k];

@@ -72,7 +72,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     elem_ji(d, e, j, i);
     const double dtd = C->dt;
     if (e == 0) C->dtavg = C->dtavg + dtd; // fl_rheol.f90:43 (no thread reads dtavg here)
-    const R dt = R(dtd);
+    const R dt = gf_to<R>(dtd);
     R *st = (R *)A.stress0;
     const R *area = (const R *)A.area;
 
@@ -173,7 +173,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     PlasticConsts<R> pc;
     if (irh == 6 || irh >= 11)
         pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi, sizeof(R) == sizeof(float) ? R(P.f_ten_off) : R(P.ten_off));
-    R dike = A.dike_released ? R(A.dike_released[e]) : R(0);
+    R dike = A.dike_released ? gf_to<R>(A.dike_released[e]) : R(0);
     const R *dvol = (const R *)A.dvol;
     R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
     bool ok = true, plas_mod = false;
@@ -269,7 +269,11 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         R quad_area = ar[0] + ar[1] + ar[2] + ar[3];
         aps_e = aps_e + (depl[0] * ar[0] + depl[1] * ar[1] + depl[2] * ar[2] + depl[3] * ar[3]) / quad_area;
         if (aps_e < R(0.0)) aps_e = R(0.0);
-        if (P.tau_heal != 0.0) aps_e = aps_e / (R(1.0) + dt / R(P.tau_heal));
+        if constexpr (sizeof(R) == sizeof(float)) {
+            if (P.f_tau_heal != 0.0f) aps_e = aps_e / (1.0f + dt / P.f_tau_heal);
+        } else {
+            if (P.tau_heal != 0.0) aps_e = aps_e / (R(1.0) + dt / R(P.tau_heal));
+        }
         aps[e] = aps_e;
     }
     // accumulates the element-averaged start-of-step stress (s11/s22/s12 are
@@ -431,31 +435,29 @@ __device__ __forceinline__ void node_interior_f(const DevParams &P, const DevClo
         fy0 += frc[(4 * c + 1) * E + e] - (rxz * gx + rzz * gz);
     }
     float f0 = fx0;
-    float f1 = fy0 - (float)(A.rmass[n] * P.g);
-    const float dtf = (float)C->dt;
-    float drat = dtf / (float)C->dt_elastic;
+    float f1 = fy0 - gf_d2f(A.rmass[n]) * P.f_g;
+    const float dtf = gf_d2f(C->dt);
+    float drat = dtf / gf_d2f(C->dt_elastic);
     if (drat < 1.0f) drat = 1.0f;
     float h0 = A.vel_hi[n], l0 = A.vel_lo[n], h1 = A.vel_hi[d.N + n], l1 = A.vel_lo[d.N + n];
     const int c0 = A.ncod[n], c1 = A.ncod[d.N + n];
     if ((c0 & 1) != 1 && fabsf(h0) > 1.0e-13f) f0 = f0 - P.f_demf * copysignf(fabsf(f0), h0);
     if ((c1 & 2) != 2 && fabsf(h1) > 1.0e-13f) f1 = f1 - P.f_demf * copysignf(fabsf(f1), h1);
-    const float s = dtf / ((float)A.amass[n] * drat * drat);
+    const float s = dtf / (gf_d2f(A.amass[n]) * drat * drat);
     double v0, v1;
     if (c0 == 1) {
         v0 = A.bc[n];
-        h0 = (float)v0;
-        l0 = (float)(v0 - (double)h0);
+        gf_split(v0, h0, l0);
     } else {
         ff_add(h0, l0, s * f0);
-        v0 = (double)h0 + (double)l0;
+        v0 = gf_f2d(h0) + gf_f2d(l0);
     }
     if (c1 == 1) {
         v1 = A.bc[d.N + n];
-        h1 = (float)v1;
-        l1 = (float)(v1 - (double)h1);
+        gf_split(v1, h1, l1);
     } else {
         ff_add(h1, l1, s * f1);
-        v1 = (double)h1 + (double)l1;
+        v1 = gf_f2d(h1) + gf_f2d(l1);
     }
     A.vel[n] = v0;
     A.vel[d.N + n] = v1;
@@ -604,9 +606,9 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     double am = A.amass[n];
     if (sizeof(R) == sizeof(float)) {
         // FP32 increment on the FP64 velocity
-        float s = float(dt) / (float(am) * float(drat) * float(drat));
-        v0 = (c0 == 1) ? A.bc[n] : v0 + (double)(s * float(f0));
-        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + (double)(s * float(f1));
+        float s = gf_d2f(dt) / (gf_d2f(am) * gf_d2f(drat) * gf_d2f(drat));
+        v0 = (c0 == 1) ? A.bc[n] : v0 + gf_f2d(s * gf_d2f(f0));
+        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_f2d(s * gf_d2f(f1));
     } else {
         v0 = (c0 == 1) ? A.bc[n] : v0 + dt * f0 / (am * drat * drat);
         v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + dt * f1 / (am * drat * drat);
@@ -620,11 +622,13 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     vel[n] = v0;
     vel[d.N + n] = v1;
     if (sizeof(R) == sizeof(float)) {
-        float h0 = (float)v0, h1 = (float)v1;
+        float h0, l0, h1, l1;
+        gf_split(v0, h0, l0);
+        gf_split(v1, h1, l1);
         A.vel_hi[n] = h0;
-        A.vel_lo[n] = (float)(v0 - (double)h0);
+        A.vel_lo[n] = l0;
         A.vel_hi[d.N + n] = h1;
-        A.vel_lo[d.N + n] = (float)(v1 - (double)h1);
+        A.vel_lo[d.N + n] = l1;
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
@@ -638,9 +642,10 @@ __device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArray
     const double c = A.cord[n] + A.vel[n] * C->dt;
     A.cord[n] = c;
     if (A.cord_hi) {
-        const float h = (float)c;
+        float h, l;
+        gf_split(c, h, l);
         A.cord_hi[n] = h;
-        A.cord_lo[n] = (float)(c - (double)h);
+        A.cord_lo[n] = l;
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
@@ -678,8 +683,8 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
     // the surface nodes also moved by diff_topo's dtopo (zero without it)
     float tz[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (fp32 && j == 0) {
-        tz[0] = (float)A.dtopo[i];
-        tz[2] = (float)A.dtopo[i + 1];
+        tz[0] = gf_d2f(A.dtopo[i]);
+        tz[2] = gf_d2f(A.dtopo[i + 1]);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -704,7 +709,7 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
             // as (det_new - det_old)*area_old with the change of det expanded
             // in this step's displacements u = vel*dt, which FP32 resolves.
             const float *x = qf.x, *y = qf.y;
-            const float dtf = (float)dtd;
+            const float dtf = gf_d2f(dtd);
             float Bx = x[b] - x[a], By = y[b] - y[a];
             float Cx = x[c] - x[a], Cy = y[c] - y[a];
             float dBx = (rvx[b] - rvx[a]) * dtf, dBy = (rvy[b] - rvy[a]) * dtf + (tz[b] - tz[a]);
@@ -977,7 +982,7 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     float cp_eff = P.f_cp[iph], cond_eff = P.f_cond[iph], den = P.f_den[iph];
     float dissip = (P.ishearh == 1 && P.itherm != 2) ? ((const float *)A.shrheat)[e] : 0.0f;
     float diff = cond_eff / den / cp_eff;
-    float src = ((float)A.source[e] + dissip / den) / cp_eff;
+    float src = (gf_d2f(A.source[e]) + dissip / den) / cp_eff;
     QuadF q;
     load_quad_rel(A, d, j, i, q);
     const float *area = (const float *)A.area;
@@ -1044,11 +1049,11 @@ __device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ 
     }
     if (j != nz - 1 && i != nx - 1)
         tri(gf_elem(d, j, i), 0, 0, 0, 0.0f, 1, dT(Nd(j + 1, i), false), 2, dT(Nd(j, i + 1), false));
-    float inc = rhs * float(C->dt) / area_n;
+    float inc = rhs * gf_d2f(C->dt) / area_n;
     if (!final_sweep)
         d0[n] = inc;
     else
-        tnew[n] = A.temp[n] + (double)inc;
+        tnew[n] = A.temp[n] + gf_f2d(inc);
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep) {
     b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -1063,9 +1068,10 @@ __device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ 
     const double t = therm_bc_value(*Pp, A, d, [tnew](long long m) { return tnew[m]; }, j, i);
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
-    const float h = (float)t;
+    float h, l;
+    gf_split(t, h, l);
     A.temp_hi[n] = h;
-    A.temp_lo[n] = (float)(t - (double)h);
+    A.temp_lo[n] = l;
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew) {
     b_k_therm_apply32(Pp, A, d, tnew, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -1084,7 +1090,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams
         // mixed: FP32 density and FP32 triangle shares
         float fval = 0.0f;
         const float dens = eff_dens_f32(*Pp, A, d, j, i, e, &wrote, &fval);
-        A.e_dens[e] = (double)dens;
+        A.e_dens[e] = gf_f2d(dens);
         float *tri = (float *)A.e_tri;
 #pragma unroll
         for (int k = 0; k < 4; ++k) tri[k * d.E + e] = (1.0f / 12.0f) / area[gf_ek(d, e, k)] * dens;
@@ -1174,7 +1180,8 @@ __device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, d
 #pragma unroll
             for (int t = 0; t < 3; ++t) acc = acc + tri[c_vtx_tris[lv[q]][t] * d.E + e];
         }
-    out[n] = (double)acc;
+    if constexpr (sizeof(T) == sizeof(float)) out[n] = gf_f2d(acc);
+    else out[n] = acc;
 }
 template <class T>
 __global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d) {
@@ -1183,6 +1190,47 @@ __global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const T *__restr
 
 // ======================================================================
 // dt_mass (dt_mass.f90:16-232)
+// The CTA's minimum edge measure, maximum |velocity|, maximum diffusivity
+// and phase mask (each warp's already reduced in its lane 0) combined in
+// shared memory, then one atomic per quantity and CTA (per-warp atomics on
+// the same four words serialise).  min / max are exact in any order.  Every
+// thread of the CTA calls it; `diffu` (mixed path) turns the phase mask into
+// the maximum diffusivity, otherwise dmax is used.
+__device__ __forceinline__ void dt_block_commit(DevClock *__restrict__ C, double dl, double vmax, double dmax,
+                                                unsigned pm, const double *diffu, int nphase) {
+    __shared__ unsigned long long s_dl[GF_THREADS_MAX / 32], s_v[GF_THREADS_MAX / 32], s_d[GF_THREADS_MAX / 32];
+    __shared__ unsigned s_pm[GF_THREADS_MAX / 32];
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_dl[w] = (unsigned long long)__double_as_longlong(dl);
+        s_v[w] = (unsigned long long)__double_as_longlong(vmax);
+        s_d[w] = (unsigned long long)__double_as_longlong(dmax);
+        s_pm[w] = pm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = s_dl[0], b = s_v[0], c = s_d[0];
+        unsigned m = s_pm[0];
+        for (int k = 1; k < nw; ++k) {
+            a = min(a, s_dl[k]);
+            b = max(b, s_v[k]);
+            c = max(c, s_d[k]);
+            m |= s_pm[k];
+        }
+        if (diffu) { // the largest diffusivity of the phases present (dt_mass.f90:108)
+            double dm = 0.0;
+            for (int k = 0; k < nphase; ++k)
+                if (m & (1u << k)) dm = fmax(dm, diffu[k]);
+            c = (unsigned long long)__double_as_longlong(dm);
+        }
+        atomicMin(&C->r_dlmin, a);
+        atomicMax(&C->r_velmax, b);
+        atomicMax(&C->r_diffmax, c);
+        atomicOr(&C->phase_mask, m);
+    }
+    __syncthreads(); // the shared slots are free for the CTA's next item
+}
+
 template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long t) {
     const DevParams &P = *Pp;
     double dl = 1e300, vmax = 0.0, dmax = 0.0;
@@ -1219,15 +1267,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
         df = warp_min(df);
         vf = warp_max(vf);
         for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
-        if ((threadIdx.x & 31) == 0) {
-            atomic_min_pos(&C->r_dlmin, df < 1e30f ? (double)df : 1e300);
-            atomic_max_pos(&C->r_velmax, (double)vf);
-            // the largest diffusivity of the phases present (dt_mass.f90:108)
-            for (int k = 0; k < P.nphase; ++k)
-                if (pm & (1u << k)) dmax = fmax(dmax, P.diffu[k]);
-            atomic_max_pos(&C->r_diffmax, dmax);
-            atomicOr(&C->phase_mask, pm);
-        }
+        dt_block_commit(C, df < 1e30f ? gf_f2d(df) : 1e300, gf_f2d(vf), 0.0, pm, P.diffu, P.nphase);
         return;
     } else {
         if (t < d.E) {
@@ -1259,12 +1299,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
         vmax = warp_max(vmax);
         dmax = warp_max(dmax);
         for (int o = 16; o > 0; o >>= 1) pm |= __shfl_xor_sync(0xffffffffu, pm, o);
-        if ((threadIdx.x & 31) == 0) {
-            atomic_min_pos(&C->r_dlmin, dl);
-            atomic_max_pos(&C->r_velmax, vmax);
-            atomic_max_pos(&C->r_diffmax, dmax);
-            atomicOr(&C->phase_mask, pm);
-        }
+        dt_block_commit(C, dl, vmax, dmax, pm, nullptr, 0);
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
@@ -1335,7 +1370,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
         if (rho_inert > rho_inert2) rho_inert = rho_inert2;
     }
     if constexpr (sizeof(R) == sizeof(float)) {
-        const float r = (float)(c1d12 * rho_inert);
+        const float r = gf_d2f(c1d12 * rho_inert);
         float *tri = (float *)A.e_tri;
 #pragma unroll
         for (int k = 0; k < 4; ++k) tri[k * d.E + e] = r / area[gf_ek(d, e, k)];
@@ -1492,7 +1527,7 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     int k = (n - 1) % 2 + 1;
     int j = ((n - k) / 2) % (nz - 1);
     int i = (n - k) / 2 / (nz - 1);
-    const float a1 = (float)A.mark_a1[kk], a2 = (float)A.mark_a2[kk], a3 = 1.0f - a1 - a2;
+    const float a1 = gf_d2f(A.mark_a1[kk]), a2 = gf_d2f(A.mark_a2[kk]), a3 = 1.0f - a1 - a2;
     long long p1, p2, p3;
     if (k == 1) {
         p1 = gf_node(d, j, i); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j, i + 1);
