@@ -632,7 +632,14 @@ def bench_surrogate(args, workdir: str):
            "gate": {k: v for k, v in cal.items()},
            "rel_err": {k: {"median": float(np.median(v)), "p90": float(np.quantile(v, 0.9)), "max": float(np.max(v))}
                        for k, v in err.items()},
-           "members_over_2pct": {k: int(np.count_nonzero(err[k] > 0.02)) for k in ("topography", "plastic_strain")}}
+           "members_over_2pct": {k: int(np.count_nonzero(err[k] > 0.02)) for k in ("topography", "plastic_strain")},
+           # per member: the 4 sweep parameters, elements, gate residual,
+           # rerun, relative L2 error of topography and plastic strain
+           "per_member": [[round(float(v), 4) for v in (pp["friction"], pp["crust_km"], pp["moho_t"], pp["v_cm_yr"])] +
+                          [int((fb[k][0].params.nx - 1) * (fb[k][0].params.nz - 1)),
+                           float(res["residual"][k]), int(k in res["rerun"]),
+                           float(err["topography"][k]), float(err["plastic_strain"][k])]
+                          for k, pp in enumerate(p for _, p in fb)]}
     for b in (ba, bb):
         b.close()
     for m, _ in fa + fb:

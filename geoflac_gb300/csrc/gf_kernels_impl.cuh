@@ -1359,6 +1359,24 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     const R *area = (const R *)A.area;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        // mixed: the inertial density in FP32 (pwave / vel_sound^2 ~ 1e21,
+        // well inside the FP32 range), from FP32 copies of the inputs
+        const int iph = A.iphase[e] - 1;
+        const float pwave = gf_d2f(P.rl[iph]) + 0.6666f * P.f_rm[iph];
+        const float vel_sound = gf_d2f(C->dlmin) * gf_d2f(C->frac) / gf_d2f(C->dt_elastic);
+        float rho_inert = pwave / (vel_sound * vel_sound);
+        const float vel_max = gf_d2f(C->vel_max);
+        if (P.i_rey == 1 && vel_max > 0.0f) {
+            const float rho_inert2 = (gf_d2f(P.xReyn) * gf_d2f(P.v_min)) / (vel_max * fabsf(gf_d2f(P.rzbo)));
+            if (rho_inert > rho_inert2) rho_inert = rho_inert2;
+        }
+        const float r = rho_inert / 12.0f;
+        float *tri = (float *)A.e_tri;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) tri[k * d.E + e] = r / area[gf_ek(d, e, k)];
+        return;
+    }
     const double c1d12 = 1.0 / 12.0;
     double dlmin = C->dlmin, frac = C->frac, dt_elastic = C->dt_elastic, vel_max = C->vel_max;
     int iph = A.iphase[e] - 1;
@@ -1369,15 +1387,8 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
         double rho_inert2 = (P.xReyn * P.v_min) / (vel_max * fabs(P.rzbo));
         if (rho_inert > rho_inert2) rho_inert = rho_inert2;
     }
-    if constexpr (sizeof(R) == sizeof(float)) {
-        const float r = gf_d2f(c1d12 * rho_inert);
-        float *tri = (float *)A.e_tri;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) tri[k * d.E + e] = r / area[gf_ek(d, e, k)];
-    } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
-    }
+    for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
     b_k_elem_am3<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
