@@ -396,8 +396,9 @@ class Fno:
         return self.g
 
     def loss_grad(self, out, target, weight=None):
-        """mean-squared error (optionally weighted per pixel and channel of one
-        sample, weight [H, W, cout]) and its BF16 gradient w.r.t. the output"""
+        """mean-squared error, optionally weighted per pixel and channel (weight
+        [H, W, cout], the same for every sample, or [batch, H, W, cout]), and
+        its BF16 gradient w.r.t. the output"""
         torch = self.torch
         loss = torch.zeros(1, dtype=torch.float64, device="cuda")
         dout = torch.empty(out.shape, dtype=torch.bfloat16, device="cuda")
