@@ -52,7 +52,7 @@ struct gf_ctx {
     std::vector<void *> allocs;
     int sweeps = 0; // cap on the thermal sweeps (0: library cap)
     int sync = 1;
-    int frc_valid = 0; // mixed: e_frc holds the corner forces of the current stresses and mesh
+    int frc_valid = 0; // e_frc (mixed) / n_frc (FP64) hold the node-force terms of the current stresses and mesh
 };
 
 namespace {
@@ -168,6 +168,7 @@ GfLaunch launch_of(gf_ctx *c) {
     g.idt_scale = c->p.idt_scale;
     g.advance_time = 0;
     g.therm_bar = c->therm_bar;
+    g.node_terms = 0;
     return g;
 }
 
@@ -356,6 +357,7 @@ void k_node(gf_ctx *c) {
         c->frc_valid = 1;
         GfKernels<float>::node(g);
     } else {
+        g.node_terms = c->frc_valid && c->A.n_frc;
         GfKernels<double>::node(g);
     }
 }
@@ -743,6 +745,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &b.d_scalars, 4));
         A_(mesh_templates(c));
     }
+    if (mode == GF_MODE_FP64) A_(dalloc(c, &A.n_frc, 24 * E));
     if (mode == GF_MODE_MIXED) {
         A_(dalloc(c, &c->staging, 16 * E));
         A_(dalloc(c, &A.cord_hi, 2 * N));

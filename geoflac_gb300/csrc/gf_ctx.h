@@ -99,6 +99,10 @@ struct DevArrays {
     // corner c (0..3) the force of the element's stresses less its own
     // triangle-1 stress (x, z) and the geometric sums G (x, z)
     float *e_frc;
+    // FP64: each element's terms of fl_node's force sum (fl_node.f90:14-48),
+    // written by fl_rheol from the new stresses: for corner c and the k-th
+    // of its three triangles, fx at [(6c + 2k) E + e], fy at [(6c + 2k + 1) E + e]
+    double *n_frc;
     int *nmarkers;                                    // device marker count
     // magma sub-model (allocated when itype_melting = 1): melt fractions,
     // dike / MOR accumulators (E each), the last arc extrusion (nx), and
@@ -125,6 +129,7 @@ struct GfLaunch {
     int advance_time; // fold par.f90's time += dt into the step's last kernel
     double arc_rate;  // arc extrusion rate 1 - ratio_mantle_mzone - ratio_crust_mzone (diff_topo)
     unsigned *therm_bar; // grid barrier of the FP64 thermal sweeps (arrivals, generation, error flag)
+    int node_terms;      // FP64 fl_node: A.n_frc holds the terms of the current stresses and mesh
 };
 
 // Launchers, one set per precision (template instantiated in its own TU).

@@ -255,6 +255,31 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = sn[c][k];
+    if constexpr (sizeof(R) == sizeof(double)) {
+        // fl_node's force terms of this element (fl_node.f90:14-48), each
+        // the expression the node gather evaluates, from the stresses just
+        // stored: the node kernel then sums them in the reference's order
+        // instead of recomputing four elements' shape derivatives and twelve
+        // divisions per node (the mesh does not move before fl_node)
+        if (A.n_frc) {
+            const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
+            const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
+            double *nf = A.n_frc;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int qd = 3 - c;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int t = kk[qd][k], m = mm[qd][k];
+                    R factor = R(0.25) / ar[t];
+                    R fx = factor * (sn[0][t] * dx[m][t] + sn[2][t] * dz[m][t]);
+                    R fy = factor * (sn[2][t] * dx[m][t] + sn[1][t] * dz[m][t]);
+                    nf[(long long)(6 * c + 2 * k) * d.E + e] = fx;
+                    nf[(long long)(6 * c + 2 * k + 1) * d.E + e] = fy;
+                }
+            }
+        }
+    }
     if constexpr (sizeof(R) == sizeof(float)) {
         // the node gather's corner forces of the new stresses (the mesh does
         // not move before fl_node); shape derivatives taken again rather than
@@ -467,7 +492,7 @@ __device__ __forceinline__ void node_interior_f(const DevParams &P, const DevClo
     A.vel_lo[d.N + n] = l1;
 }
 
-template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long slot) {
+template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long slot, int terms = 0) {
     if (slot >= d.N) return;
     const long long n = node_of_slot(d, slot);
     const DevParams &P = *Pp;
@@ -524,6 +549,23 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         }
         f0 = gx;
         f1 = gy - A.rmass[n] * P.g;
+    } else if (terms) {
+        // FP64 path, terms written by fl_rheol: the reference's sum order
+        R fx0 = R(0.0), fy0 = R(0.0);
+#pragma unroll
+        for (int qd = 0; qd < 4; ++qd) {
+            int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
+            if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
+            const long long e = gf_elem(d, je, ie);
+            const int c = 3 - qd;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                fx0 = fx0 - A.n_frc[(long long)(6 * c + 2 * k) * d.E + e];
+                fy0 = fy0 - A.n_frc[(long long)(6 * c + 2 * k + 1) * d.E + e];
+            }
+        }
+        f0 = (double)fx0;
+        f1 = (double)fy0 - A.rmass[n] * P.g;
     } else {
         // FP64 path: the reference's gather from the four quads
         R fx0 = R(0.0), fy0 = R(0.0);
@@ -631,8 +673,8 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         A.vel_lo[d.N + n] = l1;
     }
 }
-template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    b_k_node<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int terms) {
+    b_k_node<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x, terms);
 }
 
 // ======================================================================
@@ -778,7 +820,9 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     int iph = A.iphase[e] - 1;
     double cp_eff = P.cp[iph], cond_eff = P.conduct[iph];
     double dissip = (P.ishearh == 1 && P.itherm != 2) ? (double)((const R *)A.shrheat)[e] : 0.0;
-    double diff = cond_eff / P.den[iph] / cp_eff;
+    // conduct / den / cp of the phase: the same two IEEE divisions as the
+    // reference's cond_eff / dens / cp_eff, taken once per phase at set-up
+    double diff = P.diffu[iph];
     double src = (A.source[e] + dissip / P.den[iph]) / cp_eff;
     Quad q;
     load_quad(A.cord, d, j, i, q);
@@ -1427,6 +1471,24 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     int k = (n - 1) % 2 + 1;
     int j = ((n - k) / 2) % (nz - 1);
     int i = (n - k) / 2 / (nz - 1);
+    // Exclusions that change no output, ahead of the FP64 evaluation: a
+    // phase without a rule, and a marker certainly deeper than its rule
+    // reaches (below 200 km; 150 km for mantle phases 4 and 8).  The marker
+    // lies in its triangle, so its depth is at least the surface height less
+    // the highest corner; FP32 copies of those heights err by under 0.1 m
+    // and the test keeps a 10 m margin.
+    {
+        const int ph = A.mark_phase[kk];
+        if (!(ph == 4 || ph == 8 || ph == 10 || ph == 3 || ph == 7 || ph == 9 || ph == 1 || ph == 11 || ph == 17 ||
+              ph == 5 || ph == 16))
+            return;
+        const double *zc = A.cord + d.N;
+        const long long q1 = gf_node(d, j, i), q3 = gf_node(d, j, i + 1);
+        float zmax = fmaxf(fmaxf(gf_d2f(zc[q1]), gf_d2f(zc[q1 + 1])), fmaxf(gf_d2f(zc[q3]), gf_d2f(zc[q3 + 1])));
+        const float surf = 0.5f * (gf_d2f(zc[gf_node(d, 0, i)]) + gf_d2f(zc[gf_node(d, 0, i + 1)]));
+        const float lim = (ph == 4 || ph == 8) ? 150e3f : 200e3f;
+        if (surf - zmax > lim + 10.0f) return;
+    }
     double a1 = A.mark_a1[kk], a2 = A.mark_a2[kk];
     const double *cord = A.cord, *T = A.temp;
     double yy, tmpr;
@@ -1834,7 +1896,7 @@ template <class R> void GfKernels<R>::elem_forces(const GfLaunch &g) {
 
 template <class R> void GfKernels<R>::node(const GfLaunch &g) {
     using namespace gfk;
-    GF_LAUNCH(k_node<R>, g.d.N, g.P, g.C, g.A, g.d);
+    GF_LAUNCH(k_node<R>, g.d.N, g.P, g.C, g.A, g.d, g.node_terms);
 }
 
 template <class R> void GfKernels<R>::move_cord(const GfLaunch &g) {
