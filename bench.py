@@ -590,8 +590,7 @@ def bench_surrogate(args, workdir: str):
     cal = S.calibrate_tolerance(tb, cfg.H, cfg.W)
     t_data = time.time() - t0
     sur = S.Surrogate(cfg, S.Normaliser.fit(snaps), seed=0)
-    info = sur.train(snaps, epochs=args.sur_epochs, batch=64, lr=args.sur_lr,
-                     relative_topography=bool(args.sur_relative_topo))
+    info = sur.train(snaps, epochs=args.sur_epochs, batch=64, lr=args.sur_lr)
     pairs = nt * (args.sur_snaps - 1)
     del snaps
     tb.close()
@@ -621,7 +620,6 @@ def bench_surrogate(args, workdir: str):
     res = S.screen(bb, sur, [p for _, p in fb], interval, cal["tol"])
     err = S.rel_errors(res["fields"], truth, res["raw_t"])
     out = {"members": n, "training_members": nt, "snapshots_per_member": args.sur_snaps,
-           "relative_topography_loss": bool(args.sur_relative_topo),
            "interval_steps": interval, "grid": [cfg.H, cfg.W], "width": cfg.C,
            "modes": [cfg.m1, cfg.m2], "layers": cfg.layers, "training_pairs": pairs, "epochs": args.sur_epochs,
            "train_seconds": info["seconds"], "train_loss_first": info["first_loss"],
@@ -845,8 +843,6 @@ def main():
     ap.add_argument("--sur-interval", type=int, default=500, help="steps between snapshots and of the forecast")
     ap.add_argument("--sur-start", type=int, default=1000, help="plain steps of the fresh sweep before the forecast")
     ap.add_argument("--sur-lr", type=float, default=2e-3)
-    ap.add_argument("--sur-relative-topo", type=int, default=0,
-                    help="1: topography loss weighted per sample by its inverse mean square")
     ap.add_argument("--fno-batch", type=int, default=64, help="batch of the fno profiling run")
     ap.add_argument("--only", choices=["surrogate"], default=None, help="run one leg only (development)")
     ap.add_argument("--profile", choices=["fp64", "mixed", "batch", "fno", "magma"], default=None,

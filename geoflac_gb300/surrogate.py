@@ -104,16 +104,10 @@ class Surrogate:
                                        self.cfg.W, self.s), "pack_input")
 
     def train(self, snaps: Snapshots, epochs: int, batch: int = 64, lr: float = 1e-3, seed: int = 0,
-              max_pairs: Optional[int] = None, surface_weight: float = 64.0,
-              relative_topography: bool = False) -> Dict[str, float]:
+              max_pairs: Optional[int] = None, surface_weight: float = 64.0) -> Dict[str, float]:
         """Adam over all (t, t + interval) pairs, cosine learning rate; the
         displacement channel of the top grid rows (the topography) is
-        weighted by `surface_weight` in the loss.  With
-        `relative_topography`, that weight is scaled per sample by the mean
-        square topography of the training set over the sample's own at
-        t + interval (clamped to 0.05 .. 20): the forecast is judged by each
-        member's relative topography error, which a plain MSE lets grow on
-        the members whose surface moves least."""
+        weighted by `surface_weight` in the loss."""
         import torch
 
         cfg = self.cfg
@@ -132,10 +126,6 @@ class Surrogate:
         inp = torch.empty((batch, cfg.H, cfg.W, cfg.cin), dtype=torch.bfloat16, device="cuda")
         tgt = torch.empty((batch, cfg.H, cfg.W, cfg.cout), dtype=torch.float32, device="cuda")
         prm_b = torch.empty((batch, 4), dtype=torch.float32, device="cuda")
-        if relative_topography:
-            top = snaps.grids[:, 1:, 0, :, 8]
-            ref2 = float((top * top).mean())
-            wb = torch.empty((batch, cfg.H, cfg.W, cfg.cout), dtype=torch.float32, device="cuda")
         steps = epochs * (len(pairs) // batch)
         t0 = time.time()
         it = 0
@@ -153,14 +143,7 @@ class Surrogate:
                 _ck(self.lib.gf_fno_pack_target(_p(yb), _p(xb), _p(self.norm.stats_d), _p(tgt),
                                                 batch * cfg.H * cfg.W, self.s), "pack_target")
                 out = self.net.forward(inp, train=True)
-                w_use = wgt
-                if relative_topography:
-                    n2 = (yb[:, 0, :, 8] * yb[:, 0, :, 8]).mean(dim=1)
-                    sc = (ref2 / n2.clamp_min(1e-30)).clamp(0.05, 20.0)
-                    wb.copy_(wgt.unsqueeze(0).expand_as(wb))
-                    wb[:, :2, :, 8] *= sc[:, None, None]
-                    w_use = wb
-                loss, dout = self.net.loss_grad(out, tgt, w_use)
+                loss, dout = self.net.loss_grad(out, tgt, wgt)
                 self.net.backward(dout)
                 lr_t = 0.5 * lr * (1.0 + math.cos(math.pi * it / max(steps, 1)))
                 self.net.adam(lr=lr_t)
