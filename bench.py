@@ -415,6 +415,9 @@ def run_ours(args):
                                 "rel_err": {k: {q: _r(v) for q, v in sg["rel_err"][k].items()}
                                             for k in ("topography", "plastic_strain")},
                                 "members_over_2pct": sg["members_over_2pct"]}
+    c1 = bench_config1(d)
+    detail["config1"] = c1
+    out["config1"] = {k: c1[k] for k in ("fp64", "mixed", "unit")}
     if args.c3_steps > 0:
         c3 = bench_config3(args, d)
         detail["config3"] = c3
@@ -457,6 +460,37 @@ def mixed_error_steps(inp: str, steps: int):
     a.close()
     b.close()
     return err
+
+
+def bench_config1(workdir: str, steps: int = 2000):
+    """The 60x20 extension model (1,200 elements; config 1 of the workload
+    list) over its full 2000 steps, FP64 and mixed, graph-replayed steps
+    timed with CUDA events: a mesh this small is bound by launch and
+    synchronisation latency, not by the kernels' work."""
+    import torch
+
+    from geoflac_gb300 import inpgen, new_state
+    from geoflac_gb300.flac import Flac
+
+    inp = inpgen.extension_60x20().write(os.path.join(workdir, "extension_60x20.inp"))
+    out = {"workload": "extension_60x20 (1,200 elements, 9 markers per element)", "steps": steps,
+           "unit": "element-steps/s"}
+    for mode in ("fp64", "mixed"):
+        g = Flac(*new_state(inp), mode)
+        stream = torch.cuda.ExternalStream(g.stream)
+        g.step(10)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        g.status()
+        t = e0.elapsed_time(e1) / 1e3
+        out[mode] = _r(1200 * steps / t)
+        out[f"ms_per_step_{mode}"] = _r(1e3 * t / steps)
+        g.close()
+    return out
 
 
 def bench_config3(args, workdir: str):
