@@ -1327,13 +1327,18 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
             };
             double a0 = (double)area[gf_ek(d, e, 0)], a1 = (double)area[gf_ek(d, e, 1)],
                    a2 = (double)area[gf_ek(d, e, 2)], a3 = (double)area[gf_ek(d, e, 3)];
-            double l;
-            l = len(1, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a2 * l));
-            l = len(3, 1); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a2 * l));
-            l = len(3, 2); dl = fmin(dl, 1.0 / (a1 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-            l = len(2, 0); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-            l = len(3, 0); dl = fmin(dl, 1.0 / (a2 * l)); dl = fmin(dl, 1.0 / (a3 * l));
-            l = len(1, 2); dl = fmin(dl, 1.0 / (a0 * l)); dl = fmin(dl, 1.0 / (a1 * l));
+            // the smallest of the twelve quotients 1/(area*length) of
+            // dlmin_prop (dt_mass.f90:174-231) is the quotient of the largest
+            // product: correctly rounded division is monotone, so
+            // min fl(1/x_k) = fl(1/max x_k) exactly, for one division
+            double l, xm = 0.0;
+            l = len(1, 0); xm = fmax(xm, a0 * l); xm = fmax(xm, a2 * l);
+            l = len(3, 1); xm = fmax(xm, a1 * l); xm = fmax(xm, a2 * l);
+            l = len(3, 2); xm = fmax(xm, a1 * l); xm = fmax(xm, a3 * l);
+            l = len(2, 0); xm = fmax(xm, a0 * l); xm = fmax(xm, a3 * l);
+            l = len(3, 0); xm = fmax(xm, a2 * l); xm = fmax(xm, a3 * l);
+            l = len(1, 2); xm = fmax(xm, a0 * l); xm = fmax(xm, a1 * l);
+            dl = fmin(dl, 1.0 / xm);
             int iph = A.iphase[e] - 1;
             dmax = P.conduct[iph] / P.den[iph] / P.cp[iph];
             pm = 1u << iph;

@@ -140,3 +140,51 @@ def test_batch_rejects_fp64_and_mismatched_schedules(workdir):
     with pytest.raises(capi.GfError) as e:
         Batch([a, c])
     assert e.value.code == -2
+
+
+# members of the workload's own sweep (mesh 80x25 .. 400x120 quads): the
+# smallest and largest of the first 40 draws, an extension and a convergence
+SWEEP_MEMBERS = (4, 37, 1, 24)
+
+
+def test_batch_sweep_members_against_single_models_and_oracle(workdir):
+    """Members at the sweep's real sizes (84x26 .. 397x119 quads) advanced
+    10 steps by the ensemble kernel: against the same members stepped alone
+    by the single-model mixed kernels (rounding level, as above), and against
+    the FP64 oracle from its own start-up state (the mixed path's 10-step
+    bounds: coordinates 1e-8, temperature 1e-9, stress 1e-6, velocity 2e-4 of
+    each field's largest value; integer fields exact)."""
+    from oracle.oracle import Oracle
+
+    from ._util import oracle_state, rel_diff
+
+    paths, batched, alone, orcs = [], [], [], []
+    for k in SWEEP_MEMBERS:
+        m, _ = inpgen.ensemble_member(k)
+        path = m.write(str(workdir / f"sweep_{k}.inp"))
+        paths.append(path)
+        batched.append(Flac(*new_state(path), "mixed"))
+        alone.append(Flac(*new_state(path), "mixed"))
+        o = Oracle(*oracle_state(path))
+        o.finish_setflac()
+        orcs.append(o)
+    sizes = [(g.params.nx - 1) * (g.params.nz - 1) for g in batched]
+    assert min(sizes) < 2500 and max(sizes) > 45000
+    b = Batch(batched)
+    b.set_config(threads=256, items_per_thread=2, ctas_per_sm=2, graph_steps=10)
+    b.step(10)
+    for g in alone:
+        g.step(10)
+    for o in orcs:
+        o.step(10)
+    for k, (g, h, o) in enumerate(zip(batched, alone, orcs)):
+        _assert_close(g, h, f"member {SWEEP_MEMBERS[k]} vs alone")
+        err = {f: rel_diff(g.state[f], o.s[f]) for f in ("vel", "cord", "temp", "stress0", "aps")}
+        assert err["cord"] <= 1e-8 and err["temp"] <= 1e-9, (SWEEP_MEMBERS[k], err)
+        assert err["stress0"] <= 1e-6 and err["vel"] <= 2e-4, (SWEEP_MEMBERS[k], err)
+        for f in ("iphase", "nmark_elem", "mark_ntriag"):
+            assert np.array_equal(g.state[f], o.s[f]), (SWEEP_MEMBERS[k], f)
+        assert g.clock.nloop == o.c.nloop
+    b.close()
+    for g in batched + alone:
+        g.close()
