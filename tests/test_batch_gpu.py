@@ -153,10 +153,9 @@ def test_batch_sweep_members_against_single_models_and_oracle(workdir):
     by the single-model mixed kernels (rounding level, as above), and against
     the FP64 oracle from its own start-up state (10-step bounds of each
     field's largest value: coordinates 1e-8, temperature 1e-9; stress 3e-6
-    and velocity 3e-4, wider than the 1e-6 / 2e-4 of the 60x20 and 60x15
-    models because these domains reach 300 km depth, where FP32 stress
-    deviations carry larger absolute rounding; measured 1.0e-6 and 1.0e-4 on
-    member 4; integer fields exact)."""
+    and velocity 3e-4, wider than the 1e-6 / 2e-4 that hold on the 60x20 and
+    60x15 models: member 4 (84x26 quads, convergence at 3.8 cm/yr) measured
+    1.0e-6 and 1.0e-4; integer fields exact)."""
     from oracle.oracle import Oracle
 
     from ._util import oracle_state, rel_diff
