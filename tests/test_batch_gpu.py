@@ -151,25 +151,31 @@ def test_batch_sweep_members_against_single_models_and_oracle(workdir):
     """Members at the sweep's real sizes (84x26 .. 397x119 quads) advanced
     10 steps by the ensemble kernel: against the same members stepped alone
     by the single-model mixed kernels (rounding level, as above), and against
-    the FP64 oracle from its own start-up state (10-step bounds of each
-    field's largest value: coordinates 1e-8, temperature 1e-9; stress 3e-6
-    and velocity 3e-4, wider than the 1e-6 / 2e-4 that hold on the 60x20 and
-    60x15 models: member 4 (84x26 quads, convergence at 3.8 cm/yr) measured
-    1.0e-6 and 1.0e-4; integer fields exact)."""
+    the FP64 oracle from its own start-up state: coordinates 1e-8 and
+    temperature 1e-9 of each field's largest value; stress 1e-6 and velocity
+    2e-4 (the 60x20 / 60x15 10-step bounds) or, where the member itself is
+    that sensitive, 3x the change a relative 1e-7 perturbation of its
+    initial stresses makes in the oracle's FP64 run (the damping of
+    fl_node.f90 switches with the sign of each nodal velocity); integer
+    fields exact."""
     from oracle.oracle import Oracle
 
     from ._util import oracle_state, rel_diff
 
-    paths, batched, alone, orcs = [], [], [], []
+    batched, alone, orcs, perts = [], [], [], []
     for k in SWEEP_MEMBERS:
         m, _ = inpgen.ensemble_member(k)
         path = m.write(str(workdir / f"sweep_{k}.inp"))
-        paths.append(path)
         batched.append(Flac(*new_state(path), "mixed"))
         alone.append(Flac(*new_state(path), "mixed"))
-        o = Oracle(*oracle_state(path))
-        o.finish_setflac()
-        orcs.append(o)
+        for perturb, lst in ((False, orcs), (True, perts)):
+            p, c, st = oracle_state(path)
+            if perturb:
+                rng = np.random.default_rng(k)
+                st["stress0"][...] *= 1 + 1e-7 * rng.choice([-1.0, 1.0], size=st["stress0"].shape)
+            o = Oracle(p, c, st)
+            o.finish_setflac()
+            lst.append(o)
     sizes = [(g.params.nx - 1) * (g.params.nz - 1) for g in batched]
     assert min(sizes) < 2500 and max(sizes) > 45000
     b = Batch(batched)
@@ -177,15 +183,19 @@ def test_batch_sweep_members_against_single_models_and_oracle(workdir):
     b.step(10)
     for g in alone:
         g.step(10)
-    for o in orcs:
+    for o in orcs + perts:
         o.step(10)
-    for k, (g, h, o) in enumerate(zip(batched, alone, orcs)):
-        _assert_close(g, h, f"member {SWEEP_MEMBERS[k]} vs alone")
-        err = {f: rel_diff(g.state[f], o.s[f]) for f in ("vel", "cord", "temp", "stress0", "aps")}
-        assert err["cord"] <= 1e-8 and err["temp"] <= 1e-9, (SWEEP_MEMBERS[k], err)
-        assert err["stress0"] <= 3e-6 and err["vel"] <= 3e-4, (SWEEP_MEMBERS[k], err)
+    fields = ("vel", "cord", "temp", "stress0", "aps")
+    for k, (g, h, o, q) in enumerate(zip(batched, alone, orcs, perts)):
+        who = SWEEP_MEMBERS[k]
+        _assert_close(g, h, f"member {who} vs alone")
+        err = {f: rel_diff(g.state[f], o.s[f]) for f in fields}
+        sens = {f: rel_diff(q.s[f], o.s[f]) for f in fields}
+        assert err["cord"] <= 1e-8 and err["temp"] <= 1e-9, (who, err)
+        assert err["stress0"] <= max(1e-6, 3.0 * sens["stress0"]), (who, err, sens)
+        assert err["vel"] <= max(2e-4, 3.0 * sens["vel"]), (who, err, sens)
         for f in ("iphase", "nmark_elem", "mark_ntriag"):
-            assert np.array_equal(g.state[f], o.s[f]), (SWEEP_MEMBERS[k], f)
+            assert np.array_equal(g.state[f], o.s[f]), (who, f)
         assert g.clock.nloop == o.c.nloop
     b.close()
     for g in batched + alone:
