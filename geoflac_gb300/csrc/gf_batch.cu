@@ -22,6 +22,8 @@
 // Items written in one phase are read in the next within the same kernel:
 // no pointer here may be treated as read-only for the kernel's lifetime.
 #define __restrict__
+// 32-bit indices, as in the mixed instantiation (members are mixed contexts)
+#define GF_IDX int
 #include "gf_kernels_impl.cuh"
 #include "gf_member.h"
 

@@ -622,6 +622,9 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     for (int b = 0; b < p->nofbc; ++b)
         if (mode == GF_MODE_MIXED && p->nbc[b] == 200 && p->nofside[b] == 2) return GF_ERR_UNSUPPORTED;
     if (p->nphase > 32) return GF_ERR_UNSUPPORTED;
+    // the mixed kernels index with 32-bit integers: the largest arrays hold
+    // 32 entries per element or node (mark_id_elem, the marker arrays)
+    if (mode == GF_MODE_MIXED && 32LL * (long long)p->nx * p->nz >= 0x7fffffffLL) return GF_ERR_LIMIT;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         std::fprintf(stderr, "geoflac_gb300: no CUDA device\n");

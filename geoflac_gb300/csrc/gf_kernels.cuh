@@ -69,7 +69,7 @@ struct Quad {
 };
 
 __device__ __forceinline__ void load_quad(const double *__restrict__ cord, const GfDims &d, int j, int i, Quad &q) {
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     q.x[0] = cord[n1];
     q.x[1] = cord[n1 + 1];
     q.x[2] = cord[n3];
@@ -127,12 +127,12 @@ struct QuadF {
     float x[4], y[4];
 };
 
-__device__ __forceinline__ float hl_diff(const float *__restrict__ h, const float *__restrict__ l, long long a,
-                                         long long b) {
+__device__ __forceinline__ float hl_diff(const float *__restrict__ h, const float *__restrict__ l, GF_IDX a,
+                                         GF_IDX b) {
     return (h[a] - h[b]) + (l[a] - l[b]);
 }
 
-__device__ __forceinline__ void quad_nodes(const GfDims &d, int j, int i, long long n[4]) {
+__device__ __forceinline__ void quad_nodes(const GfDims &d, int j, int i, GF_IDX n[4]) {
     n[0] = gf_node(d, j, i);
     n[1] = n[0] + 1;
     n[2] = gf_node(d, j, i + 1);
@@ -140,7 +140,7 @@ __device__ __forceinline__ void quad_nodes(const GfDims &d, int j, int i, long l
 }
 
 __device__ __forceinline__ void load_quad_rel(const DevArrays &A, const GfDims &d, int j, int i, QuadF &q) {
-    long long n[4];
+    GF_IDX n[4];
     quad_nodes(d, j, i, n);
     const float *xh = A.cord_hi, *xl = A.cord_lo, *yh = A.cord_hi + d.N, *yl = A.cord_lo + d.N;
     q.x[0] = 0.0f;
@@ -154,7 +154,7 @@ __device__ __forceinline__ void load_quad_rel(const DevArrays &A, const GfDims &
 
 __device__ __forceinline__ void load_vel_rel(const DevArrays &A, const GfDims &d, int j, int i, float vx[4],
                                              float vy[4]) {
-    long long n[4];
+    GF_IDX n[4];
     quad_nodes(d, j, i, n);
     const float *xh = A.vel_hi, *xl = A.vel_lo, *yh = A.vel_hi + d.N, *yl = A.vel_lo + d.N;
     vx[0] = 0.0f;
@@ -199,13 +199,13 @@ __device__ __forceinline__ void shape_derivs_f(const QuadF &q, const float ar[4]
 
 // Eff_visc (matprops.f90:136-215), always in FP64.
 template <class R>
-__device__ double eff_visc(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+__device__ double eff_visc(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, GF_IDX e,
                            const R *__restrict__ st) {
     for (int k = 0; k < P.ninh100; ++k)
         if (i + 1 >= P.w_ix1[k] && i + 1 <= P.w_ix2[k] && j + 1 >= P.w_iy1[k] && j + 1 <= P.w_iy2[k]) return P.v_min;
     const double adi_grad = 3e-1, r = 8.31448;
     const double *cord = A.cord, *temp = A.temp;
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
     double tmpr0 = 0.25 * (temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
     double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
@@ -252,14 +252,14 @@ __device__ double eff_visc(const DevParams &P, const DevArrays &A, const GfDims 
 // Eff_visc in FP32 for the mixed-precision path: the power-law viscosity is
 // evaluated as a sum of logarithms and clamped in log space, so no
 // intermediate leaves the FP32 range (A^(-1/n) e^(E/nRT) alone can exceed it).
-__device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+__device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, GF_IDX e,
                               const float *__restrict__ st) {
     for (int k = 0; k < P.ninh100; ++k)
         if (i + 1 >= P.w_ix1[k] && i + 1 <= P.w_ix2[k] && j + 1 >= P.w_iy1[k] && j + 1 <= P.w_iy2[k])
             return (float)P.v_min;
     const float *zh = A.cord_hi + d.N;
     const double *temp = A.temp;
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     float zcord = 0.25f * (zh[n1] + zh[n1 + 1] + zh[n3] + zh[n3 + 1]);
     float zsurf = 0.50f * (zh[gf_node(d, 0, i)] + zh[gf_node(d, 0, i + 1)]);
     float tmpr0 = 0.25f * ((float)temp[n1] + (float)temp[n1 + 1] + (float)temp[n3] + (float)temp[n3 + 1]);
@@ -300,7 +300,7 @@ __device__ float eff_visc_f32(const DevParams &P, const DevArrays &A, const GfDi
 
 template <class R>
 __device__ __forceinline__ double visc_of(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i,
-                                          long long e, const R *__restrict__ st) {
+                                          GF_IDX e, const R *__restrict__ st) {
     if (sizeof(R) == sizeof(float)) return (double)eff_visc_f32(P, A, d, j, i, e, (const float *)st);
     return eff_visc<R>(P, A, d, j, i, e, st);
 }
@@ -308,12 +308,12 @@ __device__ __forceinline__ double visc_of(const DevParams &P, const DevArrays &A
 // Eff_dens (matprops.f90:3-83), FP64.  *wrote_frac/*frac_val report the
 // write of the global frac the reference performs (matprops.f90:37,48).
 template <class R>
-__device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+__device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, GF_IDX e,
                            int *wrote_frac, double *frac_val) {
     const double adi_grad = 3e-1, den_ramp_dist = 30e3, amp410 = 0.05, amp660 = 0.085;
     const double *cord = A.cord, *temp = A.temp;
     const R *st = (const R *)A.stress0;
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     double zcord = 0.25 * (cord[d.N + n1] + cord[d.N + n1 + 1] + cord[d.N + n3] + cord[d.N + n3 + 1]);
     double tmpr0 = 0.25 * (temp[n1] + temp[n1 + 1] + temp[n3] + temp[n3 + 1]);
     double zsurf = 0.50 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]);
@@ -364,12 +364,12 @@ __device__ double eff_dens(const DevParams &P, const DevArrays &A, const GfDims 
 // Eff_dens in FP32 for the mixed path (same formula as eff_dens; depths from
 // the hi parts of the coordinates, the pressure from the stored deviations
 // plus p_ref, temperatures from the hi/lo split).
-__device__ float eff_dens_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, long long e,
+__device__ float eff_dens_f32(const DevParams &P, const DevArrays &A, const GfDims &d, int j, int i, GF_IDX e,
                               int *wrote_frac, float *frac_val) {
     const float den_ramp_dist = 30e3f, amp410 = 0.05f, amp660 = 0.085f;
     const float *zh = A.cord_hi + d.N, *th = A.temp_hi;
     const float *st = (const float *)A.stress0;
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     float zcord = 0.25f * (zh[n1] + zh[n1 + 1] + zh[n3] + zh[n3 + 1]);
     float tmpr0 = 0.25f * (th[n1] + th[n1 + 1] + th[n3] + th[n3 + 1]);
     float zsurf = 0.50f * (zh[gf_node(d, 0, i)] + zh[gf_node(d, 0, i + 1)]);
@@ -637,7 +637,7 @@ __device__ __forceinline__ bool maxwell_wins_unyielded(float sp_a, float sp_b, f
 
 // pre_plast (rh_plastic.f90:339-399)
 template <class R>
-__device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, long long e,
+__device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
                                           R aps_e, R &coh, R &phi, R &psi, R &hardn) {
     R pls_curr = aps_e;
     phi = 0; coh = 0; psi = 0; hardn = 0;

@@ -15,16 +15,16 @@
 namespace {
 namespace gfk {
 
-__device__ __forceinline__ void elem_ji(const GfDims &d, long long e, int &j, int &i) {
+__device__ __forceinline__ void elem_ji(const GfDims &d, GF_IDX e, int &j, int &i) {
     i = (int)(e / (d.nz - 1));
-    j = (int)(e - (long long)i * (d.nz - 1));
+    j = (int)(e - (GF_IDX)i * (d.nz - 1));
 }
-__device__ __forceinline__ void node_ji(const GfDims &d, long long n, int &j, int &i) {
+__device__ __forceinline__ void node_ji(const GfDims &d, GF_IDX n, int &j, int &i) {
     i = (int)(n / d.nz);
-    j = (int)(n - (long long)i * d.nz);
+    j = (int)(n - (GF_IDX)i * d.nz);
 }
 
-inline unsigned grid_for(long long n) { return (unsigned)((n + GF_THREADS - 1) / GF_THREADS); }
+inline unsigned grid_for(GF_IDX n) { return (unsigned)((n + GF_THREADS - 1) / GF_THREADS); }
 
 // ======================================================================
 // Mixed path: the element's share of the node forces of fl_node.f90.  For
@@ -37,8 +37,8 @@ inline unsigned grid_for(long long n) { return (unsigned)((n + GF_THREADS - 1) /
 // (sum_e G_c = 0 around an interior node): every FP32 term is a difference.
 // The triangle/vertex tables are fl_node.f90:7-8 for quad 4 - c.
 __device__ __forceinline__ void elem_corner_forces(const float dx[3][4], const float dz[3][4], const float ar[4],
-                                                   const float sn[4][4], float *__restrict__ frc, long long E,
-                                                   long long e) {
+                                                   const float sn[4][4], float *__restrict__ frc, GF_IDX E,
+                                                   GF_IDX e) {
     const int kk[4][3] = {{1, 2, 3}, {0, 1, 2}, {0, 1, 3}, {0, 2, 3}};
     const int mm[4][3] = {{2, 2, 1}, {1, 1, 1}, {2, 0, 2}, {0, 0, 0}};
 #pragma unroll
@@ -65,7 +65,7 @@ __device__ __forceinline__ void elem_corner_forces(const float dx[3][4], const f
 
 // ======================================================================
 // fl_rheol (fl_rheol.f90:4-389): one thread per element.
-template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, long long e) {
+template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop, GF_IDX e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -76,7 +76,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     R *st = (R *)A.stress0;
     const R *area = (const R *)A.area;
 
-    long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+    GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
     R vx[4], vy[4];
     R ar[4];
     for (int k = 0; k < 4; ++k) ar[k] = area[gf_ek(d, e, k)];
@@ -274,8 +274,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
                     R factor = R(0.25) / ar[t];
                     R fx = factor * (sn[0][t] * dx[m][t] + sn[2][t] * dz[m][t]);
                     R fy = factor * (sn[2][t] * dx[m][t] + sn[1][t] * dz[m][t]);
-                    nf[(long long)(6 * c + 2 * k) * d.E + e] = fx;
-                    nf[(long long)(6 * c + 2 * k + 1) * d.E + e] = fy;
+                    nf[(GF_IDX)(6 * c + 2 * k) * d.E + e] = fx;
+                    nf[(GF_IDX)(6 * c + 2 * k + 1) * d.E + e] = fy;
                 }
             }
         }
@@ -364,10 +364,10 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     (void)nloop;
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
-    b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset, long long e) {
+template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset, GF_IDX e) {
     if (e >= d.E) return;
     R *se2sr = (R *)A.se2sr;
     R *e2sr = (R *)A.e2sr;
@@ -385,7 +385,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__res
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset) {
-    b_k_rheol_avg<R>(C, A, d, reset, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_rheol_avg<R>(C, A, d, reset, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // scalar bookkeeping of fl_rheol: dtavg += dt at entry; dtavg = 0 at a reset
@@ -407,7 +407,7 @@ __global__ void k_rheol_clock(DevClock *C, int phase) {
 // right columns), then the interior nodes (column by column, j fastest), so
 // that the boundary nodes, which take the FP64 path with water load and
 // Winkler foundation, run in warps of their own and start first.
-__device__ __forceinline__ long long node_of_slot(const GfDims &d, long long t) {
+__device__ __forceinline__ GF_IDX node_of_slot(const GfDims &d, GF_IDX t) {
     const int nzi = d.nz - 2;
     if (t < d.nx) return gf_node(d, 0, (int)t);
     t -= d.nx;
@@ -418,7 +418,7 @@ __device__ __forceinline__ long long node_of_slot(const GfDims &d, long long t) 
     if (t < nzi) return gf_node(d, 1 + (int)t, d.nx - 1);
     t -= nzi;
     const int i = (int)(t / nzi);
-    return gf_node(d, 1 + (int)(t - (long long)i * nzi), 1 + i);
+    return gf_node(d, 1 + (int)(t - (GF_IDX)i * nzi), 1 + i);
 }
 
 // (hi, lo) + b in FP32 pairs: two-sum of hi and b, then renormalised
@@ -439,17 +439,17 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float b) {
 // the velocity increment are FP32; the velocity is carried as its hi/lo FP32
 // pair and written back to the FP64 array as hi + lo.
 __device__ __forceinline__ void node_interior_f(const DevParams &P, const DevClock *__restrict__ C, DevArrays &A,
-                                                const GfDims &d, long long n, int j, int i) {
+                                                const GfDims &d, GF_IDX n, int j, int i) {
     const float *st = (const float *)A.stress0;
     const float *frc = A.e_frc;
-    const long long E = d.E;
-    const long long en = gf_elem(d, j - 1, i - 1);
+    const GF_IDX E = d.E;
+    const GF_IDX en = gf_elem(d, j - 1, i - 1);
     const float nxx = st[gf_s(d, en, 0, 1)], nzz = st[gf_s(d, en, 1, 1)], nxz = st[gf_s(d, en, 2, 1)];
     float fx0 = 0.0f, fy0 = 0.0f;
 #pragma unroll
     for (int qd = 0; qd < 4; ++qd) {
         const int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
-        const long long e = gf_elem(d, je, ie);
+        const GF_IDX e = gf_elem(d, je, ie);
         const int c = 3 - qd; // this node's corner of element e
         const float dp = hl_diff(A.pr_hi, A.pr_lo, e, en);
         const float rxx = (st[gf_s(d, e, 0, 1)] - nxx) - dp;
@@ -492,9 +492,9 @@ __device__ __forceinline__ void node_interior_f(const DevParams &P, const DevClo
     A.vel_lo[d.N + n] = l1;
 }
 
-template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long slot, int terms = 0) {
+template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX slot, int terms = 0) {
     if (slot >= d.N) return;
-    const long long n = node_of_slot(d, slot);
+    const GF_IDX n = node_of_slot(d, slot);
     const DevParams &P = *Pp;
     int j, i;
     node_ji(d, n, j, i);
@@ -527,15 +527,15 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         for (int qd = 0; qd < 4; ++qd) {
             int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
             if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
-            const long long e = gf_elem(d, je, ie);
+            const GF_IDX e = gf_elem(d, je, ie);
             const int c = 3 - qd;
-            long long nn[4];
+            GF_IDX nn[4];
             quad_nodes(d, je, ie, nn);
             double Gx = 0.0, Gz = 0.0;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int t = kk[qd][k], m = mm[qd][k];
-                const long long u = nn[uv[t][m][0]], v = nn[uv[t][m][1]];
+                const GF_IDX u = nn[uv[t][m][0]], v = nn[uv[t][m][1]];
                 Gx += cy[u] - cy[v];
                 Gz += cx[v] - cx[u];
             }
@@ -556,12 +556,12 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         for (int qd = 0; qd < 4; ++qd) {
             int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
             if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
-            const long long e = gf_elem(d, je, ie);
+            const GF_IDX e = gf_elem(d, je, ie);
             const int c = 3 - qd;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                fx0 = fx0 - A.n_frc[(long long)(6 * c + 2 * k) * d.E + e];
-                fy0 = fy0 - A.n_frc[(long long)(6 * c + 2 * k + 1) * d.E + e];
+                fx0 = fx0 - A.n_frc[(GF_IDX)(6 * c + 2 * k) * d.E + e];
+                fy0 = fy0 - A.n_frc[(GF_IDX)(6 * c + 2 * k + 1) * d.E + e];
             }
         }
         f0 = (double)fx0;
@@ -573,7 +573,7 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         for (int qd = 0; qd < 4; ++qd) {
             int je = j + (qd < 2 ? -1 : 0), ie = i + ((qd & 1) ? 0 : -1);
             if (je < 0 || ie < 0 || je > nz - 2 || ie > nx - 2) continue;
-            long long e = gf_elem(d, je, ie);
+            GF_IDX e = gf_elem(d, je, ie);
             Quad q;
             load_quad(A.cord, d, je, ie, q);
             R ar[4];
@@ -623,13 +623,13 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         double rosubg = P.g * (P.den[ips] + P.drosub) * (1 - P.alfa[ips] * A.temp[n] + P.beta[ips] * p_est);
         double pl = 0, dlxl = 0, dlyl = 0, pr = 0, dlxr = 0, dlyr = 0;
         if (i > 0) {
-            long long m = gf_node(d, nz - 1, i - 1);
+            GF_IDX m = gf_node(d, nz - 1, i - 1);
             pl = P.pisos - rosubg * ((cord[d.N + m] + zb) / 2.0 - P.rzbo);
             dlxl = cord[n] - cord[m];
             dlyl = zb - cord[d.N + m];
         }
         if (i < nx - 1) {
-            long long m = gf_node(d, nz - 1, i + 1);
+            GF_IDX m = gf_node(d, nz - 1, i + 1);
             pr = P.pisos - rosubg * ((cord[d.N + m] + zb) / 2.0 - P.rzbo);
             dlxr = cord[m] - cord[n];
             dlyr = cord[d.N + m] - zb;
@@ -674,12 +674,12 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int terms) {
-    b_k_node<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x, terms);
+    b_k_node<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x, terms);
 }
 
 // ======================================================================
 // fl_move (fl_move.f90:3-132)
-__device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d, long long n) {
+__device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX n) {
     if (n >= 2 * d.N) return;
     const double c = A.cord[n] + A.vel[n] * C->dt;
     A.cord[n] = c;
@@ -691,10 +691,10 @@ __device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArray
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    b_k_move_cord(C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_move_cord(C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time, long long e) {
+template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time, GF_IDX e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
@@ -710,7 +710,7 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
         load_vel_rel(A, d, j, i, rvx, rvy);
     } else {
         load_quad(A.cord, d, j, i, q);
-        long long n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
+        GF_IDX n1 = gf_node(d, j, i), n3 = gf_node(d, j, i + 1);
         const double *vel = A.vel;
         xv[0] = vel[n1]; xv[1] = vel[n1 + 1]; xv[2] = vel[n3]; xv[3] = vel[n3 + 1];
         yv[0] = vel[d.N + n1]; yv[1] = vel[d.N + n1 + 1]; yv[2] = vel[d.N + n3]; yv[3] = vel[d.N + n3 + 1];
@@ -782,7 +782,7 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
     if (neg) set_status(C, 40, (int)e);
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time) {
-    b_k_move_elem<R>(C, A, d, advance_time, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_move_elem<R>(C, A, d, advance_time, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
@@ -810,7 +810,7 @@ __device__ __forceinline__ int kidx(int a, int b) {
     return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
 }
 
-template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc, long long e) {
+template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc, GF_IDX e) {
     if (e == 0)
         for (int k = 0; k < GF_THERM_KMAX; ++k) C->therm_flags[k] = 0; // before any sweep runs
     if (e >= d.E) return;
@@ -827,7 +827,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     Quad q;
     load_quad(A.cord, d, j, i, q);
     const R *area = (const R *)A.area;
-    const long long E = d.E;
+    const GF_IDX E = d.E;
     // triangle A: local vertices (q1,q2,q3); triangle B: (q3,q2,q4)
     const int tv[2][3] = {{0, 1, 2}, {2, 1, 3}};
 #pragma unroll
@@ -849,7 +849,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc) {
-    b_k_therm_prep<R>(Pp, C, A, d, tc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_therm_prep<R>(Pp, C, A, d, tc, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Temperature after the boundary conditions of fl_therm.f90:573-598 (top
@@ -879,7 +879,7 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
 // written by other CTAs of the same (persistent) launch, so their loads
 // bypass L1 (__ldcg).
 __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double dt, const double *__restrict__ tc,
-                                                 const double *Tup, double *Tout, int k, long long n) {
+                                                 const double *Tup, double *Tout, int k, GF_IDX n) {
     int j, i;
     node_ji(d, n, j, i);
     // A node's sweep-k value depends on sweep k-1 only through its upstream
@@ -887,7 +887,7 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     // sweep k-1 its value is the one it had (the same inputs give the same
     // result), and the FP64 evaluation is skipped.
     if (k > 0) {
-        const uint8_t *prev = A.t_chg + (long long)((k - 1) & 1) * d.N;
+        const uint8_t *prev = A.t_chg + (GF_IDX)((k - 1) & 1) * d.N;
         bool recompute = (j != 0 && __ldcg(prev + gf_node(d, j - 1, i))) ||
                          (i != 0 && __ldcg(prev + gf_node(d, j, i - 1))) ||
                          (i != 0 && j != d.nz - 1 && __ldcg(prev + gf_node(d, j + 1, i - 1)));
@@ -897,17 +897,17 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
         }
     }
     const int nx = d.nx, nz = d.nz;
-    const long long E = d.E;
+    const GF_IDX E = d.E;
     const double *T = A.temp;
     double rhs = 0.0, area_n = 0.0;
     auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
     auto U = [&](int jj, int ii) { return __ldcg(Tup + Nd(jj, ii)); };
     // triangle t of element e; vs = local index of the updated node; the
     // three (local vertex, temperature) terms in the reference's order
-    auto tri = [&](long long e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
+    auto tri = [&](GF_IDX e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
         double ra = tc[(12 + t) * E + e];
         area_n = area_n + ra;
-        const double *K = tc + (long long)t * 6 * E + e;
+        const double *K = tc + (GF_IDX)t * 6 * E + e;
         rhs = rhs + tc[(16 + t) * E + e] -
               tc[(14 + t) * E + e] * (T0 * K[kidx(v0, vs) * E] + T1 * K[kidx(v1, vs) * E] + T2 * K[kidx(v2, vs) * E]);
     };
@@ -915,12 +915,12 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     if (j != 0 && i != 0) // element (j-1,i-1), triangle B: vertices (j-1,i), (j,i-1), node
         tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, U(j - 1, i), 1, U(j, i - 1), 2, Ts);
     if (j != 0 && i != nx - 1) { // element (j-1,i), triangles A and B
-        long long e = gf_elem(d, j - 1, i);
+        GF_IDX e = gf_elem(d, j - 1, i);
         tri(e, 0, 1, 0, U(j - 1, i), 1, Ts, 2, T[Nd(j - 1, i + 1)]);
         tri(e, 1, 1, 0, T[Nd(j - 1, i + 1)], 1, Ts, 2, T[Nd(j, i + 1)]);
     }
     if (j != nz - 1 && i != 0) { // element (j,i-1), triangles A and B
-        long long e = gf_elem(d, j, i - 1);
+        GF_IDX e = gf_elem(d, j, i - 1);
         tri(e, 0, 2, 0, U(j, i - 1), 1, U(j + 1, i - 1), 2, Ts);
         tri(e, 1, 0, 0, Ts, 1, U(j + 1, i - 1), 2, T[Nd(j + 1, i)]);
     }
@@ -935,7 +935,7 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
 // counter in bar[1], arrivals in bar[0], error flag in bar[2].  A CTA that
 // waits longer than `limit` polls sets the flag; every CTA returns false
 // once the flag is set.
-__device__ bool gf_grid_barrier(unsigned *bar, long long limit) {
+__device__ bool gf_grid_barrier(unsigned *bar, GF_IDX limit) {
     __shared__ int bad;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -948,7 +948,7 @@ __device__ bool gf_grid_barrier(unsigned *bar, long long limit) {
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
-            long long it = 0;
+            GF_IDX it = 0;
             while (*vgen == g0) {
                 if (++it > limit) {
                     atomicExch(bar + 2, 1u);
@@ -973,18 +973,18 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__
                                                             DevArrays A, GfDims d, const double *__restrict__ tc,
                                                             double *b0, double *b1, int kmax, int keep_temp0,
                                                             unsigned *bar) {
-    const long long stride = (long long)gridDim.x * blockDim.x; // a multiple of 32
-    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long npad = (d.N + 31) / 32 * 32; // equal trip counts within a warp (the vote)
+    const GF_IDX stride = (GF_IDX)gridDim.x * blockDim.x; // a multiple of 32
+    const GF_IDX gt = (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x;
+    const GF_IDX npad = (d.N + 31) / 32 * 32; // equal trip counts within a warp (the vote)
     const double dt = C->dt;
     int kc = kmax; // the first sweep that changed nothing
     for (int k = 0; k < kmax; ++k) {
         const double *up = k == 0 ? A.temp : ((k - 1) & 1 ? b1 : b0);
         double *out = (k & 1) ? b1 : b0;
         bool any = false;
-        for (long long n = gt; n < npad; n += stride) {
+        for (GF_IDX n = gt; n < npad; n += stride) {
             bool changed = n < d.N && therm_sweep_node(A, d, dt, tc, up, out, k, n);
-            if (n < d.N) A.t_chg[(long long)(k & 1) * d.N + n] = changed ? 1 : 0;
+            if (n < d.N) A.t_chg[(GF_IDX)(k & 1) * d.N + n] = changed ? 1 : 0;
             any = any || changed;
         }
         if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) C->therm_flags[k] = 1;
@@ -1002,10 +1002,10 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__
         if (kc == kmax) C->therm_unconverged += 1;
     }
     const double *src = ((kc < kmax ? kc : kmax - 1) & 1) ? b1 : b0;
-    for (long long n = gt; n < d.N; n += stride) {
+    for (GF_IDX n = gt; n < d.N; n += stride) {
         int j, i;
         node_ji(d, n, j, i);
-        double t = therm_bc_value(*Pp, A, d, [src](long long m) { return __ldcg(src + m); }, j, i);
+        double t = therm_bc_value(*Pp, A, d, [src](GF_IDX m) { return __ldcg(src + m); }, j, i);
         if (!keep_temp0) A.temp0[n] = A.temp[n];
         A.temp[n] = t;
     }
@@ -1017,7 +1017,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__
 // accuracy that a sum of ~1000 C values would lose.  Sweep 0 is the all-old
 // (Jacobi) update, sweep 1 reuses the upstream increments of sweep 0, which
 // leaves an error of order (kappa dt/h^2)^2 relative to the increment.
-__device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc, long long e) {
+__device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc, GF_IDX e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     int j, i;
@@ -1030,7 +1030,7 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     QuadF q;
     load_quad_rel(A, d, j, i, q);
     const float *area = (const float *)A.area;
-    const long long E = d.E;
+    const GF_IDX E = d.E;
     const int tv[2][3] = {{0, 1, 2}, {2, 1, 3}};
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
@@ -1050,44 +1050,44 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc) {
-    b_k_therm_prep32(Pp, A, d, tc, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_therm_prep32(Pp, A, d, tc, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // sweep 0 (final = 0): dT0 = increment with old values; sweep 1 (final = 1):
 // upstream neighbours use T + dT0, and tnew = T + dT1 (FP64) is written.
 // The temperature differences come from the hi/lo FP32 split of T.
-__device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep, long long n) {
+__device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep, GF_IDX n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
     const int nx = d.nx, nz = d.nz;
-    const long long E = d.E;
+    const GF_IDX E = d.E;
     const float *th = A.temp_hi, *tl = A.temp_lo;
     float rhs = 0.0f, area_n = 0.0f;
     auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
     // temperature difference to the updated node; upstream nodes carry the
     // increment of sweep 0 in the final sweep
-    auto dT = [&](long long m, bool up) {
+    auto dT = [&](GF_IDX m, bool up) {
         float v = hl_diff(th, tl, m, n);
         if (up && final_sweep) v += d0[m];
         return v;
     };
-    auto tri = [&](long long e, int t, int vs, int v0, float D0, int v1, float D1, int v2, float D2) {
+    auto tri = [&](GF_IDX e, int t, int vs, int v0, float D0, int v1, float D1, int v2, float D2) {
         float ra = tc[(12 + t) * E + e];
         area_n += ra;
-        const float *K = tc + (long long)t * 6 * E + e;
+        const float *K = tc + (GF_IDX)t * 6 * E + e;
         rhs += tc[(16 + t) * E + e] - tc[(14 + t) * E + e] * (D0 * K[kidx(v0, vs) * E] + D1 * K[kidx(v1, vs) * E] +
                                                            D2 * K[kidx(v2, vs) * E]);
     };
     if (j != 0 && i != 0)
         tri(gf_elem(d, j - 1, i - 1), 1, 2, 0, dT(Nd(j - 1, i), true), 1, dT(Nd(j, i - 1), true), 2, 0.0f);
     if (j != 0 && i != nx - 1) {
-        long long e = gf_elem(d, j - 1, i);
+        GF_IDX e = gf_elem(d, j - 1, i);
         tri(e, 0, 1, 0, dT(Nd(j - 1, i), true), 1, 0.0f, 2, dT(Nd(j - 1, i + 1), false));
         tri(e, 1, 1, 0, dT(Nd(j - 1, i + 1), false), 1, 0.0f, 2, dT(Nd(j, i + 1), false));
     }
     if (j != nz - 1 && i != 0) {
-        long long e = gf_elem(d, j, i - 1);
+        GF_IDX e = gf_elem(d, j, i - 1);
         tri(e, 0, 2, 0, dT(Nd(j, i - 1), true), 1, dT(Nd(j + 1, i - 1), true), 2, 0.0f);
         tri(e, 1, 0, 0, 0.0f, 1, dT(Nd(j + 1, i - 1), true), 2, dT(Nd(j + 1, i), false));
     }
@@ -1100,16 +1100,16 @@ __device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ 
         tnew[n] = A.temp[n] + gf_f2d(inc);
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep) {
-    b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // temp0 = temp; temp = tnew with the boundary conditions (which read tnew
 // at neighbours, never the temp being overwritten), and its split
-__device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew, long long n) {
+__device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew, GF_IDX n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
-    const double t = therm_bc_value(*Pp, A, d, [tnew](long long m) { return tnew[m]; }, j, i);
+    const double t = therm_bc_value(*Pp, A, d, [tnew](GF_IDX m) { return tnew[m]; }, j, i);
     A.temp0[n] = A.temp[n];
     A.temp[n] = t;
     float h, l;
@@ -1118,13 +1118,13 @@ __device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ 
     A.temp_lo[n] = l;
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew) {
-    b_k_therm_apply32(Pp, A, d, tnew, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_therm_apply32(Pp, A, d, tnew, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
 // rmasses (rmasses.f90:236-295): per-element density, then a node gather in
 // the reference's colour order with each element's triangles in order.
-template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long e) {
+template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
@@ -1152,29 +1152,29 @@ template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams
     if (wrote) {
         // serial position of this element in the coloured sweep
         int ib = i & 1, jb = j & 1;
-        long long ci = (long long)(d.nx - 1 - ib + 1) / 2; // columns of this colour
-        long long cj = (long long)(d.nz - 1 - jb + 1) / 2;
-        long long before = 0;
+        GF_IDX ci = (GF_IDX)(d.nx - 1 - ib + 1) / 2; // columns of this colour
+        GF_IDX cj = (GF_IDX)(d.nz - 1 - jb + 1) / 2;
+        GF_IDX before = 0;
         for (int b = 0; b < ib * 2 + jb; ++b) {
             int bi = b >> 1, bj = b & 1;
-            before += (long long)((d.nx - 1 - bi + 1) / 2) * ((d.nz - 1 - bj + 1) / 2);
+            before += (GF_IDX)((d.nx - 1 - bi + 1) / 2) * ((d.nz - 1 - bj + 1) / 2);
         }
-        long long pos = before + (long long)(i >> 1) * cj + (j >> 1);
+        GF_IDX pos = before + (GF_IDX)(i >> 1) * cj + (j >> 1);
         (void)ci;
         atomicMax((unsigned long long *)&C->frac_writer, (unsigned long long)(pos + 1));
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    b_k_elem_dens<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_elem_dens<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <class R> __device__ __forceinline__ void b_k_frac_fix(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
     long long w = C->frac_writer;
     if (w <= 0) return;
-    long long pos = w - 1;
+    GF_IDX pos = w - 1;
     for (int b = 0; b < 4; ++b) {
         int bi = b >> 1, bj = b & 1;
-        long long ci = (d.nx - 1 - bi + 1) / 2, cj = (d.nz - 1 - bj + 1) / 2;
+        GF_IDX ci = (d.nx - 1 - bi + 1) / 2, cj = (d.nz - 1 - bj + 1) / 2;
         if (pos < ci * cj) {
             int i = (int)(pos / cj) * 2 + bi, j = (int)(pos % cj) * 2 + bj;
             int wrote = 0;
@@ -1203,7 +1203,7 @@ __device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3},
 // T = double: FP64 shares summed in the reference's order; T = float: the
 // mixed path's FP32 shares
 template <class T>
-__device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d, long long n) {
+__device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d, GF_IDX n) {
     if (n >= d.N) return;
     int j, i;
     node_ji(d, n, j, i);
@@ -1220,7 +1220,7 @@ __device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, d
             if (ord[q] != c) continue;
             int je = je_[q], ie = ie_[q];
             if (je < 0 || ie < 0 || je > d.nz - 2 || ie > d.nx - 2) continue;
-            long long e = gf_elem(d, je, ie);
+            GF_IDX e = gf_elem(d, je, ie);
 #pragma unroll
             for (int t = 0; t < 3; ++t) acc = acc + tri[c_vtx_tris[lv[q]][t] * d.E + e];
         }
@@ -1229,7 +1229,7 @@ __device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, d
 }
 template <class T>
 __global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d) {
-    b_k_node_gather_tri<T>(tri, out, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_node_gather_tri<T>(tri, out, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
@@ -1275,7 +1275,7 @@ __device__ __forceinline__ void dt_block_commit(DevClock *__restrict__ C, double
     __syncthreads(); // the shared slots are free for the CTA's next item
 }
 
-template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long t) {
+template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX t) {
     const DevParams &P = *Pp;
     double dl = 1e300, vmax = 0.0, dmax = 0.0;
     unsigned pm = 0;
@@ -1286,7 +1286,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
         // elements is taken on their FP64 values
         float df = 1e30f, vf = 0.0f;
         if (t < d.E) {
-            long long e = t;
+            GF_IDX e = t;
             int j, i;
             elem_ji(d, e, j, i);
             const float *area = (const float *)A.area;
@@ -1315,7 +1315,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
         return;
     } else {
         if (t < d.E) {
-            long long e = t;
+            GF_IDX e = t;
             int j, i;
             elem_ji(d, e, j, i);
             const R *area = (const R *)A.area;
@@ -1352,7 +1352,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    b_k_dt_reduce<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_dt_reduce<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 __device__ __forceinline__ void b_k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restrict__ C) {
@@ -1404,7 +1404,7 @@ __global__ void k_dt_scalars(const DevParams *__restrict__ Pp, DevClock *__restr
 
 // inertial mass share of each triangle c1d12*rho_inert/area
 // (dt_mass.f90:83-120), one element per thread
-template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, long long e) {
+template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
     const DevParams &P = *Pp;
     const R *area = (const R *)A.area;
@@ -1440,7 +1440,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
     for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
-    b_k_elem_am3<R>(Pp, C, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_elem_am3<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 __device__ __forceinline__ void b_k_dt_reset(DevClock *C) {
@@ -1455,19 +1455,19 @@ __global__ void k_dt_reset(DevClock *C) {
 
 // ======================================================================
 // init_visc
-template <class R> __device__ __forceinline__ void b_k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, long long e) {
+template <class R> __device__ __forceinline__ void b_k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
     ((R *)A.visn)[e] = R(visc_of<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
-    b_k_init_visc<R>(Pp, A, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_init_visc<R>(Pp, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
 // change_phase (change_phase.f90:35-262)
-__device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, long long kk) {
+__device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, GF_IDX kk) {
     if (kk >= nmarkers) return;
     if (A.mark_dead[kk] == 0) return;
     const DevParams &P = *Pp;
@@ -1488,7 +1488,7 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
               ph == 5 || ph == 16))
             return;
         const double *zc = A.cord + d.N;
-        const long long q1 = gf_node(d, j, i), q3 = gf_node(d, j, i + 1);
+        const GF_IDX q1 = gf_node(d, j, i), q3 = gf_node(d, j, i + 1);
         float zmax = fmaxf(fmaxf(gf_d2f(zc[q1]), gf_d2f(zc[q1 + 1])), fmaxf(gf_d2f(zc[q3]), gf_d2f(zc[q3 + 1])));
         const float surf = 0.5f * (gf_d2f(zc[gf_node(d, 0, i)]) + gf_d2f(zc[gf_node(d, 0, i + 1)]));
         const float lim = (ph == 4 || ph == 8) ? 150e3f : 200e3f;
@@ -1497,7 +1497,7 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     double a1 = A.mark_a1[kk], a2 = A.mark_a2[kk];
     const double *cord = A.cord, *T = A.temp;
     double yy, tmpr;
-    long long p1, p2, p3;
+    GF_IDX p1, p2, p3;
     if (k == 1) {
         p1 = gf_node(d, j, i); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j, i + 1);
     } else {
@@ -1508,11 +1508,11 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     double depth = 0.5 * (cord[d.N + gf_node(d, 0, i)] + cord[d.N + gf_node(d, 0, i + 1)]) - yy;
     if (depth > 200e3) return;
     int iph = A.mark_phase[kk];
-    long long e = gf_elem(d, j, i);
+    GF_IDX e = gf_elem(d, j, i);
     const double mantle_density = 3000.0;
-    long long total = (long long)P.nphase * d.E;
-    auto pr = [&](long long eb, int ph1) {
-        long long off = (long long)(ph1 - 1) + (long long)P.nphase * eb;
+    GF_IDX total = (GF_IDX)P.nphase * d.E;
+    auto pr = [&](GF_IDX eb, int ph1) {
+        GF_IDX off = (GF_IDX)(ph1 - 1) + (GF_IDX)P.nphase * eb;
         return (off < 0 || off >= total) ? 0.0 : A.phase_ratio[off];
     };
     int newph = 0;
@@ -1527,7 +1527,7 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
         if (press < trpres && press > trpres2) {
             int jb0 = min(j + 2, nz - 1), jb1 = min(j + 1 + P.nelem_serp, nz - 1);
             for (int jb = jb0; jb <= jb1; ++jb) {
-                long long eb = gf_elem(d, jb - 1, i);
+                GF_IDX eb = gf_elem(d, jb - 1, i);
                 if (pr(eb, 3) > 0.8 || pr(eb, 7) > 0.8 || pr(eb, 1) > 0.8 || pr(eb, 11) > 0.8) {
                     newph = 9;
                     break;
@@ -1589,14 +1589,14 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
-    b_k_phase_markers(Pp, A, d, nmarkers, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_phase_markers(Pp, A, d, nmarkers, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // The same rules in FP32 for the mixed path: the marker's depth below the
 // surface from coordinate differences of the hi/lo splits, its temperature
 // from the hi parts.  Decisions within FP32 rounding of a threshold may
 // differ from the FP64 path.
-__device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, long long kk) {
+__device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers, GF_IDX kk) {
     if (kk >= nmarkers) return;
     if (A.mark_dead[kk] == 0) return;
     const DevParams &P = *Pp;
@@ -1606,14 +1606,14 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     int j = ((n - k) / 2) % (nz - 1);
     int i = (n - k) / 2 / (nz - 1);
     const float a1 = gf_d2f(A.mark_a1[kk]), a2 = gf_d2f(A.mark_a2[kk]), a3 = 1.0f - a1 - a2;
-    long long p1, p2, p3;
+    GF_IDX p1, p2, p3;
     if (k == 1) {
         p1 = gf_node(d, j, i); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j, i + 1);
     } else {
         p1 = gf_node(d, j, i + 1); p2 = gf_node(d, j + 1, i); p3 = gf_node(d, j + 1, i + 1);
     }
     const float *zh = A.cord_hi + d.N, *zl = A.cord_lo + d.N, *th = A.temp_hi;
-    const long long s0 = gf_node(d, 0, i), s1 = gf_node(d, 0, i + 1);
+    const GF_IDX s0 = gf_node(d, 0, i), s1 = gf_node(d, 0, i + 1);
     // depth = 0.5 * (z_s0 + z_s1) - sum a_k z_pk, as differences to z_s0
     const float ds1 = hl_diff(zh, zl, s1, s0);
     const float y1 = hl_diff(zh, zl, p1, s0), y2 = hl_diff(zh, zl, p2, s0), y3 = hl_diff(zh, zl, p3, s0);
@@ -1621,11 +1621,11 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     if (depth > 200e3f) return;
     const float tmpr = th[p1] * a1 + th[p2] * a2 + th[p3] * a3;
     int iph = A.mark_phase[kk];
-    long long e = gf_elem(d, j, i);
+    GF_IDX e = gf_elem(d, j, i);
     const float rho_g = 3000.0f * P.f_g;
-    long long total = (long long)P.nphase * d.E;
-    auto pr = [&](long long eb, int ph1) {
-        long long off = (long long)(ph1 - 1) + (long long)P.nphase * eb;
+    GF_IDX total = (GF_IDX)P.nphase * d.E;
+    auto pr = [&](GF_IDX eb, int ph1) {
+        GF_IDX off = (GF_IDX)(ph1 - 1) + (GF_IDX)P.nphase * eb;
         return (off < 0 || off >= total) ? 0.0 : A.phase_ratio[off];
     };
     int newph = 0;
@@ -1640,7 +1640,7 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
         if (press < trpres && press > trpres2) {
             int jb0 = min(j + 2, nz - 1), jb1 = min(j + 1 + P.nelem_serp, nz - 1);
             for (int jb = jb0; jb <= jb1; ++jb) {
-                long long eb = gf_elem(d, jb - 1, i);
+                GF_IDX eb = gf_elem(d, jb - 1, i);
                 if (pr(eb, 3) > 0.8 || pr(eb, 7) > 0.8 || pr(eb, 1) > 0.8 || pr(eb, 11) > 0.8) {
                     newph = 9;
                     break;
@@ -1700,11 +1700,11 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
-    b_k_phase_markers32(Pp, A, d, nmarkers, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_phase_markers32(Pp, A, d, nmarkers, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // count_phase_ratio (marker_data.f90:140-172) for flagged elements + aps
-template <class R> __device__ __forceinline__ void b_k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all, long long e) {
+template <class R> __device__ __forceinline__ void b_k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all, GF_IDX e) {
     if (e >= d.E) return;
     if (!all && !A.e_flag[e]) return;
     const DevParams &P = *Pp;
@@ -1739,12 +1739,12 @@ template <class R> __device__ __forceinline__ void b_k_phase_recount(const DevPa
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all) {
-    b_k_phase_recount<R>(Pp, C, A, d, all, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_phase_recount<R>(Pp, C, A, d, all, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ======================================================================
 // itest_mesh angle criterion (rem_test.f90:77-118): min over all triangles
-__device__ __forceinline__ void b_k_min_angle(DevArrays A, GfDims d, unsigned long long *out, long long e) {
+__device__ __forceinline__ void b_k_min_angle(DevArrays A, GfDims d, unsigned long long *out, GF_IDX e) {
     double amin = 180.0;
     if (e < d.E) {
         int j, i;
@@ -1774,21 +1774,21 @@ __device__ __forceinline__ void b_k_min_angle(DevArrays A, GfDims d, unsigned lo
     if ((threadIdx.x & 31) == 0) atomic_min_pos(out, fmax(amin, 0.0));
 }
 __global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d, unsigned long long *out) {
-    b_k_min_angle(A, d, out, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_min_angle(A, d, out, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // FP64 host array -> R device array
-template <class R> __device__ __forceinline__ void b_k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n, long long t) {
+template <class R> __device__ __forceinline__ void b_k_convert(const double *__restrict__ src, R *__restrict__ dst, GF_IDX n, GF_IDX t) {
     if (t < n) dst[t] = R(src[t]);
 }
-template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, long long n) {
-    b_k_convert<R>(src, dst, n, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, GF_IDX n) {
+    b_k_convert<R>(src, dst, n, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
-template <class R> __device__ __forceinline__ void b_k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n, long long t) {
+template <class R> __device__ __forceinline__ void b_k_convert_back(const R *__restrict__ src, double *__restrict__ dst, GF_IDX n, GF_IDX t) {
     if (t < n) dst[t] = (double)src[t];
 }
-template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, long long n) {
-    b_k_convert_back<R>(src, dst, n, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, GF_IDX n) {
+    b_k_convert_back<R>(src, dst, n, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 } // namespace gfk
@@ -1837,8 +1837,8 @@ template <class R> void GfKernels<R>::therm(const GfLaunch &g, int sweeps, int k
         cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
         if (occ[dev] <= 0) occ[dev] = 1;
     }
-    const long long need = (g.d.N + GF_THREADS - 1) / GF_THREADS;
-    const long long cap = (long long)occ[dev] * sms[dev];
+    const GF_IDX need = (g.d.N + GF_THREADS - 1) / GF_THREADS;
+    const GF_IDX cap = (GF_IDX)occ[dev] * sms[dev];
     // arrivals and the error flag start at zero in every launch (the
     // generation counter only has to change)
     cudaMemsetAsync(g.therm_bar, 0, sizeof(unsigned), g.s);
@@ -1872,7 +1872,7 @@ template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, 
 namespace {
 namespace gfk {
 __global__ void __launch_bounds__(GF_THREADS) k_elem_forces(DevArrays A, GfDims d) {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const GF_IDX e = (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
     int j, i;
     elem_ji(d, e, j, i);
@@ -1929,7 +1929,7 @@ template <class R> void GfKernels<R>::dt_mass(const GfLaunch &g) {
     using namespace gfk;
     k_dt_reset<<<1, 1, 0, g.s>>>(g.C);
     ++*g.launches;
-    long long n = g.d.E > g.d.N ? g.d.E : g.d.N;
+    GF_IDX n = g.d.E > g.d.N ? g.d.E : g.d.N;
     GF_LAUNCH(k_dt_reduce<R>, n, g.P, g.C, g.A, g.d);
     k_dt_scalars<<<1, 1, 0, g.s>>>(g.P, g.C);
     ++*g.launches;
@@ -1949,16 +1949,16 @@ template <class R> void GfKernels<R>::init_visc(const GfLaunch &g) {
 template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarkers) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float))
-        GF_LAUNCH(k_phase_markers32, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
+        GF_LAUNCH(k_phase_markers32, (GF_IDX)nmarkers, g.P, g.A, g.d, nmarkers);
     else
-        GF_LAUNCH(k_phase_markers, (long long)nmarkers, g.P, g.A, g.d, nmarkers);
+        GF_LAUNCH(k_phase_markers, (GF_IDX)nmarkers, g.P, g.A, g.d, nmarkers);
     GF_LAUNCH(k_phase_recount<R>, g.d.E, g.P, g.C, g.A, g.d, 0);
 }
 
 namespace {
 namespace gfk {
-__global__ void k_split(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, long long n) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_split(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, GF_IDX n) {
+    GF_IDX t = (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const double v = src[t];
     const float h = (float)v;
@@ -1999,7 +1999,7 @@ void GfKernels<R>::convert_in(const GfLaunch &g, unsigned mask, const double *sr
 namespace {
 namespace gfk {
 // total stress -> (p_ref, total + p_ref on the normal components)
-template <class R> __device__ __forceinline__ void b_k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d, long long e) {
+template <class R> __device__ __forceinline__ void b_k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
     double s = 0.0;
 #pragma unroll
@@ -2012,10 +2012,10 @@ template <class R> __device__ __forceinline__ void b_k_stress_in(const double *_
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = R(c == 2 ? tot[gf_s(d, e, c, k)] : tot[gf_s(d, e, c, k)] + p);
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d) {
-    b_k_stress_in<R>(tot, st, p_ref, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_stress_in<R>(tot, st, p_ref, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-template <class R> __device__ __forceinline__ void b_k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d, long long e) {
+template <class R> __device__ __forceinline__ void b_k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
     double p = p_ref[e];
 #pragma unroll
@@ -2027,7 +2027,7 @@ template <class R> __device__ __forceinline__ void b_k_stress_out(const R *__res
         }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d) {
-    b_k_stress_out<R>(st, p_ref, tot, d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    b_k_stress_out<R>(st, p_ref, tot, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 } // namespace gfk
 } // namespace

@@ -243,7 +243,9 @@ int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L);
  * GF_MODE_MIXED.  Allocates all device storage; nothing is copied yet.
  * GF_ERR_UNSUPPORTED: applied stress boundary conditions (nystressbc = 1),
  * and, in GF_MODE_MIXED, the magma sub-model (itype_melting = 1) and the
- * flexural bottom (nbc 200 on side 2). */
+ * flexural bottom (nbc 200 on side 2).  GF_ERR_LIMIT: in GF_MODE_MIXED,
+ * meshes of 32 * nx * nz >= 2^31 (67 M nodes; its kernels index with 32-bit
+ * integers). */
 int gf_create(gf_ctx **ctx, const gf_params *p, const gf_layout *L, int mode);
 void gf_destroy(gf_ctx *ctx);
 int gf_upload(gf_ctx *ctx, unsigned field_mask);
