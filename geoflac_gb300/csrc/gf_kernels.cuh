@@ -109,6 +109,25 @@ __device__ __forceinline__ double gf_f2d(float f) {
     const unsigned hi = sign | (ed << 20) | (m >> 3);
     return __longlong_as_double((long long)(((unsigned long long)hi << 32) | ((unsigned long long)(m & 7u) << 29)));
 }
+// a / b correctly rounded (the bits of an IEEE division) from y = RN(1/b),
+// for quotients that share a denominator: one IEEE division gives y, each
+// quotient then costs a multiply and four FMAs on the FP64 pipe instead of a
+// division.  q0 = RN(a y) is within 1.5 ulp of a/b; one residual correction
+// (the residual a - b q is exact with an FMA when q is faithful) makes it
+// faithful; the second gives RN(a/b) by Markstein's theorem (a faithful
+// quotient and the correctly rounded reciprocal; P. Markstein, IBM J. Res.
+// Dev. 34 (1990) 111-119).  A zero quotient takes the sign of a * y, as IEEE
+// division's.  Normal b (|b| between 1e-300 and 1e300) only; the callers
+// divide otherwise.  Checked in exact arithmetic by tests/test_division.py.
+__device__ __forceinline__ double div_shared(double a, double b, double y) {
+    double q = a * y;
+    double r = fma(-q, b, a);
+    q = fma(r, y, q);
+    r = fma(-q, b, a);
+    q = fma(r, y, q);
+    return q == 0.0 ? a * y : q;
+}
+
 // x = hi + lo with hi = float(x): the hi/lo split of the mixed path
 __device__ __forceinline__ void gf_split(double x, float &h, float &l) {
     h = gf_d2f(x);

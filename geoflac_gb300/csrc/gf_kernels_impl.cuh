@@ -335,19 +335,25 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
                 qsum = qsum + 0.25f * qk;
             }
         } else {
+            // the 32 quotients by 2 mu (fl_rheol.f90:352-362) share one
+            // reciprocal; div_shared gives each the bits of the division
+            const R two_mu = R(2.0) * mu;
+            const bool shared = fabs(two_mu) > 1e-300 && fabs(two_mu) < 1e300;
+            const R y2mu = R(1.0) / two_mu;
+            auto by2mu = [&](R a) { return shared ? div_shared(a, two_mu, y2mu) : a / two_mu; };
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
                 R tr0 = s0v[0][k] + s0v[1][k] + s0v[3][k];
-                R e11a = (s0v[0][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-                R e22a = (s0v[1][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-                R e33a = (s0v[3][k] - (lambda / den_el) * tr0) / (R(2.0) * mu);
-                R e12a = s0v[2][k] / (R(2.0) * mu);
+                R e11a = by2mu(s0v[0][k] - (lambda / den_el) * tr0);
+                R e22a = by2mu(s0v[1][k] - (lambda / den_el) * tr0);
+                R e33a = by2mu(s0v[3][k] - (lambda / den_el) * tr0);
+                R e12a = by2mu(s0v[2][k]);
                 R tr1 = f11 + f22 + f33;
-                R e11b = (f11 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-                R e22b = (f22 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-                R e33b = (f33 - (lambda / den_el) * tr1) / (R(2.0) * mu);
-                R e12b = f12 / (R(2.0) * mu);
+                R e11b = by2mu(f11 - (lambda / den_el) * tr1);
+                R e22b = by2mu(f22 - (lambda / den_el) * tr1);
+                R e33b = by2mu(f33 - (lambda / den_el) * tr1);
+                R e12b = by2mu(f12);
                 R d11 = sr[0][k] * dt - (e11b - e11a);
                 R d22 = sr[1][k] * dt - (e22b - e22a);
                 R d12 = sr[2][k] * dt - (e12b - e12a);
