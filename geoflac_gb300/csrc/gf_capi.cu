@@ -144,6 +144,12 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.f_alfa[k] = (float)p.alfa[k];
         P.f_beta[k] = (float)p.beta[k];
         P.diffu[k] = (p.den[k] != 0.0 && p.cp[k] != 0.0) ? p.conduct[k] / p.den[k] / p.cp[k] : 0.0;
+        // the device's per-element expressions, evaluated once per phase
+        // (same IEEE operations; host code is built without contraction)
+        P.bulkm[k] = p.rl[k] + 2.0 * p.rm[k] / 3.0;
+        P.hsoft[k] = (p.plstrain2[k] != p.plstrain1[k])
+                         ? (p.cohesion2[k] - p.cohesion1[k]) / (p.plstrain2[k] - p.plstrain1[k])
+                         : 0.0;
     }
     P.f_fmagma_max = (float)p.fmagma_max;
     P.topo_kappa = p.topo_kappa;
@@ -336,7 +342,7 @@ void k_therm(gf_ctx *c) {
         GfKernels<float>::therm(g, c->sweeps);
     } else if (c->p.itype_melting == 1) {
         // temp0 = temp, then the magma sub-model changes temp before the
-        // diffusion (fl_therm.f90:46-391)
+        // diffusion (fl_therm.f90:53-391)
         cudaMemcpyAsync(c->A.temp0, c->A.temp, sizeof(double) * c->d.N, cudaMemcpyDeviceToDevice, c->s);
         GfMagma::therm(g, (int)c->L.max_markers);
         GfKernels<double>::therm(g, c->sweeps, 1);
@@ -405,7 +411,7 @@ void k_change_phase(gf_ctx *c) {
 }
 
 // The launch sequence of one `flac` call depends only on these flags.
-// mesh1 zone patterns of the x and z directions (init_cord.f90:289-327),
+// mesh1 zone patterns of the x and z directions (init_cord.f90:141-179),
 // computed on the host exactly as the start-up mesh and kept on the device
 int mesh_templates(gf_ctx *c) {
     const gf_params &p = c->p;

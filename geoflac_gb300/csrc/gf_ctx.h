@@ -35,7 +35,9 @@ struct DevParams {
         f_vactiv[GF_MAXPH];
     float f_ten_off, f_demf, f_g, f_tau_heal;
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
-    double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:108)
+    double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:130)
+    double bulkm[GF_MAXPH]; // rl + 2 rm / 3 (fl_rheol.f90:192)
+    double hsoft[GF_MAXPH]; // (cohesion2 - cohesion1) / (plstrain2 - plstrain1) (rh_plastic.f90:264)
     double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)
     // magma sub-model (itype_melting = 1)
     double prod_magma, prod_magma2, angle_mzone, ratio_mantle_mzone, ratio_crust_mzone, latent_heat_magma,
@@ -99,7 +101,7 @@ struct DevArrays {
     // corner c (0..3) the force of the element's stresses less its own
     // triangle-1 stress (x, z) and the geometric sums G (x, z)
     float *e_frc;
-    // FP64: each element's terms of fl_node's force sum (fl_node.f90:14-48),
+    // FP64: each element's terms of fl_node's force sum (fl_node.f90:50-254),
     // written by fl_rheol from the new stresses: for corner c and the k-th
     // of its three triangles, fx at [(6c + 2k) E + e], fy at [(6c + 2k + 1) E + e]
     double *n_frc;
@@ -158,7 +160,7 @@ template <class R> struct GfKernels {
     // mixed: total stress (FP64 staging) <-> stored deviations from -p_ref
     static void stress_in(const GfLaunch &g, const double *src);
     static void stress_out(const GfLaunch &g, double *dst);
-    // count_phase_ratio of every element (marker2elem.f90:49)
+    // count_phase_ratio of every element (marker2elem.f90:58)
     static void phase_recount_all(const GfLaunch &g);
     // refresh the hi/lo splits after the FP64 coordinates / velocities changed
     static void split_nodes(const GfLaunch &g);
@@ -168,7 +170,7 @@ template <class R> struct GfKernels {
 struct GfRemeshArgs {
     int mode_rem, is_flex, has_dhacc;
     double x0, z0, rxbo, rzbo;
-    double ar_x, ar_z; // mesh1 zone-pattern totals (init_cord.f90:289-327)
+    double ar_x, ar_z; // mesh1 zone-pattern totals (init_cord.f90:141-179)
     int incoming_left, incoming_right;
     int nl_left, nl_right; // nph_layer of the first / last age zone
     double hc_left[GF_MAXZONE_LAYER], hc_right[GF_MAXZONE_LAYER];

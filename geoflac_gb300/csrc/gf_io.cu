@@ -133,7 +133,7 @@ __global__ void k_frame_line(const DevParams *__restrict__ Pp, DevArrays A, GfDi
     f.lf[LF_EXTR * nx + i] = A.extrusion ? (float)A.extrusion[i] : 0.0f;
 }
 
-// marker positions (marker2xy, bar2euler.f90:86-120) and the output records
+// marker positions (marker2xy, bar2euler.f90:73-117) and the output records
 __global__ void k_frame_markers(DevArrays A, GfDims d, int nmarkers, float *fo, int *io) {
     long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmarkers) return;
@@ -449,7 +449,7 @@ int gf_saveflac(gf_ctx *ctx, const char *dir) {
     IO_CK(w8("mor_marker_vol.rs", L.mor_marker_vol, E));
     std::snprintf(line, sizeof line, " %.17E\n", p.Amin);
     IO_CK(append_line(dir, "Amin.rs", 1, line));
-    if (p.nyhydro == 2) { // read back by rsflac.f90:189-193
+    if (p.nyhydro == 2) { // read back by rsflac.f90:219-225
         std::snprintf(line, sizeof line, " %.17E\n", p.pisos);
         IO_CK(append_line(dir, "pisos.rs", 1, line));
     }
@@ -537,7 +537,7 @@ int gf_rsflac(gf_ctx *ctx, const char *dir) {
         std::fclose(f);
         if (got != 1) return GF_ERR_PARSE;
     }
-    // smallest element width and thickness (rsflac.f90:33-35)
+    // smallest element width and thickness (rsflac.f90:38-39)
     double dxmin = 1e300, dzmin = 1e300;
     for (long long i = 1; i < nx; ++i) dxmin = std::fmin(dxmin, L.cord[i * nz] - L.cord[(i - 1) * nz]);
     for (long long j = 0; j < nz - 1; ++j) dzmin = std::fmin(dzmin, L.cord[N + j] - L.cord[N + j + 1]);

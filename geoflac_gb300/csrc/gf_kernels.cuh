@@ -109,23 +109,46 @@ __device__ __forceinline__ double gf_f2d(float f) {
     const unsigned hi = sign | (ed << 20) | (m >> 3);
     return __longlong_as_double((long long)(((unsigned long long)hi << 32) | ((unsigned long long)(m & 7u) << 29)));
 }
-// a / b correctly rounded (the bits of an IEEE division) from y = RN(1/b),
-// for quotients that share a denominator: one IEEE division gives y, each
-// quotient then costs a multiply and four FMAs on the FP64 pipe instead of a
-// division.  q0 = RN(a y) is within 1.5 ulp of a/b; one residual correction
-// (the residual a - b q is exact with an FMA when q is faithful) makes it
-// faithful; the second gives RN(a/b) by Markstein's theorem (a faithful
-// quotient and the correctly rounded reciprocal; P. Markstein, IBM J. Res.
-// Dev. 34 (1990) 111-119).  A zero quotient takes the sign of a * y, as IEEE
-// division's.  Normal b (|b| between 1e-300 and 1e300) only; the callers
-// divide otherwise.  Checked in exact arithmetic by tests/test_division.py.
-__device__ __forceinline__ double div_shared(double a, double b, double y) {
-    double q = a * y;
-    double r = fma(-q, b, a);
-    q = fma(r, y, q);
-    r = fma(-q, b, a);
-    q = fma(r, y, q);
-    return q == 0.0 ? a * y : q;
+// Biased exponent field and zero test of a double, on the integer pipe (an
+// FP64 compare takes a slot of the FP64 pipe).
+__device__ __forceinline__ unsigned gf_dexp(double x) { return ((unsigned)__double2hiint(x) >> 20) & 0x7ffu; }
+__device__ __forceinline__ bool gf_dzero(double x) {
+    return (((unsigned)__double2hiint(x) & 0x7fffffffu) | (unsigned)__double2loint(x)) == 0u;
+}
+// |x| in [2^-450, 2^451) (biased exponents 573 .. 1473): quotients and the
+// products below of two such numbers are normal doubles
+__device__ __forceinline__ bool gf_dmid(double x) { return gf_dexp(x) - 573u <= 900u; }
+
+// Division by a shared denominator with the bits of IEEE division.  For a
+// denominator b: y = RN(1/b) (one IEEE division) and yl = RN(RN(1 - b y) y),
+// so that y + yl is 1/b to 2^-105 relative (1 - b y is exact in an FMA).
+// Each quotient a / b then costs one multiply and three FMAs:
+//   q = RN(a y + RN(a yl))   within 0.5 ulp + 2^-104 |a/b|: faithful,
+//   r = a - b q              exact in an FMA because q is faithful,
+//   RN(q + r y)              = RN(a/b) by Markstein's theorem (a faithful
+//                            quotient and the correctly rounded reciprocal;
+//                            P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119).
+// Operands outside gf_dmid take an IEEE division; a zero numerator gives
+// a * y, the signed zero of IEEE division.  Restated in exact arithmetic and
+// checked against IEEE division (random and near-midpoint quotients) by
+// tests/test_division.py.
+struct GfRecip {
+    double b, y, yl;
+    bool ok;
+};
+__device__ __forceinline__ GfRecip gf_recip_y(double b, double y) { // y = 1.0 / b
+    GfRecip r;
+    r.b = b;
+    r.y = y;
+    r.yl = fma(-y, b, 1.0) * y;
+    r.ok = gf_dmid(b);
+    return r;
+}
+__device__ __forceinline__ GfRecip gf_recip(double b) { return gf_recip_y(b, 1.0 / b); }
+__device__ __forceinline__ double gf_div(double a, const GfRecip &r) {
+    if (!(r.ok && gf_dmid(a))) return (r.ok && gf_dzero(a)) ? a * r.y : a / r.b;
+    const double q = fma(a, r.y, a * r.yl);
+    return fma(fma(-q, r.b, a), r.y, q);
 }
 
 // x = hi + lo with hi = float(x): the hi/lo split of the mixed path
@@ -444,17 +467,30 @@ __device__ __forceinline__ void elastic(R bulkm, R rmu, R &s11, R &s22, R &s33, 
     s33 = s33 + a2 * (de11 + de22);
 }
 
-// maxwell (rh_maxwell.f90:34-108).  Returns false where the reference stops
-// with code 22.
+// The per-element factors of maxwell (rh_maxwell.f90:17-33): the reference
+// evaluates them per triangle from the same element values.  ok is false
+// where the reference stops with code 22.
+template <class R> struct MaxwellConsts {
+    R rmu, vic1, vic2;
+    bool ok;
+};
+template <class R> __device__ __forceinline__ MaxwellConsts<R> maxwell_consts(R rmu0, R viscosity, R dt) {
+    const R visc_cut = R(1e19);
+    MaxwellConsts<R> m;
+    m.rmu = viscosity < visc_cut ? rmu0 * viscosity / visc_cut : rmu0;
+    R temp = m.rmu / (R(2) * viscosity) * dt;
+    m.ok = !(temp > R(0.5));
+    m.vic1 = R(1) - temp;
+    m.vic2 = R(1.0) / (R(1.0) + temp);
+    return m;
+}
+
+// maxwell (rh_maxwell.f90:2-76) of one triangle
 template <class R>
-__device__ __forceinline__ bool maxwell(R bulkm, R rmu0, R viscosity, R &s11, R &s22, R &s33, R &s12, R de11, R de22,
-                                        R de33, R de12, R dv, int ndim, R dt) {
-    const R c1d3 = R(1.0 / 3.0), visc_cut = R(1e19);
-    R rmu = viscosity < visc_cut ? rmu0 * viscosity / visc_cut : rmu0;
-    R temp = rmu / (R(2) * viscosity) * dt;
-    bool ok = !(temp > R(0.5));
-    R vic1 = R(1) - temp;
-    R vic2 = R(1.0) / (R(1.0) + temp);
+__device__ __forceinline__ void maxwell(R bulkm, const MaxwellConsts<R> &m, R &s11, R &s22, R &s33, R &s12, R de11,
+                                        R de22, R de33, R de12, R dv, int ndim) {
+    const R c1d3 = R(1.0 / 3.0);
+    const R rmu = m.rmu, vic1 = m.vic1, vic2 = m.vic2;
     R dev, de11d, de22d, de33d, s0, s11d, s22d, s33d;
     if (ndim == 2) {
         dev = de11 + de22;
@@ -483,10 +519,9 @@ __device__ __forceinline__ bool maxwell(R bulkm, R rmu0, R viscosity, R &s11, R 
     s11 = s11d + s0;
     s22 = s22d + s0;
     s33 = s33d + s0;
-    return ok;
 }
 
-// Per-element constants of the plastic return map (rh_plastic.f90:141-154).
+// Per-element constants of the plastic return map (rh_plastic.f90:33-46).
 // The reference evaluates them once per triangle with identical inputs; they
 // are evaluated once per element here (same values, a quarter of the
 // transcendental work).
@@ -510,7 +545,7 @@ __device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh
     return c;
 }
 
-// plastic (rh_plastic.f90:111-332), 2-D branch (icase = 1).
+// plastic (rh_plastic.f90:3-229), 2-D branch (icase = 1).
 template <class R>
 __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &depls, R hardn, R &s11, R &s22, R &s33,
                                         R &s12, R de11, R de22, R de33, R de12) {
@@ -631,7 +666,7 @@ __device__ __forceinline__ void plastic_sel(const PlasticConsts<float> &c, float
     plastic_dev(c, rmu, depls, hardn, s11, s22, s33, s12, de11, de22, de33, de12, pref, mod);
 }
 
-// fl_rheol.f90:281-296 keeps the Maxwell stress unless the plastic one has
+// fl_rheol.f90:266-288 keeps the Maxwell stress unless the plastic one has
 // the smaller second invariant.  When no triangle left its elastic trial
 // stress, the two differ by the Maxwell relaxation alone, O(dt/tau) ~ 1e-8
 // of the invariant for stiff lithosphere: below FP32 resolution, so the
@@ -654,7 +689,7 @@ __device__ __forceinline__ bool maxwell_wins_unyielded(float sp_a, float sp_b, f
     return 2.0f * W + V - Q * t * (2.0f + t) <= 0.0f;
 }
 
-// pre_plast (rh_plastic.f90:339-399)
+// pre_plast (rh_plastic.f90:231-291)
 template <class R>
 __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
                                           R aps_e, R &coh, R &phi, R &psi, R &hardn) {
@@ -682,7 +717,10 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
             f = f1 + (f2 - f1) * dpl;
             dd = d1 + (d2 - d1) * dpl;
             c = c1 + (c2 - c1) * dpl;
-            h = (c2 - c1) / (pl2 - pl1);
+            if constexpr (sizeof(R) == sizeof(float))
+                h = (c2 - c1) / (pl2 - pl1);
+            else
+                h = R(P.hsoft[k]);
         } else {
             f = f2; c = c2; dd = d2; h = 0;
         }

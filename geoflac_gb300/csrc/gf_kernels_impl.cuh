@@ -149,12 +149,12 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         bulkm = P.f_bulkm[iph];
         rmu = P.f_rm[iph];
     } else {
-        bulkm = R(P.rl[iph] + 2.0 * P.rm[iph] / 3.0);
+        bulkm = R(P.bulkm[iph]);
         rmu = R(P.rm[iph]);
     }
     R stherm = R(0.0);
     if (P.istress_therm > 0)
-        stherm = R(-P.alfa[iph] * (P.rl[iph] + 2.0 * P.rm[iph] / 3.0) * (A.temp[n1] - A.temp0[n1]));
+        stherm = R(-P.alfa[iph] * P.bulkm[iph] * (A.temp[n1] - A.temp0[n1]));
     R *aps = (R *)A.aps;
     R aps_e = aps[e];
     // mixed path: stored normal stresses are deviations from -pref
@@ -176,7 +176,10 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     R dike = A.dike_released ? gf_to<R>(A.dike_released[e]) : R(0);
     const R *dvol = (const R *)A.dvol;
     R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
-    bool ok = true, plas_mod = false;
+    bool plas_mod = false;
+    MaxwellConsts<R> mc;
+    if (irh == 3 || irh >= 11) mc = maxwell_consts<R>(rmu, vis, dt);
+    const bool ok = !(irh == 3 || irh >= 11) || mc.ok;
     R sumD = 0, sumD12 = 0; // strain-increment sums for the FP32 selection
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -190,7 +193,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         if (irh == 1) {
             elastic<R>(bulkm, rmu, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de12);
         } else if (irh == 3) {
-            ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
+            maxwell<R>(bulkm, mc, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim);
         } else if (irh == 6) {
             bool m;
             plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref,
@@ -200,7 +203,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
             plastic_sel(pc, rmu, depl[k], hardn, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de33, de12, pref,
                         m);
             plas_mod = plas_mod || m;
-            ok &= maxwell<R>(bulkm, rmu, vis, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim, dt);
+            maxwell<R>(bulkm, mc, sv[0][k], sv[1][k], sv[3][k], sv[2][k], de11, de22, de33, de12, dv, P.ndim);
             if (sizeof(R) == sizeof(float)) {
                 sumD = sumD + (de11 - de22);
                 sumD12 = sumD12 + de12;
@@ -231,14 +234,30 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int c = 0; c < 4; ++c) sn[c][k] = use_visc ? sv[c][k] : sp[c][k];
+    // FP64: the reciprocals 1/ar of the stress mixing and the node-force
+    // factors 0.25/ar, one IEEE division per triangle
+    R rar[4];
+    if constexpr (sizeof(R) == sizeof(double)) {
+        if (P.mix_stress == 1 || A.n_frc) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) rar[t] = R(1.0) / ar[t];
+        }
+    }
     if (P.mix_stress == 1) {
 #pragma unroll
         for (int h = 0; h < 4; h += 2) {
             R ra = ar[h], rb = ar[h + 1];
-            R quad_area = R(1.0) / ra + R(1.0) / rb;
             R s0a = R(0.5) * (sn[0][h] + sn[1][h]);
             R s0b = R(0.5) * (sn[0][h + 1] + sn[1][h + 1]);
-            R s0 = (s0a / rb + s0b / ra) / quad_area;
+            R s0;
+            if constexpr (sizeof(R) == sizeof(double)) {
+                const GfRecip qa = gf_recip_y(ra, rar[h]), qb = gf_recip_y(rb, rar[h + 1]);
+                R quad_area = qa.y + qb.y;
+                s0 = (gf_div(s0a, qb) + gf_div(s0b, qa)) / quad_area;
+            } else {
+                R quad_area = R(1.0) / ra + R(1.0) / rb;
+                s0 = (s0a / rb + s0b / ra) / quad_area;
+            }
             sn[0][h] = sn[0][h] - s0a + s0;
             sn[1][h] = sn[1][h] - s0a + s0;
             sn[0][h + 1] = sn[0][h + 1] - s0b + s0;
@@ -256,7 +275,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 #pragma unroll
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = sn[c][k];
     if constexpr (sizeof(R) == sizeof(double)) {
-        // fl_node's force terms of this element (fl_node.f90:14-48), each
+        // fl_node's force terms of this element (fl_node.f90:50-254), each
         // the expression the node gather evaluates, from the stresses just
         // stored: the node kernel then sums them in the reference's order
         // instead of recomputing four elements' shape derivatives and twelve
@@ -271,7 +290,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int t = kk[qd][k], m = mm[qd][k];
-                    R factor = R(0.25) / ar[t];
+                    // 0.25 * RN(1/ar) == RN(0.25/ar) while both are normal
+                    R factor = gf_dmid(ar[t]) ? R(0.25) * rar[t] : R(0.25) / ar[t];
                     R fx = factor * (sn[0][t] * dx[m][t] + sn[2][t] * dz[m][t]);
                     R fy = factor * (sn[2][t] * dx[m][t] + sn[1][t] * dz[m][t]);
                     nf[(GF_IDX)(6 * c + 2 * k) * d.E + e] = fx;
@@ -336,11 +356,9 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
             }
         } else {
             // the 32 quotients by 2 mu (fl_rheol.f90:352-362) share one
-            // reciprocal; div_shared gives each the bits of the division
-            const R two_mu = R(2.0) * mu;
-            const bool shared = fabs(two_mu) > 1e-300 && fabs(two_mu) < 1e300;
-            const R y2mu = R(1.0) / two_mu;
-            auto by2mu = [&](R a) { return shared ? div_shared(a, two_mu, y2mu) : a / two_mu; };
+            // reciprocal; gf_div gives each the bits of the division
+            const GfRecip r2mu = gf_recip(R(2.0) * mu);
+            auto by2mu = [&](R a) { return gf_div(a, r2mu); };
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
@@ -973,7 +991,7 @@ __device__ bool gf_grid_barrier(unsigned *bar, GF_IDX limit) {
 // The FP64 thermal update after k_therm_prep, in one co-resident launch:
 // sweeps until one changes nothing (at most kmax; grid barrier between
 // sweeps, every CTA reads the same flag after it), then the boundary
-// conditions and temp0 = temp (fl_therm.f90:46-48, 573-598) from the last
+// conditions and temp0 = temp (fl_therm.f90:53, 577-598) from the last
 // sweep's buffer.  Node n is always handled by the same thread.
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__restrict__ Pp, DevClock *__restrict__ C,
                                                             DevArrays A, GfDims d, const double *__restrict__ tc,
@@ -1128,7 +1146,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *_
 }
 
 // ======================================================================
-// rmasses (rmasses.f90:236-295): per-element density, then a node gather in
+// rmasses (rmasses.f90:4-63): per-element density, then a node gather in
 // the reference's colour order with each element's triangles in order.
 template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, GF_IDX e) {
     if (e >= d.E) return;
@@ -1148,7 +1166,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams
         double fval = 0.0;
         double dens = eff_dens<R>(*Pp, A, d, j, i, e, &wrote, &fval);
         A.e_dens[e] = dens;
-        // each triangle's share c1d12/area*dens (rmasses.f90:271-287),
+        // each triangle's share c1d12/area*dens (rmasses.f90:35-57),
         // computed once here with the reference's operations and gathered
         // per node
         const double c1d12 = 1.0 / 12.0;
@@ -1202,7 +1220,7 @@ template <class R> __global__ void k_frac_fix(const DevParams *__restrict__ Pp, 
 __device__ __constant__ int c_vtx_tris[4][3] = {{0, 2, 3}, {0, 1, 2}, {0, 1, 3}, {1, 2, 3}};
 
 // Node gather of per-triangle shares tri[k*E + e] in the reference's order:
-// adjacent elements by colour ((ie&1)*2 + (je&1), rmasses.f90:257-262,
+// adjacent elements by colour ((ie&1)*2 + (je&1), rmasses.f90:25-30,
 // dt_mass.f90:74-81), then each element's triangles containing the node in
 // the order A, B, C, D.  Every element in a node's neighbourhood has a
 // different colour, so this is the serial order of the coloured scatter.
@@ -1267,7 +1285,7 @@ __device__ __forceinline__ void dt_block_commit(DevClock *__restrict__ C, double
             c = max(c, s_d[k]);
             m |= s_pm[k];
         }
-        if (diffu) { // the largest diffusivity of the phases present (dt_mass.f90:108)
+        if (diffu) { // the largest diffusivity of the phases present (dt_mass.f90:130)
             double dm = 0.0;
             for (int k = 0; k < nphase; ++k)
                 if (m & (1u << k)) dm = fmax(dm, diffu[k]);

@@ -946,7 +946,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_mor_cols(const DevParams *__rest
     }
     if (lane == 0) A.mg_c[i] = dt * total_melt * P.prod_magma2 / (CX(A.cord, d, 0, i + 1) - CX(A.cord, d, 0, i));
 }
-// newphase2marker (remesh.f90:495-520) on rows j1..j2, columns i1..i2 (1-based)
+// newphase2marker (marker_data.f90:107-137) on rows j1..j2, columns i1..i2 (1-based)
 __device__ void mg_newphase(DevArrays &A, const GfDims &d, int j1, int j2, int i1, int i2, int iph) {
     const long long total = (long long)d.nphase * d.E;
     for (int i = i1; i <= i2; ++i)

@@ -20,7 +20,7 @@ __device__ __forceinline__ double CY(const double *cord, const GfDims &d, int j,
     return cord[d.N + gf_node(d, j, i)];
 }
 
-// check_inside (src/marker2elem.f90 helper, src/bar2euler.f90:126-175): the
+// check_inside (src/euler2bar.f90:102-161): the
 // two triangles of element (j,i); bar1/bar2 and the 1-based triangle number
 __device__ bool check_inside(const double *cord, const GfDims &d, double x, double y, double &bar1, double &bar2,
                              int &ntr, int i, int j) {
@@ -47,7 +47,7 @@ __device__ bool check_inside(const double *cord, const GfDims &d, double x, doub
 }
 
 // ---------------------------------------------------------------- bar2euler
-// marker2xy (src/bar2euler.f90:86-120): barycentric -> (x, y) in mark_a1/a2
+// marker2xy (src/bar2euler.f90:73-117): barycentric -> (x, y) in mark_a1/a2
 __global__ void __launch_bounds__(GF_THREADS) k_bar2euler(DevArrays A, GfDims d, int nmarkers, int has_dhacc) {
     long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmarkers || A.mark_dead[m] == 0) return;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_bar2euler(DevArrays A, GfDims d,
 }
 
 // ---------------------------------------------------------------- rem_cord
-// New x of every node (rem_cord.f90:140-170): mesh1 between the row's ends
+// New x of every node (rem_cord.f90:10-33): mesh1 between the row's ends
 __global__ void __launch_bounds__(GF_THREADS) k_regrid_x(DevArrays A, GfDims d, GfRemeshArgs a, const double *tx) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.N) return;
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_regrid_x(DevArrays A, GfDims d, 
     A.cord[gf_node(d, j, i)] = xl + tx[i] * ((xr - xl) / a.ar_x);
 }
 
-// New z (rem_cord.f90:172-220): surface and bottom by linear interpolation
+// New z (rem_cord.f90:34-79): surface and bottom by linear interpolation
 // of the old rows at the new x, then mesh1 down each column.  One thread per column.
 __global__ void __launch_bounds__(GF_THREADS) k_regrid_z(DevArrays A, GfDims d, GfRemeshArgs a, const double *tz) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -164,7 +164,7 @@ struct PtGrid {
     __device__ double Y(int j, int i) const { return xy[P + (long long)i * nzt + j]; }
 };
 
-// rem_trpars (remesh.f90:266-301): 6 coefficients per old triangle
+// rem_trpars (remesh.f90:267-320): 6 coefficients per old triangle
 __global__ void __launch_bounds__(GF_THREADS) k_trpars(PtGrid g, double *pt) {
     long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long ntri = 2LL * (g.nzt - 1) * (g.nxt - 1);
@@ -195,7 +195,7 @@ __device__ __forceinline__ void weights2(double da, double db, double &wa, doubl
     wb = 1.0 / db / (1.0 / da + 1.0 / db);
 }
 
-// rem_barcord (remesh.f90:305-452): containing old triangle of each new
+// rem_barcord (remesh.f90:327-439): containing old triangle of each new
 // point within +-4 cells, in the reference's search order; else the two
 // nearest vertices of the triangle with the smallest sum of squared weights
 __global__ void __launch_bounds__(GF_THREADS) k_barcord(PtGrid old, const double *cnew, const double *pt, int *numtr,
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_barcord(PtGrid old, const double
     bc[2 * old.P + p] = b2;
 }
 
-// rem_interpolate (remesh.f90:456-491): new value of one field plane from
+// rem_interpolate (remesh.f90:445-491): new value of one field plane from
 // the copy `src` of its old values; clamp0 applies remesh.f90:117-126 (aps >= 0)
 template <class T>
 __global__ void __launch_bounds__(GF_THREADS) k_interp(const T *__restrict__ src, T *__restrict__ dst, int nzt,
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(GF_THREADS) k_incoming(DevClock *C, DevArrays 
         for (int t = threadIdx.x; t < ncol * (nz - 1); t += blockDim.x)
             aps[gf_elem(d, t % (nz - 1), i1 - 1 + t / (nz - 1))] = R(0.0);
         for (int r = 0; r < r_n[side]; ++r) {
-            // newphase2marker (remesh.f90:495-520) on rows j1..j2 (1-based)
+            // newphase2marker (marker_data.f90:107-137) on rows j1..j2 (1-based)
             int j1 = r_j1[side][r], j2 = r_j2[side][r], iph = r_ph[side][r];
             int nj = j2 - j1 + 1;
             if (nj <= 0) continue;
@@ -417,7 +417,7 @@ __device__ bool euler2bar(const double *cord, const GfDims &d, double x, double 
     return false;
 }
 
-// lpeuler2bar (lpeuler2bar.f90:343-404), step 1: locate each live marker
+// lpeuler2bar (lpeuler2bar.f90:1-62), step 1: locate each live marker
 __global__ void __launch_bounds__(GF_THREADS) k_lp_locate(DevArrays A, GfDims d, int nmarkers, int *m_elem,
                                                           int *e_count) {
     long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, long lon
     }
 }
 
-// jmoho (marker2elem.f90:53-62): first row whose mantle phases exceed 1/2,
+// jmoho (marker2elem.f90:66-77): first row whose mantle phases exceed 1/2,
 // with the reference's flat-memory reads for phase ids above nphase
 __global__ void k_jmoho(DevArrays A, GfDims d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;

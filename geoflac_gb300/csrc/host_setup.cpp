@@ -43,7 +43,7 @@ double ipow(double x, int m) {
     return m < 0 ? 1.0 / y : y;
 }
 
-// mesh1 (src/init_cord.f90:289-327): 1-D zoned mesh between x1 and x2.
+// mesh1 (src/init_cord.f90:141-179): 1-D zoned mesh between x1 and x2.
 void mesh1(double x1, double x2, double *xmesh, int n, int nzon, const int *nelz, const double *sizez) {
     double all_ratio = 0.0;
     int nel = 0;
@@ -70,7 +70,7 @@ void mesh1(double x1, double x2, double *xmesh, int n, int nzon, const int *nelz
     for (int k = 0; k < n; ++k) xmesh[k] = x1 + xmesh[k] * magnification;
 }
 
-// init_cord (src/init_cord.f90:153-238) and test_grid (:245-283).
+// init_cord (src/init_cord.f90:5-89) and test_grid (:97-134).
 void init_cord(S &s) {
     gf_params &p = *s.p;
     int nx = p.nx, nz = p.nz;
@@ -105,7 +105,7 @@ void init_cord(S &s) {
         mesh1(p.z0, p.z0 + p.rzbo, rmesh.data(), nz, p.nzony, p.nelz_y, p.sizez_y);
         for (int j = 0; j < nz; ++j)
             for (int i = 0; i < nx; ++i) s.cord(j, i, 1) = rmesh[j];
-        // topography perturbations (init_cord.f90:197-214), 1-based node ranges
+        // topography perturbations (init_cord.f90:49-66), 1-based node ranges
         for (int n = 0; n < p.inhom; ++n) {
             if (p.igeom[n] == 20) {
                 double amp = p.xinitaps[n];
@@ -316,7 +316,7 @@ void newphase2marker(S &s, int j1, int j2, int i1, int i2, int iph) {
         }
 }
 
-// init_marker (src/init_marker.f90:1-236).  With markers_per_side = 3 this is
+// init_marker (src/init_marker.f90:1-164).  With markers_per_side = 3 this is
 // the reference's 9-point pattern; other values place m x m points with the
 // same construction (an extension with no reference counterpart).
 void init_marker(S &s) {
@@ -398,7 +398,7 @@ void init_marker(S &s) {
                 l = l + 1;
             }
         }
-    // initial heterogeneities (init_marker.f90:202-229)
+    // initial heterogeneities (init_marker.f90:131-160)
     for (int n = 0; n < p.inhom; ++n) {
         if (p.inphase[n] < 0) continue;
         if (p.igeom[n] == 0) newphase2marker(s, p.iy1[n], p.iy2[n], p.ix1[n], p.ix2[n], p.inphase[n]);
@@ -421,7 +421,7 @@ void init_marker(S &s) {
     marker2elem(s);
 }
 
-// init_areas (src/init_areas.f90:244-291): area = 1/det (inverse double area).
+// init_areas (src/init_areas.f90:8-55): area = 1/det (inverse double area).
 void init_areas(S &s) {
     int nx = s.p->nx, nz = s.p->nz;
     for (int i = 0; i < nx - 1; ++i)
@@ -615,7 +615,7 @@ void init_temp(S &s) {
     }
 }
 
-// init_stress (src/init_stress.f90:358-413): lithostatic prestress, pisos.
+// init_stress (src/init_stress.f90:5-60): lithostatic prestress, pisos.
 void init_stress(S &s) {
     gf_params &p = *s.p;
     int nx = p.nx, nz = p.nz;
@@ -814,7 +814,7 @@ extern "C" int gf_setflac_host(gf_params *p, gf_clock *c, gf_layout *L) {
 }
 
 // The host part of a restart once the saved fields are in L and marker2elem
-// has refreshed iphase and jmoho (rsflac.f90:117-118,207): check_visc_rheol
+// has refreshed iphase and jmoho (rsflac.f90:109-116,217): check_visc_rheol
 // and init_bc on the restored mesh (the boundary velocities are profiles
 // along the restored side coordinates).
 int gf_host_restart_bc(gf_params *p, gf_layout *L) {
@@ -849,7 +849,7 @@ int gf_host_geotherm_columns(gf_params *p, gf_layout *L, int zone, int i_first, 
 }
 
 // The zone pattern of mesh1 before scaling: x_k = x1 + t[k] * (x2 - x1) / all_ratio
-// (src/init_cord.f90:289-327), so a device can regrid with the host's exact values.
+// (src/init_cord.f90:141-179), so a device can regrid with the host's exact values.
 void gf_host_mesh_template(int n, int nzon, const int *nelz, const double *sizez, double *t, double *all_ratio) {
     double ar = 0.0;
     for (int k = 0; k < nzon - 1; k += 2) {

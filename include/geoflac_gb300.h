@@ -21,7 +21,7 @@
  *
  * Every entry point returns 0 on success, a positive value equal to the
  * reference's `stop` code when the reference would stop (22: Maxwell time
- * step, src/rh_maxwell.f90:58-62; 40: negative area, src/fl_move.f90:110-126;
+ * step, src/rh_maxwell.f90:24-30; 40: negative area, src/fl_move.f90:110-126;
  * 133: marker top-up failed, src/marker2elem.f90:52; 134: no marker in an
  * element, src/marker_data.f90:148), or a negative GF_ERR_* code.
  * No kernel traps: kernels record the first error in a device status word
@@ -148,11 +148,11 @@ typedef struct gf_params {
     double time_max, dtout_screen, dtout_file, dtsave_file;
     int io_flags[19];
     int lastout, lastsave;
-    /* derived at start-up (setflac.f90, init_cord.f90:228-229, init_bc.f90:210,385-409) */
+    /* derived at start-up (setflac.f90, init_cord.f90:80-81, init_bc.f90:385-409) */
     double dxmin, dzmin, vbc, Amin;
     int ivis_present, incoming_left, incoming_right, nopbmax;
     /* options with no .inp counterpart (defaults reproduce the reference) */
-    int markers_per_side; /* 3 => 9 markers per element (init_marker.f90:104-198) */
+    int markers_per_side; /* 3 => 9 markers per element (init_marker.f90:52-91) */
     int eclogite_rule;    /* 0 => Hacker-2003 lines (change_phase.f90:159-170);
                              1 => simple rule: T >= 600 C and P >= 1.5 GPa   */
     int therm_sweeps;     /* cap on the sweeps of the thermal update
@@ -231,7 +231,7 @@ int gf_read_params(const char *path, gf_params *p);
 int gf_layout_sizes(const gf_params *p, size_t *n_node, size_t *n_elem, size_t *max_markers);
 
 /* Host part of setflac (src/setflac.f90:8-66): init_cord, init_phase,
- * init_marker (serial LCG chain, init_marker.f90:104-198) with marker2elem,
+ * init_marker (serial LCG chain, init_marker.f90:52-91) with marker2elem,
  * check_visc_rheol, init_areas, Amin, init_temp, init_stress, init_bc and the
  * field defaults.  rmasses, init_visc and dt_mass (setflac.f90:71-81) run on
  * the device: see gf_finish_setflac(). */
@@ -278,7 +278,7 @@ int gf_fl_node(gf_ctx *ctx);
 /* fl_move (src/fl_move.f90:4-132): coordinate update, areas, dvol and the
  * Jaumann rotation of stress and strain; stop code 40 on a negative area. */
 int gf_fl_move(gf_ctx *ctx);
-/* rmasses (src/rmasses.f90:236-295) as a node gather in colour order. */
+/* rmasses (src/rmasses.f90:4-63) as a node gather in colour order. */
 int gf_rmasses(gf_ctx *ctx);
 /* dt_mass (src/dt_mass.f90:16-232): dlmin, vel_max, amass, dt. */
 int gf_dt_mass(gf_ctx *ctx);

@@ -440,7 +440,7 @@ subroutine init_visc
   call gf_stop_on(rc)
 end subroutine init_visc
 
-! par.f90:97: need_remeshing from the library's mesh-quality test
+! par.f90:94-95: need_remeshing from the library's mesh-quality test
 subroutine itest_mesh(need_remeshing)
   use gf_shim
   integer, intent(out) :: need_remeshing
@@ -454,7 +454,7 @@ subroutine itest_mesh(need_remeshing)
   need_remeshing = gfk%need_remeshing
 end subroutine itest_mesh
 
-! par.f90:100-106: the library's remesh event covers bar2euler, remesh,
+! par.f90:96-107: the library's remesh event covers bar2euler, remesh,
 ! lpeuler2bar, marker2elem and the dhacc_correction reset
 subroutine remesh
   use gf_shim

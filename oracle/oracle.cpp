@@ -351,7 +351,7 @@ void plastic(double bulkm, double rmu, double coh, double phi, double psi, doubl
     }
 }
 
-// pre_plast (rh_plastic.f90:339-399)
+// pre_plast (rh_plastic.f90:231-291)
 void pre_plast(St &s, long long e, double &coh, double &phi, double &psi, double &hardn) {
     const gf_params &p = *s.p;
     double pls_curr = s.L->aps[e];
@@ -1104,7 +1104,7 @@ void fl_move(St &s) {
 }
 
 // --------------------------------------------------------------------------
-// rmasses (src/rmasses.f90:236-295) and dt_mass (src/dt_mass.f90:16-232)
+// rmasses (src/rmasses.f90:4-63) and dt_mass (src/dt_mass.f90:16-232)
 
 void rmasses(St &s) {
     const gf_params &p = *s.p;
@@ -1950,7 +1950,7 @@ double ipow(double x, int m) {
     return m < 0 ? 1.0 / y : y;
 }
 
-// mesh1 (init_cord.f90:289-327)
+// mesh1 (init_cord.f90:141-179)
 void mesh1(double x1, double x2, double *xmesh, int n, int nzon, const int *nelz, const double *sizez) {
     double all_ratio = 0.0;
     int nel = 0;
@@ -2068,7 +2068,7 @@ void geotherm_column(St &s, int n, int i, double age_1n, double tp1n, double tp2
     }
 }
 
-// marker2xy (bar2euler.f90:235-279); bar2euler writes x,y into mark_a1/a2
+// marker2xy (bar2euler.f90:73-117); bar2euler writes x,y into mark_a1/a2
 void bar2euler(St &s) {
     gf_layout &L = *s.L;
     int nz = s.p->nz;
@@ -2122,7 +2122,7 @@ int euler2bar(St &s, double x, double y, double &b1, double &b2, int &ntr, int &
     return 0;
 }
 
-// lpeuler2bar (lpeuler2bar.f90:343-404), serial marker order
+// lpeuler2bar (lpeuler2bar.f90:1-62), serial marker order
 void lpeuler2bar(St &s) {
     gf_layout &L = *s.L;
     int nz = s.p->nz;
@@ -2153,7 +2153,7 @@ void lpeuler2bar(St &s) {
     }
 }
 
-// rem_cord (rem_cord.f90:140-220)
+// rem_cord (rem_cord.f90:1-81)
 void rem_cord(St &s, const std::vector<double> &cordo) {
     const gf_params &p = *s.p;
     int nx = p.nx, nz = p.nz;
@@ -2201,7 +2201,7 @@ void rem_cord(St &s, const std::vector<double> &cordo) {
     }
 }
 
-// rem_trpars / rem_barcord / rem_interpolate (remesh.f90:266-491) on a
+// rem_trpars / rem_barcord / rem_interpolate (remesh.f90:267-491) on a
 // (nzt x nxt) point grid with old points `cold` and new points `cnew`
 struct Interp {
     int nzt, nxt;

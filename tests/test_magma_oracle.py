@@ -31,7 +31,7 @@ def _state(workdir, tag, **kw):
 
 
 def _node_xy(s, n, nz):
-    """marker n's position from its barycentric coordinates (bar2euler.f90:86-120)"""
+    """marker n's position from its barycentric coordinates (bar2euler.f90:73-117)"""
     nt = s["mark_ntriag"][n]
     k = (nt - 1) % 2 + 1
     jj = ((nt - k) // 2) % (nz - 1)

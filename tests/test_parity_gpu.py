@@ -130,7 +130,7 @@ def test_thermal_sweep_cap_reports_unconverged(workdir):
 
 def test_maxwell_stop_code(workdir):
     """A viscosity far below the Maxwell limit makes the reference stop with
-    code 22 (rh_maxwell.f90:58-62); the GPU path returns the same code."""
+    code 22 (rh_maxwell.f90:24-30); the GPU path returns the same code."""
     gpu, orc = _pair(workdir, "extension_60x20")
     gpu.download()
     gpu.state["visn"][...] = 1e10
