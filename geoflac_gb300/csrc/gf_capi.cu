@@ -754,7 +754,10 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
         A_(dalloc(c, &b.d_scalars, 4));
         A_(mesh_templates(c));
     }
-    if (mode == GF_MODE_FP64) A_(dalloc(c, &A.n_frc, 24 * E));
+    if (mode == GF_MODE_FP64) {
+        A_(dalloc(c, &A.n_frc, 24 * E));
+        A_(dalloc(c, &A.plast_tab, GF_PT_STATES * GF_MAXPH * GF_PT_W));
+    }
     if (mode == GF_MODE_MIXED) {
         A_(dalloc(c, &c->staging, 16 * E));
         A_(dalloc(c, &A.cord_hi, 2 * N));
@@ -770,6 +773,10 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     DevParams P;
     fill_params(P, *p);
     A_(cuda_err(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice), "params"));
+    if (mode == GF_MODE_FP64) {
+        GfKernels<double>::plastic_table(launch_of(c));
+        A_(cuda_err(cudaGetLastError(), "plastic table"));
+    }
     DevClock C0;
     std::memset(&C0, 0, sizeof C0);
     C0.frac = p->frac;
@@ -813,6 +820,10 @@ int gf_set_params(gf_ctx *c, const gf_params *p) {
     fill_params(P, *p);
     GF_CK(cudaStreamSynchronize(c->s));
     GF_CK(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice));
+    if (c->mode == GF_MODE_FP64) {
+        GfKernels<double>::plastic_table(launch_of(c));
+        GF_CK(cudaGetLastError());
+    }
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
     c->graphs.clear();
     return GF_OK;

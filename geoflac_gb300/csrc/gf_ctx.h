@@ -63,6 +63,9 @@ struct DevClock {
 
 // Device arrays of a context.  In GF_MODE_MIXED the element fields listed
 // under "R" are FP32 (R = float); in GF_MODE_FP64 everything is double.
+#define GF_PT_STATES 3 // plastic strain before, at the start of, after softening
+#define GF_PT_W 8
+
 struct DevArrays {
     // node fields (always FP64: coordinates, temperature, masses)
     double *cord, *vel, *temp, *temp0, *amass, *rmass, *bc;
@@ -105,6 +108,9 @@ struct DevArrays {
     // written by fl_rheol from the new stresses: for corner c and the k-th
     // of its three triangles, fx at [(6c + 2k) E + e], fy at [(6c + 2k + 1) E + e]
     double *n_frc;
+    // FP64: plastic constants of single-phase elements, [GF_PT_STATES][GF_MAXPH][GF_PT_W]
+    // (anphi, anpsi, amc, e1, e2, x1, ten_max, hardn per phase and strain branch)
+    double *plast_tab;
     int *nmarkers;                                    // device marker count
     // magma sub-model (allocated when itype_melting = 1): melt fractions,
     // dike / MOR accumulators (E each), the last arc extrusion (nx), and
@@ -164,6 +170,9 @@ template <class R> struct GfKernels {
     static void phase_recount_all(const GfLaunch &g);
     // refresh the hi/lo splits after the FP64 coordinates / velocities changed
     static void split_nodes(const GfLaunch &g);
+    // FP64: the per-phase plastic constants of single-phase elements, after
+    // every upload of the model constants
+    static void plastic_table(const GfLaunch &g);
 };
 
 // Remesh event (par.f90:94-110): host-prepared constants, passed by value.

@@ -689,6 +689,32 @@ __device__ __forceinline__ bool maxwell_wins_unyielded(float sp_a, float sp_b, f
     return 2.0f * W + V - Q * t * (2.0f + t) <= 0.0f;
 }
 
+// One phase's terms of pre_plast in FP64 (rh_plastic.f90:249-280): the
+// element path and the per-phase table of single-phase elements
+// (k_plastic_table) both evaluate these operations.
+__device__ __forceinline__ void pre_plast_phase(const DevParams &P, int k, double ratio, double pls_curr, double &phi,
+                                                double &coh, double &psi, double &hardn) {
+    const double pl1 = P.plstrain1[k], pl2 = P.plstrain2[k];
+    const double f1 = P.fric1[k], f2 = P.fric2[k], c1 = P.cohesion1[k], c2 = P.cohesion2[k];
+    const double d1 = P.dilat1[k], d2 = P.dilat2[k];
+    double f, c, dd, h;
+    if (pls_curr < pl1) {
+        f = f1; c = c1; dd = d1; h = 0;
+    } else if (pls_curr < pl2) {
+        double dpl = (pls_curr - pl1) / (pl2 - pl1);
+        f = f1 + (f2 - f1) * dpl;
+        dd = d1 + (d2 - d1) * dpl;
+        c = c1 + (c2 - c1) * dpl;
+        h = P.hsoft[k];
+    } else {
+        f = f2; c = c2; dd = d2; h = 0;
+    }
+    phi = phi + ratio / f;
+    coh = coh + ratio / c;
+    psi = psi + ratio * dd;
+    hardn = hardn + ratio * h;
+}
+
 // pre_plast (rh_plastic.f90:231-291)
 template <class R>
 __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
@@ -696,38 +722,34 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
     R pls_curr = aps_e;
     phi = 0; coh = 0; psi = 0; hardn = 0;
     for (int k = 0; k < P.nphase; ++k) {
-        R ratio, f, c, dd, h, pl1, pl2, f1, f2, c1, c2, d1, d2;
         if constexpr (sizeof(R) == sizeof(float)) {
             // phase ratios are k/n with n <= 32 markers: 0.01 separates 0 from the rest in FP32 too
-            ratio = gf_d2f(A.phase_ratio[gf_pr(d, e, k)]);
+            const float ratio = gf_d2f(A.phase_ratio[gf_pr(d, e, k)]);
             if (ratio < 0.01f) continue;
-            pl1 = P.f_pl1[k]; pl2 = P.f_pl2[k];
-            f1 = P.f_fric1[k]; f2 = P.f_fric2[k]; c1 = P.f_coh1[k]; c2 = P.f_coh2[k]; d1 = P.f_dil1[k]; d2 = P.f_dil2[k];
-        } else {
-            ratio = R(A.phase_ratio[gf_pr(d, e, k)]);
-            if (A.phase_ratio[gf_pr(d, e, k)] < 0.01) continue;
-            pl1 = R(P.plstrain1[k]); pl2 = R(P.plstrain2[k]);
-            f1 = R(P.fric1[k]); f2 = R(P.fric2[k]); c1 = R(P.cohesion1[k]); c2 = R(P.cohesion2[k]);
-            d1 = R(P.dilat1[k]); d2 = R(P.dilat2[k]);
-        }
-        if (pls_curr < pl1) {
-            f = f1; c = c1; dd = d1; h = 0;
-        } else if (pls_curr < pl2) {
-            R dpl = (pls_curr - pl1) / (pl2 - pl1);
-            f = f1 + (f2 - f1) * dpl;
-            dd = d1 + (d2 - d1) * dpl;
-            c = c1 + (c2 - c1) * dpl;
-            if constexpr (sizeof(R) == sizeof(float))
+            const float pl1 = P.f_pl1[k], pl2 = P.f_pl2[k];
+            const float f1 = P.f_fric1[k], f2 = P.f_fric2[k], c1 = P.f_coh1[k], c2 = P.f_coh2[k];
+            const float d1 = P.f_dil1[k], d2 = P.f_dil2[k];
+            float f, c, dd, h;
+            if (pls_curr < pl1) {
+                f = f1; c = c1; dd = d1; h = 0;
+            } else if (pls_curr < pl2) {
+                float dpl = (pls_curr - pl1) / (pl2 - pl1);
+                f = f1 + (f2 - f1) * dpl;
+                dd = d1 + (d2 - d1) * dpl;
+                c = c1 + (c2 - c1) * dpl;
                 h = (c2 - c1) / (pl2 - pl1);
-            else
-                h = R(P.hsoft[k]);
+            } else {
+                f = f2; c = c2; dd = d2; h = 0;
+            }
+            phi = phi + ratio / f;
+            coh = coh + ratio / c;
+            psi = psi + ratio * dd;
+            hardn = hardn + ratio * h;
         } else {
-            f = f2; c = c2; dd = d2; h = 0;
+            const double ratio = A.phase_ratio[gf_pr(d, e, k)];
+            if (ratio < 0.01) continue;
+            pre_plast_phase(P, k, ratio, pls_curr, phi, coh, psi, hardn);
         }
-        phi = phi + ratio / f;
-        coh = coh + ratio / c;
-        psi = psi + ratio * dd;
-        hardn = hardn + ratio * h;
     }
     phi = R(1) / phi;
     coh = R(1) / coh;
@@ -737,6 +759,37 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
         phi = phi * (R(1) - (R(1) - w) * fma / fm);
         coh = coh * (R(1) - (R(1) - w) * fma / fm);
     }
+}
+
+// Per-phase table of the plastic constants of single-phase elements (FP64).
+// pre_plast and plastic_consts of an element whose only phase present is
+// k (phase ratio exactly 1, every other ratio below 0.01) depend on the
+// element only through the branch its plastic strain takes: before
+// softening (pls < plstrain1), at its start (pls == plstrain1, where the
+// interpolation weight is +0) or after it (pls >= plstrain2).  For those
+// the table holds the values the element path computes, from the same
+// functions on the same inputs; other elements (mixed phases, strain
+// inside the softening interval, melt weakening) take the element path.
+__device__ __forceinline__ int plastic_table_state(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
+                                                   int iph, double pls) {
+    if (P.itype_melting == 1) return -1;
+    const unsigned long long one = 0x3ff0000000000000ull, cut = (unsigned long long)__double_as_longlong(0.01);
+    for (int k = 0; k < P.nphase; ++k) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(A.phase_ratio[gf_pr(d, e, k)]);
+        if (k == iph) {
+            if (b != one) return -1;
+        } else {
+            // ratio < 0.01 on the bit pattern: true for negative numbers and
+            // -0, false for NaNs, otherwise the order of the magnitudes
+            const bool nan = (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+            const bool less = (b >> 63) ? true : b < cut;
+            if (nan || !less) return -1;
+        }
+    }
+    const double pl1 = P.plstrain1[iph], pl2 = P.plstrain2[iph];
+    if (pls < pl1) return 0;
+    if (pls < pl2) return __double_as_longlong(pls) == __double_as_longlong(pl1) ? 1 : -1;
+    return 2;
 }
 
 } // namespace gfk

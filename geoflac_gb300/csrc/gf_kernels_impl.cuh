@@ -160,8 +160,23 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     // mixed path: stored normal stresses are deviations from -pref
     R pref = R(0);
     if constexpr (sizeof(R) == sizeof(float)) pref = A.pr_hi[e]; // == float(p_ref)
-    R coh = 0, phi = 0, psi = 0, hardn = 0;
-    if (irh == 6 || irh >= 11) pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
+    R hardn = 0;
+    PlasticConsts<R> pc;
+    if (irh == 6 || irh >= 11) {
+        int pst = -1; // FP64: single-phase elements read the per-phase table
+        if constexpr (sizeof(R) == sizeof(double))
+            if (A.plast_tab) pst = plastic_table_state(P, A, d, e, iph, aps_e);
+        if (pst >= 0) {
+            const double *t = A.plast_tab + (GF_IDX)(pst * GF_MAXPH + iph) * GF_PT_W;
+            pc.anphi = t[0]; pc.anpsi = t[1]; pc.amc = t[2]; pc.e1 = t[3];
+            pc.e2 = t[4]; pc.x1 = t[5]; pc.ten_max = t[6]; hardn = t[7];
+        } else {
+            R coh = 0, phi = 0, psi = 0;
+            pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
+            pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi,
+                                   sizeof(R) == sizeof(float) ? R(P.f_ten_off) : R(P.ten_off));
+        }
+    }
     R *visn = (R *)A.visn;
     R vis;
     if ((irh == 3 || irh >= 11) && update_visc) {
@@ -170,9 +185,6 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     } else {
         vis = visn[e];
     }
-    PlasticConsts<R> pc;
-    if (irh == 6 || irh >= 11)
-        pc = plastic_consts<R>(bulkm, rmu, coh, phi, psi, sizeof(R) == sizeof(float) ? R(P.f_ten_off) : R(P.ten_off));
     R dike = A.dike_released ? gf_to<R>(A.dike_released[e]) : R(0);
     const R *dvol = (const R *)A.dvol;
     R sp[4][4], sv[4][4], depl[4] = {0, 0, 0, 0};
@@ -1827,6 +1839,37 @@ template <class R> __global__ void k_convert_back(const R *__restrict__ src, dou
         }                                                                                                              \
     } while (0)
 
+// The table read by plastic_table_state's elements: one thread per (phase,
+// state), each evaluating pre_plast_phase and plastic_consts as the element
+// path does, with a plastic strain in the state's branch (-inf: before
+// softening, plstrain1: at its start, +inf: after it).
+namespace { // internal linkage, one copy per precision's translation unit
+namespace gfk {
+__global__ void k_plastic_table(const DevParams *__restrict__ Pp, double *__restrict__ tab) {
+    const DevParams &P = *Pp;
+    const int t = threadIdx.x;
+    if (t >= GF_MAXPH * GF_PT_STATES) return;
+    const int k = t / GF_PT_STATES, s = t % GF_PT_STATES;
+    const double pls = s == 0 ? -INFINITY : (s == 1 ? P.plstrain1[k] : INFINITY);
+    double phi = 0, coh = 0, psi = 0, hardn = 0;
+    pre_plast_phase(P, k, 1.0, pls, phi, coh, psi, hardn);
+    phi = 1.0 / phi;
+    coh = 1.0 / coh;
+    const PlasticConsts<double> c = plastic_consts<double>(P.bulkm[k], P.rm[k], coh, phi, psi, P.ten_off);
+    double *o = tab + (s * GF_MAXPH + k) * GF_PT_W;
+    o[0] = c.anphi; o[1] = c.anpsi; o[2] = c.amc; o[3] = c.e1;
+    o[4] = c.e2; o[5] = c.x1; o[6] = c.ten_max; o[7] = hardn;
+}
+} // namespace gfk
+} // namespace
+template <class R> void GfKernels<R>::plastic_table(const GfLaunch &g) {
+    if constexpr (sizeof(R) == sizeof(double)) {
+        if (g.A.plast_tab) {
+            gfk::k_plastic_table<<<1, GF_MAXPH * GF_PT_STATES, 0, g.s>>>(g.P, g.A.plast_tab);
+            ++*g.launches;
+        }
+    }
+}
 template <class R> void GfKernels<R>::therm_prep(const GfLaunch &g) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float)) GF_LAUNCH(k_therm_prep32, g.d.E, g.P, g.A, g.d, (float *)g.A.t_coef);

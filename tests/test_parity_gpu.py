@@ -87,6 +87,55 @@ def test_steps_match_oracle(workdir, name, steps):
     gpu.close()
 
 
+def test_plastic_strain_branches_match_oracle(workdir):
+    """pre_plast + the plastic constants of single-phase elements come from a
+    per-phase table for plastic strain before softening, exactly at its
+    start and after it; other elements compute them.  On the 60x20
+    extension model with softening between plastic strain 0.02 and 0.2,
+    elements get strains in every branch (0, 0.02 exactly, inside the
+    interval, 0.2 and beyond; crust, mantle and the mixed rows at the
+    Moho), and fl_rheol then matches the oracle bit for bit, as do 50 steps."""
+    m = inpgen.extension_60x20()
+    for ph in m.phases:
+        ph.pls1, ph.pls2 = 0.02, 0.2
+    inp = m.write(str(workdir / "pls_branches.inp"))
+    p, c, s = new_state(inp)
+    p2, c2, s2 = oracle_state(inp)
+    orc = Oracle(p2, c2, s2)
+    orc.finish_setflac()
+    orc.step(20)
+    aps = orc.s["aps"]
+    levels = np.array([0.0, 0.02, 0.05, 0.2, 0.7])
+    jj, ii = np.indices(aps.shape)
+    aps[...] = levels[(jj + 3 * ii) % levels.size]
+    # phase mixtures: columns 10-14 with 60 % of their own phase and 40 % of
+    # another, columns 20-24 with a 0.005 trace of another phase (below the
+    # 0.01 cut-off of pre_plast) beside a ratio of exactly 1
+    pr, iph = orc.s["phase_ratio"], orc.s["iphase"]
+    for i in range(10, 15):
+        for j in range(pr.shape[1]):
+            own = iph[j, i] - 1
+            pr[:, j, i] = 0.0
+            pr[own, j, i] = 0.6
+            pr[(own + 2) % p.nphase, j, i] = 0.4
+    for i in range(20, 25):
+        for j in range(pr.shape[1]):
+            pr[(iph[j, i] - 1 + 1) % p.nphase, j, i] = 0.005
+    gpu = Flac(p, c, s, "fp64")
+    gpu.state.copy_from(orc.s)
+    for k, _ in capi.GfClock._fields_:
+        setattr(gpu.clock, k, getattr(orc.c, k))
+    gpu.upload()
+    orc.fl_rheol()
+    gpu.fl_rheol()
+    diffs = _assert_close(gpu, orc, where="fl_rheol")
+    assert max(diffs.values()) == 0.0, diffs
+    orc.step(50)
+    gpu.step(50)
+    _assert_close(gpu, orc, where="50 steps")
+    gpu.close()
+
+
 def test_graph_step_equals_flac_calls(workdir):
     """gf_step(n) (graph replay) and n gf_flac calls give identical bits."""
     a, _ = _pair(workdir, "extension_60x20")
