@@ -147,10 +147,16 @@ void fill_params(DevParams &P, const gf_params &p) {
         // the device's per-element expressions, evaluated once per phase
         // (same IEEE operations; host code is built without contraction)
         P.bulkm[k] = p.rl[k] + 2.0 * p.rm[k] / 3.0;
+        P.den_y[k] = 1.0 / p.den[k];
+        P.den_yl[k] = std::fma(-P.den_y[k], p.den[k], 1.0) * P.den_y[k];
+        P.cp_y[k] = 1.0 / p.cp[k];
+        P.cp_yl[k] = std::fma(-P.cp_y[k], p.cp[k], 1.0) * P.cp_y[k];
         P.hsoft[k] = (p.plstrain2[k] != p.plstrain1[k])
                          ? (p.cohesion2[k] - p.cohesion1[k]) / (p.plstrain2[k] - p.plstrain1[k])
                          : 0.0;
     }
+    P.sixth_y = 1.0 / 6.0;
+    P.sixth_yl = std::fma(-P.sixth_y, 6.0, 1.0) * P.sixth_y;
     P.f_fmagma_max = (float)p.fmagma_max;
     P.topo_kappa = p.topo_kappa;
     for (int k = 0; k < GF_MAXPH; ++k) P.erodibility[k] = p.erodibility[k];
@@ -756,7 +762,13 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     }
     if (mode == GF_MODE_FP64) {
         A_(dalloc(c, &A.n_frc, 24 * E));
-        A_(dalloc(c, &A.plast_tab, GF_PT_STATES * GF_MAXPH * GF_PT_W));
+        double *tab = nullptr;
+        A_(dalloc(c, &tab, GF_PT_STATES * GF_MAXPH * GF_PT_W));
+        A.plast_tab = tab;
+    } else {
+        float *tab = nullptr;
+        A_(dalloc(c, &tab, GF_PT_STATES * GF_MAXPH * GF_PT_W));
+        A.plast_tab = tab;
     }
     if (mode == GF_MODE_MIXED) {
         A_(dalloc(c, &c->staging, 16 * E));
@@ -773,10 +785,11 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     DevParams P;
     fill_params(P, *p);
     A_(cuda_err(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice), "params"));
-    if (mode == GF_MODE_FP64) {
+    if (mode == GF_MODE_FP64)
         GfKernels<double>::plastic_table(launch_of(c));
-        A_(cuda_err(cudaGetLastError(), "plastic table"));
-    }
+    else
+        GfKernels<float>::plastic_table(launch_of(c));
+    A_(cuda_err(cudaGetLastError(), "plastic table"));
     DevClock C0;
     std::memset(&C0, 0, sizeof C0);
     C0.frac = p->frac;
@@ -820,10 +833,11 @@ int gf_set_params(gf_ctx *c, const gf_params *p) {
     fill_params(P, *p);
     GF_CK(cudaStreamSynchronize(c->s));
     GF_CK(cudaMemcpy(c->dP, &P, sizeof P, cudaMemcpyHostToDevice));
-    if (c->mode == GF_MODE_FP64) {
+    if (c->mode == GF_MODE_FP64)
         GfKernels<double>::plastic_table(launch_of(c));
-        GF_CK(cudaGetLastError());
-    }
+    else
+        GfKernels<float>::plastic_table(launch_of(c));
+    GF_CK(cudaGetLastError());
     for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
     c->graphs.clear();
     return GF_OK;

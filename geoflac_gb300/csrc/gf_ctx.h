@@ -37,6 +37,9 @@ struct DevParams {
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
     double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:130)
     double bulkm[GF_MAXPH]; // rl + 2 rm / 3 (fl_rheol.f90:192)
+    // reciprocal pairs y = 1/b, yl = (1 - b y) y of the thermal divisors
+    // den, cp and 6 (gf_div: the bits of the divisions)
+    double den_y[GF_MAXPH], den_yl[GF_MAXPH], cp_y[GF_MAXPH], cp_yl[GF_MAXPH], sixth_y, sixth_yl;
     double hsoft[GF_MAXPH]; // (cohesion2 - cohesion1) / (plstrain2 - plstrain1) (rh_plastic.f90:264)
     double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)
     // magma sub-model (itype_melting = 1)
@@ -108,9 +111,10 @@ struct DevArrays {
     // written by fl_rheol from the new stresses: for corner c and the k-th
     // of its three triangles, fx at [(6c + 2k) E + e], fy at [(6c + 2k + 1) E + e]
     double *n_frc;
-    // FP64: plastic constants of single-phase elements, [GF_PT_STATES][GF_MAXPH][GF_PT_W]
-    // (anphi, anpsi, amc, e1, e2, x1, ten_max, hardn per phase and strain branch)
-    double *plast_tab;
+    // plastic constants of single-phase elements, [GF_PT_STATES][GF_MAXPH][GF_PT_W]
+    // (anphi, anpsi, amc, e1, e2, x1, ten_max, hardn per phase and strain
+    // branch), in the element fields' precision
+    void *plast_tab;
     int *nmarkers;                                    // device marker count
     // magma sub-model (allocated when itype_melting = 1): melt fractions,
     // dike / MOR accumulators (E each), the last arc extrusion (nx), and
@@ -170,8 +174,8 @@ template <class R> struct GfKernels {
     static void phase_recount_all(const GfLaunch &g);
     // refresh the hi/lo splits after the FP64 coordinates / velocities changed
     static void split_nodes(const GfLaunch &g);
-    // FP64: the per-phase plastic constants of single-phase elements, after
-    // every upload of the model constants
+    // the per-phase plastic constants of single-phase elements, after every
+    // upload of the model constants
     static void plastic_table(const GfLaunch &g);
 };
 

@@ -145,6 +145,15 @@ __device__ __forceinline__ GfRecip gf_recip_y(double b, double y) { // y = 1.0 /
     return r;
 }
 __device__ __forceinline__ GfRecip gf_recip(double b) { return gf_recip_y(b, 1.0 / b); }
+// a pair computed ahead (y = RN(1/b) exactly; yl need only be near (1 - b y) y)
+__device__ __forceinline__ GfRecip gf_recip_pre(double b, double y, double yl) {
+    GfRecip r;
+    r.b = b;
+    r.y = y;
+    r.yl = yl;
+    r.ok = gf_dmid(b);
+    return r;
+}
 __device__ __forceinline__ double gf_div(double a, const GfRecip &r) {
     if (!(r.ok && gf_dmid(a))) return (r.ok && gf_dzero(a)) ? a * r.y : a / r.b;
     const double q = fma(a, r.y, a * r.yl);
@@ -527,7 +536,15 @@ __device__ __forceinline__ void maxwell(R bulkm, const MaxwellConsts<R> &m, R &s
 // transcendental work).
 template <class R> struct PlasticConsts {
     R anphi, anpsi, amc, e1, e2, x1, ten_max;
+    float anphi_f, amc_f, ten_f; // FP64 path: FP32 copies for plastic_keeps_trial
 };
+// the FP32 copies of an FP64 element's constants (integer-pipe conversion)
+__device__ __forceinline__ void plastic_consts_f32(PlasticConsts<double> &c) {
+    c.anphi_f = gf_d2f(c.anphi);
+    c.amc_f = gf_d2f(c.amc);
+    c.ten_f = gf_d2f(c.ten_max);
+}
+__device__ __forceinline__ void plastic_consts_f32(PlasticConsts<float> &) {}
 
 template <class R>
 __device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh, R phi, R psi, R ten_off) {
@@ -542,7 +559,40 @@ __device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh
     c.e2 = bulkm - c2d3 * rmu;
     c.x1 = (c.e1 - c.e2 * c.anpsi + c.e1 * c.anphi * c.anpsi - c.e2 * c.anphi);
     c.ten_max = (phi == R(0.0)) ? ten_off : fmin(ten_off, coh / m_tand(phi));
+    plastic_consts_f32(c);
     return c;
+}
+
+// Whether plastic (FP64) keeps the elastic trial stress: no tension
+// cut-off (s1 < ten_max, rh_plastic.f90:111) and no shear yield (fs >= 0,
+// rh_plastic.f90:134-135).  Decided from an FP32 evaluation of s1 and fs with a
+// bound on its distance to the FP64 evaluation; true only where the FP32
+// margin exceeds that bound, false (take the FP64 path) otherwise.
+//
+// With A = max(|s11i|, |s22i|, |s12i|) and u = 2^-24 (the float inputs are
+// within u A of the doubles; the FP32 steps round once each, the square root
+// included, as this translation unit builds without contraction and with
+// IEEE square roots), the FP32 values are within
+//   s1:  12 u A                                       of the exact s1,
+//   fs:  u (18 A + anphi (24 A + 5 |ten_max|) + 3 amc)  of the exact fs
+// (|S0| <= A, rad <= 2 A, the square root of a sum of squares is
+// 1-Lipschitz in its vector), and the FP64 values are within the same
+// expressions in 2^-53.  The margins below are twice those sums; the
+// absolute 1e-30 covers inputs below the float range (flushed to zero), and
+// any NaN or overflow fails the comparisons.
+__device__ __forceinline__ bool plastic_keeps_trial(const PlasticConsts<double> &c, double s11i, double s22i,
+                                                    double s12i) {
+    const float a = gf_d2f(s11i), b = gf_d2f(s22i), q = gf_d2f(s12i);
+    const float A = fmaxf(fmaxf(fabsf(a), fabsf(b)), fabsf(q));
+    const float d = a - b, s0 = 0.5f * (a + b);
+    const float r = 0.5f * sqrtf(d * d + (4.0f * q) * q);
+    const float s1 = s0 - r, sii = s0 + r;
+    const float ten = c.ten_f, anphi = c.anphi_f, amc = c.amc_f, at = fabsf(ten);
+    const float s3 = fminf(sii, ten);
+    const float fs = (s1 - s3 * anphi) + amc;
+    const float e_s1 = 3.4e-6f * A + 2.4e-7f * at + 1e-30f;
+    const float e_fs = 1.2e-7f * (40.0f * A + anphi * (52.0f * A + 10.0f * at) + 4.0f * amc) + 1e-30f;
+    return (s1 + e_s1 < ten) && (fs > e_fs);
 }
 
 // plastic (rh_plastic.f90:3-229), 2-D branch (icase = 1).
@@ -555,6 +605,12 @@ __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &dep
     R s22i = s22 + (de11 + de33) * e2 + de22 * e1;
     R s12i = s12 + de12 * R(2.0) * rmu;
     R s33i = s33 + (de11 + de22) * e2 + de33 * e1;
+    if constexpr (sizeof(R) == sizeof(double)) {
+        if (plastic_keeps_trial(c, s11i, s22i, s12i)) {
+            s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;
+            return;
+        }
+    }
     R sdif = s11i - s22i;
     R s0 = R(0.5) * (s11i + s22i);
     R rad = R(0.5) * m_sqrt(sdif * sdif + R(4.0) * s12i * s12i);
@@ -715,6 +771,30 @@ __device__ __forceinline__ void pre_plast_phase(const DevParams &P, int k, doubl
     hardn = hardn + ratio * h;
 }
 
+// The same in FP32 with the mixed path's FP32 constants.
+__device__ __forceinline__ void pre_plast_phase(const DevParams &P, int k, float ratio, float pls_curr, float &phi,
+                                                float &coh, float &psi, float &hardn) {
+    const float pl1 = P.f_pl1[k], pl2 = P.f_pl2[k];
+    const float f1 = P.f_fric1[k], f2 = P.f_fric2[k], c1 = P.f_coh1[k], c2 = P.f_coh2[k];
+    const float d1 = P.f_dil1[k], d2 = P.f_dil2[k];
+    float f, c, dd, h;
+    if (pls_curr < pl1) {
+        f = f1; c = c1; dd = d1; h = 0;
+    } else if (pls_curr < pl2) {
+        float dpl = (pls_curr - pl1) / (pl2 - pl1);
+        f = f1 + (f2 - f1) * dpl;
+        dd = d1 + (d2 - d1) * dpl;
+        c = c1 + (c2 - c1) * dpl;
+        h = (c2 - c1) / (pl2 - pl1);
+    } else {
+        f = f2; c = c2; dd = d2; h = 0;
+    }
+    phi = phi + ratio / f;
+    coh = coh + ratio / c;
+    psi = psi + ratio * dd;
+    hardn = hardn + ratio * h;
+}
+
 // pre_plast (rh_plastic.f90:231-291)
 template <class R>
 __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
@@ -726,25 +806,7 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
             // phase ratios are k/n with n <= 32 markers: 0.01 separates 0 from the rest in FP32 too
             const float ratio = gf_d2f(A.phase_ratio[gf_pr(d, e, k)]);
             if (ratio < 0.01f) continue;
-            const float pl1 = P.f_pl1[k], pl2 = P.f_pl2[k];
-            const float f1 = P.f_fric1[k], f2 = P.f_fric2[k], c1 = P.f_coh1[k], c2 = P.f_coh2[k];
-            const float d1 = P.f_dil1[k], d2 = P.f_dil2[k];
-            float f, c, dd, h;
-            if (pls_curr < pl1) {
-                f = f1; c = c1; dd = d1; h = 0;
-            } else if (pls_curr < pl2) {
-                float dpl = (pls_curr - pl1) / (pl2 - pl1);
-                f = f1 + (f2 - f1) * dpl;
-                dd = d1 + (d2 - d1) * dpl;
-                c = c1 + (c2 - c1) * dpl;
-                h = (c2 - c1) / (pl2 - pl1);
-            } else {
-                f = f2; c = c2; dd = d2; h = 0;
-            }
-            phi = phi + ratio / f;
-            coh = coh + ratio / c;
-            psi = psi + ratio * dd;
-            hardn = hardn + ratio * h;
+            pre_plast_phase(P, k, ratio, pls_curr, phi, coh, psi, hardn);
         } else {
             const double ratio = A.phase_ratio[gf_pr(d, e, k)];
             if (ratio < 0.01) continue;
@@ -761,7 +823,8 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
     }
 }
 
-// Per-phase table of the plastic constants of single-phase elements (FP64).
+// Per-phase table of the plastic constants of single-phase elements, in the
+// element fields' precision.
 // pre_plast and plastic_consts of an element whose only phase present is
 // k (phase ratio exactly 1, every other ratio below 0.01) depend on the
 // element only through the branch its plastic strain takes: before
@@ -770,14 +833,18 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
 // the table holds the values the element path computes, from the same
 // functions on the same inputs; other elements (mixed phases, strain
 // inside the softening interval, melt weakening) take the element path.
+template <class R>
 __device__ __forceinline__ int plastic_table_state(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
-                                                   int iph, double pls) {
+                                                   int iph, R pls) {
     if (P.itype_melting == 1) return -1;
     const unsigned long long one = 0x3ff0000000000000ull, cut = (unsigned long long)__double_as_longlong(0.01);
     for (int k = 0; k < P.nphase; ++k) {
-        const unsigned long long b = (unsigned long long)__double_as_longlong(A.phase_ratio[gf_pr(d, e, k)]);
+        const double r = A.phase_ratio[gf_pr(d, e, k)];
+        const unsigned long long b = (unsigned long long)__double_as_longlong(r);
         if (k == iph) {
             if (b != one) return -1;
+        } else if constexpr (sizeof(R) == sizeof(float)) {
+            if (!(gf_d2f(r) < 0.01f)) return -1; // the FP32 path's own test
         } else {
             // ratio < 0.01 on the bit pattern: true for negative numbers and
             // -0, false for NaNs, otherwise the order of the magnitudes
@@ -786,9 +853,16 @@ __device__ __forceinline__ int plastic_table_state(const DevParams &P, const Dev
             if (nan || !less) return -1;
         }
     }
-    const double pl1 = P.plstrain1[iph], pl2 = P.plstrain2[iph];
-    if (pls < pl1) return 0;
-    if (pls < pl2) return __double_as_longlong(pls) == __double_as_longlong(pl1) ? 1 : -1;
+    R pl1, pl2;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        pl1 = P.f_pl1[iph]; pl2 = P.f_pl2[iph];
+        if (pls < pl1) return 0;
+        if (pls < pl2) return __float_as_uint(pls) == __float_as_uint(pl1) ? 1 : -1;
+    } else {
+        pl1 = P.plstrain1[iph]; pl2 = P.plstrain2[iph];
+        if (pls < pl1) return 0;
+        if (pls < pl2) return __double_as_longlong(pls) == __double_as_longlong(pl1) ? 1 : -1;
+    }
     return 2;
 }
 

@@ -163,13 +163,14 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     R hardn = 0;
     PlasticConsts<R> pc;
     if (irh == 6 || irh >= 11) {
-        int pst = -1; // FP64: single-phase elements read the per-phase table
-        if constexpr (sizeof(R) == sizeof(double))
-            if (A.plast_tab) pst = plastic_table_state(P, A, d, e, iph, aps_e);
+        // single-phase elements outside the softening interval read the
+        // per-phase table
+        const int pst = A.plast_tab ? plastic_table_state<R>(P, A, d, e, iph, aps_e) : -1;
         if (pst >= 0) {
-            const double *t = A.plast_tab + (GF_IDX)(pst * GF_MAXPH + iph) * GF_PT_W;
+            const R *t = (const R *)A.plast_tab + (GF_IDX)(pst * GF_MAXPH + iph) * GF_PT_W;
             pc.anphi = t[0]; pc.anpsi = t[1]; pc.amc = t[2]; pc.e1 = t[3];
             pc.e2 = t[4]; pc.x1 = t[5]; pc.ten_max = t[6]; hardn = t[7];
+            plastic_consts_f32(pc);
         } else {
             R coh = 0, phi = 0, psi = 0;
             pre_plast<R>(P, A, d, e, aps_e, coh, phi, psi, hardn);
@@ -859,7 +860,10 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     // conduct / den / cp of the phase: the same two IEEE divisions as the
     // reference's cond_eff / dens / cp_eff, taken once per phase at set-up
     double diff = P.diffu[iph];
-    double src = (A.source[e] + dissip / P.den[iph]) / cp_eff;
+    const GfRecip rden = gf_recip_pre(P.den[iph], P.den_y[iph], P.den_yl[iph]);
+    const GfRecip rcp = gf_recip_pre(cp_eff, P.cp_y[iph], P.cp_yl[iph]);
+    const GfRecip r6 = gf_recip_pre(6.0, P.sixth_y, P.sixth_yl);
+    double src = gf_div(A.source[e] + gf_div(dissip, rden), rcp);
     Quad q;
     load_quad(A.cord, d, j, i, q);
     const R *area = (const R *)A.area;
@@ -878,7 +882,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
 #pragma unroll
             for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = dd[m] * dd[n] + zz[m] * zz[n];
         double inv_area = 1.0 / a;
-        double ra = inv_area / 6.0;
+        double ra = gf_div(inv_area, r6);
         tc[(12 + t) * E + e] = ra;
         tc[(14 + t) * E + e] = 0.5 * diff * inv_area;
         tc[(16 + t) * E + e] = src * ra;
@@ -1845,31 +1849,36 @@ template <class R> __global__ void k_convert_back(const R *__restrict__ src, dou
 // softening, plstrain1: at its start, +inf: after it).
 namespace { // internal linkage, one copy per precision's translation unit
 namespace gfk {
-__global__ void k_plastic_table(const DevParams *__restrict__ Pp, double *__restrict__ tab) {
+template <class R> __global__ void k_plastic_table(const DevParams *__restrict__ Pp, R *__restrict__ tab) {
     const DevParams &P = *Pp;
     const int t = threadIdx.x;
     if (t >= GF_MAXPH * GF_PT_STATES) return;
     const int k = t / GF_PT_STATES, s = t % GF_PT_STATES;
-    const double pls = s == 0 ? -INFINITY : (s == 1 ? P.plstrain1[k] : INFINITY);
-    double phi = 0, coh = 0, psi = 0, hardn = 0;
-    pre_plast_phase(P, k, 1.0, pls, phi, coh, psi, hardn);
-    phi = 1.0 / phi;
-    coh = 1.0 / coh;
-    const PlasticConsts<double> c = plastic_consts<double>(P.bulkm[k], P.rm[k], coh, phi, psi, P.ten_off);
-    double *o = tab + (s * GF_MAXPH + k) * GF_PT_W;
+    R pl1, bulkm, rmu, ten_off;
+    if constexpr (sizeof(R) == sizeof(float)) {
+        pl1 = P.f_pl1[k]; bulkm = P.f_bulkm[k]; rmu = P.f_rm[k]; ten_off = P.f_ten_off;
+    } else {
+        pl1 = P.plstrain1[k]; bulkm = P.bulkm[k]; rmu = P.rm[k]; ten_off = P.ten_off;
+    }
+    const R pls = s == 0 ? R(-INFINITY) : (s == 1 ? pl1 : R(INFINITY));
+    R phi = 0, coh = 0, psi = 0, hardn = 0;
+    pre_plast_phase(P, k, R(1), pls, phi, coh, psi, hardn);
+    phi = R(1) / phi;
+    coh = R(1) / coh;
+    const PlasticConsts<R> c = plastic_consts<R>(bulkm, rmu, coh, phi, psi, ten_off);
+    R *o = tab + (s * GF_MAXPH + k) * GF_PT_W;
     o[0] = c.anphi; o[1] = c.anpsi; o[2] = c.amc; o[3] = c.e1;
     o[4] = c.e2; o[5] = c.x1; o[6] = c.ten_max; o[7] = hardn;
 }
 } // namespace gfk
 } // namespace
 template <class R> void GfKernels<R>::plastic_table(const GfLaunch &g) {
-    if constexpr (sizeof(R) == sizeof(double)) {
-        if (g.A.plast_tab) {
-            gfk::k_plastic_table<<<1, GF_MAXPH * GF_PT_STATES, 0, g.s>>>(g.P, g.A.plast_tab);
-            ++*g.launches;
-        }
+    if (g.A.plast_tab) {
+        gfk::k_plastic_table<R><<<1, GF_MAXPH * GF_PT_STATES, 0, g.s>>>(g.P, (R *)g.A.plast_tab);
+        ++*g.launches;
     }
 }
+
 template <class R> void GfKernels<R>::therm_prep(const GfLaunch &g) {
     using namespace gfk;
     if (sizeof(R) == sizeof(float)) GF_LAUNCH(k_therm_prep32, g.d.E, g.P, g.A, g.d, (float *)g.A.t_coef);
