@@ -118,6 +118,15 @@ __device__ __forceinline__ bool gf_dzero(double x) {
 // |x| in [2^-450, 2^451) (biased exponents 573 .. 1473): quotients and the
 // products below of two such numbers are normal doubles
 __device__ __forceinline__ bool gf_dmid(double x) { return gf_dexp(x) - 573u <= 900u; }
+// r < 0.01 (pre_plast's phase-ratio cut-off, rh_plastic.f90:250) on the bit
+// pattern: true for negative numbers and -0, false for NaNs, otherwise the
+// order of the magnitudes
+__device__ __forceinline__ bool gf_ratio_below_cut(double r) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+    const unsigned long long cut = (unsigned long long)__double_as_longlong(0.01);
+    if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return false;
+    return (b >> 63) ? true : b < cut;
+}
 
 // Division by a shared denominator with the bits of IEEE division.  For a
 // denominator b: y = RN(1/b) (one IEEE division) and yl = RN(RN(1 - b y) y),
@@ -803,13 +812,12 @@ __device__ __forceinline__ void pre_plast(const DevParams &P, const DevArrays &A
     phi = 0; coh = 0; psi = 0; hardn = 0;
     for (int k = 0; k < P.nphase; ++k) {
         if constexpr (sizeof(R) == sizeof(float)) {
-            // phase ratios are k/n with n <= 32 markers: 0.01 separates 0 from the rest in FP32 too
-            const float ratio = gf_d2f(A.phase_ratio[gf_pr(d, e, k)]);
-            if (ratio < 0.01f) continue;
-            pre_plast_phase(P, k, ratio, pls_curr, phi, coh, psi, hardn);
+            const double r = A.phase_ratio[gf_pr(d, e, k)];
+            if (gf_ratio_below_cut(r)) continue;
+            pre_plast_phase(P, k, gf_d2f(r), pls_curr, phi, coh, psi, hardn);
         } else {
             const double ratio = A.phase_ratio[gf_pr(d, e, k)];
-            if (ratio < 0.01) continue;
+            if (gf_ratio_below_cut(ratio)) continue;
             pre_plast_phase(P, k, ratio, pls_curr, phi, coh, psi, hardn);
         }
     }
@@ -837,20 +845,12 @@ template <class R>
 __device__ __forceinline__ int plastic_table_state(const DevParams &P, const DevArrays &A, const GfDims &d, GF_IDX e,
                                                    int iph, R pls) {
     if (P.itype_melting == 1) return -1;
-    const unsigned long long one = 0x3ff0000000000000ull, cut = (unsigned long long)__double_as_longlong(0.01);
     for (int k = 0; k < P.nphase; ++k) {
         const double r = A.phase_ratio[gf_pr(d, e, k)];
-        const unsigned long long b = (unsigned long long)__double_as_longlong(r);
         if (k == iph) {
-            if (b != one) return -1;
-        } else if constexpr (sizeof(R) == sizeof(float)) {
-            if (!(gf_d2f(r) < 0.01f)) return -1; // the FP32 path's own test
-        } else {
-            // ratio < 0.01 on the bit pattern: true for negative numbers and
-            // -0, false for NaNs, otherwise the order of the magnitudes
-            const bool nan = (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
-            const bool less = (b >> 63) ? true : b < cut;
-            if (nan || !less) return -1;
+            if (__double_as_longlong(r) != 0x3ff0000000000000ll) return -1; // exactly 1
+        } else if (!gf_ratio_below_cut(r)) {
+            return -1;
         }
     }
     R pl1, pl2;

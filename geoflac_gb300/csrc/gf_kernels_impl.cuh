@@ -4,11 +4,12 @@
 #include "gf_kernels.cuh"
 
 // resident CTAs per SM the register allocation of k_rheol is sized for:
-// 1 for FP64 (no spills; the kernel is bound by the FP64 pipe), 3 for the
-// mixed path (80 registers; its few spills cost less than the occupancy
-// they buy)
+// 2 for FP64 (128 registers; its spills cost less than the latency that 16
+// warps per SM hide: 0.703 -> 0.678 ms against 255 registers and 8 warps),
+// 3 for the mixed path (80 registers; its few spills cost less than the
+// occupancy they buy)
 #ifndef GF_RHEOL_MINB
-#define GF_RHEOL_MINB (sizeof(R) == sizeof(float) ? 3 : 1)
+#define GF_RHEOL_MINB (sizeof(R) == sizeof(float) ? 3 : 2)
 #endif
 
 // internal linkage: each precision's translation unit has its own copy
