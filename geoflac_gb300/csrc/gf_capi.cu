@@ -711,6 +711,7 @@ int gf_create(gf_ctx **out, const gf_params *p, const gf_layout *L, int mode) {
     A_(dalloc(c, &A.t_delta1, N));
     A_(dalloc(c, &A.t_coef, (size_t)18 * E));
     A_(dalloc(c, &A.t_chg, 2 * N));
+    if (mode == GF_MODE_FP64) A_(dalloc(c, &A.t_pred, N));
     A_(dalloc(c, &c->therm_bar, 4));
     A_(dalloc(c, &A.e_dens, E));
     A_(dalloc(c, &A.e_tri, 4 * E));

@@ -90,6 +90,7 @@ struct DevArrays {
     double *t_delta0, *t_delta1; // thermal sweep iterates (node)
     double *t_coef;              // thermal per-element coefficients (18 per element)
     uint8_t *t_chg;              // FP64 thermal sweeps: node changed in sweep k (2 x N, by parity)
+    double *t_pred;              // FP64 thermal sweeps: each node's last increment (the next start)
     double *p_ref; // mixed: per-element reference pressure; stored normal stresses are total + p_ref
     double *e_dens;                                   // per-element density (rmasses)
     double *e_tri;                                    // per-triangle mass shares (4 per element)

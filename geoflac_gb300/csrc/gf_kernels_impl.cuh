@@ -856,7 +856,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     int j, i;
     elem_ji(d, e, j, i);
     int iph = A.iphase[e] - 1;
-    double cp_eff = P.cp[iph], cond_eff = P.conduct[iph];
+    double cp_eff = P.cp[iph];
     double dissip = (P.ishearh == 1 && P.itherm != 2) ? (double)((const R *)A.shrheat)[e] : 0.0;
     // conduct / den / cp of the phase: the same two IEEE divisions as the
     // reference's cond_eff / dens / cp_eff, taken once per phase at set-up
@@ -914,11 +914,15 @@ __device__ __forceinline__ double therm_bc_value(const DevParams &P, const DevAr
     return src(gf_node(d, j, ii));
 }
 
-// One node of sweep k.  Tup holds the current iterate (Told for sweep 0);
-// self and downstream values always come from Told (A.temp).  Returns
-// whether the node's value changed.  The iterates and the change flags are
-// written by other CTAs of the same (persistent) launch, so their loads
-// bypass L1 (__ldcg).
+// One node of sweep k.  Tup holds the current iterate; the start (the
+// iterate before sweep 0) is Told + the previous step's increment
+// (A.t_pred), a guess: the fixed point does not depend on it, only how many
+// nodes the sweeps recompute before they reach it (on the 1000x300 model
+// sweep 2 recomputes 16 % of the nodes instead of 82 %).  Self and
+// downstream values always come from Told (A.temp).  Returns whether the
+// node's value changed.  The iterates and the change flags are written by
+// other CTAs of the same (persistent) launch, so their loads bypass L1
+// (__ldcg).
 __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double dt, const double *__restrict__ tc,
                                                  const double *Tup, double *Tout, int k, GF_IDX n) {
     int j, i;
@@ -942,7 +946,9 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     const double *T = A.temp;
     double rhs = 0.0, area_n = 0.0;
     auto Nd = [&](int jj, int ii) { return gf_node(d, jj, ii); };
-    auto U = [&](int jj, int ii) { return __ldcg(Tup + Nd(jj, ii)); };
+    const double *pred = A.t_pred;
+    auto start = [&](GF_IDX m) { return T[m] + pred[m]; };
+    auto U = [&](int jj, int ii) { return k == 0 ? start(Nd(jj, ii)) : __ldcg(Tup + Nd(jj, ii)); };
     // triangle t of element e; vs = local index of the updated node; the
     // three (local vertex, temperature) terms in the reference's order
     auto tri = [&](GF_IDX e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
@@ -969,7 +975,7 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
         tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
     double tn = Ts + rhs * dt / area_n;
     Tout[n] = tn;
-    return tn != __ldcg(Tup + n);
+    return tn != (k == 0 ? start(n) : __ldcg(Tup + n));
 }
 
 // Bounded grid barrier of a co-resident (cooperative) launch: generation
@@ -1047,8 +1053,10 @@ __global__ void __launch_bounds__(GF_THREADS) k_therm_sweeps(const DevParams *__
         int j, i;
         node_ji(d, n, j, i);
         double t = therm_bc_value(*Pp, A, d, [src](GF_IDX m) { return __ldcg(src + m); }, j, i);
-        if (!keep_temp0) A.temp0[n] = A.temp[n];
+        const double told = A.temp[n];
+        if (!keep_temp0) A.temp0[n] = told;
         A.temp[n] = t;
+        A.t_pred[n] = t - told; // the next step's start: its Told + this increment
     }
 }
 
