@@ -777,11 +777,14 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
             double det =
                 ((xc[b] * yc[c] - yc[b] * xc[c]) - (xc[a] * yc[c] - yc[a] * xc[c])) + (xc[a] * yc[b] - yc[a] * xc[b]);
             dvol[gf_ek(d, e, k)] = R(det * (double)ar_old - 1.0);
-            ar_new = R(1.0 / det);
-            double dw = 0.5 *
-                        (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) +
-                         yv[a] * (yc[c] - yc[b]) + yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])) /
-                        det * dtd;
+            const double rdet = 1.0 / det;
+            ar_new = R(rdet);
+            // the rotation's quotient by det from the same reciprocal (gf_div:
+            // the bits of the division)
+            double dw = gf_div(0.5 * (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) +
+                                      yv[a] * (yc[c] - yc[b]) + yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])),
+                               gf_recip_y(det, rdet)) *
+                        dtd;
             dw12 = R(dw);
         } else {
             // FP32 from edge vectors of the relative coordinates: det = B x C
