@@ -1571,12 +1571,17 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     switch (iph) {
     case 4: case 8: {
         if (depth > 150e3) break;
-        double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
-        double trpres2 = 2.1e9 + (0.6e9 - 2.1e9) * (tmpr - 730.0) / (670.0 - 730.0);
+        // the reference's expressions, each evaluated only when its branch
+        // needs it (the second pressure only below the first, the solidus
+        // only outside the serpentine window)
         double press = mantle_density * P.g * depth;
-        double pg = fabs(press * 1e-9);
-        double solidus = -5.02 * (pg * pg) + 1.32e2 * pg + 1.09e3 + 35.0;
-        if (press < trpres && press > trpres2) {
+        double trpres = 2.1e9 + (7.5e9 - 2.1e9) * (tmpr - 730.0) / (500.0 - 730.0);
+        bool serp_window = false;
+        if (press < trpres) {
+            double trpres2 = 2.1e9 + (0.6e9 - 2.1e9) * (tmpr - 730.0) / (670.0 - 730.0);
+            serp_window = press > trpres2;
+        }
+        if (serp_window) {
             int jb0 = min(j + 2, nz - 1), jb1 = min(j + 1 + P.nelem_serp, nz - 1);
             for (int jb = jb0; jb <= jb1; ++jb) {
                 GF_IDX eb = gf_elem(d, jb - 1, i);
@@ -1585,8 +1590,10 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
                     break;
                 }
             }
-        } else if (tmpr >= solidus + 35.0) {
-            newph = 18;
+        } else {
+            double pg = fabs(press * 1e-9);
+            double solidus = -5.02 * (pg * pg) + 1.32e2 * pg + 1.09e3 + 35.0;
+            if (tmpr >= solidus + 35.0) newph = 18;
         }
         break;
     }
@@ -1657,6 +1664,22 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     int k = (n - 1) % 2 + 1;
     int j = ((n - k) / 2) % (nz - 1);
     int i = (n - k) / 2 / (nz - 1);
+    // the exclusions of the FP64 kernel (a phase without a rule; a marker
+    // certainly deeper than its rule reaches, from the hi parts of the
+    // corner and surface heights with a 10 m margin), before the marker's
+    // own coordinates are read
+    {
+        const int ph = A.mark_phase[kk];
+        if (!(ph == 4 || ph == 8 || ph == 10 || ph == 3 || ph == 7 || ph == 9 || ph == 1 || ph == 11 || ph == 17 ||
+              ph == 5 || ph == 16))
+            return;
+        const float *zc = A.cord_hi + d.N;
+        const GF_IDX q1 = gf_node(d, j, i), q3 = gf_node(d, j, i + 1);
+        const float zmax = fmaxf(fmaxf(zc[q1], zc[q1 + 1]), fmaxf(zc[q3], zc[q3 + 1]));
+        const float surf = 0.5f * (zc[gf_node(d, 0, i)] + zc[gf_node(d, 0, i + 1)]);
+        const float lim = (ph == 4 || ph == 8) ? 150e3f : 200e3f;
+        if (surf - zmax > lim + 10.0f) return;
+    }
     const float a1 = gf_d2f(A.mark_a1[kk]), a2 = gf_d2f(A.mark_a2[kk]), a3 = 1.0f - a1 - a2;
     GF_IDX p1, p2, p3;
     if (k == 1) {
