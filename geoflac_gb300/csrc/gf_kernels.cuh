@@ -586,9 +586,11 @@ __device__ __forceinline__ PlasticConsts<R> plastic_consts(R bulkm, R rmu, R coh
 //   fs:  u (18 A + anphi (24 A + 5 |ten_max|) + 3 amc)  of the exact fs
 // (|S0| <= A, rad <= 2 A, the square root of a sum of squares is
 // 1-Lipschitz in its vector), and the FP64 values are within the same
-// expressions in 2^-53.  The margins below are twice those sums; the
-// absolute 1e-30 covers inputs below the float range (flushed to zero), and
-// any NaN or overflow fails the comparisons.
+// expressions in 2^-53.  The margins below exceed twice those sums and
+// cover the FP32 copies of ten_max, anphi and amc and the rounding of the
+// comparisons; the absolute 1e-30 covers inputs below the float range
+// (flushed to zero), and any NaN or overflow fails the comparisons.
+// tests/test_plastic_filter.py checks the bound on adversarial states.
 __device__ __forceinline__ bool plastic_keeps_trial(const PlasticConsts<double> &c, double s11i, double s22i,
                                                     double s12i) {
     const float a = gf_d2f(s11i), b = gf_d2f(s22i), q = gf_d2f(s12i);
