@@ -39,6 +39,16 @@ __device__ __forceinline__ float m_tand(float deg) {
 __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float m_abs(float x) { return fabsf(x); }
 
+// Programmatic dependent launch: the kernels of the step are launched with
+// programmatic stream serialization, so that each one's CTAs can be placed on
+// SMs while the kernel before it drains.  Every such kernel calls this
+// first: it lets the next kernel launch early and waits until the kernel
+// before it has finished and its writes are visible, before reading anything.
+__device__ __forceinline__ void gf_pdl_entry() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ void set_status(DevClock *C, int code, int where) {
     if (atomicCAS(&C->status, 0, code) == 0) C->status_aux = where;
 }

@@ -402,6 +402,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     (void)nloop;
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS, GF_RHEOL_MINB) k_rheol(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int update_visc, int nloop) {
+    gf_pdl_entry();
     b_k_rheol<R>(Pp, C, A, d, update_visc, nloop, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -423,6 +424,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol_avg(DevClock *__res
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_rheol_avg(DevClock *__restrict__ C, DevArrays A, GfDims d, int reset) {
+    gf_pdl_entry();
     b_k_rheol_avg<R>(C, A, d, reset, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -712,6 +714,7 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_node(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int terms) {
+    gf_pdl_entry();
     b_k_node<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x, terms);
 }
 
@@ -729,6 +732,7 @@ __device__ __forceinline__ void b_k_move_cord(DevClock *__restrict__ C, DevArray
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_move_cord(DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    gf_pdl_entry();
     b_k_move_cord(C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -823,6 +827,7 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
     if (neg) set_status(C, 40, (int)e);
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_move_elem(DevClock *__restrict__ C, DevArrays A, GfDims d, int advance_time) {
+    gf_pdl_entry();
     b_k_move_elem<R>(C, A, d, advance_time, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -893,6 +898,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc) {
+    gf_pdl_entry();
     b_k_therm_prep<R>(Pp, C, A, d, tc, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1102,6 +1108,7 @@ __device__ __forceinline__ void b_k_therm_prep32(const DevParams *__restrict__ P
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_prep32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, float *__restrict__ tc) {
+    gf_pdl_entry();
     b_k_therm_prep32(Pp, A, d, tc, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1152,6 +1159,7 @@ __device__ __forceinline__ void b_k_therm_sweep32(const DevParams *__restrict__ 
         tnew[n] = A.temp[n] + gf_f2d(inc);
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_sweep32(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, const float *__restrict__ tc, float *__restrict__ d0, double *__restrict__ tnew, int final_sweep) {
+    gf_pdl_entry();
     b_k_therm_sweep32(Pp, C, A, d, tc, d0, tnew, final_sweep, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1170,6 +1178,7 @@ __device__ __forceinline__ void b_k_therm_apply32(const DevParams *__restrict__ 
     A.temp_lo[n] = l;
 }
 __global__ void __launch_bounds__(GF_THREADS) k_therm_apply32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, const double *__restrict__ tnew) {
+    gf_pdl_entry();
     b_k_therm_apply32(Pp, A, d, tnew, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1217,6 +1226,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_dens(const DevParams
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_dens(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    gf_pdl_entry();
     b_k_elem_dens<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1281,6 +1291,7 @@ __device__ __forceinline__ void b_k_node_gather_tri(const T *__restrict__ tri, d
 }
 template <class T>
 __global__ void __launch_bounds__(GF_THREADS) k_node_gather_tri(const T *__restrict__ tri, double *__restrict__ out, GfDims d) {
+    gf_pdl_entry();
     b_k_node_gather_tri<T>(tri, out, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1404,6 +1415,7 @@ template <class R> __device__ __forceinline__ void b_k_dt_reduce(const DevParams
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_dt_reduce(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    gf_pdl_entry();
     b_k_dt_reduce<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1492,6 +1504,7 @@ template <class R> __device__ __forceinline__ void b_k_elem_am3(const DevParams 
     for (int k = 0; k < 4; ++k) A.e_tri[k * d.E + e] = c1d12 * rho_inert / (double)area[gf_ek(d, e, k)];
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_elem_am3(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d) {
+    gf_pdl_entry();
     b_k_elem_am3<R>(Pp, C, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1514,6 +1527,7 @@ template <class R> __device__ __forceinline__ void b_k_init_visc(const DevParams
     ((R *)A.visn)[e] = R(visc_of<R>(*Pp, A, d, j, i, e, (const R *)A.stress0));
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_init_visc(const DevParams *__restrict__ Pp, DevArrays A, GfDims d) {
+    gf_pdl_entry();
     b_k_init_visc<R>(Pp, A, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1648,6 +1662,7 @@ __device__ __forceinline__ void b_k_phase_markers(const DevParams *__restrict__ 
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_phase_markers(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
+    gf_pdl_entry();
     b_k_phase_markers(Pp, A, d, nmarkers, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1775,6 +1790,7 @@ __device__ __forceinline__ void b_k_phase_markers32(const DevParams *__restrict_
     }
 }
 __global__ void __launch_bounds__(GF_THREADS) k_phase_markers32(const DevParams *__restrict__ Pp, DevArrays A, GfDims d, int nmarkers) {
+    gf_pdl_entry();
     b_k_phase_markers32(Pp, A, d, nmarkers, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1814,6 +1830,7 @@ template <class R> __device__ __forceinline__ void b_k_phase_recount(const DevPa
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_phase_recount(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, int all) {
+    gf_pdl_entry();
     b_k_phase_recount<R>(Pp, C, A, d, all, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1849,6 +1866,7 @@ __device__ __forceinline__ void b_k_min_angle(DevArrays A, GfDims d, unsigned lo
     if ((threadIdx.x & 31) == 0) atomic_min_pos(out, fmax(amin, 0.0));
 }
 __global__ void __launch_bounds__(GF_THREADS) k_min_angle(DevArrays A, GfDims d, unsigned long long *out) {
+    gf_pdl_entry();
     b_k_min_angle(A, d, out, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1857,12 +1875,14 @@ template <class R> __device__ __forceinline__ void b_k_convert(const double *__r
     if (t < n) dst[t] = R(src[t]);
 }
 template <class R> __global__ void k_convert(const double *__restrict__ src, R *__restrict__ dst, GF_IDX n) {
+    gf_pdl_entry();
     b_k_convert<R>(src, dst, n, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 template <class R> __device__ __forceinline__ void b_k_convert_back(const R *__restrict__ src, double *__restrict__ dst, GF_IDX n, GF_IDX t) {
     if (t < n) dst[t] = (double)src[t];
 }
 template <class R> __global__ void k_convert_back(const R *__restrict__ src, double *__restrict__ dst, GF_IDX n) {
+    gf_pdl_entry();
     b_k_convert_back<R>(src, dst, n, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -1870,10 +1890,25 @@ template <class R> __global__ void k_convert_back(const R *__restrict__ src, dou
 } // namespace
 
 // ---------------------------------------------------------------- launchers
+// Launch with programmatic stream serialization (the kernel starts with
+// gf_pdl_entry); `n` items, GF_THREADS per CTA.
+template <class... KArgs, class... Args>
+inline void gf_launch_pdl(void (*kern)(KArgs...), unsigned grid, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(grid);
+    lc.blockDim = dim3(GF_THREADS);
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, kern, (KArgs)args...);
+}
 #define GF_LAUNCH(kern, n, ...)                                                                                        \
     do {                                                                                                               \
         if ((n) > 0) {                                                                                                 \
-            kern<<<gfk::grid_for(n), GF_THREADS, 0, g.s>>>(__VA_ARGS__);                                               \
+            gf_launch_pdl(kern, gfk::grid_for(n), g.s, __VA_ARGS__);                                                   \
             ++*g.launches;                                                                                             \
         }                                                                                                              \
     } while (0)
@@ -1983,6 +2018,7 @@ template <class R> void GfKernels<R>::rheol(const GfLaunch &g, int update_visc, 
 namespace {
 namespace gfk {
 __global__ void __launch_bounds__(GF_THREADS) k_elem_forces(DevArrays A, GfDims d) {
+    gf_pdl_entry();
     const GF_IDX e = (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= d.E) return;
     int j, i;
@@ -2069,6 +2105,7 @@ template <class R> void GfKernels<R>::change_phase(const GfLaunch &g, int nmarke
 namespace {
 namespace gfk {
 __global__ void k_split(const double *__restrict__ src, float *__restrict__ hi, float *__restrict__ lo, GF_IDX n) {
+    gf_pdl_entry();
     GF_IDX t = (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const double v = src[t];
@@ -2123,6 +2160,7 @@ template <class R> __device__ __forceinline__ void b_k_stress_in(const double *_
         for (int c = 0; c < 4; ++c) st[gf_s(d, e, c, k)] = R(c == 2 ? tot[gf_s(d, e, c, k)] : tot[gf_s(d, e, c, k)] + p);
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_in(const double *__restrict__ tot, R *__restrict__ st, double *__restrict__ p_ref, GfDims d) {
+    gf_pdl_entry();
     b_k_stress_in<R>(tot, st, p_ref, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -2138,6 +2176,7 @@ template <class R> __device__ __forceinline__ void b_k_stress_out(const R *__res
         }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_stress_out(const R *__restrict__ st, const double *__restrict__ p_ref, double *__restrict__ tot, GfDims d) {
+    gf_pdl_entry();
     b_k_stress_out<R>(st, p_ref, tot, d, (GF_IDX)blockIdx.x * blockDim.x + threadIdx.x);
 }
 } // namespace gfk
