@@ -18,7 +18,9 @@ Operands whose magnitude lies outside [2^-450, 2^451) take an IEEE division,
 and a zero numerator gives a * y.  Python's float(Fraction) rounds correctly,
 so fma(x, y, z) = float(Fraction(x) * y + z) is the fused multiply-add.  The
 cases include quotients within r * 2^-106 (r = 1, 3, 5, ...) of a rounding
-midpoint, the hardest cases for any division scheme."""
+midpoint, the hardest cases for any division scheme.  Also here: the other
+integer-pipe stand-in for an FP64 instruction, pre_plast's phase-ratio
+cut-off taken on the bit pattern (gf_ratio_below_cut)."""
 import math
 import random
 import struct
@@ -126,3 +128,25 @@ def test_zeros_and_operands_outside_the_range_give_ieee_results(b):
             continue
         assert same(div(a, r), want), (a, b)
     assert math.isnan(div(math.nan, r))
+
+
+def ratio_below_cut(r):
+    """gf_ratio_below_cut (geoflac_gb300/csrc/gf_kernels.cuh): r < 0.01 on the
+    bit pattern of r"""
+    b = struct.unpack("<Q", struct.pack("<d", r))[0]
+    cut = struct.unpack("<Q", struct.pack("<d", 0.01))[0]
+    if (b & 0x7FFFFFFFFFFFFFFF) > 0x7FF0000000000000:
+        return False
+    return True if (b >> 63) else b < cut
+
+
+def test_phase_ratio_cut_off_on_the_bit_pattern_is_the_ieee_comparison():
+    """pre_plast's `phase_ratio < 0.01` (rh_plastic.f90:250) taken on the
+    integer pipe gives the IEEE comparison's answer on every class of value."""
+    nxt = lambda x, d: struct.unpack("<d", struct.pack("<q", struct.unpack("<q", struct.pack("<d", x))[0] + d))[0]
+    vals = [0.0, -0.0, 0.01, nxt(0.01, -1), nxt(0.01, 1), -0.01, 1.0, 0.5, 1e-300, -1e-300, 5e-324, -5e-324,
+            math.inf, -math.inf, math.nan, -math.nan, 1 / 32, 1 / 3, 2.0, 1e300]
+    rng = random.Random(9)
+    vals += [rng.uniform(-1, 1) * 10.0 ** rng.uniform(-20, 5) for _ in range(5000)]
+    for v in vals:
+        assert ratio_below_cut(v) == (v < 0.01), v
