@@ -119,15 +119,96 @@ __device__ __forceinline__ double gf_f2d(float f) {
     const unsigned hi = sign | (ed << 20) | (m >> 3);
     return __longlong_as_double((long long)(((unsigned long long)hi << 32) | ((unsigned long long)(m & 7u) << 29)));
 }
-// Biased exponent field and zero test of a double, on the integer pipe (an
-// FP64 compare takes a slot of the FP64 pipe).
-__device__ __forceinline__ unsigned gf_dexp(double x) { return ((unsigned)__double2hiint(x) >> 20) & 0x7ffu; }
-__device__ __forceinline__ bool gf_dzero(double x) {
-    return (((unsigned)__double2hiint(x) & 0x7fffffffu) | (unsigned)__double2loint(x)) == 0u;
+// The two 32-bit halves of a double's bit pattern and back, through an
+// opaque move: the compiler would otherwise turn integer tests of the bits
+// (a zero test, say) back into FP64 comparisons, which take a slot of the
+// FP64 pipe.
+__device__ __forceinline__ void gf_dsplit(double x, unsigned &lo, unsigned &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
 }
-// |x| in [2^-450, 2^451) (biased exponents 573 .. 1473): quotients and the
-// products below of two such numbers are normal doubles
+__device__ __forceinline__ double gf_djoin(unsigned lo, unsigned hi) {
+    double x;
+    asm("mov.b64 %0, {%1, %2};" : "=d"(x) : "r"(lo), "r"(hi));
+    return x;
+}
+// Biased exponent field and zero test of a double, on the integer pipe.
+__device__ __forceinline__ unsigned gf_dexp(double x) {
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    return (hi >> 20) & 0x7ffu;
+}
+__device__ __forceinline__ bool gf_dzero(double x) {
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    return ((hi << 1) | lo) == 0u;
+}
+// |x| in [2^-450, 2^451) (biased exponents 573 .. 1473): quotients and
+// products of two such numbers are normal doubles
 __device__ __forceinline__ bool gf_dmid(double x) { return gf_dexp(x) - 573u <= 900u; }
+
+// FP64 multiplication on the integer pipes.  GB300 issues FP64 arithmetic
+// at 1/64 of the FP32 rate, and the FP64 kernels wait on that pipe while
+// the integer pipes idle, so a product of two doubles is formed here from
+// their 53-bit significands with four 32x32->64-bit integer multiplies and
+// rounded to nearest even: the bits of IEEE multiplication.  It covers
+// operands that are zero or inside gf_dmid (the product is then a normal
+// double or a signed zero); any other operand takes the FP64 multiply in a
+// call that is not inlined, so that the common path issues no FP64
+// instruction (a predicated-off FP64 multiply still takes its pipe slot).
+// Restated with Python integers and checked against IEEE products, exact
+// and near ties included, by tests/test_int_multiply.py.
+__device__ __noinline__ double gf_mul_rare(double a, double b) { return a * b; }
+__device__ __forceinline__ double gf_mul(double a, double b) {
+    unsigned la, ha, lb, hb;
+    gf_dsplit(a, la, ha);
+    gf_dsplit(b, lb, hb);
+    const bool za = ((ha << 1) | la) == 0u, zb = ((hb << 1) | lb) == 0u;
+    const bool ia = ((ha >> 20) & 0x7ffu) - 573u <= 900u, ib = ((hb >> 20) & 0x7ffu) - 573u <= 900u;
+    if (!((ia || za) && (ib || zb))) return gf_mul_rare(a, b);
+    // significands with the hidden bit (21 high bits : 32 low bits) and
+    // their 106-bit product w2:w1:w0:wm, w2 < 2^10
+    const unsigned mh = (ha & 0xfffffu) | 0x100000u, nh = (hb & 0xfffffu) | 0x100000u;
+    const unsigned long long p0 = (unsigned long long)la * lb;
+    unsigned long long t = (unsigned long long)la * nh + (p0 >> 32);
+    t += (unsigned long long)mh * lb;
+    const unsigned long long u = (unsigned long long)mh * nh + (t >> 32);
+    const unsigned w2 = (unsigned)(u >> 32), w1 = (unsigned)u, w0 = (unsigned)t, wm = (unsigned)p0;
+    // product of the significands in [2, 4): keep bits 105..53, else 104..52
+    const unsigned top = w2 >> 9, sh = 12u - top;
+    const unsigned mhi = __funnelshift_l(w1, w2, sh), mlo = __funnelshift_l(w0, w1, sh);
+    // the dropped bits of w0, left-aligned (round bit first; sh >= 11 low
+    // zeros), and the sticky bit of wm or the kept value's parity: round up
+    // iff rem > half, or rem == half and (sticky or odd)
+    const unsigned rem = w0 << sh, x = min(wm, 1u) | (mlo & 1u);
+    const unsigned up = (rem + x) > 0x80000000u ? 1u : 0u;
+    // sign and biased exponent less one (mhi's hidden bit adds the one); the
+    // sum of the sign bits wraps to their exclusive or, and the exponent sum
+    // ea + eb - 1024 + top lies in [122, 1923]
+    const unsigned S = (ha & 0xfff00000u) + (hb & 0xfff00000u) - (1024u << 20) + (top << 20);
+    const unsigned long long r = ((unsigned long long)(mhi + S) << 32 | mlo) + up; // a carry out of the
+                                                                                   // significand raises the exponent
+    if (za || zb) return gf_djoin(0u, (ha ^ hb) & 0x80000000u);
+    return gf_djoin((unsigned)r, (unsigned)(r >> 32));
+}
+__device__ __forceinline__ float gf_mul(float a, float b) { return a * b; }
+
+// x * 2^K (K = -2 .. 2, the constant factors 0.25 .. 4 of the step): the
+// exponent field moves by K while x and the result are normal doubles, a
+// zero keeps its bits, and anything else takes the FP64 multiply out of line.
+template <int K> __device__ __forceinline__ double gf_scale(double x) {
+    static_assert(K >= -2 && K <= 2 && K != 0, "factor 0.25, 0.5, 2 or 4");
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    constexpr unsigned lo_e = K < 0 ? 1u - K : 1u, hi_e = K < 0 ? 2046u : 2046u - K;
+    if (e - lo_e <= hi_e - lo_e) return gf_djoin(lo, hi + (unsigned)(K * (1 << 20)));
+    if (((hi << 1) | lo) == 0u) return x;
+    return gf_mul_rare(x, K == -2 ? 0.25 : K == -1 ? 0.5 : K == 1 ? 2.0 : 4.0);
+}
+template <int K> __device__ __forceinline__ float gf_scale(float x) {
+    return x * (K == -2 ? 0.25f : K == -1 ? 0.5f : K == 1 ? 2.0f : 4.0f);
+}
+
 // r < 0.01 (pre_plast's phase-ratio cut-off, rh_plastic.f90:250) on the bit
 // pattern: true for negative numbers and -0, false for NaNs, otherwise the
 // order of the magnitudes
@@ -173,9 +254,15 @@ __device__ __forceinline__ GfRecip gf_recip_pre(double b, double y, double yl) {
     r.ok = gf_dmid(b);
     return r;
 }
-__device__ __forceinline__ double gf_div(double a, const GfRecip &r) {
-    if (!(r.ok && gf_dmid(a))) return (r.ok && gf_dzero(a)) ? a * r.y : a / r.b;
-    const double q = fma(a, r.y, a * r.yl);
+// (out of line, so that the common path issues none of its FP64 instructions)
+__device__ __noinline__ double gf_div_rare(double a, double b, double y, bool ok) {
+    return (ok && gf_dzero(a)) ? a * y : a / b;
+}
+// IMUL: the product a * yl on the integer pipes (gf_mul), for kernels small
+// enough that its thirty instructions cost less than the FP64 slot
+template <bool IMUL = false> __device__ __forceinline__ double gf_div(double a, const GfRecip &r) {
+    if (!(r.ok && gf_dmid(a))) return gf_div_rare(a, r.b, r.y, r.ok);
+    const double q = fma(a, r.y, IMUL ? gf_mul(a, r.yl) : a * r.yl);
     return fma(fma(-q, r.b, a), r.y, q);
 }
 
@@ -491,7 +578,7 @@ __device__ __forceinline__ void elastic(R bulkm, R rmu, R &s11, R &s22, R &s33, 
     R a2 = bulkm - c2d3 * rmu;
     s11 = s11 + a1 * de11 + a2 * de22;
     s22 = s22 + a2 * de11 + a1 * de22;
-    s12 = s12 + R(2) * rmu * de12;
+    s12 = s12 + gf_scale<1>(rmu) * de12;
     s33 = s33 + a2 * (de11 + de22);
 }
 
@@ -522,10 +609,10 @@ __device__ __forceinline__ void maxwell(R bulkm, const MaxwellConsts<R> &m, R &s
     R dev, de11d, de22d, de33d, s0, s11d, s22d, s33d;
     if (ndim == 2) {
         dev = de11 + de22;
-        de11d = de11 - R(0.5) * dev;
-        de22d = de22 - R(0.5) * dev;
+        de11d = de11 - gf_scale<-1>(dev);
+        de22d = de22 - gf_scale<-1>(dev);
         de33d = 0;
-        s0 = R(0.5) * (s11 + s22);
+        s0 = gf_scale<-1>(s11 + s22);
         s11d = s11 - s0;
         s22d = s22 - s0;
         s33d = 0;
@@ -539,10 +626,11 @@ __device__ __forceinline__ void maxwell(R bulkm, const MaxwellConsts<R> &m, R &s
         s22d = s22 - s0;
         s33d = s33 - s0;
     }
-    s11d = (s11d * vic1 + R(2) * rmu * de11d) * vic2;
-    s22d = (s22d * vic1 + R(2) * rmu * de22d) * vic2;
-    s33d = (s33d * vic1 + R(2) * rmu * de33d) * vic2;
-    s12 = (s12 * vic1 + R(2) * rmu * de12) * vic2;
+    const R rmu2 = gf_scale<1>(rmu);
+    s11d = (s11d * vic1 + rmu2 * de11d) * vic2;
+    s22d = (s22d * vic1 + rmu2 * de22d) * vic2;
+    s33d = (s33d * vic1 + rmu2 * de33d) * vic2;
+    s12 = (s12 * vic1 + rmu2 * de12) * vic2;
     s0 = s0 + bulkm * dv;
     s11 = s11d + s0;
     s22 = s22d + s0;
@@ -624,7 +712,7 @@ __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &dep
     R e1 = c.e1, e2 = c.e2, anphi = c.anphi, anpsi = c.anpsi, ten_max = c.ten_max;
     R s11i = s11 + (de22 + de33) * e2 + de11 * e1;
     R s22i = s22 + (de11 + de33) * e2 + de22 * e1;
-    R s12i = s12 + de12 * R(2.0) * rmu;
+    R s12i = s12 + gf_scale<1>(de12) * rmu;
     R s33i = s33 + (de11 + de22) * e2 + de33 * e1;
     if constexpr (sizeof(R) == sizeof(double)) {
         if (plastic_keeps_trial(c, s11i, s22i, s12i)) {

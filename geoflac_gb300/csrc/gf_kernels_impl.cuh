@@ -106,7 +106,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
         R b0 = vy[tn[k][0]], b1 = vy[tn[k][1]], b2 = vy[tn[k][2]];
         sr[0][k] = a0 * dx[0][k] + a1 * dx[1][k] + a2 * dx[2][k];
         sr[1][k] = b0 * dz[0][k] + b1 * dz[1][k] + b2 * dz[2][k];
-        sr[2][k] = R(0.5) * (a0 * dz[0][k] + a1 * dz[1][k] + a2 * dz[2][k] + b0 * dx[0][k] + b1 * dx[1][k] + b2 * dx[2][k]);
+        sr[2][k] = gf_scale<-1>(a0 * dz[0][k] + a1 * dz[1][k] + a2 * dz[2][k] +
+                                b0 * dx[0][k] + b1 * dx[1][k] + b2 * dx[2][k]);
     }
     if (P.mix_strain == 1) {
 #pragma unroll
@@ -122,12 +123,12 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     }
     R *se2sr = (R *)A.se2sr;
     R *sshrheat = (R *)A.sshrheat;
-    R s11 = R(0.25) * (sr[0][0] + sr[0][1] + sr[0][2] + sr[0][3]);
-    R s22 = R(0.25) * (sr[1][0] + sr[1][1] + sr[1][2] + sr[1][3]);
-    R s12 = R(0.25) * (sr[2][0] + sr[2][1] + sr[2][2] + sr[2][3]);
-    R srII = R(0.5) * m_sqrt((s11 - s22) * (s11 - s22) + R(4.0) * s12 * s12);
-    R srI = R(0.5) * (s11 + s22);
-    R srs2 = (s11 - srI) * (s11 - srI) + (s22 - srI) * (s22 - srI) + R(2.0) * s12 * s12;
+    R s11 = gf_scale<-2>(sr[0][0] + sr[0][1] + sr[0][2] + sr[0][3]);
+    R s22 = gf_scale<-2>(sr[1][0] + sr[1][1] + sr[1][2] + sr[1][3]);
+    R s12 = gf_scale<-2>(sr[2][0] + sr[2][1] + sr[2][2] + sr[2][3]);
+    R srII = gf_scale<-1>(m_sqrt((s11 - s22) * (s11 - s22) + gf_scale<2>(s12) * s12));
+    R srI = gf_scale<-1>(s11 + s22);
+    R srs2 = (s11 - srI) * (s11 - srI) + (s22 - srI) * (s22 - srI) + gf_scale<1>(s12) * s12;
     se2sr[gf_ek(d, e, 0)] = se2sr[gf_ek(d, e, 0)] + s11 * dt;
     se2sr[gf_ek(d, e, 1)] = se2sr[gf_ek(d, e, 1)] + s22 * dt;
     se2sr[gf_ek(d, e, 2)] = se2sr[gf_ek(d, e, 2)] + s12 * dt;
@@ -136,10 +137,10 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int c = 0; c < 4; ++c) s0v[c][k] = st[gf_s(d, e, c, k)];
-    s11 = R(0.25) * (s0v[0][0] + s0v[0][1] + s0v[0][2] + s0v[0][3]);
-    s22 = R(0.25) * (s0v[1][0] + s0v[1][1] + s0v[1][2] + s0v[1][3]);
-    s12 = R(0.25) * (s0v[2][0] + s0v[2][1] + s0v[2][2] + s0v[2][3]);
-    R stII = R(0.5) * m_sqrt((s11 - s22) * (s11 - s22) + R(4.0) * s12 * s12);
+    s11 = gf_scale<-2>(s0v[0][0] + s0v[0][1] + s0v[0][2] + s0v[0][3]);
+    s22 = gf_scale<-2>(s0v[1][0] + s0v[1][1] + s0v[1][2] + s0v[1][3]);
+    s12 = gf_scale<-2>(s0v[2][0] + s0v[2][1] + s0v[2][2] + s0v[2][3]);
+    R stII = gf_scale<-1>(m_sqrt((s11 - s22) * (s11 - s22) + gf_scale<2>(s12) * s12));
     R shr = sshrheat[e];
     if (srII != R(0.0)) shr = shr + stII / srII * srs2 * dt;
 
@@ -230,10 +231,10 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     if (irh >= 11) {
         R a = sp[0][0] + sp[0][1] + sp[0][2] + sp[0][3] - sp[1][0] - sp[1][1] - sp[1][2] - sp[1][3];
         R b = sp[2][0] + sp[2][1] + sp[2][2] + sp[2][3];
-        R sII_plas = a * a + R(4.0) * (b * b);
+        R sII_plas = a * a + gf_scale<2>(b * b);
         a = sv[0][0] + sv[0][1] + sv[0][2] + sv[0][3] - sv[1][0] - sv[1][1] - sv[1][2] - sv[1][3];
         b = sv[2][0] + sv[2][1] + sv[2][2] + sv[2][3];
-        R sII_visc = a * a + R(4.0) * (b * b);
+        R sII_visc = a * a + gf_scale<2>(b * b);
         use_visc = !(sII_plas < sII_visc);
         if (sizeof(R) == sizeof(float) && !plas_mod) {
             R pa = sp[0][0] + sp[0][1] + sp[0][2] + sp[0][3] - sp[1][0] - sp[1][1] - sp[1][2] - sp[1][3];
@@ -261,8 +262,8 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 #pragma unroll
         for (int h = 0; h < 4; h += 2) {
             R ra = ar[h], rb = ar[h + 1];
-            R s0a = R(0.5) * (sn[0][h] + sn[1][h]);
-            R s0b = R(0.5) * (sn[0][h + 1] + sn[1][h + 1]);
+            R s0a = gf_scale<-1>(sn[0][h] + sn[1][h]);
+            R s0b = gf_scale<-1>(sn[0][h + 1] + sn[1][h + 1]);
             R s0;
             if constexpr (sizeof(R) == sizeof(double)) {
                 const GfRecip qa = gf_recip_y(ra, rar[h]), qb = gf_recip_y(rb, rar[h + 1]);
@@ -305,7 +306,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
                 for (int k = 0; k < 3; ++k) {
                     const int t = kk[qd][k], m = mm[qd][k];
                     // 0.25 * RN(1/ar) == RN(0.25/ar) while both are normal
-                    R factor = gf_dmid(ar[t]) ? R(0.25) * rar[t] : R(0.25) / ar[t];
+                    R factor = gf_dmid(ar[t]) ? gf_scale<-2>(rar[t]) : R(0.25) / ar[t];
                     R fx = factor * (sn[0][t] * dx[m][t] + sn[2][t] * dz[m][t]);
                     R fy = factor * (sn[2][t] * dx[m][t] + sn[1][t] * dz[m][t]);
                     nf[(GF_IDX)(6 * c + 2 * k) * d.E + e] = fx;
@@ -373,27 +374,30 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
             // reciprocal; gf_div gives each the bits of the division
             const GfRecip r2mu = gf_recip(R(2.0) * mu);
             auto by2mu = [&](R a) { return gf_div(a, r2mu); };
+            const R lam_den = lambda / den_el;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
                 R tr0 = s0v[0][k] + s0v[1][k] + s0v[3][k];
-                R e11a = by2mu(s0v[0][k] - (lambda / den_el) * tr0);
-                R e22a = by2mu(s0v[1][k] - (lambda / den_el) * tr0);
-                R e33a = by2mu(s0v[3][k] - (lambda / den_el) * tr0);
+                R lt0 = lam_den * tr0;
+                R e11a = by2mu(s0v[0][k] - lt0);
+                R e22a = by2mu(s0v[1][k] - lt0);
+                R e33a = by2mu(s0v[3][k] - lt0);
                 R e12a = by2mu(s0v[2][k]);
                 R tr1 = f11 + f22 + f33;
-                R e11b = by2mu(f11 - (lambda / den_el) * tr1);
-                R e22b = by2mu(f22 - (lambda / den_el) * tr1);
-                R e33b = by2mu(f33 - (lambda / den_el) * tr1);
+                R lt1 = lam_den * tr1;
+                R e11b = by2mu(f11 - lt1);
+                R e22b = by2mu(f22 - lt1);
+                R e33b = by2mu(f33 - lt1);
                 R e12b = by2mu(f12);
                 R d11 = sr[0][k] * dt - (e11b - e11a);
                 R d22 = sr[1][k] * dt - (e22b - e22a);
                 R d12 = sr[2][k] * dt - (e12b - e12a);
                 R d33 = R(0.0) - (e33b - e33a);
-                R a11 = R(0.5) * (s0v[0][k] + f11), a22 = R(0.5) * (s0v[1][k] + f22),
-                  a12 = R(0.5) * (s0v[2][k] + f12), a33 = R(0.5) * (s0v[3][k] + f33);
-                R qk = a11 * d11 + a22 * d22 + R(2.0) * a12 * d12 + a33 * d33;
-                qsum = qsum + R(0.25) * qk;
+                R a11 = gf_scale<-1>(s0v[0][k] + f11), a22 = gf_scale<-1>(s0v[1][k] + f22),
+                  a12 = gf_scale<-1>(s0v[2][k] + f12), a33 = gf_scale<-1>(s0v[3][k] + f33);
+                R qk = a11 * d11 + a22 * d22 + gf_scale<1>(a12) * d12 + a33 * d33;
+                qsum = qsum + gf_scale<-2>(qk);
             }
         }
         shr = shr + qsum;
@@ -778,17 +782,20 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
         R dw12, ar_new;
         if (!fp32) {
             // fl_move.f90:70-90 with the reference's operations
-            double det =
-                ((xc[b] * yc[c] - yc[b] * xc[c]) - (xc[a] * yc[c] - yc[a] * xc[c])) + (xc[a] * yc[b] - yc[a] * xc[b]);
-            dvol[gf_ek(d, e, k)] = R(det * (double)ar_old - 1.0);
+            // (products on the integer pipes: gf_mul, the bits of the FP64
+            // multiply, which this FP64-bound kernel has few enough of)
+            double det = ((gf_mul(xc[b], yc[c]) - gf_mul(yc[b], xc[c])) - (gf_mul(xc[a], yc[c]) - gf_mul(yc[a], xc[c]))) +
+                         (gf_mul(xc[a], yc[b]) - gf_mul(yc[a], xc[b]));
+            dvol[gf_ek(d, e, k)] = R(gf_mul(det, (double)ar_old) - 1.0);
             const double rdet = 1.0 / det;
             ar_new = R(rdet);
             // the rotation's quotient by det from the same reciprocal (gf_div:
             // the bits of the division)
-            double dw = gf_div(0.5 * (xv[a] * (xc[c] - xc[b]) + xv[b] * (xc[a] - xc[c]) + xv[c] * (xc[b] - xc[a]) +
-                                      yv[a] * (yc[c] - yc[b]) + yv[b] * (yc[a] - yc[c]) + yv[c] * (yc[b] - yc[a])),
-                               gf_recip_y(det, rdet)) *
-                        dtd;
+            double dw = gf_mul(gf_div<true>(gf_scale<-1>(gf_mul(xv[a], xc[c] - xc[b]) + gf_mul(xv[b], xc[a] - xc[c]) +
+                                                         gf_mul(xv[c], xc[b] - xc[a]) + gf_mul(yv[a], yc[c] - yc[b]) +
+                                                         gf_mul(yv[b], yc[a] - yc[c]) + gf_mul(yv[c], yc[b] - yc[a])),
+                                            gf_recip_y(det, rdet)),
+                               dtd);
             dw12 = R(dw);
         } else {
             // FP32 from edge vectors of the relative coordinates: det = B x C
@@ -814,14 +821,14 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
         area[gf_ek(d, e, k)] = ar_new;
         neg |= !(ar_new > R(0));
         R s11 = st[gf_s(d, e, 0, k)], s22 = st[gf_s(d, e, 1, k)], s12 = st[gf_s(d, e, 2, k)];
-        st[gf_s(d, e, 0, k)] = s11 + s12 * R(2) * dw12;
-        st[gf_s(d, e, 1, k)] = s22 - s12 * R(2) * dw12;
-        st[gf_s(d, e, 2, k)] = s12 + dw12 * (s22 - s11);
+        st[gf_s(d, e, 0, k)] = s11 + gf_mul(gf_scale<1>(s12), dw12);
+        st[gf_s(d, e, 1, k)] = s22 - gf_mul(gf_scale<1>(s12), dw12);
+        st[gf_s(d, e, 2, k)] = s12 + gf_mul(dw12, s22 - s11);
         if (k == 0) {
             R e11 = strain[gf_ek(d, e, 0)], e22 = strain[gf_ek(d, e, 1)], e12 = strain[gf_ek(d, e, 2)];
-            strain[gf_ek(d, e, 0)] = e11 + e12 * R(2) * dw12;
-            strain[gf_ek(d, e, 1)] = e22 - e12 * R(2) * dw12;
-            strain[gf_ek(d, e, 2)] = e12 + dw12 * (e22 - e11);
+            strain[gf_ek(d, e, 0)] = e11 + gf_mul(gf_scale<1>(e12), dw12);
+            strain[gf_ek(d, e, 1)] = e22 - gf_mul(gf_scale<1>(e12), dw12);
+            strain[gf_ek(d, e, 2)] = e12 + gf_mul(dw12, e22 - e11);
         }
     }
     if (neg) set_status(C, 40, (int)e);
@@ -872,7 +879,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     const GfRecip rden = gf_recip_pre(P.den[iph], P.den_y[iph], P.den_yl[iph]);
     const GfRecip rcp = gf_recip_pre(cp_eff, P.cp_y[iph], P.cp_yl[iph]);
     const GfRecip r6 = gf_recip_pre(6.0, P.sixth_y, P.sixth_yl);
-    double src = gf_div(A.source[e] + gf_div(dissip, rden), rcp);
+    double src = gf_div<true>(A.source[e] + gf_div<true>(dissip, rden), rcp);
     Quad q;
     load_quad(A.cord, d, j, i, q);
     const R *area = (const R *)A.area;
@@ -884,17 +891,19 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
         double a = (double)area[gf_ek(d, e, t)];
         double y1 = q.y[tv[t][0]], y2 = q.y[tv[t][1]], y3 = q.y[tv[t][2]];
         double x1 = q.x[tv[t][0]], x2 = q.x[tv[t][1]], x3 = q.x[tv[t][2]];
-        double dd[3] = {(y2 - y3) * a, (y3 - y1) * a, (y1 - y2) * a};
-        double zz[3] = {(x3 - x2) * a, (x1 - x3) * a, (x2 - x1) * a};
+        // (products on the integer pipes: gf_mul, the bits of the FP64
+        // multiply, which this FP64-bound kernel has few enough of)
+        double dd[3] = {gf_mul(y2 - y3, a), gf_mul(y3 - y1, a), gf_mul(y1 - y2, a)};
+        double zz[3] = {gf_mul(x3 - x2, a), gf_mul(x1 - x3, a), gf_mul(x2 - x1, a)};
 #pragma unroll
         for (int m = 0; m < 3; ++m)
 #pragma unroll
-            for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = dd[m] * dd[n] + zz[m] * zz[n];
+            for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = gf_mul(dd[m], dd[n]) + gf_mul(zz[m], zz[n]);
         double inv_area = 1.0 / a;
-        double ra = gf_div(inv_area, r6);
+        double ra = gf_div<true>(inv_area, r6);
         tc[(12 + t) * E + e] = ra;
-        tc[(14 + t) * E + e] = 0.5 * diff * inv_area;
-        tc[(16 + t) * E + e] = src * ra;
+        tc[(14 + t) * E + e] = gf_mul(gf_scale<-1>(diff), inv_area);
+        tc[(16 + t) * E + e] = gf_mul(src, ra);
     }
 }
 template <class R> __global__ void __launch_bounds__(GF_THREADS) k_therm_prep(const DevParams *__restrict__ Pp, DevClock *__restrict__ C, DevArrays A, GfDims d, double *__restrict__ tc) {
