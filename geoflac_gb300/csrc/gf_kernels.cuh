@@ -209,6 +209,55 @@ template <int K> __device__ __forceinline__ float gf_scale(float x) {
     return x * (K == -2 ? 0.25f : K == -1 ? 0.5f : K == 1 ? 2.0f : 4.0f);
 }
 
+// Additions and products with an operand that is +0 in the step's usual
+// configuration (no thermal stress, no dike, plane strain), on the integer
+// pipes: x + (+0) is x except that -0 gives +0, x - (+0) is x, +0 - x is -x
+// except that +0 gives +0, and +0 * y is +0 for y in [+0, +max].  Any other
+// operand takes the FP64 instruction out of line.  (A NaN x keeps its bits.)
+__device__ __noinline__ double gf_add_rare(double a, double b) { return a + b; }
+__device__ __forceinline__ bool gf_is_pzero(double z) {
+    unsigned lo, hi;
+    gf_dsplit(z, lo, hi);
+    return (lo | hi) == 0u;
+}
+__device__ __forceinline__ double gf_plus_pzero(double x) {
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    return gf_djoin(lo, (lo == 0u && hi == 0x80000000u) ? 0u : hi);
+}
+__device__ __forceinline__ double gf_add_z(double x, double z) { // x + z
+    return gf_is_pzero(z) ? gf_plus_pzero(x) : gf_add_rare(x, z);
+}
+__device__ __forceinline__ double gf_sub_z(double x, double z) { // x - z
+    return gf_is_pzero(z) ? x : gf_add_rare(x, -z);
+}
+__device__ __forceinline__ double gf_zero_minus(double x) { // +0 - x
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    return gf_djoin(lo, (lo | hi) == 0u ? 0u : hi ^ 0x80000000u);
+}
+__device__ __forceinline__ double gf_mul_z(double z, double y) { // z * y
+    unsigned zl, zh, yl, yh;
+    gf_dsplit(z, zl, zh);
+    gf_dsplit(y, yl, yh);
+    if ((zl | zh) == 0u && yh < 0x7ff00000u) return 0.0;
+    return gf_mul_rare(z, y);
+}
+// |x| > c for a positive finite constant c, on the bit patterns (a NaN x
+// gives false, as the FP64 comparison does)
+__device__ __forceinline__ bool gf_abs_gt(double x, double c) {
+    unsigned lo, hi, cl, ch;
+    gf_dsplit(x, lo, hi);
+    gf_dsplit(c, cl, ch);
+    const unsigned long long ax = (unsigned long long)(hi & 0x7fffffffu) << 32 | lo;
+    const unsigned long long ac = (unsigned long long)ch << 32 | cl;
+    return ax > ac && ax <= 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ float gf_add_z(float x, float z) { return x + z; }
+__device__ __forceinline__ float gf_sub_z(float x, float z) { return x - z; }
+__device__ __forceinline__ float gf_zero_minus(float x) { return 0.0f - x; }
+__device__ __forceinline__ float gf_mul_z(float z, float y) { return z * y; }
+
 // r < 0.01 (pre_plast's phase-ratio cut-off, rh_plastic.f90:250) on the bit
 // pattern: true for negative numbers and -0, false for NaNs, otherwise the
 // order of the magnitudes
@@ -588,7 +637,18 @@ __device__ __forceinline__ void elastic(R bulkm, R rmu, R &s11, R &s22, R &s33, 
 template <class R> struct MaxwellConsts {
     R rmu, vic1, vic2;
     bool ok;
+    bool pos; // vic1, 2 rmu and vic2 in [+0, +max] (FP64): +0 * each is +0
 };
+__device__ __forceinline__ bool gf_nonneg_finite(double x) {
+    unsigned lo, hi;
+    gf_dsplit(x, lo, hi);
+    return hi < 0x7ff00000u;
+}
+// s33 of a triangle whose s33d, de33d are not known to be +0 (out of line)
+__device__ __noinline__ double gf_maxwell_s33(double s33d, double vic1, double rmu2, double de33d, double vic2,
+                                              double s0) {
+    return (s33d * vic1 + rmu2 * de33d) * vic2 + s0;
+}
 template <class R> __device__ __forceinline__ MaxwellConsts<R> maxwell_consts(R rmu0, R viscosity, R dt) {
     const R visc_cut = R(1e19);
     MaxwellConsts<R> m;
@@ -597,6 +657,9 @@ template <class R> __device__ __forceinline__ MaxwellConsts<R> maxwell_consts(R 
     m.ok = !(temp > R(0.5));
     m.vic1 = R(1) - temp;
     m.vic2 = R(1.0) / (R(1.0) + temp);
+    m.pos = false;
+    if constexpr (sizeof(R) == sizeof(double))
+        m.pos = gf_nonneg_finite(m.vic1) && gf_nonneg_finite(gf_scale<1>(m.rmu)) && gf_nonneg_finite(m.vic2);
     return m;
 }
 
@@ -629,12 +692,18 @@ __device__ __forceinline__ void maxwell(R bulkm, const MaxwellConsts<R> &m, R &s
     const R rmu2 = gf_scale<1>(rmu);
     s11d = (s11d * vic1 + rmu2 * de11d) * vic2;
     s22d = (s22d * vic1 + rmu2 * de22d) * vic2;
-    s33d = (s33d * vic1 + rmu2 * de33d) * vic2;
     s12 = (s12 * vic1 + rmu2 * de12) * vic2;
     s0 = s0 + bulkm * dv;
     s11 = s11d + s0;
     s22 = s22d + s0;
-    s33 = s33d + s0;
+    if constexpr (sizeof(R) == sizeof(double)) {
+        // plane strain: s33d and de33d are +0, so (s33d vic1 + 2 rmu de33d)
+        // vic2 is +0 for factors in [+0, +max], and s33 = +0 + s0
+        s33 = (ndim == 2 && m.pos) ? gf_plus_pzero(s0) : gf_maxwell_s33(s33d, vic1, rmu2, de33d, vic2, s0);
+    } else {
+        s33d = (s33d * vic1 + rmu2 * de33d) * vic2;
+        s33 = s33d + s0;
+    }
 }
 
 // Per-element constants of the plastic return map (rh_plastic.f90:33-46).
@@ -710,10 +779,12 @@ __device__ __forceinline__ void plastic(const PlasticConsts<R> &c, R rmu, R &dep
                                         R &s12, R de11, R de22, R de33, R de12) {
     depls = R(0.0);
     R e1 = c.e1, e2 = c.e2, anphi = c.anphi, anpsi = c.anpsi, ten_max = c.ten_max;
-    R s11i = s11 + (de22 + de33) * e2 + de11 * e1;
-    R s22i = s22 + (de11 + de33) * e2 + de22 * e1;
+    // (de33 is +0 in plane strain: gf_add_z / gf_mul_z take it on the
+    // integer pipes)
+    R s11i = s11 + gf_add_z(de22, de33) * e2 + de11 * e1;
+    R s22i = s22 + gf_add_z(de11, de33) * e2 + de22 * e1;
     R s12i = s12 + gf_scale<1>(de12) * rmu;
-    R s33i = s33 + (de11 + de22) * e2 + de33 * e1;
+    R s33i = gf_add_z(s33 + (de11 + de22) * e2, gf_mul_z(de33, e1));
     if constexpr (sizeof(R) == sizeof(double)) {
         if (plastic_keeps_trial(c, s11i, s22i, s12i)) {
             s11 = s11i; s22 = s22i; s33 = s33i; s12 = s12i;

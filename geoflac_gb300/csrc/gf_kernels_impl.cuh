@@ -199,11 +199,13 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         R de11 = sr[0][k] * dt, de22 = sr[1][k] * dt, de12 = sr[2][k] * dt, de33 = R(0.0);
-        R dv = dvol[gf_ek(d, e, k)] - dike;
-        sp[0][k] = s0v[0][k] + stherm;
-        sp[1][k] = s0v[1][k] + stherm;
+        // (dike and stherm are +0 without dikes and thermal stress:
+        // gf_sub_z / gf_add_z take them on the integer pipes)
+        R dv = gf_sub_z(dvol[gf_ek(d, e, k)], dike);
+        sp[0][k] = gf_add_z(s0v[0][k], stherm);
+        sp[1][k] = gf_add_z(s0v[1][k], stherm);
         sp[2][k] = s0v[2][k];
-        sp[3][k] = s0v[3][k] + stherm;
+        sp[3][k] = gf_add_z(s0v[3][k], stherm);
         sv[0][k] = sp[0][k]; sv[1][k] = sp[1][k]; sv[2][k] = sp[2][k]; sv[3][k] = sp[3][k];
         if (irh == 1) {
             elastic<R>(bulkm, rmu, sp[0][k], sp[1][k], sp[3][k], sp[2][k], de11, de22, de12);
@@ -281,9 +283,9 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        sn[0][k] = sn[0][k] - stherm;
-        sn[1][k] = sn[1][k] - stherm;
-        sn[3][k] = sn[3][k] - stherm;
+        sn[0][k] = gf_sub_z(sn[0][k], stherm);
+        sn[1][k] = gf_sub_z(sn[1][k], stherm);
+        sn[3][k] = gf_sub_z(sn[3][k], stherm);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -393,7 +395,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
                 R d11 = sr[0][k] * dt - (e11b - e11a);
                 R d22 = sr[1][k] * dt - (e22b - e22a);
                 R d12 = sr[2][k] * dt - (e12b - e12a);
-                R d33 = R(0.0) - (e33b - e33a);
+                R d33 = gf_zero_minus(e33b - e33a);
                 R a11 = gf_scale<-1>(s0v[0][k] + f11), a22 = gf_scale<-1>(s0v[1][k] + f22),
                   a12 = gf_scale<-1>(s0v[2][k] + f12), a33 = gf_scale<-1>(s0v[3][k] + f33);
                 R qk = a11 * d11 + a22 * d22 + gf_scale<1>(a12) * d12 + a33 * d33;
@@ -609,7 +611,7 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
             }
         }
         f0 = (double)fx0;
-        f1 = (double)fy0 - A.rmass[n] * P.g;
+        f1 = (double)fy0 - gf_mul(A.rmass[n], P.g);
     } else {
         // FP64 path: the reference's gather from the four quads
         R fx0 = R(0.0), fy0 = R(0.0);
@@ -687,8 +689,10 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
     double *vel = A.vel;
     double v0 = vel[n], v1 = vel[d.N + n];
     int c0 = A.ncod[n], c1 = A.ncod[d.N + n];
-    if ((c0 & 1) != 1 && fabs(v0) > 1.0e-13) f0 = f0 - P.demf * copysign(fabs(f0), v0);
-    if ((c1 & 2) != 2 && fabs(v1) > 1.0e-13) f1 = f1 - P.demf * copysign(fabs(f1), v1);
+    // (the products and the |v| > 1e-13 tests on the integer pipes: gf_mul,
+    // gf_abs_gt)
+    if ((c0 & 1) != 1 && gf_abs_gt(v0, 1.0e-13)) f0 = f0 - gf_mul(P.demf, copysign(fabs(f0), v0));
+    if ((c1 & 2) != 2 && gf_abs_gt(v1, 1.0e-13)) f1 = f1 - gf_mul(P.demf, copysign(fabs(f1), v1));
     double am = A.amass[n];
     if (sizeof(R) == sizeof(float)) {
         // FP32 increment on the FP64 velocity
@@ -696,8 +700,9 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         v0 = (c0 == 1) ? A.bc[n] : v0 + gf_f2d(s * gf_d2f(f0));
         v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_f2d(s * gf_d2f(f1));
     } else {
-        v0 = (c0 == 1) ? A.bc[n] : v0 + dt * f0 / (am * drat * drat);
-        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + dt * f1 / (am * drat * drat);
+        const double den = gf_mul(gf_mul(am, drat), drat);
+        v0 = (c0 == 1) ? A.bc[n] : v0 + gf_mul(dt, f0) / den;
+        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_mul(dt, f1) / den;
     }
     if (P.i_prestress == 1 && C->time < 600e3 * GF_SEC_YEAR) {
         if (j == nz - 1 || i == 0 || i == nx - 1) {

@@ -11,7 +11,8 @@ the FP64 multiply.  gf_scale multiplies by 0.25, 0.5, 2 or 4 by moving the
 exponent field while operand and result are normal.  The cases include exact
 ties and products within one unit of the last dropped bit of a tie (the
 rounding decisions), significands whose rounding carries into the exponent,
-signed zeros, and exponents at both ends of the covered range."""
+signed zeros, and exponents at both ends of the covered range.  Also the
+integer-pipe forms of additions and products with a +0 operand."""
 import math
 import random
 import struct
@@ -161,3 +162,67 @@ def test_power_of_two_scaling():
         for v in vals:
             got, want = gf_scale(v, k), v * 2.0 ** k
             assert same(got, want), (v, k, got, want)
+
+
+def plus_pzero(x):
+    """gf_plus_pzero: x + (+0) on the bit pattern"""
+    lo, hi = split(x)
+    return join(lo, 0 if (lo == 0 and hi == 0x80000000) else hi)
+
+
+def zero_minus(x):
+    """gf_zero_minus: +0 - x on the bit pattern"""
+    lo, hi = split(x)
+    return join(lo, 0 if (lo | hi) == 0 else hi ^ 0x80000000)
+
+
+def mul_z_shortcut(z, y):
+    """gf_mul_z's integer case: +0 * y for y in [+0, +max]"""
+    zl, zh = split(z)
+    yl, yh = split(y)
+    return 0.0 if (zl | zh) == 0 and yh < 0x7FF00000 else None
+
+
+def test_plus_zero_operand_shortcuts():
+    """The +0 operands of the plane-strain step without dikes or thermal
+    stress (gf_add_z, gf_sub_z, gf_zero_minus, gf_mul_z, and the Maxwell
+    s33 of a plane-strain triangle) give the IEEE results."""
+    rng = random.Random(24)
+    vals = [rng.uniform(-1, 1) * 10.0 ** rng.uniform(-300, 300) for _ in range(5000)]
+    vals += [0.0, -0.0, 5e-324, -5e-324, 1.7976931348623157e308, -1.7976931348623157e308, math.inf, -math.inf]
+    for x in vals:
+        assert same(plus_pzero(x), x + 0.0), x
+        assert same(x, x - 0.0), x                    # gf_sub_z returns x
+        assert same(zero_minus(x), 0.0 - x), x
+        got = mul_z_shortcut(0.0, x)
+        if got is not None:
+            assert same(got, 0.0 * x) and x >= 0.0, x
+        else:
+            assert math.copysign(1.0, x) < 0 or not math.isfinite(x), x  # the FP64 multiply out of line
+    # Maxwell, plane strain: s33d = de33d = +0 and s33 = (s33d vic1 +
+    # 2 rmu de33d) vic2 + s0 is +0 + s0 for vic1, 2 rmu, vic2 in [+0, +max]
+    pos = [0.0, 5e-324, 0.5, 1.0, 3e10, 1.7976931348623157e308]
+    for vic1 in pos:
+        for rmu2 in pos:
+            for vic2 in pos:
+                for s0 in (0.0, -0.0, -1e8, 2.5, 5e-324):
+                    full = (0.0 * vic1 + rmu2 * 0.0) * vic2 + s0
+                    assert same(full, plus_pzero(s0)), (vic1, rmu2, vic2, s0)
+    # the plastic trial with de33 = +0: (de + de33) and s + de33 * e1
+    for de in vals[:2000]:
+        assert same(de + 0.0, plus_pzero(de))
+        for e1 in (1e10, 5e-324, 0.0):
+            assert same(de + 0.0 * e1, plus_pzero(de))
+
+
+def test_magnitude_comparison_on_bits():
+    """gf_abs_gt (the damping test |v| > 1e-13 of fl_node) on the bit
+    patterns gives the FP64 comparison's answer."""
+    c = 1.0e-13
+    cb = struct.unpack("<Q", struct.pack("<d", c))[0]
+    rng = random.Random(25)
+    vals = [rng.uniform(-1, 1) * 10.0 ** rng.uniform(-20, 5) for _ in range(5000)]
+    vals += [0.0, -0.0, c, -c, math.nextafter(c, 1.0), math.nextafter(c, 0.0), math.inf, -math.inf, math.nan]
+    for v in vals:
+        ax = struct.unpack("<Q", struct.pack("<d", v))[0] & 0x7FFFFFFFFFFFFFFF
+        assert (ax > cb and ax <= 0x7FF0000000000000) == (abs(v) > c), v
