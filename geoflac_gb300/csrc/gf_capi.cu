@@ -154,6 +154,12 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.hsoft[k] = (p.plstrain2[k] != p.plstrain1[k])
                          ? (p.cohesion2[k] - p.cohesion1[k]) / (p.plstrain2[k] - p.plstrain1[k])
                          : 0.0;
+        const double lambda = P.bulkm[k] - (2.0 / 3.0) * p.rm[k];
+        double den_el = 3.0 * lambda + 2.0 * p.rm[k];
+        if (std::fabs(den_el) < 1e-30) den_el = den_el < 0.0 ? -1e-30 : 1e-30;
+        P.sh_lam_den[k] = lambda / den_el;
+        P.sh_r2mu_y[k] = 1.0 / (2.0 * p.rm[k]);
+        P.sh_r2mu_yl[k] = std::fma(-P.sh_r2mu_y[k], 2.0 * p.rm[k], 1.0) * P.sh_r2mu_y[k];
     }
     P.sixth_y = 1.0 / 6.0;
     P.sixth_yl = std::fma(-P.sixth_y, 6.0, 1.0) * P.sixth_y;

@@ -41,6 +41,9 @@ struct DevParams {
     // den, cp and 6 (gf_div: the bits of the divisions)
     double den_y[GF_MAXPH], den_yl[GF_MAXPH], cp_y[GF_MAXPH], cp_yl[GF_MAXPH], sixth_y, sixth_yl;
     double hsoft[GF_MAXPH]; // (cohesion2 - cohesion1) / (plstrain2 - plstrain1) (rh_plastic.f90:264)
+    // shear heating's per-phase factors (fl_rheol.f90:344-361): lambda / den_el
+    // and the reciprocal pair of 2 mu
+    double sh_lam_den[GF_MAXPH], sh_r2mu_y[GF_MAXPH], sh_r2mu_yl[GF_MAXPH];
     double topo_kappa, erodibility[GF_MAXPH]; // surface processes (diff_topo)
     // magma sub-model (itype_melting = 1)
     double prod_magma, prod_magma2, angle_mzone, ratio_mantle_mzone, ratio_crust_mzone, latent_heat_magma,

@@ -350,10 +350,10 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     strain[gf_ek(d, e, 2)] = strain[gf_ek(d, e, 2)] + s12 * dt;
     if (P.ishearh == 1) {
         R qsum = R(0.0);
-        R lambda = bulkm - R(2.0 / 3.0) * rmu, mu = rmu;
-        R den_el = R(3.0) * lambda + R(2.0) * mu;
-        if (m_abs(den_el) < R(1e-30)) den_el = den_el < R(0) ? R(-1e-30) : R(1e-30);
         if constexpr (sizeof(R) == sizeof(float)) {
+            R lambda = bulkm - R(2.0 / 3.0) * rmu, mu = rmu;
+            R den_el = R(3.0) * lambda + R(2.0) * mu;
+            if (m_abs(den_el) < R(1e-30)) den_el = den_el < R(0) ? R(-1e-30) : R(1e-30);
             // the same elastic-strain differences with one reciprocal and the
             // stress changes taken first
             const float lamr = lambda / den_el, inv2mu = 1.0f / (2.0f * mu);
@@ -373,10 +373,12 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
             }
         } else {
             // the 32 quotients by 2 mu (fl_rheol.f90:352-362) share one
-            // reciprocal; gf_div gives each the bits of the division
-            const GfRecip r2mu = gf_recip(R(2.0) * mu);
+            // reciprocal; gf_div gives each the bits of the division.  The
+            // phase's lambda / den_el and reciprocal pair of 2 mu are the
+            // same expressions evaluated once per phase at set-up.
+            const GfRecip r2mu = gf_recip_pre(R(2.0) * rmu, P.sh_r2mu_y[iph], P.sh_r2mu_yl[iph]);
             auto by2mu = [&](R a) { return gf_div(a, r2mu); };
-            const R lam_den = lambda / den_el;
+            const R lam_den = P.sh_lam_den[iph];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 R f11 = sn[0][k], f22 = sn[1][k], f12 = sn[2][k], f33 = sn[3][k];
