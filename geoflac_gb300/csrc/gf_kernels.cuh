@@ -253,6 +253,14 @@ __device__ __forceinline__ bool gf_abs_gt(double x, double c) {
     const unsigned long long ac = (unsigned long long)ch << 32 | cl;
     return ax > ac && ax <= 0x7ff0000000000000ull;
 }
+// a == b (IEEE: +0 equals -0, a NaN equals nothing) on the bit patterns
+__device__ __forceinline__ bool gf_deq(double a, double b) {
+    unsigned al, ah, bl, bh;
+    gf_dsplit(a, al, ah);
+    gf_dsplit(b, bl, bh);
+    const bool nan = ((ah & 0x7fffffffu) > 0x7ff00000u) || ((ah & 0x7fffffffu) == 0x7ff00000u && al != 0u);
+    return (al == bl && ah == bh && !nan) || (((ah | bh) << 1) == 0u && (al | bl) == 0u);
+}
 __device__ __forceinline__ float gf_add_z(float x, float z) { return x + z; }
 __device__ __forceinline__ float gf_sub_z(float x, float z) { return x - z; }
 __device__ __forceinline__ float gf_zero_minus(float x) { return 0.0f - x; }

@@ -976,12 +976,15 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     auto U = [&](int jj, int ii) { return k == 0 ? start(Nd(jj, ii)) : __ldcg(Tup + Nd(jj, ii)); };
     // triangle t of element e; vs = local index of the updated node; the
     // three (local vertex, temperature) terms in the reference's order
+    // (products on the integer pipes: gf_mul, the bits of the FP64 multiply;
+    // the first sweeps are bound by the FP64 pipe)
     auto tri = [&](GF_IDX e, int t, int vs, int v0, double T0, int v1, double T1, int v2, double T2) {
         double ra = tc[(12 + t) * E + e];
         area_n = area_n + ra;
         const double *K = tc + (GF_IDX)t * 6 * E + e;
         rhs = rhs + tc[(16 + t) * E + e] -
-              tc[(14 + t) * E + e] * (T0 * K[kidx(v0, vs) * E] + T1 * K[kidx(v1, vs) * E] + T2 * K[kidx(v2, vs) * E]);
+              gf_mul(tc[(14 + t) * E + e], gf_mul(T0, K[kidx(v0, vs) * E]) + gf_mul(T1, K[kidx(v1, vs) * E]) +
+                                               gf_mul(T2, K[kidx(v2, vs) * E]));
     };
     double Ts = T[n];
     if (j != 0 && i != 0) // element (j-1,i-1), triangle B: vertices (j-1,i), (j,i-1), node
@@ -998,9 +1001,9 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     }
     if (j != nz - 1 && i != nx - 1) // element (j,i), triangle A
         tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
-    double tn = Ts + rhs * dt / area_n;
+    double tn = Ts + gf_mul(rhs, dt) / area_n;
     Tout[n] = tn;
-    return tn != (k == 0 ? start(n) : __ldcg(Tup + n));
+    return !gf_deq(tn, k == 0 ? start(n) : __ldcg(Tup + n));
 }
 
 // Bounded grid barrier of a co-resident (cooperative) launch: generation

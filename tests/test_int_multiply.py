@@ -226,3 +226,21 @@ def test_magnitude_comparison_on_bits():
     for v in vals:
         ax = struct.unpack("<Q", struct.pack("<d", v))[0] & 0x7FFFFFFFFFFFFFFF
         assert (ax > cb and ax <= 0x7FF0000000000000) == (abs(v) > c), v
+
+
+def deq(a, b):
+    """gf_deq: IEEE a == b on the bit patterns"""
+    al, ah = split(a)
+    bl, bh = split(b)
+    nan = (ah & 0x7FFFFFFF) > 0x7FF00000 or ((ah & 0x7FFFFFFF) == 0x7FF00000 and al != 0)
+    return (al == bl and ah == bh and not nan) or ((((ah | bh) << 1) & M32) == 0 and (al | bl) == 0)
+
+
+def test_equality_on_bits():
+    """gf_deq (the thermal sweeps' change test) is IEEE equality."""
+    rng = random.Random(26)
+    vals = [rng.uniform(-1, 1) * 10.0 ** rng.uniform(-300, 300) for _ in range(300)]
+    vals += [0.0, -0.0, math.inf, -math.inf, math.nan, 5e-324, -5e-324, 1.0, math.nextafter(1.0, 2.0)]
+    for a in vals:
+        for b in vals[-12:] + [a, -a]:
+            assert deq(a, b) == (a == b), (a, b)
