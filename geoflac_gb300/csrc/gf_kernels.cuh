@@ -192,6 +192,50 @@ __device__ __forceinline__ double gf_mul(double a, double b) {
 }
 __device__ __forceinline__ float gf_mul(float a, float b) { return a * b; }
 
+// RN(1/b) without the FP64 pipe, for b inside gf_dmid (other b, and zero,
+// take the IEEE division out of line).  With b = M 2^(E-1075), M in
+// (2^52, 2^53), the significand of 1/b is q = RN(T), T = 2^105 / M in
+// (2^52, 2^53):
+//   1. float-float on the FP32 pipe: r = RN32(1/Mh) for the top 24 bits Mh
+//      of M, corrected by the next 24 bits Ml (r + r (1 - (Mh + Ml) r)):
+//      t1 = that times 2^53, within about 2^8 units of T;
+//   2. one Newton step in 64-bit integers: R = 2^105 - M t1 (below 2^62,
+//      so its low 64 bits are exact), t = t1 + floor(R t1 / 2^105), within
+//      one unit of T;
+//   3. the midpoint tests 2^106 - M (2t + 1) > 0 and 2^106 - M (2t - 1) < 0
+//      (exact in 64 bits; never zero, as 2^106 / M is no half-integer for
+//      M not a power of two) move t to RN(T).
+// A power-of-two b has the exact reciprocal.  Restated on words and checked
+// against IEEE division by tests/test_int_reciprocal.py.
+__device__ __noinline__ double gf_rcp_rare(double b) { return 1.0 / b; }
+__device__ __forceinline__ double gf_rcp(double b) {
+    unsigned lo, hi;
+    gf_dsplit(b, lo, hi);
+    const unsigned E = (hi >> 20) & 0x7ffu;
+    if (E - 573u > 900u) return gf_rcp_rare(b);
+    const unsigned sign = hi & 0x80000000u, mhi = hi & 0xfffffu;
+    if ((mhi | lo) == 0u) return gf_djoin(0u, sign | ((2046u - E) << 20));
+    const float Mh = __uint_as_float(0x3f800000u | (((mhi << 3) | (lo >> 29)) & 0x7fffffu));
+    const float Ml = __uint2float_rn((lo >> 5) & 0xffffffu) * 0x1p-47f; // exact
+    const float r = __frcp_rn(Mh);
+    const float e2 = fmaf(-Ml, r, fmaf(-Mh, r, 1.0f));
+    const float rl = __fmul_rn(r, e2);
+    // t1 = r 2^53 + trunc(rl 2^53) from the floats' bits (r in (0.5, 1],
+    // |rl| < 2^-22)
+    const unsigned ur = __float_as_uint(r), ul = __float_as_uint(rl);
+    const int er = (int)((ur >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu), sh = el - 97;
+    const unsigned Sl = (ul & 0x7fffffu) | 0x800000u;
+    const unsigned v = el == 0 ? 0u : sh >= 0 ? Sl << sh : sh > -32 ? Sl >> -sh : 0u;
+    long long t = ((long long)((ur & 0x7fffffu) | 0x800000u) << (er - 97)) + ((ul >> 31) ? -(long long)v : (long long)v);
+    const unsigned long long M = ((unsigned long long)(mhi | 0x100000u) << 32) | lo;
+    const long long R = -(long long)(M * (unsigned long long)t);
+    t += __mul64hi(R, t) >> 41;
+    const long long Dp = -(long long)(M * (unsigned long long)(2 * t + 1));
+    t += Dp > 0 ? 1 : (Dp + (long long)(2 * M) < 0 ? -1 : 0);
+    const unsigned long long bits = ((unsigned long long)(2044u - E) << 52) + (unsigned long long)t;
+    return gf_djoin((unsigned)bits, (unsigned)(bits >> 32) | sign);
+}
+
 // x * 2^K (K = -2 .. 2, the constant factors 0.25 .. 4 of the step): the
 // exponent field moves by K while x and the result are normal doubles, a
 // zero keeps its bits, and anything else takes the FP64 multiply out of line.
@@ -200,7 +244,7 @@ template <int K> __device__ __forceinline__ double gf_scale(double x) {
     unsigned lo, hi;
     gf_dsplit(x, lo, hi);
     const unsigned e = (hi >> 20) & 0x7ffu;
-    constexpr unsigned lo_e = K < 0 ? 1u - K : 1u, hi_e = K < 0 ? 2046u : 2046u - K;
+    constexpr unsigned lo_e = (unsigned)(K < 0 ? 1 - K : 1), hi_e = (unsigned)(K < 0 ? 2046 : 2046 - K);
     if (e - lo_e <= hi_e - lo_e) return gf_djoin(lo, hi + (unsigned)(K * (1 << 20)));
     if (((hi << 1) | lo) == 0u) return x;
     return gf_mul_rare(x, K == -2 ? 0.25 : K == -1 ? 0.5 : K == 1 ? 2.0 : 4.0);
@@ -664,7 +708,8 @@ template <class R> __device__ __forceinline__ MaxwellConsts<R> maxwell_consts(R 
     R temp = m.rmu / (R(2) * viscosity) * dt;
     m.ok = !(temp > R(0.5));
     m.vic1 = R(1) - temp;
-    m.vic2 = R(1.0) / (R(1.0) + temp);
+    if constexpr (sizeof(R) == sizeof(double)) m.vic2 = gf_rcp(R(1.0) + temp); // RN(1/(1 + temp))
+    else m.vic2 = R(1.0) / (R(1.0) + temp);
     m.pos = false;
     if constexpr (sizeof(R) == sizeof(double))
         m.pos = gf_nonneg_finite(m.vic1) && gf_nonneg_finite(gf_scale<1>(m.rmu)) && gf_nonneg_finite(m.vic2);

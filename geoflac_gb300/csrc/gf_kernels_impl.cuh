@@ -257,7 +257,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     if constexpr (sizeof(R) == sizeof(double)) {
         if (P.mix_stress == 1 || A.n_frc) {
 #pragma unroll
-            for (int t = 0; t < 4; ++t) rar[t] = R(1.0) / ar[t];
+            for (int t = 0; t < 4; ++t) rar[t] = gf_rcp(ar[t]); // RN(1/ar) off the FP64 pipe
         }
     }
     if (P.mix_stress == 1) {
@@ -794,7 +794,7 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
             double det = ((gf_mul(xc[b], yc[c]) - gf_mul(yc[b], xc[c])) - (gf_mul(xc[a], yc[c]) - gf_mul(yc[a], xc[c]))) +
                          (gf_mul(xc[a], yc[b]) - gf_mul(yc[a], xc[b]));
             dvol[gf_ek(d, e, k)] = R(gf_mul(det, (double)ar_old) - 1.0);
-            const double rdet = 1.0 / det;
+            const double rdet = gf_rcp(det); // RN(1/det) off the FP64 pipe
             ar_new = R(rdet);
             // the rotation's quotient by det from the same reciprocal (gf_div:
             // the bits of the division)
@@ -906,7 +906,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
         for (int m = 0; m < 3; ++m)
 #pragma unroll
             for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = gf_mul(dd[m], dd[n]) + gf_mul(zz[m], zz[n]);
-        double inv_area = 1.0 / a;
+        double inv_area = gf_rcp(a); // RN(1/a) off the FP64 pipe
         double ra = gf_div<true>(inv_area, r6);
         tc[(12 + t) * E + e] = ra;
         tc[(14 + t) * E + e] = gf_mul(gf_scale<-1>(diff), inv_area);
