@@ -147,10 +147,6 @@ void fill_params(DevParams &P, const gf_params &p) {
         // the device's per-element expressions, evaluated once per phase
         // (same IEEE operations; host code is built without contraction)
         P.bulkm[k] = p.rl[k] + 2.0 * p.rm[k] / 3.0;
-        P.den_y[k] = 1.0 / p.den[k];
-        P.den_yl[k] = std::fma(-P.den_y[k], p.den[k], 1.0) * P.den_y[k];
-        P.cp_y[k] = 1.0 / p.cp[k];
-        P.cp_yl[k] = std::fma(-P.cp_y[k], p.cp[k], 1.0) * P.cp_y[k];
         P.hsoft[k] = (p.plstrain2[k] != p.plstrain1[k])
                          ? (p.cohesion2[k] - p.cohesion1[k]) / (p.plstrain2[k] - p.plstrain1[k])
                          : 0.0;
@@ -161,8 +157,6 @@ void fill_params(DevParams &P, const gf_params &p) {
         P.sh_r2mu_y[k] = 1.0 / (2.0 * p.rm[k]);
         P.sh_r2mu_yl[k] = std::fma(-P.sh_r2mu_y[k], 2.0 * p.rm[k], 1.0) * P.sh_r2mu_y[k];
     }
-    P.sixth_y = 1.0 / 6.0;
-    P.sixth_yl = std::fma(-P.sixth_y, 6.0, 1.0) * P.sixth_y;
     P.f_fmagma_max = (float)p.fmagma_max;
     P.topo_kappa = p.topo_kappa;
     for (int k = 0; k < GF_MAXPH; ++k) P.erodibility[k] = p.erodibility[k];

@@ -37,9 +37,6 @@ struct DevParams {
     float f_alfa[GF_MAXPH], f_beta[GF_MAXPH], f_fmagma_max, f_rho_magma;
     double diffu[GF_MAXPH]; // conduct / den / cp (dt_mass.f90:130)
     double bulkm[GF_MAXPH]; // rl + 2 rm / 3 (fl_rheol.f90:192)
-    // reciprocal pairs y = 1/b, yl = (1 - b y) y of the thermal divisors
-    // den, cp and 6 (gf_div: the bits of the divisions)
-    double den_y[GF_MAXPH], den_yl[GF_MAXPH], cp_y[GF_MAXPH], cp_yl[GF_MAXPH], sixth_y, sixth_yl;
     double hsoft[GF_MAXPH]; // (cohesion2 - cohesion1) / (plstrain2 - plstrain1) (rh_plastic.f90:264)
     // shear heating's per-phase factors (fl_rheol.f90:344-361): lambda / den_el
     // and the reciprocal pair of 2 mu

@@ -208,13 +208,8 @@ __device__ __forceinline__ float gf_mul(float a, float b) { return a * b; }
 // A power-of-two b has the exact reciprocal.  Restated on words and checked
 // against IEEE division by tests/test_int_reciprocal.py.
 __device__ __noinline__ double gf_rcp_rare(double b) { return 1.0 / b; }
-__device__ __forceinline__ double gf_rcp(double b) {
-    unsigned lo, hi;
-    gf_dsplit(b, lo, hi);
-    const unsigned E = (hi >> 20) & 0x7ffu;
-    if (E - 573u > 900u) return gf_rcp_rare(b);
-    const unsigned sign = hi & 0x80000000u, mhi = hi & 0xfffffu;
-    if ((mhi | lo) == 0u) return gf_djoin(0u, sign | ((2046u - E) << 20));
+// RN(2^105 / M) for the significand M = 2^52 + mhi:lo (steps 1-3 above)
+__device__ __forceinline__ long long gf_rcp_sig(unsigned mhi, unsigned lo) {
     const float Mh = __uint_as_float(0x3f800000u | (((mhi << 3) | (lo >> 29)) & 0x7fffffu));
     const float Ml = __uint2float_rn((lo >> 5) & 0xffffffu) * 0x1p-47f; // exact
     const float r = __frcp_rn(Mh);
@@ -231,8 +226,51 @@ __device__ __forceinline__ double gf_rcp(double b) {
     const long long R = -(long long)(M * (unsigned long long)t);
     t += __mul64hi(R, t) >> 41;
     const long long Dp = -(long long)(M * (unsigned long long)(2 * t + 1));
-    t += Dp > 0 ? 1 : (Dp + (long long)(2 * M) < 0 ? -1 : 0);
-    const unsigned long long bits = ((unsigned long long)(2044u - E) << 52) + (unsigned long long)t;
+    return t + (Dp > 0 ? 1 : (Dp + (long long)(2 * M) < 0 ? -1 : 0));
+}
+__device__ __forceinline__ double gf_rcp(double b) {
+    unsigned lo, hi;
+    gf_dsplit(b, lo, hi);
+    const unsigned E = (hi >> 20) & 0x7ffu;
+    if (E - 573u > 900u) return gf_rcp_rare(b);
+    const unsigned sign = hi & 0x80000000u, mhi = hi & 0xfffffu;
+    if ((mhi | lo) == 0u) return gf_djoin(0u, sign | ((2046u - E) << 20));
+    const unsigned long long bits = ((unsigned long long)(2044u - E) << 52) + (unsigned long long)gf_rcp_sig(mhi, lo);
+    return gf_djoin((unsigned)bits, (unsigned)(bits >> 32) | sign);
+}
+
+// RN(a/b) without the FP64 pipe, for a zero or inside gf_dmid and b inside
+// gf_dmid (others take the IEEE division out of line).  With significands
+// Ma, Mb, the quotient's significand is RN(Q), Q = Ma 2^k / Mb in
+// [2^52, 2^53) (k = 52 if Ma >= Mb, else 53): q = floor(Ma t / 2^(105-k))
+// from t = RN(2^105 / Mb) lies within 2 of Q; the exact residual
+// Ma 2^k - Mb q (below 2^55 in magnitude, so its low 64 bits are exact)
+// brings q to floor(Q) with at most two steps each way, and 2 (residual) >
+// Mb rounds it up (no ties: a quotient of two 53-bit significands is never
+// halfway between two 53-bit values).  Restated on words and checked
+// against IEEE division by tests/test_int_reciprocal.py.
+__device__ __noinline__ double gf_ddiv_rare(double a, double b) { return a / b; }
+__device__ __forceinline__ double gf_ddiv(double a, double b) {
+    unsigned la, ha, lb, hb;
+    gf_dsplit(a, la, ha);
+    gf_dsplit(b, lb, hb);
+    const unsigned Ea = (ha >> 20) & 0x7ffu, Eb = (hb >> 20) & 0x7ffu;
+    const bool za = ((ha << 1) | la) == 0u;
+    if (!((Ea - 573u <= 900u || za) && Eb - 573u <= 900u)) return gf_ddiv_rare(a, b);
+    const unsigned sign = (ha ^ hb) & 0x80000000u;
+    if (za) return gf_djoin(0u, sign);
+    const unsigned long long Ma = ((unsigned long long)((ha & 0xfffffu) | 0x100000u) << 32) | la;
+    const unsigned long long Mb = ((unsigned long long)((hb & 0xfffffu) | 0x100000u) << 32) | lb;
+    const unsigned long long t = (unsigned long long)gf_rcp_sig(hb & 0xfffffu, lb);
+    const int k = Ma >= Mb ? 52 : 53;
+    unsigned long long q = (__umul64hi(Ma, t) << (k - 41)) | ((Ma * t) >> (105 - k));
+    long long res = (long long)((Ma << k) - Mb * q);
+    if (res < 0) { --q; res += (long long)Mb; }
+    if (res < 0) { --q; res += (long long)Mb; }
+    if (res >= (long long)Mb) { ++q; res -= (long long)Mb; }
+    if (res >= (long long)Mb) { ++q; res -= (long long)Mb; }
+    q += 2 * res > (long long)Mb ? 1u : 0u;
+    const unsigned long long bits = ((unsigned long long)(1074 - k + (int)Ea - (int)Eb) << 52) + q;
     return gf_djoin((unsigned)bits, (unsigned)(bits >> 32) | sign);
 }
 
@@ -345,7 +383,6 @@ __device__ __forceinline__ GfRecip gf_recip_y(double b, double y) { // y = 1.0 /
     r.ok = gf_dmid(b);
     return r;
 }
-__device__ __forceinline__ GfRecip gf_recip(double b) { return gf_recip_y(b, 1.0 / b); }
 // a pair computed ahead (y = RN(1/b) exactly; yl need only be near (1 - b y) y)
 __device__ __forceinline__ GfRecip gf_recip_pre(double b, double y, double yl) {
     GfRecip r;

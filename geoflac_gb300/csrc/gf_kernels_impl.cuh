@@ -686,7 +686,7 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         f1 = f1 + 0.5 * pl * dlxl + 0.5 * pr * dlxr;
     }
     double dt = C->dt;
-    double drat = dt / C->dt_elastic;
+    double drat = gf_ddiv(dt, C->dt_elastic); // (divisions off the FP64 pipe: gf_ddiv)
     if (drat < 1.0) drat = 1.0;
     double *vel = A.vel;
     double v0 = vel[n], v1 = vel[d.N + n];
@@ -703,8 +703,8 @@ template <class R> __device__ __forceinline__ void b_k_node(const DevParams *__r
         v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_f2d(s * gf_d2f(f1));
     } else {
         const double den = gf_mul(gf_mul(am, drat), drat);
-        v0 = (c0 == 1) ? A.bc[n] : v0 + gf_mul(dt, f0) / den;
-        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_mul(dt, f1) / den;
+        v0 = (c0 == 1) ? A.bc[n] : v0 + gf_ddiv(gf_mul(dt, f0), den);
+        v1 = (c1 == 1) ? A.bc[d.N + n] : v1 + gf_ddiv(gf_mul(dt, f1), den);
     }
     if (P.i_prestress == 1 && C->time < 600e3 * GF_SEC_YEAR) {
         if (j == nz - 1 || i == 0 || i == nx - 1) {
@@ -796,12 +796,11 @@ template <class R> __device__ __forceinline__ void b_k_move_elem(DevClock *__res
             dvol[gf_ek(d, e, k)] = R(gf_mul(det, (double)ar_old) - 1.0);
             const double rdet = gf_rcp(det); // RN(1/det) off the FP64 pipe
             ar_new = R(rdet);
-            // the rotation's quotient by det from the same reciprocal (gf_div:
-            // the bits of the division)
-            double dw = gf_mul(gf_div<true>(gf_scale<-1>(gf_mul(xv[a], xc[c] - xc[b]) + gf_mul(xv[b], xc[a] - xc[c]) +
-                                                         gf_mul(xv[c], xc[b] - xc[a]) + gf_mul(yv[a], yc[c] - yc[b]) +
-                                                         gf_mul(yv[b], yc[a] - yc[c]) + gf_mul(yv[c], yc[b] - yc[a])),
-                                            gf_recip_y(det, rdet)),
+            // the rotation's quotient by det (gf_ddiv: the bits of the division)
+            double dw = gf_mul(gf_ddiv(gf_scale<-1>(gf_mul(xv[a], xc[c] - xc[b]) + gf_mul(xv[b], xc[a] - xc[c]) +
+                                                    gf_mul(xv[c], xc[b] - xc[a]) + gf_mul(yv[a], yc[c] - yc[b]) +
+                                                    gf_mul(yv[b], yc[a] - yc[c]) + gf_mul(yv[c], yc[b] - yc[a])),
+                                       det),
                                dtd);
             dw12 = R(dw);
         } else {
@@ -883,10 +882,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     // conduct / den / cp of the phase: the same two IEEE divisions as the
     // reference's cond_eff / dens / cp_eff, taken once per phase at set-up
     double diff = P.diffu[iph];
-    const GfRecip rden = gf_recip_pre(P.den[iph], P.den_y[iph], P.den_yl[iph]);
-    const GfRecip rcp = gf_recip_pre(cp_eff, P.cp_y[iph], P.cp_yl[iph]);
-    const GfRecip r6 = gf_recip_pre(6.0, P.sixth_y, P.sixth_yl);
-    double src = gf_div<true>(A.source[e] + gf_div<true>(dissip, rden), rcp);
+    double src = gf_ddiv(A.source[e] + gf_ddiv(dissip, P.den[iph]), cp_eff);
     Quad q;
     load_quad(A.cord, d, j, i, q);
     const R *area = (const R *)A.area;
@@ -907,7 +903,7 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
 #pragma unroll
             for (int n = m; n < 3; ++n) tc[(t * 6 + kidx(m, n)) * E + e] = gf_mul(dd[m], dd[n]) + gf_mul(zz[m], zz[n]);
         double inv_area = gf_rcp(a); // RN(1/a) off the FP64 pipe
-        double ra = gf_div<true>(inv_area, r6);
+        double ra = gf_ddiv(inv_area, 6.0);
         tc[(12 + t) * E + e] = ra;
         tc[(14 + t) * E + e] = gf_mul(gf_scale<-1>(diff), inv_area);
         tc[(16 + t) * E + e] = gf_mul(src, ra);
@@ -1001,7 +997,7 @@ __device__ __forceinline__ bool therm_sweep_node(DevArrays A, GfDims d, double d
     }
     if (j != nz - 1 && i != nx - 1) // element (j,i), triangle A
         tri(gf_elem(d, j, i), 0, 0, 0, Ts, 1, T[Nd(j + 1, i)], 2, T[Nd(j, i + 1)]);
-    double tn = Ts + gf_mul(rhs, dt) / area_n;
+    double tn = Ts + gf_ddiv(gf_mul(rhs, dt), area_n);
     Tout[n] = tn;
     return !gf_deq(tn, k == 0 ? start(n) : __ldcg(Tup + n));
 }

@@ -1,4 +1,4 @@
-"""Division by a shared denominator in the FP64 path (gf_recip / gf_div in
+"""Division by a shared denominator in the FP64 path (gf_recip_y / gf_div in
 geoflac_gb300/csrc/gf_kernels.cuh), restated with exact arithmetic and
 checked against IEEE division.  For a denominator b:
 
