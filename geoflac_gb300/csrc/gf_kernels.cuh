@@ -273,6 +273,7 @@ __device__ __forceinline__ double gf_ddiv(double a, double b) {
     const unsigned long long bits = ((unsigned long long)(1074 - k + (int)Ea - (int)Eb) << 52) + q;
     return gf_djoin((unsigned)bits, (unsigned)(bits >> 32) | sign);
 }
+__device__ __forceinline__ float gf_ddiv(float a, float b) { return a / b; }
 
 // x * 2^K (K = -2 .. 2, the constant factors 0.25 .. 4 of the step): the
 // exponent field moves by K while x and the result are normal doubles, a
@@ -741,8 +742,8 @@ __device__ __noinline__ double gf_maxwell_s33(double s33d, double vic1, double r
 template <class R> __device__ __forceinline__ MaxwellConsts<R> maxwell_consts(R rmu0, R viscosity, R dt) {
     const R visc_cut = R(1e19);
     MaxwellConsts<R> m;
-    m.rmu = viscosity < visc_cut ? rmu0 * viscosity / visc_cut : rmu0;
-    R temp = m.rmu / (R(2) * viscosity) * dt;
+    m.rmu = viscosity < visc_cut ? gf_ddiv(rmu0 * viscosity, visc_cut) : rmu0;
+    R temp = gf_ddiv(m.rmu, gf_scale<1>(viscosity)) * dt;
     m.ok = !(temp > R(0.5));
     m.vic1 = R(1) - temp;
     if constexpr (sizeof(R) == sizeof(double)) m.vic2 = gf_rcp(R(1.0) + temp); // RN(1/(1 + temp))

@@ -142,7 +142,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     s12 = gf_scale<-2>(s0v[2][0] + s0v[2][1] + s0v[2][2] + s0v[2][3]);
     R stII = gf_scale<-1>(m_sqrt((s11 - s22) * (s11 - s22) + gf_scale<2>(s12) * s12));
     R shr = sshrheat[e];
-    if (srII != R(0.0)) shr = shr + stII / srII * srs2 * dt;
+    if (srII != R(0.0)) shr = shr + gf_ddiv(stII, srII) * srs2 * dt;
 
     int iph = A.iphase[e] - 1;
     int irh = P.irheol[iph];
@@ -270,7 +270,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
             if constexpr (sizeof(R) == sizeof(double)) {
                 const GfRecip qa = gf_recip_y(ra, rar[h]), qb = gf_recip_y(rb, rar[h + 1]);
                 R quad_area = qa.y + qb.y;
-                s0 = (gf_div(s0a, qb) + gf_div(s0b, qa)) / quad_area;
+                s0 = gf_ddiv(gf_div(s0a, qb) + gf_div(s0b, qa), quad_area);
             } else {
                 R quad_area = R(1.0) / ra + R(1.0) / rb;
                 s0 = (s0a / rb + s0b / ra) / quad_area;
@@ -329,7 +329,7 @@ template <class R> __device__ __forceinline__ void b_k_rheol(const DevParams *__
     }
     if (irh == 6 || irh >= 11) {
         R quad_area = ar[0] + ar[1] + ar[2] + ar[3];
-        aps_e = aps_e + (depl[0] * ar[0] + depl[1] * ar[1] + depl[2] * ar[2] + depl[3] * ar[3]) / quad_area;
+        aps_e = aps_e + gf_ddiv(depl[0] * ar[0] + depl[1] * ar[1] + depl[2] * ar[2] + depl[3] * ar[3], quad_area);
         if (aps_e < R(0.0)) aps_e = R(0.0);
         if constexpr (sizeof(R) == sizeof(float)) {
             if (P.f_tau_heal != 0.0f) aps_e = aps_e / (1.0f + dt / P.f_tau_heal);
