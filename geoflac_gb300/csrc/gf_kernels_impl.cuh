@@ -882,6 +882,8 @@ template <class R> __device__ __forceinline__ void b_k_therm_prep(const DevParam
     // conduct / den / cp of the phase: the same two IEEE divisions as the
     // reference's cond_eff / dens / cp_eff, taken once per phase at set-up
     double diff = P.diffu[iph];
+    // the source's quotients by den and cp (gf_ddiv: the bits of the IEEE
+    // divisions, off the FP64 pipe)
     double src = gf_ddiv(A.source[e] + gf_ddiv(dissip, P.den[iph]), cp_eff);
     Quad q;
     load_quad(A.cord, d, j, i, q);
