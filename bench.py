@@ -389,7 +389,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .inp model)",
         "config": bench_config(ws),
         "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
-        "roofline": {k: _r(roofline[k]) for k in ("bound", "achieved", "peak", "unit", "frac", "traffic")},
+        "roofline": {k: _r(roofline[k]) for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "compute")},
         "gpu_launches": fp["launches"],
         "clocks": {k: fp["clocks"].get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")},
         "mixed": {"value": _r(mixed_value), "ms_per_step": _r(1e3 * res["mixed"]["t"] / args.steps),
