@@ -81,8 +81,6 @@ template <class T> int dalloc(gf_ctx *c, T **ptr, size_t count) {
     return GF_OK;
 }
 
-size_t rsize(const gf_ctx *c) { return c->mode == GF_MODE_MIXED ? sizeof(float) : sizeof(double); }
-
 int ralloc(gf_ctx *c, void **ptr, size_t count) {
     if (c->mode == GF_MODE_MIXED) return dalloc(c, (float **)ptr, count);
     return dalloc(c, (double **)ptr, count);
