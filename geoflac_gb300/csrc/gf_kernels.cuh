@@ -199,9 +199,9 @@ __device__ __forceinline__ float gf_mul(float a, float b) { return a * b; }
 //   1. float-float on the FP32 pipe: r = RN32(1/Mh) for the top 24 bits Mh
 //      of M, corrected by the next 24 bits Ml (r + r (1 - (Mh + Ml) r)):
 //      t1 = that times 2^53, within about 2^8 units of T;
-//   2. one Newton step in 64-bit integers: R = 2^105 - M t1 (below 2^62,
-//      so its low 64 bits are exact), t = t1 + floor(R t1 / 2^105), within
-//      one unit of T;
+//   2. one Newton-Raphson step for the reciprocal, t + t (1 - M t / 2^105),
+//      in 64-bit integers: R = 2^105 - M t1 (below 2^62, so its low 64 bits
+//      are exact), t = t1 + floor(R t1 / 2^105), within one unit of T;
 //   3. the midpoint tests 2^106 - M (2t + 1) > 0 and 2^106 - M (2t - 1) < 0
 //      (exact in 64 bits; never zero, as 2^106 / M is no half-integer for
 //      M not a power of two) move t to RN(T).
